@@ -1,0 +1,313 @@
+"""Benchmark of the GB300 WCSPH hot path on the 2M-particle 3D jet in crossflow.
+
+One step = one Integrator::integrate (src/Integration.cpp:233): CFL time step, two neighbour
+searches, the pre-passes, and a full Runge-Kutta-4 step with its four residual evaluations.
+The input state is a seeded synthetic jet (fjsph_gb300.cases.jet_crossflow), resident in HBM
+when the timed region starts; the state and neighbour arrays exceed the 129 MB L2, so no flush
+is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n PARTICLES]
+
+Prints one JSON line (rank 0).  `--impl reference` times the CPU restatement of the reference
+algorithm (the oracle; the reference itself cannot be built here) on the host cores, on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s, 2M-particle jet: FP32+learned aero vs plain FP64, same GB300"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=2_000_000, help="target particle count of the jet")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                        reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+# ---------------------------------------------------------------------------------------------
+def resid_bytes_per_particle(s) -> int:
+    """Algorithmic bytes of one residual evaluation per fluid particle (FP64 form).
+
+    Reads each logical field once: x 3, search x 3, v 3, rho, p, m, aVisc 3, deltaD, cellV 3,
+    cellP, cellRho, lam_nb, woccl (8 B each), cellID, part_id (8 B), b, surfzone (4 B), CSR
+    offset (8 B); ALE adds vPert 3.  Writes acc 3, Af 3, Rrho.  Neighbour re-reads do not count.
+    """
+    from fjsph_gb300 import _cdefs as d
+    D = s.dim
+    r8 = 3 * D + 3 + 3 + D + 1 + D + 2 + 2 + 2 + 1
+    if s.variant & d.VAR_ALE:
+        r8 += D
+    if s.variant & d.VAR_NOFROZEN:
+        r8 += D
+    w8 = 2 * D + 1
+    return 8 * (r8 + w8) + 4 * 2
+
+
+def make_case(n_target: int, precision: str):
+    from fjsph_gb300 import cases, _cdefs as d
+    c = cases.jet_crossflow(n_target=n_target)
+    if precision == "mixed":
+        c.settings.precision = d.PREC_MIXED
+    return c
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300.api import Context
+
+    c = make_case(args.n, args.precision)
+    s = c.settings
+    nf = c.n_fluid
+    ctx = Context(s, c.state.n + 1024, c.blocks)
+    ctx.set_states(c.state, c.state)
+    for _ in range(args.warmup):
+        ctx.integrate()
+    barrier(ws)
+    clocks = Clocks(local)
+    clocks.start()
+    ctx.profile(True)
+    ctx.launch_stats(reset=True)
+    ctx.event_record(0)
+    for _ in range(args.steps):
+        ctx.integrate()
+    ctx.event_record(1)
+    ms = ctx.event_elapsed(0, 1)
+    launches = ctx.launch_stats()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    clk = clocks.stop()
+    ms = reduce_max(ws, ms)
+    rep = ctx.step_report()
+    value = nf * args.steps * ws / (ms / 1e3)
+
+    # roofline of the dominant kernel: the residual
+    peaks = measured_peaks()
+    r_ms, r_cnt = prof["residual"]
+    bpp = resid_bytes_per_particle(s)
+    per_launch = r_ms / max(r_cnt, 1) / 1e3
+    achieved = bpp * nf / per_launch / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+            "frac": round(achieved / peaks.get("hbm_gbs", 6800.0), 4), "traffic": None,
+            "kernel": "k_resid (get_acc_and_Rrho)", "launch_ms": round(per_launch * 1e3, 3),
+            "bytes_per_launch": bpp * nf, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
+
+    # end to end through the public API with host buffers: upload both states, one step,
+    # download the new state, every step
+    e2e = None
+    if args.e2e_steps > 0:
+        host = ctx.download()
+        t0 = time.perf_counter()
+        ctx.event_record(2)
+        for _ in range(args.e2e_steps):
+            ctx.upload(d.PNP1, host)
+            ctx.upload(d.PN, host)
+            ctx.integrate()
+            host = ctx.download()
+        ctx.event_record(3)
+        e2e_ms = ctx.event_elapsed(2, 3)
+        wall = time.perf_counter() - t0
+        e2e_ms = reduce_max(ws, max(e2e_ms, wall * 1e3))
+        nbytes = state_bytes(host)
+        e2e = {"value": nf * args.e2e_steps * ws / (e2e_ms / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes}
+    return dict(value=value, ms=ms, nf=nf, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches,
+                prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s, case=c)
+
+
+def state_bytes(st) -> int:
+    from fjsph_gb300.state import ALL_FIELDS
+    return int(sum(getattr(st, f).nbytes for f in ALL_FIELDS))
+
+
+def cpu_sample_case(c, n_sample: int):
+    """A spatially contiguous cut of the workload: the fluid particles nearest the pipe exit plus
+    the walls they touch, about n_sample particles."""
+    import numpy as np
+    from fjsph_gb300.state import BlockSpec
+    st = c.state
+    nb = sum(b.second - b.first for b in c.blocks if not b.is_fluid)
+    fl = np.arange(nb, st.n)
+    order = fl[np.argsort(np.linalg.norm(st.xi[fl] - np.array([0.0, 0.0, 0.0]), axis=1))]
+    keep_f = np.sort(order[: max(n_sample - nb // 4, 1000)])
+    xmax = np.linalg.norm(st.xi[keep_f], axis=1).max() + 4 * c.settings.H
+    wb = np.arange(nb)
+    keep_b = wb[np.linalg.norm(st.xi[wb], axis=1) < xmax]
+    idx = np.concatenate([keep_b, keep_f])
+    sub = st.take(idx)
+    sub.part_id[:] = np.arange(sub.n)
+    blocks = []
+    if len(keep_b):
+        b0 = [b for b in c.blocks if not b.is_fluid][0]
+        blocks.append(BlockSpec(0, len(keep_b), False, bound_solver=b0.bound_solver))
+    fb = [b for b in c.blocks if b.is_fluid][0]
+    blocks.append(BlockSpec(len(keep_b), sub.n, True, aero_norm=fb.aero_norm, aeroconst=fb.aeroconst))
+    return sub, blocks, len(keep_f)
+
+
+def run_cpu(c, steps: int, warmup: int, n_sample: int, threads: int):
+    from oracle.pyoracle import Oracle, set_threads
+    set_threads(threads)
+    sub, blocks, nf = cpu_sample_case(c, n_sample)
+    o = Oracle(c.settings, blocks)
+    o.set_states(sub, sub)
+    for _ in range(warmup):
+        o.integrate()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.integrate()
+    dt = time.perf_counter() - t0
+    return nf * steps / dt, nf, dt
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        c = make_case(args.n, "fp64")
+        v, nf, dt = run_cpu(c, args.steps, min(args.warmup, 1), args.cpu_sample, threads)
+        sample = (f"{nf} fluid particles nearest the pipe exit cut from the {c.n_fluid}-particle jet, "
+                  f"{args.steps} Integrator::integrate steps, OpenMP")
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "jet_in_crossflow_3d", "particles": c.state.n, "fluid": c.n_fluid},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    if ws > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(0)
+        dist.init_process_group("nccl")
+    r = run_ours(args, ws, rank, local)
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            v, nf, dt = run_cpu(r["case"], 1, 0, args.cpu_sample, threads)
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"1 integrate step of {nf} fluid particles cut from the jet (CPU restatement, "
+                             f"{dt:.1f} s)"}
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+                "data": "synthetic",
+                "config": {"workload": "jet_in_crossflow_3d", "particles": r["n"], "fluid": r["nf"],
+                           "form": args.precision, "integrator": "runge_kutta4",
+                           "l2": "inputs larger than L2 (state ~1 GB)", "parallelism": f"replicas{ws}"},
+                "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
+                "gpu_launches": r["launches"], "passes_ms": r["prof"]}
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

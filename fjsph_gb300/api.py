@@ -1,0 +1,235 @@
+"""Host-side mirror of FJSPH's hot-path interface, backed by the GB300 C-ABI library.
+
+Method names follow the reference functions they replace; each operates on the context's
+working state `pnp1` (and reads `pn`), as the reference functions do on SPHState references:
+
+  update_neighbours      src/Neighbours.cpp:7        dSPH_PreStep        src/Shifting.cpp:12
+  get_aero_velocity      src/Resid.cpp:471            Detect_Surface      src/Geometry.cpp:14
+  dissipation_terms      src/Shifting.cpp:126         particle_shift      src/Shifting.cpp:189
+  Check_Pipe_Outlet      src/Containment.cpp:822      Get_Boundary_Pressure src/Resid.cpp:21
+  Boundary_Ghost         src/Resid.cpp:122            Boundary_DBC        src/Resid.cpp:78
+  Set_No_Slip            src/Resid.cpp:162            get_acc_and_Rrho    src/Resid.cpp:426
+  find_timestep          src/Integration.cpp:370      Get_First_RK        src/Runge_Kutta.cpp:462
+  Runge_Kutta4           src/Runge_Kutta.cpp:480      Do_NB_Iter          src/Newmark_Beta.cpp:54
+  Newmark_Beta           src/Newmark_Beta.cpp:303     integrate_no_update src/Integration.cpp:27
+  integrate              src/Integration.cpp:233
+
+Errors raise FJSPHError (the reference prints and exits instead).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _cdefs as d
+from ._lib import check, lib
+from .state import BlockSpec, InletSpec, SPHState, blocks_to_c
+
+
+class Context:
+    """One device context: two particle states (pn, pnp1), neighbour lists, integrator scratch."""
+
+    def __init__(self, settings: d.Settings, capacity: int, blocks: list[BlockSpec],
+                 inlets: list[InletSpec] = ()):
+        self._lib = lib()
+        self.dim = settings.dim
+        h = C.c_void_p()
+        check("fjsph_ctx_create", self._lib.fjsph_ctx_create(C.byref(settings), int(capacity), C.byref(h)))
+        self._h = h
+        self.blocks = list(blocks)
+        self.n_bound_blocks = sum(1 for b in blocks if not b.is_fluid)
+        arr = blocks_to_c(self.blocks)
+        check("fjsph_set_limits", self._lib.fjsph_set_limits(self._h, arr, len(self.blocks), self.n_bound_blocks))
+        self._inlets = list(inlets)
+        for inl in self._inlets:
+            self._set_inlet(inl)
+
+    def _set_inlet(self, inl: InletSpec) -> None:
+        back = np.ascontiguousarray(inl.back, dtype=np.int64)
+        buf = np.ascontiguousarray(inl.buffer, dtype=np.int64)
+        c = d.Inlet()
+        c.block = inl.block
+        c.n_back = back.shape[0]
+        c.depth = buf.shape[1] if buf.ndim == 2 else 0
+        c.back = back.ctypes.data_as(C.POINTER(C.c_int64))
+        c.buffer = buf.ctypes.data_as(C.POINTER(C.c_int64))
+        check("fjsph_set_inlet", self._lib.fjsph_set_inlet(self._h, C.byref(c)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fjsph_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- settings and state ------------------------------------------------------------------
+    @property
+    def settings(self) -> d.Settings:
+        s = d.Settings()
+        check("fjsph_get_settings", self._lib.fjsph_get_settings(self._h, C.byref(s)))
+        return s
+
+    @settings.setter
+    def settings(self, s: d.Settings) -> None:
+        check("fjsph_set_settings", self._lib.fjsph_set_settings(self._h, C.byref(s)))
+
+    def upload(self, which: int, st: SPHState) -> None:
+        v = st.view()
+        check("fjsph_state_upload", self._lib.fjsph_state_upload(self._h, which, C.byref(v)))
+
+    def download(self, which: int = d.PNP1) -> SPHState:
+        n = C.c_int64()
+        check("fjsph_particle_count", self._lib.fjsph_particle_count(self._h, C.byref(n), None))
+        st = SPHState(n.value, self.dim)
+        v = st.view()
+        check("fjsph_state_download", self._lib.fjsph_state_download(self._h, which, C.byref(v)))
+        return st
+
+    def set_states(self, pn: SPHState, pnp1: SPHState) -> None:
+        self.upload(d.PNP1, pnp1)
+        self.upload(d.PN, pn)
+
+    # ---- neighbour search --------------------------------------------------------------------
+    def update_neighbours(self) -> int:
+        n = C.c_int64()
+        check("fjsph_update_neighbours", self._lib.fjsph_update_neighbours(self._h, C.byref(n)))
+        self._n_pairs = n.value
+        return n.value
+
+    def neighbours(self):
+        """(offsets, neighbour indices, squared distances) in reference order, lists sorted."""
+        n = C.c_int64()
+        self._lib.fjsph_particle_count(self._h, C.byref(n), None)
+        off = np.zeros(n.value + 1, dtype=np.int64)
+        idx = np.zeros(self._n_pairs, dtype=np.int64)
+        d2 = np.zeros(self._n_pairs, dtype=np.float64)
+        check("fjsph_neighbours_export", self._lib.fjsph_neighbours_export(
+            self._h, off.ctypes.data_as(C.POINTER(C.c_int64)), idx.ctypes.data_as(C.POINTER(C.c_int64)),
+            d2.ctypes.data_as(C.POINTER(C.c_double))))
+        return off, idx, d2
+
+    # ---- pre-passes ----------------------------------------------------------------------------
+    def dSPH_PreStep(self) -> float:
+        npd = C.c_double()
+        check("fjsph_dsph_prestep", self._lib.fjsph_dsph_prestep(self._h, C.byref(npd)))
+        return npd.value
+
+    def get_aero_velocity(self) -> None:
+        check("fjsph_get_aero_velocity", self._lib.fjsph_get_aero_velocity(self._h))
+
+    def Detect_Surface(self) -> None:
+        check("fjsph_detect_surface", self._lib.fjsph_detect_surface(self._h))
+
+    def dissipation_terms(self) -> None:
+        check("fjsph_dissipation_terms", self._lib.fjsph_dissipation_terms(self._h))
+
+    def particle_shift(self) -> None:
+        check("fjsph_particle_shift", self._lib.fjsph_particle_shift(self._h))
+
+    def Check_Pipe_Outlet(self) -> None:
+        check("fjsph_check_pipe_outlet", self._lib.fjsph_check_pipe_outlet(self._h))
+
+    # ---- boundary passes and residual ----------------------------------------------------------
+    def Get_Boundary_Pressure(self) -> None:
+        check("fjsph_get_boundary_pressure", self._lib.fjsph_get_boundary_pressure(self._h))
+
+    def Boundary_Ghost(self) -> np.ndarray:
+        n, nb = C.c_int64(), C.c_int64()
+        self._lib.fjsph_particle_count(self._h, C.byref(n), C.byref(nb))
+        out = np.zeros(max(nb.value, 1), dtype=np.int32)
+        check("fjsph_boundary_ghost", self._lib.fjsph_boundary_ghost(self._h, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out[: nb.value]
+
+    def Boundary_DBC(self) -> None:
+        check("fjsph_boundary_dbc", self._lib.fjsph_boundary_dbc(self._h))
+
+    def Set_No_Slip(self) -> None:
+        check("fjsph_set_no_slip", self._lib.fjsph_set_no_slip(self._h))
+
+    def get_acc_and_Rrho(self, npd: float) -> None:
+        check("fjsph_get_acc_and_rrho", self._lib.fjsph_get_acc_and_rrho(self._h, float(npd)))
+
+    # ---- integrators ----------------------------------------------------------------------------
+    def find_timestep(self) -> float:
+        dt = C.c_double()
+        check("fjsph_find_timestep", self._lib.fjsph_find_timestep(self._h, C.byref(dt)))
+        return dt.value
+
+    def Get_First_RK(self, npd: float) -> float:
+        lb = C.c_double()
+        check("fjsph_get_first_rk", self._lib.fjsph_get_first_rk(self._h, float(npd), C.byref(lb)))
+        return lb.value
+
+    def Runge_Kutta4(self, npd: float, logbase: float) -> float:
+        r = C.c_double()
+        check("fjsph_runge_kutta4", self._lib.fjsph_runge_kutta4(self._h, float(npd), float(logbase), C.byref(r)))
+        return r.value
+
+    def Do_NB_Iter(self, npd: float) -> None:
+        check("fjsph_nb_iter", self._lib.fjsph_nb_iter(self._h, float(npd)))
+
+    def Newmark_Beta(self, npd: float, logbase: float, iteration: int):
+        lb, it, r = C.c_double(logbase), C.c_int32(iteration), C.c_double()
+        check("fjsph_newmark_beta", self._lib.fjsph_newmark_beta(self._h, float(npd), C.byref(lb), C.byref(it),
+                                                                  C.byref(r)))
+        return r.value, lb.value, it.value
+
+    def integrate_no_update(self) -> float:
+        r = C.c_double()
+        check("fjsph_integrate_no_update", self._lib.fjsph_integrate_no_update(self._h, C.byref(r)))
+        return r.value
+
+    def integrate(self) -> float:
+        r = C.c_double()
+        check("fjsph_integrate", self._lib.fjsph_integrate(self._h, C.byref(r)))
+        return r.value
+
+    def integrate_n(self, n_steps: int) -> float:
+        r = C.c_double()
+        check("fjsph_integrate_n", self._lib.fjsph_integrate_n(self._h, int(n_steps), C.byref(r)))
+        return r.value
+
+    def step_report(self) -> dict:
+        out = (C.c_double * 5)()
+        check("fjsph_step_report", self._lib.fjsph_step_report(self._h, out))
+        return dict(maxRho_pc=out[0], maxf=out[1], maxAf=out[2], maxShift=out[3], iteration=int(out[4]))
+
+    def launch_stats(self, reset: bool = False) -> int:
+        n = C.c_int64()
+        check("fjsph_launch_stats", self._lib.fjsph_launch_stats(self._h, C.byref(n), int(reset)))
+        return n.value
+
+    def event_record(self, slot: int) -> None:
+        check("fjsph_event_record", self._lib.fjsph_event_record(self._h, int(slot)))
+
+    def event_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        check("fjsph_event_elapsed", self._lib.fjsph_event_elapsed(self._h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
+    def profile(self, on: bool) -> None:
+        check("fjsph_profile_enable", self._lib.fjsph_profile_enable(self._h, int(on)))
+
+    def profile_read(self) -> dict:
+        """{pass name: (milliseconds, section count)} accumulated since the last read."""
+        npass = 12
+        ms = (C.c_double * npass)()
+        cnt = (C.c_int64 * npass)()
+        check("fjsph_profile_read", self._lib.fjsph_profile_read(self._h, ms, cnt))
+        return {self._lib.fjsph_profile_pass_name(k).decode(): (ms[k], cnt[k]) for k in range(npass)}
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        check("fjsph_ctx_stream", self._lib.fjsph_ctx_stream(self._h, C.byref(p)))
+        return p.value or 0

@@ -1,0 +1,76 @@
+"""In-tree build of the GB300 WCSPH library (libfjsph_gb300.so) for sm_103a.
+
+Each translation unit is compiled by nvcc in parallel into fjsph_gb300/_build/ and the objects
+are linked into fjsph_gb300/libfjsph_gb300.so.  No CMake, no torch extension machinery: the
+library is plain CUDA C++ behind the C ABI declared in include/fjsph_gb300.h.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libfjsph_gb300.so"
+
+SOURCES = ["capi.cu", "neighbours.cu", "sweeps.cu", "integrate.cu", "state.cu", "settings.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-fno-strict-aliasing", "-I", str(ROOT / "include")]
+
+
+def _nvcc() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cand = Path(cuda) / "bin" / "nvcc"
+    if cand.exists():
+        return str(cand)
+    found = shutil.which("nvcc")
+    if not found:
+        raise RuntimeError("nvcc not found; set CUDA_HOME")
+    return found
+
+
+def _compile(src: Path, extra: list[str]) -> Path:
+    obj = BUILD / (src.name + ".o")
+    if obj.exists() and obj.stat().st_mtime >= max(
+        src.stat().st_mtime,
+        max(p.stat().st_mtime for p in CSRC.glob("*.cuh")),
+        max(p.stat().st_mtime for p in CSRC.glob("*.h")),
+        (ROOT / "include" / "fjsph_gb300.h").stat().st_mtime,
+    ):
+        return obj
+    cmd = [_nvcc(), *ARCH, *NVFLAGS, *extra, "-c", str(src), "-o", str(obj)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stderr}\n{res.stdout}")
+    if res.stderr.strip():
+        sys.stderr.write(res.stderr)
+    return obj
+
+
+def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
+    """Compile every translation unit for sm_103a and link the shared library; returns its path."""
+    BUILD.mkdir(exist_ok=True)
+    extra = list(extra or [])
+    srcs = [CSRC / s for s in SOURCES]
+    with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
+    if LIB.exists() and LIB.stat().st_mtime >= max(o.stat().st_mtime for o in objs):
+        return LIB
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stderr}\n{res.stdout}")
+    if verbose:
+        print(f"built {LIB}")
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, extra=sys.argv[1:])

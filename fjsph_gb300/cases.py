@@ -1,0 +1,322 @@
+"""Synthetic input states for the hot path.
+
+These builders stand in for the reference's geometry files (src/shapes/*, src/Init.cpp); they
+produce the particle layouts that the benchmark configurations describe:
+
+  dam_break_2d   water column in a 2D tank, square lattice, hydrostatic density (config 0)
+  dam_break_3d   3D dam break, jittered lattice, ALE (config 1); hydrostatic along z
+  droplet_3d     spherical droplet in a uniform air stream, Gissler aero + pairwise surface
+                 tension (the droplets of config 4)
+  jet_crossflow  liquid column leaving a pipe into an analytic crossflow, broken into ligaments and
+                 droplets downstream (configs 2-3); the air field is uniform v_inf, as the
+                 reference's constant-velocity source supplies it
+
+Boundary particles form `layers` rows outside the fluid region at the lattice spacing.  All
+random numbers come from numpy's PCG64 with the given seed.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _cdefs as d
+from .settings import defaults, derive
+from .state import BlockSpec, InletSpec, SPHState
+
+
+@dataclass
+class Case:
+    name: str
+    settings: d.Settings
+    state: SPHState
+    blocks: list[BlockSpec]
+    inlets: list[InletSpec] = field(default_factory=list)
+
+    @property
+    def n_fluid(self) -> int:
+        return self.state.n - sum(b.second - b.first for b in self.blocks if not b.is_fluid)
+
+
+def _eos_density(s: d.Settings, p: np.ndarray) -> np.ndarray:
+    if s.pressure_rel == d.ISO_EOS:
+        return (p - s.press_back) / (s.speed_sound ** 2) + s.rho_rest
+    return s.rho_rest * np.power((p - s.press_back) / s.B + 1.0, 1.0 / s.gam)
+
+
+def _assemble(s: d.Settings, bound: np.ndarray, fluid: np.ndarray, b_fluid: int = d.FREE):
+    dim = s.dim
+    nb, nf = len(bound), len(fluid)
+    st = SPHState(nb + nf, dim)
+    if nb:
+        st.xi[:nb] = bound
+    st.xi[nb:] = fluid
+    st.m[:] = s.sim_mass
+    st.rho[:] = s.rho_rest
+    st.b[:nb] = d.BOUND
+    st.b[nb:] = b_fluid
+    st.cellRho[:] = s.rho_g
+    st.cellP[:] = s.p_ref
+    st.cellV[:] = np.asarray(s.v_inf[:dim])
+    st.part_id[:] = np.arange(nb + nf)
+    return st
+
+
+def _blocks(nb: int, n: int, bound_solver: int = d.PRESSURE_G, no_slip: int = 0) -> list[BlockSpec]:
+    out = []
+    if nb:
+        out.append(BlockSpec(0, nb, False, name="walls", bound_solver=bound_solver, no_slip=no_slip))
+    out.append(BlockSpec(nb, n, True, name="fluid"))
+    return out
+
+
+def _hydrostatic(s: d.Settings, st: SPHState, axis: int, height: float) -> None:
+    """Init_Particles' hydrostatic option (src/Init.cpp:480-493) along `axis`."""
+    g = abs(s.grav[axis])
+    p = np.maximum(0.0, s.rho_rest * g * (height - st.xi[:, axis]))
+    st.p[:] = p
+    st.rho[:] = _eos_density(s, p)
+
+
+def dam_break_2d(dx: float = 0.01, column=(1.0, 2.0), tank=(4.0, 3.0), layers: int = 3,
+                 solver: int = d.RUNGE_KUTTA, cfl: float = 0.2) -> Case:
+    """Config 0: 1.0 x 2.0 m column in a 4.0 x 3.0 m tank, dx = 0.01 (20,000 fluid particles)."""
+    s = defaults(2)
+    s.st_model = d.ST_NOST
+    s.particle_step = dx
+    s.H_fac = 1.3
+    s.rho_rest = 1000.0
+    s.gam = 7.0
+    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * column[1])
+    s.dsph_delta = 0.1
+    s.visc_alpha = 0.01
+    s.sig = 0.0
+    s.grav[:] = [0.0, -9.81, 0.0]
+    s.solver_type = solver
+    s.cfl = s.cfl_min = s.cfl_max = cfl
+    s.delta_t_min = 1e-9
+    derive(s)
+    nx, ny = int(round(column[0] / dx)), int(round(column[1] / dx))
+    fx, fy = np.meshgrid((np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dx, indexing="ij")
+    fluid = np.stack([fx.ravel(), fy.ravel()], axis=1)
+    tx, ty = int(round(tank[0] / dx)), int(round(tank[1] / dx))
+    walls = []
+    for k in range(layers):
+        xs = (np.arange(-layers, tx + layers) + 0.5) * dx
+        walls.append(np.stack([xs, np.full_like(xs, -(k + 0.5) * dx)], axis=1))
+    ys = (np.arange(ty) + 0.5) * dx
+    for k in range(layers):
+        walls.append(np.stack([np.full_like(ys, -(k + 0.5) * dx), ys], axis=1))
+        walls.append(np.stack([np.full_like(ys, tank[0] + (k + 0.5) * dx), ys], axis=1))
+    bound = np.concatenate(walls)
+    st = _assemble(s, bound, fluid)
+    _hydrostatic(s, st, 1, column[1])
+    return Case("dam_break_2d", s, st, _blocks(len(bound), st.n))
+
+
+def dam_break_3d(dx: float = 0.003, column=(0.6, 0.6, 1.2), tank=(1.6, 0.6, 1.2), layers: int = 3,
+                 jitter: float = 0.01, seed: int = 12345, ale: bool = True, solver: int = d.RUNGE_KUTTA,
+                 cfl: float = 0.2) -> Case:
+    """Config 1: 0.6 x 0.6 x 1.2 m column in a 1.6 x 0.6 x 1.2 m tank (dx = 3 mm: 16M fluid)."""
+    s = defaults(3)
+    s.variant = d.VAR_ALE if ale else 0
+    s.st_model = d.ST_NOST
+    s.particle_step = dx
+    s.H_fac = 1.3
+    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * column[2])
+    s.dsph_delta = 0.1
+    s.visc_alpha = 0.01
+    s.sig = 0.0
+    s.grav[:] = [0.0, 0.0, -9.81]
+    s.solver_type = solver
+    s.cfl = s.cfl_min = s.cfl_max = cfl
+    s.delta_t_min = 1e-9
+    s.max_shift_vel = 5.0
+    derive(s)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = [int(round(column[k] / dx)) for k in range(3)]
+    g = np.meshgrid(*[(np.arange(n[k]) + 0.5) * dx for k in range(3)], indexing="ij")
+    fluid = np.stack([a.ravel() for a in g], axis=1)
+    fluid += rng.uniform(-jitter * dx, jitter * dx, size=fluid.shape)
+    t = [int(round(tank[k] / dx)) for k in range(3)]
+    walls = []
+    # floor: z < 0, covering the tank footprint plus the side walls
+    gx, gy = np.meshgrid((np.arange(-layers, t[0] + layers) + 0.5) * dx, (np.arange(-layers, t[1] + layers) + 0.5) * dx,
+                         indexing="ij")
+    for k in range(layers):
+        walls.append(np.stack([gx.ravel(), gy.ravel(), np.full(gx.size, -(k + 0.5) * dx)], axis=1))
+    zs = (np.arange(t[2]) + 0.5) * dx
+    # x walls (full y extent incl. corners), y walls (tank x extent)
+    ay, az = np.meshgrid((np.arange(-layers, t[1] + layers) + 0.5) * dx, zs, indexing="ij")
+    for k in range(layers):
+        walls.append(np.stack([np.full(ay.size, -(k + 0.5) * dx), ay.ravel(), az.ravel()], axis=1))
+        walls.append(np.stack([np.full(ay.size, tank[0] + (k + 0.5) * dx), ay.ravel(), az.ravel()], axis=1))
+    bx, bz = np.meshgrid((np.arange(t[0]) + 0.5) * dx, zs, indexing="ij")
+    for k in range(layers):
+        walls.append(np.stack([bx.ravel(), np.full(bx.size, -(k + 0.5) * dx), bz.ravel()], axis=1))
+        walls.append(np.stack([bx.ravel(), np.full(bx.size, tank[1] + (k + 0.5) * dx), bz.ravel()], axis=1))
+    bound = np.concatenate(walls)
+    st = _assemble(s, bound, fluid)
+    _hydrostatic(s, st, 2, column[2])
+    return Case("dam_break_3d", s, st, _blocks(len(bound), st.n))
+
+
+def _air(s: d.Settings, speed: float) -> None:
+    s.acase = d.GISSLER
+    s.v_inf[:] = [speed, 0.0, 0.0]
+    s.rho_g = 1.225
+    s.mu_g = 1.8e-5
+    s.p_ref = 101325.0
+
+
+def _liquid(s: d.Settings) -> None:
+    s.rho_rest = 800.0
+    s.mu = 1.5e-3
+    s.sig = 0.025
+    s.st_model = d.ST_PAIRWISE
+
+
+def _sphere_points(diam: float, dx: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
+    r = 0.5 * diam
+    m = int(math.ceil(r / dx)) + 1
+    ax = np.arange(-m, m + 1) * dx
+    g = np.meshgrid(ax, ax, ax, indexing="ij")
+    pts = np.stack([a.ravel() for a in g], axis=1)
+    pts = pts[np.einsum("ij,ij->i", pts, pts) <= r * r]
+    return pts + np.asarray(centre)
+
+
+def droplet_3d(diam: float = 1e-3, dx: float = 5e-5, air_speed: float = 30.0, seed: int = 7,
+               solver: int = d.RUNGE_KUTTA, cfl: float = 0.5, ale: bool = False) -> Case:
+    """A spherical droplet of the config-2 liquid in a uniform air stream (config 4 unit)."""
+    s = defaults(3)
+    _liquid(s)
+    _air(s, air_speed)
+    s.variant = d.VAR_ALE if ale else 0
+    s.particle_step = dx
+    s.H_fac = 1.3
+    s.speed_sound = 40.0
+    s.visc_alpha = 0.05
+    s.grav[:] = [0.0, 0.0, 0.0]
+    s.solver_type = solver
+    s.cfl = cfl
+    s.cfl_min = 0.1
+    s.cfl_max = cfl
+    s.delta_t_min = 1e-12
+    s.delta_t_max = 1e-5
+    derive(s)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pts = _sphere_points(diam, dx)
+    pts += rng.uniform(-0.01 * dx, 0.01 * dx, size=pts.shape)
+    st = _assemble(s, np.zeros((0, 3)), pts)
+    return Case("droplet_3d", s, st, _blocks(0, st.n))
+
+
+def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, jet_speed: float = 10.0,
+                  air_speed: float = 50.0, seed: int = 2024, ale: bool = False, solver: int = d.RUNGE_KUTTA,
+                  pipe_layers: int = 2) -> Case:
+    """Config-2 liquid jet in crossflow, ~n_target particles.
+
+    A ghost-walled pipe (diameter D) feeds a column that rises along +z and bends downstream along
+    +x with the crossflow; past the bend the column is broken into ligaments and droplets of
+    log-uniform diameter.  Liquid rho = 800, mu = 1.5e-3, sigma = 0.025; air 1.225 kg/m^3 moving at
+    air_speed along +x.  Fluid particles carry the jet velocity plus the local crossflow drift.
+    """
+    s = defaults(3)
+    _liquid(s)
+    _air(s, air_speed)
+    s.variant = d.VAR_ALE if ale else 0
+    s.particle_step = dx
+    s.H_fac = 1.3
+    s.speed_sound = 10.0 * jet_speed
+    s.visc_alpha = 0.05
+    s.grav[:] = [0.0, 0.0, -9.81]
+    s.solver_type = solver
+    s.cfl = 0.5
+    s.cfl_min = 0.1
+    s.cfl_max = 0.5
+    s.delta_t_min = 1e-12
+    s.delta_t_max = 1e-5
+    s.max_points = 2_000_000
+    derive(s)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R = 0.5 * D
+    m = int(math.ceil(R / dx)) + 1
+    ax = np.arange(-m, m + 1) * dx
+    gx, gy = np.meshgrid(ax, ax, indexing="ij")
+    disk = np.stack([gx.ravel(), gy.ravel()], axis=1)
+    disk = disk[np.einsum("ij,ij->i", disk, disk) <= R * R]
+    # pipe walls: rings from R + dx/2 outward, z in [-4D, 0)
+    pipe_len = 4.0 * D
+    zs = (np.arange(int(pipe_len / dx)) + 0.5) * dx - pipe_len
+    wall = []
+    for k in range(pipe_layers):
+        rr = R + (k + 0.5) * dx
+        nth = int(round(2 * math.pi * rr / dx))
+        th = np.arange(nth) * 2 * math.pi / nth
+        ring = np.stack([rr * np.cos(th), rr * np.sin(th)], axis=1)
+        for z in zs:
+            wall.append(np.concatenate([ring, np.full((nth, 1), z)], axis=1))
+    bound = np.concatenate(wall)
+    parts, vels, types = [], [], []
+    # liquid inside the pipe: PIPE particles
+    for z in zs:
+        parts.append(np.concatenate([disk, np.full((len(disk), 1), z)], axis=1))
+        vels.append(np.tile([0.0, 0.0, jet_speed], (len(disk), 1)))
+        types.append(np.full(len(disk), d.PIPE))
+    # intact column: centreline bends from +z towards +x over a quarter circle of radius 5D
+    Rb = 5.0 * D
+    arc = 0.5 * math.pi * Rb
+    nlay = int(arc / dx)
+    for k in range(nlay):
+        phi = (k * dx) / Rb
+        c = np.array([Rb * (1 - math.cos(phi)), 0.0, Rb * math.sin(phi)])
+        t = np.array([math.sin(phi), 0.0, math.cos(phi)])
+        e1 = np.array([math.cos(phi), 0.0, -math.sin(phi)])
+        e2 = np.array([0.0, 1.0, 0.0])
+        pts = c + disk[:, :1] * e1 + disk[:, 1:2] * e2
+        parts.append(pts)
+        vels.append(np.tile(jet_speed * t + np.array([0.2 * air_speed * math.sin(phi), 0.0, 0.0]), (len(pts), 1)))
+        types.append(np.full(len(pts), d.FREE))
+    n_now = sum(len(p) for p in parts)
+    # droplets downstream of the bend, x in [5.5D, 20D], |y| < 4D, z in [3D, 9D]; an occupancy grid
+    # at the lattice spacing keeps droplets at least 2 dx apart
+    lo = np.array([Rb + 0.5 * D - D, -5 * D, 2 * D])
+    hi = np.array([21 * D, 5 * D, 10 * D])
+    shape = tuple(np.ceil((hi - lo) / dx).astype(int) + 1)
+    occ = np.zeros(shape, dtype=bool)
+    tries = 0
+    while n_now < n_target and tries < 200000:
+        tries += 1
+        dd = math.exp(rng.uniform(math.log(6 * dx), math.log(0.9 * D)))
+        centre = np.array([rng.uniform(Rb + 0.5 * D, 20 * D), rng.uniform(-4 * D, 4 * D), rng.uniform(3 * D, 9 * D)])
+        pts = _sphere_points(dd, dx, centre)
+        if len(pts) == 0:
+            continue
+        gi = np.floor((pts - lo) / dx).astype(np.int64)
+        if np.any(occ[gi[:, 0], gi[:, 1], gi[:, 2]]):
+            continue
+        for ox in (-2, -1, 0, 1, 2):
+            for oy in (-2, -1, 0, 1, 2):
+                for oz in (-2, -1, 0, 1, 2):
+                    g2 = gi + np.array([ox, oy, oz])
+                    g2 = np.clip(g2, 0, np.array(shape) - 1)
+                    occ[g2[:, 0], g2[:, 1], g2[:, 2]] = True
+        parts.append(pts)
+        drift = 0.5 * air_speed * (centre[0] - Rb) / (20 * D - Rb)
+        vels.append(np.tile([jet_speed * 0.3 + drift, 0.0, 0.2 * jet_speed], (len(pts), 1)))
+        types.append(np.full(len(pts), d.FREE))
+        n_now += len(pts)
+    fluid = np.concatenate(parts)
+    v = np.concatenate(vels)
+    b = np.concatenate(types)
+    fluid += rng.uniform(-0.01 * dx, 0.01 * dx, size=fluid.shape)
+    st = _assemble(s, bound, fluid)
+    st.v[len(bound):] = v
+    st.b[len(bound):] = b
+    blocks = _blocks(len(bound), st.n, bound_solver=d.GHOST)
+    fl = blocks[-1]
+    fl.aero_norm = (0.0, 0.0, 1.0)
+    fl.aeroconst = 0.0
+    return Case("jet_crossflow", s, st, blocks)

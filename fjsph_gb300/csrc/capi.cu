@@ -1,0 +1,1488 @@
+/*
+ * capi.cu -- the C ABI of the GB300 WCSPH hot path: device context, state hand-over, and the
+ * host-side sequencing of the kernels that replaces Integrator (src/Integration.cpp) and the free
+ * functions of src/Neighbours.cpp, src/Shifting.cpp, src/Geometry.cpp, src/Resid.cpp,
+ * src/Runge_Kutta.cpp and src/Newmark_Beta.cpp.
+ *
+ * Within one step nothing returns to the host except the scalars the reference's control flow
+ * branches on: the time step (find_timestep), the neighbour-list size (to size the CSR storage)
+ * and, for Newmark-Beta, the residual of each sub-iteration.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+using namespace fjsph;
+
+#define CU(call)                                                                                              \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess) {                                                                              \
+            std::fprintf(stderr, "fjsph: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return FJSPH_E_CUDA;                                                                              \
+        }                                                                                                     \
+    } while (0)
+
+#define TRY(call)                           \
+    do {                                    \
+        int r_ = (call);                    \
+        if (r_ != FJSPH_OK) return r_;      \
+    } while (0)
+
+namespace {
+
+struct HostInlet {
+    int32_t block = -1, fixed_vel_or_dynamic = 0;
+    int64_t n_back = 0, depth = 0;
+    std::vector<int64_t> back_ref, buffer_ref; /* reference indices as given */
+    int32_t *d_back = nullptr, *d_buffer = nullptr;
+    double unorm[3] = {0, 0, 0};
+};
+
+} // namespace
+
+/* Pass profiler: pairs of events around each timed section, resolved lazily. */
+enum Pass {
+    PASS_SEARCH = 0,
+    PASS_REORDER,
+    PASS_PRESTEP,
+    PASS_SURFACE,
+    PASS_DISSIPATION,
+    PASS_SHIFT,
+    PASS_BOUNDARY,
+    PASS_RESID,
+    PASS_UPDATE,
+    PASS_REDUCE,
+    PASS_COPY,
+    PASS_TRANSFER,
+    PASS_COUNT
+};
+static_assert(PASS_COUNT == FJSPH_NPASS, "pass table");
+const char *kPassNames[PASS_COUNT] = {"neighbour_search", "reorder", "dsph_prestep", "detect_surface",
+                                      "dissipation", "particle_shift", "boundary", "residual",
+                                      "stage_update", "reductions", "state_copy", "host_transfer"};
+
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<std::pair<int, size_t>> marks; /* pass, index of start event (end = +1) */
+    double ms[PASS_COUNT] = {};
+    int64_t count[PASS_COUNT] = {};
+};
+
+struct fjsph_ctx {
+    fjsph_settings s{};
+    int D = 3;
+    int64_t cap = 0, n = 0, nb = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocs;
+
+    DevState st[3]{};
+    int ipn = 0, iW = 1, isp = 2;
+    int64_t *key = nullptr; /* reference index of each slot (shared by pn and W) */
+    int32_t *blk = nullptr; /* block of each slot */
+
+    double *xs[3] = {nullptr, nullptr, nullptr};
+    CellGrid G{};
+    int32_t *nbr_counts = nullptr;
+    int64_t *nbr_off = nullptr;
+    int32_t *nbr_idx = nullptr;
+    int64_t nbr_cap = 0, n_pairs = 0;
+    bool nbr_valid = false;
+    int64_t *scan_tmp64 = nullptr;
+    int64_t scan_tmp64_len = 0;
+    int32_t *new_of_old = nullptr, *reorder_tmp = nullptr;
+    int64_t reorder_tmp_len = 0;
+    int64_t searches = 0;
+    bool reorder_pending = true;
+
+    RKScratch S{};
+    double *nrm_tmp[3] = {nullptr, nullptr, nullptr};
+    double *vtmp[3] = {nullptr, nullptr, nullptr};
+    double *npd_part = nullptr;
+    DevScalars *dsc = nullptr; /* device */
+    DevScalars *hsc = nullptr; /* pinned host mirror */
+
+    std::vector<fjsph_block> blocks;
+    int64_t n_bound_blocks = 0;
+    std::vector<HostInlet> inlets;
+
+    bool pn_equals_W = false;
+    /* Integrator members (src/Integration.h:52-67) */
+    double safe_dt = 0, maxf = kEps, maxAf = kEps, maxRho_pc = kEps, maxRhoi = kEps, maxdrho = kEps;
+    double minST = 9999999.0, maxU = kEps, maxShift = kEps;
+    uint32_t iteration = 0;
+    int64_t launches = 0;
+    Profiler prof;
+    cudaEvent_t user_ev[16] = {};
+};
+
+namespace {
+
+DevState &PN(fjsph_ctx *c) { return c->st[c->ipn]; }
+DevState &WS(fjsph_ctx *c) { return c->st[c->iW]; }
+
+template <typename T>
+int dalloc(fjsph_ctx *c, T **p, int64_t count) {
+    *p = nullptr;
+    if (count <= 0) count = 1;
+    void *q = nullptr;
+    CU(cudaMalloc(&q, sizeof(T) * (size_t)count));
+    c->allocs.push_back(q);
+    *p = static_cast<T *>(q);
+    return FJSPH_OK;
+}
+
+int alloc_state(fjsph_ctx *c, DevState &S) {
+    const int D = c->D;
+    const int64_t cap = c->cap;
+    std::memset(&S, 0, sizeof(S));
+    auto vec = [&](double **a) -> int {
+        for (int k = 0; k < D; ++k) TRY(dalloc(c, &a[k], cap));
+        return FJSPH_OK;
+    };
+    TRY(vec(S.x));
+    TRY(vec(S.v));
+    TRY(vec(S.acc));
+    TRY(vec(S.Af));
+    TRY(vec(S.aVisc));
+    TRY(vec(S.cellV));
+    TRY(vec(S.gradRho));
+    TRY(vec(S.norm));
+    TRY(vec(S.vPert));
+    for (int k = 0; k < D * D; ++k) TRY(dalloc(c, &S.L[k], cap));
+    double **sc[] = {&S.Rrho, &S.rho,    &S.p,       &S.m,       &S.curve,  &S.norm_curve, &S.woccl,  &S.pDist,
+                     &S.deltaD, &S.cellP, &S.cellRho, &S.colourG, &S.colour, &S.lam,        &S.lam_nb, &S.kernsum};
+    for (double **a : sc) TRY(dalloc(c, a, cap));
+    TRY(dalloc(c, &S.part_id, cap));
+    TRY(dalloc(c, &S.cellID, cap));
+    TRY(dalloc(c, &S.b, cap));
+    TRY(dalloc(c, &S.surf, cap));
+    TRY(dalloc(c, &S.surfzone, cap));
+    S.key = c->key;
+    S.blk = c->blk;
+    return FJSPH_OK;
+}
+
+int64_t next_pow2(int64_t v) {
+    int64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+int validate_settings(const fjsph_settings *s) {
+    if (!s) return FJSPH_E_ARG;
+    if (s->dim != 2 && s->dim != 3) return FJSPH_E_ARG;
+    if (!(s->H > 0) || !(s->sr > 0) || !(s->W_correc > 0)) return FJSPH_E_ARG;
+    if (s->st_model < FJSPH_ST_PAIRWISE || s->st_model > FJSPH_ST_CSF) return FJSPH_E_ARG;
+    /* -DNOFROZEN -DLINEAR does not compile upstream (src/Resid.cpp:381 uses fluid.rho0) */
+    if ((s->variant & FJSPH_VAR_NOFROZEN) && (s->variant & FJSPH_VAR_LINEAR)) return FJSPH_E_UNSUPPORTED;
+    if (s->precision != FJSPH_PREC_FP64) return FJSPH_E_UNSUPPORTED;
+    if (s->asource != 0) return FJSPH_E_UNSUPPORTED;
+    return FJSPH_OK;
+}
+
+/* Boundary velocity at the current time: RK rule (src/Runge_Kutta.cpp:39-63) and NB rule
+ * (src/Newmark_Beta.cpp:71-96). */
+void block_velocities(const fjsph_ctx *c, const fjsph_block &B, double *vrk, double *vnb) {
+    for (int k = 0; k < 3; ++k) vrk[k] = vnb[k] = 0.0;
+    if (B.n_times != 0) {
+        for (int t = 0; t < B.n_times && t < FJSPH_MAX_TIMES; ++t) {
+            if (B.times[t] > c->s.current_time)
+                for (int k = 0; k < 3; ++k) vrk[k] = B.vels[t][k];
+            if (c->s.current_time > B.times[t])
+                for (int k = 0; k < 3; ++k) vnb[k] = B.vels[t][k];
+        }
+    } else {
+        for (int k = 0; k < 3; ++k) vrk[k] = vnb[k] = B.vels[0][k];
+    }
+}
+
+Params make_params(const fjsph_ctx *c) {
+    Params P;
+    std::memset(&P, 0, sizeof(P));
+    const fjsph_settings &s = c->s;
+    P.D = c->D;
+    P.variant = s.variant;
+    P.st_model = s.st_model;
+    P.pressure_rel = s.pressure_rel;
+    P.acase = s.acase;
+    P.use_lam = s.use_lam;
+    P.use_TAB_def = s.use_TAB_def;
+    P.H = s.H;
+    P.H_sq = s.H_sq;
+    P.sr = s.sr;
+    P.W_correc = s.W_correc;
+    P.W_dx = s.W_dx;
+    P.dx = s.dx;
+    P.particle_step = s.particle_step;
+    P.rho_rest = s.rho_rest;
+    P.B = s.B;
+    P.gam = s.gam;
+    P.speed_sound = s.speed_sound;
+    P.press_back = s.press_back;
+    P.rho_min = s.rho_min;
+    P.rho_max = s.rho_max;
+    P.visc_alpha = s.visc_alpha;
+    P.mu = s.mu;
+    P.nu = s.nu;
+    P.sig = s.sig;
+    P.dsph_cont = s.dsph_cont;
+    P.max_shift_vel = s.max_shift_vel;
+    for (int k = 0; k < 3; ++k) {
+        P.grav[k] = s.grav[k];
+        P.v_inf[k] = s.v_inf[k];
+    }
+    P.L = s.L;
+    P.A_sphere = s.A_sphere;
+    P.A_plate = s.A_plate;
+    P.mu_g = s.mu_g;
+    P.sos = s.sos;
+    P.gamma_g = s.gamma_g;
+    P.lam_cutoff = s.lam_cutoff;
+    P.interp_fac = s.interp_fac;
+    P.i_n_full = s.i_n_full;
+    P.ycoef = s.ycoef;
+    P.Cb = s.Cb;
+    P.rho_g = s.rho_g;
+    P.nb_beta = s.nb_beta;
+    P.nb_gamma = s.nb_gamma;
+    P.n = c->n;
+    P.nb = c->nb;
+    P.nblocks = (int32_t)std::min<size_t>(c->blocks.size(), kMaxBlocks);
+    for (int b = 0; b < P.nblocks; ++b) {
+        const fjsph_block &B = c->blocks[b];
+        DevBlock &d = P.blocks[b];
+        d.is_fluid = B.is_fluid;
+        d.bound_solver = B.bound_solver;
+        d.no_slip = B.no_slip;
+        d.block_type = B.block_type;
+        d.fixed_vel_or_dynamic = B.fixed_vel_or_dynamic;
+        d.n_times = B.n_times;
+        block_velocities(c, B, d.vel_rk, d.vel_nb);
+        for (int k = 0; k < 3; ++k) d.aero_norm[k] = B.aero_norm[k];
+        d.aeroconst = B.aeroconst;
+        double nrm = 0.0;
+        for (int k = 0; k < c->D; ++k) nrm += B.insert_norm[k] * B.insert_norm[k];
+        nrm = std::sqrt(nrm);
+        for (int k = 0; k < 3; ++k) d.insert_unorm[k] = nrm > 0 ? B.insert_norm[k] / nrm : B.insert_norm[k];
+    }
+    return P;
+}
+
+DevNbr make_nbr(const fjsph_ctx *c) {
+    DevNbr N;
+    N.off = c->nbr_off;
+    N.idx = c->nbr_idx;
+    for (int k = 0; k < 3; ++k) N.xs[k] = c->xs[k];
+    return N;
+}
+
+int sync(fjsph_ctx *c) {
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaGetLastError());
+    return FJSPH_OK;
+}
+
+/* Scoped profiling section: records a start event on construction and an end event on
+ * destruction when the profiler is on. */
+struct Section {
+    fjsph_ctx *c;
+    int pass;
+    size_t idx = (size_t)-1;
+    Section(fjsph_ctx *c_, int pass_) : c(c_), pass(pass_) {
+        Profiler &p = c->prof;
+        if (!p.on) return;
+        if (p.used + 2 > p.pool.size()) {
+            for (int k = 0; k < 64; ++k) {
+                cudaEvent_t e;
+                if (cudaEventCreate(&e) != cudaSuccess) return;
+                p.pool.push_back(e);
+            }
+        }
+        idx = p.used;
+        p.used += 2;
+        cudaEventRecord(p.pool[idx], c->stream);
+    }
+    ~Section() {
+        if (idx == (size_t)-1) return;
+        Profiler &p = c->prof;
+        cudaEventRecord(p.pool[idx + 1], c->stream);
+        p.marks.push_back({pass, idx});
+    }
+};
+
+int profile_collect(fjsph_ctx *c) {
+    Profiler &p = c->prof;
+    if (p.marks.empty()) return FJSPH_OK;
+    CU(cudaStreamSynchronize(c->stream));
+    for (auto &m : p.marks) {
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, p.pool[m.second], p.pool[m.second + 1]));
+        p.ms[m.first] += ms;
+        p.count[m.first] += 1;
+    }
+    p.marks.clear();
+    p.used = 0;
+    return FJSPH_OK;
+}
+
+/* ---- slot <-> reference index --------------------------------------------------------------- */
+int download_keys(fjsph_ctx *c, std::vector<int64_t> &keys) {
+    keys.resize(c->n);
+    if (c->n) CU(cudaMemcpyAsync(keys.data(), c->key, sizeof(int64_t) * c->n, cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int block_of_ref(const fjsph_ctx *c, int64_t r) {
+    for (size_t b = 0; b < c->blocks.size(); ++b)
+        if (r >= c->blocks[b].first && r < c->blocks[b].second) return (int)b;
+    return -1;
+}
+
+int upload_blk(fjsph_ctx *c, const std::vector<int64_t> &keys) {
+    std::vector<int32_t> hb(c->n);
+    for (int64_t s = 0; s < c->n; ++s) {
+        int b = block_of_ref(c, keys[s]);
+        if (b < 0) return FJSPH_E_ARG;
+        hb[s] = b;
+    }
+    if (c->n) CU(cudaMemcpyAsync(c->blk, hb.data(), sizeof(int32_t) * c->n, cudaMemcpyHostToDevice, c->stream));
+    return sync(c);
+}
+
+int upload_inlets(fjsph_ctx *c, const std::vector<int64_t> &keys) {
+    if (c->inlets.empty()) return FJSPH_OK;
+    std::vector<int32_t> slot_of_ref(c->n, -1);
+    for (int64_t s = 0; s < c->n; ++s)
+        if (keys[s] >= 0 && keys[s] < c->n) slot_of_ref[keys[s]] = (int32_t)s;
+    for (HostInlet &I : c->inlets) {
+        std::vector<int32_t> b(I.n_back), f(I.n_back * I.depth);
+        for (int64_t i = 0; i < I.n_back; ++i) {
+            if (I.back_ref[i] < 0 || I.back_ref[i] >= c->n) return FJSPH_E_ARG;
+            b[i] = slot_of_ref[I.back_ref[i]];
+        }
+        for (int64_t i = 0; i < I.n_back * I.depth; ++i) {
+            if (I.buffer_ref[i] < 0 || I.buffer_ref[i] >= c->n) return FJSPH_E_ARG;
+            f[i] = slot_of_ref[I.buffer_ref[i]];
+        }
+        if (!b.empty()) CU(cudaMemcpyAsync(I.d_back, b.data(), sizeof(int32_t) * b.size(), cudaMemcpyHostToDevice, c->stream));
+        if (!f.empty())
+            CU(cudaMemcpyAsync(I.d_buffer, f.data(), sizeof(int32_t) * f.size(), cudaMemcpyHostToDevice, c->stream));
+    }
+    return sync(c);
+}
+
+/* ---- host <-> device state transfer ----------------------------------------------------------- */
+struct HostField {
+    const char *name;
+    int comps; /* 1, D or D*D */
+    int type;  /* 0 double, 1 int64, 2 int32 */
+};
+
+void view_ptrs(const fjsph_state_view *v, std::vector<void *> &ptr) {
+    ptr = {v->xi,         v->v,      v->acc,   v->Af,      v->aVisc,   v->cellV,  v->gradRho, v->norm,
+           v->vPert,      v->L,      v->Rrho,  v->rho,     v->p,       v->m,      v->curve,   v->norm_curve,
+           v->woccl,      v->pDist,  v->deltaD, v->cellP,  v->cellRho, v->colourG, v->colour, v->lam,
+           v->lam_nb,     v->kernsum, v->part_id, v->cellID, v->b,      v->surf,   v->surfzone};
+}
+
+/* Device arrays in the same order as view_ptrs, with component counts. */
+void dev_ptrs(const DevState &S, int D, std::vector<std::vector<void *>> &ptr, std::vector<int> &type) {
+    ptr.clear();
+    type.clear();
+    auto vec = [&](double *const a[3]) {
+        std::vector<void *> p;
+        for (int k = 0; k < D; ++k) p.push_back(a[k]);
+        ptr.push_back(p);
+        type.push_back(0);
+    };
+    vec(S.x);
+    vec(S.v);
+    vec(S.acc);
+    vec(S.Af);
+    vec(S.aVisc);
+    vec(S.cellV);
+    vec(S.gradRho);
+    vec(S.norm);
+    vec(S.vPert);
+    {
+        std::vector<void *> p;
+        for (int k = 0; k < D * D; ++k) p.push_back(S.L[k]);
+        ptr.push_back(p);
+        type.push_back(0);
+    }
+    double *sc[] = {S.Rrho, S.rho,     S.p,       S.m,      S.curve, S.norm_curve, S.woccl,  S.pDist,
+                    S.deltaD, S.cellP, S.cellRho, S.colourG, S.colour, S.lam,      S.lam_nb, S.kernsum};
+    for (double *a : sc) {
+        ptr.push_back({a});
+        type.push_back(0);
+    }
+    ptr.push_back({S.part_id});
+    type.push_back(1);
+    ptr.push_back({S.cellID});
+    type.push_back(1);
+    ptr.push_back({S.b});
+    type.push_back(2);
+    ptr.push_back({S.surf});
+    type.push_back(2);
+    ptr.push_back({S.surfzone});
+    type.push_back(2);
+}
+
+int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, const std::vector<int64_t> &keys, bool up) {
+    std::vector<void *> hp;
+    view_ptrs(v, hp);
+    std::vector<std::vector<void *>> dp;
+    std::vector<int> type;
+    dev_ptrs(S, c->D, dp, type);
+    const int64_t n = c->n;
+    for (void *p : hp)
+        if (!p) return FJSPH_E_ARG;
+    std::vector<char> tmp(sizeof(double) * std::max<int64_t>(n, 1));
+    for (size_t f = 0; f < dp.size(); ++f) {
+        const int comps = (int)dp[f].size();
+        const size_t es = type[f] == 2 ? 4 : 8;
+        for (int k = 0; k < comps; ++k) {
+            if (up) {
+                for (int64_t s = 0; s < n; ++s) {
+                    const int64_t r = keys[s];
+                    std::memcpy(&tmp[s * es], static_cast<char *>(hp[f]) + (r * comps + k) * es, es);
+                }
+                CU(cudaMemcpy(dp[f][k], tmp.data(), es * n, cudaMemcpyHostToDevice));
+            } else {
+                CU(cudaMemcpy(tmp.data(), dp[f][k], es * n, cudaMemcpyDeviceToHost));
+                for (int64_t s = 0; s < n; ++s) {
+                    const int64_t r = keys[s];
+                    std::memcpy(static_cast<char *>(hp[f]) + (r * comps + k) * es, &tmp[s * es], es);
+                }
+            }
+        }
+    }
+    return FJSPH_OK;
+}
+
+/* ---- neighbour search --------------------------------------------------------------------------- */
+int reorder_states(fjsph_ctx *c, const Params &P) {
+    cudaStream_t s = c->stream;
+    launch_reorder_map(P, c->G, c->new_of_old, c->reorder_tmp, c->reorder_tmp_len, s);
+    c->launches += 5;
+    /* permute pn and W through the spare state */
+    for (int which = 0; which < 2; ++which) {
+        int &role = which == 0 ? c->ipn : c->iW;
+        launch_permute(state_fields(c->st[role], c->D), state_fields(c->st[c->isp], c->D), c->new_of_old, c->n, s);
+        std::swap(role, c->isp);
+        c->launches += 1;
+    }
+    /* shared per-slot arrays: key and blk (through the spare state's i64/i32 scratch) */
+    {
+        FieldList a, b;
+        a.i64[a.ni64++] = c->key;
+        b.i64[b.ni64++] = c->st[c->isp].part_id;
+        a.i32[a.ni32++] = c->blk;
+        b.i32[b.ni32++] = c->st[c->isp].b;
+        launch_permute(a, b, c->new_of_old, c->n, s);
+        CU(cudaMemcpyAsync(c->key, c->st[c->isp].part_id, sizeof(int64_t) * c->n, cudaMemcpyDeviceToDevice, s));
+        CU(cudaMemcpyAsync(c->blk, c->st[c->isp].b, sizeof(int32_t) * c->n, cudaMemcpyDeviceToDevice, s));
+        c->launches += 1;
+    }
+    for (HostInlet &I : c->inlets) {
+        launch_remap_i32(I.d_back, I.n_back, c->new_of_old, s);
+        launch_remap_i32(I.d_buffer, I.n_back * I.depth, c->new_of_old, s);
+        c->launches += 2;
+    }
+    for (int k = 0; k < c->D; ++k)
+        CU(cudaMemcpyAsync(c->xs[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
+    launch_refresh_xf(P, c->xs, c->G, s);
+    c->launches += 1;
+    return FJSPH_OK;
+}
+
+int search(fjsph_ctx *c) {
+    if (c->n == 0) return FJSPH_E_STATE;
+    if (c->prof.on && c->prof.used > 4096) TRY(profile_collect(c));
+    cudaStream_t s = c->stream;
+    Params P = make_params(c);
+    Section sec(c, PASS_SEARCH);
+    launch_bbox(P, WS(c), c->G, s);
+    launch_hash_and_count(P, WS(c), c->xs, c->G, s);
+    launch_scan_i32(c->G.count, c->G.start, c->G.table_size, c->G.scan_tmp, s);
+    launch_scatter_sort(P, c->G, s);
+    c->launches += 2 + 1 + 3 + 2;
+    const bool due = c->s.reorder_interval > 0 && (c->reorder_pending || (c->searches % c->s.reorder_interval) == 0);
+    if (due) {
+        Section sr(c, PASS_REORDER);
+        TRY(reorder_states(c, P));
+        c->reorder_pending = false;
+    }
+    c->searches++;
+    launch_nbr_count(P, c->xs, c->G, c->nbr_counts, s);
+    launch_scan_i64(c->nbr_counts, c->nbr_off, c->n, c->scan_tmp64, s);
+    c->launches += 4;
+    int64_t total = 0;
+    CU(cudaMemcpyAsync(&c->hsc->red[15], c->nbr_off + c->n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    TRY(sync(c));
+    std::memcpy(&total, &c->hsc->red[15], sizeof(int64_t));
+    if (total > c->nbr_cap) {
+        int64_t ncap = std::max<int64_t>(total + total / 4, c->nbr_cap * 2);
+        if (ncap >= ((int64_t)1 << 31)) return FJSPH_E_NEIGHBOUR;
+        CU(cudaFree(c->nbr_idx));
+        c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->nbr_idx), c->allocs.end());
+        TRY(dalloc(c, &c->nbr_idx, ncap));
+        c->nbr_cap = ncap;
+    }
+    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, s);
+    c->launches += 1;
+    c->n_pairs = total;
+    c->nbr_valid = true;
+    return FJSPH_OK;
+}
+
+/* ---- passes ----------------------------------------------------------------------------------------- */
+__global__ void k_finish_npd(DevScalars *d, double inv_n) { d->npd = d->red[0] * inv_n; }
+__global__ void k_set_scalar(double *dst, double v) { *dst = v; }
+
+int prestep_npd(fjsph_ctx *c, const Params &P) {
+    Section sec(c, PASS_PRESTEP);
+    launch_dsph_prestep(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+    launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
+    k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
+    c->launches += 4;
+    return FJSPH_OK;
+}
+
+/* npd only (Runge-Kutta first pre-pass, see integrate_no_update) */
+int npd_only(fjsph_ctx *c, const Params &P) {
+    Section sec(c, PASS_PRESTEP);
+    launch_npd_only(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+    launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
+    k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
+    c->launches += 4;
+    return FJSPH_OK;
+}
+
+int prestep_passes(fjsph_ctx *c) {
+    if (!c->nbr_valid) return FJSPH_E_STATE;
+    Params P = make_params(c);
+    DevNbr N = make_nbr(c);
+    cudaStream_t s = c->stream;
+    TRY(prestep_npd(c, P));
+    {
+        Section sec(c, PASS_SURFACE);
+        launch_aero_velocity(P, WS(c), N, s);
+        launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
+        c->launches += 4;
+    }
+    if (!(c->s.variant & FJSPH_VAR_NOFROZEN)) {
+        Section sec(c, PASS_DISSIPATION);
+        launch_dissipation(P, WS(c), N, s);
+        c->launches++;
+    }
+    if (c->s.variant & FJSPH_VAR_ALE) {
+        Section sec(c, PASS_SHIFT);
+        launch_particle_shift(P, WS(c), N, s);
+        c->launches++;
+    }
+    {
+        Section sec(c, PASS_UPDATE);
+        launch_pipe_outlet(P, WS(c), s);
+        c->launches++;
+    }
+    c->pn_equals_W = false;
+    return FJSPH_OK;
+}
+
+bool has_solver(const fjsph_ctx *c, int solver) {
+    for (int64_t b = 0; b < c->n_bound_blocks; ++b)
+        if (c->blocks[b].bound_solver == solver) return true;
+    return false;
+}
+bool has_no_slip(const fjsph_ctx *c) {
+    for (int64_t b = 0; b < c->n_bound_blocks; ++b)
+        if (c->blocks[b].no_slip) return true;
+    return false;
+}
+
+/* Boundary section of a stage: velocities, no-slip mirror, solver pass. */
+int boundary_section(fjsph_ctx *c, const Params &P, int nb_rule) {
+    if (c->nb == 0) return FJSPH_OK;
+    Section sec(c, PASS_BOUNDARY);
+    DevNbr N = make_nbr(c);
+    cudaStream_t s = c->stream;
+    launch_bound_velocity(P, WS(c), nb_rule, s);
+    c->launches++;
+    if (has_no_slip(c)) {
+        launch_no_slip(P, WS(c), N, c->vtmp, s);
+        c->launches += 2;
+    }
+    if (has_solver(c, FJSPH_DBC)) {
+        launch_bound_dbc(P, WS(c), s);
+        c->launches++;
+    }
+    if (has_solver(c, FJSPH_PRESSURE_G)) {
+        launch_bound_pressure(P, WS(c), N, s);
+        c->launches++;
+    }
+    if (has_solver(c, FJSPH_GHOST)) {
+        launch_bound_ghost(P, WS(c), N, c->S.near_inlet, s);
+        c->launches++;
+    }
+    return FJSPH_OK;
+}
+
+DevInlet dev_inlet(const fjsph_ctx *c, const HostInlet &I) {
+    DevInlet d;
+    d.block = I.block;
+    d.fixed_vel_or_dynamic = I.fixed_vel_or_dynamic;
+    d.n_back = I.n_back;
+    d.depth = I.depth;
+    d.back = I.d_back;
+    d.buffer = I.d_buffer;
+    for (int k = 0; k < 3; ++k) d.unorm[k] = I.unorm[k];
+    (void)c;
+    return d;
+}
+
+void inlet_buffers(fjsph_ctx *c, const Params &P, int mode, double dt_scale) {
+    for (const HostInlet &I : c->inlets) {
+        if (I.n_back == 0 || I.depth == 0) continue;
+        launch_inlet_buffers(P, PN(c), WS(c), c->S, dev_inlet(c, I), mode, &c->dsc->dt, dt_scale, c->stream);
+        c->launches++;
+    }
+}
+
+/* do_runge_kutta_intermediate_step on W (W already holds part_prev). stage 1, 2, 3. */
+int rk_intermediate(fjsph_ctx *c, int stage, double dt_scale) {
+    Params P = make_params(c);
+    cudaStream_t s = c->stream;
+    TRY(boundary_section(c, P, 0));
+    const double sum_w = stage == 2 ? 2.0 : (stage == 3 ? 1.0 : 0.0);
+    if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
+        launch_bound_rho_update(P, PN(c), WS(c), c->S, 0, sum_w, &c->dsc->dt, dt_scale, s);
+        c->launches++;
+    }
+    {
+        Section sec(c, PASS_RESID);
+        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, s);
+    }
+    {
+        Section sec(c, PASS_UPDATE);
+        launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, &c->dsc->dt, dt_scale, s);
+    }
+    c->launches += 2;
+    inlet_buffers(c, P, 0, dt_scale);
+    c->pn_equals_W = false;
+    return FJSPH_OK;
+}
+
+int rk_final(fjsph_ctx *c) {
+    Params P = make_params(c);
+    cudaStream_t s = c->stream;
+    TRY(boundary_section(c, P, 0));
+    if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
+        launch_bound_rho_update(P, PN(c), WS(c), c->S, 1, 0.0, &c->dsc->dt, 1.0, s);
+        c->launches++;
+    }
+    {
+        Section sec(c, PASS_RESID);
+        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, s);
+    }
+    {
+        Section sec(c, PASS_UPDATE);
+        for (int k = 0; k < c->D; ++k)
+            CU(cudaMemcpyAsync(c->S.xsnap[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
+        launch_rk_final_update(P, PN(c), WS(c), c->S, &c->dsc->dt, s);
+    }
+    c->launches += 2;
+    inlet_buffers(c, P, 1, 1.0);
+    c->pn_equals_W = false;
+    return FJSPH_OK;
+}
+
+int sq_disp(fjsph_ctx *c, double *const ref[3], double *out_host) {
+    Params P = make_params(c);
+    Section sec(c, PASS_REDUCE);
+    launch_sq_disp_sum(P, WS(c), ref, c->S, &c->dsc->red[1], c->stream);
+    c->launches += 2;
+    CU(cudaMemcpyAsync(&c->hsc->red[1], &c->dsc->red[1], sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    TRY(sync(c));
+    *out_host = c->hsc->red[1];
+    return FJSPH_OK;
+}
+
+int set_dt_device(fjsph_ctx *c) {
+    k_set_scalar<<<1, 1, 0, c->stream>>>(&c->dsc->dt, c->s.delta_t);
+    c->launches++;
+    return FJSPH_OK;
+}
+int set_npd_device(fjsph_ctx *c, double npd) {
+    k_set_scalar<<<1, 1, 0, c->stream>>>(&c->dsc->npd, npd);
+    c->launches++;
+    return FJSPH_OK;
+}
+
+int copy_state(fjsph_ctx *c, int from, int to) {
+    Section sec(c, PASS_COPY);
+    launch_copy(state_fields(c->st[from], c->D), state_fields(c->st[to], c->D), c->n, c->stream);
+    c->launches++;
+    return FJSPH_OK;
+}
+
+/* find_timestep (src/Integration.cpp:370-443): reductions on the device, the scalar tail here. */
+int find_timestep(fjsph_ctx *c, double *dt_out) {
+    Params P = make_params(c);
+    Section sec(c, PASS_REDUCE);
+    launch_timestep_reduce(P, WS(c), c->S, &c->dsc->red[2], c->stream);
+    c->launches += 2;
+    CU(cudaMemcpyAsync(&c->hsc->red[2], &c->dsc->red[2], sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
+    TRY(sync(c));
+    const double *r = &c->hsc->red[2];
+    const fjsph_settings &s = c->s;
+    const bool any = c->n > c->nb;
+    c->maxf = any ? r[0] : kEps;
+    c->maxAf = any ? r[1] : kEps;
+    c->maxdrho = any ? r[2] : kEps;
+    c->maxRhoi = any ? r[3] : kEps;
+    c->minST = any ? r[4] : 9999999.0;
+    c->maxU = any ? r[5] : kEps;
+    if ((s.variant & FJSPH_VAR_ALE) && any) c->maxShift = std::max(c->maxShift, r[6]);
+    c->maxRho_pc = 100 * c->maxRhoi / s.rho_rest;
+    const double kPi_ = 3.14159265358979323846;
+    (void)kPi_;
+    double fac[6] = {0.25 * std::sqrt(s.H / c->maxf), 2 * s.H / c->maxU, 0.125 * s.H_sq * s.rho_rest / s.mu,
+                     0.067 * c->minST, 0.5 * std::sqrt(s.H / c->maxdrho), 1.5 * s.H / s.speed_sound};
+    double mn = fac[0];
+    for (int k = 1; k < 6; ++k)
+        if (fac[k] < mn) mn = fac[k];
+    c->safe_dt = 0.75 * mn;
+    double dt = s.cfl * c->safe_dt;
+    if (dt < s.delta_t_min)
+        dt = s.delta_t_min;
+    else if (dt > s.delta_t_max)
+        dt = s.delta_t_max;
+    if (dt > s.last_frame_time + s.frame_time_interval - s.current_time)
+        dt = s.last_frame_time + s.frame_time_interval - s.current_time + s.delta_t_min;
+    *dt_out = dt;
+    return FJSPH_OK;
+}
+
+/* Newmark_Beta::Do_NB_Iter on W. */
+int nb_iter(fjsph_ctx *c) {
+    Params P = make_params(c);
+    cudaStream_t s = c->stream;
+    TRY(boundary_section(c, P, 1));
+    {
+        Section sec(c, PASS_RESID);
+        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, s);
+    }
+    c->launches++;
+    if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
+        launch_bound_rho_update(P, PN(c), WS(c), c->S, 2, 0.0, &c->dsc->dt, 1.0, s);
+        c->launches++;
+    }
+    launch_nb_update(P, PN(c), WS(c), &c->dsc->dt, s);
+    c->launches++;
+    inlet_buffers(c, P, 2, 1.0);
+    c->pn_equals_W = false;
+    return FJSPH_OK;
+}
+
+/* Newmark_Beta::Check_Error (src/Newmark_Beta.cpp:10-52); xih is S.xsnap. */
+int nb_check_error(fjsph_ctx *c, double &rms_error, double &logbase, int &state) {
+    double errsum = 0.0;
+    TRY(sq_disp(c, c->S.xsnap, &errsum));
+    const double nf = double(c->n - c->nb);
+    const double log_error = std::log10(std::sqrt(errsum / nf));
+    if (c->iteration == 0) logbase = log_error;
+    rms_error = log_error - logbase;
+    state = 0;
+    if ((int64_t)c->iteration > (int64_t)c->s.max_subits) {
+        if (rms_error > 0.0) {
+            TRY(copy_state(c, c->ipn, c->iW));
+            TRY(search(c));
+            c->s.delta_t = 0.5 * c->s.delta_t;
+            TRY(set_dt_device(c));
+            c->iteration = 0;
+            rms_error = 0.0;
+            state = -1;
+            return FJSPH_OK;
+        }
+        state = 1;
+    }
+    return FJSPH_OK;
+}
+
+int save_xsnap(fjsph_ctx *c) {
+    for (int k = 0; k < c->D; ++k)
+        CU(cudaMemcpyAsync(c->S.xsnap[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    return FJSPH_OK;
+}
+
+int newmark_beta_loop(fjsph_ctx *c, double &logbase, double &rms_error) {
+    rms_error = 0.0;
+    int restarts = 0;
+    while (rms_error > c->s.min_residual) {
+        TRY(save_xsnap(c));
+        TRY(nb_iter(c));
+        int st = 0;
+        TRY(nb_check_error(c, rms_error, logbase, st));
+        if (st == 0)
+            c->iteration++;
+        else if (st == 1)
+            break;
+        else if (++restarts > 64)
+            return FJSPH_E_NONFINITE; /* the reference would halve dt without bound here */
+    }
+    return FJSPH_OK;
+}
+
+int get_first_rk(fjsph_ctx *c, double &logbase) {
+    TRY(set_dt_device(c));
+    if (!c->pn_equals_W) TRY(copy_state(c, c->ipn, c->iW));
+    TRY(rk_intermediate(c, 1, 0.5));
+    double e = 0.0;
+    TRY(sq_disp(c, PN(c).x, &e));
+    logbase = std::log10(std::sqrt(e / double(c->n - c->nb)));
+    return FJSPH_OK;
+}
+
+int runge_kutta4(fjsph_ctx *c, double logbase, double &rms) {
+    TRY(set_dt_device(c));
+    Params P = make_params(c);
+    launch_rk_init_sums(P, PN(c), WS(c), c->S, c->stream);
+    c->launches++;
+    TRY(rk_intermediate(c, 2, 0.5));
+    TRY(rk_intermediate(c, 3, 1.0));
+    TRY(rk_final(c));
+    double e = 0.0;
+    TRY(sq_disp(c, c->S.xsnap, &e));
+    rms = std::log10(std::sqrt(e / double(c->n - c->nb))) - logbase;
+    return FJSPH_OK;
+}
+
+bool needs_update_data(const fjsph_ctx *c) {
+    for (int64_t b = c->n_bound_blocks; b < (int64_t)c->blocks.size(); ++b) {
+        if (c->blocks[b].block_type == kInletZone) return true;
+        if (c->blocks[b].delconst != kDefaultVal) return true;
+    }
+    return false;
+}
+
+/* Integrator::integrate_no_update (src/Integration.cpp:27-107).  skip_dead: under Runge-Kutta the
+ * first pre-pass results on pnp1 are overwritten by Get_First_RK's copy of pn before anything
+ * reads them, except npd; the whole-step path then only computes npd. */
+int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
+    c->iteration = 0;
+    double logbase = 0.0;
+    rms_error = 0.0;
+    double dt = 0.0;
+    TRY(find_timestep(c, &dt));
+    c->s.delta_t = dt;
+    TRY(set_dt_device(c));
+    TRY(search(c));
+    const bool rk = c->s.solver_type == FJSPH_RUNGE_KUTTA;
+    if (rk && skip_dead) {
+        if (c->s.st_model == FJSPH_ST_PAIRWISE) {
+            Params P = make_params(c);
+            TRY(npd_only(c, P));
+        }
+    } else {
+        TRY(prestep_passes(c));
+    }
+    if (rk) {
+        TRY(get_first_rk(c, logbase));
+    } else {
+        TRY(save_xsnap(c));
+        TRY(nb_iter(c));
+        int st = 0;
+        TRY(nb_check_error(c, rms_error, logbase, st));
+        c->iteration++;
+    }
+    TRY(search(c));
+    TRY(prestep_passes(c));
+    if (rk) {
+        TRY(runge_kutta4(c, logbase, rms_error));
+    } else {
+        TRY(newmark_beta_loop(c, logbase, rms_error));
+    }
+    return FJSPH_OK;
+}
+
+/* Integrator::integrate (src/Integration.cpp:233-303). */
+int integrate(fjsph_ctx *c, double &step_error) {
+    if (needs_update_data(c)) return FJSPH_E_UNSUPPORTED;
+    TRY(integrate_no_update(c, step_error, true));
+    /* update_data: zero-density guard (src/Integration.cpp:116-124) and pn = pnp1 */
+    launch_density_guard(make_params(c), WS(c), c->stream);
+    c->launches++;
+    TRY(copy_state(c, c->iW, c->ipn));
+    c->pn_equals_W = true;
+    fjsph_settings &I = c->s;
+    I.current_time += I.delta_t;
+    if (step_error > I.min_residual || c->maxRho_pc > I.rho_max_iter) {
+        if (step_error > 0.6 * I.min_residual) {
+            I.cfl = std::max(I.cfl_min, I.cfl - I.cfl_step);
+            I.n_unstable = 0;
+        } else if (I.n_unstable > I.n_unstable_limit) {
+            I.cfl = std::max(I.cfl_min, I.cfl - I.cfl_step);
+            I.n_unstable = 0;
+        } else
+            I.n_unstable++;
+    } else
+        I.n_unstable = 0;
+    if (c->iteration < I.subits_factor * I.max_subits && I.n_unstable == 0) {
+        if (I.n_stable > I.n_stable_limit) {
+            I.cfl = std::min(I.cfl_max, I.cfl + I.cfl_step);
+            I.n_stable = 0;
+        } else
+            I.n_stable++;
+    } else
+        I.n_stable = 0;
+    return FJSPH_OK;
+}
+
+int check_ctx(fjsph_ctx *c) { return c ? FJSPH_OK : FJSPH_E_ARG; }
+int need_state(fjsph_ctx *c) { return (c && c->n > 0) ? FJSPH_OK : FJSPH_E_STATE; }
+int need_nbr(fjsph_ctx *c) {
+    if (!c || c->n == 0) return FJSPH_E_STATE;
+    return c->nbr_valid ? FJSPH_OK : FJSPH_E_STATE;
+}
+
+} // namespace
+
+/* ================================================================================================ */
+extern "C" {
+
+const char *fjsph_status_string(int status) {
+    switch (status) {
+    case FJSPH_OK:
+        return "ok";
+    case FJSPH_E_ARG:
+        return "invalid argument";
+    case FJSPH_E_CUDA:
+        return "CUDA runtime error";
+    case FJSPH_E_CAPACITY:
+        return "particle count above context capacity";
+    case FJSPH_E_NEIGHBOUR:
+        return "neighbour list storage exhausted";
+    case FJSPH_E_NONFINITE:
+        return "non-finite values or divergent integration";
+    case FJSPH_E_UNSUPPORTED:
+        return "unsupported option or variant combination";
+    case FJSPH_E_STATE:
+        return "call order error";
+    default:
+        return "unknown status";
+    }
+}
+
+int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out) {
+    if (!out) return FJSPH_E_ARG;
+    *out = nullptr;
+    TRY(validate_settings(s));
+    if (capacity <= 0 || capacity >= ((int64_t)1 << 31)) return FJSPH_E_ARG;
+    fjsph_ctx *c = new fjsph_ctx();
+    c->s = *s;
+    c->D = s->dim;
+    c->cap = capacity;
+    auto fail = [&](int r) {
+        fjsph_ctx_destroy(c);
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FJSPH_E_CUDA);
+    int r = FJSPH_OK;
+#define A(call)                  \
+    do {                         \
+        r = (call);              \
+        if (r != FJSPH_OK) return fail(r); \
+    } while (0)
+    A(dalloc(c, &c->key, capacity));
+    A(dalloc(c, &c->blk, capacity));
+    for (int i = 0; i < 3; ++i) A(alloc_state(c, c->st[i]));
+    for (int k = 0; k < c->D; ++k) {
+        A(dalloc(c, &c->xs[k], capacity));
+        A(dalloc(c, &c->nrm_tmp[k], capacity));
+        A(dalloc(c, &c->vtmp[k], capacity));
+        A(dalloc(c, &c->S.Sx[k], capacity));
+        A(dalloc(c, &c->S.Sv[k], capacity));
+        A(dalloc(c, &c->S.xsnap[k], capacity));
+    }
+    A(dalloc(c, &c->S.Sr, capacity));
+    A(dalloc(c, &c->S.near_inlet, capacity));
+    c->S.part_len = 16 * 1216;
+    A(dalloc(c, &c->S.part, c->S.part_len));
+    A(dalloc(c, &c->npd_part, capacity));
+    CellGrid &G = c->G;
+    G.table_size = next_pow2(std::max<int64_t>(2 * capacity, 1024));
+    A(dalloc(c, &G.hash, capacity));
+    A(dalloc(c, &G.count, G.table_size + 1));
+    A(dalloc(c, &G.start, G.table_size + 1));
+    A(dalloc(c, &G.sorted, capacity));
+    A(dalloc(c, &G.sorted_xf, capacity));
+    A(dalloc(c, &G.xf, capacity));
+    A(dalloc(c, &G.bbox, 8));
+    A(dalloc(c, &G.grid, 4));
+    G.scan_tmp_len = std::max<int64_t>(G.table_size / 2048 + 16, 304 * 6 * 2 + 16);
+    A(dalloc(c, &G.scan_tmp, G.scan_tmp_len));
+    A(dalloc(c, &c->nbr_counts, capacity));
+    A(dalloc(c, &c->nbr_off, capacity + 1));
+    c->scan_tmp64_len = capacity / 2048 + 16;
+    A(dalloc(c, &c->scan_tmp64, c->scan_tmp64_len));
+    c->nbr_cap = capacity * (c->D == 3 ? 96 : 28);
+    A(dalloc(c, &c->nbr_idx, c->nbr_cap));
+    A(dalloc(c, &c->new_of_old, capacity));
+    c->reorder_tmp_len = 2 * capacity + 1 + capacity / 2048 + 16;
+    A(dalloc(c, &c->reorder_tmp, c->reorder_tmp_len));
+    A(dalloc(c, &c->dsc, 1));
+#undef A
+    if (cudaMallocHost(&c->hsc, sizeof(DevScalars)) != cudaSuccess) return fail(FJSPH_E_CUDA);
+    std::memset(c->hsc, 0, sizeof(DevScalars));
+    if (cudaMemsetAsync(c->dsc, 0, sizeof(DevScalars), c->stream) != cudaSuccess) return fail(FJSPH_E_CUDA);
+    if (cudaMemsetAsync(c->S.near_inlet, 0, sizeof(int32_t) * capacity, c->stream) != cudaSuccess)
+        return fail(FJSPH_E_CUDA);
+    for (int k = 0; k < c->D; ++k)
+        if (cudaMemsetAsync(c->nrm_tmp[k], 0, sizeof(double) * capacity, c->stream) != cudaSuccess)
+            return fail(FJSPH_E_CUDA);
+    if (sync(c) != FJSPH_OK) return fail(FJSPH_E_CUDA);
+    *out = c;
+    return FJSPH_OK;
+}
+
+int fjsph_ctx_destroy(fjsph_ctx *c) {
+    if (!c) return FJSPH_E_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (HostInlet &I : c->inlets) {
+        if (I.d_back) cudaFree(I.d_back);
+        if (I.d_buffer) cudaFree(I.d_buffer);
+    }
+    for (void *p : c->allocs) cudaFree(p);
+    for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->user_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->hsc) cudaFreeHost(c->hsc);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FJSPH_OK;
+}
+
+int fjsph_set_settings(fjsph_ctx *c, const fjsph_settings *s) {
+    TRY(check_ctx(c));
+    TRY(validate_settings(s));
+    if (s->dim != c->D) return FJSPH_E_ARG;
+    c->s = *s;
+    return FJSPH_OK;
+}
+
+int fjsph_get_settings(fjsph_ctx *c, fjsph_settings *s) {
+    TRY(check_ctx(c));
+    if (!s) return FJSPH_E_ARG;
+    *s = c->s;
+    return FJSPH_OK;
+}
+
+int fjsph_set_limits(fjsph_ctx *c, const fjsph_block *blocks, int32_t nblocks, int64_t n_bound_blocks) {
+    TRY(check_ctx(c));
+    if (!blocks || nblocks <= 0 || nblocks > kMaxBlocks || n_bound_blocks < 0 || n_bound_blocks > nblocks)
+        return FJSPH_E_ARG;
+    std::vector<fjsph_block> b(blocks, blocks + nblocks);
+    int64_t expect = 0;
+    for (int32_t i = 0; i < nblocks; ++i) {
+        if (b[i].first != expect || b[i].second < b[i].first) return FJSPH_E_ARG;
+        if ((i < n_bound_blocks) == (b[i].is_fluid != 0)) return FJSPH_E_ARG;
+        if (b[i].n_times < 0 || b[i].n_times > FJSPH_MAX_TIMES) return FJSPH_E_ARG;
+        expect = b[i].second;
+    }
+    c->blocks = b;
+    c->n_bound_blocks = n_bound_blocks;
+    c->nb = n_bound_blocks > 0 ? b[n_bound_blocks - 1].second : 0;
+    if (c->n > 0) {
+        if (expect != c->n) return FJSPH_E_ARG;
+        std::vector<int64_t> keys;
+        TRY(download_keys(c, keys));
+        TRY(upload_blk(c, keys));
+    }
+    return FJSPH_OK;
+}
+
+int fjsph_set_inlet(fjsph_ctx *c, const fjsph_inlet *in) {
+    TRY(check_ctx(c));
+    if (!in || in->block < 0 || in->block >= (int32_t)c->blocks.size() || in->n_back < 0 || in->depth < 0)
+        return FJSPH_E_ARG;
+    if ((in->n_back > 0 && !in->back) || (in->n_back * in->depth > 0 && !in->buffer)) return FJSPH_E_ARG;
+    HostInlet I;
+    for (HostInlet &old : c->inlets)
+        if (old.block == in->block) {
+            if (old.d_back) cudaFree(old.d_back);
+            if (old.d_buffer) cudaFree(old.d_buffer);
+            old.d_back = old.d_buffer = nullptr;
+            old.block = -1;
+        }
+    c->inlets.erase(std::remove_if(c->inlets.begin(), c->inlets.end(), [](const HostInlet &h) { return h.block < 0; }),
+                    c->inlets.end());
+    const fjsph_block &B = c->blocks[in->block];
+    I.block = in->block;
+    I.fixed_vel_or_dynamic = B.fixed_vel_or_dynamic;
+    I.n_back = in->n_back;
+    I.depth = in->depth;
+    I.back_ref.assign(in->back, in->back + in->n_back);
+    I.buffer_ref.assign(in->buffer, in->buffer + in->n_back * in->depth);
+    double nrm = 0.0;
+    for (int k = 0; k < c->D; ++k) nrm += B.insert_norm[k] * B.insert_norm[k];
+    nrm = std::sqrt(nrm);
+    for (int k = 0; k < 3; ++k) I.unorm[k] = nrm > 0 ? B.insert_norm[k] / nrm : B.insert_norm[k];
+    CU(cudaMalloc(&I.d_back, sizeof(int32_t) * std::max<int64_t>(I.n_back, 1)));
+    CU(cudaMalloc(&I.d_buffer, sizeof(int32_t) * std::max<int64_t>(I.n_back * I.depth, 1)));
+    c->inlets.push_back(I);
+    if (c->n > 0) {
+        std::vector<int64_t> keys;
+        TRY(download_keys(c, keys));
+        TRY(upload_inlets(c, keys));
+    }
+    return FJSPH_OK;
+}
+
+int fjsph_get_inlet(fjsph_ctx *c, fjsph_inlet *in) {
+    TRY(check_ctx(c));
+    if (!in) return FJSPH_E_ARG;
+    for (HostInlet &I : c->inlets)
+        if (I.block == in->block) {
+            in->n_back = I.n_back;
+            in->depth = I.depth;
+            if (in->back) std::copy(I.back_ref.begin(), I.back_ref.end(), in->back);
+            if (in->buffer) std::copy(I.buffer_ref.begin(), I.buffer_ref.end(), in->buffer);
+            return FJSPH_OK;
+        }
+    return FJSPH_E_ARG;
+}
+
+int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) {
+    TRY(check_ctx(c));
+    TRY(sync(c));
+    if (!st || (which != FJSPH_PN && which != FJSPH_PNP1)) return FJSPH_E_ARG;
+    if (st->n < 0) return FJSPH_E_ARG;
+    if (st->n > c->cap) return FJSPH_E_CAPACITY;
+    if (c->blocks.empty()) return FJSPH_E_STATE;
+    if (c->blocks.back().second != st->n) return FJSPH_E_ARG;
+    std::vector<int64_t> keys;
+    if (st->n != c->n || c->n == 0) {
+        /* new particle set: identity mapping, re-sort at the next search */
+        c->n = st->n;
+        keys.resize(c->n);
+        for (int64_t i = 0; i < c->n; ++i) keys[i] = i;
+        if (c->n) CU(cudaMemcpy(c->key, keys.data(), sizeof(int64_t) * c->n, cudaMemcpyHostToDevice));
+        TRY(upload_blk(c, keys));
+        TRY(upload_inlets(c, keys));
+        c->reorder_pending = true;
+    } else {
+        TRY(download_keys(c, keys));
+    }
+    TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, keys, true));
+    if (which == FJSPH_PNP1) c->nbr_valid = false;
+    c->pn_equals_W = false;
+    return FJSPH_OK;
+}
+
+int fjsph_state_download(fjsph_ctx *c, int32_t which, fjsph_state_view *st) {
+    TRY(need_state(c));
+    if (!st || (which != FJSPH_PN && which != FJSPH_PNP1)) return FJSPH_E_ARG;
+    if (st->n != c->n) return FJSPH_E_ARG;
+    TRY(sync(c));
+    std::vector<int64_t> keys;
+    TRY(download_keys(c, keys));
+    return transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, keys, false);
+}
+
+int fjsph_particle_count(fjsph_ctx *c, int64_t *n_total, int64_t *n_bound) {
+    TRY(check_ctx(c));
+    if (n_total) *n_total = c->n;
+    if (n_bound) *n_bound = c->nb;
+    return FJSPH_OK;
+}
+
+int fjsph_update_neighbours(fjsph_ctx *c, int64_t *n_pairs) {
+    TRY(need_state(c));
+    TRY(search(c));
+    if (n_pairs) *n_pairs = c->n_pairs;
+    return FJSPH_OK;
+}
+
+int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double *d2) {
+    TRY(need_nbr(c));
+    TRY(sync(c));
+    const int64_t n = c->n;
+    std::vector<int64_t> keys;
+    TRY(download_keys(c, keys));
+    std::vector<int64_t> off(n + 1);
+    std::vector<int32_t> id(c->n_pairs);
+    std::vector<double> xs(c->D * n);
+    CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+    if (c->n_pairs) CU(cudaMemcpy(id.data(), c->nbr_idx, sizeof(int32_t) * c->n_pairs, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < c->D; ++k) CU(cudaMemcpy(&xs[k * n], c->xs[k], sizeof(double) * n, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> slot_of_ref(n);
+    for (int64_t s = 0; s < n; ++s) slot_of_ref[keys[s]] = s;
+    int64_t w = 0;
+    std::vector<std::pair<int64_t, double>> row;
+    for (int64_t r = 0; r < n; ++r) {
+        const int64_t s = slot_of_ref[r];
+        if (offsets) offsets[r] = w;
+        row.clear();
+        for (int64_t e = off[s]; e < off[s + 1]; ++e) {
+            const int64_t j = id[e];
+            double d0 = xs[s] - xs[j];
+            double rr = d0 * d0;
+            for (int k = 1; k < c->D; ++k) {
+                double dk = xs[k * n + s] - xs[k * n + j];
+                rr = std::fma(dk, dk, rr);
+            }
+            row.push_back({keys[j], rr});
+        }
+        std::sort(row.begin(), row.end());
+        for (auto &p : row) {
+            if (idx) idx[w] = p.first;
+            if (d2) d2[w] = p.second;
+            ++w;
+        }
+    }
+    if (offsets) offsets[n] = w;
+    return FJSPH_OK;
+}
+
+int fjsph_dsph_prestep(fjsph_ctx *c, double *npd) {
+    TRY(need_nbr(c));
+    Params P = make_params(c);
+    TRY(prestep_npd(c, P));
+    c->pn_equals_W = false;
+    if (npd) {
+        CU(cudaMemcpyAsync(&c->hsc->npd, &c->dsc->npd, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        TRY(sync(c));
+        *npd = c->hsc->npd;
+    }
+    return FJSPH_OK;
+}
+
+int fjsph_get_aero_velocity(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    launch_aero_velocity(make_params(c), WS(c), make_nbr(c), c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_detect_surface(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_dissipation_terms(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    launch_dissipation(make_params(c), WS(c), make_nbr(c), c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_particle_shift(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    if (!(c->s.variant & FJSPH_VAR_ALE)) return FJSPH_E_UNSUPPORTED;
+    launch_particle_shift(make_params(c), WS(c), make_nbr(c), c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_check_pipe_outlet(fjsph_ctx *c) {
+    TRY(need_state(c));
+    launch_pipe_outlet(make_params(c), WS(c), c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_get_boundary_pressure(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    launch_bound_pressure(make_params(c), WS(c), make_nbr(c), c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_boundary_ghost(fjsph_ctx *c, int32_t *near_inlet) {
+    TRY(need_nbr(c));
+    launch_bound_ghost(make_params(c), WS(c), make_nbr(c), c->S.near_inlet, c->stream);
+    c->pn_equals_W = false;
+    TRY(sync(c));
+    if (near_inlet && c->nb > 0) {
+        std::vector<int64_t> keys;
+        TRY(download_keys(c, keys));
+        std::vector<int32_t> tmp(c->nb);
+        CU(cudaMemcpy(tmp.data(), c->S.near_inlet, sizeof(int32_t) * c->nb, cudaMemcpyDeviceToHost));
+        for (int64_t s = 0; s < c->nb; ++s) near_inlet[keys[s]] = tmp[s];
+    }
+    return FJSPH_OK;
+}
+
+int fjsph_boundary_dbc(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    launch_bound_dbc(make_params(c), WS(c), c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_set_no_slip(fjsph_ctx *c) {
+    TRY(need_nbr(c));
+    launch_no_slip(make_params(c), WS(c), make_nbr(c), c->vtmp, c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_get_acc_and_rrho(fjsph_ctx *c, double npd) {
+    TRY(need_nbr(c));
+    TRY(set_npd_device(c, npd));
+    launch_resid(make_params(c), WS(c), make_nbr(c), &c->dsc->npd, c->stream);
+    c->pn_equals_W = false;
+    return sync(c);
+}
+
+int fjsph_find_timestep(fjsph_ctx *c, double *dt) {
+    TRY(need_state(c));
+    double d = 0.0;
+    TRY(find_timestep(c, &d));
+    if (dt) *dt = d;
+    return FJSPH_OK;
+}
+
+int fjsph_get_first_rk(fjsph_ctx *c, double npd, double *logbase) {
+    TRY(need_nbr(c));
+    TRY(set_npd_device(c, npd));
+    double lb = 0.0;
+    c->pn_equals_W = false; /* the caller may have changed W since the last copy */
+    TRY(get_first_rk(c, lb));
+    if (logbase) *logbase = lb;
+    return FJSPH_OK;
+}
+
+int fjsph_runge_kutta4(fjsph_ctx *c, double npd, double logbase, double *rms_error) {
+    TRY(need_nbr(c));
+    TRY(set_npd_device(c, npd));
+    double r = 0.0;
+    TRY(runge_kutta4(c, logbase, r));
+    if (rms_error) *rms_error = r;
+    return FJSPH_OK;
+}
+
+int fjsph_nb_iter(fjsph_ctx *c, double npd) {
+    TRY(need_nbr(c));
+    TRY(set_npd_device(c, npd));
+    TRY(set_dt_device(c));
+    TRY(nb_iter(c));
+    return sync(c);
+}
+
+int fjsph_newmark_beta(fjsph_ctx *c, double npd, double *logbase, int32_t *iteration, double *rms_error) {
+    TRY(need_nbr(c));
+    if (!logbase || !iteration) return FJSPH_E_ARG;
+    TRY(set_npd_device(c, npd));
+    TRY(set_dt_device(c));
+    c->iteration = (uint32_t)*iteration;
+    double r = 0.0;
+    TRY(newmark_beta_loop(c, *logbase, r));
+    *iteration = (int32_t)c->iteration;
+    if (rms_error) *rms_error = r;
+    return FJSPH_OK;
+}
+
+int fjsph_integrate_no_update(fjsph_ctx *c, double *rms_error) {
+    TRY(need_state(c));
+    double r = 0.0;
+    TRY(integrate_no_update(c, r, false));
+    if (rms_error) *rms_error = r;
+    return sync(c);
+}
+
+int fjsph_integrate(fjsph_ctx *c, double *rms_error) {
+    TRY(need_state(c));
+    double r = 0.0;
+    TRY(integrate(c, r));
+    if (rms_error) *rms_error = r;
+    return sync(c);
+}
+
+int fjsph_integrate_n(fjsph_ctx *c, int32_t n_steps, double *last_error) {
+    TRY(need_state(c));
+    double r = 0.0;
+    for (int32_t k = 0; k < n_steps; ++k) TRY(integrate(c, r));
+    if (last_error) *last_error = r;
+    return sync(c);
+}
+
+int fjsph_step_report(fjsph_ctx *c, double *out5) {
+    TRY(check_ctx(c));
+    if (!out5) return FJSPH_E_ARG;
+    out5[0] = c->maxRho_pc;
+    out5[1] = c->maxf;
+    out5[2] = c->maxAf;
+    out5[3] = c->maxShift;
+    out5[4] = (double)c->iteration;
+    return FJSPH_OK;
+}
+
+int fjsph_launch_stats(fjsph_ctx *c, int64_t *n_launches, int32_t reset) {
+    TRY(check_ctx(c));
+    if (n_launches) *n_launches = c->launches;
+    if (reset) c->launches = 0;
+    return FJSPH_OK;
+}
+
+int fjsph_ctx_stream(fjsph_ctx *c, void **stream) {
+    TRY(check_ctx(c));
+    if (!stream) return FJSPH_E_ARG;
+    *stream = (void *)c->stream;
+    return FJSPH_OK;
+}
+
+int fjsph_event_record(fjsph_ctx *c, int32_t slot) {
+    TRY(check_ctx(c));
+    if (slot < 0 || slot >= 16) return FJSPH_E_ARG;
+    if (!c->user_ev[slot]) CU(cudaEventCreate(&c->user_ev[slot]));
+    CU(cudaEventRecord(c->user_ev[slot], c->stream));
+    return FJSPH_OK;
+}
+
+int fjsph_event_elapsed(fjsph_ctx *c, int32_t a, int32_t b, double *ms) {
+    TRY(check_ctx(c));
+    if (a < 0 || a >= 16 || b < 0 || b >= 16 || !ms || !c->user_ev[a] || !c->user_ev[b]) return FJSPH_E_ARG;
+    CU(cudaEventSynchronize(c->user_ev[b]));
+    float f = 0.f;
+    CU(cudaEventElapsedTime(&f, c->user_ev[a], c->user_ev[b]));
+    *ms = f;
+    return FJSPH_OK;
+}
+
+int fjsph_profile_enable(fjsph_ctx *c, int32_t on) {
+    TRY(check_ctx(c));
+    if (!on) TRY(profile_collect(c));
+    c->prof.on = on != 0;
+    return FJSPH_OK;
+}
+
+int fjsph_profile_read(fjsph_ctx *c, double *ms, int64_t *launches) {
+    TRY(check_ctx(c));
+    TRY(profile_collect(c));
+    for (int k = 0; k < PASS_COUNT; ++k) {
+        if (ms) ms[k] = c->prof.ms[k];
+        if (launches) launches[k] = c->prof.count[k];
+        c->prof.ms[k] = 0.0;
+        c->prof.count[k] = 0;
+    }
+    return FJSPH_OK;
+}
+
+const char *fjsph_profile_pass_name(int32_t k) {
+    if (k < 0 || k >= PASS_COUNT) return "";
+    return kPassNames[k];
+}
+
+} /* extern "C" */

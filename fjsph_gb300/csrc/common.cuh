@@ -1,0 +1,187 @@
+/*
+ * common.cuh -- device-side layout and helpers shared by the GB300 WCSPH kernels.
+ *
+ * Particle state lives in HBM as structure-of-arrays: one array per scalar component, so that a
+ * warp reading one field of 32 consecutive particles issues one 256-byte (FP64) transaction.
+ * A context holds two full states, pn (time n) and W (the working state pnp1 of the reference),
+ * plus the neighbour lists and the scratch arrays of the integrators.
+ *
+ * Particles are kept in "slot" order: boundary particles first (slots [0, nb)), then fluid
+ * particles, each group sorted by grid cell at the last re-ordering.  Every slot carries its
+ * reference ordinal (`key`), from which download restores the reference index order.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fjsph_gb300.h"
+
+#define FJSPH_HD __host__ __device__ __forceinline__
+
+namespace fjsph {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kEps = 2.220446049250313080847e-16; /* numeric_limits<double>::epsilon() */
+constexpr double kDefaultVal = 9999999.0;
+constexpr int64_t kNoCell = -3;
+constexpr int kInletZone = 6;
+constexpr int kMaxBlocks = 32;
+
+/* One full particle state on the device (structure of arrays, capacity-sized). */
+struct DevState {
+    double *x[3], *v[3], *acc[3], *Af[3], *aVisc[3], *cellV[3], *gradRho[3], *norm[3], *vPert[3];
+    double *L[9];
+    double *Rrho, *rho, *p, *m, *curve, *norm_curve, *woccl, *pDist, *deltaD;
+    double *cellP, *cellRho, *colourG, *colour, *lam, *lam_nb, *kernsum;
+    int64_t *part_id, *cellID, *key;
+    int32_t *b, *surf, *surfzone, *blk;
+};
+
+/* Block (LIMITS entry) data the kernels need. */
+struct DevBlock {
+    int32_t is_fluid, bound_solver, no_slip, block_type, fixed_vel_or_dynamic, n_times;
+    double vel_rk[3], vel_nb[3]; /* boundary velocity at the current time, RK and NB rules */
+    double aero_norm[3], aeroconst;
+    double insert_unorm[3];
+};
+
+/* Everything a kernel reads that is constant over one launch. */
+struct Params {
+    int32_t D;
+    uint32_t variant;
+    int32_t st_model, pressure_rel, acase, use_lam, use_TAB_def;
+    double H, H_sq, sr, W_correc, W_dx, dx, particle_step;
+    double rho_rest, B, gam, speed_sound, press_back, rho_min, rho_max;
+    double visc_alpha, mu, nu, sig, dsph_cont, max_shift_vel;
+    double grav[3], v_inf[3];
+    double L, A_sphere, A_plate, mu_g, sos, gamma_g, lam_cutoff, interp_fac, i_n_full, ycoef, Cb, rho_g;
+    double nb_beta, nb_gamma;
+    int64_t n, nb; /* total particles, boundary particles (slots [0, nb)) */
+    int32_t nblocks;
+    DevBlock blocks[kMaxBlocks];
+};
+
+/* Neighbour lists: CSR over slots, plus the positions at search time (the reference keeps the
+ * squared distance of each pair from search time, src/Resid.cpp:288). */
+struct DevNbr {
+    const int64_t *off;
+    const int32_t *idx;
+    const double *xs[3];
+};
+
+FJSPH_HD bool has(const Params &P, uint32_t bit) { return (P.variant & bit) != 0; }
+
+/* Squared distance, accumulated as nanoflann does under -ffast-math on FMA hardware:
+ * fma(dz,dz,fma(dy,dy,dx*dx)), d = query - candidate. */
+template <int D>
+__device__ __forceinline__ double dist2(const double *q, const double *c) {
+    double d0 = q[0] - c[0];
+    double r = __dmul_rn(d0, d0);
+#pragma unroll
+    for (int k = 1; k < D; ++k) {
+        double dk = __dsub_rn(q[k], c[k]);
+        r = __fma_rn(dk, dk, r);
+    }
+    return r;
+}
+
+template <int D, typename R>
+__device__ __forceinline__ R dot(const R *a, const R *b) {
+    R r = a[0] * b[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) r += a[k] * b[k];
+    return r;
+}
+
+template <int D, typename R>
+__device__ __forceinline__ R vnorm(const R *a) {
+    return sqrt(dot<D, R>(a, a));
+}
+
+/* Eigen normalized(): v/|v|, zero stays zero. */
+template <int D, typename R>
+__device__ __forceinline__ void normalized(const R *a, R *out) {
+    R z = dot<D, R>(a, a);
+    if (z > R(0)) {
+        R n = sqrt(z);
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = a[k] / n;
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = a[k];
+    }
+}
+
+/* (1 - q/2)^n for the Wendland C2 kernel, q = r/H. */
+template <typename R>
+__device__ __forceinline__ R wend_base(R r, R H) {
+    return R(1) - R(0.5) * r / H;
+}
+
+/* Kernel.h:37-45 / :11-21 */
+template <typename R>
+__device__ __forceinline__ R kernel_w(R r, R H, R Wc, bool cubic) {
+    if (cubic) {
+        R q = r / H;
+        if (q < R(1)) return Wc * (R(1) - R(1.5) * q * q * (R(1) - R(0.5) * q));
+        if (q < R(2)) {
+            R t = R(2) - q;
+            return Wc * R(0.25) * t * t * t;
+        }
+        return R(0);
+    }
+    R b = wend_base(r, H);
+    R b2 = b * b;
+    return b2 * b2 * (R(2) * r / H + R(1)) * Wc;
+}
+
+/* Kernel.h:48-61 / :23-33: gradient = Rij * (returned scalar). */
+template <typename R>
+__device__ __forceinline__ R gradk_scale(R r, R H, R Wc, bool cubic) {
+    if (cubic) {
+        R q = r / H;
+        if (q < R(1)) return Wc * (R(3) * (R(0.75) * q - R(1))) / (H * H);
+        if (q < R(2)) return Wc * R(-0.75) * (R(2) - q) * (R(2) - q) / (r * H);
+        return R(0);
+    }
+    if (r / H < R(1e-12)) return R(0);
+    R b = wend_base(r, H);
+    return R(5) / (H * H) * (b * b * b) * Wc;
+}
+
+/* FLUID::get_pressure / get_density (Var.h:203-236). */
+__device__ __forceinline__ double eos_pressure(const Params &P, double rho) {
+    if (P.pressure_rel == FJSPH_ISO_EOS) return P.speed_sound * P.speed_sound * (rho - P.rho_rest) + P.press_back;
+    return P.B * (pow(rho / P.rho_rest, P.gam) - 1.0) + P.press_back;
+}
+__device__ __forceinline__ double eos_density(const Params &P, double press) {
+    if (P.pressure_rel == FJSPH_ISO_EOS) return (press - P.press_back) / (P.speed_sound * P.speed_sound) + P.rho_rest;
+    return P.rho_rest * pow(((press - P.press_back) / P.B) + 1.0, 1.0 / P.gam);
+}
+__device__ __forceinline__ double clamp_rho(const Params &P, double lo, double v) { return fmax(lo, fmin(P.rho_max, v)); }
+
+template <int D>
+__device__ __forceinline__ void load3(double *const a[3], int64_t i, double *o) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) o[k] = a[k][i];
+}
+template <int D>
+__device__ __forceinline__ void store3(double *const a[3], int64_t i, const double *o) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) a[k][i] = o[k];
+}
+
+inline unsigned grid_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+/* Device-resident scalars of the integrator (read by kernels so that a step needs no host
+ * round trip). */
+struct DevScalars {
+    double dt;         /* svar.integrator.delta_t                              */
+    double npd;        /* numerical particle density from dSPH_PreStep         */
+    double red[16];    /* reduction results                                    */
+    int32_t status;    /* device-side error bits                               */
+    int32_t pad;
+};
+
+} // namespace fjsph

@@ -1,0 +1,118 @@
+/*
+ * kernels.h -- launchers of the device kernels, grouped by translation unit.  Each launcher
+ * dispatches on Params::D (2 or 3) and enqueues on the given stream; none of them synchronises.
+ */
+#pragma once
+
+#include "common.cuh"
+
+namespace fjsph {
+
+/* ---- neighbours.cu ------------------------------------------------------------------------ */
+struct CellGrid {
+    int64_t table_size;      /* power of two                                  */
+    uint32_t *hash;          /* [cap]  bucket of each slot                    */
+    int32_t *count;          /* [table_size + 1]                              */
+    int32_t *start;          /* [table_size + 1] exclusive scan of count      */
+    int32_t *sorted;         /* [cap]  slots ordered by bucket                */
+    float4 *sorted_xf;       /* [cap]  float positions in bucket order        */
+    float4 *xf;              /* [cap]  float positions by slot                */
+    double *bbox;            /* [8]    lo[3], hi[3], band, spare (device)     */
+    int64_t *grid;           /* [4]    nx, ny, nz, wrap flag (device)         */
+    int32_t *scan_tmp;       /* scan partials                                 */
+    int64_t scan_tmp_len;
+};
+
+void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s);
+void launch_hash_and_count(const Params &P, const DevState &W, double *const xs[3], CellGrid &G, cudaStream_t s);
+void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, cudaStream_t s);
+void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s);
+void launch_scatter_sort(const Params &P, CellGrid &G, cudaStream_t s);
+void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s);
+void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
+                     cudaStream_t s);
+/* Float positions by slot from xs (after a re-ordering moved the slots). */
+void launch_refresh_xf(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s);
+/* Re-ordering: new slot of every old slot, boundary group first, each group in bucket order. */
+void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,
+                        cudaStream_t s);
+
+/* ---- sweeps.cu ---------------------------------------------------------------------------- */
+void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s);
+void launch_npd_only(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s);
+void launch_aero_velocity(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
+void launch_detect_surface(const Params &P, const DevState &W, const DevNbr &N, double *const nrm_tmp[3],
+                           cudaStream_t s);
+void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
+void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
+void launch_pipe_outlet(const Params &P, const DevState &W, cudaStream_t s);
+/* boundary passes over slots [0, nb) */
+void launch_bound_velocity(const Params &P, const DevState &W, int nb_rule, cudaStream_t s);
+void launch_no_slip(const Params &P, const DevState &W, const DevNbr &N, double *const vtmp[3], cudaStream_t s);
+void launch_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
+void launch_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, int32_t *near_inlet, cudaStream_t s);
+void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s);
+/* residual (src/Resid.cpp:426) over fluid slots */
+void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, cudaStream_t s);
+
+/* ---- integrate.cu ------------------------------------------------------------------------- */
+struct RKScratch {
+    double *Sx[3], *Sv[3], *Sr; /* RK4 weighted sums                                  */
+    double *xsnap[3];           /* positions before the last update (error norm)      */
+    int32_t *near_inlet;        /* ghost boundary flag per slot                       */
+    double *part;               /* reduction partials                                 */
+    int64_t part_len;
+};
+
+/* Boundary density/pressure updates.  mode 0 = RK intermediate, 1 = RK final, 2 = Newmark-Beta. */
+void launch_bound_rho_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S, int mode,
+                             double sum_w, const double *dt_dev, double dt_scale, cudaStream_t s);
+/* RK4 accumulator initialisation at Runge_Kutta4 entry (st_1 = W). */
+void launch_rk_init_sums(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S, cudaStream_t s);
+/* Fluid stage update: stage 1..3 intermediate (weight for the sums) or final. */
+void launch_rk_stage_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S, int stage,
+                            const double *dt_dev, double dt_scale, cudaStream_t s);
+void launch_rk_final_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S,
+                            const double *dt_dev, cudaStream_t s);
+void launch_nb_update(const Params &P, const DevState &pn, const DevState &W, const double *dt_dev, cudaStream_t s);
+/* Inlet buffer particles.  mode 0 = RK intermediate, 1 = RK final, 2 = NB. */
+struct DevInlet {
+    int32_t block, fixed_vel_or_dynamic;
+    int64_t n_back, depth;
+    int32_t *back;   /* slots */
+    int32_t *buffer; /* slots, n_back * depth */
+    double unorm[3];
+};
+void launch_inlet_buffers(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S,
+                          const DevInlet &I, int mode, const double *dt_dev, double dt_scale, cudaStream_t s);
+/* Sum over fluid slots of |W.x - ref|^2, written to out[0]. */
+void launch_sq_disp_sum(const Params &P, const DevState &W, double *const ref[3], RKScratch &S, double *out,
+                        cudaStream_t s);
+void launch_density_guard(const Params &P, const DevState &W, cudaStream_t s);
+/* Sum of an array over [0, n) into out[0], deterministic (two-pass). */
+void launch_sum(const double *in, int64_t n, double *part, int64_t part_len, double *out, cudaStream_t s);
+/* find_timestep reductions over fluid slots: out[0..6] = maxf, maxAf, maxdrho, maxRhoi, minST, maxU,
+ * maxShift (the last one only if ALE). */
+void launch_timestep_reduce(const Params &P, const DevState &W, RKScratch &S, double *out, cudaStream_t s);
+
+/* ---- state.cu ------------------------------------------------------------------------------ */
+/* Field lists of a state: every array that holds per-slot data. */
+constexpr int kMaxF64Fields = 64;
+constexpr int kMaxI64Fields = 4;
+constexpr int kMaxI32Fields = 8;
+struct FieldList {
+    int n64 = 0, ni64 = 0, ni32 = 0;
+    double *f64[kMaxF64Fields];
+    int64_t *i64[kMaxI64Fields];
+    int32_t *i32[kMaxI32Fields];
+};
+/* Per-state fields (excludes the shared key/blk arrays). */
+FieldList state_fields(const DevState &S, int D);
+/* dst[new_of_old[o]] = src[o] for every field, o in [0, n). */
+void launch_permute(const FieldList &src, const FieldList &dst, const int32_t *new_of_old, int64_t n, cudaStream_t s);
+/* dst = src over [0, n) for every field. */
+void launch_copy(const FieldList &src, const FieldList &dst, int64_t n, cudaStream_t s);
+/* a[i] = new_of_old[a[i]] */
+void launch_remap_i32(int32_t *a, int64_t n, const int32_t *new_of_old, cudaStream_t s);
+
+} // namespace fjsph

@@ -1,0 +1,459 @@
+/*
+ * neighbours.cu -- GPU cell-linked list replacing the nanoflann KD-tree radius search of
+ * src/Neighbours.cpp:7-47.
+ *
+ * Build per search:
+ *   1. bounding box of all positions and the grid over it (cell edge = search radius * (1+1e-6));
+ *   2. every particle hashes its cell's linear index into a power-of-two bucket table;
+ *      while the grid has no more cells than buckets the hash is the identity, so a row of three
+ *      x-adjacent cells is one contiguous bucket range;
+ *   3. counting sort of particles by bucket (histogram, exclusive scan, scatter, then an
+ *      in-bucket sort by slot so the order is deterministic);
+ *   4. per particle, count and then write its neighbours in CSR form.
+ * Membership is the reference's test, d2 < sr with d2 = fma(dz,dz,fma(dy,dy,dx*dx)) in FP64.
+ * It is decided first in FP32 on positions relative to the box corner, and in FP64 only when
+ * the FP32 value falls inside a band whose width bounds the FP32 rounding error; so the lists are
+ * exactly the FP64 ones while the bulk of the candidate tests run on the FP32 pipe.
+ */
+#include "kernels.h"
+
+namespace fjsph {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int64_t kMaxAxis = (int64_t)1 << 20;
+
+__device__ __forceinline__ double cell_edge(const Params &P) { return sqrt(P.sr) * (1.0 + 1e-6); }
+
+/* ---- bounding box ----------------------------------------------------------------------------- */
+__global__ void k_bbox_part(Params P, DevState W, double *part) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int k = 0; k < P.D; ++k) {
+            const double x = W.x[k][i];
+            lo[k] = fmin(lo[k], x);
+            hi[k] = fmax(hi[k], x);
+        }
+    }
+    __shared__ double sh[6][kThreads];
+    for (int k = 0; k < 3; ++k) {
+        sh[k][threadIdx.x] = lo[k];
+        sh[3 + k][threadIdx.x] = hi[k];
+    }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int k = 0; k < 3; ++k) {
+                sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
+                sh[3 + k][threadIdx.x] = fmax(sh[3 + k][threadIdx.x], sh[3 + k][threadIdx.x + s]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 6; ++k) part[blockIdx.x * 6 + k] = sh[k][0];
+}
+
+__global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bbox, int64_t *grid, int64_t table) {
+    if (threadIdx.x != 0) return;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = INFINITY;
+        hi[k] = -INFINITY;
+    }
+    for (int b = 0; b < nblk; ++b)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fmin(lo[k], part[b * 6 + k]);
+            hi[k] = fmax(hi[k], part[b * 6 + 3 + k]);
+        }
+    const double cs = cell_edge(P);
+    int64_t nc[3] = {1, 1, 1};
+    double ext = 0.0;
+    for (int k = 0; k < P.D; ++k) {
+        if (!(lo[k] <= hi[k])) { /* empty or non-finite */
+            lo[k] = 0.0;
+            hi[k] = 0.0;
+        }
+        double c = floor((hi[k] - lo[k]) / cs) + 1.0;
+        if (!(c < (double)kMaxAxis)) c = (double)kMaxAxis;
+        nc[k] = (int64_t)c;
+        ext = fmax(ext, hi[k] - lo[k]);
+    }
+    for (int k = 0; k < 3; ++k) {
+        bbox[k] = lo[k];
+        bbox[3 + k] = hi[k];
+    }
+    /* FP32 band.  xf = fl(x - lo) has |err| <= u ext per axis (u = 2^-24), so near the sphere
+     * |d2_f32 - d2| <= D (4 u ext R + 3 u R^2) + 2 u R^2 with R = sqrt(sr); twice that, relative
+     * to sr, is the band inside which the FP64 test decides. */
+    const double u = 5.9604644775390625e-08;
+    const double R = sqrt(P.sr);
+    const double rel = 2.0 * (P.D * 4.0 * u * ext / R + (3.0 * P.D + 2.0) * u) + 1e-7;
+    bbox[6] = rel;
+    grid[0] = nc[0];
+    grid[1] = nc[1];
+    grid[2] = nc[2];
+    const double ncells = (double)nc[0] * (double)nc[1] * (double)nc[2];
+    grid[3] = ncells > (double)table ? 1 : 0;
+}
+
+/* ---- hashing ---------------------------------------------------------------------------------- */
+template <int D>
+__device__ __forceinline__ void cell_coords(const Params &P, const double *x, const double *lo, const int64_t *nc,
+                                            int64_t *c) {
+    const double cs = cell_edge(P);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[k] = 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        double f = floor((x[k] - lo[k]) / cs);
+        int64_t v = (f > 0.0) ? (int64_t)fmin(f, (double)(nc[k] - 1)) : 0;
+        c[k] = v;
+    }
+}
+
+__device__ __forceinline__ uint64_t lin_index(const int64_t *c, const int64_t *nc) {
+    return (uint64_t)c[0] + (uint64_t)nc[0] * ((uint64_t)c[1] + (uint64_t)nc[1] * (uint64_t)c[2]);
+}
+
+template <int D>
+__global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, double *xs2, CellGrid G) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double *const xs[3] = {xs0, xs1, xs2};
+    double x[3] = {0, 0, 0}, lo[3];
+    int64_t nc[3], c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = G.bbox[k];
+        nc[k] = G.grid[k];
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        x[k] = W.x[k][i];
+        xs[k][i] = x[k];
+    }
+    cell_coords<D>(P, x, lo, nc, c);
+    const uint32_t h = (uint32_t)(lin_index(c, nc) & (uint64_t)(G.table_size - 1));
+    G.hash[i] = h;
+    G.xf[i] = make_float4((float)(x[0] - lo[0]), (float)(x[1] - lo[1]), D == 3 ? (float)(x[2] - lo[2]) : 0.0f, 0.0f);
+    atomicAdd(&G.count[h], 1);
+}
+
+__global__ void k_scatter(Params P, CellGrid G, int32_t *cursor) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t h = G.hash[i];
+    const int32_t pos = G.start[h] + atomicAdd(&cursor[h], 1);
+    G.sorted[pos] = (int32_t)i;
+}
+
+/* Insertion sort of each bucket by slot, then gather the float positions in bucket order. */
+__global__ void k_bucket_sort(CellGrid G, int64_t nbuckets) {
+    const int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (h >= nbuckets) return;
+    const int32_t s0 = G.start[h], s1 = G.start[h + 1];
+    for (int32_t a = s0 + 1; a < s1; ++a) {
+        const int32_t v = G.sorted[a];
+        int32_t b = a - 1;
+        while (b >= s0 && G.sorted[b] > v) {
+            G.sorted[b + 1] = G.sorted[b];
+            --b;
+        }
+        G.sorted[b + 1] = v;
+    }
+    for (int32_t a = s0; a < s1; ++a) G.sorted_xf[a] = G.xf[G.sorted[a]];
+}
+
+/* ---- neighbour walk --------------------------------------------------------------------------- */
+/* Visits every candidate of particle i once and calls f(j) for each member (d2 < sr). */
+template <int D, class F>
+__device__ __forceinline__ void walk(const Params &P, double *const xs[3], const CellGrid &G, int64_t i, F &&f) {
+    double lo[3], xi[3] = {0, 0, 0};
+    int64_t nc[3], c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = G.bbox[k];
+        nc[k] = G.grid[k];
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) xi[k] = xs[k][i];
+    cell_coords<D>(P, xi, lo, nc, c);
+    const bool wrap = G.grid[3] != 0;
+    const float4 fi = G.xf[i];
+    const double band = G.bbox[6];
+    const float sr_lo = (float)(P.sr * (1.0 - band)), sr_hi = (float)(P.sr * (1.0 + band));
+    const uint64_t mask = (uint64_t)(G.table_size - 1);
+    const int zr = (D == 3) ? 1 : 0;
+    const int64_t x0 = c[0] > 0 ? c[0] - 1 : 0;
+    const int64_t x1 = c[0] + 1 < nc[0] ? c[0] + 1 : nc[0] - 1;
+    /* wrapped table: true if an earlier neighbour cell of this walk hashes to bucket h */
+    auto visited_before = [&](int dz, int dy, int64_t cx, uint64_t h) -> bool {
+        for (int dz2 = -zr; dz2 <= zr; ++dz2) {
+            const int64_t cz2 = c[2] + dz2;
+            if (cz2 < 0 || cz2 >= nc[2]) continue;
+            for (int dy2 = -1; dy2 <= 1; ++dy2) {
+                const int64_t cy2 = c[1] + dy2;
+                if (cy2 < 0 || cy2 >= nc[1]) continue;
+                for (int64_t cx2 = x0; cx2 <= x1; ++cx2) {
+                    if (dz2 == dz && dy2 == dy && cx2 == cx) return false;
+                    int64_t c2[3] = {cx2, cy2, cz2};
+                    if ((lin_index(c2, nc) & mask) == h) return true;
+                }
+            }
+        }
+        return false;
+    };
+    auto test = [&](int32_t e) {
+        const int32_t j = G.sorted[e];
+        const float4 fj = G.sorted_xf[e];
+        const float dx = fi.x - fj.x, dy = fi.y - fj.y;
+        float d2f = dx * dx + dy * dy;
+        if (D == 3) {
+            const float dz = fi.z - fj.z;
+            d2f += dz * dz;
+        }
+        bool in;
+        if (d2f < sr_lo)
+            in = true;
+        else if (d2f > sr_hi)
+            in = false;
+        else {
+            double xj[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) xj[k] = xs[k][j];
+            in = dist2<D>(xi, xj) < P.sr;
+        }
+        if (in) f(j);
+    };
+    for (int dz = -zr; dz <= zr; ++dz) {
+        const int64_t cz = c[2] + dz;
+        if (cz < 0 || cz >= nc[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int64_t cy = c[1] + dy;
+            if (cy < 0 || cy >= nc[1]) continue;
+            if (!wrap) {
+                /* identity hash: cells x0..x1 of this row are consecutive buckets */
+                int64_t cc[3] = {x0, cy, cz};
+                const uint64_t h0 = lin_index(cc, nc);
+                const int32_t e0 = G.start[h0], e1 = G.start[h0 + (x1 - x0) + 1];
+                for (int32_t e = e0; e < e1; ++e) test(e);
+            } else {
+                for (int64_t cx = x0; cx <= x1; ++cx) {
+                    int64_t cc[3] = {cx, cy, cz};
+                    const uint64_t h = lin_index(cc, nc) & mask;
+                    if (visited_before(dz, dy, cx, h)) continue;
+                    const int32_t e0 = G.start[h], e1 = G.start[h + 1];
+                    for (int32_t e = e0; e < e1; ++e) test(e);
+                }
+            }
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_nbr_count(Params P, double *xs0, double *xs1, double *xs2, CellGrid G,
+                                                         int32_t *counts) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double *const xs[3] = {xs0, xs1, xs2};
+    int32_t cnt = 0;
+    walk<D>(P, xs, G, i, [&](int32_t) { ++cnt; });
+    counts[i] = cnt;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, double *xs1, double *xs2, CellGrid G,
+                                                        const int64_t *off, int32_t *idx) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double *const xs[3] = {xs0, xs1, xs2};
+    int64_t w = off[i];
+    const int64_t wend = off[i + 1];
+    walk<D>(P, xs, G, i, [&](int32_t j) {
+        if (w < wend) idx[w] = j;
+        ++w;
+    });
+}
+
+/* ---- scans ------------------------------------------------------------------------------------ */
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+/* exclusive scan of one block's tile of kScanThreads*kScanItems items; returns the tile total */
+template <typename TI, typename TO>
+__device__ TO block_tile_scan(const TI *in, TO *out, int64_t base, int64_t n, TO carry, bool write) {
+    __shared__ TO wsum[kScanThreads / 32];
+    TO v[kScanItems];
+    TO local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t idx = base + (int64_t)threadIdx.x * kScanItems + k;
+        v[k] = idx < n ? (TO)in[idx] : (TO)0;
+        local += v[k];
+    }
+    TO incl = warp_incl_scan<TO>(local);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        TO s = lane < kScanThreads / 32 ? wsum[lane] : (TO)0;
+        s = warp_incl_scan<TO>(s);
+        if (lane < kScanThreads / 32) wsum[lane] = s;
+    }
+    __syncthreads();
+    const TO warp_off = wid > 0 ? wsum[wid - 1] : (TO)0;
+    const TO total = wsum[kScanThreads / 32 - 1];
+    if (write) {
+        TO run = carry + warp_off + incl - local;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            const int64_t idx = base + (int64_t)threadIdx.x * kScanItems + k;
+            if (idx < n) out[idx] = run;
+            run += v[k];
+        }
+    }
+    __syncthreads();
+    return total;
+}
+
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const TI *in, int64_t n, TO *tile_sums) {
+    const int64_t base = (int64_t)blockIdx.x * kScanThreads * kScanItems;
+    TO t = block_tile_scan<TI, TO>(in, (TO *)nullptr, base, n, (TO)0, false);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = t;
+}
+
+template <typename TO>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(TO *tile_sums, int64_t ntiles) {
+    /* exclusive scan of the tile totals, in place, one block walking tiles of the tile array */
+    TO carry = 0;
+    for (int64_t base = 0; base < ntiles; base += (int64_t)kScanThreads * kScanItems) {
+        TO t = block_tile_scan<TO, TO>(tile_sums, tile_sums, base, ntiles, carry, true);
+        carry += t;
+    }
+    if (threadIdx.x == 0) tile_sums[ntiles] = carry;
+}
+
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const TI *in, TO *out, int64_t n, const TO *tile_sums) {
+    const int64_t base = (int64_t)blockIdx.x * kScanThreads * kScanItems;
+    block_tile_scan<TI, TO>(in, out, base, n, tile_sums[blockIdx.x], true);
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tile_sums[gridDim.x];
+}
+
+template <typename TI, typename TO>
+void scan_exclusive(const TI *in, TO *out, int64_t n, TO *tmp, cudaStream_t s) {
+    const int64_t tile = (int64_t)kScanThreads * kScanItems;
+    const int64_t ntiles = (n + tile - 1) / tile;
+    if (ntiles == 0) {
+        cudaMemsetAsync(out, 0, sizeof(TO), s);
+        return;
+    }
+    k_scan_reduce<TI, TO><<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tmp);
+    k_scan_tiles<TO><<<1, kScanThreads, 0, s>>>(tmp, ntiles);
+    k_scan_apply<TI, TO><<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, out, n, tmp);
+}
+
+/* ---- re-ordering ------------------------------------------------------------------------------ */
+__global__ void k_bound_flags(Params P, const int32_t *sorted, int32_t *flag) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    flag[p] = sorted[p] < P.nb ? 1 : 0;
+}
+
+__global__ void k_reorder_map(Params P, int32_t *sorted, const int32_t *flag, const int32_t *ex, int32_t *new_of_old) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int32_t old = sorted[p];
+    const int32_t ns = flag[p] ? ex[p] : (int32_t)(P.nb + p - ex[p]);
+    new_of_old[old] = ns;
+    sorted[p] = ns;
+}
+
+__global__ void k_refresh_xf(Params P, const double *xs0, const double *xs1, const double *xs2, CellGrid G) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const double lo0 = G.bbox[0], lo1 = G.bbox[1], lo2 = G.bbox[2];
+    G.xf[i] = make_float4((float)(xs0[i] - lo0), (float)(xs1[i] - lo1), P.D == 3 ? (float)(xs2[i] - lo2) : 0.0f, 0.0f);
+}
+
+} // namespace
+
+void launch_refresh_xf(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s) {
+    if (P.n == 0) return;
+    k_refresh_xf<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G);
+}
+
+void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s) {
+    /* partials live in the upper part of scan_tmp (reinterpreted) */
+    int nblk = (int)std::min<int64_t>(grid_for(P.n, kThreads), 304);
+    if (nblk < 1) nblk = 1;
+    double *part = reinterpret_cast<double *>(G.scan_tmp);
+    k_bbox_part<<<nblk, kThreads, 0, s>>>(P, W, part);
+    k_bbox_finish<<<1, 32, 0, s>>>(P, part, nblk, G.bbox, G.grid, G.table_size);
+}
+
+void launch_hash_and_count(const Params &P, const DevState &W, double *const xs[3], CellGrid &G, cudaStream_t s) {
+    cudaMemsetAsync(G.count, 0, sizeof(int32_t) * (G.table_size + 1), s);
+    if (P.n == 0) return;
+    if (P.D == 2)
+        k_hash_count<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, W, xs[0], xs[1], xs[2], G);
+    else
+        k_hash_count<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, W, xs[0], xs[1], xs[2], G);
+}
+
+void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, cudaStream_t s) {
+    scan_exclusive<int32_t, int32_t>(in, out, n, tmp, s);
+}
+void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s) {
+    scan_exclusive<int32_t, int64_t>(in, out, n, tmp, s);
+}
+
+void launch_scatter_sort(const Params &P, CellGrid &G, cudaStream_t s) {
+    /* G.count is reused as the scatter cursor */
+    cudaMemsetAsync(G.count, 0, sizeof(int32_t) * (G.table_size + 1), s);
+    if (P.n == 0) return;
+    k_scatter<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, G.count);
+    k_bucket_sort<<<grid_for(G.table_size, kThreads), kThreads, 0, s>>>(G, G.table_size);
+}
+
+void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s) {
+    if (P.n == 0) return;
+    if (P.D == 2)
+        k_nbr_count<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, counts);
+    else
+        k_nbr_count<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, counts);
+}
+
+void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
+                     cudaStream_t s) {
+    if (P.n == 0) return;
+    if (P.D == 2)
+        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx);
+    else
+        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx);
+}
+
+void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,
+                        cudaStream_t s) {
+    /* tmp: [n] flags, [n+1] exclusive scan, then scan partials */
+    (void)tmp_len;
+    if (P.n == 0) return;
+    int32_t *flag = tmp, *ex = tmp + P.n, *part = tmp + 2 * P.n + 1;
+    k_bound_flags<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G.sorted, flag);
+    scan_exclusive<int32_t, int32_t>(flag, ex, P.n, part, s);
+    k_reorder_map<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G.sorted, flag, ex, new_of_old);
+}
+
+} // namespace fjsph

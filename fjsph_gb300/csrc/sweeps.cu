@@ -1,0 +1,967 @@
+/*
+ * sweeps.cu -- the per-particle neighbour sweeps of one WCSPH step, FP64 form.
+ *
+ * One thread owns one particle and walks its CSR neighbour list.  Neighbour data are gathered
+ * from slot-ordered SoA arrays; slots are cell-sorted, so neighbouring threads share most of
+ * their neighbours through L1/L2.  The squared distance of a pair is re-evaluated from the
+ * positions frozen at search time (xs), which reproduces the reference's stored `jj.second`
+ * bit for bit, while the separation vector uses current positions (src/Resid.cpp:286-290).
+ */
+#include "kernels.h"
+#include "linalg.cuh"
+
+namespace fjsph {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+template <int D>
+__device__ __forceinline__ double pair_rr(const DevNbr &N, int64_t i, int64_t j) {
+    double a[D], b[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        a[k] = N.xs[k][i];
+        b[k] = N.xs[k][j];
+    }
+    return dist2<D>(a, b);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* dSPH_PreStep (src/Shifting.cpp:12-123), all slots                                            */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_dsph_prestep(Params P, DevState W, DevNbr N, double *npd_part) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    double xi[D];
+    load3<D>(W.x, i, xi);
+    const double rho_i = W.rho[i];
+    double Lm[D * D], Lnb[D * D], gR[D], nr[D];
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) {
+        Lm[k] = 0.0;
+        Lnb[k] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        gR[k] = 0.0;
+        nr[k] = 0.0;
+    }
+    double kernsum = 0.0, colour = 0.0, npd = 0.0;
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i) {
+            kernsum += P.W_correc;
+            continue;
+        }
+        double Rji[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Rji[k] = W.x[k][j] - xi[k];
+        const double r = sqrt(pair_rr<D>(N, i, j));
+        const double volj = W.m[j] / W.rho[j];
+        const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);
+        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        double Grad[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Grad[k] = -Rji[k] * gs;
+        const bool fl = W.b[j] > FJSPH_PISTON;
+        const double drho = volj * (W.rho[j] - rho_i);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const double vr = volj * Rji[a];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                Lm[a * D + c] -= vr * Grad[c];
+                if (fl) Lnb[a * D + c] -= vr * Grad[c];
+            }
+            gR[a] += drho * Grad[a];
+        }
+        if (fl) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) nr[k] += volj * Grad[k];
+            kernsum += kern;
+            colour += volj * kern;
+            npd += kern;
+        }
+    }
+    double Linv[D * D];
+    if (!qr_inverse<D>(Lm, Linv)) {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int c = 0; c < D; ++c) Linv[a * D + c] = (a == c) ? 1.0 : 0.0;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double g = 0.0, n = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            g += Linv[a * D + c] * gR[c];
+            n += Linv[a * D + c] * nr[c];
+        }
+        W.gradRho[a][i] = g;
+        W.norm[a][i] = n;
+    }
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) W.L[k][i] = Linv[k];
+    double lam, lam_nb;
+    if (W.b[i] == FJSPH_BOUND) {
+        lam = 1.0;
+        lam_nb = 1.0;
+    } else {
+        lam = min_eig<D>(Lm);
+        lam_nb = min_eig<D>(Lnb);
+    }
+    W.lam[i] = lam;
+    W.lam_nb[i] = lam_nb;
+    W.colourG[i] = (lam > 0.7) ? 2.0 : 2.0 * fmax(1.0, 1.0 / (2.0 * colour));
+    W.kernsum[i] = kernsum;
+    W.colour[i] = colour;
+    npd_part[i] = npd;
+}
+
+/* Numerical particle density alone: the npd sum of dSPH_PreStep without its other outputs. */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_npd_only(Params P, DevState W, DevNbr N, double *npd_part) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    double npd = 0.0;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i || W.b[j] <= FJSPH_PISTON) continue;
+        npd += kernel_w<double>(sqrt(pair_rr<D>(N, i, j)), P.H, P.W_correc, cubic);
+    }
+    npd_part[i] = npd;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* get_aero_velocity, constVel source (src/Resid.cpp:569-611), fluid slots                     */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void k_aero_velocity(Params P, DevState W, DevNbr N) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    bool on;
+    if (P.use_lam)
+        on = W.lam_nb[i] < P.lam_cutoff && W.b[i] == FJSPH_FREE;
+    else
+        on = double(N.off[i + 1] - N.off[i]) * P.i_n_full < P.lam_cutoff && W.b[i] == FJSPH_FREE;
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.cellV[k][i] = on ? P.v_inf[k] : 0.0;
+    W.cellID[i] = on ? 1 : kNoCell;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Detect_Surface (src/Geometry.cpp:14-280), fluid slots, three passes                         */
+/* ------------------------------------------------------------------------------------------ */
+/* pass 1: surface flag (Marrone et al. 2010) and the eigenvalue-gradient normal */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_surface_normal(Params P, DevState W, DevNbr N, double *nrm0,
+                                                              double *nrm1, double *nrm2) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double *const nrm_tmp[3] = {nrm0, nrm1, nrm2};
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    const double h = 1.33 * P.particle_step;
+    double xi[D], ni[D], nh[D];
+    load3<D>(W.x, i, xi);
+    load3<D>(W.norm, i, ni);
+    normalized<D, double>(ni, nh);
+    const int b = W.b[i];
+    const double lam_nb = W.lam_nb[i], lam = W.lam[i];
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    if (b < FJSPH_PIPE) {
+        W.surf[i] = 0;
+        W.woccl[i] = 1.0;
+    } else if (lam_nb < 0.2) {
+        W.surf[i] = 1;
+    } else if (lam_nb < 0.75) {
+        double pointT[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) pointT[k] = xi[k] + h * nh[k];
+        double th[D];
+        if (D == 2) {
+            double tau[D];
+            tau[0] = ni[1];
+            tau[1] = -ni[0];
+            normalized<D, double>(tau, th);
+        }
+        int surf = 1;
+        for (int64_t e = e0; e < e1; ++e) {
+            const int64_t j = N.idx[e];
+            if (j == i) continue;
+            double xj[D], x_jT[D];
+            load3<D>(W.x, j, xj);
+#pragma unroll
+            for (int k = 0; k < D; ++k) x_jT[k] = xj[k] - pointT[k];
+            const double r = sqrt(pair_rr<D>(N, i, j));
+            if (r >= sqrt(2.0) * h) {
+                if (vnorm<D, double>(x_jT) < h) {
+                    surf = 0;
+                    break;
+                }
+            } else if (D == 2) {
+                if ((fabs(dot<D, double>(nh, x_jT)) + fabs(dot<D, double>(th, x_jT))) < h) {
+                    surf = 0;
+                    break;
+                }
+            } else {
+                double u[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) u[k] = -(xi[k] - xj[k]) / r;
+                if (acos(dot<D, double>(nh, u)) < kPi / 4.0) {
+                    surf = 0;
+                    break;
+                }
+            }
+        }
+        W.surf[i] = surf;
+    } else {
+        W.surf[i] = 0;
+    }
+    double nrm[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) nrm[k] = 0.0;
+    const bool inside = lam > 0.7;
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i) continue;
+        double Rij[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Rij[k] = xi[k] - W.x[k][j];
+        const double r = sqrt(pair_rr<D>(N, i, j));
+        const double volj = W.m[j] / W.rho[j];
+        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        const double w = inside ? volj * (W.lam[j] - lam) : volj * W.lam[j];
+#pragma unroll
+        for (int k = 0; k < D; ++k) nrm[k] += w * (Rij[k] * gs);
+    }
+    double n2[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double s = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) s += W.L[a * D + c][i] * nrm[c];
+        n2[a] = s;
+    }
+    double out[D];
+    if (vnorm<D, double>(n2) > 0.1 * lam / P.H) {
+        normalized<D, double>(n2, out);
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) nrm_tmp[k][i] = out[k];
+}
+
+/* pass 2: curvature from the normals and the Gissler occlusion factor */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_surface_curvature(Params P, DevState W, DevNbr N, const double *nrm0,
+                                                                 const double *nrm1, const double *nrm2) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const double *const nt[3] = {nrm0, nrm1, nrm2};
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    const bool gissler = P.acase == FJSPH_GISSLER;
+    const int b = W.b[i];
+    double xi[D], vi[D], ni[D], Vdiff[D];
+    load3<D>(W.x, i, xi);
+    load3<D>(W.v, i, vi);
+#pragma unroll
+    for (int k = 0; k < D; ++k) ni[k] = nt[k][i];
+    const bool occl = (b == FJSPH_FREE) && gissler;
+#pragma unroll
+    for (int k = 0; k < D; ++k) Vdiff[k] = (occl && W.cellID[i] != -1) ? P.v_inf[k] - vi[k] : 0.0;
+    double Li[D * D];
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) Li[k] = W.L[k][i];
+    const double nin = vnorm<D, double>(ni), vdn = vnorm<D, double>(Vdiff);
+    double curve = 0.0, woccl_ = 0.0;
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i) continue;
+        double Rij[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Rij[k] = W.x[k][j] - xi[k];
+        const double r = sqrt(pair_rr<D>(N, i, j));
+        double nj[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) nj[k] = nt[k][j];
+        if (nin > 0.0 && vnorm<D, double>(nj) > 0.0) {
+            const double volj = W.m[j] / W.rho[j];
+            const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+            double s = 0.0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double Ld = 0.0;
+#pragma unroll
+                for (int c = 0; c < D; ++c) Ld += Li[a * D + c] * (nj[c] - ni[c]);
+                s += Ld * (Rij[a] * gs);
+            }
+            curve += volj * s;
+        }
+        if (occl) {
+            const double frac = -dot<D, double>(Rij, Vdiff) / (vdn * r);
+            if (frac > woccl_) woccl_ = frac;
+        }
+    }
+    W.woccl[i] = (W.lam_nb[i] < P.lam_cutoff) ? fmax(0.0, fmin(woccl_, 1.0)) : 1.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.norm[k][i] = ni[k];
+    W.curve[i] = curve;
+    W.norm_curve[i] = P.dx * curve;
+    W.pDist[i] = W.lam[i];
+}
+
+/* pass 3 (ALE/TIC builds): surface zone = any neighbour (self included) on the surface */
+__global__ void k_surface_zone(Params P, DevState W, DevNbr N) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    int sz = 0;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e)
+        if (W.surf[N.idx[e]] == 1) {
+            sz = 1;
+            break;
+        }
+    W.surfzone[i] = sz;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Artificial viscosity (src/Kernel.h:217-244): returns the scalar multiplying gradK.           */
+/* ------------------------------------------------------------------------------------------ */
+__device__ __forceinline__ double art_visc_scale(const Params &P, double vdotr, double idist2, double rho_i,
+                                                 double rho_j) {
+    if (vdotr > 0.0) return 0.0;
+    const double muij = P.H * vdotr * idist2;
+    const double rhoij = 0.5 * (rho_i + rho_j);
+    const double cbar = 0.5 * (sqrt((P.B * P.gam) / rho_i) + sqrt((P.B * P.gam) / rho_j));
+    return P.visc_alpha * cbar * muij / rhoij;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* dissipation_terms (src/Shifting.cpp:126-186), fluid slots                                   */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, DevNbr N) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const bool cubic = has(P, FJSPH_VAR_CUBIC), linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH);
+    double xi[D], vi[D], gRi[D];
+    load3<D>(W.x, i, xi);
+    load3<D>(W.v, i, vi);
+    load3<D>(W.gradRho, i, gRi);
+    const double rho_i = W.rho[i];
+    double av[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) av[k] = 0.0;
+    double Rrhod = 0.0;
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i) continue;
+        double Rji[D], Vji[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            Rji[k] = W.x[k][j] - xi[k];
+            Vji[k] = W.v[k][j] - vi[k];
+        }
+        const double rr = pair_rr<D>(N, i, j);
+        const double r = sqrt(rr);
+        const double idist2 = 1.0 / (rr + 0.0001 * P.H_sq);
+        const double rho_j = W.rho[j];
+        const double volj = W.m[j] / rho_j;
+        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        double g[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
+        const bool fl = W.b[j] > FJSPH_PISTON;
+        if (fl) {
+            const double vdotr = dot<D, double>(Vji, Rji);
+            const double c = linear ? volj * idist2 * vdotr : W.m[j] * art_visc_scale(P, vdotr, idist2, rho_i, rho_j);
+#pragma unroll
+            for (int k = 0; k < D; ++k) av[k] += c * g[k];
+        }
+        if (!nodsph) {
+            const double rg = dot<D, double>(Rji, g);
+            double t = rho_j - rho_i;
+            if (fl) {
+                double gs2[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) gs2[k] = gRi[k] + W.gradRho[k][j];
+                t += 0.5 * dot<D, double>(gs2, Rji);
+            }
+            Rrhod += volj * t * rg * idist2;
+        }
+    }
+    if (linear) {
+        const double c = P.visc_alpha * P.H * P.speed_sound * P.rho_rest / rho_i;
+#pragma unroll
+        for (int k = 0; k < D; ++k) av[k] *= c;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.aVisc[k][i] = av[k];
+    if (!nodsph) W.deltaD[i] = P.dsph_cont * Rrhod;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* particle_shift (src/Shifting.cpp:189-290, -DALE), fluid slots                               */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_particle_shift(Params P, DevState W, DevNbr N) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const double lam_nb = W.lam_nb[i];
+    if (lam_nb < 0.55 || W.b[i] == FJSPH_BUFFER) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) W.vPert[k][i] = 0.0;
+        return;
+    }
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    double xi[D], vi[D], ni[D], nh[D];
+    load3<D>(W.x, i, xi);
+    load3<D>(W.v, i, vi);
+    load3<D>(W.norm, i, ni);
+    normalized<D, double>(ni, nh);
+    double dU[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) dU[k] = 0.0;
+    double maxUij = 0.0, woccl = 0.0;
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i) continue;
+        double Rji[D], dv[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            Rji[k] = W.x[k][j] - xi[k];
+            dv[k] = W.v[k][j] - vi[k];
+        }
+        const double r = sqrt(pair_rr<D>(N, i, j));
+        const double volj = W.m[j] / W.rho[j];
+        const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);
+        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        const double q = kern / P.W_dx;
+        const double q2 = q * q;
+        const double c = (1.0 + 0.2 * (q2 * q2));
+#pragma unroll
+        for (int k = 0; k < D; ++k) dU[k] += c * (Rji[k] * gs) * volj;
+        if (W.b[j] > FJSPH_PISTON) {
+            double nj[D], njh[D];
+            load3<D>(W.norm, j, nj);
+            normalized<D, double>(nj, njh);
+            const double theta = acos(dot<D, double>(nh, njh));
+            if (theta > woccl) woccl = theta;
+        }
+        const double dvn = vnorm<D, double>(dv);
+        if (dvn > maxUij) maxUij = dvn;
+    }
+    const double sc = -2.0 * P.H * vnorm<D, double>(vi);
+#pragma unroll
+    for (int k = 0; k < D; ++k) dU[k] *= sc;
+    const double mag = fmin(vnorm<D, double>(dU), fmin(maxUij / 2.0, P.max_shift_vel));
+    double dUn[D];
+    normalized<D, double>(dU, dUn);
+#pragma unroll
+    for (int k = 0; k < D; ++k) dU[k] = mag * dUn[k];
+    double out[D];
+    if (W.surfzone[i] == 0 && lam_nb > 0.55) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = dU[k];
+    } else if (woccl < kPi / 12.0) {
+        double nn[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) nn[k] = -nh[k];
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) s += ((a == c ? 1.0 : 0.0) - nn[a] * nn[c]) * dU[c];
+            out[a] = s;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.vPert[k][i] = out[k];
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Check_Pipe_Outlet (src/Containment.cpp:822-894), analytic air source                        */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void k_pipe_outlet(Params P, DevState W) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    if (W.b[i] != FJSPH_PIPE) return;
+    const DevBlock &B = P.blocks[W.blk[i]];
+    double s = W.x[0][i] * B.aero_norm[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) s += W.x[k][i] * B.aero_norm[k];
+    if (s > B.aeroconst) W.b[i] = FJSPH_FREE;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Boundary passes (src/Resid.cpp:21-186), boundary slots [0, nb)                               */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void k_bound_velocity(Params P, DevState W, int nb_rule) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    const DevBlock &B = P.blocks[W.blk[i]];
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.v[k][i] = nb_rule ? B.vel_nb[k] : B.vel_rk[k];
+}
+
+/* Set_No_Slip: the reference applies it per block after setting the block velocity; the mirror
+ * velocity reads fluid velocities only, so the blocks are independent. */
+template <int D>
+__global__ void k_no_slip(Params P, DevState W, DevNbr N, double *vt0, double *vt1, double *vt2) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    double *const vt[3] = {vt0, vt1, vt2};
+    const DevBlock &B = P.blocks[W.blk[i]];
+    double vi[D];
+    load3<D>(W.v, i, vi);
+    if (B.no_slip) {
+        const bool cubic = has(P, FJSPH_VAR_CUBIC);
+        double vs[D], ks = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) vs[k] = 0.0;
+        for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+            const int64_t j = N.idx[e];
+            if (j == i || W.b[j] <= FJSPH_PISTON) continue;
+            const double r = sqrt(pair_rr<D>(N, i, j));
+            const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);
+            ks += kern;
+#pragma unroll
+            for (int k = 0; k < D; ++k) vs[k] += W.v[k][j] * kern;
+        }
+        if (ks > 0.0)
+#pragma unroll
+            for (int k = 0; k < D; ++k) vi[k] = 2.0 * vi[k] - vs[k] / ks;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) vt[k][i] = vi[k];
+}
+
+template <int D>
+__global__ void k_copy_bound_v(Params P, DevState W, const double *vt0, const double *vt1, const double *vt2) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    const double *const vt[3] = {vt0, vt1, vt2};
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.v[k][i] = vt[k][i];
+}
+
+/* Get_Boundary_Pressure (Adami, Hu & Adams 2012), src/Resid.cpp:21-76 */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_bound_pressure(Params P, DevState W, DevNbr N) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    if (P.blocks[W.blk[i]].bound_solver != FJSPH_PRESSURE_G) return;
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    double xi[D];
+    load3<D>(W.x, i, xi);
+    int near = 0;
+    double kernsum = 0.0, pkern = 0.0, acck[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) acck[k] = 0.0;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int64_t j = N.idx[e];
+        if (W.b[j] <= FJSPH_PISTON) continue;
+        const double r = sqrt(pair_rr<D>(N, i, j));
+        const double rho_j = W.rho[j];
+        const double kern = (W.m[j] / rho_j) * kernel_w<double>(r, P.H, P.W_correc, cubic);
+        kernsum += kern;
+        pkern += W.p[j] * kern;
+#pragma unroll
+        for (int k = 0; k < D; ++k) acck[k] += kern * rho_j * (xi[k] - W.x[k][j]);
+        if (W.surfzone[j]) near = 1;
+    }
+    double p = 0.0;
+    if (kernsum > 0.0) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) s += (P.grav[k] - W.acc[k][i]) * acck[k];
+        p = (pkern + s) / kernsum;
+        if (near) p = fmax(0.0, p);
+    }
+    W.p[i] = p;
+    W.rho[i] = eos_density(P, p);
+}
+
+/* Boundary_Ghost (src/Resid.cpp:122-160): density rate of ghost walls and the near-inlet flag. */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_bound_ghost(Params P, DevState W, DevNbr N, int32_t *near_inlet) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    if (P.blocks[W.blk[i]].bound_solver != FJSPH_GHOST) return;
+    const bool cubic = has(P, FJSPH_VAR_CUBIC);
+    double xi[D], vi[D];
+    load3<D>(W.x, i, xi);
+    load3<D>(W.v, i, vi);
+    double Rr = 0.0;
+    int ni = 1;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int64_t j = N.idx[e];
+        if (j == i) continue;
+        const int bj = W.b[j];
+        if (bj == FJSPH_PIPE || bj == FJSPH_FREE) ni = 0;
+        const double r = sqrt(pair_rr<D>(N, i, j));
+        const double volj = W.m[j] / W.rho[j];
+        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) s += (W.v[k][j] - vi[k]) * ((W.x[k][j] - xi[k]) * gs);
+        Rr -= volj * s;
+    }
+    near_inlet[i] = ni;
+    W.Rrho[i] = Rr * W.rho[i];
+}
+
+/* Boundary_DBC (src/Resid.cpp:78-117).  The reference scatters the DBC terms into an array indexed
+ * by neighbour and then copies back only the boundary range, which the scatter never touches;
+ * its observable effect is a zero boundary acceleration. */
+template <int D>
+__global__ void k_bound_dbc(Params P, DevState W) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    if (P.blocks[W.blk[i]].bound_solver != FJSPH_DBC) return;
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.acc[k][i] = 0.0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Residual (src/Resid.cpp:243-469, src/Kernel.h:153-269, src/Aero.h:10-263), fluid slots       */
+/* ------------------------------------------------------------------------------------------ */
+__device__ __forceinline__ double get_cd(double Re) {
+    return (1.0 + 0.197 * pow(Re, 0.63) + 2.6e-04 * pow(Re, 1.38)) * (24.0 / (Re + 0.00001));
+}
+
+template <int D>
+__device__ void aero_acc(const Params &P, const DevState &W, int64_t i, const double *Vd, double lam,
+                         double nneigh, double *out) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = 0.0;
+    const double Vn = vnorm<D, double>(Vd);
+    if (P.acase == FJSPH_GISSLER) {
+        const double Re = 2.0 * W.cellRho[i] * Vn * P.L / P.mu_g;
+        const double frac2 = P.use_lam ? fmin(P.interp_fac * lam, 1.0) : fmin(P.interp_fac * nneigh * P.i_n_full, 1.0);
+        const double frac1 = 1.0 - frac2;
+        const double Cds = get_cd(Re);
+        double Cdl = Cds, Adrop = P.A_sphere;
+        if (P.use_TAB_def) {
+            double ymax = dot<D, double>(Vd, Vd) * P.ycoef;
+            if (ymax > 1.0) ymax = 1.0;
+            Cdl = Cds * (1 + 2.632 * ymax);
+            if (D == 3) {
+                const double t = P.L + P.Cb * P.L * ymax;
+                Adrop = kPi * t * t;
+            } else {
+                Adrop = P.A_sphere + 2 * (P.Cb * P.L * ymax);
+            }
+        }
+        const double Cdi = frac1 * Cdl + frac2;
+        const double Ai = (1.0 - W.woccl[i]) * (frac1 * Adrop + frac2 * P.A_plate);
+        const double c = 0.5 * Vn;
+        const double tail = P.gamma_g * W.cellP[i] * Cdi * Ai / W.m[i];
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = c * Vd[k] / (P.sos * P.sos) * tail;
+        return;
+    }
+    double nrm[D], nh[D];
+    load3<D>(W.norm, i, nrm);
+    normalized<D, double>(nrm, nh);
+    const double m_i = W.m[i];
+    if (P.acase == FJSPH_INDUCED_PRESSURE) {
+        double vh[D], mnh[D];
+        normalized<D, double>(Vd, vh);
+#pragma unroll
+        for (int k = 0; k < D; ++k) mnh[k] = -nh[k];
+        const double theta = fabs(acos(dot<D, double>(mnh, vh)));
+        double Cp_s, Cp_p, Cp_b, Cp_tot;
+        if (theta < 2.4455) {
+            const double s = sin(theta);
+            Cp_s = 1.0 - 2.25 * s * s;
+        } else
+            Cp_s = 0.075;
+        if (theta < 1.570797)
+            Cp_p = cos(theta);
+        else if (theta < 1.9918)
+            Cp_p = -pow(cos(6.0 * theta + 0.5 * kPi), 1.5);
+        else if (theta < 2.0838)
+            Cp_p = 5.5836 * theta - 11.5601;
+        else
+            Cp_p = 0.075;
+        if (theta < 0.7854)
+            Cp_b = 1.0;
+        else if (theta < 1.570797)
+            Cp_b = 0.5 * (cos(4.0 * theta - kPi) + 1.0);
+        else
+            Cp_b = 0.0;
+        const double nc = W.norm_curve[i];
+        if (nc < -0.25)
+            Cp_tot = Cp_b;
+        else if (nc < 0.0) {
+            const double fr = (nc + 0.25) * 4.0;
+            Cp_tot = fr * Cp_b + (1.0 - fr) * Cp_p;
+        } else if (nc < 0.25) {
+            const double fr = nc * 4.0;
+            Cp_tot = fr * Cp_p + (1.0 - fr) * Cp_s;
+        } else
+            Cp_tot = Cp_s;
+        const double cellP = W.cellP[i], cellRho = W.cellRho[i];
+        const double Pi = 0.5 * dot<D, double>(Vd, Vd) / (P.sos * P.sos) * P.gamma_g * cellP * Cp_tot;
+        const double Cdi = get_cd(cellRho * Vn * P.L / P.mu_g);
+        const double Vnorm = dot<D, double>(Vd, nh);
+        double Vpar[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Vpar[k] = Vd[k] - Vnorm * nh[k];
+        const double Vparn = vnorm<D, double>(Vpar);
+        const double Cf = 0.027 / pow(cellRho * Vparn * P.L / P.mu_g + 1e-6, 1.0 / 7.0);
+        const double frac1 = P.use_lam ? fmin(P.interp_fac * lam, 1.0) : fmin(P.interp_fac * nneigh * P.i_n_full, 1.0);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const double drop = 0.5 * Vd[k] * Vn / (P.sos * P.sos) * P.gamma_g * cellP * (kPi * P.L * P.L * 0.25) * Cdi / m_i;
+            const double kern = -Pi * P.A_plate * nh[k] / m_i;
+            const double skin = 0.5 * Vparn * Vpar[k] / (P.sos * P.sos) * P.gamma_g * cellP * Cf * P.A_plate / m_i;
+            out[k] = frac1 * (kern + skin) + (1.0 - frac1) * drop;
+        }
+        return;
+    }
+    if (P.acase == FJSPH_SKIN_FRIC) {
+        const double Vnorm = dot<D, double>(Vd, nh);
+        if (Vnorm > 0.001) {
+            const double Re = P.rho_g * Vn * P.L / P.mu_g;
+            double Vpar[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) Vpar[k] = Vd[k] - fabs(Vnorm) * nh[k];
+            const double Cf = 0.027 / pow(Re, 1.0 / 7.0);
+            const double Vparn = vnorm<D, double>(Vpar);
+            const double frac2 = fmin(1.5 * lam, 1.0), frac1 = 1.0 - frac2;
+            const double Cdi = get_cd(Re);
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const double press = 0.5 * P.rho_g * Vnorm * Vnorm * P.A_plate * nh[k] / m_i;
+                const double skin = 0.5 * P.rho_g * Vparn * Cf * P.A_plate * Vpar[k] / m_i;
+                const double drop = 0.5 * P.rho_g * Vn * Vd[k] * (kPi * P.L * P.L / 4) * Cdi / m_i;
+                out[k] = frac2 * (press + skin) + frac1 * drop;
+            }
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr N, const double *npd_dev) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const bool cubic = has(P, FJSPH_VAR_CUBIC), ale = has(P, FJSPH_VAR_ALE), linear = has(P, FJSPH_VAR_LINEAR),
+               nofrozen = has(P, FJSPH_VAR_NOFROZEN), nodsph = has(P, FJSPH_VAR_NODSPH), tic = has(P, FJSPH_VAR_TIC);
+    const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE, csf = P.st_model == FJSPH_ST_CSF;
+    double npdm2 = 0.0;
+    if (pairwise) {
+        const double npd = *npd_dev;
+        const double H2 = 2.0 * P.H;
+        const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (kPi * kPi * kPi * kPi) *
+                            (9.0 / 4.0 * (kPi * kPi * kPi) - 6.0 * kPi - 4.0));
+        npdm2 = (0.5 * P.sig / lam) / (npd * npd);
+    }
+    const double pi3o4 = 3.0 * kPi / 4.0;
+    double xi[D], vi[D], vPi[D], gRi[D];
+    load3<D>(W.x, i, xi);
+    load3<D>(W.v, i, vi);
+    if (ale) load3<D>(W.vPert, i, vPi);
+    if (nofrozen) load3<D>(W.gradRho, i, gRi);
+    const double rho_i = W.rho[i], p_i = W.p[i], m_i = W.m[i];
+    const int b_i = W.b[i], sz_i = W.surfzone[i];
+    const int64_t pid_i = W.part_id[i];
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    double acc[D], acc_ale[D], visc[D], st[D], art[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        acc[k] = 0.0;
+        acc_ale[k] = 0.0;
+        visc[k] = 0.0;
+        st[k] = 0.0;
+        art[k] = 0.0;
+    }
+    double Rrho = 0.0, Rrhoc = 0.0, Rrho_d = 0.0;
+    if (W.cellID[i] != -1) {
+        double Vd[D], aero[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Vd[k] = W.cellV[k][i] - vi[k];
+        aero_acc<D>(P, W, i, Vd, W.lam_nb[i], double(e1 - e0), aero);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            acc[k] += aero[k];
+            W.Af[k][i] = aero[k];
+        }
+    }
+    const double a_i0 = p_i / (rho_i * rho_i);
+    const double a_i = (tic && sz_i != 1) ? fabs(a_i0) : a_i0;
+    const double p_lin_i = (tic && sz_i != 1) ? fabs(p_i) : p_i;
+    const bool st_on = pairwise && (!ale || sz_i == 1);
+    for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = N.idx[e];
+        if (W.part_id[j] == pid_i) continue;
+        double Rji[D], Vji[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            Rji[k] = W.x[k][j] - xi[k];
+            Vji[k] = W.v[k][j] - vi[k];
+        }
+        const double rr = pair_rr<D>(N, i, j);
+        const double r = sqrt(rr);
+        const double idist2 = 1.0 / (rr + 0.001 * P.H_sq);
+        const double rho_j = W.rho[j], m_j = W.m[j], p_j = W.p[j];
+        const int b_j = W.b[j];
+        const double volj = m_j / rho_j;
+        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        double g[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
+        /* pressure (PressureContrib, src/Resid.cpp:188-210) */
+        const double pc = linear ? (p_lin_i + p_j) * volj : m_j * (a_i + p_j / (rho_j * rho_j));
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k] -= pc * g[k];
+        /* laminar viscosity (Morris), src/Kernel.h:262-269 */
+        const double rg = dot<D, double>(Rji, g);
+        const double vc = m_j * (P.nu * (rho_i + rho_j) / (rho_i * rho_j) * rg * idist2);
+#pragma unroll
+        for (int k = 0; k < D; ++k) visc[k] += vc * Vji[k];
+        /* pairwise surface tension (Nair & Poeschel), src/Kernel.h:88-113 */
+        if (st_on) {
+            const double fac = (b_i == FJSPH_BOUND || b_j == FJSPH_BOUND) ? 1.0 + 0.5 * cos(0.5 * kPi * 7.0 / 9.0) : 1.0;
+            const double c = -npdm2 * fac * cos(pi3o4 * r / P.H) / r;
+#pragma unroll
+            for (int k = 0; k < D; ++k) st[k] += c * Rji[k];
+        }
+        if (ale) {
+            double vj[D], vPj[D];
+            load3<D>(W.vPert, j, vPj);
+#pragma unroll
+            for (int k = 0; k < D; ++k) vj[k] = W.v[k][j];
+            const double gj = dot<D, double>(vPj, g), gi = dot<D, double>(vPi, g);
+            double dvp[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) dvp[k] = vPj[k] - vPi[k];
+            const double q = dot<D, double>(dvp, g);
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc_ale[a] += (vj[a] * gj + vi[a] * gi - vi[a] * q) * volj;
+            double w1 = 0.0, w2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                w1 += ((vj[k] + vPj[k]) - (vi[k] + vPi[k])) * g[k];
+                w2 += (rho_j * vPj[k] + rho_i * vPi[k]) * g[k];
+            }
+            Rrho -= w1 * volj;
+            Rrhoc += w2 * volj;
+        } else {
+            Rrho -= volj * dot<D, double>(Vji, g);
+        }
+        if (nofrozen) {
+            if (b_j > FJSPH_PISTON) {
+                if (!nodsph) {
+                    double gsum[D];
+#pragma unroll
+                    for (int k = 0; k < D; ++k) gsum[k] = gRi[k] + W.gradRho[k][j];
+                    Rrho_d += volj * ((rho_j - rho_i) + 0.5 * dot<D, double>(gsum, Rji)) * rg * idist2;
+                }
+                const double vdotr = dot<D, double>(Vji, Rji);
+                const double c = linear ? volj * idist2 * vdotr : m_j * art_visc_scale(P, vdotr, idist2, rho_i, rho_j);
+#pragma unroll
+                for (int k = 0; k < D; ++k) art[k] += c * g[k];
+            } else if (!nodsph) {
+                Rrho_d += volj * (rho_j - rho_i) * rg * idist2;
+            }
+        }
+    }
+    if (linear)
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k] /= rho_i;
+    if (csf) {
+        const double c = 1.0 / rho_i * P.sig * W.curve[i] * W.colourG[i];
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k] += c * W.norm[k][i];
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double av = nofrozen ? art[k] : W.aVisc[k][i];
+        double t = acc[k];
+        if (ale) t += acc_ale[k];
+        W.acc[k][i] = t + av + visc[k] + st[k] / m_i + P.grav[k];
+    }
+    double R = Rrho * rho_i;
+    if (ale) R += Rrhoc;
+    if (!nodsph) R += nofrozen ? P.dsph_cont * Rrho_d : W.deltaD[i];
+    W.Rrho[i] = R;
+}
+
+inline unsigned fluid_grid(const Params &P) { return grid_for(P.n - P.nb, kThreads); }
+inline unsigned bound_grid(const Params &P) { return grid_for(P.nb, kThreads); }
+inline unsigned all_grid(const Params &P) { return grid_for(P.n, kThreads); }
+
+} // namespace
+
+#define FJSPH_DISPATCH(P, KERNEL, GRID, ...)                                              \
+    do {                                                                                  \
+        if ((GRID) == 0) break;                                                           \
+        if ((P).D == 2)                                                                   \
+            KERNEL<2><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                           \
+        else                                                                              \
+            KERNEL<3><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                           \
+    } while (0)
+
+void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_dsph_prestep, all_grid(P), P, W, N, npd_part);
+}
+void launch_npd_only(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_npd_only, all_grid(P), P, W, N, npd_part);
+}
+void launch_aero_velocity(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_aero_velocity, fluid_grid(P), P, W, N);
+}
+void launch_detect_surface(const Params &P, const DevState &W, const DevNbr &N, double *const nrm_tmp[3],
+                           cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_surface_normal, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2]);
+    FJSPH_DISPATCH(P, k_surface_curvature, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2]);
+    if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fluid_grid(P) > 0)
+        k_surface_zone<<<fluid_grid(P), kThreads, 0, s>>>(P, W, N);
+}
+void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_dissipation, fluid_grid(P), P, W, N);
+}
+void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_particle_shift, fluid_grid(P), P, W, N);
+}
+void launch_pipe_outlet(const Params &P, const DevState &W, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_pipe_outlet, fluid_grid(P), P, W);
+}
+void launch_bound_velocity(const Params &P, const DevState &W, int nb_rule, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_bound_velocity, bound_grid(P), P, W, nb_rule);
+}
+void launch_no_slip(const Params &P, const DevState &W, const DevNbr &N, double *const vtmp[3], cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_no_slip, bound_grid(P), P, W, N, vtmp[0], vtmp[1], vtmp[2]);
+    FJSPH_DISPATCH(P, k_copy_bound_v, bound_grid(P), P, W, vtmp[0], vtmp[1], vtmp[2]);
+}
+void launch_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_bound_pressure, bound_grid(P), P, W, N);
+}
+void launch_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, int32_t *near_inlet, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_bound_ghost, bound_grid(P), P, W, N, near_inlet);
+}
+void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_bound_dbc, bound_grid(P), P, W);
+}
+void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_resid, fluid_grid(P), P, W, N, npd_dev);
+}
+
+} // namespace fjsph

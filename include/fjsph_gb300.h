@@ -1,0 +1,266 @@
+/*
+ * fjsph_gb300.h -- C ABI of the GB300 WCSPH hot path.
+ *
+ * This library replaces three subsystems of FJSPH (farg-bristol/FJSPH) with device-resident
+ * sm_103a kernels: the neighbour search (src/Neighbours.cpp), the particle residual and its
+ * pre-passes (src/Resid.cpp, src/Shifting.cpp, src/Geometry.cpp:14-308, src/Kernel.h,
+ * src/Aero.h) and the time integrators with the CFL time-step reduction (src/Runge_Kutta.cpp,
+ * src/Newmark_Beta.cpp, src/Integration.cpp).
+ *
+ * Conventions (all entry points):
+ *   - Plain C types only; every pointer is a host pointer unless the name says otherwise.
+ *   - Every function returns an int status: FJSPH_OK (0) or a negative FJSPH_E_* code.  The
+ *     reference prints and calls exit(-1) on errors; this library never exits.
+ *   - A context owns its device memory and one CUDA stream.  Calls on one context must come from
+ *     one host thread at a time (the reference functions are not re-entrant either).
+ *   - Particle order at the boundary is the reference's index order: boundary blocks first, then
+ *     fluid blocks, each block a contiguous index range (LIMITS, src/Var.h:820-883).  Inside the
+ *     context particles are kept in cell order; upload and download convert.
+ *   - Vectors are stored per particle as `dim` consecutive doubles (x,y[,z]); the 2x2/3x3 L
+ *     matrix as dim*dim doubles, row-major.
+ */
+#ifndef FJSPH_GB300_H
+#define FJSPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------- */
+#define FJSPH_OK 0
+#define FJSPH_E_ARG (-1)         /* bad argument (null pointer, size, unsupported option)    */
+#define FJSPH_E_CUDA (-2)        /* a CUDA runtime call failed                               */
+#define FJSPH_E_CAPACITY (-3)    /* particle count above the context capacity                */
+#define FJSPH_E_NEIGHBOUR (-4)   /* neighbour list storage could not be grown                */
+#define FJSPH_E_NONFINITE (-5)   /* NaN/Inf found in positions or in the residual            */
+#define FJSPH_E_UNSUPPORTED (-6) /* variant combination the reference cannot build either    */
+#define FJSPH_E_STATE (-7)       /* call order error (e.g. residual before neighbour search) */
+
+/* ---- particle types (src/VarDefs.h:92-102) ------------------------------------------------- */
+enum fjsph_part_type {
+    FJSPH_BOUND = 0,
+    FJSPH_PISTON = 1,
+    FJSPH_BUFFER = 2,
+    FJSPH_BACK = 3,
+    FJSPH_PIPE = 4,
+    FJSPH_FREE = 5,
+    FJSPH_OUTLET = 6,
+    FJSPH_LOST = 7
+};
+
+/* ---- compile-time physics variants of the reference, as run-time bits -------------------- */
+/* Each bit stands for one -D flag of the reference makefile (README "Building"). */
+#define FJSPH_VAR_ALE (1u << 0)      /* -DALE: ALE momentum/continuity + particle shifting  */
+#define FJSPH_VAR_LINEAR (1u << 1)   /* -DLINEAR: Marrone pressure form, linear art. visc.  */
+#define FJSPH_VAR_NOFROZEN (1u << 2) /* -DNOFROZEN: art. visc. + delta-SPH inside residual   */
+#define FJSPH_VAR_NODSPH (1u << 3)   /* -DNODSPH: no delta-SPH continuity term              */
+#define FJSPH_VAR_TIC (1u << 4)      /* -DTIC: tensile-instability control                  */
+#define FJSPH_VAR_CUBIC (1u << 5)    /* -DCUBIC: cubic spline kernel instead of Wendland C2 */
+
+/* Surface-tension model (-DPAIRWISE default, -DCSF, -DNOST; -DHESF does not build upstream). */
+enum fjsph_st_model { FJSPH_ST_PAIRWISE = 0, FJSPH_ST_NOST = 1, FJSPH_ST_CSF = 2 };
+
+/* Enumerations mirrored from src/VarDefs.h:129-166. */
+enum fjsph_solver { FJSPH_NEWMARK_BETA = 0, FJSPH_RUNGE_KUTTA = 1 };
+enum fjsph_bound_solver { FJSPH_DBC = 0, FJSPH_PRESSURE_G = 1, FJSPH_GHOST = 2 };
+enum fjsph_eos { FJSPH_COLE_EOS = 0, FJSPH_ISO_EOS = 1 };
+enum fjsph_aero_case { FJSPH_NOAERO = 0, FJSPH_GISSLER = 1, FJSPH_INDUCED_PRESSURE = 2, FJSPH_SKIN_FRIC = 3 };
+
+/* Arithmetic form of the pair kernels. */
+enum fjsph_precision {
+    FJSPH_PREC_FP64 = 0,  /* plain FP64 everywhere                                            */
+    FJSPH_PREC_MIXED = 1  /* FP32 pair arithmetic on cell-relative positions, compensated sums, */
+                          /* FP64 membership test / integration / dt / global sums             */
+};
+
+/* Aerodynamic closure used inside the residual. */
+enum fjsph_aero_closure {
+    FJSPH_CLOSURE_PLAIN = 0,  /* Gissler occlusion + drag (src/Aero.h:37-98)         */
+    FJSPH_CLOSURE_LEARNED = 1 /* BF16 MLP stand-in for occlusion and drag coefficient */
+};
+
+/*
+ * Settings: the subset of SIM / FLUID / AERO / INTEG_SETT (src/Var.h:63-394) that the hot path
+ * reads, with the values that Set_Values (src/IO.cpp:26-128) derives already filled in.
+ * fjsph_settings_defaults() + fjsph_settings_derive() give the reference's defaults and
+ * derivations; the Python host layer fills the same struct from a para file.
+ */
+typedef struct fjsph_settings {
+    int32_t dim;            /* SIMDIM: 2 or 3                                           */
+    uint32_t variant;       /* FJSPH_VAR_* bits                                         */
+    int32_t st_model;       /* fjsph_st_model                                           */
+    int32_t precision;      /* fjsph_precision                                          */
+    int32_t aero_closure;   /* fjsph_aero_closure                                       */
+    int32_t solver_type;    /* fjsph_solver                                             */
+
+    /* FLUID */
+    int32_t pressure_rel;   /* fjsph_eos                                                */
+    double H, H_sq, sr, H_fac, W_dx, W_correc;
+    double rho_rest, rho_pipe, press_pipe, press_back, rho_max, rho_min, rho_var, rho_max_iter;
+    double sim_mass, bnd_mass, visc_alpha, speed_sound, mu, nu, sig, gam, B, contangb;
+    double dsph_delta, dsph_cont;
+
+    /* SIM */
+    double particle_step, dx, scale;
+    double grav[3];
+    int32_t asource;        /* 0 = constVel (only analytic source supported)            */
+    int32_t init_hydro_pressure;
+    double hydro_height;
+    int64_t max_points;
+
+    /* AERO */
+    int32_t acase, use_lam, use_TAB_def, use_dx;
+    double v_inf[3];
+    double L, td, omega, tmax, ycoef, Cf, Ck, Cd, Cb, Cdef, A_sphere, A_plate;
+    double v_ref, p_ref, rho_g, mu_g, mass_g, temp_g, R_g, gamma_g, sos, i_sos_sq, M_ref;
+    double lam_cutoff, interp_fac, i_interp_fac, n_full, i_n_full, i_n_count;
+
+    /* INTEG_SETT */
+    int32_t max_subits, n_stable, n_stable_limit, n_unstable, n_unstable_limit;
+    double subits_factor, cfl, cfl_step, cfl_max, cfl_min, current_time, last_frame_time;
+    double frame_time_interval, min_residual, delta_t, delta_t_max, delta_t_min;
+    double nb_beta, nb_gamma, max_shift_vel;
+
+    /* Extensions of this library (no reference counterpart). */
+    int32_t reorder_interval; /* re-sort particle storage every N neighbour searches (0 = never) */
+    int32_t learned_judge_interval; /* re-run the plain closure every N steps (learned form) */
+} fjsph_settings;
+
+/* One LIMITS entry (src/Var.h:820-881). */
+#define FJSPH_MAX_TIMES 16
+typedef struct fjsph_block {
+    int64_t first, second;      /* index range [first, second)                         */
+    int32_t is_fluid;           /* 0 = boundary block, 1 = fluid block                  */
+    int32_t bound_solver;       /* fjsph_bound_solver (boundary blocks)                 */
+    int32_t no_slip;
+    int32_t block_type;         /* shape_type (src/VarDefs.h:116-127); 6 = inletZone    */
+    int32_t fixed_vel_or_dynamic;
+    int32_t n_times;            /* motion table length; 0 = constant vels[0]           */
+    double times[FJSPH_MAX_TIMES];
+    double vels[FJSPH_MAX_TIMES][3];
+    double delete_norm[3], delconst;
+    double insert_norm[3], insconst;
+    double aero_norm[3], aeroconst;
+} fjsph_block;
+
+/* Inlet bookkeeping of one inletZone block: back[n_back], buffer[n_back][depth] (reference indices). */
+typedef struct fjsph_inlet {
+    int32_t block;
+    int64_t n_back, depth;
+    int64_t *back;
+    int64_t *buffer;
+} fjsph_inlet;
+
+/*
+ * Host view of an SPHState (src/Var.h:499-642, only the fields the hot path touches), as
+ * structure-of-arrays.  n particles; vector fields hold n*dim doubles, L holds n*dim*dim.
+ */
+typedef struct fjsph_state_view {
+    int64_t n;
+    double *xi, *v, *acc, *Af, *aVisc, *cellV, *gradRho, *norm, *vPert; /* n*dim   */
+    double *L;                                                            /* n*dim^2 */
+    double *Rrho, *rho, *p, *m, *curve, *norm_curve, *woccl, *pDist, *deltaD;
+    double *cellP, *cellRho, *colourG, *colour, *lam, *lam_nb, *kernsum;
+    int64_t *part_id, *cellID;
+    int32_t *b, *surf, *surfzone;
+} fjsph_state_view;
+
+/* Opaque device context. */
+typedef struct fjsph_ctx fjsph_ctx;
+
+/* Which of the two states a call reads or writes: time n (pn) or the working state (pnp1). */
+#define FJSPH_PN 0
+#define FJSPH_PNP1 1
+
+/* ---- settings helpers (src/Var.h defaults, src/IO.cpp:26-128 Set_Values) -------------------- */
+int fjsph_settings_defaults(fjsph_settings *s, int32_t dim);
+int fjsph_settings_derive(fjsph_settings *s);
+
+/* ---- context ------------------------------------------------------------------------------ */
+/* capacity = maximum particle count (SIM::max_points analogue).  Replaces the setup half of
+ * src/FJSPH.cpp:104-149 (state vectors, KD-tree adaptor). */
+int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out);
+int fjsph_ctx_destroy(fjsph_ctx *ctx);
+int fjsph_set_settings(fjsph_ctx *ctx, const fjsph_settings *s);
+int fjsph_get_settings(fjsph_ctx *ctx, fjsph_settings *s);
+/* LIMITS (src/Var.h:883) and the inlet back/buffer tables (src/shapes/inlet.cpp:578-640). */
+int fjsph_set_limits(fjsph_ctx *ctx, const fjsph_block *blocks, int32_t nblocks, int64_t n_bound_blocks);
+int fjsph_set_inlet(fjsph_ctx *ctx, const fjsph_inlet *inlet);
+int fjsph_get_inlet(fjsph_ctx *ctx, fjsph_inlet *inlet);
+/* Replaces the SPHState hand-over between Integrator and its callers (src/Integration.h:15-68). */
+int fjsph_state_upload(fjsph_ctx *ctx, int32_t which, const fjsph_state_view *st);
+int fjsph_state_download(fjsph_ctx *ctx, int32_t which, fjsph_state_view *st);
+int fjsph_particle_count(fjsph_ctx *ctx, int64_t *n_total, int64_t *n_bound);
+
+/* ---- neighbour search (src/Neighbours.cpp:7-47) ------------------------------------------- */
+/* update_neighbours on pnp1: all pairs with squared distance < sr, self included. */
+int fjsph_update_neighbours(fjsph_ctx *ctx, int64_t *n_pairs);
+/* Export the lists in reference order: offsets[n+1], idx[n_pairs], d2[n_pairs] (each list sorted
+ * by neighbour index).  Any pointer may be NULL to skip it. */
+int fjsph_neighbours_export(fjsph_ctx *ctx, int64_t *offsets, int64_t *idx, double *d2);
+
+/* ---- pre-passes ------------------------------------------------------------------------------ */
+int fjsph_dsph_prestep(fjsph_ctx *ctx, double *npd);       /* src/Shifting.cpp:12-123      */
+int fjsph_get_aero_velocity(fjsph_ctx *ctx);               /* src/Resid.cpp:471-613, constVel */
+int fjsph_detect_surface(fjsph_ctx *ctx);                  /* src/Geometry.cpp:14-280      */
+int fjsph_dissipation_terms(fjsph_ctx *ctx);               /* src/Shifting.cpp:126-186     */
+int fjsph_particle_shift(fjsph_ctx *ctx);                  /* src/Shifting.cpp:189-290     */
+int fjsph_check_pipe_outlet(fjsph_ctx *ctx);               /* src/Containment.cpp:822-894 (constVel) */
+
+/* ---- boundary passes and residual on pnp1 -------------------------------------------------- */
+int fjsph_get_boundary_pressure(fjsph_ctx *ctx);           /* src/Resid.cpp:21-76          */
+int fjsph_boundary_ghost(fjsph_ctx *ctx, int32_t *near_inlet); /* src/Resid.cpp:122-160    */
+int fjsph_boundary_dbc(fjsph_ctx *ctx);                    /* src/Resid.cpp:78-117         */
+int fjsph_set_no_slip(fjsph_ctx *ctx);                     /* src/Resid.cpp:162-186        */
+int fjsph_get_acc_and_rrho(fjsph_ctx *ctx, double npd);    /* src/Resid.cpp:426-469        */
+
+/* ---- integrators and time step --------------------------------------------------------------- */
+int fjsph_find_timestep(fjsph_ctx *ctx, double *dt);       /* src/Integration.cpp:370-443  */
+/* Get_First_RK (src/Runge_Kutta.cpp:462-476): pnp1 = intermediate(pn, pn, dt/2). */
+int fjsph_get_first_rk(fjsph_ctx *ctx, double npd, double *logbase);
+/* Runge_Kutta4 (src/Runge_Kutta.cpp:480-515) with st_1 = pnp1 on entry; pnp1 = result. */
+int fjsph_runge_kutta4(fjsph_ctx *ctx, double npd, double logbase, double *rms_error);
+/* Newmark_Beta::Do_NB_Iter (src/Newmark_Beta.cpp:54-301), one sub-iteration on pnp1. */
+int fjsph_nb_iter(fjsph_ctx *ctx, double npd);
+/* Newmark_Beta::Newmark_Beta (src/Newmark_Beta.cpp:303-331), full sub-iteration loop. */
+int fjsph_newmark_beta(fjsph_ctx *ctx, double npd, double *logbase, int32_t *iteration, double *rms_error);
+
+/* Integrator::integrate_no_update (src/Integration.cpp:27-107). */
+int fjsph_integrate_no_update(fjsph_ctx *ctx, double *rms_error);
+/* Integrator::integrate (src/Integration.cpp:233-303): one full step incl. update_data. */
+int fjsph_integrate(fjsph_ctx *ctx, double *rms_error);
+/* Run n_steps of integrate() back to back without host round trips where possible. */
+int fjsph_integrate_n(fjsph_ctx *ctx, int32_t n_steps, double *last_error);
+
+/* ---- diagnostics -------------------------------------------------------------------------- */
+/* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
+int fjsph_step_report(fjsph_ctx *ctx, double *out5);
+/* Count and total duration (ms) of kernel launches recorded since the last reset. */
+int fjsph_launch_stats(fjsph_ctx *ctx, int64_t *n_launches, int32_t reset);
+/* CUDA stream of the context (a cudaStream_t), for callers that time with events. */
+int fjsph_ctx_stream(fjsph_ctx *ctx, void **stream);
+/* Timing support (no counterpart in the reference, which times whole steps with a wall clock,
+ * src/Integration.cpp:239-252).  Events are recorded on the context's stream.
+ * fjsph_event_record(ctx, slot) records event `slot` (0..15); fjsph_event_elapsed gives the
+ * milliseconds between two recorded slots after synchronising on the later one. */
+int fjsph_event_record(fjsph_ctx *ctx, int32_t slot);
+int fjsph_event_elapsed(fjsph_ctx *ctx, int32_t slot_a, int32_t slot_b, double *ms);
+/* Per-pass device time: when enabled, every pass of the step is bracketed by events.
+ * fjsph_profile_read fills ms[FJSPH_NPASS] and launches[FJSPH_NPASS] accumulated since the last
+ * read (and clears them); fjsph_profile_pass_name names pass k. */
+#define FJSPH_NPASS 12
+int fjsph_profile_enable(fjsph_ctx *ctx, int32_t on);
+int fjsph_profile_read(fjsph_ctx *ctx, double *ms, int64_t *launches);
+const char *fjsph_profile_pass_name(int32_t k);
+const char *fjsph_status_string(int status);
+/* ABI check for bindings: sizes[0..3] = sizeof(fjsph_settings), sizeof(fjsph_block),
+ * sizeof(fjsph_inlet), sizeof(fjsph_state_view).  No counterpart in the reference. */
+int fjsph_abi_sizes(int64_t *sizes4);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FJSPH_GB300_H */
