@@ -64,6 +64,8 @@ PROTOTYPES = {
     "fjsph_profile_enable": (C.c_int, [_P, _i32]),
     "fjsph_profile_read": (C.c_int, [_P, _dp, _i64p]),
     "fjsph_profile_pass_name": (C.c_char_p, [_i32]),
+    "fjsph_find_timestep_noalloc": (C.c_int, [C.POINTER(d.Settings), _i64, C.POINTER(_dp), C.POINTER(_dp), _dp, _dp,
+                                              _dp, C.POINTER(_dp), C.POINTER(_dp), _P, _dp, _dp]),
 }
 
 _lib = None

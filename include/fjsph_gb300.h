@@ -234,6 +234,28 @@ int fjsph_integrate(fjsph_ctx *ctx, double *rms_error);
 /* Run n_steps of integrate() back to back without host round trips where possible. */
 int fjsph_integrate_n(fjsph_ctx *ctx, int32_t n_steps, double *last_error);
 
+/* ---- time-step bound without allocation --------------------------------------------------- */
+/* No counterpart in the reference.  The CFL time-step bound of fjsph_find_timestep for callers
+ * that may not call cudaMalloc (their device memory belongs to another allocator or pool, or no
+ * allocation is allowed on their time-step path).  No context is needed and nothing is
+ * allocated: the reduction's scratch is a fixed 256 KB __device__ array held by every GPU that
+ * loads this library.
+ *   - acc, Af, v, vPert: arrays of `dim` device pointers (x, y[, z] components); Rrho, rho, curve:
+ *     device pointers; each holds the n_fluid fluid particles.  vPert is read only with
+ *     FJSPH_VAR_ALE (may be NULL otherwise).
+ *   - n_fluid <= 16,777,216; larger counts return FJSPH_E_CAPACITY.
+ *   - dt (host) receives the time step of src/Integration.cpp:370-443 under the settings' cfl,
+ *     dt limits and frame time; maxima7 (host) receives maxf, maxAf, maxdrho, maxRhoi, minST,
+ *     maxU, maxShift.
+ *   - stream: a cudaStream_t (NULL = default stream); the call synchronises it before returning.
+ *   - The first call on a device looks up the scratch array's device address (once per device,
+ *     with that device current); make that first call before any stream capture.
+ *   - All calls share the scratch array: calls that overlap on the GPU race; serialise them. */
+int fjsph_find_timestep_noalloc(const fjsph_settings *s, int64_t n_fluid, const double *const acc[3],
+                                const double *const Af[3], const double *Rrho, const double *rho,
+                                const double *curve, const double *const v[3], const double *const vPert[3],
+                                void *stream, double *dt, double *maxima7);
+
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
 int fjsph_step_report(fjsph_ctx *ctx, double *out5);
