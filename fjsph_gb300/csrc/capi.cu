@@ -121,6 +121,10 @@ struct fjsph_ctx {
     int64_t launches = 0;
     Profiler prof;
     cudaEvent_t user_ev[16] = {};
+    /* FP32 split-precision form */
+    Packed K{};
+    bool packed_alloc = false;
+    bool dirty_full = true, dirty_all = true, dirty_bound = true;
 };
 
 namespace {
@@ -183,7 +187,7 @@ int validate_settings(const fjsph_settings *s) {
     if (s->st_model < FJSPH_ST_PAIRWISE || s->st_model > FJSPH_ST_CSF) return FJSPH_E_ARG;
     /* -DNOFROZEN -DLINEAR does not compile upstream (src/Resid.cpp:381 uses fluid.rho0) */
     if ((s->variant & FJSPH_VAR_NOFROZEN) && (s->variant & FJSPH_VAR_LINEAR)) return FJSPH_E_UNSUPPORTED;
-    if (s->precision != FJSPH_PREC_FP64) return FJSPH_E_UNSUPPORTED;
+    if (s->precision != FJSPH_PREC_FP64 && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
     if (s->asource != 0) return FJSPH_E_UNSUPPORTED;
     return FJSPH_OK;
 }
@@ -282,6 +286,41 @@ DevNbr make_nbr(const fjsph_ctx *c) {
     N.idx = c->nbr_idx;
     for (int k = 0; k < 3; ++k) N.xs[k] = c->xs[k];
     return N;
+}
+
+bool mixed(const fjsph_ctx *c) { return c->s.precision == FJSPH_PREC_MIXED; }
+
+int alloc_packed(fjsph_ctx *c) {
+    if (c->packed_alloc) return FJSPH_OK;
+    Packed &K = c->K;
+    float4 **arrs[] = {&K.A, &K.B, &K.C, &K.E, &K.F, &K.G, &K.N, &K.T};
+    for (float4 **a : arrs) TRY(dalloc(c, a, c->cap));
+    TRY(dalloc(c, &K.bits, c->cap));
+    TRY(dalloc(c, &K.rr, c->nbr_cap));
+    c->packed_alloc = true;
+    c->dirty_full = true;
+    return FJSPH_OK;
+}
+
+void mark_full(fjsph_ctx *c) { c->dirty_full = true; }
+void mark_all(fjsph_ctx *c) { c->dirty_all = true; }
+void mark_bound(fjsph_ctx *c) { c->dirty_bound = true; }
+
+/* Refresh the packed FP32 inputs of the mixed form where the FP64 state changed. */
+void ensure_pack(fjsph_ctx *c) {
+    if (!mixed(c) || !c->packed_alloc || c->n == 0) return;
+    Params P = make_params(c);
+    if (c->dirty_full) {
+        launch_m_pack(P, WS(c), c->K, 0, c->n, 1, c->stream);
+        c->launches++;
+    } else if (c->dirty_all) {
+        launch_m_pack(P, WS(c), c->K, 0, c->n, 0, c->stream);
+        c->launches++;
+    } else if (c->dirty_bound) {
+        launch_m_pack(P, WS(c), c->K, 0, c->nb, 0, c->stream);
+        c->launches++;
+    }
+    c->dirty_full = c->dirty_all = c->dirty_bound = false;
 }
 
 int sync(fjsph_ctx *c) {
@@ -501,6 +540,7 @@ int reorder_states(fjsph_ctx *c, const Params &P) {
         CU(cudaMemcpyAsync(c->xs[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
     launch_refresh_xf(P, c->xs, c->G, s);
     c->launches += 1;
+    mark_full(c);
     return FJSPH_OK;
 }
 
@@ -535,9 +575,18 @@ int search(fjsph_ctx *c) {
         CU(cudaFree(c->nbr_idx));
         c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->nbr_idx), c->allocs.end());
         TRY(dalloc(c, &c->nbr_idx, ncap));
+        if (c->packed_alloc) {
+            CU(cudaFree(c->K.rr));
+            c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->K.rr), c->allocs.end());
+            TRY(dalloc(c, &c->K.rr, ncap));
+        }
         c->nbr_cap = ncap;
     }
-    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, s);
+    if (mixed(c)) {
+        TRY(alloc_packed(c));
+        ensure_pack(c);
+    }
+    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? &c->K : nullptr, s);
     c->launches += 1;
     c->n_pairs = total;
     c->nbr_valid = true;
@@ -550,7 +599,12 @@ __global__ void k_set_scalar(double *dst, double v) { *dst = v; }
 
 int prestep_npd(fjsph_ctx *c, const Params &P) {
     Section sec(c, PASS_PRESTEP);
-    launch_dsph_prestep(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_dsph(P, WS(c), make_nbr(c), c->K, c->npd_part, c->stream);
+    } else {
+        launch_dsph_prestep(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+    }
     launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
     k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
     c->launches += 4;
@@ -560,7 +614,12 @@ int prestep_npd(fjsph_ctx *c, const Params &P) {
 /* npd only (Runge-Kutta first pre-pass, see integrate_no_update) */
 int npd_only(fjsph_ctx *c, const Params &P) {
     Section sec(c, PASS_PRESTEP);
-    launch_npd_only(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_npd(P, make_nbr(c), c->K, c->npd_part, c->stream);
+    } else {
+        launch_npd_only(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+    }
     launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
     k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
     c->launches += 4;
@@ -576,23 +635,33 @@ int prestep_passes(fjsph_ctx *c) {
     {
         Section sec(c, PASS_SURFACE);
         launch_aero_velocity(P, WS(c), N, s);
-        launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
+        if (mixed(c))
+            launch_m_surface(P, WS(c), N, c->K, s);
+        else
+            launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
         c->launches += 4;
     }
     if (!(c->s.variant & FJSPH_VAR_NOFROZEN)) {
         Section sec(c, PASS_DISSIPATION);
-        launch_dissipation(P, WS(c), N, s);
+        if (mixed(c))
+            launch_m_dissipation(P, WS(c), N, c->K, s);
+        else
+            launch_dissipation(P, WS(c), N, s);
         c->launches++;
     }
     if (c->s.variant & FJSPH_VAR_ALE) {
         Section sec(c, PASS_SHIFT);
-        launch_particle_shift(P, WS(c), N, s);
+        if (mixed(c))
+            launch_m_particle_shift(P, WS(c), N, c->K, s);
+        else
+            launch_particle_shift(P, WS(c), N, s);
         c->launches++;
     }
     {
         Section sec(c, PASS_UPDATE);
         launch_pipe_outlet(P, WS(c), s);
         c->launches++;
+        mark_all(c);
     }
     c->pn_equals_W = false;
     return FJSPH_OK;
@@ -625,15 +694,37 @@ int boundary_section(fjsph_ctx *c, const Params &P, int nb_rule) {
         launch_bound_dbc(P, WS(c), s);
         c->launches++;
     }
+    if (mixed(c)) {
+        mark_bound(c); /* boundary velocities changed */
+        ensure_pack(c);
+    }
     if (has_solver(c, FJSPH_PRESSURE_G)) {
-        launch_bound_pressure(P, WS(c), N, s);
+        if (mixed(c))
+            launch_m_bound_pressure(P, WS(c), N, c->K, s);
+        else
+            launch_bound_pressure(P, WS(c), N, s);
         c->launches++;
     }
     if (has_solver(c, FJSPH_GHOST)) {
-        launch_bound_ghost(P, WS(c), N, c->S.near_inlet, s);
+        if (mixed(c))
+            launch_m_bound_ghost(P, WS(c), N, c->K, c->S.near_inlet, s);
+        else
+            launch_bound_ghost(P, WS(c), N, c->S.near_inlet, s);
         c->launches++;
     }
+    mark_bound(c);
     return FJSPH_OK;
+}
+
+/* The residual in the configured form. */
+void resid(fjsph_ctx *c, const Params &P) {
+    Section sec(c, PASS_RESID);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_resid(P, WS(c), make_nbr(c), c->K, &c->dsc->npd, c->stream);
+    } else {
+        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, c->stream);
+    }
 }
 
 DevInlet dev_inlet(const fjsph_ctx *c, const HostInlet &I) {
@@ -667,16 +758,14 @@ int rk_intermediate(fjsph_ctx *c, int stage, double dt_scale) {
         launch_bound_rho_update(P, PN(c), WS(c), c->S, 0, sum_w, &c->dsc->dt, dt_scale, s);
         c->launches++;
     }
-    {
-        Section sec(c, PASS_RESID);
-        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, s);
-    }
+    resid(c, P);
     {
         Section sec(c, PASS_UPDATE);
         launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, &c->dsc->dt, dt_scale, s);
     }
     c->launches += 2;
     inlet_buffers(c, P, 0, dt_scale);
+    mark_all(c);
     c->pn_equals_W = false;
     return FJSPH_OK;
 }
@@ -689,10 +778,7 @@ int rk_final(fjsph_ctx *c) {
         launch_bound_rho_update(P, PN(c), WS(c), c->S, 1, 0.0, &c->dsc->dt, 1.0, s);
         c->launches++;
     }
-    {
-        Section sec(c, PASS_RESID);
-        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, s);
-    }
+    resid(c, P);
     {
         Section sec(c, PASS_UPDATE);
         for (int k = 0; k < c->D; ++k)
@@ -701,6 +787,7 @@ int rk_final(fjsph_ctx *c) {
     }
     c->launches += 2;
     inlet_buffers(c, P, 1, 1.0);
+    mark_all(c);
     c->pn_equals_W = false;
     return FJSPH_OK;
 }
@@ -731,6 +818,7 @@ int copy_state(fjsph_ctx *c, int from, int to) {
     Section sec(c, PASS_COPY);
     launch_copy(state_fields(c->st[from], c->D), state_fields(c->st[to], c->D), c->n, c->stream);
     c->launches++;
+    if (to == c->iW) mark_full(c);
     return FJSPH_OK;
 }
 
@@ -777,10 +865,7 @@ int nb_iter(fjsph_ctx *c) {
     Params P = make_params(c);
     cudaStream_t s = c->stream;
     TRY(boundary_section(c, P, 1));
-    {
-        Section sec(c, PASS_RESID);
-        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, s);
-    }
+    resid(c, P);
     c->launches++;
     if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
         launch_bound_rho_update(P, PN(c), WS(c), c->S, 2, 0.0, &c->dsc->dt, 1.0, s);
@@ -789,6 +874,7 @@ int nb_iter(fjsph_ctx *c) {
     launch_nb_update(P, PN(c), WS(c), &c->dsc->dt, s);
     c->launches++;
     inlet_buffers(c, P, 2, 1.0);
+    mark_all(c);
     c->pn_equals_W = false;
     return FJSPH_OK;
 }
@@ -921,6 +1007,7 @@ int integrate(fjsph_ctx *c, double &step_error) {
     /* update_data: zero-density guard (src/Integration.cpp:116-124) and pn = pnp1 */
     launch_density_guard(make_params(c), WS(c), c->stream);
     c->launches++;
+    mark_all(c);
     TRY(copy_state(c, c->iW, c->ipn));
     c->pn_equals_W = true;
     fjsph_settings &I = c->s;
@@ -1040,6 +1127,7 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     c->reorder_tmp_len = 2 * capacity + 1 + capacity / 2048 + 16;
     A(dalloc(c, &c->reorder_tmp, c->reorder_tmp_len));
     A(dalloc(c, &c->dsc, 1));
+    if (s->precision == FJSPH_PREC_MIXED) A(alloc_packed(c));
 #undef A
     if (cudaMallocHost(&c->hsc, sizeof(DevScalars)) != cudaSuccess) return fail(FJSPH_E_CUDA);
     std::memset(c->hsc, 0, sizeof(DevScalars));
@@ -1075,7 +1163,15 @@ int fjsph_set_settings(fjsph_ctx *c, const fjsph_settings *s) {
     TRY(check_ctx(c));
     TRY(validate_settings(s));
     if (s->dim != c->D) return FJSPH_E_ARG;
+    const bool was_mixed = mixed(c);
     c->s = *s;
+    if (mixed(c)) {
+        TRY(alloc_packed(c));
+        if (!was_mixed) {
+            mark_full(c);
+            c->nbr_valid = false; /* the lists need their FP32 squared distances */
+        }
+    }
     return FJSPH_OK;
 }
 
@@ -1183,7 +1279,10 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         TRY(download_keys(c, keys));
     }
     TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, keys, true));
-    if (which == FJSPH_PNP1) c->nbr_valid = false;
+    if (which == FJSPH_PNP1) {
+        c->nbr_valid = false;
+        mark_full(c);
+    }
     c->pn_equals_W = false;
     return FJSPH_OK;
 }
@@ -1275,14 +1374,24 @@ int fjsph_get_aero_velocity(fjsph_ctx *c) {
 
 int fjsph_detect_surface(fjsph_ctx *c) {
     TRY(need_nbr(c));
-    launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_surface(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
+    } else {
+        launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, c->stream);
+    }
     c->pn_equals_W = false;
     return sync(c);
 }
 
 int fjsph_dissipation_terms(fjsph_ctx *c) {
     TRY(need_nbr(c));
-    launch_dissipation(make_params(c), WS(c), make_nbr(c), c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_dissipation(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
+    } else {
+        launch_dissipation(make_params(c), WS(c), make_nbr(c), c->stream);
+    }
     c->pn_equals_W = false;
     return sync(c);
 }
@@ -1290,7 +1399,12 @@ int fjsph_dissipation_terms(fjsph_ctx *c) {
 int fjsph_particle_shift(fjsph_ctx *c) {
     TRY(need_nbr(c));
     if (!(c->s.variant & FJSPH_VAR_ALE)) return FJSPH_E_UNSUPPORTED;
-    launch_particle_shift(make_params(c), WS(c), make_nbr(c), c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_particle_shift(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
+    } else {
+        launch_particle_shift(make_params(c), WS(c), make_nbr(c), c->stream);
+    }
     c->pn_equals_W = false;
     return sync(c);
 }
@@ -1299,19 +1413,31 @@ int fjsph_check_pipe_outlet(fjsph_ctx *c) {
     TRY(need_state(c));
     launch_pipe_outlet(make_params(c), WS(c), c->stream);
     c->pn_equals_W = false;
+    mark_all(c);
     return sync(c);
 }
 
 int fjsph_get_boundary_pressure(fjsph_ctx *c) {
     TRY(need_nbr(c));
-    launch_bound_pressure(make_params(c), WS(c), make_nbr(c), c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_bound_pressure(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
+    } else {
+        launch_bound_pressure(make_params(c), WS(c), make_nbr(c), c->stream);
+    }
+    mark_bound(c);
     c->pn_equals_W = false;
     return sync(c);
 }
 
 int fjsph_boundary_ghost(fjsph_ctx *c, int32_t *near_inlet) {
     TRY(need_nbr(c));
-    launch_bound_ghost(make_params(c), WS(c), make_nbr(c), c->S.near_inlet, c->stream);
+    if (mixed(c)) {
+        ensure_pack(c);
+        launch_m_bound_ghost(make_params(c), WS(c), make_nbr(c), c->K, c->S.near_inlet, c->stream);
+    } else {
+        launch_bound_ghost(make_params(c), WS(c), make_nbr(c), c->S.near_inlet, c->stream);
+    }
     c->pn_equals_W = false;
     TRY(sync(c));
     if (near_inlet && c->nb > 0) {
@@ -1335,13 +1461,14 @@ int fjsph_set_no_slip(fjsph_ctx *c) {
     TRY(need_nbr(c));
     launch_no_slip(make_params(c), WS(c), make_nbr(c), c->vtmp, c->stream);
     c->pn_equals_W = false;
+    mark_bound(c);
     return sync(c);
 }
 
 int fjsph_get_acc_and_rrho(fjsph_ctx *c, double npd) {
     TRY(need_nbr(c));
     TRY(set_npd_device(c, npd));
-    launch_resid(make_params(c), WS(c), make_nbr(c), &c->dsc->npd, c->stream);
+    resid(c, make_params(c));
     c->pn_equals_W = false;
     return sync(c);
 }

@@ -8,6 +8,13 @@
 
 namespace fjsph {
 
+/* Packed FP32 split-precision inputs of the mixed form (see sweeps_mixed.cu). */
+struct Packed {
+    float4 *A, *B, *C, *E, *F, *G, *N, *T;
+    int32_t *bits;
+    float *rr; /* search-time squared distance per CSR pair */
+};
+
 /* ---- neighbours.cu ------------------------------------------------------------------------ */
 struct CellGrid {
     int64_t table_size;      /* power of two                                  */
@@ -29,8 +36,10 @@ void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, c
 void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s);
 void launch_scatter_sort(const Params &P, CellGrid &G, cudaStream_t s);
 void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s);
+/* K (may be null): when given, the squared distance of each pair is also written to K->rr, in FP32
+ * from the hi/lo split positions in K->A / K->B. */
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     cudaStream_t s);
+                     const Packed *K, cudaStream_t s);
 /* Float positions by slot from xs (after a re-ordering moved the slots). */
 void launch_refresh_xf(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s);
 /* Re-ordering: new slot of every old slot, boundary group first, each group in bucket order. */
@@ -54,6 +63,21 @@ void launch_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, int
 void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s);
 /* residual (src/Resid.cpp:426) over fluid slots */
 void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, cudaStream_t s);
+
+/* ---- sweeps_mixed.cu (FP32 split-precision form) ------------------------------------------ */
+void launch_m_pack(const Params &P, const DevState &W, const Packed &K, int64_t i0, int64_t i1, int full,
+                   cudaStream_t s);
+void launch_m_npd(const Params &P, const DevNbr &N, const Packed &K, double *npd_part, cudaStream_t s);
+void launch_m_dsph(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, double *npd_part,
+                   cudaStream_t s);
+void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
+void launch_m_dissipation(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
+void launch_m_particle_shift(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
+void launch_m_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
+void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, int32_t *near_inlet,
+                          cudaStream_t s);
+void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
+                    cudaStream_t s);
 
 /* ---- integrate.cu ------------------------------------------------------------------------- */
 struct RKScratch {

@@ -266,12 +266,32 @@ __global__ void __launch_bounds__(kThreads) k_nbr_count(Params P, double *xs0, d
 
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, double *xs1, double *xs2, CellGrid G,
-                                                        const int64_t *off, int32_t *idx) {
+                                                        const int64_t *off, int32_t *idx, const float4 *A,
+                                                        const float4 *B, float *rr) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     double *const xs[3] = {xs0, xs1, xs2};
     int64_t w = off[i];
     const int64_t wend = off[i + 1];
+    if (rr) {
+        /* squared distance in FP32 from the hi/lo split (about 1e-7 relative) */
+        const float4 Ai = A[i], Bi = B[i];
+        walk<D>(P, xs, G, i, [&](int32_t j) {
+            if (w < wend) {
+                idx[w] = j;
+                const float4 Aj = A[j], Bj = B[j];
+                const float dx = (Aj.x - Ai.x) + (Bj.x - Bi.x), dy = (Aj.y - Ai.y) + (Bj.y - Bi.y);
+                float d2 = dx * dx + dy * dy;
+                if (D == 3) {
+                    const float dz = (Aj.z - Ai.z) + (Bj.z - Bi.z);
+                    d2 += dz * dz;
+                }
+                rr[w] = d2;
+            }
+            ++w;
+        });
+        return;
+    }
     walk<D>(P, xs, G, i, [&](int32_t j) {
         if (w < wend) idx[w] = j;
         ++w;
@@ -437,12 +457,14 @@ void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, i
 }
 
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     cudaStream_t s) {
+                     const Packed *K, cudaStream_t s) {
     if (P.n == 0) return;
+    const float4 *A = K ? K->A : nullptr, *B = K ? K->B : nullptr;
+    float *rr = K ? K->rr : nullptr;
     if (P.D == 2)
-        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx);
+        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, A, B, rr);
     else
-        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx);
+        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, A, B, rr);
 }
 
 void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,

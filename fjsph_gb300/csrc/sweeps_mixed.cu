@@ -1,0 +1,899 @@
+/*
+ * sweeps_mixed.cu -- the neighbour sweeps of one WCSPH step in the FP32 split-precision form.
+ *
+ * Pair arithmetic runs on the FP32 pipe.  Quantities whose neighbour differences matter keep
+ * about 48 significant bits through a hi/lo split:
+ *   x = xhi + xlo, v = vhi + vlo with xhi = fl32(x), xlo = fl32(x - xhi);
+ *   x_j - x_i = (xhi_j - xhi_i) + (xlo_j - xlo_i): the hi difference is exact for close values
+ *   (Sterbenz) and the lo difference carries the rest, so the separation vector is accurate to
+ *   FP32 rounding of the difference itself, independent of the coordinates' magnitude;
+ *   rho is carried as rho - rho_rest, so density differences are exact to FP32 of the difference.
+ * The squared distance at search time comes from the neighbour search (one float per pair),
+ * which decided membership with the reference's FP64 test.  Density-rate and acceleration sums
+ * are compensated (Kahan).  Results are written to the FP64 state, so integration, the time-step
+ * reduction and global sums stay FP64.
+ *
+ * Packed per-slot inputs (refreshed by k_pack_state whenever x, v, rho, p, m or a flag changes):
+ *   A = (xhi, m/rho)   B = (xlo, p/rho^2)   C = (vhi, rho - rho_rest)   E = (vlo, 0)
+ *   F = (vPert, p)     G = (gradRho, lam)   N = (surface normal, 0)     T = (normal from pass 1)
+ *   bits = b | surf << 3 | surfzone << 4
+ */
+#include "aero.cuh"
+#include "kernels.h"
+#include "linalg.cuh"
+
+namespace fjsph {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+struct Pf { /* float copies of the constants a pair term needs */
+    float H, H_sq, Wc, W_dx, rho0, Bgam, nu, alpha, dsph_cont, max_shift_vel;
+    float grav[3];
+    bool cubic;
+};
+
+__device__ __forceinline__ Pf make_pf(const Params &P) {
+    Pf f;
+    f.H = (float)P.H;
+    f.H_sq = (float)P.H_sq;
+    f.Wc = (float)P.W_correc;
+    f.W_dx = (float)P.W_dx;
+    f.rho0 = (float)P.rho_rest;
+    f.Bgam = (float)(P.B * P.gam);
+    f.nu = (float)P.nu;
+    f.alpha = (float)P.visc_alpha;
+    f.dsph_cont = (float)P.dsph_cont;
+    f.max_shift_vel = (float)P.max_shift_vel;
+    for (int k = 0; k < 3; ++k) f.grav[k] = (float)P.grav[k];
+    f.cubic = has(P, FJSPH_VAR_CUBIC);
+    return f;
+}
+
+/* Kahan-compensated FP32 accumulator */
+struct KSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ int bits_b(int w) { return w & 7; }
+__device__ __forceinline__ int bits_surf(int w) { return (w >> 3) & 1; }
+__device__ __forceinline__ int bits_zone(int w) { return (w >> 4) & 1; }
+
+/* separation x_j - x_i from the hi/lo split */
+template <int D>
+__device__ __forceinline__ void sep(const float4 &Ai, const float4 &Bi, const float4 &Aj, const float4 &Bj, float *R) {
+    R[0] = (Aj.x - Ai.x) + (Bj.x - Bi.x);
+    R[1] = (Aj.y - Ai.y) + (Bj.y - Bi.y);
+    if (D == 3) R[2] = (Aj.z - Ai.z) + (Bj.z - Bi.z);
+}
+
+template <int D>
+__device__ __forceinline__ float fdot(const float *a, const float *b) {
+    float r = a[0] * b[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) r += a[k] * b[k];
+    return r;
+}
+
+template <int D>
+__device__ __forceinline__ void fnormalized(const float *a, float *o) {
+    const float z = fdot<D>(a, a);
+    if (z > 0.f) {
+        const float n = sqrtf(z);
+#pragma unroll
+        for (int k = 0; k < D; ++k) o[k] = a[k] / n;
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) o[k] = a[k];
+    }
+}
+
+__device__ __forceinline__ float f_kernel(const Pf &f, float r) { return kernel_w<float>(r, f.H, f.Wc, f.cubic); }
+__device__ __forceinline__ float f_gscale(const Pf &f, float r) { return gradk_scale<float>(r, f.H, f.Wc, f.cubic); }
+
+/* ------------------------------------------------------------------------------------------ */
+/* packing                                                                                       */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void k_pack_state(Params P, DevState W, Packed K, int64_t i0, int64_t i1, int full) {
+    const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= i1) return;
+    float xh[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0}, vp[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double x = W.x[k][i], v = W.v[k][i];
+        xh[k] = (float)x;
+        xl[k] = (float)(x - (double)xh[k]);
+        vh[k] = (float)v;
+        vl[k] = (float)(v - (double)vh[k]);
+        vp[k] = (float)W.vPert[k][i];
+    }
+    const double rho = W.rho[i], p = W.p[i];
+    K.A[i] = make_float4(xh[0], xh[1], xh[2], (float)(W.m[i] / rho));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], (float)(p / (rho * rho)));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
+    K.E[i] = make_float4(vl[0], vl[1], vl[2], 0.f);
+    K.F[i] = make_float4(vp[0], vp[1], vp[2], (float)p);
+    K.bits[i] = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
+    if (full) {
+        float g[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            g[k] = (float)W.gradRho[k][i];
+            n[k] = (float)W.norm[k][i];
+        }
+        K.G[i] = make_float4(g[0], g[1], g[2], (float)W.lam[i]);
+        K.N[i] = make_float4(n[0], n[1], n[2], (float)W.lam_nb[i]);
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* npd alone                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_npd(Params P, DevNbr N, Packed K, double *npd_part) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Pf f = make_pf(P);
+    float npd = 0.f;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i || bits_b(K.bits[j]) <= FJSPH_PISTON) continue;
+        npd += f_kernel(f, sqrtf(K.rr[e]));
+    }
+    npd_part[i] = npd;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* dSPH_PreStep (src/Shifting.cpp:12-123)                                                        */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNbr N, Packed K, double *npd_part) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Pf f = make_pf(P);
+    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float drho_i = K.C[i].w;
+    float Lm[D * D], Lnb[D * D], gR[D], nr[D];
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) {
+        Lm[k] = 0.f;
+        Lnb[k] = 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        gR[k] = 0.f;
+        nr[k] = 0.f;
+    }
+    float kernsum = 0.f, colour = 0.f, npd = 0.f;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) {
+            kernsum += f.Wc;
+            continue;
+        }
+        const float4 Aj = K.A[j], Bj = K.B[j];
+        float Rji[D];
+        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        const float r = sqrtf(K.rr[e]);
+        const float volj = Aj.w;
+        const float kern = f_kernel(f, r);
+        const float gs = f_gscale(f, r);
+        const bool fl = bits_b(K.bits[j]) > FJSPH_PISTON;
+        const float drho = volj * (K.C[j].w - drho_i);
+        /* Lm -= volj Rji (x) Grad with Grad = -Rji gs */
+        const float w = volj * gs;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const float t = w * Rji[a] * Rji[c];
+                Lm[a * D + c] += t;
+                if (fl) Lnb[a * D + c] += t;
+            }
+            gR[a] -= drho * gs * Rji[a];
+        }
+        if (fl) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) nr[k] -= w * Rji[k];
+            kernsum += kern;
+            colour += volj * kern;
+            npd += kern;
+        }
+    }
+    float Linv[D * D];
+    if (!qr_inverse<D, float>(Lm, Linv)) {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int c = 0; c < D; ++c) Linv[a * D + c] = (a == c) ? 1.f : 0.f;
+    }
+    float g[D], n[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        float sg = 0.f, sn = 0.f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            sg += Linv[a * D + c] * gR[c];
+            sn += Linv[a * D + c] * nr[c];
+        }
+        g[a] = sg;
+        n[a] = sn;
+        W.gradRho[a][i] = sg;
+        W.norm[a][i] = sn;
+    }
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) W.L[k][i] = Linv[k];
+    float lam, lam_nb;
+    if (W.b[i] == FJSPH_BOUND) {
+        lam = 1.f;
+        lam_nb = 1.f;
+    } else {
+        lam = min_eig<D, float>(Lm);
+        lam_nb = min_eig<D, float>(Lnb);
+    }
+    W.lam[i] = lam;
+    W.lam_nb[i] = lam_nb;
+    W.colourG[i] = (lam > 0.7f) ? 2.0 : 2.0 * fmax(1.0, 1.0 / (2.0 * (double)colour));
+    W.kernsum[i] = kernsum;
+    W.colour[i] = colour;
+    npd_part[i] = npd;
+    K.G[i] = make_float4(g[0], g[1], D == 3 ? g[2] : 0.f, lam);
+    K.N[i] = make_float4(n[0], n[1], D == 3 ? n[2] : 0.f, lam_nb);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Detect_Surface (src/Geometry.cpp:14-280)                                                      */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevState W, DevNbr N, Packed K) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Pf f = make_pf(P);
+    const float h = (float)(1.33 * P.particle_step);
+    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float4 Ni = K.N[i]; /* dSPH normal, lam_nb */
+    float ni[D], nh[D];
+    ni[0] = Ni.x;
+    ni[1] = Ni.y;
+    if (D == 3) ni[2] = Ni.z;
+    fnormalized<D>(ni, nh);
+    const int b = W.b[i];
+    const float lam_nb = (float)W.lam_nb[i], lam = K.G[i].w;
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    int surf = W.surf[i];
+    if (b < FJSPH_PIPE) {
+        surf = 0;
+        W.woccl[i] = 1.0;
+    } else if (lam_nb < 0.2f) {
+        surf = 1;
+    } else if (lam_nb < 0.75f) {
+        /* x_j - pointT = (x_j - x_i) - h n_hat */
+        float th[D];
+        if (D == 2) {
+            float tau[D];
+            tau[0] = ni[1];
+            tau[1] = -ni[0];
+            fnormalized<D>(tau, th);
+        }
+        surf = 1;
+        const float sq2h = sqrtf(2.f) * h;
+        for (int64_t e = e0; e < e1; ++e) {
+            const int32_t j = N.idx[e];
+            if (j == i) continue;
+            float Rji[D], xT[D];
+            sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
+#pragma unroll
+            for (int k = 0; k < D; ++k) xT[k] = Rji[k] - h * nh[k];
+            const float r = sqrtf(K.rr[e]);
+            if (r >= sq2h) {
+                if (sqrtf(fdot<D>(xT, xT)) < h) {
+                    surf = 0;
+                    break;
+                }
+            } else if (D == 2) {
+                if (fabsf(fdot<D>(nh, xT)) + fabsf(fdot<D>(th, xT)) < h) {
+                    surf = 0;
+                    break;
+                }
+            } else {
+                float u[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) u[k] = Rji[k] / r;
+                if (acosf(fdot<D>(nh, u)) < (float)(kPi / 4.0)) {
+                    surf = 0;
+                    break;
+                }
+            }
+        }
+    } else {
+        surf = 0;
+    }
+    W.surf[i] = surf;
+    K.bits[i] = (K.bits[i] & ~8) | (surf << 3);
+    float nrm[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) nrm[k] = 0.f;
+    const bool inside = lam > 0.7f;
+    for (int64_t e = e0; e < e1; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) continue;
+        float Rji[D];
+        sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
+        const float r = sqrtf(K.rr[e]);
+        const float volj = K.A[j].w;
+        const float gs = f_gscale(f, r);
+        const float lj = K.G[j].w;
+        const float w = inside ? volj * (lj - lam) : volj * lj;
+        /* GradK(Rij) with Rij = x_i - x_j = -Rji */
+#pragma unroll
+        for (int k = 0; k < D; ++k) nrm[k] -= w * (Rji[k] * gs);
+    }
+    float n2[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        float s = 0.f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) s += (float)W.L[a * D + c][i] * nrm[c];
+        n2[a] = s;
+    }
+    float out[D];
+    if (sqrtf(fdot<D>(n2, n2)) > 0.1f * lam / f.H) {
+        fnormalized<D>(n2, out);
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = 0.f;
+    }
+    K.T[i] = make_float4(out[0], out[1], D == 3 ? out[2] : 0.f, 0.f);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevState W, DevNbr N, Packed K) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Pf f = make_pf(P);
+    const bool gissler = P.acase == FJSPH_GISSLER;
+    const int b = W.b[i];
+    const float4 Ai = K.A[i], Bi = K.B[i], Ti = K.T[i];
+    const float4 Ci = K.C[i], Ei = K.E[i];
+    float ni[D], Vdiff[D];
+    ni[0] = Ti.x;
+    ni[1] = Ti.y;
+    if (D == 3) ni[2] = Ti.z;
+    const bool occl = (b == FJSPH_FREE) && gissler;
+    const bool vd_on = occl && W.cellID[i] != -1;
+    Vdiff[0] = vd_on ? (float)(P.v_inf[0] - W.v[0][i]) : 0.f;
+    Vdiff[1] = vd_on ? (float)(P.v_inf[1] - W.v[1][i]) : 0.f;
+    if (D == 3) Vdiff[2] = vd_on ? (float)(P.v_inf[2] - W.v[2][i]) : 0.f;
+    (void)Ci;
+    (void)Ei;
+    float Li[D * D];
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) Li[k] = (float)W.L[k][i];
+    const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
+    float curve = 0.f, woccl_ = 0.f;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) continue;
+        float Rij[D]; /* = x_j - x_i, the reference's naming in this loop */
+        sep<D>(Ai, Bi, K.A[j], K.B[j], Rij);
+        const float r = sqrtf(K.rr[e]);
+        const float4 Tj = K.T[j];
+        float nj[D];
+        nj[0] = Tj.x;
+        nj[1] = Tj.y;
+        if (D == 3) nj[2] = Tj.z;
+        if (nin > 0.f && fdot<D>(nj, nj) > 0.f) {
+            const float volj = K.A[j].w;
+            const float gs = f_gscale(f, r);
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                float Ld = 0.f;
+#pragma unroll
+                for (int c = 0; c < D; ++c) Ld += Li[a * D + c] * (nj[c] - ni[c]);
+                s += Ld * (Rij[a] * gs);
+            }
+            curve += volj * s;
+        }
+        if (occl) {
+            const float frac = -fdot<D>(Rij, Vdiff) / (vdn * r);
+            if (frac > woccl_) woccl_ = frac;
+        }
+    }
+    W.woccl[i] = ((float)W.lam_nb[i] < (float)P.lam_cutoff) ? fmaxf(0.f, fminf(woccl_, 1.f)) : 1.0f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.norm[k][i] = ni[k];
+    W.curve[i] = curve;
+    W.norm_curve[i] = P.dx * (double)curve;
+    W.pDist[i] = W.lam[i];
+    K.N[i] = make_float4(ni[0], ni[1], D == 3 ? ni[2] : 0.f, (float)W.lam_nb[i]);
+}
+
+__global__ void k_m_surface_zone(Params P, DevState W, DevNbr N, Packed K) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    int sz = 0;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e)
+        if (bits_surf(K.bits[N.idx[e]])) {
+            sz = 1;
+            break;
+        }
+    W.surfzone[i] = sz;
+    atomicAnd(&K.bits[i], ~16);
+    if (sz) atomicOr(&K.bits[i], 16);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* artificial viscosity scalar (src/Kernel.h:217-244)                                           */
+/* ------------------------------------------------------------------------------------------ */
+__device__ __forceinline__ float f_art_visc(const Pf &f, float vdotr, float idist2, float rho_i, float rho_j) {
+    if (vdotr > 0.f) return 0.f;
+    const float muij = f.H * vdotr * idist2;
+    const float rhoij = 0.5f * (rho_i + rho_j);
+    const float cbar = 0.5f * (sqrtf(f.Bgam / rho_i) + sqrtf(f.Bgam / rho_j));
+    return f.alpha * cbar * muij / rhoij;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* dissipation_terms (src/Shifting.cpp:126-186)                                                  */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_dissipation(Params P, DevState W, DevNbr N, Packed K) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Pf f = make_pf(P);
+    const bool linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH);
+    const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Gi = K.G[i];
+    const float rho_i = f.rho0 + Ci.w;
+    float gRi[D];
+    gRi[0] = Gi.x;
+    gRi[1] = Gi.y;
+    if (D == 3) gRi[2] = Gi.z;
+    float av[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) av[k] = 0.f;
+    KSum Rrhod;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) continue;
+        const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
+        float Rji[D], Vji[D];
+        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        sep<D>(Ci, Ei, Cj, Ej, Vji);
+        const float rr = K.rr[e];
+        const float r = sqrtf(rr);
+        const float idist2 = 1.f / (rr + 0.0001f * f.H_sq);
+        const float volj = Aj.w;
+        const float rho_j = f.rho0 + Cj.w;
+        const float gs = f_gscale(f, r);
+        float g[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
+        const bool fl = bits_b(K.bits[j]) > FJSPH_PISTON;
+        if (fl) {
+            const float vdotr = fdot<D>(Vji, Rji);
+            const float c = linear ? volj * idist2 * vdotr : (volj * rho_j) * f_art_visc(f, vdotr, idist2, rho_i, rho_j);
+#pragma unroll
+            for (int k = 0; k < D; ++k) av[k] += c * g[k];
+        }
+        if (!nodsph) {
+            const float rg = fdot<D>(Rji, g);
+            float t = Cj.w - Ci.w;
+            if (fl) {
+                const float4 Gj = K.G[j];
+                float gsum[D];
+                gsum[0] = gRi[0] + Gj.x;
+                gsum[1] = gRi[1] + Gj.y;
+                if (D == 3) gsum[2] = gRi[2] + Gj.z;
+                t += 0.5f * fdot<D>(gsum, Rji);
+            }
+            Rrhod.add(volj * t * rg * idist2);
+        }
+    }
+    if (linear) {
+        const float c = (float)(P.visc_alpha * P.H * P.speed_sound * P.rho_rest) / rho_i;
+#pragma unroll
+        for (int k = 0; k < D; ++k) av[k] *= c;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.aVisc[k][i] = av[k];
+    if (!nodsph) W.deltaD[i] = P.dsph_cont * Rrhod.value();
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* particle_shift (src/Shifting.cpp:189-290, -DALE)                                              */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_particle_shift(Params P, DevState W, DevNbr N, Packed K) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float lam_nb = (float)W.lam_nb[i];
+    if (lam_nb < 0.55f || W.b[i] == FJSPH_BUFFER) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) W.vPert[k][i] = 0.0;
+        K.F[i] = make_float4(0.f, 0.f, 0.f, K.F[i].w);
+        return;
+    }
+    const Pf f = make_pf(P);
+    const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Ni = K.N[i];
+    float ni[D], nh[D], vi[D];
+    ni[0] = Ni.x;
+    ni[1] = Ni.y;
+    if (D == 3) ni[2] = Ni.z;
+    fnormalized<D>(ni, nh);
+    vi[0] = Ci.x + Ei.x;
+    vi[1] = Ci.y + Ei.y;
+    if (D == 3) vi[2] = Ci.z + Ei.z;
+    float dU[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) dU[k] = 0.f;
+    float maxUij = 0.f, woccl = 0.f;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) continue;
+        float Rji[D], dv[D];
+        sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
+        sep<D>(Ci, Ei, K.C[j], K.E[j], dv);
+        const float r = sqrtf(K.rr[e]);
+        const float volj = K.A[j].w;
+        const float kern = f_kernel(f, r);
+        const float gs = f_gscale(f, r);
+        const float q = kern / f.W_dx;
+        const float q2 = q * q;
+        const float c = (1.f + 0.2f * (q2 * q2)) * volj * gs;
+#pragma unroll
+        for (int k = 0; k < D; ++k) dU[k] += c * Rji[k];
+        if (bits_b(K.bits[j]) > FJSPH_PISTON) {
+            const float4 Nj = K.N[j];
+            float nj[D], njh[D];
+            nj[0] = Nj.x;
+            nj[1] = Nj.y;
+            if (D == 3) nj[2] = Nj.z;
+            fnormalized<D>(nj, njh);
+            const float theta = acosf(fdot<D>(nh, njh));
+            if (theta > woccl) woccl = theta;
+        }
+        const float dvn = sqrtf(fdot<D>(dv, dv));
+        if (dvn > maxUij) maxUij = dvn;
+    }
+    const float sc = -2.f * f.H * sqrtf(fdot<D>(vi, vi));
+#pragma unroll
+    for (int k = 0; k < D; ++k) dU[k] *= sc;
+    const float mag = fminf(sqrtf(fdot<D>(dU, dU)), fminf(maxUij / 2.f, f.max_shift_vel));
+    float dUn[D];
+    fnormalized<D>(dU, dUn);
+#pragma unroll
+    for (int k = 0; k < D; ++k) dU[k] = mag * dUn[k];
+    float out[D];
+    if (W.surfzone[i] == 0 && lam_nb > 0.55f) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = dU[k];
+    } else if (woccl < (float)(kPi / 12.0)) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            float s = 0.f;
+#pragma unroll
+            for (int c = 0; c < D; ++c) s += ((a == c ? 1.f : 0.f) - nh[a] * nh[c]) * dU[c];
+            out[a] = s;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.vPert[k][i] = out[k];
+    K.F[i] = make_float4(out[0], out[1], D == 3 ? out[2] : 0.f, K.F[i].w);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* boundary passes (src/Resid.cpp:21-186)                                                        */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_bound_pressure(Params P, DevState W, DevNbr N, Packed K) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    if (P.blocks[W.blk[i]].bound_solver != FJSPH_PRESSURE_G) return;
+    const Pf f = make_pf(P);
+    const float4 Ai = K.A[i], Bi = K.B[i];
+    int near = 0;
+    KSum kernsum, pkern;
+    float acck[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) acck[k] = 0.f;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        const int bj = K.bits[j];
+        if (bits_b(bj) <= FJSPH_PISTON) continue;
+        const float4 Aj = K.A[j], Bj = K.B[j];
+        float Rji[D];
+        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        const float r = sqrtf(K.rr[e]);
+        const float rho_j = f.rho0 + K.C[j].w;
+        const float kern = Aj.w * f_kernel(f, r);
+        kernsum.add(kern);
+        pkern.add(K.F[j].w * kern);
+        /* (x_i - x_j) = -Rji */
+#pragma unroll
+        for (int k = 0; k < D; ++k) acck[k] -= kern * rho_j * Rji[k];
+        if (bits_zone(bj)) near = 1;
+    }
+    double p = 0.0;
+    const double ks = kernsum.value();
+    if (ks > 0.0) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) s += (P.grav[k] - W.acc[k][i]) * (double)acck[k];
+        p = (pkern.value() + s) / ks;
+        if (near) p = fmax(0.0, p);
+    }
+    W.p[i] = p;
+    W.rho[i] = eos_density(P, p);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W, DevNbr N, Packed K,
+                                                              int32_t *near_inlet) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    if (P.blocks[W.blk[i]].bound_solver != FJSPH_GHOST) return;
+    const Pf f = make_pf(P);
+    const float4 Ai = K.A[i], Bi = K.B[i];
+    /* boundary velocity: set this stage, read from the FP64 state */
+    float vi[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) vi[k] = (float)W.v[k][i];
+    KSum Rr;
+    int ni = 1;
+    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) continue;
+        const int bj = bits_b(K.bits[j]);
+        if (bj == FJSPH_PIPE || bj == FJSPH_FREE) ni = 0;
+        float Rji[D];
+        sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
+        const float r = sqrtf(K.rr[e]);
+        const float gs = f_gscale(f, r);
+        const float4 Cj = K.C[j], Ej = K.E[j];
+        float s = 0.f;
+        s += ((Cj.x + Ej.x) - vi[0]) * Rji[0];
+        s += ((Cj.y + Ej.y) - vi[1]) * Rji[1];
+        if (D == 3) s += ((Cj.z + Ej.z) - vi[2]) * Rji[2];
+        Rr.add(-K.A[j].w * s * gs);
+    }
+    near_inlet[i] = ni;
+    W.Rrho[i] = Rr.value() * W.rho[i];
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* residual (src/Resid.cpp:243-469)                                                               */
+/* ------------------------------------------------------------------------------------------ */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Pf f = make_pf(P);
+    const bool ale = has(P, FJSPH_VAR_ALE), linear = has(P, FJSPH_VAR_LINEAR), nofrozen = has(P, FJSPH_VAR_NOFROZEN),
+               nodsph = has(P, FJSPH_VAR_NODSPH), tic = has(P, FJSPH_VAR_TIC);
+    const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE, csf = P.st_model == FJSPH_ST_CSF;
+    float npdm2 = 0.f;
+    if (pairwise) {
+        const double npd = *npd_dev;
+        const double H2 = 2.0 * P.H;
+        const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (kPi * kPi * kPi * kPi) *
+                            (9.0 / 4.0 * (kPi * kPi * kPi) - 6.0 * kPi - 4.0));
+        npdm2 = (float)((0.5 * P.sig / lam) / (npd * npd));
+    }
+    const float pi3o4_H = (float)(3.0 * kPi / 4.0 / P.H);
+    const float fac_bound = (float)(1.0 + 0.5 * cos(0.5 * kPi * 7.0 / 9.0));
+    const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Fi = K.F[i];
+    const float rho_i = f.rho0 + Ci.w;
+    const float m_i = Ai.w * rho_i;
+    const float pr_i0 = Bi.w;
+    const int bits_i = K.bits[i];
+    const int b_i = bits_b(bits_i), sz_i = bits_zone(bits_i);
+    const float pr_i = (tic && sz_i != 1) ? fabsf(pr_i0) : pr_i0;
+    const float p_i = (tic && sz_i != 1) ? fabsf(Fi.w) : Fi.w;
+    float vPi[D], gRi[D];
+    vPi[0] = Fi.x;
+    vPi[1] = Fi.y;
+    if (D == 3) vPi[2] = Fi.z;
+    if (nofrozen) {
+        const float4 Gi = K.G[i];
+        gRi[0] = Gi.x;
+        gRi[1] = Gi.y;
+        if (D == 3) gRi[2] = Gi.z;
+    }
+    float vi[D];
+    vi[0] = Ci.x + Ei.x;
+    vi[1] = Ci.y + Ei.y;
+    if (D == 3) vi[2] = Ci.z + Ei.z;
+    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    KSum acc[D];
+    float acc_ale[D], visc[D], st[D], art[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        acc_ale[k] = 0.f;
+        visc[k] = 0.f;
+        st[k] = 0.f;
+        art[k] = 0.f;
+    }
+    KSum Rrho, Rrhoc, Rrho_d;
+    double aero[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) aero[k] = 0.0;
+    const bool aero_on = W.cellID[i] != -1;
+    if (aero_on) {
+        double Vd[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Vd[k] = W.cellV[k][i] - W.v[k][i];
+        aero_acc<D>(P, W, i, Vd, W.lam_nb[i], double(e1 - e0), aero);
+    }
+    const bool st_on = pairwise && (!ale || sz_i == 1);
+    for (int64_t e = e0; e < e1; ++e) {
+        const int32_t j = N.idx[e];
+        if (j == i) continue;
+        const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
+        float Rji[D], Vji[D];
+        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        sep<D>(Ci, Ei, Cj, Ej, Vji);
+        const float rr = K.rr[e];
+        const float r = sqrtf(rr);
+        const float idist2 = 1.f / (rr + 0.001f * f.H_sq);
+        const float volj = Aj.w;
+        const float rho_j = f.rho0 + Cj.w;
+        const float m_j = volj * rho_j;
+        const int b_j = bits_b(K.bits[j]);
+        const float gs = f_gscale(f, r);
+        float g[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
+        float pc;
+        if (linear)
+            pc = (p_i + K.F[j].w) * volj;
+        else
+            pc = m_j * (pr_i + Bj.w);
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k].add(-pc * g[k]);
+        const float rg = fdot<D>(Rji, g);
+        const float vc = m_j * (f.nu * (rho_i + rho_j) / (rho_i * rho_j) * rg * idist2);
+#pragma unroll
+        for (int k = 0; k < D; ++k) visc[k] += vc * Vji[k];
+        if (st_on) {
+            const float fac = (b_i == FJSPH_BOUND || b_j == FJSPH_BOUND) ? fac_bound : 1.f;
+            const float c = -npdm2 * fac * cosf(pi3o4_H * r) / r;
+#pragma unroll
+            for (int k = 0; k < D; ++k) st[k] += c * Rji[k];
+        }
+        if (ale) {
+            const float4 Fj = K.F[j];
+            float vPj[D], vj[D];
+            vPj[0] = Fj.x;
+            vPj[1] = Fj.y;
+            if (D == 3) vPj[2] = Fj.z;
+            vj[0] = Cj.x + Ej.x;
+            vj[1] = Cj.y + Ej.y;
+            if (D == 3) vj[2] = Cj.z + Ej.z;
+            const float gj = fdot<D>(vPj, g), gi = fdot<D>(vPi, g);
+            float q = 0.f, w1 = 0.f, w2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                q += (vPj[k] - vPi[k]) * g[k];
+                w1 += (Vji[k] + (vPj[k] - vPi[k])) * g[k];
+                w2 += (rho_j * vPj[k] + rho_i * vPi[k]) * g[k];
+            }
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc_ale[a] += (vj[a] * gj + vi[a] * gi - vi[a] * q) * volj;
+            Rrho.add(-w1 * volj);
+            Rrhoc.add(w2 * volj);
+        } else {
+            Rrho.add(-volj * fdot<D>(Vji, g));
+        }
+        if (nofrozen) {
+            if (b_j > FJSPH_PISTON) {
+                if (!nodsph) {
+                    const float4 Gj = K.G[j];
+                    float gsum[D];
+                    gsum[0] = gRi[0] + Gj.x;
+                    gsum[1] = gRi[1] + Gj.y;
+                    if (D == 3) gsum[2] = gRi[2] + Gj.z;
+                    Rrho_d.add(volj * ((Cj.w - Ci.w) + 0.5f * fdot<D>(gsum, Rji)) * rg * idist2);
+                }
+                const float vdotr = fdot<D>(Vji, Rji);
+                const float c = m_j * f_art_visc(f, vdotr, idist2, rho_i, rho_j);
+#pragma unroll
+                for (int k = 0; k < D; ++k) art[k] += c * g[k];
+            } else if (!nodsph) {
+                Rrho_d.add(volj * (Cj.w - Ci.w) * rg * idist2);
+            }
+        }
+    }
+    double accd[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        accd[k] = aero[k] + acc[k].value();
+        if (linear) accd[k] /= (double)rho_i;
+    }
+    if (csf) {
+        const double c = 1.0 / W.rho[i] * P.sig * W.curve[i] * W.colourG[i];
+#pragma unroll
+        for (int k = 0; k < D; ++k) accd[k] += c * W.norm[k][i];
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double av = nofrozen ? (double)art[k] : W.aVisc[k][i];
+        double t = accd[k];
+        if (ale) t += acc_ale[k];
+        W.acc[k][i] = t + av + visc[k] + (double)st[k] / (double)m_i + P.grav[k];
+        if (aero_on) W.Af[k][i] = aero[k];
+    }
+    double R = Rrho.value() * (double)rho_i;
+    if (ale) R += Rrhoc.value();
+    if (!nodsph) R += nofrozen ? P.dsph_cont * Rrho_d.value() : W.deltaD[i];
+    W.Rrho[i] = R;
+}
+
+inline unsigned fgrid(const Params &P) { return grid_for(P.n - P.nb, kThreads); }
+inline unsigned bgrid(const Params &P) { return grid_for(P.nb, kThreads); }
+inline unsigned agrid(const Params &P) { return grid_for(P.n, kThreads); }
+
+} // namespace
+
+#define FJSPH_DISPATCH_M(P, KERNEL, GRID, ...)                                             \
+    do {                                                                                   \
+        if ((GRID) == 0) break;                                                            \
+        if ((P).D == 2)                                                                    \
+            KERNEL<2><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                            \
+        else                                                                               \
+            KERNEL<3><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                            \
+    } while (0)
+
+void launch_m_pack(const Params &P, const DevState &W, const Packed &K, int64_t i0, int64_t i1, int full,
+                   cudaStream_t s) {
+    if (i1 <= i0) return;
+    const unsigned g = grid_for(i1 - i0, 256);
+    if (P.D == 2)
+        k_pack_state<2><<<g, 256, 0, s>>>(P, W, K, i0, i1, full);
+    else
+        k_pack_state<3><<<g, 256, 0, s>>>(P, W, K, i0, i1, full);
+}
+void launch_m_npd(const Params &P, const DevNbr &N, const Packed &K, double *npd_part, cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_npd, agrid(P), P, N, K, npd_part);
+}
+void launch_m_dsph(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, double *npd_part,
+                   cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_dsph, agrid(P), P, W, N, K, npd_part);
+}
+void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_surface_normal, fgrid(P), P, W, N, K);
+    FJSPH_DISPATCH_M(P, k_m_surface_curvature, fgrid(P), P, W, N, K);
+    if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fgrid(P) > 0)
+        k_m_surface_zone<<<fgrid(P), kThreads, 0, s>>>(P, W, N, K);
+}
+void launch_m_dissipation(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_dissipation, fgrid(P), P, W, N, K);
+}
+void launch_m_particle_shift(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_particle_shift, fgrid(P), P, W, N, K);
+}
+void launch_m_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_bound_pressure, bgrid(P), P, W, N, K);
+}
+void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, int32_t *near_inlet,
+                          cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_bound_ghost, bgrid(P), P, W, N, K, near_inlet);
+}
+void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
+                    cudaStream_t s) {
+    FJSPH_DISPATCH_M(P, k_m_resid, fgrid(P), P, W, N, K, npd_dev);
+}
+
+} // namespace fjsph
