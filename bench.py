@@ -38,7 +38,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000, help="target particle count of the jet")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the plain FP64 form timed beside (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
@@ -176,27 +177,73 @@ def run_ours(args, ws, rank, local):
             "kernel": "k_resid (get_acc_and_Rrho)", "launch_ms": round(per_launch * 1e3, 3),
             "bytes_per_launch": bpp * nf, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
 
-    # end to end through the public API with host buffers: upload both states, one step,
-    # download the new state, every step
+    # end to end through the public API with host buffers in pinned memory: upload both states,
+    # one step, download the new state, every step
     e2e = None
     if args.e2e_steps > 0:
-        host = ctx.download()
-        t0 = time.perf_counter()
+        host = pinned_state(ctx.download())
         ctx.event_record(2)
+        t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             ctx.upload(d.PNP1, host)
             ctx.upload(d.PN, host)
             ctx.integrate()
-            host = ctx.download()
+            download_into(ctx, host)
         ctx.event_record(3)
         e2e_ms = ctx.event_elapsed(2, 3)
         wall = time.perf_counter() - t0
         e2e_ms = reduce_max(ws, max(e2e_ms, wall * 1e3))
         nbytes = state_bytes(host)
         e2e = {"value": nf * args.e2e_steps * ws / (e2e_ms / 1e3), "unit": UNIT,
-               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes}
-    return dict(value=value, ms=ms, nf=nf, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches,
+               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes, "pinned": host._pinned}
+
+    # the plain FP64 form on the same state, same GPU
+    fp64 = None
+    if args.fp64_steps > 0 and s.precision != d.PREC_FP64:
+        s64 = s.copy()
+        s64.precision = d.PREC_FP64
+        c64 = Context(s64, c.state.n + 1024, c.blocks)
+        c64.set_states(c.state, c.state)
+        c64.integrate()
+        c64.event_record(0)
+        for _ in range(args.fp64_steps):
+            c64.integrate()
+        c64.event_record(1)
+        ms64 = reduce_max(ws, c64.event_elapsed(0, 1))
+        fp64 = {"value": nf * args.fp64_steps * ws / (ms64 / 1e3), "ms_per_step": ms64 / args.fp64_steps,
+                "steps": args.fp64_steps}
+        c64.close()
+    return dict(value=value, ms=ms, nf=nf, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches, fp64=fp64,
                 prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s, case=c)
+
+
+def pinned_state(st):
+    """Copy of st whose arrays live in page-locked host memory (torch is used only to allocate)."""
+    from fjsph_gb300.state import ALL_FIELDS
+    out = st.copy()
+    out._pinned = False
+    try:
+        import torch
+        if torch.cuda.is_available():
+            for f in ALL_FIELDS:
+                a = getattr(st, f)
+                t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+                arr = t.numpy()
+                arr[...] = a
+                setattr(out, f, arr)
+                out.__dict__.setdefault("_keep", []).append(t)
+            out._pinned = True
+    except Exception:
+        pass
+    return out
+
+
+def download_into(ctx, st) -> None:
+    import ctypes as C
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300._lib import check
+    v = st.view()
+    check("fjsph_state_download", ctx._lib.fjsph_state_download(ctx._h, d.PNP1, C.byref(v)))
 
 
 def state_bytes(st) -> int:
@@ -301,6 +348,7 @@ def main():
                            "form": args.precision, "integrator": "runge_kutta4",
                            "l2": "inputs larger than L2 (state ~1 GB)", "parallelism": f"replicas{ws}"},
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
+                "fp64_form": r["fp64"],
                 "gpu_launches": r["launches"], "passes_ms": r["prof"]}
         print(json.dumps(line))
     if ws > 1:

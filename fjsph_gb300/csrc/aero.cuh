@@ -21,6 +21,9 @@ __device__ __forceinline__ void aero_acc(const Params &P, const DevState &W, int
     for (int k = 0; k < D; ++k) out[k] = 0.0;
     const double Vn = vnorm<D, double>(Vd);
     if (P.acase == FJSPH_GISSLER) {
+        /* fully occluded (woccl = 1): the exposed area (1 - woccl) * A is exactly zero, so the
+         * force is zero for any finite relative velocity; skip the two pow() of the drag law */
+        if (W.woccl[i] == 1.0 && isfinite(Vn)) return;
         const double Re = 2.0 * W.cellRho[i] * Vn * P.L / P.mu_g;
         const double frac2 = P.use_lam ? fmin(P.interp_fac * lam, 1.0) : fmin(P.interp_fac * nneigh * P.i_n_full, 1.0);
         const double frac1 = 1.0 - frac2;

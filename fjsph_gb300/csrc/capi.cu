@@ -93,6 +93,7 @@ struct fjsph_ctx {
     int32_t *nbr_counts = nullptr;
     int64_t *nbr_off = nullptr;
     int32_t *nbr_idx = nullptr;
+    int2 *nbr_pair = nullptr; /* split-precision form: (slot, r^2) per pair */
     int64_t nbr_cap = 0, n_pairs = 0;
     bool nbr_valid = false;
     int64_t *scan_tmp64 = nullptr;
@@ -101,11 +102,13 @@ struct fjsph_ctx {
     int64_t reorder_tmp_len = 0;
     int64_t searches = 0;
     bool reorder_pending = true;
+    int64_t table_want = 0;
 
     RKScratch S{};
     double *nrm_tmp[3] = {nullptr, nullptr, nullptr};
     double *vtmp[3] = {nullptr, nullptr, nullptr};
     double *npd_part = nullptr;
+    double *stage = nullptr;   /* host-transfer staging, capacity * 9 doubles */
     DevScalars *dsc = nullptr; /* device */
     DevScalars *hsc = nullptr; /* pinned host mirror */
 
@@ -178,6 +181,34 @@ int64_t next_pow2(int64_t v) {
     int64_t p = 1;
     while (p < v) p <<= 1;
     return p;
+}
+
+template <typename T>
+int dfree(fjsph_ctx *c, T *&p) {
+    if (p) {
+        CU(cudaFree(p));
+        c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)p), c->allocs.end());
+        p = nullptr;
+    }
+    return FJSPH_OK;
+}
+
+/* Bucket table of the cell list: while the grid over the particles' bounding box has no more
+ * cells than buckets, the hash is the identity and rows of cells are contiguous. */
+constexpr int64_t kMinTable = (int64_t)1 << 22;
+constexpr int64_t kMaxTable = (int64_t)1 << 26;
+
+int alloc_table(fjsph_ctx *c, int64_t size) {
+    CellGrid &G = c->G;
+    TRY(dfree(c, G.count));
+    TRY(dfree(c, G.start));
+    TRY(dfree(c, G.scan_tmp));
+    G.table_size = size;
+    TRY(dalloc(c, &G.count, G.table_size + 1));
+    TRY(dalloc(c, &G.start, G.table_size + 1));
+    G.scan_tmp_len = std::max<int64_t>(G.table_size / 2048 + 16, 304 * 6 * 2 + 16);
+    TRY(dalloc(c, &G.scan_tmp, G.scan_tmp_len));
+    return FJSPH_OK;
 }
 
 int validate_settings(const fjsph_settings *s) {
@@ -283,7 +314,9 @@ Params make_params(const fjsph_ctx *c) {
 DevNbr make_nbr(const fjsph_ctx *c) {
     DevNbr N;
     N.off = c->nbr_off;
-    N.idx = c->nbr_idx;
+    const bool m = c->s.precision == FJSPH_PREC_MIXED;
+    N.idx = m ? nullptr : c->nbr_idx;
+    N.pair = m ? c->nbr_pair : nullptr;
     for (int k = 0; k < 3; ++k) N.xs[k] = c->xs[k];
     return N;
 }
@@ -296,7 +329,7 @@ int alloc_packed(fjsph_ctx *c) {
     float4 **arrs[] = {&K.A, &K.B, &K.C, &K.E, &K.F, &K.G, &K.N, &K.T};
     for (float4 **a : arrs) TRY(dalloc(c, a, c->cap));
     TRY(dalloc(c, &K.bits, c->cap));
-    TRY(dalloc(c, &K.rr, c->nbr_cap));
+    TRY(dalloc(c, &c->nbr_pair, c->nbr_cap));
     c->packed_alloc = true;
     c->dirty_full = true;
     return FJSPH_OK;
@@ -475,7 +508,8 @@ void dev_ptrs(const DevState &S, int D, std::vector<std::vector<void *>> &ptr, s
     type.push_back(2);
 }
 
-int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, const std::vector<int64_t> &keys, bool up) {
+int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up) {
+    Section sec(c, PASS_TRANSFER);
     std::vector<void *> hp;
     view_ptrs(v, hp);
     std::vector<std::vector<void *>> dp;
@@ -484,25 +518,21 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, const std::ve
     const int64_t n = c->n;
     for (void *p : hp)
         if (!p) return FJSPH_E_ARG;
-    std::vector<char> tmp(sizeof(double) * std::max<int64_t>(n, 1));
     for (size_t f = 0; f < dp.size(); ++f) {
         const int comps = (int)dp[f].size();
-        const size_t es = type[f] == 2 ? 4 : 8;
-        for (int k = 0; k < comps; ++k) {
-            if (up) {
-                for (int64_t s = 0; s < n; ++s) {
-                    const int64_t r = keys[s];
-                    std::memcpy(&tmp[s * es], static_cast<char *>(hp[f]) + (r * comps + k) * es, es);
-                }
-                CU(cudaMemcpy(dp[f][k], tmp.data(), es * n, cudaMemcpyHostToDevice));
-            } else {
-                CU(cudaMemcpy(tmp.data(), dp[f][k], es * n, cudaMemcpyDeviceToHost));
-                for (int64_t s = 0; s < n; ++s) {
-                    const int64_t r = keys[s];
-                    std::memcpy(static_cast<char *>(hp[f]) + (r * comps + k) * es, &tmp[s * es], es);
-                }
-            }
+        const int es = type[f] == 2 ? 4 : 8;
+        const size_t bytes = (size_t)es * comps * n;
+        FieldPtrs fp{};
+        for (int k = 0; k < comps; ++k) fp.p[k] = dp[f][k];
+        if (up) {
+            CU(cudaMemcpyAsync(c->stage, hp[f], bytes, cudaMemcpyHostToDevice, c->stream));
+            launch_field_in(c->stage, comps, es, c->key, fp, n, c->stream);
+        } else {
+            launch_field_out(c->stage, comps, es, c->key, fp, n, c->stream);
+            CU(cudaMemcpyAsync(hp[f], c->stage, bytes, cudaMemcpyDeviceToHost, c->stream));
         }
+        /* the staging buffer is reused by the next field */
+        CU(cudaStreamSynchronize(c->stream));
     }
     return FJSPH_OK;
 }
@@ -538,14 +568,16 @@ int reorder_states(fjsph_ctx *c, const Params &P) {
     }
     for (int k = 0; k < c->D; ++k)
         CU(cudaMemcpyAsync(c->xs[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
-    launch_refresh_xf(P, c->xs, c->G, s);
-    c->launches += 1;
     mark_full(c);
     return FJSPH_OK;
 }
 
 int search(fjsph_ctx *c) {
     if (c->n == 0) return FJSPH_E_STATE;
+    if (c->table_want > c->G.table_size) {
+        TRY(sync(c));
+        TRY(alloc_table(c, c->table_want));
+    }
     if (c->prof.on && c->prof.used > 4096) TRY(profile_collect(c));
     cudaStream_t s = c->stream;
     Params P = make_params(c);
@@ -562,13 +594,22 @@ int search(fjsph_ctx *c) {
         c->reorder_pending = false;
     }
     c->searches++;
+    launch_sorted_pos(P, c->xs, c->G, s);
     launch_nbr_count(P, c->xs, c->G, c->nbr_counts, s);
     launch_scan_i64(c->nbr_counts, c->nbr_off, c->n, c->scan_tmp64, s);
     c->launches += 4;
-    int64_t total = 0;
+    int64_t total = 0, grid[4] = {0, 0, 0, 0};
     CU(cudaMemcpyAsync(&c->hsc->red[15], c->nbr_off + c->n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(&c->hsc->red[10], c->G.grid, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     TRY(sync(c));
     std::memcpy(&total, &c->hsc->red[15], sizeof(int64_t));
+    std::memcpy(grid, &c->hsc->red[10], 4 * sizeof(int64_t));
+    if (grid[3]) {
+        /* the grid outgrew the table: this search used the wrapped (slower) walk; grow the table
+         * for the next one when the grid is of a reasonable size */
+        const double ncells = (double)grid[0] * (double)grid[1] * (double)grid[2];
+        if (ncells <= (double)kMaxTable) c->table_want = next_pow2((int64_t)ncells);
+    }
     if (total > c->nbr_cap) {
         int64_t ncap = std::max<int64_t>(total + total / 4, c->nbr_cap * 2);
         if (ncap >= ((int64_t)1 << 31)) return FJSPH_E_NEIGHBOUR;
@@ -576,17 +617,14 @@ int search(fjsph_ctx *c) {
         c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->nbr_idx), c->allocs.end());
         TRY(dalloc(c, &c->nbr_idx, ncap));
         if (c->packed_alloc) {
-            CU(cudaFree(c->K.rr));
-            c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->K.rr), c->allocs.end());
-            TRY(dalloc(c, &c->K.rr, ncap));
+            CU(cudaFree(c->nbr_pair));
+            c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->nbr_pair), c->allocs.end());
+            TRY(dalloc(c, &c->nbr_pair, ncap));
         }
         c->nbr_cap = ncap;
     }
-    if (mixed(c)) {
-        TRY(alloc_packed(c));
-        ensure_pack(c);
-    }
-    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? &c->K : nullptr, s);
+    if (mixed(c)) TRY(alloc_packed(c));
+    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? c->nbr_pair : nullptr, s);
     c->launches += 1;
     c->n_pairs = total;
     c->nbr_valid = true;
@@ -1105,18 +1143,15 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     c->S.part_len = 16 * 1216;
     A(dalloc(c, &c->S.part, c->S.part_len));
     A(dalloc(c, &c->npd_part, capacity));
+    A(dalloc(c, &c->stage, capacity * 9));
     CellGrid &G = c->G;
-    G.table_size = next_pow2(std::max<int64_t>(2 * capacity, 1024));
     A(dalloc(c, &G.hash, capacity));
-    A(dalloc(c, &G.count, G.table_size + 1));
-    A(dalloc(c, &G.start, G.table_size + 1));
+    A(alloc_table(c, next_pow2(std::max<int64_t>(2 * capacity, kMinTable))));
     A(dalloc(c, &G.sorted, capacity));
-    A(dalloc(c, &G.sorted_xf, capacity));
-    A(dalloc(c, &G.xf, capacity));
+    A(dalloc(c, &G.sorted_hi, capacity));
+    A(dalloc(c, &G.sorted_lo, capacity));
     A(dalloc(c, &G.bbox, 8));
     A(dalloc(c, &G.grid, 4));
-    G.scan_tmp_len = std::max<int64_t>(G.table_size / 2048 + 16, 304 * 6 * 2 + 16);
-    A(dalloc(c, &G.scan_tmp, G.scan_tmp_len));
     A(dalloc(c, &c->nbr_counts, capacity));
     A(dalloc(c, &c->nbr_off, capacity + 1));
     c->scan_tmp64_len = capacity / 2048 + 16;
@@ -1275,10 +1310,8 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         TRY(upload_blk(c, keys));
         TRY(upload_inlets(c, keys));
         c->reorder_pending = true;
-    } else {
-        TRY(download_keys(c, keys));
     }
-    TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, keys, true));
+    TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true));
     if (which == FJSPH_PNP1) {
         c->nbr_valid = false;
         mark_full(c);
@@ -1292,9 +1325,7 @@ int fjsph_state_download(fjsph_ctx *c, int32_t which, fjsph_state_view *st) {
     if (!st || (which != FJSPH_PN && which != FJSPH_PNP1)) return FJSPH_E_ARG;
     if (st->n != c->n) return FJSPH_E_ARG;
     TRY(sync(c));
-    std::vector<int64_t> keys;
-    TRY(download_keys(c, keys));
-    return transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, keys, false);
+    return transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, false);
 }
 
 int fjsph_particle_count(fjsph_ctx *c, int64_t *n_total, int64_t *n_bound) {
@@ -1321,7 +1352,15 @@ int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double
     std::vector<int32_t> id(c->n_pairs);
     std::vector<double> xs(c->D * n);
     CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
-    if (c->n_pairs) CU(cudaMemcpy(id.data(), c->nbr_idx, sizeof(int32_t) * c->n_pairs, cudaMemcpyDeviceToHost));
+    if (c->n_pairs) {
+        if (mixed(c)) {
+            std::vector<int2> pr(c->n_pairs);
+            CU(cudaMemcpy(pr.data(), c->nbr_pair, sizeof(int2) * c->n_pairs, cudaMemcpyDeviceToHost));
+            for (int64_t e = 0; e < c->n_pairs; ++e) id[e] = pr[e].x;
+        } else {
+            CU(cudaMemcpy(id.data(), c->nbr_idx, sizeof(int32_t) * c->n_pairs, cudaMemcpyDeviceToHost));
+        }
+    }
     for (int k = 0; k < c->D; ++k) CU(cudaMemcpy(&xs[k * n], c->xs[k], sizeof(double) * n, cudaMemcpyDeviceToHost));
     std::vector<int64_t> slot_of_ref(n);
     for (int64_t s = 0; s < n; ++s) slot_of_ref[keys[s]] = s;

@@ -66,7 +66,8 @@ struct Params {
  * squared distance of each pair from search time, src/Resid.cpp:288). */
 struct DevNbr {
     const int64_t *off;
-    const int32_t *idx;
+    const int32_t *idx;  /* FP64 form: neighbour slots                                    */
+    const int2 *pair;    /* split-precision form: (slot, FP32 squared distance bits)      */
     const double *xs[3];
 };
 

@@ -12,7 +12,6 @@ namespace fjsph {
 struct Packed {
     float4 *A, *B, *C, *E, *F, *G, *N, *T;
     int32_t *bits;
-    float *rr; /* search-time squared distance per CSR pair */
 };
 
 /* ---- neighbours.cu ------------------------------------------------------------------------ */
@@ -22,8 +21,8 @@ struct CellGrid {
     int32_t *count;          /* [table_size + 1]                              */
     int32_t *start;          /* [table_size + 1] exclusive scan of count      */
     int32_t *sorted;         /* [cap]  slots ordered by bucket                */
-    float4 *sorted_xf;       /* [cap]  float positions in bucket order        */
-    float4 *xf;              /* [cap]  float positions by slot                */
+    float4 *sorted_hi;       /* [cap]  (fl32(x), slot bits) in bucket order   */
+    float4 *sorted_lo;       /* [cap]  fl32(x - hi) in bucket order           */
     double *bbox;            /* [8]    lo[3], hi[3], band, spare (device)     */
     int64_t *grid;           /* [4]    nx, ny, nz, wrap flag (device)         */
     int32_t *scan_tmp;       /* scan partials                                 */
@@ -36,12 +35,11 @@ void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, c
 void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s);
 void launch_scatter_sort(const Params &P, CellGrid &G, cudaStream_t s);
 void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s);
-/* K (may be null): when given, the squared distance of each pair is also written to K->rr, in FP32
- * from the hi/lo split positions in K->A / K->B. */
+/* Writes idx (FP64 form) or, when pair is given, (slot, FP32 squared distance) pairs. */
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     const Packed *K, cudaStream_t s);
-/* Float positions by slot from xs (after a re-ordering moved the slots). */
-void launch_refresh_xf(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s);
+                     int2 *pair, cudaStream_t s);
+/* Bucket-ordered hi/lo coordinates for the neighbour walk (after any re-ordering). */
+void launch_sorted_pos(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s);
 /* Re-ordering: new slot of every old slot, boundary group first, each group in bucket order. */
 void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,
                         cudaStream_t s);
@@ -136,6 +134,15 @@ FieldList state_fields(const DevState &S, int D);
 void launch_permute(const FieldList &src, const FieldList &dst, const int32_t *new_of_old, int64_t n, cudaStream_t s);
 /* dst = src over [0, n) for every field. */
 void launch_copy(const FieldList &src, const FieldList &dst, int64_t n, cudaStream_t s);
+/* Host-layout field transfer through a device staging buffer (reference order, components
+ * interleaved per particle): in = stage -> slot-order arrays, out = the reverse. */
+struct FieldPtrs {
+    void *p[9];
+};
+void launch_field_in(const void *stage, int comps, int elem, const int64_t *key, const FieldPtrs &dst, int64_t n,
+                     cudaStream_t s);
+void launch_field_out(void *stage, int comps, int elem, const int64_t *key, const FieldPtrs &src, int64_t n,
+                      cudaStream_t s);
 /* a[i] = new_of_old[a[i]] */
 void launch_remap_i32(int32_t *a, int64_t n, const int32_t *new_of_old, cudaStream_t s);
 

@@ -11,9 +11,12 @@
  *      in-bucket sort by slot so the order is deterministic);
  *   4. per particle, count and then write its neighbours in CSR form.
  * Membership is the reference's test, d2 < sr with d2 = fma(dz,dz,fma(dy,dy,dx*dx)) in FP64.
- * It is decided first in FP32 on positions relative to the box corner, and in FP64 only when
- * the FP32 value falls inside a band whose width bounds the FP32 rounding error; so the lists are
- * exactly the FP64 ones while the bulk of the candidate tests run on the FP32 pipe.
+ * It is decided first in FP32 on the rounded coordinates, and in FP64 only when the FP32 value
+ * falls inside a band whose width bounds the FP32 rounding error; so the lists are exactly the
+ * FP64 ones while the bulk of the candidate tests run on the FP32 pipe.  Candidates are read from
+ * bucket-ordered copies of the coordinates (hi = fl32(x), lo = fl32(x - hi)), so a thread's walk
+ * over a row of cells is a contiguous read; the lo part gives members an FP32 squared distance
+ * accurate to FP32 rounding of the separation (used by the split-precision form).
  */
 #include "kernels.h"
 
@@ -57,20 +60,27 @@ __global__ void k_bbox_part(Params P, DevState W, double *part) {
 }
 
 __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bbox, int64_t *grid, int64_t table) {
-    if (threadIdx.x != 0) return;
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int k = 0; k < 3; ++k) {
-        lo[k] = INFINITY;
-        hi[k] = -INFINITY;
-    }
-    for (int b = 0; b < nblk; ++b)
+    __shared__ double sh[6][32];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = threadIdx.x; b < nblk; b += 32)
         for (int k = 0; k < 3; ++k) {
             lo[k] = fmin(lo[k], part[b * 6 + k]);
             hi[k] = fmax(hi[k], part[b * 6 + 3 + k]);
         }
+    for (int k = 0; k < 3; ++k) {
+        sh[k][threadIdx.x] = lo[k];
+        sh[3 + k][threadIdx.x] = hi[k];
+    }
+    __syncwarp();
+    if (threadIdx.x != 0) return;
+    for (int t = 1; t < 32; ++t)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fmin(lo[k], sh[k][t]);
+            hi[k] = fmax(hi[k], sh[3 + k][t]);
+        }
     const double cs = cell_edge(P);
     int64_t nc[3] = {1, 1, 1};
-    double ext = 0.0;
+    double mag = 0.0;
     for (int k = 0; k < P.D; ++k) {
         if (!(lo[k] <= hi[k])) { /* empty or non-finite */
             lo[k] = 0.0;
@@ -79,18 +89,18 @@ __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bb
         double c = floor((hi[k] - lo[k]) / cs) + 1.0;
         if (!(c < (double)kMaxAxis)) c = (double)kMaxAxis;
         nc[k] = (int64_t)c;
-        ext = fmax(ext, hi[k] - lo[k]);
+        mag = fmax(mag, fmax(fabs(lo[k]), fabs(hi[k])));
     }
     for (int k = 0; k < 3; ++k) {
         bbox[k] = lo[k];
         bbox[3 + k] = hi[k];
     }
-    /* FP32 band.  xf = fl(x - lo) has |err| <= u ext per axis (u = 2^-24), so near the sphere
-     * |d2_f32 - d2| <= D (4 u ext R + 3 u R^2) + 2 u R^2 with R = sqrt(sr); twice that, relative
-     * to sr, is the band inside which the FP64 test decides. */
+    /* FP32 band.  fl32(x) has |err| <= u |x| <= u M per axis (u = 2^-24, M = largest coordinate
+     * magnitude), so near the sphere |d2_f32 - d2| <= D (4 u M R + 3 u R^2) + 2 u R^2 with
+     * R = sqrt(sr); twice that, relative to sr, is the band inside which the FP64 test decides. */
     const double u = 5.9604644775390625e-08;
     const double R = sqrt(P.sr);
-    const double rel = 2.0 * (P.D * 4.0 * u * ext / R + (3.0 * P.D + 2.0) * u) + 1e-7;
+    const double rel = 2.0 * (P.D * 4.0 * u * mag / R + (3.0 * P.D + 2.0) * u) + 1e-7;
     bbox[6] = rel;
     grid[0] = nc[0];
     grid[1] = nc[1];
@@ -138,7 +148,6 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
     cell_coords<D>(P, x, lo, nc, c);
     const uint32_t h = (uint32_t)(lin_index(c, nc) & (uint64_t)(G.table_size - 1));
     G.hash[i] = h;
-    G.xf[i] = make_float4((float)(x[0] - lo[0]), (float)(x[1] - lo[1]), D == 3 ? (float)(x[2] - lo[2]) : 0.0f, 0.0f);
     atomicAdd(&G.count[h], 1);
 }
 
@@ -150,7 +159,7 @@ __global__ void k_scatter(Params P, CellGrid G, int32_t *cursor) {
     G.sorted[pos] = (int32_t)i;
 }
 
-/* Insertion sort of each bucket by slot, then gather the float positions in bucket order. */
+/* Insertion sort of each bucket by slot (deterministic order within a bucket). */
 __global__ void k_bucket_sort(CellGrid G, int64_t nbuckets) {
     const int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (h >= nbuckets) return;
@@ -164,7 +173,17 @@ __global__ void k_bucket_sort(CellGrid G, int64_t nbuckets) {
         }
         G.sorted[b + 1] = v;
     }
-    for (int32_t a = s0; a < s1; ++a) G.sorted_xf[a] = G.xf[G.sorted[a]];
+}
+
+/* Coordinates in bucket order: hi = (fl32(x), slot bits), lo = fl32(x - hi). */
+__global__ void k_sorted_pos(Params P, const double *xs0, const double *xs1, const double *xs2, CellGrid G) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= P.n) return;
+    const int32_t s = G.sorted[e];
+    const double x0 = xs0[s], x1 = xs1[s], x2 = P.D == 3 ? xs2[s] : 0.0;
+    const float h0 = (float)x0, h1 = (float)x1, h2 = (float)x2;
+    G.sorted_hi[e] = make_float4(h0, h1, h2, __int_as_float(s));
+    G.sorted_lo[e] = make_float4((float)(x0 - (double)h0), (float)(x1 - (double)h1), (float)(x2 - (double)h2), 0.f);
 }
 
 /* ---- neighbour walk --------------------------------------------------------------------------- */
@@ -182,7 +201,9 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     for (int k = 0; k < D; ++k) xi[k] = xs[k][i];
     cell_coords<D>(P, xi, lo, nc, c);
     const bool wrap = G.grid[3] != 0;
-    const float4 fi = G.xf[i];
+    float fi[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < D; ++k) fi[k] = (float)xi[k];
     const double band = G.bbox[6];
     const float sr_lo = (float)(P.sr * (1.0 - band)), sr_hi = (float)(P.sr * (1.0 + band));
     const uint64_t mask = (uint64_t)(G.table_size - 1);
@@ -207,14 +228,14 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
         return false;
     };
     auto test = [&](int32_t e) {
-        const int32_t j = G.sorted[e];
-        const float4 fj = G.sorted_xf[e];
-        const float dx = fi.x - fj.x, dy = fi.y - fj.y;
+        const float4 fj = G.sorted_hi[e];
+        const float dx = fi[0] - fj.x, dy = fi[1] - fj.y;
         float d2f = dx * dx + dy * dy;
         if (D == 3) {
-            const float dz = fi.z - fj.z;
+            const float dz = fi[2] - fj.z;
             d2f += dz * dz;
         }
+        const int32_t j = __float_as_int(fj.w);
         bool in;
         if (d2f < sr_lo)
             in = true;
@@ -226,7 +247,7 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
             for (int k = 0; k < D; ++k) xj[k] = xs[k][j];
             in = dist2<D>(xi, xj) < P.sr;
         }
-        if (in) f(j);
+        if (in) f(j, e);
     };
     for (int dz = -zr; dz <= zr; ++dz) {
         const int64_t cz = c[2] + dz;
@@ -260,39 +281,43 @@ __global__ void __launch_bounds__(kThreads) k_nbr_count(Params P, double *xs0, d
     if (i >= P.n) return;
     double *const xs[3] = {xs0, xs1, xs2};
     int32_t cnt = 0;
-    walk<D>(P, xs, G, i, [&](int32_t) { ++cnt; });
+    walk<D>(P, xs, G, i, [&](int32_t, int32_t) { ++cnt; });
     counts[i] = cnt;
 }
 
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, double *xs1, double *xs2, CellGrid G,
-                                                        const int64_t *off, int32_t *idx, const float4 *A,
-                                                        const float4 *B, float *rr) {
+                                                        const int64_t *off, int32_t *idx, int2 *pair) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     double *const xs[3] = {xs0, xs1, xs2};
     int64_t w = off[i];
     const int64_t wend = off[i + 1];
-    if (rr) {
-        /* squared distance in FP32 from the hi/lo split (about 1e-7 relative) */
-        const float4 Ai = A[i], Bi = B[i];
-        walk<D>(P, xs, G, i, [&](int32_t j) {
+    if (pair) {
+        /* (slot, FP32 squared distance from the hi/lo split, about 1e-7 relative) */
+        float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const double x = xs[k][i];
+            hi[k] = (float)x;
+            lo[k] = (float)(x - (double)hi[k]);
+        }
+        walk<D>(P, xs, G, i, [&](int32_t j, int32_t e) {
             if (w < wend) {
-                idx[w] = j;
-                const float4 Aj = A[j], Bj = B[j];
-                const float dx = (Aj.x - Ai.x) + (Bj.x - Bi.x), dy = (Aj.y - Ai.y) + (Bj.y - Bi.y);
+                const float4 hj = G.sorted_hi[e], lj = G.sorted_lo[e];
+                const float dx = (hj.x - hi[0]) + (lj.x - lo[0]), dy = (hj.y - hi[1]) + (lj.y - lo[1]);
                 float d2 = dx * dx + dy * dy;
                 if (D == 3) {
-                    const float dz = (Aj.z - Ai.z) + (Bj.z - Bi.z);
+                    const float dz = (hj.z - hi[2]) + (lj.z - lo[2]);
                     d2 += dz * dz;
                 }
-                rr[w] = d2;
+                pair[w] = make_int2(j, __float_as_int(d2));
             }
             ++w;
         });
         return;
     }
-    walk<D>(P, xs, G, i, [&](int32_t j) {
+    walk<D>(P, xs, G, i, [&](int32_t j, int32_t) {
         if (w < wend) idx[w] = j;
         ++w;
     });
@@ -401,18 +426,11 @@ __global__ void k_reorder_map(Params P, int32_t *sorted, const int32_t *flag, co
     sorted[p] = ns;
 }
 
-__global__ void k_refresh_xf(Params P, const double *xs0, const double *xs1, const double *xs2, CellGrid G) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const double lo0 = G.bbox[0], lo1 = G.bbox[1], lo2 = G.bbox[2];
-    G.xf[i] = make_float4((float)(xs0[i] - lo0), (float)(xs1[i] - lo1), P.D == 3 ? (float)(xs2[i] - lo2) : 0.0f, 0.0f);
-}
-
 } // namespace
 
-void launch_refresh_xf(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s) {
+void launch_sorted_pos(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s) {
     if (P.n == 0) return;
-    k_refresh_xf<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G);
+    k_sorted_pos<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G);
 }
 
 void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s) {
@@ -457,14 +475,12 @@ void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, i
 }
 
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     const Packed *K, cudaStream_t s) {
+                     int2 *pair, cudaStream_t s) {
     if (P.n == 0) return;
-    const float4 *A = K ? K->A : nullptr, *B = K ? K->B : nullptr;
-    float *rr = K ? K->rr : nullptr;
     if (P.D == 2)
-        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, A, B, rr);
+        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair);
     else
-        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, A, B, rr);
+        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair);
 }
 
 void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,

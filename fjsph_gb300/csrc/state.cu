@@ -64,6 +64,48 @@ void launch_copy(const FieldList &src, const FieldList &dst, int64_t n, cudaStre
     k_permute<<<grid_for(n, kThreads), kThreads, 0, s>>>(src, dst, nullptr, n);
 }
 
+namespace {
+
+/* dst_k[s] = stage[key[s] * comps + k]: reference-order, component-interleaved host layout to
+ * slot-order structure of arrays (and the reverse for download). */
+template <typename T>
+__global__ void k_field_in(const T *stage, int comps, const int64_t *key, FieldPtrs dst, int64_t n) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int64_t r = key[s];
+    for (int k = 0; k < comps; ++k) static_cast<T *>(dst.p[k])[s] = stage[r * comps + k];
+}
+
+template <typename T>
+__global__ void k_field_out(T *stage, int comps, const int64_t *key, FieldPtrs src, int64_t n) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int64_t r = key[s];
+    for (int k = 0; k < comps; ++k) stage[r * comps + k] = static_cast<const T *>(src.p[k])[s];
+}
+
+} // namespace
+
+void launch_field_in(const void *stage, int comps, int elem, const int64_t *key, const FieldPtrs &dst, int64_t n,
+                     cudaStream_t s) {
+    if (n == 0) return;
+    const unsigned g = grid_for(n, kThreads);
+    if (elem == 8)
+        k_field_in<int64_t><<<g, kThreads, 0, s>>>(static_cast<const int64_t *>(stage), comps, key, dst, n);
+    else
+        k_field_in<int32_t><<<g, kThreads, 0, s>>>(static_cast<const int32_t *>(stage), comps, key, dst, n);
+}
+
+void launch_field_out(void *stage, int comps, int elem, const int64_t *key, const FieldPtrs &src, int64_t n,
+                      cudaStream_t s) {
+    if (n == 0) return;
+    const unsigned g = grid_for(n, kThreads);
+    if (elem == 8)
+        k_field_out<int64_t><<<g, kThreads, 0, s>>>(static_cast<int64_t *>(stage), comps, key, src, n);
+    else
+        k_field_out<int32_t><<<g, kThreads, 0, s>>>(static_cast<int32_t *>(stage), comps, key, src, n);
+}
+
 void launch_remap_i32(int32_t *a, int64_t n, const int32_t *new_of_old, cudaStream_t s) {
     if (n == 0) return;
     k_remap<<<grid_for(n, kThreads), kThreads, 0, s>>>(a, n, new_of_old);

@@ -536,7 +536,8 @@ __global__ void k_no_slip(Params P, DevState W, DevNbr N, double *vt0, double *v
 #pragma unroll
         for (int k = 0; k < D; ++k) vs[k] = 0.0;
         for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-            const int64_t j = N.idx[e];
+            /* also used by the split-precision form, whose lists hold (slot, r^2) pairs */
+            const int64_t j = N.pair ? N.pair[e].x : N.idx[e];
             if (j == i || W.b[j] <= FJSPH_PISTON) continue;
             const double r = sqrt(pair_rr<D>(N, i, j));
             const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);

@@ -14,7 +14,7 @@
  * reduction and global sums stay FP64.
  *
  * Packed per-slot inputs (refreshed by k_pack_state whenever x, v, rho, p, m or a flag changes):
- *   A = (xhi, m/rho)   B = (xlo, p/rho^2)   C = (vhi, rho - rho_rest)   E = (vlo, 0)
+ *   A = (xhi, m/rho)   B = (xlo, p/rho^2)   C = (vhi, rho - rho_rest)   E = (vlo, bits at packing)
  *   F = (vPert, p)     G = (gradRho, lam)   N = (surface normal, 0)     T = (normal from pass 1)
  *   bits = b | surf << 3 | surfzone << 4
  */
@@ -120,9 +120,10 @@ __global__ void k_pack_state(Params P, DevState W, Packed K, int64_t i0, int64_t
     K.A[i] = make_float4(xh[0], xh[1], xh[2], (float)(W.m[i] / rho));
     K.B[i] = make_float4(xl[0], xl[1], xl[2], (float)(p / (rho * rho)));
     K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
-    K.E[i] = make_float4(vl[0], vl[1], vl[2], 0.f);
+    const int bits = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
+    K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(bits));
     K.F[i] = make_float4(vp[0], vp[1], vp[2], (float)p);
-    K.bits[i] = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
+    K.bits[i] = bits;
     if (full) {
         float g[3] = {0, 0, 0}, n[3] = {0, 0, 0};
 #pragma unroll
@@ -145,9 +146,10 @@ __global__ void __launch_bounds__(kThreads) k_m_npd(Params P, DevNbr N, Packed K
     const Pf f = make_pf(P);
     float npd = 0.f;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i || bits_b(K.bits[j]) <= FJSPH_PISTON) continue;
-        npd += f_kernel(f, sqrtf(K.rr[e]));
+        npd += f_kernel(f, sqrtf(__int_as_float(pe.y)));
     }
     npd_part[i] = npd;
 }
@@ -175,7 +177,8 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
     }
     float kernsum = 0.f, colour = 0.f, npd = 0.f;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) {
             kernsum += f.Wc;
             continue;
@@ -183,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
         const float4 Aj = K.A[j], Bj = K.B[j];
         float Rji[D];
         sep<D>(Ai, Bi, Aj, Bj, Rji);
-        const float r = sqrtf(K.rr[e]);
+        const float r = sqrtf(__int_as_float(pe.y));
         const float volj = Aj.w;
         const float kern = f_kernel(f, r);
         const float gs = f_gscale(f, r);
@@ -287,13 +290,14 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         surf = 1;
         const float sq2h = sqrtf(2.f) * h;
         for (int64_t e = e0; e < e1; ++e) {
-            const int32_t j = N.idx[e];
+            const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
             if (j == i) continue;
             float Rji[D], xT[D];
             sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
 #pragma unroll
             for (int k = 0; k < D; ++k) xT[k] = Rji[k] - h * nh[k];
-            const float r = sqrtf(K.rr[e]);
+            const float r = sqrtf(__int_as_float(pe.y));
             if (r >= sq2h) {
                 if (sqrtf(fdot<D>(xT, xT)) < h) {
                     surf = 0;
@@ -324,11 +328,12 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
     for (int k = 0; k < D; ++k) nrm[k] = 0.f;
     const bool inside = lam > 0.7f;
     for (int64_t e = e0; e < e1; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) continue;
         float Rji[D];
         sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
-        const float r = sqrtf(K.rr[e]);
+        const float r = sqrtf(__int_as_float(pe.y));
         const float volj = K.A[j].w;
         const float gs = f_gscale(f, r);
         const float lj = K.G[j].w;
@@ -381,11 +386,12 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
     float curve = 0.f, woccl_ = 0.f;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) continue;
         float Rij[D]; /* = x_j - x_i, the reference's naming in this loop */
         sep<D>(Ai, Bi, K.A[j], K.B[j], Rij);
-        const float r = sqrtf(K.rr[e]);
+        const float r = sqrtf(__int_as_float(pe.y));
         const float4 Tj = K.T[j];
         float nj[D];
         nj[0] = Tj.x;
@@ -423,7 +429,7 @@ __global__ void k_m_surface_zone(Params P, DevState W, DevNbr N, Packed K) {
     if (i >= P.n) return;
     int sz = 0;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e)
-        if (bits_surf(K.bits[N.idx[e]])) {
+        if (bits_surf(K.bits[N.pair[e].x])) {
             sz = 1;
             break;
         }
@@ -463,13 +469,14 @@ __global__ void __launch_bounds__(kThreads) k_m_dissipation(Params P, DevState W
     for (int k = 0; k < D; ++k) av[k] = 0.f;
     KSum Rrhod;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) continue;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
         float Rji[D], Vji[D];
         sep<D>(Ai, Bi, Aj, Bj, Rji);
         sep<D>(Ci, Ei, Cj, Ej, Vji);
-        const float rr = K.rr[e];
+        const float rr = __int_as_float(pe.y);
         const float r = sqrtf(rr);
         const float idist2 = 1.f / (rr + 0.0001f * f.H_sq);
         const float volj = Aj.w;
@@ -538,12 +545,13 @@ __global__ void __launch_bounds__(kThreads) k_m_particle_shift(Params P, DevStat
     for (int k = 0; k < D; ++k) dU[k] = 0.f;
     float maxUij = 0.f, woccl = 0.f;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) continue;
         float Rji[D], dv[D];
         sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
         sep<D>(Ci, Ei, K.C[j], K.E[j], dv);
-        const float r = sqrtf(K.rr[e]);
+        const float r = sqrtf(__int_as_float(pe.y));
         const float volj = K.A[j].w;
         const float kern = f_kernel(f, r);
         const float gs = f_gscale(f, r);
@@ -610,13 +618,14 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_pressure(Params P, DevStat
 #pragma unroll
     for (int k = 0; k < D; ++k) acck[k] = 0.f;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         const int bj = K.bits[j];
         if (bits_b(bj) <= FJSPH_PISTON) continue;
         const float4 Aj = K.A[j], Bj = K.B[j];
         float Rji[D];
         sep<D>(Ai, Bi, Aj, Bj, Rji);
-        const float r = sqrtf(K.rr[e]);
+        const float r = sqrtf(__int_as_float(pe.y));
         const float rho_j = f.rho0 + K.C[j].w;
         const float kern = Aj.w * f_kernel(f, r);
         kernsum.add(kern);
@@ -654,13 +663,14 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
     KSum Rr;
     int ni = 1;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) continue;
         const int bj = bits_b(K.bits[j]);
         if (bj == FJSPH_PIPE || bj == FJSPH_FREE) ni = 0;
         float Rji[D];
         sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
-        const float r = sqrtf(K.rr[e]);
+        const float r = sqrtf(__int_as_float(pe.y));
         const float gs = f_gscale(f, r);
         const float4 Cj = K.C[j], Ej = K.E[j];
         float s = 0.f;
@@ -676,13 +686,13 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
 /* ------------------------------------------------------------------------------------------ */
 /* residual (src/Resid.cpp:243-469)                                                               */
 /* ------------------------------------------------------------------------------------------ */
-template <int D>
+template <int D, bool ALE, bool NOFROZEN>
 __global__ void __launch_bounds__(kThreads) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const Pf f = make_pf(P);
-    const bool ale = has(P, FJSPH_VAR_ALE), linear = has(P, FJSPH_VAR_LINEAR), nofrozen = has(P, FJSPH_VAR_NOFROZEN),
-               nodsph = has(P, FJSPH_VAR_NODSPH), tic = has(P, FJSPH_VAR_TIC);
+    constexpr bool ale = ALE, nofrozen = NOFROZEN;
+    const bool linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH), tic = has(P, FJSPH_VAR_TIC);
     const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE, csf = P.st_model == FJSPH_ST_CSF;
     float npdm2 = 0.f;
     if (pairwise) {
@@ -739,19 +749,20 @@ __global__ void __launch_bounds__(kThreads) k_m_resid(Params P, DevState W, DevN
     }
     const bool st_on = pairwise && (!ale || sz_i == 1);
     for (int64_t e = e0; e < e1; ++e) {
-        const int32_t j = N.idx[e];
+        const int2 pe = N.pair[e];
+        const int32_t j = pe.x;
         if (j == i) continue;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
         float Rji[D], Vji[D];
         sep<D>(Ai, Bi, Aj, Bj, Rji);
         sep<D>(Ci, Ei, Cj, Ej, Vji);
-        const float rr = K.rr[e];
+        const float rr = __int_as_float(pe.y);
         const float r = sqrtf(rr);
         const float idist2 = 1.f / (rr + 0.001f * f.H_sq);
         const float volj = Aj.w;
         const float rho_j = f.rho0 + Cj.w;
         const float m_j = volj * rho_j;
-        const int b_j = bits_b(K.bits[j]);
+        const int b_j = bits_b(__float_as_int(Ej.w));
         const float gs = f_gscale(f, r);
         float g[D];
 #pragma unroll
@@ -893,7 +904,22 @@ void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, c
 }
 void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
                     cudaStream_t s) {
-    FJSPH_DISPATCH_M(P, k_m_resid, fgrid(P), P, W, N, K, npd_dev);
+    const unsigned g = fgrid(P);
+    if (g == 0) return;
+    const bool ale = has(P, FJSPH_VAR_ALE), nf = has(P, FJSPH_VAR_NOFROZEN);
+#define FJSPH_RESID_M(DD, A, NF) k_m_resid<DD, A, NF><<<g, kThreads, 0, s>>>(P, W, N, K, npd_dev)
+    if (P.D == 2) {
+        if (ale)
+            nf ? FJSPH_RESID_M(2, true, true) : FJSPH_RESID_M(2, true, false);
+        else
+            nf ? FJSPH_RESID_M(2, false, true) : FJSPH_RESID_M(2, false, false);
+    } else {
+        if (ale)
+            nf ? FJSPH_RESID_M(3, true, true) : FJSPH_RESID_M(3, true, false);
+        else
+            nf ? FJSPH_RESID_M(3, false, true) : FJSPH_RESID_M(3, false, false);
+    }
+#undef FJSPH_RESID_M
 }
 
 } // namespace fjsph
