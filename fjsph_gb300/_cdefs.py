@@ -19,6 +19,8 @@ COLE_EOS, ISO_EOS = 0, 1
 NOAERO, GISSLER, INDUCED_PRESSURE, SKIN_FRIC = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 CLOSURE_PLAIN, CLOSURE_LEARNED = 0, 1
+CLOSURE_ARM_JUDGE, CLOSURE_ARM_LOG = 1, 2
+MLP_INPUTS, MLP_OUTPUTS = 12, 2
 PN, PNP1 = 0, 1
 INLET_ZONE = 6
 MAX_TIMES = 16
@@ -97,3 +99,9 @@ VIEW_I32 = ["b", "surf", "surfzone"]
 class StateView(C.Structure):
     _fields_ = ([("n", _i64)] + [(f, C.POINTER(_d)) for f in VIEW_F64] + [(f, C.POINTER(_i64)) for f in VIEW_I64]
                 + [(f, C.POINTER(_i32)) for f in VIEW_I32])
+
+
+class ClosureReport(C.Structure):
+    _fields_ = [("judged", _i64), ("judged_particles", _i64), ("last_rel_rms", _d), ("max_rel_rms", _d),
+                ("judge_tol", _d), ("logged", _i64), ("log_capacity", _i64), ("steps", _i64),
+                ("learned_active", _i32), ("fallback", _i32)]

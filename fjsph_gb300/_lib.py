@@ -19,6 +19,7 @@ _i64 = C.c_int64
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)
 _i32p = C.POINTER(C.c_int32)
+_fp = C.POINTER(C.c_float)
 
 PROTOTYPES = {
     "fjsph_settings_defaults": (C.c_int, [C.POINTER(d.Settings), _i32]),
@@ -64,6 +65,17 @@ PROTOTYPES = {
     "fjsph_profile_enable": (C.c_int, [_P, _i32]),
     "fjsph_profile_read": (C.c_int, [_P, _dp, _i64p]),
     "fjsph_profile_pass_name": (C.c_char_p, [_i32]),
+    "fjsph_mlp_num_params": (C.c_int, []),
+    "fjsph_mlp_forward": (C.c_int, [_fp, _fp, _i64, _fp]),
+    "fjsph_mlp_gradient": (C.c_int, [_fp, _fp, _fp, _i64, _fp, _dp]),
+    "fjsph_mlp_train": (C.c_int, [_fp, _fp, _fp, _i64, _i32, _i32, C.c_float, C.c_uint64, _dp]),
+    "fjsph_closure_set_weights": (C.c_int, [_P, _fp, C.c_double]),
+    "fjsph_closure_get_weights": (C.c_int, [_P, _fp]),
+    "fjsph_closure_log": (C.c_int, [_P, _i64, _i32]),
+    "fjsph_closure_log_read": (C.c_int, [_P, _fp, _fp, _i64, _i64p, _i32]),
+    "fjsph_closure_arm": (C.c_int, [_P, _i32]),
+    "fjsph_closure_report_get": (C.c_int, [_P, C.POINTER(d.ClosureReport)]),
+    "fjsph_closure_reset": (C.c_int, [_P]),
     "fjsph_find_timestep_noalloc": (C.c_int, [C.POINTER(d.Settings), _i64, C.POINTER(_dp), C.POINTER(_dp), _dp, _dp,
                                               _dp, C.POINTER(_dp), C.POINTER(_dp), _P, _dp, _dp]),
 }

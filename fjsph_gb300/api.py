@@ -233,3 +233,47 @@ class Context:
         p = C.c_void_p()
         check("fjsph_ctx_stream", self._lib.fjsph_ctx_stream(self._h, C.byref(p)))
         return p.value or 0
+
+    # ---- learned aerodynamic closure -----------------------------------------------------------
+    def closure_set_weights(self, params: np.ndarray, judge_tol: float = 0.05) -> None:
+        """Weights of the learned closure (used when settings.aero_closure == CLOSURE_LEARNED)."""
+        w = np.ascontiguousarray(params, dtype=np.float32)
+        if w.size != self._lib.fjsph_mlp_num_params():
+            raise ValueError(f"expected {self._lib.fjsph_mlp_num_params()} parameters, got {w.size}")
+        check("fjsph_closure_set_weights",
+              self._lib.fjsph_closure_set_weights(self._h, _fptr(w), float(judge_tol)))
+
+    def closure_get_weights(self) -> np.ndarray:
+        w = np.empty(self._lib.fjsph_mlp_num_params(), dtype=np.float32)
+        check("fjsph_closure_get_weights", self._lib.fjsph_closure_get_weights(self._h, _fptr(w)))
+        return w
+
+    def closure_log(self, capacity: int, every_n_steps: int = 1) -> None:
+        """Log (inputs, targets) of the plain closure on the device; capacity 0 frees the log."""
+        check("fjsph_closure_log", self._lib.fjsph_closure_log(self._h, int(capacity), int(every_n_steps)))
+
+    def closure_log_read(self, reset: bool = True) -> tuple[np.ndarray, np.ndarray]:
+        rep = self.closure_report()
+        m = int(rep["logged"])
+        X = np.empty((m, d.MLP_INPUTS), dtype=np.float32)
+        T = np.empty((m, d.MLP_OUTPUTS), dtype=np.float32)
+        cnt = C.c_int64()
+        check("fjsph_closure_log_read",
+              self._lib.fjsph_closure_log_read(self._h, _fptr(X), _fptr(T), m, C.byref(cnt), int(reset)))
+        return X[:cnt.value], T[:cnt.value]
+
+    def closure_arm(self, what: int) -> None:
+        """One-shot: the next residual judges (CLOSURE_ARM_JUDGE) or logs (CLOSURE_ARM_LOG)."""
+        check("fjsph_closure_arm", self._lib.fjsph_closure_arm(self._h, int(what)))
+
+    def closure_report(self) -> dict:
+        r = d.ClosureReport()
+        check("fjsph_closure_report_get", self._lib.fjsph_closure_report_get(self._h, C.byref(r)))
+        return {f: getattr(r, f) for f, _ in d.ClosureReport._fields_}
+
+    def closure_reset(self) -> None:
+        check("fjsph_closure_reset", self._lib.fjsph_closure_reset(self._h))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))

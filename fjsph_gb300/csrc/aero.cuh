@@ -14,6 +14,32 @@ __device__ __forceinline__ double get_cd(double Re) {
     return (1.0 + 0.197 * pow(Re, 0.63) + 2.6e-04 * pow(Re, 1.38)) * (24.0 / (Re + 0.00001));
 }
 
+/* Gissler drag coefficient Cd_i and un-occluded area A_i of one particle (src/Aero.h:37-98):
+ * Cd_i = (1 - f) Cd_drop + f, A_i = (1 - f) A_drop + f A_plate, f from lambda or the neighbour
+ * count; Cd_drop from the sphere law with the TAB deformation factor when enabled. */
+template <int D>
+__device__ __forceinline__ void gissler_coeff(const Params &P, double cellRho, double Vn, double V2, double lam,
+                                              double nneigh, double &Cdi, double &Aun) {
+    const double Re = 2.0 * cellRho * Vn * P.L / P.mu_g;
+    const double frac2 = P.use_lam ? fmin(P.interp_fac * lam, 1.0) : fmin(P.interp_fac * nneigh * P.i_n_full, 1.0);
+    const double frac1 = 1.0 - frac2;
+    const double Cds = get_cd(Re);
+    double Cdl = Cds, Adrop = P.A_sphere;
+    if (P.use_TAB_def) {
+        double ymax = V2 * P.ycoef;
+        if (ymax > 1.0) ymax = 1.0;
+        Cdl = Cds * (1 + 2.632 * ymax);
+        if (D == 3) {
+            const double t = P.L + P.Cb * P.L * ymax;
+            Adrop = kPi * t * t;
+        } else {
+            Adrop = P.A_sphere + 2 * (P.Cb * P.L * ymax);
+        }
+    }
+    Cdi = frac1 * Cdl + frac2;
+    Aun = frac1 * Adrop + frac2 * P.A_plate;
+}
+
 template <int D>
 __device__ __forceinline__ void aero_acc(const Params &P, const DevState &W, int64_t i, const double *Vd, double lam,
                          double nneigh, double *out) {
@@ -24,24 +50,9 @@ __device__ __forceinline__ void aero_acc(const Params &P, const DevState &W, int
         /* fully occluded (woccl = 1): the exposed area (1 - woccl) * A is exactly zero, so the
          * force is zero for any finite relative velocity; skip the two pow() of the drag law */
         if (W.woccl[i] == 1.0 && isfinite(Vn)) return;
-        const double Re = 2.0 * W.cellRho[i] * Vn * P.L / P.mu_g;
-        const double frac2 = P.use_lam ? fmin(P.interp_fac * lam, 1.0) : fmin(P.interp_fac * nneigh * P.i_n_full, 1.0);
-        const double frac1 = 1.0 - frac2;
-        const double Cds = get_cd(Re);
-        double Cdl = Cds, Adrop = P.A_sphere;
-        if (P.use_TAB_def) {
-            double ymax = dot<D, double>(Vd, Vd) * P.ycoef;
-            if (ymax > 1.0) ymax = 1.0;
-            Cdl = Cds * (1 + 2.632 * ymax);
-            if (D == 3) {
-                const double t = P.L + P.Cb * P.L * ymax;
-                Adrop = kPi * t * t;
-            } else {
-                Adrop = P.A_sphere + 2 * (P.Cb * P.L * ymax);
-            }
-        }
-        const double Cdi = frac1 * Cdl + frac2;
-        const double Ai = (1.0 - W.woccl[i]) * (frac1 * Adrop + frac2 * P.A_plate);
+        double Cdi, Aun;
+        gissler_coeff<D>(P, W.cellRho[i], Vn, dot<D, double>(Vd, Vd), lam, nneigh, Cdi, Aun);
+        const double Ai = (1.0 - W.woccl[i]) * Aun;
         const double c = 0.5 * Vn;
         const double tail = P.gamma_g * W.cellP[i] * Cdi * Ai / W.m[i];
 #pragma unroll

@@ -128,6 +128,20 @@ struct fjsph_ctx {
     Packed K{};
     bool packed_alloc = false;
     bool dirty_full = true, dirty_all = true, dirty_bound = true;
+    /* learned aerodynamic closure */
+    float *mlp_params = nullptr;
+    __nv_bfloat16 *mlp_w = nullptr, *mlp_wt = nullptr;
+    bool mlp_ready = false, occ_valid = false, closure_fallback = false, judge_pending = false;
+    double judge_tol = 0.05;
+    double *judge_dev = nullptr; /* [3] */
+    double *judge_host = nullptr; /* pinned [3] */
+    int64_t judged = 0, judged_particles = 0, closure_steps = 0;
+    double last_rel_rms = 0.0, max_rel_rms = 0.0;
+    int32_t arm = 0;             /* FJSPH_CLOSURE_ARM_* for the next residual */
+    float *log_X = nullptr, *log_T = nullptr;
+    unsigned long long *log_count = nullptr;
+    int64_t log_cap = 0;
+    int32_t log_every = 1;
 };
 
 namespace {
@@ -220,6 +234,9 @@ int validate_settings(const fjsph_settings *s) {
     if ((s->variant & FJSPH_VAR_NOFROZEN) && (s->variant & FJSPH_VAR_LINEAR)) return FJSPH_E_UNSUPPORTED;
     if (s->precision != FJSPH_PREC_FP64 && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
     if (s->asource != 0) return FJSPH_E_UNSUPPORTED;
+    if (s->aero_closure != FJSPH_CLOSURE_PLAIN && s->aero_closure != FJSPH_CLOSURE_LEARNED) return FJSPH_E_ARG;
+    /* the learned closure lives in the split-precision residual */
+    if (s->aero_closure == FJSPH_CLOSURE_LEARNED && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
     return FJSPH_OK;
 }
 
@@ -326,7 +343,7 @@ bool mixed(const fjsph_ctx *c) { return c->s.precision == FJSPH_PREC_MIXED; }
 int alloc_packed(fjsph_ctx *c) {
     if (c->packed_alloc) return FJSPH_OK;
     Packed &K = c->K;
-    float4 **arrs[] = {&K.A, &K.B, &K.C, &K.E, &K.F, &K.G, &K.N, &K.T};
+    float4 **arrs[] = {&K.A, &K.B, &K.C, &K.E, &K.F, &K.G, &K.N, &K.T, &K.O};
     for (float4 **a : arrs) TRY(dalloc(c, a, c->cap));
     TRY(dalloc(c, &K.bits, c->cap));
     TRY(dalloc(c, &c->nbr_pair, c->nbr_cap));
@@ -568,6 +585,12 @@ int reorder_states(fjsph_ctx *c, const Params &P) {
     }
     for (int k = 0; k < c->D; ++k)
         CU(cudaMemcpyAsync(c->xs[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
+    if (c->packed_alloc && c->occ_valid) { /* occlusion statistics follow their particles */
+        float4 *tmp = reinterpret_cast<float4 *>(c->stage);
+        launch_m_permute_f4(c->K.O, tmp, c->new_of_old, c->n, s);
+        CU(cudaMemcpyAsync(c->K.O, tmp, sizeof(float4) * c->n, cudaMemcpyDeviceToDevice, s));
+        c->launches += 1;
+    }
     mark_full(c);
     return FJSPH_OK;
 }
@@ -673,10 +696,12 @@ int prestep_passes(fjsph_ctx *c) {
     {
         Section sec(c, PASS_SURFACE);
         launch_aero_velocity(P, WS(c), N, s);
-        if (mixed(c))
+        if (mixed(c)) {
             launch_m_surface(P, WS(c), N, c->K, s);
-        else
+            c->occ_valid = true;
+        } else {
             launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
+        }
         c->launches += 4;
     }
     if (!(c->s.variant & FJSPH_VAR_NOFROZEN)) {
@@ -754,15 +779,70 @@ int boundary_section(fjsph_ctx *c, const Params &P, int nb_rule) {
     return FJSPH_OK;
 }
 
+bool learned_wanted(const fjsph_ctx *c) { return c->s.aero_closure == FJSPH_CLOSURE_LEARNED; }
+bool learned_active(const fjsph_ctx *c) {
+    return learned_wanted(c) && mixed(c) && c->s.acase == FJSPH_GISSLER && c->mlp_ready && !c->closure_fallback;
+}
+
+/* Closure of the next residual: plain, learned, or a one-shot judge / log call.  The learned
+ * closure needs the occlusion statistics of a surface pass on the current particle set; until
+ * one has run the residual uses the plain closure. */
+Closure next_closure(fjsph_ctx *c) {
+    Closure C{};
+    C.mode = kClosurePlain;
+    C.occ = c->K.O;
+    C.M = mlp::DevMlp{c->mlp_params, c->mlp_w, c->mlp_wt};
+    C.judge = c->judge_dev;
+    C.logX = c->log_X;
+    C.logT = c->log_T;
+    C.log_count = c->log_count;
+    C.log_cap = c->log_cap;
+    /* an armed judge / log waits for the first residual that can honour it */
+    if (!mixed(c) || c->s.acase != FJSPH_GISSLER || !c->occ_valid) return C;
+    if (learned_active(c)) {
+        C.mode = kClosureLearned;
+        if (c->arm == FJSPH_CLOSURE_ARM_JUDGE && c->judge_dev) {
+            C.mode = kClosureJudge;
+            c->arm = 0;
+        }
+    } else if (c->arm == FJSPH_CLOSURE_ARM_LOG && c->log_cap > 0) {
+        C.mode = kClosureLog;
+        c->arm = 0;
+    }
+    return C;
+}
+
+/* Judge result of the last judge residual (after the stream reached it). */
+int closure_collect(fjsph_ctx *c) {
+    if (!c->judge_pending) return FJSPH_OK;
+    TRY(sync(c));
+    c->judge_pending = false;
+    const double d2 = c->judge_host[0], p2 = c->judge_host[1];
+    c->judged_particles = (int64_t)c->judge_host[2];
+    c->last_rel_rms = p2 > 0.0 ? std::sqrt(d2 / p2) : (d2 > 0.0 ? INFINITY : 0.0);
+    c->max_rel_rms = std::max(c->max_rel_rms, c->last_rel_rms);
+    c->judged++;
+    if (!(c->last_rel_rms <= c->judge_tol)) c->closure_fallback = true;
+    return FJSPH_OK;
+}
+
 /* The residual in the configured form. */
-void resid(fjsph_ctx *c, const Params &P) {
+int resid(fjsph_ctx *c, const Params &P) {
+    if (learned_wanted(c) && !(mixed(c) && c->mlp_ready)) return FJSPH_E_STATE;
     Section sec(c, PASS_RESID);
     if (mixed(c)) {
         ensure_pack(c);
-        launch_m_resid(P, WS(c), make_nbr(c), c->K, &c->dsc->npd, c->stream);
+        const Closure C = next_closure(c);
+        if (C.mode == kClosureJudge) CU(cudaMemsetAsync(c->judge_dev, 0, 3 * sizeof(double), c->stream));
+        launch_m_resid(P, WS(c), make_nbr(c), c->K, &c->dsc->npd, C, c->stream);
+        if (C.mode == kClosureJudge) {
+            CU(cudaMemcpyAsync(c->judge_host, c->judge_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+            c->judge_pending = true;
+        }
     } else {
         launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, c->stream);
     }
+    return FJSPH_OK;
 }
 
 DevInlet dev_inlet(const fjsph_ctx *c, const HostInlet &I) {
@@ -796,7 +876,7 @@ int rk_intermediate(fjsph_ctx *c, int stage, double dt_scale) {
         launch_bound_rho_update(P, PN(c), WS(c), c->S, 0, sum_w, &c->dsc->dt, dt_scale, s);
         c->launches++;
     }
-    resid(c, P);
+    TRY(resid(c, P));
     {
         Section sec(c, PASS_UPDATE);
         launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, &c->dsc->dt, dt_scale, s);
@@ -816,7 +896,7 @@ int rk_final(fjsph_ctx *c) {
         launch_bound_rho_update(P, PN(c), WS(c), c->S, 1, 0.0, &c->dsc->dt, 1.0, s);
         c->launches++;
     }
-    resid(c, P);
+    TRY(resid(c, P));
     {
         Section sec(c, PASS_UPDATE);
         for (int k = 0; k < c->D; ++k)
@@ -903,7 +983,7 @@ int nb_iter(fjsph_ctx *c) {
     Params P = make_params(c);
     cudaStream_t s = c->stream;
     TRY(boundary_section(c, P, 1));
-    resid(c, P);
+    TRY(resid(c, P));
     c->launches++;
     if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
         launch_bound_rho_update(P, PN(c), WS(c), c->S, 2, 0.0, &c->dsc->dt, 1.0, s);
@@ -1041,7 +1121,17 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
 /* Integrator::integrate (src/Integration.cpp:233-303). */
 int integrate(fjsph_ctx *c, double &step_error) {
     if (needs_update_data(c)) return FJSPH_E_UNSUPPORTED;
+    /* judge / log schedule of the closure: the first residual of every n-th step */
+    const int64_t k = c->closure_steps++;
+    if (learned_active(c) && c->s.learned_judge_interval > 0 && k % c->s.learned_judge_interval == 0)
+        c->arm = FJSPH_CLOSURE_ARM_JUDGE;
+    else if (!learned_active(c) && c->log_cap > 0 && c->log_every > 0 && k % c->log_every == 0)
+        c->arm = FJSPH_CLOSURE_ARM_LOG;
+    else
+        c->arm = 0;
     TRY(integrate_no_update(c, step_error, true));
+    c->arm = 0;
+    TRY(closure_collect(c));
     /* update_data: zero-density guard (src/Integration.cpp:116-124) and pn = pnp1 */
     launch_density_guard(make_params(c), WS(c), c->stream);
     c->launches++;
@@ -1189,6 +1279,7 @@ int fjsph_ctx_destroy(fjsph_ctx *c) {
     for (cudaEvent_t e : c->user_ev)
         if (e) cudaEventDestroy(e);
     if (c->hsc) cudaFreeHost(c->hsc);
+    if (c->judge_host) cudaFreeHost(c->judge_host);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FJSPH_OK;
@@ -1300,6 +1391,7 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
     if (st->n > c->cap) return FJSPH_E_CAPACITY;
     if (c->blocks.empty()) return FJSPH_E_STATE;
     if (c->blocks.back().second != st->n) return FJSPH_E_ARG;
+    c->occ_valid = false; /* occlusion statistics belong to the previous state */
     std::vector<int64_t> keys;
     if (st->n != c->n || c->n == 0) {
         /* new particle set: identity mapping, re-sort at the next search */
@@ -1416,6 +1508,7 @@ int fjsph_detect_surface(fjsph_ctx *c) {
     if (mixed(c)) {
         ensure_pack(c);
         launch_m_surface(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
+        c->occ_valid = true;
     } else {
         launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, c->stream);
     }
@@ -1507,7 +1600,7 @@ int fjsph_set_no_slip(fjsph_ctx *c) {
 int fjsph_get_acc_and_rrho(fjsph_ctx *c, double npd) {
     TRY(need_nbr(c));
     TRY(set_npd_device(c, npd));
-    resid(c, make_params(c));
+    TRY(resid(c, make_params(c)));
     c->pn_equals_W = false;
     return sync(c);
 }
@@ -1649,6 +1742,116 @@ int fjsph_profile_read(fjsph_ctx *c, double *ms, int64_t *launches) {
 const char *fjsph_profile_pass_name(int32_t k) {
     if (k < 0 || k >= PASS_COUNT) return "";
     return kPassNames[k];
+}
+
+/* ---- learned aerodynamic closure ------------------------------------------------------------ */
+int fjsph_closure_set_weights(fjsph_ctx *c, const float *params, double judge_tol) {
+    TRY(check_ctx(c));
+    if (!params || !(judge_tol > 0.0)) return FJSPH_E_ARG;
+    for (int k = 0; k < mlp::kNumParams; ++k)
+        if (!std::isfinite(params[k])) return FJSPH_E_NONFINITE;
+    if (!c->mlp_params) {
+        TRY(dalloc(c, &c->mlp_params, mlp::kNumParams));
+        TRY(dalloc(c, &c->mlp_w, mlp::kNumBf16));
+        TRY(dalloc(c, &c->mlp_wt, mlp::mlp_num_bf16_t()));
+        TRY(dalloc(c, &c->judge_dev, 3));
+        if (!c->judge_host) CU(cudaMallocHost(&c->judge_host, 3 * sizeof(double)));
+    }
+    TRY(sync(c));
+    TRY(mlp::mlp_upload(params, c->mlp_params, c->mlp_w, c->mlp_wt, c->stream));
+    TRY(sync(c));
+    c->mlp_ready = true;
+    c->judge_tol = judge_tol;
+    return FJSPH_OK;
+}
+
+int fjsph_closure_get_weights(fjsph_ctx *c, float *params) {
+    TRY(check_ctx(c));
+    if (!params) return FJSPH_E_ARG;
+    if (!c->mlp_ready) return FJSPH_E_STATE;
+    TRY(sync(c));
+    CU(cudaMemcpy(params, c->mlp_params, sizeof(float) * mlp::kNumParams, cudaMemcpyDeviceToHost));
+    return FJSPH_OK;
+}
+
+int fjsph_closure_log(fjsph_ctx *c, int64_t capacity, int32_t every_n_steps) {
+    TRY(check_ctx(c));
+    if (capacity < 0 || every_n_steps <= 0) return FJSPH_E_ARG;
+    TRY(sync(c));
+    if (capacity != c->log_cap) {
+        TRY(dfree(c, c->log_X));
+        TRY(dfree(c, c->log_T));
+        TRY(dfree(c, c->log_count));
+        c->log_cap = 0;
+        if (capacity > 0) {
+            TRY(dalloc(c, &c->log_X, capacity * mlp::kIn));
+            TRY(dalloc(c, &c->log_T, capacity * mlp::kOut));
+            TRY(dalloc(c, &c->log_count, 1));
+            CU(cudaMemset(c->log_count, 0, sizeof(unsigned long long)));
+            c->log_cap = capacity;
+        }
+    }
+    c->log_every = every_n_steps;
+    return FJSPH_OK;
+}
+
+int64_t log_held(fjsph_ctx *c) {
+    if (c->log_cap == 0) return 0;
+    unsigned long long n = 0;
+    if (cudaMemcpy(&n, c->log_count, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return std::min<int64_t>((int64_t)n, c->log_cap);
+}
+
+int fjsph_closure_log_read(fjsph_ctx *c, float *X, float *T, int64_t max_samples, int64_t *count, int32_t reset) {
+    TRY(check_ctx(c));
+    if (max_samples < 0 || (max_samples > 0 && (!X || !T))) return FJSPH_E_ARG;
+    TRY(sync(c));
+    const int64_t held = log_held(c);
+    if (held < 0) return FJSPH_E_CUDA;
+    const int64_t m = std::min(held, max_samples);
+    if (m > 0) {
+        CU(cudaMemcpy(X, c->log_X, sizeof(float) * mlp::kIn * m, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(T, c->log_T, sizeof(float) * mlp::kOut * m, cudaMemcpyDeviceToHost));
+    }
+    if (count) *count = m;
+    if (reset && c->log_cap > 0) CU(cudaMemset(c->log_count, 0, sizeof(unsigned long long)));
+    return FJSPH_OK;
+}
+
+int fjsph_closure_arm(fjsph_ctx *c, int32_t what) {
+    TRY(check_ctx(c));
+    if (what != 0 && what != FJSPH_CLOSURE_ARM_JUDGE && what != FJSPH_CLOSURE_ARM_LOG) return FJSPH_E_ARG;
+    c->arm = what;
+    return FJSPH_OK;
+}
+
+int fjsph_closure_report_get(fjsph_ctx *c, fjsph_closure_report *out) {
+    TRY(check_ctx(c));
+    if (!out) return FJSPH_E_ARG;
+    TRY(closure_collect(c));
+    TRY(sync(c));
+    std::memset(out, 0, sizeof(*out));
+    out->judged = c->judged;
+    out->judged_particles = c->judged_particles;
+    out->last_rel_rms = c->last_rel_rms;
+    out->max_rel_rms = c->max_rel_rms;
+    out->judge_tol = c->judge_tol;
+    out->logged = log_held(c);
+    if (out->logged < 0) return FJSPH_E_CUDA;
+    out->log_capacity = c->log_cap;
+    out->steps = c->closure_steps;
+    out->learned_active = learned_active(c) ? 1 : 0;
+    out->fallback = c->closure_fallback ? 1 : 0;
+    return FJSPH_OK;
+}
+
+int fjsph_closure_reset(fjsph_ctx *c) {
+    TRY(check_ctx(c));
+    TRY(closure_collect(c));
+    c->closure_fallback = false;
+    c->judged = c->judged_particles = 0;
+    c->last_rel_rms = c->max_rel_rms = 0.0;
+    return FJSPH_OK;
 }
 
 } /* extern "C" */

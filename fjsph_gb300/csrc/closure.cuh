@@ -1,0 +1,201 @@
+/*
+ * closure.cuh -- the learned stand-in for the Gissler occlusion and drag-coefficient closure
+ * (src/Aero.h:37-98, occlusion factor src/Geometry.cpp:233-255), evaluated inside the residual
+ * kernel of the split-precision form.
+ *
+ * Per particle the network maps 12 inputs to 2 outputs:
+ *   inputs  0  sum_j w_j max(c_j, 0)     c_j = -(x_j - x_i).V / (|V| r_ij): cosine between the
+ *           1  sum_j w_j max(-c_j, 0)    neighbour direction and the upwind direction, V = v_inf - v_i
+ *           2  sum_j w_j c_j^2           as in the occlusion test; w_j = vol_j W(r_ij)
+ *           3  max(0, max_j c_j)         the plain closure's occlusion statistic before clamping
+ *           4  neighbour count / n_full
+ *           5  log10(1 + |U|)            U = cellV - v at the stage (relative air velocity)
+ *           6  log10(1 + We)             We = rho_air |U|^2 L / sigma (0 without surface tension)
+ *           7  log10(1 + Re)             Re = 2 rho_air |U| L / mu_air
+ *           8  |n|                       surface normal
+ *           9  n.U / |U|
+ *          10  lambda_nb
+ *          11  lambda
+ *   outputs 0  log10(Cd_i A_i / A_sphere) drag coefficient x un-occluded area, sphere-referenced
+ *           1  woccl                     occlusion factor (clamped to [0, 1] on use)
+ * and the force is the plain closure's  a = |U| U / (2 sos^2) gamma p_air Cd_i A_i (1 - woccl) / m.
+ * Inputs 0-3 come from the surface-curvature pass (which already walks the neighbours for the
+ * occlusion test); the others are read at the stage.  Particles past the lambda_nb cutoff keep
+ * woccl = 1 (zero force) without the network, as in the plain closure.
+ */
+#pragma once
+
+#include "aero.cuh"
+#include "common.cuh"
+#include "mlp.cuh"
+
+namespace fjsph {
+
+enum ClosureMode : int32_t { kClosurePlain = 0, kClosureLearned = 1, kClosureJudge = 2, kClosureLog = 3 };
+
+struct Closure {
+    int32_t mode;
+    mlp::DevMlp M;
+    const float4 *occ;             /* inputs 0-3 per slot (surface-curvature pass)           */
+    double *judge;                 /* [3]: sum |a_l - a_p|^2, sum |a_p|^2, particles judged    */
+    float *logX, *logT;            /* sample log: 12 inputs, 2 targets per sample              */
+    unsigned long long *log_count; /* samples offered (may exceed log_cap)                    */
+    int64_t log_cap;
+};
+
+struct MlpWarpSmem {
+    __nv_bfloat16 X[32][mlp::kInP];
+    float Y[32][2];
+};
+
+template <int D>
+__device__ __forceinline__ void closure_inputs(const Params &P, float4 occ, double nneigh, const double *U,
+                                               double cellRho, float4 nrm, float lam, float (&x)[mlp::kIn]) {
+    const double U2 = dot<D, double>(U, U);
+    const double Un = sqrt(U2);
+    x[0] = occ.x;
+    x[1] = occ.y;
+    x[2] = occ.z;
+    x[3] = occ.w;
+    x[4] = (float)(nneigh * P.i_n_full);
+    x[5] = log10f(1.f + (float)Un);
+    x[6] = P.sig > 0.0 ? log10f(1.f + (float)(cellRho * U2 * P.L / P.sig)) : 0.f;
+    x[7] = log10f(1.f + (float)(2.0 * cellRho * Un * P.L / P.mu_g));
+    const float n[3] = {nrm.x, nrm.y, nrm.z};
+    float nn = 0.f, nu = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        nn += n[k] * n[k];
+        nu += n[k] * (float)U[k];
+    }
+    x[8] = sqrtf(nn);
+    x[9] = Un > 0.0 ? nu / (float)Un : 0.f;
+    x[10] = nrm.w;
+    x[11] = lam;
+}
+
+/* Network outputs for the lanes with `want` set; every lane of the warp must call. */
+__device__ __forceinline__ void mlp_warp(const mlp::DevMlp &M, bool want, const float (&x)[mlp::kIn],
+                                         MlpWarpSmem &S, float &y0, float &y1) {
+    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (bal == 0u) return;
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int cnt = __popc(bal);
+    const int rank = __popc(bal & ((1u << lane) - 1u));
+    uint4 *Xz = reinterpret_cast<uint4 *>(&S.X[0][0]); /* 32 rows x 32 B */
+    Xz[lane] = make_uint4(0u, 0u, 0u, 0u);
+    Xz[lane + 32] = make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();
+    if (want) {
+#pragma unroll
+        for (int c = 0; c < mlp::kIn; ++c)
+            S.X[rank][c] =
+                __float2bfloat16_rn((x[c] - __ldg(M.params + mlp::oInShift + c)) * __ldg(M.params + mlp::oInScale + c));
+    }
+    __syncwarp();
+    for (int tile = 0; tile * 16 < cnt; ++tile) {
+        float Y[4];
+        mlp::forward_tile(M, &S.X[tile * 16][0], Y);
+        if (t == 0) {
+            S.Y[tile * 16 + g][0] = Y[0];
+            S.Y[tile * 16 + g][1] = Y[1];
+            S.Y[tile * 16 + g + 8][0] = Y[2];
+            S.Y[tile * 16 + g + 8][1] = Y[3];
+        }
+    }
+    __syncwarp();
+    if (want) {
+        y0 = S.Y[rank][0];
+        y1 = S.Y[rank][1];
+    }
+    __syncwarp();
+}
+
+/* Aerodynamic acceleration of a live, aero-active particle from the closure outputs. */
+template <int D>
+__device__ __forceinline__ void learned_acc(const Params &P, const DevState &W, int64_t i, const double *U, float y0,
+                                            float y1, double *out) {
+    const double Un = vnorm<D, double>(U);
+    const double CdA = (double)exp10f(y0) * P.A_sphere;
+    const double wo = (double)fminf(fmaxf(y1, 0.f), 1.f);
+    const double tail = P.gamma_g * W.cellP[i] * CdA * (1.0 - wo) / W.m[i];
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = 0.5 * Un * U[k] / (P.sos * P.sos) * tail;
+}
+
+/* The aerodynamic term of the residual for particle i under the closure mode.  All lanes of the
+ * warp call (the network runs on whole warps); lanes with live == false contribute nothing.
+ * Not inlined: the residual's register allocation then does not absorb the network's. */
+template <int D>
+__device__ __noinline__ void closure_aero(const Params &P, const DevState &W, const Closure &C, const float4 *Kn,
+                                             const float4 *Kg, int64_t i, bool live, double nneigh, MlpWarpSmem &S,
+                                             bool &aero_on, double *aero) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) aero[k] = 0.0;
+    aero_on = live && W.cellID[i] != -1;
+    double U[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) U[k] = aero_on ? W.cellV[k][i] - W.v[k][i] : 0.0;
+    if (C.mode == kClosurePlain) {
+        if (aero_on) aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, aero);
+        return;
+    }
+    /* the network covers the particles whose occlusion factor is not fixed at 1 by lambda_nb */
+    const bool want = aero_on && (float)W.lam_nb[i] < (float)P.lam_cutoff;
+    float x[mlp::kIn];
+    if (want) closure_inputs<D>(P, C.occ[i], nneigh, U, W.cellRho[i], Kn[i], Kg[i].w, x);
+    if (C.mode == kClosureLog) {
+        if (aero_on) aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, aero);
+        const unsigned bal = __ballot_sync(0xffffffffu, want);
+        if (bal == 0u) return;
+        const int lane = threadIdx.x & 31;
+        unsigned long long base = 0;
+        if (lane == __ffs(bal) - 1) base = atomicAdd(C.log_count, (unsigned long long)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, __ffs(bal) - 1);
+        if (want) {
+            const unsigned long long slot = base + (unsigned long long)__popc(bal & ((1u << lane) - 1u));
+            if (slot < (unsigned long long)C.log_cap) {
+                double Cdi, Aun;
+                const double Un = vnorm<D, double>(U);
+                gissler_coeff<D>(P, W.cellRho[i], Un, dot<D, double>(U, U), W.lam_nb[i], nneigh, Cdi, Aun);
+#pragma unroll
+                for (int c = 0; c < mlp::kIn; ++c) C.logX[slot * mlp::kIn + c] = x[c];
+                C.logT[slot * 2] = (float)log10(Cdi * Aun / P.A_sphere);
+                C.logT[slot * 2 + 1] = (float)W.woccl[i];
+            }
+        }
+        return;
+    }
+    float y0 = 0.f, y1 = 0.f;
+    mlp_warp(C.M, want, x, S, y0, y1);
+    if (want)
+        learned_acc<D>(P, W, i, U, y0, y1, aero);
+    else if (aero_on)
+        aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, aero);
+    if (C.mode == kClosureJudge) {
+        double d2 = 0.0, p2 = 0.0, cnt = 0.0;
+        if (want) {
+            double ref[D];
+            aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, ref);
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                d2 += (aero[k] - ref[k]) * (aero[k] - ref[k]);
+                p2 += ref[k] * ref[k];
+            }
+            cnt = 1.0;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if ((threadIdx.x & 31) == 0 && cnt > 0.0) {
+            atomicAdd(&C.judge[0], d2);
+            atomicAdd(&C.judge[1], p2);
+            atomicAdd(&C.judge[2], cnt);
+        }
+    }
+}
+
+} // namespace fjsph

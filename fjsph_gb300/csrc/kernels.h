@@ -4,6 +4,7 @@
  */
 #pragma once
 
+#include "closure.cuh"
 #include "common.cuh"
 
 namespace fjsph {
@@ -11,8 +12,16 @@ namespace fjsph {
 /* Packed FP32 split-precision inputs of the mixed form (see sweeps_mixed.cu). */
 struct Packed {
     float4 *A, *B, *C, *E, *F, *G, *N, *T;
+    float4 *O; /* occlusion statistics of the surface-curvature pass (learned-closure inputs 0-3) */
     int32_t *bits;
 };
+
+/* ---- mlp_train.cu ------------------------------------------------------------------------- */
+namespace mlp {
+/* FP32 parameters (host) -> device master copy and its BF16 forward / transposed copies */
+int mlp_upload(const float *host_params, float *dparams, __nv_bfloat16 *dw, __nv_bfloat16 *dwt, cudaStream_t s);
+int mlp_num_bf16_t();
+} // namespace mlp
 
 /* ---- neighbours.cu ------------------------------------------------------------------------ */
 struct CellGrid {
@@ -75,7 +84,9 @@ void launch_m_bound_pressure(const Params &P, const DevState &W, const DevNbr &N
 void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, int32_t *near_inlet,
                           cudaStream_t s);
 void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
-                    cudaStream_t s);
+                    const Closure &C, cudaStream_t s);
+/* dst[new_of_old[i]] = src[i] for a per-slot float4 array */
+void launch_m_permute_f4(const float4 *src, float4 *dst, const int32_t *new_of_old, int64_t n, cudaStream_t s);
 
 /* ---- integrate.cu ------------------------------------------------------------------------- */
 struct RKScratch {

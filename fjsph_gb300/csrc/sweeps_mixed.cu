@@ -19,6 +19,7 @@
  *   bits = b | surf << 3 | surfzone << 4
  */
 #include "aero.cuh"
+#include "closure.cuh"
 #include "kernels.h"
 #include "linalg.cuh"
 
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
 #pragma unroll
     for (int k = 0; k < D * D; ++k) Li[k] = (float)W.L[k][i];
     const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
-    float curve = 0.f, woccl_ = 0.f;
+    float curve = 0.f, woccl_ = 0.f, o0 = 0.f, o1 = 0.f, o2 = 0.f;
     for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
         const int2 pe = N.pair[e];
         const int32_t j = pe.x;
@@ -413,9 +414,16 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
         if (occl) {
             const float frac = -fdot<D>(Rij, Vdiff) / (vdn * r);
             if (frac > woccl_) woccl_ = frac;
+            if (vdn > 0.f) { /* inputs 0-2 of the learned closure */
+                const float w = K.A[j].w * kernel_w<float>(r, f.H, f.Wc, f.cubic);
+                o0 += w * fmaxf(frac, 0.f);
+                o1 += w * fmaxf(-frac, 0.f);
+                o2 += w * frac * frac;
+            }
         }
     }
     W.woccl[i] = ((float)W.lam_nb[i] < (float)P.lam_cutoff) ? fmaxf(0.f, fminf(woccl_, 1.f)) : 1.0f;
+    K.O[i] = make_float4(o0, o1, o2, woccl_);
 #pragma unroll
     for (int k = 0; k < D; ++k) W.norm[k][i] = ni[k];
     W.curve[i] = curve;
@@ -687,9 +695,17 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
 /* residual (src/Resid.cpp:243-469)                                                               */
 /* ------------------------------------------------------------------------------------------ */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev) {
+__global__ void __launch_bounds__(kThreads, 4) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
+                                                      Closure C) {
+    __shared__ __align__(16) MlpWarpSmem mlp_smem[kThreads / 32];
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    const bool live = i < P.n;
+    /* the aerodynamic term first: the learned closure runs on whole warps */
+    double aero[D];
+    bool aero_on;
+    closure_aero<D>(P, W, C, K.N, K.G, i, live, live ? double(N.off[i + 1] - N.off[i]) : 0.0, mlp_smem[threadIdx.x >> 5],
+                    aero_on, aero);
+    if (!live) return;
     const Pf f = make_pf(P);
     constexpr bool ale = ALE, nofrozen = NOFROZEN;
     const bool linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH), tic = has(P, FJSPH_VAR_TIC);
@@ -737,16 +753,6 @@ __global__ void __launch_bounds__(kThreads) k_m_resid(Params P, DevState W, DevN
         art[k] = 0.f;
     }
     KSum Rrho, Rrhoc, Rrho_d;
-    double aero[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) aero[k] = 0.0;
-    const bool aero_on = W.cellID[i] != -1;
-    if (aero_on) {
-        double Vd[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) Vd[k] = W.cellV[k][i] - W.v[k][i];
-        aero_acc<D>(P, W, i, Vd, W.lam_nb[i], double(e1 - e0), aero);
-    }
     const bool st_on = pairwise && (!ale || sz_i == 1);
     for (int64_t e = e0; e < e1; ++e) {
         const int2 pe = N.pair[e];
@@ -852,6 +858,11 @@ __global__ void __launch_bounds__(kThreads) k_m_resid(Params P, DevState W, DevN
     W.Rrho[i] = R;
 }
 
+__global__ void k_permute_f4(const float4 *src, float4 *dst, const int32_t *new_of_old, int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[new_of_old[i]] = src[i];
+}
+
 inline unsigned fgrid(const Params &P) { return grid_for(P.n - P.nb, kThreads); }
 inline unsigned bgrid(const Params &P) { return grid_for(P.nb, kThreads); }
 inline unsigned agrid(const Params &P) { return grid_for(P.n, kThreads); }
@@ -875,6 +886,9 @@ void launch_m_pack(const Params &P, const DevState &W, const Packed &K, int64_t 
         k_pack_state<2><<<g, 256, 0, s>>>(P, W, K, i0, i1, full);
     else
         k_pack_state<3><<<g, 256, 0, s>>>(P, W, K, i0, i1, full);
+}
+void launch_m_permute_f4(const float4 *src, float4 *dst, const int32_t *new_of_old, int64_t n, cudaStream_t s) {
+    if (n > 0) k_permute_f4<<<grid_for(n, 256), 256, 0, s>>>(src, dst, new_of_old, n);
 }
 void launch_m_npd(const Params &P, const DevNbr &N, const Packed &K, double *npd_part, cudaStream_t s) {
     FJSPH_DISPATCH_M(P, k_m_npd, agrid(P), P, N, K, npd_part);
@@ -903,11 +917,11 @@ void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, c
     FJSPH_DISPATCH_M(P, k_m_bound_ghost, bgrid(P), P, W, N, K, near_inlet);
 }
 void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
-                    cudaStream_t s) {
+                    const Closure &C, cudaStream_t s) {
     const unsigned g = fgrid(P);
     if (g == 0) return;
     const bool ale = has(P, FJSPH_VAR_ALE), nf = has(P, FJSPH_VAR_NOFROZEN);
-#define FJSPH_RESID_M(DD, A, NF) k_m_resid<DD, A, NF><<<g, kThreads, 0, s>>>(P, W, N, K, npd_dev)
+#define FJSPH_RESID_M(DD, A, NF) k_m_resid<DD, A, NF><<<g, kThreads, 0, s>>>(P, W, N, K, npd_dev, C)
     if (P.D == 2) {
         if (ale)
             nf ? FJSPH_RESID_M(2, true, true) : FJSPH_RESID_M(2, true, false);

@@ -256,6 +256,64 @@ int fjsph_find_timestep_noalloc(const fjsph_settings *s, int64_t n_fluid, const 
                                 const double *curve, const double *const v[3], const double *const vPert[3],
                                 void *stream, double *dt, double *maxima7);
 
+/* ---- learned aerodynamic closure ------------------------------------------------------------ */
+/* No counterpart in the reference: a 12 -> 64 -> 64 -> 64 -> 2 GELU network (BF16 weights, FP32
+ * accumulation) that stands in for the Gissler occlusion factor and drag coefficient
+ * (src/Aero.h:37-98, src/Geometry.cpp:233-255) in the split-precision residual.  Its inputs and
+ * outputs per particle are listed in fjsph_gb300/csrc/closure.cuh.  Parameters are one FP32
+ * vector of fjsph_mlp_num_params() floats:
+ *   W1[64][16] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
+ *   in_shift[16] in_scale[16] out_shift[2] out_scale[2]
+ * (row = output; inputs padded to 16 and outputs to 8 with zero weights; the network sees
+ * (x - in_shift) * in_scale and returns y * out_scale + out_shift). */
+#define FJSPH_MLP_INPUTS 12
+#define FJSPH_MLP_OUTPUTS 2
+#define FJSPH_CLOSURE_ARM_JUDGE 1 /* next residual: learned closure judged against the plain one */
+#define FJSPH_CLOSURE_ARM_LOG 2   /* next residual: plain closure, inputs and targets logged    */
+
+typedef struct fjsph_closure_report {
+    int64_t judged;           /* judge evaluations completed                                   */
+    int64_t judged_particles; /* particles compared by the last evaluation                     */
+    double last_rel_rms;      /* RMS |a_learned - a_plain| / RMS |a_plain|, last evaluation    */
+    double max_rel_rms;       /* largest over all evaluations                                  */
+    double judge_tol;         /* fallback threshold                                            */
+    int64_t logged;           /* samples held in the log                                       */
+    int64_t log_capacity;
+    int64_t steps;            /* integrate() steps counted by the judge / log schedule         */
+    int32_t learned_active;   /* 1 while residuals use the learned closure                     */
+    int32_t fallback;         /* 1 once an evaluation exceeded judge_tol (plain closure since) */
+} fjsph_closure_report;
+
+int fjsph_mlp_num_params(void);
+/* Host arrays: X[n][12] -> Y[n][2] (outputs un-normalised). */
+int fjsph_mlp_forward(const float *params, const float *X, int64_t n, float *Y);
+/* Mean squared error over the 2 normalised outputs, summed, per sample: loss = (1/n) sum_s
+ * sum_o ((y_so - t_so) / out_scale_o)^2 in normalised units, and its gradient with respect to the
+ * trainable part of params (the first kNumWeights floats; the normalisation stays fixed). */
+int fjsph_mlp_gradient(const float *params, const float *X, const float *T, int64_t n, float *grad, double *loss);
+/* Adam on the GPU over (X, T): `epochs` passes in a seeded random order, mini-batches of `batch`
+ * samples, learning rate lr with a cosine decay to lr/20.  params is updated in place;
+ * final_loss receives the mean loss of the last epoch. */
+int fjsph_mlp_train(float *params, const float *X, const float *T, int64_t n, int32_t epochs, int32_t batch, float lr,
+                    uint64_t seed, double *final_loss);
+/* Weights of the context's learned closure (settings.aero_closure = FJSPH_CLOSURE_LEARNED uses
+ * them in the split-precision residual).  Every settings.learned_judge_interval-th step the
+ * first residual also runs the plain closure; once the relative RMS aero-force error exceeds
+ * judge_tol the context falls back to the plain closure (see fjsph_closure_report). */
+int fjsph_closure_set_weights(fjsph_ctx *ctx, const float *params, double judge_tol);
+int fjsph_closure_get_weights(fjsph_ctx *ctx, float *params);
+/* Sample log on the device: while the plain closure is in use, the first residual of every
+ * every_n_steps-th step appends (inputs, targets) of each particle the network would cover.
+ * capacity 0 frees the log. */
+int fjsph_closure_log(fjsph_ctx *ctx, int64_t capacity, int32_t every_n_steps);
+/* Copies up to max_samples logged samples to X[.][12], T[.][2]; *count = samples copied. */
+int fjsph_closure_log_read(fjsph_ctx *ctx, float *X, float *T, int64_t max_samples, int64_t *count, int32_t reset);
+/* One-shot: make the next residual a judge (FJSPH_CLOSURE_ARM_JUDGE) or log (..._LOG) call. */
+int fjsph_closure_arm(fjsph_ctx *ctx, int32_t what);
+int fjsph_closure_report_get(fjsph_ctx *ctx, fjsph_closure_report *out);
+/* Clears the fallback flag and the judge statistics. */
+int fjsph_closure_reset(fjsph_ctx *ctx);
+
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
 int fjsph_step_report(fjsph_ctx *ctx, double *out5);
