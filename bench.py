@@ -6,6 +6,12 @@ The input state is a seeded synthetic jet (fjsph_gb300.cases.jet_crossflow), res
 when the timed region starts; the state and neighbour arrays exceed the 129 MB L2, so no flush
 is needed between steps.
 
+The headline form is FP32 split precision with the learned aerodynamic closure.  Before the
+timed region (untimed) the closure network is trained on the GPU: samples are logged from seeded
+plain-closure jets (jet speed ~ U(5, 20) m/s, crossflow ~ U(30, 80) m/s) and fitted by the
+library's own BF16 training kernels.  The plain FP64 form and the FP32 form with the plain
+closure are timed beside it on the same state.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n PARTICLES]
 
 Prints one JSON line (rank 0).  `--impl reference` times the CPU restatement of the reference
@@ -43,6 +49,13 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--closure", default="learned", choices=["learned", "plain"])
+    ap.add_argument("--train-samples", type=int, default=5_000_000)
+    ap.add_argument("--train-jets", type=int, default=10, help="seeded jets the samples are logged from")
+    ap.add_argument("--train-epochs", type=int, default=12)
+    ap.add_argument("--closure-weights", default="", help="load trained weights from this .npy (skip training)")
+    ap.add_argument("--save-weights", default="", help="save the trained weights to this .npy")
+    ap.add_argument("--plain-steps", type=int, default=2, help="steps of the FP32 form with the plain closure")
     return ap.parse_args()
 
 
@@ -111,14 +124,30 @@ def measured_peaks() -> dict:
 
 # ---------------------------------------------------------------------------------------------
 def resid_bytes_per_particle(s) -> int:
-    """Algorithmic bytes of one residual evaluation per fluid particle (FP64 form).
+    """Algorithmic bytes of one residual evaluation per fluid particle.
 
-    Reads each logical field once: x 3, search x 3, v 3, rho, p, m, aVisc 3, deltaD, cellV 3,
-    cellP, cellRho, lam_nb, woccl (8 B each), cellID, part_id (8 B), b, surfzone (4 B), CSR
-    offset (8 B); ALE adds vPert 3.  Writes acc 3, Af 3, Rrho.  Neighbour re-reads do not count.
+    Each logical field is counted once per launch; neighbour re-reads and the pair list do not
+    count.  FP64 form (8 B words): x 3, search x 3, v 3, rho, p, m, aVisc 3, deltaD, cellV 3,
+    cellP, cellRho, lam_nb, woccl (8 B each), cellID, CSR offset (8 B), b, surfzone (4 B); ALE adds
+    vPert 3, NOFROZEN gradRho 3.  Writes acc 3, Af 3, Rrho.
+    FP32 split-precision form: x and v as FP32 hi/lo pairs (8 B per component), rho, p, volume and
+    flags at 4 B; aVisc 3 and deltaD (FP64 state), CSR offset and cellID (8 B); the closure reads
+    cellV 3, cellP, cellRho, m, lam_nb, woccl (8 B), the learned closure also the four occlusion
+    inputs, the normal and lambda (4 B each).  Writes acc 3, Af 3, Rrho at 8 B.
     """
     from fjsph_gb300 import _cdefs as d
     D = s.dim
+    if s.precision == d.PREC_MIXED:
+        b = 8 * D * 2 + 4 * 4                      # x, v (hi/lo), rho, p, volume, flags
+        b += 8 * (D + 1) + 8 * 2                   # aVisc, deltaD, CSR offset, cellID
+        b += 8 * (D + 5)                           # cellV, cellP, cellRho, m, lam_nb, woccl
+        if s.aero_closure == d.CLOSURE_LEARNED:
+            b += 4 * (4 + D + 1)                   # occlusion inputs, normal, lambda
+        if s.variant & d.VAR_ALE:
+            b += 4 * D
+        if s.variant & d.VAR_NOFROZEN:
+            b += 4 * D
+        return b + 8 * (2 * D + 1)
     r8 = 3 * D + 3 + 3 + D + 1 + D + 2 + 2 + 2 + 1
     if s.variant & d.VAR_ALE:
         r8 += D
@@ -128,12 +157,46 @@ def resid_bytes_per_particle(s) -> int:
     return 8 * (r8 + w8) + 4 * 2
 
 
-def make_case(n_target: int, precision: str):
+def train_closure(args, log):
+    """Untimed: log samples from seeded plain-closure jets and train the network on the GPU."""
+    import numpy as np
+    from fjsph_gb300 import closure as cl
+    info = {}
+    if args.closure_weights and Path(args.closure_weights).exists():
+        info["weights"] = f"loaded from {args.closure_weights}"
+        return np.load(args.closure_weights).astype(np.float32), info
+    t0 = time.perf_counter()
+    specs = cl.jet_specs(args.train_jets, 800_000, seed=2024)
+    X, T = cl.collect_samples(specs, args.train_samples, steps=8)
+    t1 = time.perf_counter()
+    p0 = cl.init_params(X, T, seed=7)
+    p, loss = cl.train(p0, X, T, epochs=args.train_epochs, batch=4096, lr=2e-3, seed=8)
+    t2 = time.perf_counter()
+    info.update(samples=int(len(X)), jets=len(specs), log_s=round(t1 - t0, 2), train_s=round(t2 - t1, 2),
+                epochs=args.train_epochs, final_loss=loss,
+                jet_speeds=[round(sp.jet_speed, 2) for sp in specs], air_speeds=[round(sp.air_speed, 2) for sp in specs])
+    if args.save_weights:
+        np.save(args.save_weights, p)
+    log(f"closure trained: {info}")
+    return p, info
+
+
+def make_case(n_target: int, precision: str, closure: str = "plain"):
     from fjsph_gb300 import cases, _cdefs as d
     c = cases.jet_crossflow(n_target=n_target)
     if precision == "mixed":
         c.settings.precision = d.PREC_MIXED
+        if closure == "learned":
+            c.settings.aero_closure = d.CLOSURE_LEARNED
     return c
+
+
+def timed_steps(ctx, steps: int, ws: int) -> float:
+    ctx.event_record(0)
+    for _ in range(steps):
+        ctx.integrate()
+    ctx.event_record(1)
+    return reduce_max(ws, ctx.event_elapsed(0, 1))
 
 
 def run_ours(args, ws, rank, local):
@@ -141,11 +204,15 @@ def run_ours(args, ws, rank, local):
     from fjsph_gb300 import _cdefs as d
     from fjsph_gb300.api import Context
 
-    c = make_case(args.n, args.precision)
+    learned = args.precision == "mixed" and args.closure == "learned"
+    weights, closure_info = (train_closure(args, lambda m: print(m, file=sys.stderr)) if learned else (None, None))
+    c = make_case(args.n, args.precision, args.closure)
     s = c.settings
     nf = c.n_fluid
     ctx = Context(s, c.state.n + 1024, c.blocks)
     ctx.set_states(c.state, c.state)
+    if learned:
+        ctx.closure_set_weights(weights, 0.05)
     for _ in range(args.warmup):
         ctx.integrate()
     barrier(ws)
@@ -159,6 +226,7 @@ def run_ours(args, ws, rank, local):
     ctx.event_record(1)
     ms = ctx.event_elapsed(0, 1)
     launches = ctx.launch_stats()
+    n_pairs = ctx.update_neighbours()  # pairs of the last search (outside the timed region)
     prof = ctx.profile_read()
     ctx.profile(False)
     clk = clocks.stop()
@@ -174,8 +242,18 @@ def run_ours(args, ws, rank, local):
     achieved = bpp * nf / per_launch / 1e9
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
             "frac": round(achieved / peaks.get("hbm_gbs", 6800.0), 4), "traffic": None,
-            "kernel": "k_resid (get_acc_and_Rrho)", "launch_ms": round(per_launch * 1e3, 3),
+            "kernel": ("k_m_resid" if s.precision == d.PREC_MIXED else "k_resid") + " (get_acc_and_Rrho)", "launch_ms": round(per_launch * 1e3, 3),
             "bytes_per_launch": bpp * nf, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
+
+    # the learned closure judged against the plain one on the state the timed steps reached
+    if learned:
+        ctx.closure_arm(d.CLOSURE_ARM_JUDGE)
+        ctx.integrate()
+        rep_c = ctx.closure_report()
+        closure_info.update(judge_rel_rms=rep_c["last_rel_rms"], judge_particles=rep_c["judged_particles"],
+                            judged=rep_c["judged"], fallback=bool(rep_c["fallback"]),
+                            learned_active=bool(rep_c["learned_active"]),
+                            judge_interval_steps=s.learned_judge_interval)
 
     # end to end through the public API with host buffers in pinned memory: upload both states,
     # one step, download the new state, every step
@@ -197,11 +275,28 @@ def run_ours(args, ws, rank, local):
         e2e = {"value": nf * args.e2e_steps * ws / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes, "pinned": host._pinned}
 
+    # the FP32 form with the plain closure on the same state
+    plain = None
+    if learned and args.plain_steps > 0:
+        sp_ = s.copy()
+        sp_.aero_closure = d.CLOSURE_PLAIN
+        cp = Context(sp_, c.state.n + 1024, c.blocks)
+        cp.set_states(c.state, c.state)
+        cp.integrate()
+        cp.profile(True)
+        msp = timed_steps(cp, args.plain_steps, ws)
+        pp = cp.profile_read()
+        plain = {"value": nf * args.plain_steps * ws / (msp / 1e3), "ms_per_step": msp / args.plain_steps,
+                 "residual_ms_per_launch": round(pp["residual"][0] / max(pp["residual"][1], 1), 4),
+                 "steps": args.plain_steps}
+        cp.close()
+
     # the plain FP64 form on the same state, same GPU
     fp64 = None
     if args.fp64_steps > 0 and s.precision != d.PREC_FP64:
         s64 = s.copy()
         s64.precision = d.PREC_FP64
+        s64.aero_closure = d.CLOSURE_PLAIN
         c64 = Context(s64, c.state.n + 1024, c.blocks)
         c64.set_states(c.state, c.state)
         c64.integrate()
@@ -214,7 +309,8 @@ def run_ours(args, ws, rank, local):
                 "steps": args.fp64_steps}
         c64.close()
     return dict(value=value, ms=ms, nf=nf, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches, fp64=fp64,
-                prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s, case=c)
+                prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s, case=c,
+                plain=plain, closure=closure_info, pairs=n_pairs)
 
 
 def pinned_state(st):
@@ -342,13 +438,16 @@ def main():
                              f"{dt:.1f} s)"}
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else ("f32+f64+bf16" if args.closure == "learned" else "f32+f64"),
                 "data": "synthetic",
                 "config": {"workload": "jet_in_crossflow_3d", "particles": r["n"], "fluid": r["nf"],
-                           "form": args.precision, "integrator": "runge_kutta4",
+                           "form": args.precision, "closure": args.closure if args.precision == "mixed" else "plain",
+                           "integrator": "runge_kutta4",
                            "l2": "inputs larger than L2 (state ~1 GB)", "parallelism": f"replicas{ws}"},
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
-                "fp64_form": r["fp64"],
+                "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"], "closure": r["closure"],
+                "neighbour_pairs": r["pairs"],
+                "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
                 "gpu_launches": r["launches"], "passes_ms": r["prof"]}
         print(json.dumps(line))
     if ws > 1:
