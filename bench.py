@@ -157,6 +157,12 @@ def resid_bytes_per_particle(s) -> int:
     return 8 * (r8 + w8) + 4 * 2
 
 
+# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
+# 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
+# the benchmark's particle count (traffic grows with the particle and pair counts).
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 590.6e6 / 620_210}
+
+
 def train_closure(args, log):
     """Untimed: log samples from seeded plain-closure jets and train the network on the GPU."""
     import numpy as np
@@ -240,8 +246,11 @@ def run_ours(args, ws, rank, local):
     bpp = resid_bytes_per_particle(s)
     per_launch = r_ms / max(r_cnt, 1) / 1e3
     achieved = bpp * nf / per_launch / 1e9
+    tkey = "fp64" if s.precision == d.PREC_FP64 else ("mixed_learned" if learned else None)
+    traffic = round(RESID_TRAFFIC_PER_PARTICLE[tkey] * nf) if tkey else None
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-            "frac": round(achieved / peaks.get("hbm_gbs", 6800.0), 4), "traffic": None,
+            "frac": round(achieved / peaks.get("hbm_gbs", 6800.0), 4), "traffic": traffic,
+            "traffic_source": "ncu capture on the 634k-particle jet, scaled by fluid particles" if tkey else None,
             "kernel": ("k_m_resid" if s.precision == d.PREC_MIXED else "k_resid") + " (get_acc_and_Rrho)", "launch_ms": round(per_launch * 1e3, 3),
             "bytes_per_launch": bpp * nf, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
 
