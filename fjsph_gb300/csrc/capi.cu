@@ -93,8 +93,10 @@ struct fjsph_ctx {
     int32_t *nbr_counts = nullptr;
     int64_t *nbr_off = nullptr;
     int32_t *nbr_idx = nullptr;
-    int2 *nbr_pair = nullptr; /* split-precision form: (slot, r^2) per pair */
-    int64_t nbr_cap = 0, n_pairs = 0;
+    int2 *nbr_pair = nullptr; /* split-precision form: (slot, r^2) per pair, sliced-ELL */
+    int32_t *slice_w = nullptr;   /* entries per slice of kSlice slots                    */
+    int64_t *slice_off = nullptr; /* first entry of each slice (exclusive scan of slice_w) */
+    int64_t nbr_cap = 0, n_pairs = 0, nbr_storage = 0;
     bool nbr_valid = false;
     int64_t *scan_tmp64 = nullptr;
     int64_t scan_tmp64_len = 0;
@@ -334,6 +336,8 @@ DevNbr make_nbr(const fjsph_ctx *c) {
     const bool m = c->s.precision == FJSPH_PREC_MIXED;
     N.idx = m ? nullptr : c->nbr_idx;
     N.pair = m ? c->nbr_pair : nullptr;
+    N.cnt = m ? c->nbr_counts : nullptr;
+    N.slice = m ? c->slice_off : nullptr;
     for (int k = 0; k < 3; ++k) N.xs[k] = c->xs[k];
     return N;
 }
@@ -621,20 +625,29 @@ int search(fjsph_ctx *c) {
     launch_nbr_count(P, c->xs, c->G, c->nbr_counts, s);
     launch_scan_i64(c->nbr_counts, c->nbr_off, c->n, c->scan_tmp64, s);
     c->launches += 4;
-    int64_t total = 0, grid[4] = {0, 0, 0, 0};
+    const int64_t nslices = (c->n + kSlice - 1) / kSlice;
+    if (mixed(c)) {
+        launch_slice_width(c->nbr_counts, c->n, c->slice_w, s);
+        launch_scan_i64(c->slice_w, c->slice_off, nslices, c->scan_tmp64, s);
+        c->launches += 4;
+        CU(cudaMemcpyAsync(&c->hsc->red[14], c->slice_off + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    }
+    int64_t total = 0, storage = 0, grid[4] = {0, 0, 0, 0};
     CU(cudaMemcpyAsync(&c->hsc->red[15], c->nbr_off + c->n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(&c->hsc->red[10], c->G.grid, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     TRY(sync(c));
     std::memcpy(&total, &c->hsc->red[15], sizeof(int64_t));
     std::memcpy(grid, &c->hsc->red[10], 4 * sizeof(int64_t));
+    if (mixed(c)) std::memcpy(&storage, &c->hsc->red[14], sizeof(int64_t));
+    const int64_t need = std::max(total, storage);
     if (grid[3]) {
         /* the grid outgrew the table: this search used the wrapped (slower) walk; grow the table
          * for the next one when the grid is of a reasonable size */
         const double ncells = (double)grid[0] * (double)grid[1] * (double)grid[2];
         if (ncells <= (double)kMaxTable) c->table_want = next_pow2((int64_t)ncells);
     }
-    if (total > c->nbr_cap) {
-        int64_t ncap = std::max<int64_t>(total + total / 4, c->nbr_cap * 2);
+    if (need > c->nbr_cap) {
+        int64_t ncap = std::max<int64_t>(need + need / 4, c->nbr_cap * 2);
         if (ncap >= ((int64_t)1 << 31)) return FJSPH_E_NEIGHBOUR;
         CU(cudaFree(c->nbr_idx));
         c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->nbr_idx), c->allocs.end());
@@ -647,9 +660,11 @@ int search(fjsph_ctx *c) {
         c->nbr_cap = ncap;
     }
     if (mixed(c)) TRY(alloc_packed(c));
-    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? c->nbr_pair : nullptr, s);
+    launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? c->nbr_pair : nullptr, c->slice_off,
+                    c->nbr_counts, s);
     c->launches += 1;
     c->n_pairs = total;
+    c->nbr_storage = mixed(c) ? storage : total;
     c->nbr_valid = true;
     return FJSPH_OK;
 }
@@ -1244,6 +1259,8 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     A(dalloc(c, &G.grid, 4));
     A(dalloc(c, &c->nbr_counts, capacity));
     A(dalloc(c, &c->nbr_off, capacity + 1));
+    A(dalloc(c, &c->slice_w, capacity / kSlice + 2));
+    A(dalloc(c, &c->slice_off, capacity / kSlice + 3));
     c->scan_tmp64_len = capacity / 2048 + 16;
     A(dalloc(c, &c->scan_tmp64, c->scan_tmp64_len));
     c->nbr_cap = capacity * (c->D == 3 ? 96 : 28);
@@ -1445,10 +1462,15 @@ int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double
     std::vector<double> xs(c->D * n);
     CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
     if (c->n_pairs) {
-        if (mixed(c)) {
-            std::vector<int2> pr(c->n_pairs);
-            CU(cudaMemcpy(pr.data(), c->nbr_pair, sizeof(int2) * c->n_pairs, cudaMemcpyDeviceToHost));
-            for (int64_t e = 0; e < c->n_pairs; ++e) id[e] = pr[e].x;
+        if (mixed(c)) { /* sliced-ELL -> CSR */
+            const int64_t nslices = (n + kSlice - 1) / kSlice;
+            std::vector<int2> pr(c->nbr_storage);
+            std::vector<int64_t> so(nslices + 1);
+            CU(cudaMemcpy(pr.data(), c->nbr_pair, sizeof(int2) * c->nbr_storage, cudaMemcpyDeviceToHost));
+            CU(cudaMemcpy(so.data(), c->slice_off, sizeof(int64_t) * (nslices + 1), cudaMemcpyDeviceToHost));
+            for (int64_t i = 0; i < n; ++i)
+                for (int64_t k = 0; k < off[i + 1] - off[i]; ++k)
+                    id[off[i] + k] = pr[so[i / kSlice] + k * kSlice + i % kSlice].x;
         } else {
             CU(cudaMemcpy(id.data(), c->nbr_idx, sizeof(int32_t) * c->n_pairs, cudaMemcpyDeviceToHost));
         }

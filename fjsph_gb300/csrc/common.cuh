@@ -62,14 +62,36 @@ struct Params {
     DevBlock blocks[kMaxBlocks];
 };
 
-/* Neighbour lists: CSR over slots, plus the positions at search time (the reference keeps the
- * squared distance of each pair from search time, src/Resid.cpp:288). */
+/* Neighbour lists plus the positions at search time (the reference keeps the squared distance
+ * of each pair from search time, src/Resid.cpp:288).
+ *  - FP64 form: CSR, off[n + 1] and idx (neighbour slots).
+ *  - split-precision form: (slot, FP32 squared distance bits) pairs in sliced-ELL order with
+ *    slices of 32 consecutive slots: pair k of slot i is at slice[i / 32] + 32 k + i % 32, and
+ *    slot i has cnt[i] pairs.  A warp walking 32 consecutive slots' lists in step reads 32
+ *    consecutive pairs per load.  off is still filled (CSR offsets of the counts). */
+constexpr int kSlice = 32;
 struct DevNbr {
     const int64_t *off;
-    const int32_t *idx;  /* FP64 form: neighbour slots                                    */
-    const int2 *pair;    /* split-precision form: (slot, FP32 squared distance bits)      */
+    const int32_t *idx;   /* FP64 form                                    */
+    const int2 *pair;     /* split-precision form, sliced-ELL             */
+    const int32_t *cnt;   /* split-precision form: pairs per slot         */
+    const int64_t *slice; /* split-precision form: first entry per slice  */
     const double *xs[3];
 };
+
+/* The pairs of slot i: entry k at base + k * stride. */
+struct NbrRange {
+    int64_t base;
+    int32_t stride, n;
+};
+__device__ __forceinline__ NbrRange nbr_range(const DevNbr &N, int64_t i) {
+    if (N.pair) return NbrRange{N.slice[i / kSlice] + (i % kSlice), kSlice, N.cnt[i]};
+    return NbrRange{N.off[i], 1, (int32_t)(N.off[i + 1] - N.off[i])};
+}
+__device__ __forceinline__ int64_t nbr_slot(const DevNbr &N, const NbrRange &R, int32_t k) {
+    const int64_t e = R.base + (int64_t)k * R.stride;
+    return N.pair ? (int64_t)N.pair[e].x : (int64_t)N.idx[e];
+}
 
 FJSPH_HD bool has(const Params &P, uint32_t bit) { return (P.variant & bit) != 0; }
 

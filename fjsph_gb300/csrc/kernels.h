@@ -44,9 +44,12 @@ void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, c
 void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s);
 void launch_scatter_sort(const Params &P, CellGrid &G, cudaStream_t s);
 void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s);
-/* Writes idx (FP64 form) or, when pair is given, (slot, FP32 squared distance) pairs. */
+/* Writes idx (FP64 form, CSR by off) or, when pair is given, (slot, FP32 squared distance) pairs
+ * in the sliced-ELL order of DevNbr (slice offsets `slice`, counts per slot `counts`). */
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     int2 *pair, cudaStream_t s);
+                     int2 *pair, const int64_t *slice, const int32_t *counts, cudaStream_t s);
+/* width[s] = kSlice x the largest count of slice s (slices of kSlice slots from slot 0). */
+void launch_slice_width(const int32_t *counts, int64_t n, int32_t *width, cudaStream_t s);
 /* Bucket-ordered hi/lo coordinates for the neighbour walk (after any re-ordering). */
 void launch_sorted_pos(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s);
 /* Re-ordering: new slot of every old slot, boundary group first, each group in bucket order. */

@@ -285,15 +285,27 @@ __global__ void __launch_bounds__(kThreads) k_nbr_count(Params P, double *xs0, d
     counts[i] = cnt;
 }
 
+/* Entries per slice of kSlice slots: kSlice x the largest count in the slice (one warp per
+ * slice; the launch covers whole warps from slot 0). */
+__global__ void k_slice_width(const int32_t *counts, int64_t n, int32_t *width) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int32_t c = i < n ? counts[i] : 0;
+    const int32_t m = __reduce_max_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && i < n) width[i / kSlice] = m * kSlice;
+}
+
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, double *xs1, double *xs2, CellGrid G,
-                                                        const int64_t *off, int32_t *idx, int2 *pair) {
+                                                        const int64_t *off, int32_t *idx, int2 *pair,
+                                                        const int64_t *slice, const int32_t *counts) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     double *const xs[3] = {xs0, xs1, xs2};
-    int64_t w = off[i];
-    const int64_t wend = off[i + 1];
     if (pair) {
+        /* sliced-ELL: pair k of slot i at slice[i / 32] + 32 k + i % 32 */
+        int2 *dst = pair + slice[i / kSlice] + (i % kSlice);
+        const int32_t kend = counts[i];
+        int32_t k = 0;
         /* (slot, FP32 squared distance from the hi/lo split, about 1e-7 relative) */
         float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
 #pragma unroll
@@ -303,7 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
             lo[k] = (float)(x - (double)hi[k]);
         }
         walk<D>(P, xs, G, i, [&](int32_t j, int32_t e) {
-            if (w < wend) {
+            if (k < kend) {
                 const float4 hj = G.sorted_hi[e], lj = G.sorted_lo[e];
                 const float dx = (hj.x - hi[0]) + (lj.x - lo[0]), dy = (hj.y - hi[1]) + (lj.y - lo[1]);
                 float d2 = dx * dx + dy * dy;
@@ -311,12 +323,14 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
                     const float dz = (hj.z - hi[2]) + (lj.z - lo[2]);
                     d2 += dz * dz;
                 }
-                pair[w] = make_int2(j, __float_as_int(d2));
+                dst[(int64_t)k * kSlice] = make_int2(j, __float_as_int(d2));
             }
-            ++w;
+            ++k;
         });
         return;
     }
+    int64_t w = off[i];
+    const int64_t wend = off[i + 1];
     walk<D>(P, xs, G, i, [&](int32_t j, int32_t) {
         if (w < wend) idx[w] = j;
         ++w;
@@ -475,12 +489,18 @@ void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, i
 }
 
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     int2 *pair, cudaStream_t s) {
+                     int2 *pair, const int64_t *slice, const int32_t *counts, cudaStream_t s) {
     if (P.n == 0) return;
     if (P.D == 2)
-        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair);
+        k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair, slice,
+                                                                   counts);
     else
-        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair);
+        k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair, slice,
+                                                                   counts);
+}
+
+void launch_slice_width(const int32_t *counts, int64_t n, int32_t *width, cudaStream_t s) {
+    if (n > 0) k_slice_width<<<grid_for(n, kThreads), kThreads, 0, s>>>(counts, n, width);
 }
 
 void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,

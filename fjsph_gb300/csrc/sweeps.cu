@@ -150,7 +150,7 @@ __global__ void k_aero_velocity(Params P, DevState W, DevNbr N) {
     if (P.use_lam)
         on = W.lam_nb[i] < P.lam_cutoff && W.b[i] == FJSPH_FREE;
     else
-        on = double(N.off[i + 1] - N.off[i]) * P.i_n_full < P.lam_cutoff && W.b[i] == FJSPH_FREE;
+        on = double(nbr_range(N, i).n) * P.i_n_full < P.lam_cutoff && W.b[i] == FJSPH_FREE;
 #pragma unroll
     for (int k = 0; k < D; ++k) W.cellV[k][i] = on ? P.v_inf[k] : 0.0;
     W.cellID[i] = on ? 1 : kNoCell;
@@ -535,9 +535,9 @@ __global__ void k_no_slip(Params P, DevState W, DevNbr N, double *vt0, double *v
         double vs[D], ks = 0.0;
 #pragma unroll
         for (int k = 0; k < D; ++k) vs[k] = 0.0;
-        for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-            /* also used by the split-precision form, whose lists hold (slot, r^2) pairs */
-            const int64_t j = N.pair ? N.pair[e].x : N.idx[e];
+        const NbrRange R = nbr_range(N, i); /* also used by the split-precision form */
+        for (int32_t k = 0; k < R.n; ++k) {
+            const int64_t j = nbr_slot(N, R, k);
             if (j == i || W.b[j] <= FJSPH_PISTON) continue;
             const double r = sqrt(pair_rr<D>(N, i, j));
             const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);

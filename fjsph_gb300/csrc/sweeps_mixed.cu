@@ -68,6 +68,22 @@ __device__ __forceinline__ int bits_b(int w) { return w & 7; }
 __device__ __forceinline__ int bits_surf(int w) { return (w >> 3) & 1; }
 __device__ __forceinline__ int bits_zone(int w) { return (w >> 4) & 1; }
 
+/* the pairs of slot i in the sliced-ELL list: L[k] for k < L.n */
+struct SellList {
+    const int2 *p;
+    int32_t n;
+    __device__ __forceinline__ int2 operator[](int32_t k) const { return p[(int64_t)k * kSlice]; }
+};
+__device__ __forceinline__ SellList sell(const DevNbr &N, int64_t i) {
+    return SellList{N.pair + N.slice[i / kSlice] + (i % kSlice), N.cnt[i]};
+}
+
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+/* Pair-list rows fetched into L1 ahead of use by the residual; with the sliced-ELL order one row
+ * of a warp is one 256-byte line. */
+constexpr int32_t kListAhead = 4;
+
 /* separation x_j - x_i from the hi/lo split */
 template <int D>
 __device__ __forceinline__ void sep(const float4 &Ai, const float4 &Bi, const float4 &Aj, const float4 &Bj, float *R) {
@@ -146,8 +162,9 @@ __global__ void __launch_bounds__(kThreads) k_m_npd(Params P, DevNbr N, Packed K
     if (i >= P.n) return;
     const Pf f = make_pf(P);
     float npd = 0.f;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i || bits_b(K.bits[j]) <= FJSPH_PISTON) continue;
         npd += f_kernel(f, sqrtf(__int_as_float(pe.y)));
@@ -177,8 +194,9 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
         nr[k] = 0.f;
     }
     float kernsum = 0.f, colour = 0.f, npd = 0.f;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) {
             kernsum += f.Wc;
@@ -272,7 +290,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
     fnormalized<D>(ni, nh);
     const int b = W.b[i];
     const float lam_nb = (float)W.lam_nb[i], lam = K.G[i].w;
-    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    const SellList L = sell(N, i);
     int surf = W.surf[i];
     if (b < FJSPH_PIPE) {
         surf = 0;
@@ -290,8 +308,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         }
         surf = 1;
         const float sq2h = sqrtf(2.f) * h;
-        for (int64_t e = e0; e < e1; ++e) {
-            const int2 pe = N.pair[e];
+        for (int32_t e = 0; e < L.n; ++e) {
+            const int2 pe = L[e];
         const int32_t j = pe.x;
             if (j == i) continue;
             float Rji[D], xT[D];
@@ -328,8 +346,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
 #pragma unroll
     for (int k = 0; k < D; ++k) nrm[k] = 0.f;
     const bool inside = lam > 0.7f;
-    for (int64_t e = e0; e < e1; ++e) {
-        const int2 pe = N.pair[e];
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
         float Rji[D];
@@ -386,8 +404,9 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     for (int k = 0; k < D * D; ++k) Li[k] = (float)W.L[k][i];
     const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
     float curve = 0.f, woccl_ = 0.f, o0 = 0.f, o1 = 0.f, o2 = 0.f;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
         float Rij[D]; /* = x_j - x_i, the reference's naming in this loop */
@@ -436,8 +455,9 @@ __global__ void k_m_surface_zone(Params P, DevState W, DevNbr N, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     int sz = 0;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e)
-        if (bits_surf(K.bits[N.pair[e].x])) {
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e)
+        if (bits_surf(K.bits[L[e].x])) {
             sz = 1;
             break;
         }
@@ -476,8 +496,9 @@ __global__ void __launch_bounds__(kThreads) k_m_dissipation(Params P, DevState W
 #pragma unroll
     for (int k = 0; k < D; ++k) av[k] = 0.f;
     KSum Rrhod;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
@@ -552,8 +573,9 @@ __global__ void __launch_bounds__(kThreads) k_m_particle_shift(Params P, DevStat
 #pragma unroll
     for (int k = 0; k < D; ++k) dU[k] = 0.f;
     float maxUij = 0.f, woccl = 0.f;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
         float Rji[D], dv[D];
@@ -625,8 +647,9 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_pressure(Params P, DevStat
     float acck[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) acck[k] = 0.f;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         const int bj = K.bits[j];
         if (bits_b(bj) <= FJSPH_PISTON) continue;
@@ -670,8 +693,9 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
     for (int k = 0; k < D; ++k) vi[k] = (float)W.v[k][i];
     KSum Rr;
     int ni = 1;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e) {
-        const int2 pe = N.pair[e];
+    const SellList L = sell(N, i);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
         const int bj = bits_b(K.bits[j]);
@@ -695,7 +719,7 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
 /* residual (src/Resid.cpp:243-469)                                                               */
 /* ------------------------------------------------------------------------------------------ */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads, 4) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
+__global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
                                                       Closure C) {
     __shared__ __align__(16) MlpWarpSmem mlp_smem[kThreads / 32];
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -703,7 +727,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_m_resid(Params P, DevState W, D
     /* the aerodynamic term first: the learned closure runs on whole warps */
     double aero[D];
     bool aero_on;
-    closure_aero<D>(P, W, C, K.N, K.G, i, live, live ? double(N.off[i + 1] - N.off[i]) : 0.0, mlp_smem[threadIdx.x >> 5],
+    closure_aero<D>(P, W, C, K.N, K.G, i, live, double(N.cnt[i]), mlp_smem[threadIdx.x >> 5],
                     aero_on, aero);
     if (!live) return;
     const Pf f = make_pf(P);
@@ -742,7 +766,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_m_resid(Params P, DevState W, D
     vi[0] = Ci.x + Ei.x;
     vi[1] = Ci.y + Ei.y;
     if (D == 3) vi[2] = Ci.z + Ei.z;
-    const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    const SellList L = sell(N, i);
     KSum acc[D];
     float acc_ale[D], visc[D], st[D], art[D];
 #pragma unroll
@@ -754,11 +778,27 @@ __global__ void __launch_bounds__(kThreads, 4) k_m_resid(Params P, DevState W, D
     }
     KSum Rrho, Rrhoc, Rrho_d;
     const bool st_on = pairwise && (!ale || sz_i == 1);
-    for (int64_t e = e0; e < e1; ++e) {
-        const int2 pe = N.pair[e];
+    /* software pipeline: after this pair's own gathers are issued, the next pair is read and its
+     * neighbour's packed inputs are prefetched into L1 while this pair is computed; list rows
+     * are fetched kListAhead ahead */
+    int2 nxt = L.n > 0 ? L[0] : make_int2((int32_t)i, 0);
+    for (int32_t q = 1; q < kListAhead && q < L.n; ++q) prefetch_l1(&L.p[(int64_t)q * kSlice]);
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = nxt;
+        if (e + kListAhead < L.n) prefetch_l1(&L.p[(int64_t)(e + kListAhead) * kSlice]);
         const int32_t j = pe.x;
-        if (j == i) continue;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
+        if (e + 1 < L.n) {
+            nxt = L[e + 1];
+            const int32_t jn = nxt.x;
+            prefetch_l1(K.A + jn);
+            prefetch_l1(K.B + jn);
+            prefetch_l1(K.C + jn);
+            prefetch_l1(K.E + jn);
+            if (linear || ale) prefetch_l1(K.F + jn);
+            if (nofrozen) prefetch_l1(K.G + jn);
+        }
+        if (j == i) continue;
         float Rji[D], Vji[D];
         sep<D>(Ai, Bi, Aj, Bj, Rji);
         sep<D>(Ci, Ei, Cj, Ej, Vji);
