@@ -200,6 +200,31 @@ class Context:
         check("fjsph_integrate_n", self._lib.fjsph_integrate_n(self._h, int(n_steps), C.byref(r)))
         return r.value
 
+    def limits(self) -> list:
+        """(first, second) of every LIMITS entry as update_data left them."""
+        nb = C.c_int32()
+        check("fjsph_get_limits", self._lib.fjsph_get_limits(self._h, None, 0, C.byref(nb)))
+        arr = (d.Block * nb.value)()
+        check("fjsph_get_limits", self._lib.fjsph_get_limits(self._h, arr, nb.value, C.byref(nb)))
+        return [(arr[i].first, arr[i].second) for i in range(nb.value)]
+
+    def get_inlet(self, block: int, n_back: int, depth: int):
+        """The inlet's back and buffer tables (reference indices) as they are now."""
+        back = np.zeros(n_back, dtype=np.int64)
+        buf = np.zeros(n_back * depth, dtype=np.int64)
+        c = d.Inlet()
+        c.block, c.n_back, c.depth = block, n_back, depth
+        c.back = back.ctypes.data_as(C.POINTER(C.c_int64))
+        c.buffer = buf.ctypes.data_as(C.POINTER(C.c_int64))
+        check("fjsph_get_inlet", self._lib.fjsph_get_inlet(self._h, C.byref(c)))
+        return back, buf.reshape(n_back, depth)
+
+    def update_counts(self) -> tuple[int, int]:
+        """Particles inserted and deleted by update_data since the context was created."""
+        a, b = C.c_int64(), C.c_int64()
+        check("fjsph_update_counts", self._lib.fjsph_update_counts(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def step_report(self) -> dict:
         out = (C.c_double * 5)()
         check("fjsph_step_report", self._lib.fjsph_step_report(self._h, out))

@@ -320,3 +320,94 @@ def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, 
     fl.aero_norm = (0.0, 0.0, 1.0)
     fl.aeroconst = 0.0
     return Case("jet_crossflow", s, st, blocks)
+
+
+def jet_inlet(D: float = 1e-3, dx: float = 5e-5, jet_speed: float = 10.0, air_speed: float = 50.0,
+              pipe_layers: int = 30, column_layers: int = 40, depth: int = 4, seed: int = 77,
+              max_points: int | None = None, solver: int = d.RUNGE_KUTTA) -> Case:
+    """A live inlet feeding a straight jet (the insertion and deletion paths of config 2).
+
+    One fluid block of type inletZone (src/shapes/inlet.cpp): per disk column, `depth` BUFFER
+    layers below one BACK layer at z_b, PIPE layers above it inside ghost-walled pipe walls, and
+    a FREE column above the pipe exit at z = 0.  The insertion plane sits 0.02 dx above the BACK
+    layer, so every column advances in the first step and a new BUFFER particle is inserted one
+    dx upstream of each column's last; the deletion plane sits half a dx below the column top, so
+    the top layer is deleted at the first update.  max_points caps the insertions.
+    """
+    s = defaults(3)
+    _liquid(s)
+    _air(s, air_speed)
+    s.particle_step = dx
+    s.H_fac = 1.3
+    s.speed_sound = 10.0 * jet_speed
+    s.visc_alpha = 0.05
+    s.grav[:] = [0.0, 0.0, -9.81]
+    s.solver_type = solver
+    s.cfl = 0.5
+    s.cfl_min = 0.1
+    s.cfl_max = 0.5
+    s.delta_t_min = 1e-12
+    s.delta_t_max = 1e-5
+    derive(s)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R = 0.5 * D
+    m = int(math.ceil(R / dx)) + 1
+    ax = np.arange(-m, m + 1) * dx
+    gx, gy = np.meshgrid(ax, ax, indexing="ij")
+    disk = np.stack([gx.ravel(), gy.ravel()], axis=1)
+    disk = disk[np.einsum("ij,ij->i", disk, disk) <= R * R]
+    nd = len(disk)
+    z_b = -pipe_layers * dx
+    # pipe walls (two ghost rings) from below the deepest buffer layer to the pipe exit
+    zs = z_b - depth * dx + np.arange(pipe_layers + depth + 1) * dx
+    wall = []
+    for k in range(2):
+        rr = R + (k + 0.5) * dx
+        nth = int(round(2 * math.pi * rr / dx))
+        th = np.arange(nth) * 2 * math.pi / nth
+        ring = np.stack([rr * np.cos(th), rr * np.sin(th)], axis=1)
+        for z in zs:
+            wall.append(np.concatenate([ring, np.full((nth, 1), z)], axis=1))
+    bound = np.concatenate(wall)
+
+    def layer(z):
+        return np.concatenate([disk, np.full((nd, 1), z)], axis=1)
+
+    # fluid order by age, as insertion produces it: downstream (oldest) first -- the FREE column
+    # from the top, the PIPE layers, BACK, then the BUFFER layers (newest last).  The reference's
+    # bookkeeping relies on it: deletion shifts the inlet tables by every deletion in the block.
+    parts, types = [], []
+    for k in reversed(range(column_layers)):
+        parts.append(layer(k * dx))
+        types.append(np.full(nd, d.FREE))
+    for k in reversed(range(1, pipe_layers)):
+        parts.append(layer(z_b + k * dx))
+        types.append(np.full(nd, d.PIPE))
+    parts.append(layer(z_b))
+    types.append(np.full(nd, d.BACK))
+    for j in range(depth):  # buffer layer j is (j + 1) dx below BACK
+        parts.append(layer(z_b - (j + 1) * dx))
+        types.append(np.full(nd, d.BUFFER))
+    fluid = np.concatenate(parts)
+    fluid[:, :2] += rng.uniform(-0.01 * dx, 0.01 * dx, size=(len(fluid), 2))
+    st = _assemble(s, bound, fluid)
+    nb = len(bound)
+    st.b[nb:] = np.concatenate(types)
+    st.v[nb:] = [0.0, 0.0, jet_speed]
+    free = st.b == d.FREE
+    st.v[free, 0] = 0.05 * air_speed
+    s.max_points = max_points if max_points is not None else st.n + 4 * nd
+    blocks = _blocks(nb, st.n, bound_solver=d.GHOST)
+    fl = blocks[-1]
+    fl.block_type = 6  # inletZone
+    fl.insert_norm = (0.0, 0.0, 1.0)
+    fl.insconst = z_b + 0.02 * dx
+    fl.delete_norm = (0.0, 0.0, 1.0)
+    fl.delconst = (column_layers - 1) * dx - 0.5 * dx
+    fl.aero_norm = (0.0, 0.0, 1.0)
+    fl.aeroconst = 0.0
+    # columns: BACK index and buffer indices, buffer[ii][0] the layer next to BACK
+    first_back = nb + (column_layers + pipe_layers - 1) * nd
+    back = first_back + np.arange(nd)
+    buffer = np.stack([first_back + (j + 1) * nd + np.arange(nd) for j in range(depth)], axis=1)
+    return Case("jet_inlet", s, st, blocks, [InletSpec(len(blocks) - 1, back, buffer)])

@@ -144,6 +144,10 @@ struct fjsph_ctx {
     unsigned long long *log_count = nullptr;
     int64_t log_cap = 0;
     int32_t log_every = 1;
+    /* update_data: insertion / deletion */
+    int32_t *upd_i32 = nullptr;             /* 4 * capacity + 64 scratch                 */
+    unsigned long long *upd_cnt = nullptr;  /* deletions per block                       */
+    int64_t part_id_next = 0, inserted = 0, deleted = 0;
 };
 
 namespace {
@@ -1085,13 +1089,6 @@ int runge_kutta4(fjsph_ctx *c, double logbase, double &rms) {
     return FJSPH_OK;
 }
 
-bool needs_update_data(const fjsph_ctx *c) {
-    for (int64_t b = c->n_bound_blocks; b < (int64_t)c->blocks.size(); ++b) {
-        if (c->blocks[b].block_type == kInletZone) return true;
-        if (c->blocks[b].delconst != kDefaultVal) return true;
-    }
-    return false;
-}
 
 /* Integrator::integrate_no_update (src/Integration.cpp:27-107).  skip_dead: under Runge-Kutta the
  * first pre-pass results on pnp1 are overwritten by Get_First_RK's copy of pn before anything
@@ -1133,9 +1130,173 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
     return FJSPH_OK;
 }
 
+/* update_buffer_region (src/shapes/inlet.cpp:578-640) for every inlet block, in block and
+ * column order: a BACK particle past the insertion plane becomes PIPE, the column's first
+ * BUFFER particle becomes BACK and the column shifts; while the particle count is below
+ * max_points (and the context capacity), a new BUFFER particle one dx upstream of the column's
+ * last one is inserted at the end of the block's reference range. */
+int inlet_advance(fjsph_ctx *c) {
+    if (c->inlets.empty()) return FJSPH_OK;
+    const int64_t limit = std::min<int64_t>(c->s.max_points, c->cap);
+    const int64_t n_old = c->n;
+    int64_t n_new = c->n;
+    std::vector<InsertOp> ops;
+    std::vector<int64_t> ins(c->blocks.size(), 0);
+    std::vector<HostInlet *> order;
+    for (HostInlet &I : c->inlets) order.push_back(&I);
+    std::sort(order.begin(), order.end(), [](HostInlet *a, HostInlet *b) { return a->block < b->block; });
+    int32_t *flag = c->upd_i32;
+    for (HostInlet *Ip : order) {
+        HostInlet &I = *Ip;
+        fjsph_block &B = c->blocks[I.block];
+        if (B.block_type != kInletZone || I.n_back == 0 || I.depth == 0) continue;
+        launch_inlet_cross(WS(c), c->D, I.d_back, I.n_back, B.insert_norm, B.insconst, flag, c->stream);
+        c->launches++;
+        std::vector<int32_t> f(I.n_back), back(I.n_back), buf(I.n_back * I.depth);
+        CU(cudaMemcpyAsync(f.data(), flag, sizeof(int32_t) * I.n_back, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaMemcpyAsync(back.data(), I.d_back, sizeof(int32_t) * I.n_back, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaMemcpyAsync(buf.data(), I.d_buffer, sizeof(int32_t) * buf.size(), cudaMemcpyDeviceToHost, c->stream));
+        TRY(sync(c));
+        bool changed = false;
+        for (int64_t ii = 0; ii < I.n_back; ++ii) {
+            if (!f[ii]) continue;
+            changed = true;
+            int32_t *col = &buf[ii * I.depth];
+            InsertOp op{};
+            op.to_pipe = back[ii];
+            op.to_back = col[0];
+            back[ii] = col[0];
+            for (int64_t jj = 0; jj + 1 < I.depth; ++jj) col[jj] = col[jj + 1];
+            op.dst = -1;
+            if (n_new < limit) {
+                op.src = col[I.depth - 1]; /* the column's last particle before the shift */
+                op.dst = (int32_t)n_new;
+                op.block = I.block;
+                op.key = B.second;
+                op.part_id = c->part_id_next++;
+                for (int k = 0; k < 3; ++k) op.norm[k] = B.insert_norm[k];
+                col[I.depth - 1] = (int32_t)n_new;
+                ++n_new;
+                ++ins[I.block];
+                B.second++;
+                for (size_t jb = I.block + 1; jb < c->blocks.size(); ++jb) {
+                    c->blocks[jb].first++;
+                    c->blocks[jb].second++;
+                }
+            }
+            ops.push_back(op);
+        }
+        if (changed) {
+            CU(cudaMemcpyAsync(I.d_back, back.data(), sizeof(int32_t) * I.n_back, cudaMemcpyHostToDevice, c->stream));
+            CU(cudaMemcpyAsync(I.d_buffer, buf.data(), sizeof(int32_t) * buf.size(), cudaMemcpyHostToDevice, c->stream));
+        }
+    }
+    if (ops.empty()) return FJSPH_OK;
+    /* existing particles of later blocks move up by the insertions before them */
+    BlockShift sh{};
+    int64_t acc = 0;
+    for (size_t b = 0; b < c->blocks.size() && b < (size_t)kMaxBlocks; ++b) {
+        sh.v[b] = acc;
+        acc += ins[b];
+    }
+    if (acc > 0) {
+        launch_shift_keys(c->key, c->blk, n_old, sh, c->stream);
+        c->launches++;
+    }
+    InsertOp *d_ops = reinterpret_cast<InsertOp *>(c->stage);
+    CU(cudaMemcpyAsync(d_ops, ops.data(), sizeof(InsertOp) * ops.size(), cudaMemcpyHostToDevice, c->stream));
+    c->n = n_new;
+    launch_insert(WS(c), c->D, d_ops, (int64_t)ops.size(), c->s.dx, c->stream);
+    c->launches++;
+    if (c->packed_alloc && n_new > n_old) /* new BUFFER particles carry no occlusion inputs */
+        CU(cudaMemsetAsync(c->K.O + n_old, 0, sizeof(float4) * (n_new - n_old), c->stream));
+    c->inserted += n_new - n_old;
+    TRY(sync(c)); /* the host vector `ops` is released on return */
+    return FJSPH_OK;
+}
+
+/* Deletion past the fluid blocks' deletion planes (src/Integration.cpp:127-205, analytic air
+ * source): deleted slots are compacted out in slot order and the remaining reference indices
+ * close up. */
+int delete_particles(fjsph_ctx *c) {
+    DeletePlanes DP{};
+    bool any = false;
+    for (size_t b = c->n_bound_blocks; b < c->blocks.size() && b < (size_t)kMaxBlocks; ++b) {
+        const fjsph_block &B = c->blocks[b];
+        if (B.delconst == kDefaultVal) continue;
+        DP.on[b] = 1;
+        for (int k = 0; k < 3; ++k) DP.norm[b][k] = B.delete_norm[k];
+        DP.c[b] = B.delconst;
+        any = true;
+    }
+    if (!any || c->n == 0) return FJSPH_OK;
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    int32_t *flag = c->upd_i32, *keep = flag + n, *keep_ex = keep + n, *by_ref = keep_ex + n + 1;
+    CU(cudaMemsetAsync(c->upd_cnt, 0, sizeof(unsigned long long) * kMaxBlocks, s));
+    Params P = make_params(c);
+    launch_delete_flags(P, WS(c), DP, flag, keep, c->upd_cnt, s);
+    std::vector<unsigned long long> cnt(kMaxBlocks);
+    CU(cudaMemcpyAsync(cnt.data(), c->upd_cnt, sizeof(unsigned long long) * kMaxBlocks, cudaMemcpyDeviceToHost, s));
+    TRY(sync(c));
+    int64_t total = 0;
+    for (unsigned long long v : cnt) total += (int64_t)v;
+    c->launches++;
+    if (total == 0) return FJSPH_OK;
+    /* new slots (stable order of the kept ones) and closed-up reference indices */
+    int64_t *ref_ex = c->nbr_off; /* the lists are rebuilt at the next search */
+    launch_scan_i32(keep, keep_ex, n, c->G.scan_tmp, s);
+    launch_compact_map(flag, c->key, n, by_ref, nullptr, nullptr, nullptr, nullptr, 0, s);
+    launch_scan_i64(by_ref, ref_ex, n, c->scan_tmp64, s);
+    launch_compact_map(flag, c->key, n, by_ref, keep_ex, ref_ex, c->new_of_old, c->key, 1, s);
+    c->launches += 8;
+    launch_permute(state_fields(WS(c), c->D), state_fields(c->st[c->isp], c->D), c->new_of_old, n, s);
+    std::swap(c->iW, c->isp);
+    DevState &spare = c->st[c->isp];
+    launch_permute_key_blk(c->key, c->blk, spare.part_id, spare.b, c->new_of_old, n, s);
+    const int64_t n2 = n - total;
+    CU(cudaMemcpyAsync(c->key, spare.part_id, sizeof(int64_t) * n2, cudaMemcpyDeviceToDevice, s));
+    CU(cudaMemcpyAsync(c->blk, spare.b, sizeof(int32_t) * n2, cudaMemcpyDeviceToDevice, s));
+    if (c->packed_alloc && c->occ_valid) {
+        float4 *tmp = reinterpret_cast<float4 *>(c->stage);
+        launch_m_permute_f4(c->K.O, tmp, c->new_of_old, n, s);
+        CU(cudaMemcpyAsync(c->K.O, tmp, sizeof(float4) * n2, cudaMemcpyDeviceToDevice, s));
+    }
+    for (HostInlet &I : c->inlets) {
+        launch_remap_i32(I.d_back, I.n_back, c->new_of_old, s);
+        launch_remap_i32(I.d_buffer, I.n_back * I.depth, c->new_of_old, s);
+    }
+    c->launches += 4;
+    int64_t shift = 0;
+    for (size_t b = c->n_bound_blocks; b < c->blocks.size(); ++b) {
+        fjsph_block &B = c->blocks[b];
+        B.first -= shift;
+        if (b < (size_t)kMaxBlocks) shift += (int64_t)cnt[b];
+        B.second -= shift;
+    }
+    c->n = n2;
+    c->deleted += total;
+    return sync(c);
+}
+
+/* Integrator::update_data (src/Integration.cpp:109-226): insertion, zero-density guard
+ * (:116-124), deletion; the neighbour lists and packed inputs are stale afterwards. */
+int update_data(fjsph_ctx *c) {
+    const int64_t n0 = c->n;
+    TRY(inlet_advance(c));
+    launch_density_guard(make_params(c), WS(c), c->stream);
+    c->launches++;
+    TRY(delete_particles(c));
+    if (c->n != n0) {
+        c->nbr_valid = false;
+        mark_full(c);
+    }
+    mark_all(c);
+    return FJSPH_OK;
+}
+
 /* Integrator::integrate (src/Integration.cpp:233-303). */
 int integrate(fjsph_ctx *c, double &step_error) {
-    if (needs_update_data(c)) return FJSPH_E_UNSUPPORTED;
     /* judge / log schedule of the closure: the first residual of every n-th step */
     const int64_t k = c->closure_steps++;
     if (learned_active(c) && c->s.learned_judge_interval > 0 && k % c->s.learned_judge_interval == 0)
@@ -1147,10 +1308,7 @@ int integrate(fjsph_ctx *c, double &step_error) {
     TRY(integrate_no_update(c, step_error, true));
     c->arm = 0;
     TRY(closure_collect(c));
-    /* update_data: zero-density guard (src/Integration.cpp:116-124) and pn = pnp1 */
-    launch_density_guard(make_params(c), WS(c), c->stream);
-    c->launches++;
-    mark_all(c);
+    TRY(update_data(c));
     TRY(copy_state(c, c->iW, c->ipn));
     c->pn_equals_W = true;
     fjsph_settings &I = c->s;
@@ -1269,6 +1427,8 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     c->reorder_tmp_len = 2 * capacity + 1 + capacity / 2048 + 16;
     A(dalloc(c, &c->reorder_tmp, c->reorder_tmp_len));
     A(dalloc(c, &c->dsc, 1));
+    A(dalloc(c, &c->upd_i32, 4 * capacity + 64));
+    A(dalloc(c, &c->upd_cnt, kMaxBlocks));
     if (s->precision == FJSPH_PREC_MIXED) A(alloc_packed(c));
 #undef A
     if (cudaMallocHost(&c->hsc, sizeof(DevScalars)) != cudaSuccess) return fail(FJSPH_E_CUDA);
@@ -1393,11 +1553,42 @@ int fjsph_get_inlet(fjsph_ctx *c, fjsph_inlet *in) {
         if (I.block == in->block) {
             in->n_back = I.n_back;
             in->depth = I.depth;
-            if (in->back) std::copy(I.back_ref.begin(), I.back_ref.end(), in->back);
-            if (in->buffer) std::copy(I.buffer_ref.begin(), I.buffer_ref.end(), in->buffer);
+            if (!in->back && !in->buffer) return FJSPH_OK;
+            if (c->n == 0) { /* no state yet: the tables as given */
+                if (in->back) std::copy(I.back_ref.begin(), I.back_ref.end(), in->back);
+                if (in->buffer) std::copy(I.buffer_ref.begin(), I.buffer_ref.end(), in->buffer);
+                return FJSPH_OK;
+            }
+            /* current tables: device slots -> reference indices */
+            TRY(sync(c));
+            std::vector<int64_t> keys;
+            TRY(download_keys(c, keys));
+            std::vector<int32_t> b(I.n_back), f(I.n_back * I.depth);
+            if (!b.empty()) CU(cudaMemcpy(b.data(), I.d_back, sizeof(int32_t) * b.size(), cudaMemcpyDeviceToHost));
+            if (!f.empty()) CU(cudaMemcpy(f.data(), I.d_buffer, sizeof(int32_t) * f.size(), cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < b.size(); ++k)
+                if (in->back) in->back[k] = (b[k] >= 0 && b[k] < c->n) ? keys[b[k]] : -1;
+            for (size_t k = 0; k < f.size(); ++k)
+                if (in->buffer) in->buffer[k] = (f[k] >= 0 && f[k] < c->n) ? keys[f[k]] : -1;
             return FJSPH_OK;
         }
     return FJSPH_E_ARG;
+}
+
+int fjsph_get_limits(fjsph_ctx *c, fjsph_block *blocks, int32_t max_blocks, int32_t *nblocks) {
+    TRY(check_ctx(c));
+    if (nblocks) *nblocks = (int32_t)c->blocks.size();
+    if (!blocks) return FJSPH_OK;
+    if (max_blocks < (int32_t)c->blocks.size()) return FJSPH_E_ARG;
+    std::copy(c->blocks.begin(), c->blocks.end(), blocks);
+    return FJSPH_OK;
+}
+
+int fjsph_update_counts(fjsph_ctx *c, int64_t *inserted, int64_t *deleted) {
+    TRY(check_ctx(c));
+    if (inserted) *inserted = c->inserted;
+    if (deleted) *deleted = c->deleted;
+    return FJSPH_OK;
 }
 
 int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) {
@@ -1421,6 +1612,10 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         c->reorder_pending = true;
     }
     TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true));
+    if (which == FJSPH_PNP1 && st->part_id) { /* ids of inserted particles continue from here */
+        c->part_id_next = 0;
+        for (int64_t i = 0; i < st->n; ++i) c->part_id_next = std::max<int64_t>(c->part_id_next, st->part_id[i] + 1);
+    }
     if (which == FJSPH_PNP1) {
         c->nbr_valid = false;
         mark_full(c);

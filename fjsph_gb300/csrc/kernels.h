@@ -16,6 +16,35 @@ struct Packed {
     int32_t *bits;
 };
 
+/* ---- update.cu: particle-set changes of update_data ---------------------------------------- */
+struct BlockShift {
+    int64_t v[kMaxBlocks]; /* added to the key of every slot of block b */
+};
+struct InsertOp {
+    int32_t to_pipe, to_back; /* slots whose type changes (old BACK, new BACK)      */
+    int32_t src, dst;         /* copied slot and new slot (dst < 0: no new particle) */
+    int32_t block, pad;
+    int64_t key, part_id;     /* reference index and id of the new particle          */
+    double norm[3];           /* insertion normal of the block                       */
+};
+struct DeletePlanes {
+    int32_t on[kMaxBlocks];
+    double norm[kMaxBlocks][3];
+    double c[kMaxBlocks];
+};
+void launch_inlet_cross(const DevState &W, int D, const int32_t *back, int64_t n_back, const double *norm, double c,
+                        int32_t *flag, cudaStream_t s);
+void launch_shift_keys(int64_t *key, const int32_t *blk, int64_t n, const BlockShift &sh, cudaStream_t s);
+void launch_insert(const DevState &W, int D, const InsertOp *ops, int64_t nops, double dx, cudaStream_t s);
+void launch_delete_flags(const Params &P, const DevState &W, const DeletePlanes &DP, int32_t *flag, int32_t *keep,
+                         unsigned long long *count, cudaStream_t s);
+/* phase 0: by_ref[key[s]] = flag[s]; phase 1 (after the scans): new_of_old and compacted keys */
+void launch_compact_map(const int32_t *flag, const int64_t *key, int64_t n, int32_t *by_ref, const int32_t *keep_ex,
+                        const int64_t *ref_ex_after_scan, int32_t *new_of_old, int64_t *key_out, int phase,
+                        cudaStream_t s);
+void launch_permute_key_blk(const int64_t *key, const int32_t *blk, int64_t *key2, int32_t *blk2,
+                            const int32_t *new_of_old, int64_t n, cudaStream_t s);
+
 /* ---- mlp_train.cu ------------------------------------------------------------------------- */
 namespace mlp {
 /* FP32 parameters (host) -> device master copy and its BF16 forward / transposed copies */
@@ -88,7 +117,7 @@ void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, c
                           cudaStream_t s);
 void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
                     const Closure &C, cudaStream_t s);
-/* dst[new_of_old[i]] = src[i] for a per-slot float4 array */
+/* dst[new_of_old[i]] = src[i] for a per-slot float4 array (entries mapped to -1 are dropped) */
 void launch_m_permute_f4(const float4 *src, float4 *dst, const int32_t *new_of_old, int64_t n, cudaStream_t s);
 
 /* ---- integrate.cu ------------------------------------------------------------------------- */
@@ -144,7 +173,7 @@ struct FieldList {
 };
 /* Per-state fields (excludes the shared key/blk arrays). */
 FieldList state_fields(const DevState &S, int D);
-/* dst[new_of_old[o]] = src[o] for every field, o in [0, n). */
+/* dst[new_of_old[o]] = src[o] for every field, o in [0, n); entries with new_of_old < 0 are dropped. */
 void launch_permute(const FieldList &src, const FieldList &dst, const int32_t *new_of_old, int64_t n, cudaStream_t s);
 /* dst = src over [0, n) for every field. */
 void launch_copy(const FieldList &src, const FieldList &dst, int64_t n, cudaStream_t s);

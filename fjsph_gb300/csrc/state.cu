@@ -41,6 +41,7 @@ __global__ void k_permute(FieldList src, FieldList dst, const int32_t *new_of_ol
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= n) return;
     const int64_t t = new_of_old ? new_of_old[o] : o;
+    if (t < 0) return; /* deleted */
     for (int k = 0; k < src.n64; ++k) dst.f64[k][t] = src.f64[k][o];
     for (int k = 0; k < src.ni64; ++k) dst.i64[k][t] = src.i64[k][o];
     for (int k = 0; k < src.ni32; ++k) dst.i32[k][t] = src.i32[k][o];

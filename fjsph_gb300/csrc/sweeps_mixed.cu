@@ -900,7 +900,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
 
 __global__ void k_permute_f4(const float4 *src, float4 *dst, const int32_t *new_of_old, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) dst[new_of_old[i]] = src[i];
+    if (i < n && new_of_old[i] >= 0) dst[new_of_old[i]] = src[i];
 }
 
 inline unsigned fgrid(const Params &P) { return grid_for(P.n - P.nb, kThreads); }

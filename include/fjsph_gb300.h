@@ -188,7 +188,12 @@ int fjsph_get_settings(fjsph_ctx *ctx, fjsph_settings *s);
 /* LIMITS (src/Var.h:883) and the inlet back/buffer tables (src/shapes/inlet.cpp:578-640). */
 int fjsph_set_limits(fjsph_ctx *ctx, const fjsph_block *blocks, int32_t nblocks, int64_t n_bound_blocks);
 int fjsph_set_inlet(fjsph_ctx *ctx, const fjsph_inlet *inlet);
-int fjsph_get_inlet(fjsph_ctx *ctx, fjsph_inlet *inlet);
+int fjsph_get_inlet(fjsph_ctx *ctx, fjsph_inlet *inlet); /* current tables, reference indices */
+/* The LIMITS table as the particle-set changes of update_data left it (ranges move with
+ * insertion and deletion, src/shapes/inlet.cpp:621-626, src/Integration.cpp:190-205). */
+int fjsph_get_limits(fjsph_ctx *ctx, fjsph_block *blocks, int32_t max_blocks, int32_t *nblocks);
+/* Particles inserted and deleted by update_data since the context was created. */
+int fjsph_update_counts(fjsph_ctx *ctx, int64_t *inserted, int64_t *deleted);
 /* Replaces the SPHState hand-over between Integrator and its callers (src/Integration.h:15-68). */
 int fjsph_state_upload(fjsph_ctx *ctx, int32_t which, const fjsph_state_view *st);
 int fjsph_state_download(fjsph_ctx *ctx, int32_t which, fjsph_state_view *st);

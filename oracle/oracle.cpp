@@ -1859,6 +1859,19 @@ int orc_set_limits(orc_sim *o, const fjsph_block *blocks, int32_t nblocks, int64
     return 0;
 }
 
+int orc_get_limits(orc_sim *o, fjsph_block *blocks, int32_t max_blocks, int32_t *nblocks) {
+    if (nblocks) *nblocks = (int32_t)o->limits.size();
+    if (!blocks) return 0;
+    if (max_blocks < (int32_t)o->limits.size()) return -1;
+    for (size_t b = 0; b < o->limits.size(); ++b) blocks[b] = o->limits[b].d;
+    return 0;
+}
+
+int orc_update_counts(orc_sim *o, int64_t *deleted) {
+    if (deleted) *deleted = o->delete_count;
+    return 0;
+}
+
 int orc_set_inlet(orc_sim *o, const fjsph_inlet *in) {
     if (in->block < 0 || in->block >= (int32_t)o->limits.size()) return -1;
     Block &B = o->limits[in->block];

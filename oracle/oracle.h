@@ -28,6 +28,8 @@ void orc_get_settings(orc_sim *o, fjsph_settings *s);
 int orc_set_limits(orc_sim *o, const fjsph_block *blocks, int32_t nblocks, int64_t n_bound_blocks);
 int orc_set_inlet(orc_sim *o, const fjsph_inlet *inlet);
 int orc_get_inlet(orc_sim *o, fjsph_inlet *inlet);
+int orc_get_limits(orc_sim *o, fjsph_block *blocks, int32_t max_blocks, int32_t *nblocks);
+int orc_update_counts(orc_sim *o, int64_t *deleted);
 int orc_set_state(orc_sim *o, int32_t which, const fjsph_state_view *st);
 int orc_get_state(orc_sim *o, int32_t which, fjsph_state_view *st);
 int64_t orc_particle_count(orc_sim *o);

@@ -28,6 +28,8 @@ _PROTO = {
     "orc_set_limits": (C.c_int, [_P, C.POINTER(d.Block), C.c_int32, C.c_int64]),
     "orc_set_inlet": (C.c_int, [_P, C.POINTER(d.Inlet)]),
     "orc_get_inlet": (C.c_int, [_P, C.POINTER(d.Inlet)]),
+    "orc_get_limits": (C.c_int, [_P, C.POINTER(d.Block), C.c_int32, C.POINTER(C.c_int32)]),
+    "orc_update_counts": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "orc_set_state": (C.c_int, [_P, C.c_int32, C.POINTER(d.StateView)]),
     "orc_get_state": (C.c_int, [_P, C.c_int32, C.POINTER(d.StateView)]),
     "orc_particle_count": (C.c_int64, [_P]),
@@ -213,6 +215,29 @@ class Oracle:
         for _ in range(n_steps):
             r = self.integrate()
         return r
+
+    def limits(self) -> list:
+        """(first, second) of every LIMITS entry as update_data left them."""
+        nb = C.c_int32()
+        self._l.orc_get_limits(self._h, None, 0, C.byref(nb))
+        arr = (d.Block * nb.value)()
+        self._l.orc_get_limits(self._h, arr, nb.value, C.byref(nb))
+        return [(arr[i].first, arr[i].second) for i in range(nb.value)]
+
+    def get_inlet(self, block: int, n_back: int, depth: int):
+        back = np.zeros(n_back, dtype=np.int64)
+        buf = np.zeros(n_back * depth, dtype=np.int64)
+        c = d.Inlet()
+        c.block, c.n_back, c.depth = block, n_back, depth
+        c.back = back.ctypes.data_as(_i64p)
+        c.buffer = buf.ctypes.data_as(_i64p)
+        self._l.orc_get_inlet(self._h, C.byref(c))
+        return back, buf.reshape(n_back, depth)
+
+    def deleted(self) -> int:
+        v = C.c_int64()
+        self._l.orc_update_counts(self._h, C.byref(v))
+        return v.value
 
     def step_report(self) -> dict:
         out = (C.c_double * 5)()
