@@ -219,6 +219,29 @@ class Context:
         check("fjsph_get_inlet", self._lib.fjsph_get_inlet(self._h, C.byref(c)))
         return back, buf.reshape(n_back, depth)
 
+    # ---- independent simulations sharing the context --------------------------------------------
+    def set_groups(self, first, v_inf) -> None:
+        """Groups of reference indices [first[g], first[g+1]) with their free-stream velocities."""
+        f = np.ascontiguousarray(first, dtype=np.int64)
+        vi = np.ascontiguousarray(np.asarray(v_inf, dtype=np.float64).reshape(-1, 3))
+        self._ngroups = len(f) - 1
+        check("fjsph_set_groups", self._lib.fjsph_set_groups(
+            self._h, self._ngroups, f.ctypes.data_as(C.POINTER(C.c_int64)), vi.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def integrate_groups(self, n_steps: int, graph: bool = True) -> None:
+        check("fjsph_integrate_groups", self._lib.fjsph_integrate_groups(self._h, int(n_steps), int(graph)))
+
+    def group_report(self) -> dict:
+        g = self._ngroups
+        out = {k: np.zeros(g) for k in ("time", "dt", "cfl", "err")}
+        steps = np.zeros(g, dtype=np.int64)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        check("fjsph_group_report", self._lib.fjsph_group_report(
+            self._h, dp(out["time"]), dp(out["dt"]), dp(out["cfl"]), dp(out["err"]),
+            steps.ctypes.data_as(C.POINTER(C.c_int64))))
+        out["steps"] = steps
+        return out
+
     def update_counts(self) -> tuple[int, int]:
         """Particles inserted and deleted by update_data since the context was created."""
         a, b = C.c_int64(), C.c_int64()

@@ -411,3 +411,58 @@ def jet_inlet(D: float = 1e-3, dx: float = 5e-5, jet_speed: float = 10.0, air_sp
     back = first_back + np.arange(nd)
     buffer = np.stack([first_back + (j + 1) * nd + np.arange(nd) for j in range(depth)], axis=1)
     return Case("jet_inlet", s, st, blocks, [InletSpec(len(blocks) - 1, back, buffer)])
+
+
+@dataclass
+class DropletBatch:
+    """Independent droplets in one state: droplet g is reference indices first[g]..first[g+1]-1
+    with free-stream velocity v_inf[g]."""
+
+    case: Case
+    first: np.ndarray
+    v_inf: np.ndarray
+    counts: np.ndarray
+    diam: np.ndarray
+    we: np.ndarray
+
+    def single(self, g: int) -> Case:
+        """Droplet g alone, as its own case (same settings, its own free stream)."""
+        s = self.case.settings.copy()
+        s.v_inf[:] = list(self.v_inf[g])
+        st = self.case.state.take(np.arange(self.first[g], self.first[g + 1]))
+        st.part_id[:] = np.arange(st.n)
+        return Case(f"droplet_{g}", s, st, _blocks(0, st.n))
+
+
+def droplet_batch(n_drops: int = 256, n_min: int = 2000, n_max: int = 60000, dx: float = 5e-5,
+                  we_range=(10.0, 500.0), seed: int = 4242, cfl: float = 0.5) -> DropletBatch:
+    """Config-4 batch: n_drops spherical droplets of the config-2 liquid, particle counts
+    log-uniform in [n_min, n_max] (diameter from the count at spacing dx), each in its own air
+    stream along +x with speed set by a Weber number drawn from we_range (We = rho_air U^2 d / sigma).
+    Droplets sit on a cubic grid with gaps of 8 smoothing lengths, so no two interact."""
+    base = droplet_3d(diam=4 * dx, dx=dx, cfl=cfl)
+    s = base.settings
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_drops)).astype(np.int64)
+    diam = dx * np.cbrt(6.0 * counts / math.pi)
+    we = rng.uniform(we_range[0], we_range[1], n_drops)
+    speed = np.sqrt(we * s.sig / (s.rho_g * diam))
+    pitch = diam.max() + 8.0 * s.H + 2 * dx
+    side = int(math.ceil(n_drops ** (1.0 / 3.0)))
+    parts, first, vinf = [], [0], []
+    for g in range(n_drops):
+        ix, iy, iz = g % side, (g // side) % side, g // (side * side)
+        centre = np.array([ix, iy, iz], dtype=np.float64) * pitch
+        pts = _sphere_points(diam[g], dx, centre)
+        pts += rng.uniform(-0.01 * dx, 0.01 * dx, size=pts.shape)
+        parts.append(pts)
+        first.append(first[-1] + len(pts))
+        vinf.append([speed[g], 0.0, 0.0])
+    st = _assemble(s, np.zeros((0, 3)), np.concatenate(parts))
+    vinf = np.array(vinf)
+    first = np.array(first, dtype=np.int64)
+    for g in range(n_drops):
+        st.cellV[first[g]:first[g + 1]] = vinf[g]
+    s.max_points = st.n
+    case = Case("droplet_batch", s, st, _blocks(0, st.n))
+    return DropletBatch(case, first, vinf, np.diff(first), diam, we)

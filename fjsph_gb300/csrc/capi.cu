@@ -148,6 +148,17 @@ struct fjsph_ctx {
     int32_t *upd_i32 = nullptr;             /* 4 * capacity + 64 scratch                 */
     unsigned long long *upd_cnt = nullptr;  /* deletions per block                       */
     int64_t part_id_next = 0, inserted = 0, deleted = 0;
+    /* independent simulations sharing the context (groups) */
+    int32_t ngrp = 0;
+    int32_t *grp = nullptr;          /* group of every slot (permuted with the slots) */
+    std::vector<int64_t> grp_first;  /* reference-index boundaries, ngrp + 1          */
+    double *g_vinf = nullptr;
+    GroupDev gs{};
+    double *g_red = nullptr, *g_sum = nullptr;
+    bool graph_mode = false;         /* steps enqueue without host round trips        */
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t graph_launches[4] = {0, 0, 0, 0};
+    int64_t graph_uses = 0;
 };
 
 namespace {
@@ -297,6 +308,8 @@ Params make_params(const fjsph_ctx *c) {
         P.grav[k] = s.grav[k];
         P.v_inf[k] = s.v_inf[k];
     }
+    P.grp = c->ngrp > 0 ? c->grp : nullptr;
+    P.g_vinf = c->g_vinf;
     P.L = s.L;
     P.A_sphere = s.A_sphere;
     P.A_plate = s.A_plate;
@@ -347,6 +360,10 @@ DevNbr make_nbr(const fjsph_ctx *c) {
 }
 
 bool mixed(const fjsph_ctx *c) { return c->s.precision == FJSPH_PREC_MIXED; }
+bool grouped(const fjsph_ctx *c) { return c->ngrp > 0; }
+/* time step and npd as the kernels read them: one scalar, or one per group */
+const double *dt_ptr(const fjsph_ctx *c) { return grouped(c) ? c->gs.dt : &c->dsc->dt; }
+const double *npd_ptr(const fjsph_ctx *c) { return grouped(c) ? c->gs.npd : &c->dsc->npd; }
 
 int alloc_packed(fjsph_ctx *c) {
     if (c->packed_alloc) return FJSPH_OK;
@@ -567,12 +584,16 @@ int reorder_states(fjsph_ctx *c, const Params &P) {
     cudaStream_t s = c->stream;
     launch_reorder_map(P, c->G, c->new_of_old, c->reorder_tmp, c->reorder_tmp_len, s);
     c->launches += 5;
-    /* permute pn and W through the spare state */
+    /* permute pn and W through the spare state (in graph mode the result is copied back, so
+     * that every captured launch keeps addressing the same buffers) */
     for (int which = 0; which < 2; ++which) {
         int &role = which == 0 ? c->ipn : c->iW;
         launch_permute(state_fields(c->st[role], c->D), state_fields(c->st[c->isp], c->D), c->new_of_old, c->n, s);
-        std::swap(role, c->isp);
-        c->launches += 1;
+        if (c->graph_mode)
+            launch_copy(state_fields(c->st[c->isp], c->D), state_fields(c->st[role], c->D), c->n, s);
+        else
+            std::swap(role, c->isp);
+        c->launches += c->graph_mode ? 2 : 1;
     }
     /* shared per-slot arrays: key and blk (through the spare state's i64/i32 scratch) */
     {
@@ -581,9 +602,15 @@ int reorder_states(fjsph_ctx *c, const Params &P) {
         b.i64[b.ni64++] = c->st[c->isp].part_id;
         a.i32[a.ni32++] = c->blk;
         b.i32[b.ni32++] = c->st[c->isp].b;
+        if (grouped(c)) {
+            a.i32[a.ni32++] = c->grp;
+            b.i32[b.ni32++] = c->st[c->isp].surf;
+        }
         launch_permute(a, b, c->new_of_old, c->n, s);
         CU(cudaMemcpyAsync(c->key, c->st[c->isp].part_id, sizeof(int64_t) * c->n, cudaMemcpyDeviceToDevice, s));
         CU(cudaMemcpyAsync(c->blk, c->st[c->isp].b, sizeof(int32_t) * c->n, cudaMemcpyDeviceToDevice, s));
+        if (grouped(c))
+            CU(cudaMemcpyAsync(c->grp, c->st[c->isp].surf, sizeof(int32_t) * c->n, cudaMemcpyDeviceToDevice, s));
         c->launches += 1;
     }
     for (HostInlet &I : c->inlets) {
@@ -634,8 +661,18 @@ int search(fjsph_ctx *c) {
         launch_slice_width(c->nbr_counts, c->n, c->slice_w, s);
         launch_scan_i64(c->slice_w, c->slice_off, nslices, c->scan_tmp64, s);
         c->launches += 4;
-        CU(cudaMemcpyAsync(&c->hsc->red[14], c->slice_off + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     }
+    if (c->graph_mode) {
+        /* no host round trip: the lists must fit the storage sized before capture; the fill
+         * raises a device status bit otherwise */
+        launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? c->nbr_pair : nullptr, c->slice_off,
+                        c->nbr_counts, c->nbr_cap, &c->dsc->status, s);
+        c->launches += 1;
+        c->nbr_valid = true;
+        return FJSPH_OK;
+    }
+    if (mixed(c))
+        CU(cudaMemcpyAsync(&c->hsc->red[14], c->slice_off + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     int64_t total = 0, storage = 0, grid[4] = {0, 0, 0, 0};
     CU(cudaMemcpyAsync(&c->hsc->red[15], c->nbr_off + c->n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(&c->hsc->red[10], c->G.grid, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -665,7 +702,7 @@ int search(fjsph_ctx *c) {
     }
     if (mixed(c)) TRY(alloc_packed(c));
     launch_nbr_fill(P, c->xs, c->G, c->nbr_off, c->nbr_idx, mixed(c) ? c->nbr_pair : nullptr, c->slice_off,
-                    c->nbr_counts, s);
+                    c->nbr_counts, c->nbr_cap, &c->dsc->status, s);
     c->launches += 1;
     c->n_pairs = total;
     c->nbr_storage = mixed(c) ? storage : total;
@@ -677,6 +714,21 @@ int search(fjsph_ctx *c) {
 __global__ void k_finish_npd(DevScalars *d, double inv_n) { d->npd = d->red[0] * inv_n; }
 __global__ void k_set_scalar(double *dst, double v) { *dst = v; }
 
+/* npd = mean kernel sum over all particles (per group when the context holds several) */
+int finish_npd(fjsph_ctx *c) {
+    if (grouped(c)) {
+        CU(cudaMemsetAsync(c->g_sum, 0, sizeof(double) * c->ngrp, c->stream));
+        launch_group_sum(c->grp, c->npd_part, 0, c->n, c->g_sum, c->stream);
+        launch_group_npd(c->gs.npd, c->g_sum, c->gs.count, c->ngrp, c->stream);
+        c->launches += 3;
+        return FJSPH_OK;
+    }
+    launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
+    k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
+    c->launches += 4;
+    return FJSPH_OK;
+}
+
 int prestep_npd(fjsph_ctx *c, const Params &P) {
     Section sec(c, PASS_PRESTEP);
     if (mixed(c)) {
@@ -685,10 +737,7 @@ int prestep_npd(fjsph_ctx *c, const Params &P) {
     } else {
         launch_dsph_prestep(P, WS(c), make_nbr(c), c->npd_part, c->stream);
     }
-    launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
-    k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
-    c->launches += 4;
-    return FJSPH_OK;
+    return finish_npd(c);
 }
 
 /* npd only (Runge-Kutta first pre-pass, see integrate_no_update) */
@@ -700,10 +749,7 @@ int npd_only(fjsph_ctx *c, const Params &P) {
     } else {
         launch_npd_only(P, WS(c), make_nbr(c), c->npd_part, c->stream);
     }
-    launch_sum(c->npd_part, c->n, c->S.part, c->S.part_len, &c->dsc->red[0], c->stream);
-    k_finish_npd<<<1, 1, 0, c->stream>>>(c->dsc, 1.0 / double(c->n));
-    c->launches += 4;
-    return FJSPH_OK;
+    return finish_npd(c);
 }
 
 int prestep_passes(fjsph_ctx *c) {
@@ -853,13 +899,13 @@ int resid(fjsph_ctx *c, const Params &P) {
         ensure_pack(c);
         const Closure C = next_closure(c);
         if (C.mode == kClosureJudge) CU(cudaMemsetAsync(c->judge_dev, 0, 3 * sizeof(double), c->stream));
-        launch_m_resid(P, WS(c), make_nbr(c), c->K, &c->dsc->npd, C, c->stream);
+        launch_m_resid(P, WS(c), make_nbr(c), c->K, npd_ptr(c), C, c->stream);
         if (C.mode == kClosureJudge) {
             CU(cudaMemcpyAsync(c->judge_host, c->judge_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
             c->judge_pending = true;
         }
     } else {
-        launch_resid(P, WS(c), make_nbr(c), &c->dsc->npd, c->stream);
+        launch_resid(P, WS(c), make_nbr(c), npd_ptr(c), c->stream);
     }
     return FJSPH_OK;
 }
@@ -880,7 +926,7 @@ DevInlet dev_inlet(const fjsph_ctx *c, const HostInlet &I) {
 void inlet_buffers(fjsph_ctx *c, const Params &P, int mode, double dt_scale) {
     for (const HostInlet &I : c->inlets) {
         if (I.n_back == 0 || I.depth == 0) continue;
-        launch_inlet_buffers(P, PN(c), WS(c), c->S, dev_inlet(c, I), mode, &c->dsc->dt, dt_scale, c->stream);
+        launch_inlet_buffers(P, PN(c), WS(c), c->S, dev_inlet(c, I), mode, dt_ptr(c), dt_scale, c->stream);
         c->launches++;
     }
 }
@@ -892,13 +938,13 @@ int rk_intermediate(fjsph_ctx *c, int stage, double dt_scale) {
     TRY(boundary_section(c, P, 0));
     const double sum_w = stage == 2 ? 2.0 : (stage == 3 ? 1.0 : 0.0);
     if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
-        launch_bound_rho_update(P, PN(c), WS(c), c->S, 0, sum_w, &c->dsc->dt, dt_scale, s);
+        launch_bound_rho_update(P, PN(c), WS(c), c->S, 0, sum_w, dt_ptr(c), dt_scale, s);
         c->launches++;
     }
     TRY(resid(c, P));
     {
         Section sec(c, PASS_UPDATE);
-        launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, &c->dsc->dt, dt_scale, s);
+        launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, dt_ptr(c), dt_scale, s);
     }
     c->launches += 2;
     inlet_buffers(c, P, 0, dt_scale);
@@ -912,7 +958,7 @@ int rk_final(fjsph_ctx *c) {
     cudaStream_t s = c->stream;
     TRY(boundary_section(c, P, 0));
     if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
-        launch_bound_rho_update(P, PN(c), WS(c), c->S, 1, 0.0, &c->dsc->dt, 1.0, s);
+        launch_bound_rho_update(P, PN(c), WS(c), c->S, 1, 0.0, dt_ptr(c), 1.0, s);
         c->launches++;
     }
     TRY(resid(c, P));
@@ -920,7 +966,7 @@ int rk_final(fjsph_ctx *c) {
         Section sec(c, PASS_UPDATE);
         for (int k = 0; k < c->D; ++k)
             CU(cudaMemcpyAsync(c->S.xsnap[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
-        launch_rk_final_update(P, PN(c), WS(c), c->S, &c->dsc->dt, s);
+        launch_rk_final_update(P, PN(c), WS(c), c->S, dt_ptr(c), s);
     }
     c->launches += 2;
     inlet_buffers(c, P, 1, 1.0);
@@ -1005,10 +1051,10 @@ int nb_iter(fjsph_ctx *c) {
     TRY(resid(c, P));
     c->launches++;
     if (has_solver(c, FJSPH_DBC) || has_solver(c, FJSPH_GHOST)) {
-        launch_bound_rho_update(P, PN(c), WS(c), c->S, 2, 0.0, &c->dsc->dt, 1.0, s);
+        launch_bound_rho_update(P, PN(c), WS(c), c->S, 2, 0.0, dt_ptr(c), 1.0, s);
         c->launches++;
     }
-    launch_nb_update(P, PN(c), WS(c), &c->dsc->dt, s);
+    launch_nb_update(P, PN(c), WS(c), dt_ptr(c), s);
     c->launches++;
     inlet_buffers(c, P, 2, 1.0);
     mark_all(c);
@@ -1335,6 +1381,111 @@ int integrate(fjsph_ctx *c, double &step_error) {
     return FJSPH_OK;
 }
 
+/* ---- independent simulations sharing the context (groups) ------------------------------------ */
+GroupConst group_const(const fjsph_ctx *c) {
+    const fjsph_settings &s = c->s;
+    GroupConst K;
+    K.rho_rest = s.rho_rest;
+    K.H = s.H;
+    K.H_sq = s.H_sq;
+    K.mu = s.mu;
+    K.speed_sound = s.speed_sound;
+    K.dt_min = s.delta_t_min;
+    K.dt_max = s.delta_t_max;
+    K.last_frame_time = s.last_frame_time;
+    K.frame_interval = s.frame_time_interval;
+    K.min_residual = s.min_residual;
+    K.rho_max_iter = s.rho_max_iter;
+    K.cfl_min = s.cfl_min;
+    K.cfl_max = s.cfl_max;
+    K.cfl_step = s.cfl_step;
+    K.subits_factor = s.subits_factor;
+    K.max_subits = s.max_subits;
+    K.n_stable_limit = s.n_stable_limit;
+    K.n_unstable_limit = s.n_unstable_limit;
+    K.ale = (s.variant & FJSPH_VAR_ALE) ? 1 : 0;
+    return K;
+}
+
+/* find_timestep per group: reductions and the scalar tail on the device */
+int group_timestep(fjsph_ctx *c) {
+    Params P = make_params(c);
+    Section sec(c, PASS_REDUCE);
+    launch_group_timestep(P, WS(c), c->g_red, c->ngrp, c->stream);
+    launch_group_dt(c->gs, c->g_red, c->ngrp, group_const(c), c->stream);
+    c->launches += 3;
+    return FJSPH_OK;
+}
+
+/* log10 RMS position change per group against ref: mode 0 sets logbase, mode 1 the error */
+int group_err(fjsph_ctx *c, double *const ref[3], int mode) {
+    Params P = make_params(c);
+    Section sec(c, PASS_REDUCE);
+    CU(cudaMemsetAsync(c->g_sum, 0, sizeof(double) * c->ngrp, c->stream));
+    launch_group_sq_disp(P, WS(c), ref, c->g_sum, c->stream);
+    launch_group_err(c->gs, c->g_sum, c->ngrp, mode, c->stream);
+    c->launches += 3;
+    return FJSPH_OK;
+}
+
+/* One Integrator::integrate of every group (Runge-Kutta, no insertion or deletion): the same
+ * pass sequence as the single-simulation step, with every scalar decision made per group on the
+ * device, so nothing waits for the host. */
+int group_step(fjsph_ctx *c) {
+    TRY(group_timestep(c));
+    TRY(search(c));
+    if (c->s.st_model == FJSPH_ST_PAIRWISE) TRY(npd_only(c, make_params(c)));
+    if (!c->pn_equals_W) TRY(copy_state(c, c->ipn, c->iW));
+    TRY(rk_intermediate(c, 1, 0.5));
+    TRY(group_err(c, PN(c).x, 0));
+    TRY(search(c));
+    TRY(prestep_passes(c));
+    launch_rk_init_sums(make_params(c), PN(c), WS(c), c->S, c->stream);
+    c->launches++;
+    TRY(rk_intermediate(c, 2, 0.5));
+    TRY(rk_intermediate(c, 3, 1.0));
+    TRY(rk_final(c));
+    TRY(group_err(c, c->S.xsnap, 1));
+    launch_density_guard(make_params(c), WS(c), c->stream);
+    c->launches++;
+    mark_all(c);
+    TRY(copy_state(c, c->iW, c->ipn));
+    c->pn_equals_W = true;
+    launch_group_adapt(c->gs, c->ngrp, group_const(c), c->stream);
+    c->launches++;
+    return FJSPH_OK;
+}
+
+/* group of every slot from its reference index */
+int upload_groups(fjsph_ctx *c) {
+    if (!grouped(c) || c->n == 0) return FJSPH_OK;
+    std::vector<int64_t> keys;
+    TRY(download_keys(c, keys));
+    std::vector<int32_t> g(c->n);
+    for (int64_t s = 0; s < c->n; ++s) {
+        const auto it = std::upper_bound(c->grp_first.begin(), c->grp_first.end(), keys[s]);
+        g[s] = (int32_t)(it - c->grp_first.begin()) - 1;
+    }
+    CU(cudaMemcpy(c->grp, g.data(), sizeof(int32_t) * c->n, cudaMemcpyHostToDevice));
+    return FJSPH_OK;
+}
+
+int graph_release(fjsph_ctx *c) {
+    for (cudaGraphExec_t &g : c->graph)
+        if (g) {
+            CU(cudaGraphExecDestroy(g));
+            g = nullptr;
+        }
+    return FJSPH_OK;
+}
+
+/* which searches of the next step re-order the particles (bit 0: first, bit 1: second) */
+int graph_variant(const fjsph_ctx *c) {
+    const int64_t iv = c->s.reorder_interval;
+    if (iv <= 0) return 0;
+    return ((c->searches % iv) == 0 ? 1 : 0) | (((c->searches + 1) % iv) == 0 ? 2 : 0);
+}
+
 int check_ctx(fjsph_ctx *c) { return c ? FJSPH_OK : FJSPH_E_ARG; }
 int need_state(fjsph_ctx *c) { return (c && c->n > 0) ? FJSPH_OK : FJSPH_E_STATE; }
 int need_nbr(fjsph_ctx *c) {
@@ -1447,6 +1598,7 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
 int fjsph_ctx_destroy(fjsph_ctx *c) {
     if (!c) return FJSPH_E_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    graph_release(c);
     for (HostInlet &I : c->inlets) {
         if (I.d_back) cudaFree(I.d_back);
         if (I.d_buffer) cudaFree(I.d_buffer);
@@ -1612,6 +1764,7 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         c->reorder_pending = true;
     }
     TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true));
+    if (grouped(c)) TRY(upload_groups(c));
     if (which == FJSPH_PNP1 && st->part_id) { /* ids of inserted particles continue from here */
         c->part_id_next = 0;
         for (int64_t i = 0; i < st->n; ++i) c->part_id_next = std::max<int64_t>(c->part_id_next, st->part_id[i] + 1);
@@ -1959,6 +2112,159 @@ int fjsph_profile_read(fjsph_ctx *c, double *ms, int64_t *launches) {
 const char *fjsph_profile_pass_name(int32_t k) {
     if (k < 0 || k >= PASS_COUNT) return "";
     return kPassNames[k];
+}
+
+/* ---- independent simulations (groups) -------------------------------------------------------- */
+int fjsph_set_groups(fjsph_ctx *c, int32_t ngroups, const int64_t *first, const double *v_inf) {
+    TRY(check_ctx(c));
+    if (ngroups <= 0 || !first || !v_inf || c->blocks.empty()) return FJSPH_E_ARG;
+    const int64_t n_ref = c->blocks.back().second;
+    if (first[0] != 0 || first[ngroups] != n_ref) return FJSPH_E_ARG;
+    for (int32_t g = 0; g < ngroups; ++g)
+        if (first[g + 1] <= first[g]) return FJSPH_E_ARG;
+    /* the device step of groups covers Runge-Kutta without insertion or deletion */
+    if (c->s.solver_type != FJSPH_RUNGE_KUTTA || !c->inlets.empty()) return FJSPH_E_UNSUPPORTED;
+    for (const fjsph_block &B : c->blocks)
+        if (B.delconst != kDefaultVal || B.block_type == kInletZone) return FJSPH_E_UNSUPPORTED;
+    TRY(sync(c));
+    TRY(graph_release(c));
+    if (c->ngrp != ngroups) {
+        TRY(dfree(c, c->g_vinf));
+        TRY(dfree(c, c->g_red));
+        TRY(dfree(c, c->g_sum));
+        double **d8[] = {&c->gs.dt, &c->gs.npd, &c->gs.time, &c->gs.cfl, &c->gs.maxShift, &c->gs.maxRho_pc, &c->gs.logbase,
+                         &c->gs.err};
+        for (double **a : d8) TRY(dfree(c, *a));
+        TRY(dfree(c, c->gs.n_stable));
+        TRY(dfree(c, c->gs.n_unstable));
+        TRY(dfree(c, c->gs.steps));
+        TRY(dfree(c, c->gs.nfluid));
+        TRY(dfree(c, c->gs.count));
+        TRY(dalloc(c, &c->g_vinf, 3 * ngroups));
+        TRY(dalloc(c, &c->g_red, 8 * ngroups));
+        TRY(dalloc(c, &c->g_sum, ngroups));
+        for (double **a : d8) TRY(dalloc(c, a, ngroups));
+        TRY(dalloc(c, &c->gs.n_stable, ngroups));
+        TRY(dalloc(c, &c->gs.n_unstable, ngroups));
+        TRY(dalloc(c, &c->gs.steps, ngroups));
+        TRY(dalloc(c, &c->gs.nfluid, ngroups));
+        TRY(dalloc(c, &c->gs.count, ngroups));
+    }
+    if (!c->grp) TRY(dalloc(c, &c->grp, c->cap));
+    c->ngrp = ngroups;
+    c->grp_first.assign(first, first + ngroups + 1);
+    const int64_t nb_ref = c->n_bound_blocks > 0 ? c->blocks[c->n_bound_blocks - 1].second : 0;
+    std::vector<int64_t> cnt(ngroups), nf(ngroups), zero(ngroups, 0);
+    std::vector<int32_t> ns(ngroups, c->s.n_stable), nu(ngroups, c->s.n_unstable);
+    std::vector<double> dt(ngroups, c->s.delta_t), t(ngroups, c->s.current_time), cfl(ngroups, c->s.cfl),
+        shift(ngroups, kEps), z(ngroups, 0.0);
+    for (int32_t g = 0; g < ngroups; ++g) {
+        cnt[g] = first[g + 1] - first[g];
+        nf[g] = std::max<int64_t>(0, first[g + 1] - std::max(first[g], nb_ref));
+        if (nf[g] == 0) return FJSPH_E_ARG;
+    }
+    cudaStream_t s = c->stream;
+    CU(cudaMemcpyAsync(c->g_vinf, v_inf, sizeof(double) * 3 * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.dt, dt.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.time, t.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.cfl, cfl.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.maxShift, shift.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.maxRho_pc, z.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.logbase, z.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.err, z.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.npd, z.data(), sizeof(double) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.n_stable, ns.data(), sizeof(int32_t) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.n_unstable, nu.data(), sizeof(int32_t) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.steps, zero.data(), sizeof(int64_t) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.nfluid, nf.data(), sizeof(int64_t) * ngroups, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(c->gs.count, cnt.data(), sizeof(int64_t) * ngroups, cudaMemcpyHostToDevice, s));
+    TRY(sync(c));
+    return upload_groups(c);
+}
+
+int fjsph_integrate_groups(fjsph_ctx *c, int32_t n_steps, int32_t use_graph) {
+    TRY(need_state(c));
+    if (!grouped(c)) return FJSPH_E_STATE;
+    if (n_steps < 0) return FJSPH_E_ARG;
+    int32_t k = 0;
+    if (use_graph) {
+        /* the captured step replays the host decisions of a steady step: settle the lists, the
+         * table size and the first re-ordering with one ordinary step first */
+        if (c->reorder_pending || !c->nbr_valid || c->table_want > c->G.table_size || c->graph_uses == 0) {
+            if (k < n_steps) {
+                TRY(group_step(c));
+                ++k;
+            }
+        }
+        /* neighbour storage with room for the lists to grow while the graphs run */
+        TRY(sync(c));
+        const int64_t want = c->nbr_storage + c->nbr_storage / 2;
+        if (want > c->nbr_cap && want < ((int64_t)1 << 31)) {
+            TRY(graph_release(c));
+            TRY(dfree(c, c->nbr_idx));
+            TRY(dalloc(c, &c->nbr_idx, want));
+            if (c->packed_alloc) {
+                TRY(dfree(c, c->nbr_pair));
+                TRY(dalloc(c, &c->nbr_pair, want));
+            }
+            c->nbr_cap = want;
+        }
+        c->hsc->status = 0;
+        CU(cudaMemsetAsync(&c->dsc->status, 0, sizeof(int32_t), c->stream));
+        const bool prof = c->prof.on;
+        c->prof.on = false;
+        c->graph_mode = true;
+        int rc = FJSPH_OK;
+        for (; k < n_steps && rc == FJSPH_OK; ++k) {
+            const int v = graph_variant(c);
+            if (!c->graph[v]) {
+                const int64_t searches = c->searches, launches = c->launches;
+                cudaGraph_t g = nullptr;
+                if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                    rc = FJSPH_E_CUDA;
+                    break;
+                }
+                rc = group_step(c);
+                const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+                if (rc == FJSPH_OK && e != cudaSuccess) rc = FJSPH_E_CUDA;
+                if (rc == FJSPH_OK && cudaGraphInstantiate(&c->graph[v], g, 0) != cudaSuccess) rc = FJSPH_E_CUDA;
+                if (g) cudaGraphDestroy(g);
+                if (rc != FJSPH_OK) break;
+                c->graph_launches[v] = c->launches - launches;
+                c->searches = searches;
+                c->launches = launches;
+            }
+            if (cudaGraphLaunch(c->graph[v], c->stream) != cudaSuccess) {
+                rc = FJSPH_E_CUDA;
+                break;
+            }
+            c->searches += 2;
+            c->launches += c->graph_launches[v];
+            c->graph_uses++;
+        }
+        c->graph_mode = false;
+        c->prof.on = prof;
+        TRY(rc);
+        CU(cudaMemcpyAsync(&c->hsc->status, &c->dsc->status, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+        TRY(sync(c));
+        if (c->hsc->status & kStatusNbrOverflow) return FJSPH_E_NEIGHBOUR;
+        return FJSPH_OK;
+    }
+    for (; k < n_steps; ++k) TRY(group_step(c));
+    return sync(c);
+}
+
+int fjsph_group_report(fjsph_ctx *c, double *time, double *dt, double *cfl, double *err, int64_t *steps) {
+    TRY(check_ctx(c));
+    if (!grouped(c)) return FJSPH_E_STATE;
+    TRY(sync(c));
+    const size_t g = (size_t)c->ngrp;
+    if (time) CU(cudaMemcpy(time, c->gs.time, sizeof(double) * g, cudaMemcpyDeviceToHost));
+    if (dt) CU(cudaMemcpy(dt, c->gs.dt, sizeof(double) * g, cudaMemcpyDeviceToHost));
+    if (cfl) CU(cudaMemcpy(cfl, c->gs.cfl, sizeof(double) * g, cudaMemcpyDeviceToHost));
+    if (err) CU(cudaMemcpy(err, c->gs.err, sizeof(double) * g, cudaMemcpyDeviceToHost));
+    if (steps) CU(cudaMemcpy(steps, c->gs.steps, sizeof(int64_t) * g, cudaMemcpyDeviceToHost));
+    return FJSPH_OK;
 }
 
 /* ---- learned aerodynamic closure ------------------------------------------------------------ */

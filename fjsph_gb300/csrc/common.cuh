@@ -60,7 +60,17 @@ struct Params {
     int64_t n, nb; /* total particles, boundary particles (slots [0, nb)) */
     int32_t nblocks;
     DevBlock blocks[kMaxBlocks];
+    /* Independent simulations sharing the context (batched droplets): group of every slot and
+     * each group's free-stream velocity; null for a single simulation.  Per-group dt and npd
+     * are then arrays indexed by group. */
+    const int32_t *grp;
+    const double *g_vinf; /* 3 per group */
 };
+
+__device__ __forceinline__ int32_t grp_of(const Params &P, int64_t i) { return P.grp ? P.grp[i] : 0; }
+__device__ __forceinline__ double vinf_of(const Params &P, int64_t i, int k) {
+    return P.grp ? P.g_vinf[3 * P.grp[i] + k] : P.v_inf[k];
+}
 
 /* Neighbour lists plus the positions at search time (the reference keeps the squared distance
  * of each pair from search time, src/Resid.cpp:288).
@@ -199,6 +209,8 @@ inline unsigned grid_for(int64_t n, int threads) { return (unsigned)((n + thread
 
 /* Device-resident scalars of the integrator (read by kernels so that a step needs no host
  * round trip). */
+constexpr int32_t kStatusNbrOverflow = 1; /* DevScalars::status bit: neighbour storage too small */
+
 struct DevScalars {
     double dt;         /* svar.integrator.delta_t                              */
     double npd;        /* numerical particle density from dSPH_PreStep         */

@@ -17,11 +17,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRedThreads = 256;
 
-template <int D>
-__device__ __forceinline__ double dt_of(const double *dt_dev, double scale) {
-    return scale * (*dt_dev);
-}
-
 /* ---- boundary density / pressure updates --------------------------------------------------- */
 /* mode 0: RK intermediate (src/Runge_Kutta.cpp:73-131); mode 1: RK final (:278-349);
  * mode 2: Newmark-Beta (src/Newmark_Beta.cpp:142-197).  In mode 0, sum_w (0, 2 or 1 for stages
@@ -32,7 +27,7 @@ __global__ void k_bound_rho_update(Params P, DevState pn, DevState W, RKScratch 
     if (i >= P.nb) return;
     const int solver = P.blocks[W.blk[i]].bound_solver;
     if (solver == FJSPH_PRESSURE_G) return;
-    const double dt = dt_scale * (*dt_dev);
+    const double dt = dt_scale * dt_dev[grp_of(P, i)];
     double target;
     if (mode == 0) {
         target = pn.rho[i] + dt * W.Rrho[i];
@@ -85,7 +80,7 @@ __global__ void k_rk_stage_update(Params P, DevState pn, DevState W, RKScratch S
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool ale = has(P, FJSPH_VAR_ALE);
-    const double dt = dt_scale * (*dt_dev);
+    const double dt = dt_scale * dt_dev[grp_of(P, i)];
     const int b = W.b[i];
     if (stage >= 2) {
         const double w = (stage == 2) ? 2.0 : 1.0;
@@ -121,7 +116,7 @@ __global__ void k_rk_final_update(Params P, DevState pn, DevState W, RKScratch S
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool ale = has(P, FJSPH_VAR_ALE);
-    const double dt = *dt_dev;
+    const double dt = dt_dev[grp_of(P, i)];
     const int b = W.b[i];
     if (b > FJSPH_BUFFER && b != FJSPH_OUTLET) {
 #pragma unroll
@@ -145,7 +140,7 @@ __global__ void k_nb_update(Params P, DevState pn, DevState W, const double *dt_
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool ale = has(P, FJSPH_VAR_ALE);
-    const double dt = *dt_dev, dt2 = dt * dt;
+    const double dt = dt_dev[grp_of(P, i)], dt2 = dt * dt;
     const double g1 = P.nb_gamma, g2 = 1 - g1, b1 = P.nb_beta, b2 = 0.5 * (1 - 2 * b1);
     const int b = W.b[i];
     if (b > FJSPH_BUFFER && b != FJSPH_OUTLET) {

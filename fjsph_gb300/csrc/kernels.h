@@ -45,6 +45,28 @@ void launch_compact_map(const int32_t *flag, const int64_t *key, int64_t n, int3
 void launch_permute_key_blk(const int64_t *key, const int32_t *blk, int64_t *key2, int32_t *blk2,
                             const int32_t *new_of_old, int64_t n, cudaStream_t s);
 
+/* ---- groups.cu: independent simulations in one context --------------------------------------- */
+struct GroupDev {
+    double *dt, *npd, *time, *cfl, *maxShift, *maxRho_pc, *logbase, *err;
+    int32_t *n_stable, *n_unstable;
+    int64_t *steps, *nfluid, *count;
+};
+struct GroupConst {
+    double rho_rest, H, H_sq, mu, speed_sound, dt_min, dt_max, last_frame_time, frame_interval;
+    double min_residual, rho_max_iter, cfl_min, cfl_max, cfl_step, subits_factor;
+    int32_t max_subits, n_stable_limit, n_unstable_limit, ale;
+};
+void launch_group_fill(double *a, int64_t n, double v, cudaStream_t s);
+/* out[g] += sum of vals over slots [i0, i1) of group g (out zeroed by the caller) */
+void launch_group_sum(const int32_t *grp, const double *vals, int64_t i0, int64_t i1, double *out, cudaStream_t s);
+void launch_group_sq_disp(const Params &P, const DevState &W, double *const ref[3], double *out, cudaStream_t s);
+/* red[g * 8 + k]: maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift of group g */
+void launch_group_timestep(const Params &P, const DevState &W, double *red, int32_t ng, cudaStream_t s);
+void launch_group_dt(const GroupDev &G, const double *red, int32_t ng, const GroupConst &K, cudaStream_t s);
+void launch_group_npd(double *npd, const double *sum, const int64_t *count, int32_t ng, cudaStream_t s);
+void launch_group_err(const GroupDev &G, const double *sum, int32_t ng, int mode, cudaStream_t s);
+void launch_group_adapt(const GroupDev &G, int32_t ng, const GroupConst &K, cudaStream_t s);
+
 /* ---- mlp_train.cu ------------------------------------------------------------------------- */
 namespace mlp {
 /* FP32 parameters (host) -> device master copy and its BF16 forward / transposed copies */
@@ -76,7 +98,8 @@ void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, i
 /* Writes idx (FP64 form, CSR by off) or, when pair is given, (slot, FP32 squared distance) pairs
  * in the sliced-ELL order of DevNbr (slice offsets `slice`, counts per slot `counts`). */
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     int2 *pair, const int64_t *slice, const int32_t *counts, cudaStream_t s);
+                     int2 *pair, const int64_t *slice, const int32_t *counts, int64_t cap, int32_t *status,
+                     cudaStream_t s);
 /* width[s] = kSlice x the largest count of slice s (slices of kSlice slots from slot 0). */
 void launch_slice_width(const int32_t *counts, int64_t n, int32_t *width, cudaStream_t s);
 /* Bucket-ordered hi/lo coordinates for the neighbour walk (after any re-ordering). */

@@ -297,14 +297,20 @@ __global__ void k_slice_width(const int32_t *counts, int64_t n, int32_t *width) 
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, double *xs1, double *xs2, CellGrid G,
                                                         const int64_t *off, int32_t *idx, int2 *pair,
-                                                        const int64_t *slice, const int32_t *counts) {
+                                                        const int64_t *slice, const int32_t *counts, int64_t cap,
+                                                        int32_t *status) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     double *const xs[3] = {xs0, xs1, xs2};
     if (pair) {
         /* sliced-ELL: pair k of slot i at slice[i / 32] + 32 k + i % 32 */
-        int2 *dst = pair + slice[i / kSlice] + (i % kSlice);
+        const int64_t base = slice[i / kSlice] + (i % kSlice);
+        int2 *dst = pair + base;
         const int32_t kend = counts[i];
+        if (kend > 0 && base + (int64_t)(kend - 1) * kSlice >= cap) { /* storage too small */
+            atomicOr(status, kStatusNbrOverflow);
+            return;
+        }
         int32_t k = 0;
         /* (slot, FP32 squared distance from the hi/lo split, about 1e-7 relative) */
         float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
@@ -331,6 +337,10 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
     }
     int64_t w = off[i];
     const int64_t wend = off[i + 1];
+    if (wend > cap) {
+        atomicOr(status, kStatusNbrOverflow);
+        return;
+    }
     walk<D>(P, xs, G, i, [&](int32_t j, int32_t) {
         if (w < wend) idx[w] = j;
         ++w;
@@ -489,14 +499,15 @@ void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, i
 }
 
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
-                     int2 *pair, const int64_t *slice, const int32_t *counts, cudaStream_t s) {
+                     int2 *pair, const int64_t *slice, const int32_t *counts, int64_t cap, int32_t *status,
+                     cudaStream_t s) {
     if (P.n == 0) return;
     if (P.D == 2)
         k_nbr_fill<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair, slice,
-                                                                   counts);
+                                                                   counts, cap, status);
     else
         k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair, slice,
-                                                                   counts);
+                                                                   counts, cap, status);
 }
 
 void launch_slice_width(const int32_t *counts, int64_t n, int32_t *width, cudaStream_t s) {

@@ -152,7 +152,7 @@ __global__ void k_aero_velocity(Params P, DevState W, DevNbr N) {
     else
         on = double(nbr_range(N, i).n) * P.i_n_full < P.lam_cutoff && W.b[i] == FJSPH_FREE;
 #pragma unroll
-    for (int k = 0; k < D; ++k) W.cellV[k][i] = on ? P.v_inf[k] : 0.0;
+    for (int k = 0; k < D; ++k) W.cellV[k][i] = on ? vinf_of(P, i, k) : 0.0;
     W.cellID[i] = on ? 1 : kNoCell;
 }
 
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(kThreads) k_surface_curvature(Params P, DevSta
     for (int k = 0; k < D; ++k) ni[k] = nt[k][i];
     const bool occl = (b == FJSPH_FREE) && gissler;
 #pragma unroll
-    for (int k = 0; k < D; ++k) Vdiff[k] = (occl && W.cellID[i] != -1) ? P.v_inf[k] - vi[k] : 0.0;
+    for (int k = 0; k < D; ++k) Vdiff[k] = (occl && W.cellID[i] != -1) ? vinf_of(P, i, k) - vi[k] : 0.0;
     double Li[D * D];
 #pragma unroll
     for (int k = 0; k < D * D; ++k) Li[k] = W.L[k][i];
@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr
     const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE, csf = P.st_model == FJSPH_ST_CSF;
     double npdm2 = 0.0;
     if (pairwise) {
-        const double npd = *npd_dev;
+        const double npd = npd_dev[grp_of(P, i)];
         const double H2 = 2.0 * P.H;
         const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (kPi * kPi * kPi * kPi) *
                             (9.0 / 4.0 * (kPi * kPi * kPi) - 6.0 * kPi - 4.0));

@@ -394,9 +394,9 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     if (D == 3) ni[2] = Ti.z;
     const bool occl = (b == FJSPH_FREE) && gissler;
     const bool vd_on = occl && W.cellID[i] != -1;
-    Vdiff[0] = vd_on ? (float)(P.v_inf[0] - W.v[0][i]) : 0.f;
-    Vdiff[1] = vd_on ? (float)(P.v_inf[1] - W.v[1][i]) : 0.f;
-    if (D == 3) Vdiff[2] = vd_on ? (float)(P.v_inf[2] - W.v[2][i]) : 0.f;
+    Vdiff[0] = vd_on ? (float)(vinf_of(P, i, 0) - W.v[0][i]) : 0.f;
+    Vdiff[1] = vd_on ? (float)(vinf_of(P, i, 1) - W.v[1][i]) : 0.f;
+    if (D == 3) Vdiff[2] = vd_on ? (float)(vinf_of(P, i, 2) - W.v[2][i]) : 0.f;
     (void)Ci;
     (void)Ei;
     float Li[D * D];
@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
     const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE, csf = P.st_model == FJSPH_ST_CSF;
     float npdm2 = 0.f;
     if (pairwise) {
-        const double npd = *npd_dev;
+        const double npd = npd_dev[grp_of(P, i)];
         const double H2 = 2.0 * P.H;
         const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (kPi * kPi * kPi * kPi) *
                             (9.0 / 4.0 * (kPi * kPi * kPi) - 6.0 * kPi - 4.0));

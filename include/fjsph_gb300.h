@@ -261,6 +261,24 @@ int fjsph_find_timestep_noalloc(const fjsph_settings *s, int64_t n_fluid, const 
                                 const double *curve, const double *const v[3], const double *const vPert[3],
                                 void *stream, double *dt, double *maxima7);
 
+/* ---- independent simulations in one context ------------------------------------------------- */
+/* No reference counterpart.  Many independent simulations of the same settings (the batched
+ * droplet workload) share one context: the state holds all of them, each a contiguous range of
+ * reference indices first[g] .. first[g + 1] - 1 (first[0] = 0, first[ngroups] = particle count),
+ * placed far enough apart that no particle of one is within the support of another.  Each group
+ * keeps its own free-stream velocity v_inf[3 g .. 3 g + 2], time step, npd, CFL number, time and
+ * Runge-Kutta error, exactly as a context holding it alone would.  Runge-Kutta only; no inlets or
+ * deletion planes.  Set after the limits and before (or after) the state upload. */
+int fjsph_set_groups(fjsph_ctx *ctx, int32_t ngroups, const int64_t *first, const double *v_inf);
+/* n_steps Integrator::integrate steps of every group, enqueued without host round trips.  With
+ * use_graph the step is captured once as a CUDA graph (one per pattern of re-ordering searches)
+ * and replayed; the neighbour storage is then fixed at 1.5x the lists of the last ordinary step
+ * and FJSPH_E_NEIGHBOUR reports lists that outgrew it (run again: the storage grows). */
+int fjsph_integrate_groups(fjsph_ctx *ctx, int32_t n_steps, int32_t use_graph);
+/* Per-group time, dt of the last step, CFL number, log10 RMS error and steps taken (arrays of
+ * ngroups; any pointer may be NULL). */
+int fjsph_group_report(fjsph_ctx *ctx, double *time, double *dt, double *cfl, double *err, int64_t *steps);
+
 /* ---- learned aerodynamic closure ------------------------------------------------------------ */
 /* No counterpart in the reference: a 12 -> 64 -> 64 -> 64 -> 2 GELU network (BF16 weights, FP32
  * accumulation) that stands in for the Gissler occlusion factor and drag coefficient
