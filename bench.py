@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--closure-weights", default="", help="load trained weights from this .npy (skip training)")
     ap.add_argument("--save-weights", default="", help="save the trained weights to this .npy")
     ap.add_argument("--plain-steps", type=int, default=2, help="steps of the FP32 form with the plain closure")
+    ap.add_argument("--drops", type=int, default=256, help="droplets of the batched workload (0 = skip)")
+    ap.add_argument("--drop-steps", type=int, default=10)
+    ap.add_argument("--drop-steps-fp64", type=int, default=3)
+    ap.add_argument("--drop-sample", type=int, default=16, help="droplets timed alone for the per-droplet times")
+    ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
 
@@ -205,6 +210,83 @@ def timed_steps(ctx, steps: int, ws: int) -> float:
     return reduce_max(ws, ctx.event_elapsed(0, 1))
 
 
+def run_droplets(args, ws, rank, weights):
+    """Config 4: a batch of independent droplets in one context per GPU (droplets shared out over
+    the ranks with no exchange), each step one CUDA-graph replay; plain FP64, FP32 with the plain
+    closure and FP32 with the learned closure.  Rank 0 also times a sample of droplets alone (one
+    context each) for the per-droplet step times of the unbatched form."""
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300 import cases
+    from fjsph_gb300.api import Context
+    full = cases.droplet_batch(n_drops=args.drops)
+    ids = cases.shard_ids(len(full.counts), full.counts, rank, ws)
+    b = full.subset(ids) if ws > 1 else full
+    n = b.case.state.n
+    total = full.case.state.n
+    out = {"droplets": int(len(full.counts)), "particles": int(total), "counts_range": [int(full.counts.min()),
+           int(full.counts.max())], "we_range": [round(float(full.we.min()), 1), round(float(full.we.max()), 1)],
+           "sharding": f"{ws} rank(s), greedy particle balance, no collective but the final timing max",
+           "config_steps": 3000, "forms": {}}
+    forms = [("fp64", d.PREC_FP64, d.CLOSURE_PLAIN, args.drop_steps_fp64),
+             ("fp32_plain_closure", d.PREC_MIXED, d.CLOSURE_PLAIN, args.drop_steps),
+             ("fp32_learned_closure", d.PREC_MIXED, d.CLOSURE_LEARNED, args.drop_steps)]
+    for name, prec, closure, steps in forms:
+        if closure == d.CLOSURE_LEARNED and weights is None:
+            continue
+        s = b.case.settings.copy()
+        s.precision = prec
+        s.aero_closure = closure
+        ctx = Context(s, n + 64, b.case.blocks)
+        ctx.set_groups(b.first, b.v_inf)
+        ctx.set_states(b.case.state, b.case.state)
+        if closure == d.CLOSURE_LEARNED:
+            ctx.closure_set_weights(weights, 0.05)
+        tune = ctx.autotune(3)["chosen"] if prec == d.PREC_MIXED and not args.no_tune else None
+        ctx.integrate_groups(2, graph=True)  # one ordinary step, then the graph capture
+        barrier(ws)
+        ctx.launch_stats(reset=True)
+        ctx.event_record(0)
+        ctx.integrate_groups(steps, graph=True)
+        ctx.event_record(1)
+        ms = reduce_max(ws, ctx.event_elapsed(0, 1))
+        rep = ctx.group_report()
+        out["forms"][name] = {"value": total * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                              "steps": steps, "gpu_launches_per_step": ctx.launch_stats() / steps,
+                              "graph": True, "autotune": tune,
+                              "per_droplet_step_ms": {"p50": ms / steps, "p99": ms / steps},
+                              "dt_range": [float(rep["dt"].min()), float(rep["dt"].max())]}
+        ctx.close()
+    if rank == 0 and args.drop_sample > 0:
+        order = np.argsort(full.counts)
+        pick = order[np.linspace(0, len(order) - 1, min(args.drop_sample, len(order))).astype(int)]
+        t_ms, ns = [], []
+        for g in pick:
+            c = full.single(int(g))
+            s = c.settings.copy()
+            s.precision = d.PREC_MIXED
+            ctx = Context(s, c.state.n + 64, c.blocks)
+            ctx.set_states(c.state, c.state)
+            for _ in range(2):
+                ctx.integrate()
+            ctx.event_record(0)
+            for _ in range(3):
+                ctx.integrate()
+            ctx.event_record(1)
+            t_ms.append(ctx.event_elapsed(0, 1) / 3)
+            ns.append(c.state.n)
+            ctx.close()
+        t_ms, ns = np.array(t_ms), np.array(ns, dtype=np.float64)
+        a, b0 = np.polyfit(ns, t_ms, 1)
+        seq_ms = float(np.sum(np.maximum(a * full.counts + b0, t_ms.min())))
+        out["alone_fp32_plain_closure"] = {
+            "sample": f"{len(pick)} droplets spread over the count range, one context each, 3 steps",
+            "per_droplet_step_ms": {"p50": float(np.percentile(t_ms, 50)), "p99": float(np.percentile(t_ms, 99))},
+            "sequential_step_ms_all_droplets": seq_ms,
+            "value": total / (seq_ms / 1e3), "unit": UNIT}
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     from fjsph_gb300 import _cdefs as d
@@ -221,6 +303,9 @@ def run_ours(args, ws, rank, local):
         ctx.closure_set_weights(weights, 0.05)
     for _ in range(args.warmup):
         ctx.integrate()
+    tune = ctx.autotune(3) if s.precision == d.PREC_MIXED and not args.no_tune else None
+    if tune:
+        ctx.integrate()  # one more warm-up step under the chosen configuration
     barrier(ws)
     clocks = Clocks(local)
     clocks.start()
@@ -319,7 +404,7 @@ def run_ours(args, ws, rank, local):
         c64.close()
     return dict(value=value, ms=ms, nf=nf, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches, fp64=fp64,
                 prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s, case=c,
-                plain=plain, closure=closure_info, pairs=n_pairs)
+                plain=plain, closure=closure_info, pairs=n_pairs, tune=tune, weights=weights)
 
 
 def pinned_state(st):
@@ -438,6 +523,7 @@ def main():
         torch.cuda.set_device(0)
         dist.init_process_group("nccl")
     r = run_ours(args, ws, rank, local)
+    drops = run_droplets(args, ws, rank, r["weights"]) if args.drops > 0 else None
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -455,7 +541,7 @@ def main():
                            "l2": "inputs larger than L2 (state ~1 GB)", "parallelism": f"replicas{ws}"},
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
                 "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"], "closure": r["closure"],
-                "neighbour_pairs": r["pairs"],
+                "neighbour_pairs": r["pairs"], "autotune": r["tune"], "droplet_batch": drops,
                 "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
                 "gpu_launches": r["launches"], "passes_ms": r["prof"]}
         print(json.dumps(line))

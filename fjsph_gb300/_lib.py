@@ -67,6 +67,9 @@ PROTOTYPES = {
     "fjsph_profile_pass_name": (C.c_char_p, [_i32]),
     "fjsph_get_limits": (C.c_int, [_P, C.POINTER(d.Block), _i32, _i32p]),
     "fjsph_set_groups": (C.c_int, [_P, _i32, _i64p, _dp]),
+    "fjsph_set_tuning": (C.c_int, [_P, _i32p]),
+    "fjsph_get_tuning": (C.c_int, [_P, _i32p]),
+    "fjsph_autotune": (C.c_int, [_P, _i32, _i32p, _dp]),
     "fjsph_integrate_groups": (C.c_int, [_P, _i32, _i32]),
     "fjsph_group_report": (C.c_int, [_P, _dp, _dp, _dp, _dp, _i64p]),
     "fjsph_update_counts": (C.c_int, [_P, _i64p, _i64p]),

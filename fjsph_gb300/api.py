@@ -242,6 +242,26 @@ class Context:
         out["steps"] = steps
         return out
 
+    # ---- launch-configuration autotuner --------------------------------------------------------
+    def autotune(self, repeats: int = 3) -> dict:
+        """Pick the fastest pair-sweep / residual launch configuration on the current state."""
+        cfg = (C.c_int32 * 3)()
+        ms = (C.c_double * 8)()
+        check("fjsph_autotune", self._lib.fjsph_autotune(self._h, int(repeats), cfg, ms))
+        tried = [("sweep", b, None) for b in (64, 128)] + [("resid", b, a) for b in (64, 128) for a in (2, 4, 8)]
+        return {"chosen": {"sweep_threads": cfg[0], "resid_threads": cfg[1], "list_ahead": cfg[2]},
+                "trials_ms": [dict(kind=k, threads=b, list_ahead=a, ms=ms[i]) for i, (k, b, a) in enumerate(tried)]}
+
+    def tuning(self, cfg=None):
+        """Get (cfg None) or set the launch configuration (sweep threads, residual threads, rows ahead)."""
+        arr = (C.c_int32 * 3)()
+        if cfg is None:
+            check("fjsph_get_tuning", self._lib.fjsph_get_tuning(self._h, arr))
+            return tuple(arr)
+        arr[:] = list(cfg)
+        check("fjsph_set_tuning", self._lib.fjsph_set_tuning(self._h, arr))
+        return tuple(cfg)
+
     def update_counts(self) -> tuple[int, int]:
         """Particles inserted and deleted by update_data since the context was created."""
         a, b = C.c_int64(), C.c_int64()

@@ -425,6 +425,19 @@ class DropletBatch:
     diam: np.ndarray
     we: np.ndarray
 
+    def subset(self, ids) -> "DropletBatch":
+        """The droplets `ids` (in that order) as a batch of their own."""
+        ids = np.asarray(ids, dtype=np.int64)
+        idx = np.concatenate([np.arange(self.first[g], self.first[g + 1]) for g in ids]) if len(ids) else \
+            np.zeros(0, dtype=np.int64)
+        st = self.case.state.take(idx)
+        st.part_id[:] = np.arange(st.n)
+        first = np.concatenate([[0], np.cumsum(self.counts[ids])]).astype(np.int64)
+        s = self.case.settings.copy()
+        s.max_points = st.n
+        return DropletBatch(Case(self.case.name, s, st, _blocks(0, st.n)), first, self.v_inf[ids].copy(),
+                            self.counts[ids].copy(), self.diam[ids].copy(), self.we[ids].copy())
+
     def single(self, g: int) -> Case:
         """Droplet g alone, as its own case (same settings, its own free stream)."""
         s = self.case.settings.copy()
@@ -466,3 +479,18 @@ def droplet_batch(n_drops: int = 256, n_min: int = 2000, n_max: int = 60000, dx:
     s.max_points = st.n
     case = Case("droplet_batch", s, st, _blocks(0, st.n))
     return DropletBatch(case, first, vinf, np.diff(first), diam, we)
+
+
+def shard_ids(n_drops: int, counts, rank: int, world: int) -> np.ndarray:
+    """Droplets of one rank when a batch is split over `world` GPUs with no exchange between them:
+    greedy balance of particle counts (largest droplet to the least-loaded rank, ties to the lower
+    rank), identical on every rank."""
+    counts = np.asarray(counts)
+    order = np.argsort(-counts, kind="stable")
+    load = np.zeros(world, dtype=np.int64)
+    owner = np.empty(n_drops, dtype=np.int64)
+    for g in order:
+        r = int(np.argmin(load))
+        owner[g] = r
+        load[r] += counts[g]
+    return np.flatnonzero(owner == rank)

@@ -156,6 +156,7 @@ struct fjsph_ctx {
     GroupDev gs{};
     double *g_red = nullptr, *g_sum = nullptr;
     bool graph_mode = false;         /* steps enqueue without host round trips        */
+    int32_t tune[3] = {128, 128, 4}; /* sweep block size, residual block size, list rows ahead */
     cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     int64_t graph_launches[4] = {0, 0, 0, 0};
     int64_t graph_uses = 0;
@@ -310,6 +311,9 @@ Params make_params(const fjsph_ctx *c) {
     }
     P.grp = c->ngrp > 0 ? c->grp : nullptr;
     P.g_vinf = c->g_vinf;
+    P.sweep_threads = c->tune[0];
+    P.resid_threads = c->tune[1];
+    P.list_ahead = c->tune[2];
     P.L = s.L;
     P.A_sphere = s.A_sphere;
     P.A_plate = s.A_plate;
@@ -2265,6 +2269,107 @@ int fjsph_group_report(fjsph_ctx *c, double *time, double *dt, double *cfl, doub
     if (err) CU(cudaMemcpy(err, c->gs.err, sizeof(double) * g, cudaMemcpyDeviceToHost));
     if (steps) CU(cudaMemcpy(steps, c->gs.steps, sizeof(int64_t) * g, cudaMemcpyDeviceToHost));
     return FJSPH_OK;
+}
+
+/* ---- launch-configuration autotuner ---------------------------------------------------------- */
+} /* extern "C" */
+namespace {
+bool valid_tune(const int32_t *t) {
+    auto bs = [](int32_t v) { return v == 32 || v == 64 || v == 96 || v == 128; };
+    return bs(t[0]) && bs(t[1]) && t[2] >= 1 && t[2] <= 16;
+}
+
+/* mean milliseconds of `repeats` runs of fn on the context's stream */
+template <class F>
+int time_ms(fjsph_ctx *c, int repeats, F &&fn, double *ms) {
+    cudaEvent_t a, b;
+    CU(cudaEventCreate(&a));
+    CU(cudaEventCreate(&b));
+    int rc = fn(); /* warm-up */
+    if (rc == FJSPH_OK && cudaEventRecord(a, c->stream) != cudaSuccess) rc = FJSPH_E_CUDA;
+    for (int r = 0; r < repeats && rc == FJSPH_OK; ++r) rc = fn();
+    if (rc == FJSPH_OK && cudaEventRecord(b, c->stream) != cudaSuccess) rc = FJSPH_E_CUDA;
+    float f = 0.f;
+    if (rc == FJSPH_OK && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&f, a, b) != cudaSuccess))
+        rc = FJSPH_E_CUDA;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f / repeats;
+    return rc;
+}
+} // namespace
+extern "C" {
+
+int fjsph_set_tuning(fjsph_ctx *c, const int32_t *cfg3) {
+    TRY(check_ctx(c));
+    if (!cfg3 || !valid_tune(cfg3)) return FJSPH_E_ARG;
+    TRY(sync(c));
+    TRY(graph_release(c)); /* captured launches carry the old configuration */
+    std::copy(cfg3, cfg3 + 3, c->tune);
+    return FJSPH_OK;
+}
+
+int fjsph_get_tuning(fjsph_ctx *c, int32_t *cfg3) {
+    TRY(check_ctx(c));
+    if (!cfg3) return FJSPH_E_ARG;
+    std::copy(c->tune, c->tune + 3, cfg3);
+    return FJSPH_OK;
+}
+
+/* Times the pre-passes under each sweep block size and the residual under each residual block
+ * size and list prefetch distance on the context's current state (all of them recompute the same
+ * outputs from the same inputs, so the state is unchanged) and keeps the fastest.  times_ms, if
+ * given, receives the 2 + 2 * 3 measured configurations in the order tried. */
+int fjsph_autotune(fjsph_ctx *c, int32_t repeats, int32_t *chosen3, double *times_ms) {
+    TRY(need_state(c));
+    if (!mixed(c)) return FJSPH_E_UNSUPPORTED;
+    if (repeats <= 0) return FJSPH_E_ARG;
+    if (!c->nbr_valid) TRY(search(c));
+    TRY(sync(c));
+    TRY(graph_release(c));
+    const bool prof = c->prof.on;
+    c->prof.on = false;
+    int k = 0, rc = FJSPH_OK;
+    const int32_t bs[2] = {64, 128}, la[3] = {2, 4, 8};
+    double best = 1e300;
+    int32_t best_sweep = c->tune[0];
+    for (int32_t v : bs) {
+        c->tune[0] = v;
+        double ms = 0.0;
+        rc = time_ms(c, repeats, [&] { return prestep_passes(c); }, &ms);
+        if (rc != FJSPH_OK) break;
+        if (times_ms) times_ms[k] = ms;
+        ++k;
+        if (ms < best) {
+            best = ms;
+            best_sweep = v;
+        }
+    }
+    c->tune[0] = best_sweep;
+    best = 1e300;
+    int32_t best_res = c->tune[1], best_la = c->tune[2];
+    for (int32_t v : bs)
+        for (int32_t a : la) {
+            if (rc != FJSPH_OK) break;
+            c->tune[1] = v;
+            c->tune[2] = a;
+            double ms = 0.0;
+            rc = time_ms(c, repeats, [&] { return resid(c, make_params(c)); }, &ms);
+            if (rc != FJSPH_OK) break;
+            if (times_ms) times_ms[k] = ms;
+            ++k;
+            if (ms < best) {
+                best = ms;
+                best_res = v;
+                best_la = a;
+            }
+        }
+    c->tune[1] = best_res;
+    c->tune[2] = best_la;
+    c->prof.on = prof;
+    TRY(rc);
+    if (chosen3) std::copy(c->tune, c->tune + 3, chosen3);
+    return sync(c);
 }
 
 /* ---- learned aerodynamic closure ------------------------------------------------------------ */

@@ -65,6 +65,8 @@ struct Params {
      * are then arrays indexed by group. */
     const int32_t *grp;
     const double *g_vinf; /* 3 per group */
+    /* launch configuration of the split-precision pair sweeps (the autotuner's choices) */
+    int32_t sweep_threads, resid_threads, list_ahead;
 };
 
 __device__ __forceinline__ int32_t grp_of(const Params &P, int64_t i) { return P.grp ? P.grp[i] : 0; }

@@ -80,8 +80,8 @@ __device__ __forceinline__ SellList sell(const DevNbr &N, int64_t i) {
 
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
-/* Pair-list rows fetched into L1 ahead of use by the residual; with the sliced-ELL order one row
- * of a warp is one 256-byte line. */
+/* Pair-list rows fetched into L1 ahead of use by the residual (default; Params::list_ahead is the
+ * tuned value); with the sliced-ELL order one row of a warp is one 256-byte line. */
 constexpr int32_t kListAhead = 4;
 
 /* separation x_j - x_i from the hi/lo split */
@@ -781,11 +781,12 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
     /* software pipeline: after this pair's own gathers are issued, the next pair is read and its
      * neighbour's packed inputs are prefetched into L1 while this pair is computed; list rows
      * are fetched kListAhead ahead */
+    const int32_t ahead = P.list_ahead > 0 ? P.list_ahead : kListAhead;
     int2 nxt = L.n > 0 ? L[0] : make_int2((int32_t)i, 0);
-    for (int32_t q = 1; q < kListAhead && q < L.n; ++q) prefetch_l1(&L.p[(int64_t)q * kSlice]);
+    for (int32_t q = 1; q < ahead && q < L.n; ++q) prefetch_l1(&L.p[(int64_t)q * kSlice]);
     for (int32_t e = 0; e < L.n; ++e) {
         const int2 pe = nxt;
-        if (e + kListAhead < L.n) prefetch_l1(&L.p[(int64_t)(e + kListAhead) * kSlice]);
+        if (e + ahead < L.n) prefetch_l1(&L.p[(int64_t)(e + ahead) * kSlice]);
         const int32_t j = pe.x;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
         if (e + 1 < L.n) {
@@ -903,9 +904,12 @@ __global__ void k_permute_f4(const float4 *src, float4 *dst, const int32_t *new_
     if (i < n && new_of_old[i] >= 0) dst[new_of_old[i]] = src[i];
 }
 
-inline unsigned fgrid(const Params &P) { return grid_for(P.n - P.nb, kThreads); }
-inline unsigned bgrid(const Params &P) { return grid_for(P.nb, kThreads); }
-inline unsigned agrid(const Params &P) { return grid_for(P.n, kThreads); }
+/* block size of the pair sweeps: the tuned value (<= kThreads, the compiled maximum) */
+inline int sweep_bs(const Params &P) { return P.sweep_threads > 0 ? P.sweep_threads : kThreads; }
+inline int resid_bs(const Params &P) { return P.resid_threads > 0 ? P.resid_threads : kThreads; }
+inline unsigned fgrid(const Params &P) { return grid_for(P.n - P.nb, sweep_bs(P)); }
+inline unsigned bgrid(const Params &P) { return grid_for(P.nb, sweep_bs(P)); }
+inline unsigned agrid(const Params &P) { return grid_for(P.n, sweep_bs(P)); }
 
 } // namespace
 
@@ -913,9 +917,9 @@ inline unsigned agrid(const Params &P) { return grid_for(P.n, kThreads); }
     do {                                                                                   \
         if ((GRID) == 0) break;                                                            \
         if ((P).D == 2)                                                                    \
-            KERNEL<2><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                            \
+            KERNEL<2><<<(GRID), sweep_bs(P), 0, s>>>(__VA_ARGS__);                         \
         else                                                                               \
-            KERNEL<3><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                            \
+            KERNEL<3><<<(GRID), sweep_bs(P), 0, s>>>(__VA_ARGS__);                         \
     } while (0)
 
 void launch_m_pack(const Params &P, const DevState &W, const Packed &K, int64_t i0, int64_t i1, int full,
@@ -941,7 +945,7 @@ void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const
     FJSPH_DISPATCH_M(P, k_m_surface_normal, fgrid(P), P, W, N, K);
     FJSPH_DISPATCH_M(P, k_m_surface_curvature, fgrid(P), P, W, N, K);
     if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fgrid(P) > 0)
-        k_m_surface_zone<<<fgrid(P), kThreads, 0, s>>>(P, W, N, K);
+        k_m_surface_zone<<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
 }
 void launch_m_dissipation(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
     FJSPH_DISPATCH_M(P, k_m_dissipation, fgrid(P), P, W, N, K);
@@ -958,10 +962,10 @@ void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, c
 }
 void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
                     const Closure &C, cudaStream_t s) {
-    const unsigned g = fgrid(P);
+    const unsigned g = grid_for(P.n - P.nb, resid_bs(P));
     if (g == 0) return;
     const bool ale = has(P, FJSPH_VAR_ALE), nf = has(P, FJSPH_VAR_NOFROZEN);
-#define FJSPH_RESID_M(DD, A, NF) k_m_resid<DD, A, NF><<<g, kThreads, 0, s>>>(P, W, N, K, npd_dev, C)
+#define FJSPH_RESID_M(DD, A, NF) k_m_resid<DD, A, NF><<<g, resid_bs(P), 0, s>>>(P, W, N, K, npd_dev, C)
     if (P.D == 2) {
         if (ale)
             nf ? FJSPH_RESID_M(2, true, true) : FJSPH_RESID_M(2, true, false);

@@ -279,6 +279,16 @@ int fjsph_integrate_groups(fjsph_ctx *ctx, int32_t n_steps, int32_t use_graph);
  * ngroups; any pointer may be NULL). */
 int fjsph_group_report(fjsph_ctx *ctx, double *time, double *dt, double *cfl, double *err, int64_t *steps);
 
+/* ---- launch-configuration autotuner (split-precision form) --------------------------------- */
+/* No reference counterpart.  cfg3 = {block size of the pair sweeps, block size of the residual,
+ * pair-list rows prefetched ahead by the residual}; block sizes 32, 64, 96 or 128, rows 1-16. */
+int fjsph_set_tuning(fjsph_ctx *ctx, const int32_t *cfg3);
+int fjsph_get_tuning(fjsph_ctx *ctx, int32_t *cfg3);
+/* Times each candidate (sweep block 64/128; residual block 64/128 x rows ahead 2/4/8) `repeats`
+ * times on the current state and neighbour lists, keeps the fastest and returns it in chosen3;
+ * times_ms (8 doubles, may be NULL) receives the mean time of every candidate in that order. */
+int fjsph_autotune(fjsph_ctx *ctx, int32_t repeats, int32_t *chosen3, double *times_ms);
+
 /* ---- learned aerodynamic closure ------------------------------------------------------------ */
 /* No counterpart in the reference: a 12 -> 64 -> 64 -> 64 -> 2 GELU network (BF16 weights, FP32
  * accumulation) that stands in for the Gissler occlusion factor and drag coefficient

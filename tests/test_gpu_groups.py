@@ -77,3 +77,35 @@ def test_graph_replay_matches_launches():
     assert rel_err(g.rho - b.case.state.rho, a.rho - b.case.state.rho) < 1e-6
     np.testing.assert_allclose(rg["time"], ra["time"], rtol=1e-12)
     np.testing.assert_array_equal(rg["steps"], ra["steps"])
+
+
+def test_autotune_choice_and_identical_results():
+    """Every candidate launch configuration computes the same per-particle results (the sums of a
+    particle run in one thread in list order), so the tuner only changes the time."""
+    from fjsph_gb300.api import Context
+    b = _batch()
+    s = b.case.settings.copy()
+    s.precision = d.PREC_MIXED
+    ctx = Context(s, b.case.state.n + 64, b.case.blocks)
+    ctx.set_groups(b.first, b.v_inf)
+    ctx.set_states(b.case.state, b.case.state)
+    ctx.update_neighbours()
+    res = []
+    for cfg in [(128, 128, 4), (64, 64, 2), (96, 32, 8)]:
+        ctx.tuning(cfg)
+        npd = ctx.dSPH_PreStep()
+        ctx.get_aero_velocity()
+        ctx.Detect_Surface()
+        ctx.dissipation_terms()
+        ctx.get_acc_and_Rrho(npd)
+        res.append(ctx.download())
+    for r in res[1:]:
+        np.testing.assert_array_equal(r.Rrho, res[0].Rrho)
+        np.testing.assert_array_equal(r.acc, res[0].acc)
+        np.testing.assert_array_equal(r.norm, res[0].norm)
+    out = ctx.autotune(2)
+    ch = out["chosen"]
+    assert ch["sweep_threads"] in (64, 128) and ch["resid_threads"] in (64, 128) and ch["list_ahead"] in (2, 4, 8)
+    assert len(out["trials_ms"]) == 8 and all(t["ms"] > 0 for t in out["trials_ms"])
+    assert ctx.tuning() == (ch["sweep_threads"], ch["resid_threads"], ch["list_ahead"])
+    ctx.close()
