@@ -314,6 +314,26 @@ Params make_params(const fjsph_ctx *c) {
     P.sweep_threads = c->tune[0];
     P.resid_threads = c->tune[1];
     P.list_ahead = c->tune[2];
+    {
+        FConst &f = P.fc;
+        f.H = (float)s.H;
+        f.H_sq = (float)s.H_sq;
+        f.Wc = (float)s.W_correc;
+        f.W_dx = (float)s.W_dx;
+        f.rho0 = (float)s.rho_rest;
+        f.Bgam = (float)(s.B * s.gam);
+        f.nu = (float)s.nu;
+        f.alpha = (float)s.visc_alpha;
+        f.dsph_cont = (float)s.dsph_cont;
+        f.max_shift_vel = (float)s.max_shift_vel;
+        for (int k = 0; k < 3; ++k) f.grav[k] = (float)s.grav[k];
+        const double pi = 3.14159265358979323846;
+        f.pi3o4_H = (float)(3.0 * pi / 4.0 / s.H);
+        f.fac_bound = (float)(1.0 + 0.5 * std::cos(0.5 * pi * 7.0 / 9.0));
+        const double H2 = 2.0 * s.H;
+        const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (pi * pi * pi * pi) * (9.0 / 4.0 * (pi * pi * pi) - 6.0 * pi - 4.0));
+        f.st_coef = 0.5 * s.sig / lam;
+    }
     P.L = s.L;
     P.A_sphere = s.A_sphere;
     P.A_plate = s.A_plate;

@@ -46,6 +46,16 @@ struct DevBlock {
     double insert_unorm[3];
 };
 
+/* FP32 constants of the split-precision pair terms, converted once on the host. */
+struct FConst {
+    float H, H_sq, Wc, W_dx, rho0, Bgam, nu, alpha, dsph_cont, max_shift_vel;
+    float grav[3];
+    float pi3o4_H;   /* 3 pi / (4 H), pairwise surface tension  */
+    float fac_bound; /* 1 + cos(7 pi / 18) / 2 (Kernel.h:88-113) */
+    float pad;
+    double st_coef;  /* sigma / (2 lambda) of the pairwise model: npdm2 = st_coef / npd^2 */
+};
+
 /* Everything a kernel reads that is constant over one launch. */
 struct Params {
     int32_t D;
@@ -67,6 +77,7 @@ struct Params {
     const double *g_vinf; /* 3 per group */
     /* launch configuration of the split-precision pair sweeps (the autotuner's choices) */
     int32_t sweep_threads, resid_threads, list_ahead;
+    FConst fc;
 };
 
 __device__ __forceinline__ int32_t grp_of(const Params &P, int64_t i) { return P.grp ? P.grp[i] : 0; }

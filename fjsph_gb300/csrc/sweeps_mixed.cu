@@ -36,18 +36,19 @@ struct Pf { /* float copies of the constants a pair term needs */
 };
 
 __device__ __forceinline__ Pf make_pf(const Params &P) {
+    const FConst &c = P.fc;
     Pf f;
-    f.H = (float)P.H;
-    f.H_sq = (float)P.H_sq;
-    f.Wc = (float)P.W_correc;
-    f.W_dx = (float)P.W_dx;
-    f.rho0 = (float)P.rho_rest;
-    f.Bgam = (float)(P.B * P.gam);
-    f.nu = (float)P.nu;
-    f.alpha = (float)P.visc_alpha;
-    f.dsph_cont = (float)P.dsph_cont;
-    f.max_shift_vel = (float)P.max_shift_vel;
-    for (int k = 0; k < 3; ++k) f.grav[k] = (float)P.grav[k];
+    f.H = c.H;
+    f.H_sq = c.H_sq;
+    f.Wc = c.Wc;
+    f.W_dx = c.W_dx;
+    f.rho0 = c.rho0;
+    f.Bgam = c.Bgam;
+    f.nu = c.nu;
+    f.alpha = c.alpha;
+    f.dsph_cont = c.dsph_cont;
+    f.max_shift_vel = c.max_shift_vel;
+    for (int k = 0; k < 3; ++k) f.grav[k] = c.grav[k];
     f.cubic = has(P, FJSPH_VAR_CUBIC);
     return f;
 }
@@ -83,6 +84,20 @@ __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefe
 /* Pair-list rows fetched into L1 ahead of use by the residual (default; Params::list_ahead is the
  * tuned value); with the sliced-ELL order one row of a warp is one 256-byte line. */
 constexpr int32_t kListAhead = 4;
+/* pairs whose neighbour inputs are in flight ahead of the residual's current pair */
+#ifndef FJSPH_GATHER_AHEAD
+#define FJSPH_GATHER_AHEAD 1
+#endif
+constexpr int kGatherAhead = FJSPH_GATHER_AHEAD;
+
+__device__ __forceinline__ void prefetch_pair_inputs(const Packed &K, int32_t j, bool f, bool g) {
+    prefetch_l1(K.A + j);
+    prefetch_l1(K.B + j);
+    prefetch_l1(K.C + j);
+    prefetch_l1(K.E + j);
+    if (f) prefetch_l1(K.F + j);
+    if (g) prefetch_l1(K.G + j);
+}
 
 /* separation x_j - x_i from the hi/lo split */
 template <int D>
@@ -737,13 +752,10 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
     float npdm2 = 0.f;
     if (pairwise) {
         const double npd = npd_dev[grp_of(P, i)];
-        const double H2 = 2.0 * P.H;
-        const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (kPi * kPi * kPi * kPi) *
-                            (9.0 / 4.0 * (kPi * kPi * kPi) - 6.0 * kPi - 4.0));
-        npdm2 = (float)((0.5 * P.sig / lam) / (npd * npd));
+        npdm2 = (float)P.fc.st_coef / (float)(npd * npd);
     }
-    const float pi3o4_H = (float)(3.0 * kPi / 4.0 / P.H);
-    const float fac_bound = (float)(1.0 + 0.5 * cos(0.5 * kPi * 7.0 / 9.0));
+    const float pi3o4_H = P.fc.pi3o4_H;
+    const float fac_bound = P.fc.fac_bound;
     const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Fi = K.F[i];
     const float rho_i = f.rho0 + Ci.w;
     const float m_i = Ai.w * rho_i;
@@ -782,22 +794,28 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
      * neighbour's packed inputs are prefetched into L1 while this pair is computed; list rows
      * are fetched kListAhead ahead */
     const int32_t ahead = P.list_ahead > 0 ? P.list_ahead : kListAhead;
-    int2 nxt = L.n > 0 ? L[0] : make_int2((int32_t)i, 0);
-    for (int32_t q = 1; q < ahead && q < L.n; ++q) prefetch_l1(&L.p[(int64_t)q * kSlice]);
+    /* the next kGatherAhead pairs wait in registers; the newest one's neighbour inputs are
+     * prefetched into L1 when it is read, kGatherAhead iterations before they are gathered */
+    int2 q[kGatherAhead];
+#pragma unroll
+    for (int a = 0; a < kGatherAhead; ++a) {
+        q[a] = make_int2((int32_t)i, 0);
+        if (a < L.n) {
+            q[a] = L[a];
+            if (a > 0) prefetch_pair_inputs(K, q[a].x, linear || ale, nofrozen);
+        }
+    }
+    for (int32_t r_ = kGatherAhead; r_ < ahead && r_ < L.n; ++r_) prefetch_l1(&L.p[(int64_t)r_ * kSlice]);
     for (int32_t e = 0; e < L.n; ++e) {
-        const int2 pe = nxt;
+        const int2 pe = q[0];
         if (e + ahead < L.n) prefetch_l1(&L.p[(int64_t)(e + ahead) * kSlice]);
         const int32_t j = pe.x;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
-        if (e + 1 < L.n) {
-            nxt = L[e + 1];
-            const int32_t jn = nxt.x;
-            prefetch_l1(K.A + jn);
-            prefetch_l1(K.B + jn);
-            prefetch_l1(K.C + jn);
-            prefetch_l1(K.E + jn);
-            if (linear || ale) prefetch_l1(K.F + jn);
-            if (nofrozen) prefetch_l1(K.G + jn);
+#pragma unroll
+        for (int a = 0; a + 1 < kGatherAhead; ++a) q[a] = q[a + 1];
+        if (e + kGatherAhead < L.n) {
+            q[kGatherAhead - 1] = L[e + kGatherAhead];
+            prefetch_pair_inputs(K, q[kGatherAhead - 1].x, linear || ale, nofrozen);
         }
         if (j == i) continue;
         float Rji[D], Vji[D];
@@ -885,12 +903,13 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
 #pragma unroll
         for (int k = 0; k < D; ++k) accd[k] += c * W.norm[k][i];
     }
+    const double inv_m = 1.0 / (double)m_i;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const double av = nofrozen ? (double)art[k] : W.aVisc[k][i];
         double t = accd[k];
         if (ale) t += acc_ale[k];
-        W.acc[k][i] = t + av + visc[k] + (double)st[k] / (double)m_i + P.grav[k];
+        W.acc[k][i] = t + av + visc[k] + (double)st[k] * inv_m + P.grav[k];
         if (aero_on) W.Af[k][i] = aero[k];
     }
     double R = Rrho.value() * (double)rho_i;
