@@ -1842,7 +1842,7 @@ int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double
             CU(cudaMemcpy(so.data(), c->slice_off, sizeof(int64_t) * (nslices + 1), cudaMemcpyDeviceToHost));
             for (int64_t i = 0; i < n; ++i)
                 for (int64_t k = 0; k < off[i + 1] - off[i]; ++k)
-                    id[off[i] + k] = pr[so[i / kSlice] + k * kSlice + i % kSlice].x;
+                    id[off[i] + k] = pr[sell_entry(so[i / kSlice] + (i % kSlice) * kChunk, (int32_t)k)].x;
         } else {
             CU(cudaMemcpy(id.data(), c->nbr_idx, sizeof(int32_t) * c->n_pairs, cudaMemcpyDeviceToHost));
         }

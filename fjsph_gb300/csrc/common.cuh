@@ -89,10 +89,13 @@ __device__ __forceinline__ double vinf_of(const Params &P, int64_t i, int k) {
  * of each pair from search time, src/Resid.cpp:288).
  *  - FP64 form: CSR, off[n + 1] and idx (neighbour slots).
  *  - split-precision form: (slot, FP32 squared distance bits) pairs in sliced-ELL order with
- *    slices of 32 consecutive slots: pair k of slot i is at slice[i / 32] + 32 k + i % 32, and
- *    slot i has cnt[i] pairs.  A warp walking 32 consecutive slots' lists in step reads 32
- *    consecutive pairs per load.  off is still filled (CSR offsets of the counts). */
+ *    slices of kSlice = 32 consecutive slots and chunks of kChunk = 4 pairs per slot: pair k of
+ *    slot i is entry slice[i / 32] + (k / 4) * 128 + (i % 32) * 4 + k % 4, and slot i has cnt[i]
+ *    pairs.  A warp walking 32 slots' lists in step reads one 1 KB row every four pairs, and a
+ *    lane writes its pairs as whole 32-byte sectors.  off is still filled (CSR offsets of the
+ *    counts). */
 constexpr int kSlice = 32;
+constexpr int kChunk = 4;
 struct DevNbr {
     const int64_t *off;
     const int32_t *idx;   /* FP64 form                                    */
@@ -102,18 +105,22 @@ struct DevNbr {
     const double *xs[3];
 };
 
-/* The pairs of slot i: entry k at base + k * stride. */
+FJSPH_HD int64_t sell_entry(int64_t slot_base, int32_t k) {
+    return slot_base + (int64_t)(k / kChunk) * (kSlice * kChunk) + (k % kChunk);
+}
+
+/* The pairs of slot i: entry k at nbr_entry(R, k). */
 struct NbrRange {
     int64_t base;
-    int32_t stride, n;
+    int32_t n;
+    bool sell;
 };
 __device__ __forceinline__ NbrRange nbr_range(const DevNbr &N, int64_t i) {
-    if (N.pair) return NbrRange{N.slice[i / kSlice] + (i % kSlice), kSlice, N.cnt[i]};
-    return NbrRange{N.off[i], 1, (int32_t)(N.off[i + 1] - N.off[i])};
+    if (N.pair) return NbrRange{N.slice[i / kSlice] + (i % kSlice) * kChunk, N.cnt[i], true};
+    return NbrRange{N.off[i], (int32_t)(N.off[i + 1] - N.off[i]), false};
 }
 __device__ __forceinline__ int64_t nbr_slot(const DevNbr &N, const NbrRange &R, int32_t k) {
-    const int64_t e = R.base + (int64_t)k * R.stride;
-    return N.pair ? (int64_t)N.pair[e].x : (int64_t)N.idx[e];
+    return R.sell ? (int64_t)N.pair[sell_entry(R.base, k)].x : (int64_t)N.idx[R.base + k];
 }
 
 FJSPH_HD bool has(const Params &P, uint32_t bit) { return (P.variant & bit) != 0; }

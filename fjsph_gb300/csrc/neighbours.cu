@@ -291,7 +291,7 @@ __global__ void k_slice_width(const int32_t *counts, int64_t n, int32_t *width) 
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int32_t c = i < n ? counts[i] : 0;
     const int32_t m = __reduce_max_sync(0xffffffffu, c);
-    if ((threadIdx.x & 31) == 0 && i < n) width[i / kSlice] = m * kSlice;
+    if ((threadIdx.x & 31) == 0 && i < n) width[i / kSlice] = ((m + kChunk - 1) / kChunk) * kChunk * kSlice;
 }
 
 template <int D>
@@ -303,15 +303,14 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
     if (i >= P.n) return;
     double *const xs[3] = {xs0, xs1, xs2};
     if (pair) {
-        /* sliced-ELL: pair k of slot i at slice[i / 32] + 32 k + i % 32 */
-        const int64_t base = slice[i / kSlice] + (i % kSlice);
-        int2 *dst = pair + base;
+        /* sliced-ELL with chunks of kChunk pairs per slot: whole chunks are written as two
+         * 16-byte stores (one 32-byte sector) */
+        const int64_t base = slice[i / kSlice] + (i % kSlice) * kChunk;
         const int32_t kend = counts[i];
-        if (kend > 0 && base + (int64_t)(kend - 1) * kSlice >= cap) { /* storage too small */
+        if (kend > 0 && sell_entry(base, ((kend - 1) / kChunk) * kChunk + kChunk - 1) >= cap) { /* too small */
             atomicOr(status, kStatusNbrOverflow);
             return;
         }
-        int32_t k = 0;
         /* (slot, FP32 squared distance from the hi/lo split, about 1e-7 relative) */
         float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
 #pragma unroll
@@ -320,6 +319,16 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
             hi[k] = (float)x;
             lo[k] = (float)(x - (double)hi[k]);
         }
+        /* one chunk per thread staged in shared memory (registers are the walk's) */
+        __shared__ __align__(16) int2 stage[kThreads][kChunk];
+        int2 *buf = stage[threadIdx.x];
+        int32_t k = 0;
+        auto flush = [&](int32_t chunk) {
+            const int4 *src = reinterpret_cast<const int4 *>(buf);
+            int4 *dst = reinterpret_cast<int4 *>(pair + base + (int64_t)chunk * (kSlice * kChunk));
+            dst[0] = src[0];
+            dst[1] = src[1];
+        };
         walk<D>(P, xs, G, i, [&](int32_t j, int32_t e) {
             if (k < kend) {
                 const float4 hj = G.sorted_hi[e], lj = G.sorted_lo[e];
@@ -329,10 +338,12 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
                     const float dz = (hj.z - hi[2]) + (lj.z - lo[2]);
                     d2 += dz * dz;
                 }
-                dst[(int64_t)k * kSlice] = make_int2(j, __float_as_int(d2));
+                buf[k % kChunk] = make_int2(j, __float_as_int(d2));
+                if (k % kChunk == kChunk - 1) flush(k / kChunk);
             }
             ++k;
         });
+        if (kend % kChunk != 0) flush(kend / kChunk);
         return;
     }
     int64_t w = off[i];

@@ -73,10 +73,11 @@ __device__ __forceinline__ int bits_zone(int w) { return (w >> 4) & 1; }
 struct SellList {
     const int2 *p;
     int32_t n;
-    __device__ __forceinline__ int2 operator[](int32_t k) const { return p[(int64_t)k * kSlice]; }
+    __device__ __forceinline__ int2 operator[](int32_t k) const { return p[sell_entry(0, k)]; }
+    __device__ __forceinline__ const int2 *at(int32_t k) const { return p + sell_entry(0, k); }
 };
 __device__ __forceinline__ SellList sell(const DevNbr &N, int64_t i) {
-    return SellList{N.pair + N.slice[i / kSlice] + (i % kSlice), N.cnt[i]};
+    return SellList{N.pair + N.slice[i / kSlice] + (i % kSlice) * kChunk, N.cnt[i]};
 }
 
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
@@ -805,10 +806,10 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
             if (a > 0) prefetch_pair_inputs(K, q[a].x, linear || ale, nofrozen);
         }
     }
-    for (int32_t r_ = kGatherAhead; r_ < ahead && r_ < L.n; ++r_) prefetch_l1(&L.p[(int64_t)r_ * kSlice]);
+    for (int32_t r_ = kChunk; r_ < ahead && r_ < L.n; r_ += kChunk) prefetch_l1(L.at(r_));
     for (int32_t e = 0; e < L.n; ++e) {
         const int2 pe = q[0];
-        if (e + ahead < L.n) prefetch_l1(&L.p[(int64_t)(e + ahead) * kSlice]);
+        if (((e + ahead) % kChunk) == 0 && e + ahead < L.n) prefetch_l1(L.at(e + ahead)); /* next chunk */
         const int32_t j = pe.x;
         const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
 #pragma unroll
