@@ -97,6 +97,8 @@ struct fjsph_ctx {
     int32_t *slice_w = nullptr;   /* entries per slice of kSlice slots                    */
     int64_t *slice_off = nullptr; /* first entry of each slice (exclusive scan of slice_w) */
     int64_t nbr_cap = 0, n_pairs = 0, nbr_storage = 0;
+    int32_t wcap = 0;    /* split-precision single-pass lists: entries per slot (0: count first) */
+    int32_t maxcnt = 0;  /* largest neighbour count of the last search                         */
     bool nbr_valid = false;
     int64_t *scan_tmp64 = nullptr;
     int64_t scan_tmp64_len = 0;
@@ -654,6 +656,68 @@ int reorder_states(fjsph_ctx *c, const Params &P) {
     return FJSPH_OK;
 }
 
+int32_t wcap_for(int64_t maxcnt) {
+    const int64_t w = maxcnt + maxcnt / 4 + kChunk;
+    return (int32_t)(((w + kChunk - 1) / kChunk) * kChunk);
+}
+
+int grow_pairs(fjsph_ctx *c, int64_t need) {
+    if (need <= c->nbr_cap) return FJSPH_OK;
+    const int64_t ncap = need + need / 8;
+    if (ncap >= ((int64_t)1 << 31) * 4) return FJSPH_E_NEIGHBOUR;
+    TRY(dfree(c, c->nbr_pair));
+    TRY(dalloc(c, &c->nbr_pair, ncap));
+    if (c->nbr_idx) {
+        TRY(dfree(c, c->nbr_idx));
+        TRY(dalloc(c, &c->nbr_idx, ncap));
+    }
+    c->nbr_cap = ncap;
+    return FJSPH_OK;
+}
+
+/* Split-precision lists in one walk: wcap entries of storage per slot, a re-run with a larger
+ * wcap if any slot has more neighbours. */
+int search_fixed(fjsph_ctx *c, const Params &P) {
+    cudaStream_t s = c->stream;
+    const int64_t nslices = (c->n + kSlice - 1) / kSlice;
+    for (int attempt = 0;; ++attempt) {
+        const int64_t need = nslices * kSlice * (int64_t)c->wcap;
+        if (need > c->nbr_cap) {
+            if (c->graph_mode) return FJSPH_E_NEIGHBOUR; /* sized before capture */
+            TRY(grow_pairs(c, need));
+        }
+        CU(cudaMemsetAsync(&c->dsc->maxcnt, 0, sizeof(int32_t) + sizeof(unsigned long long), s));
+        launch_nbr_fill_fixed(P, c->xs, c->G, c->nbr_pair, c->nbr_counts, c->slice_off, c->wcap, c->dsc, s);
+        c->launches += 3;
+        c->nbr_storage = need;
+        if (c->graph_mode) {
+            c->nbr_valid = true;
+            return FJSPH_OK;
+        }
+        int64_t grid[4];
+        CU(cudaMemcpyAsync(&c->hsc->status, &c->dsc->status, sizeof(DevScalars) - offsetof(DevScalars, status),
+                           cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(&c->hsc->red[10], c->G.grid, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        TRY(sync(c));
+        std::memcpy(grid, &c->hsc->red[10], 4 * sizeof(int64_t));
+        if (grid[3]) {
+            const double ncells = (double)grid[0] * (double)grid[1] * (double)grid[2];
+            if (ncells <= (double)kMaxTable) c->table_want = next_pow2((int64_t)ncells);
+        }
+        c->maxcnt = c->hsc->maxcnt;
+        if (c->hsc->status & kStatusNbrOverflow) {
+            CU(cudaMemsetAsync(&c->dsc->status, 0, sizeof(int32_t), s));
+            c->hsc->status = 0;
+            if (attempt >= 3) return FJSPH_E_NEIGHBOUR;
+            c->wcap = wcap_for(c->maxcnt);
+            continue;
+        }
+        c->n_pairs = (int64_t)c->hsc->pairs;
+        c->nbr_valid = true;
+        return FJSPH_OK;
+    }
+}
+
 int search(fjsph_ctx *c) {
     if (c->n == 0) return FJSPH_E_STATE;
     if (c->table_want > c->G.table_size) {
@@ -677,6 +741,7 @@ int search(fjsph_ctx *c) {
     }
     c->searches++;
     launch_sorted_pos(P, c->xs, c->G, s);
+    if (mixed(c) && c->wcap > 0) return search_fixed(c, P);
     launch_nbr_count(P, c->xs, c->G, c->nbr_counts, s);
     launch_scan_i64(c->nbr_counts, c->nbr_off, c->n, c->scan_tmp64, s);
     c->launches += 4;
@@ -730,6 +795,10 @@ int search(fjsph_ctx *c) {
     c->launches += 1;
     c->n_pairs = total;
     c->nbr_storage = mixed(c) ? storage : total;
+    if (mixed(c) && c->n > 0) { /* later searches: one walk with room for 1.6x the mean count */
+        const int64_t mean = (total + c->n - 1) / c->n;
+        c->wcap = wcap_for(mean + mean / 3);
+    }
     c->nbr_valid = true;
     return FJSPH_OK;
 }
@@ -1832,7 +1901,14 @@ int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double
     std::vector<int64_t> off(n + 1);
     std::vector<int32_t> id(c->n_pairs);
     std::vector<double> xs(c->D * n);
-    CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+    if (mixed(c)) { /* offsets from the per-slot counts (single-pass lists keep no CSR) */
+        std::vector<int32_t> cnt(n);
+        CU(cudaMemcpy(cnt.data(), c->nbr_counts, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        off[0] = 0;
+        for (int64_t i = 0; i < n; ++i) off[i + 1] = off[i] + cnt[i];
+    } else {
+        CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+    }
     if (c->n_pairs) {
         if (mixed(c)) { /* sliced-ELL -> CSR */
             const int64_t nslices = (n + kSlice - 1) / kSlice;
@@ -2222,6 +2298,14 @@ int fjsph_integrate_groups(fjsph_ctx *c, int32_t n_steps, int32_t use_graph) {
         }
         /* neighbour storage with room for the lists to grow while the graphs run */
         TRY(sync(c));
+        if (mixed(c) && c->wcap > 0) {
+            const int32_t w = wcap_for(c->maxcnt + c->maxcnt / 4);
+            if (w > c->wcap) {
+                TRY(graph_release(c));
+                c->wcap = w;
+            }
+            c->nbr_storage = ((c->n + kSlice - 1) / kSlice) * kSlice * (int64_t)c->wcap;
+        }
         const int64_t want = c->nbr_storage + c->nbr_storage / 2;
         if (want > c->nbr_cap && want < ((int64_t)1 << 31)) {
             TRY(graph_release(c));

@@ -236,7 +236,8 @@ struct DevScalars {
     double npd;        /* numerical particle density from dSPH_PreStep         */
     double red[16];    /* reduction results                                    */
     int32_t status;    /* device-side error bits                               */
-    int32_t pad;
+    int32_t maxcnt;    /* largest neighbour count of the last single-pass fill */
+    unsigned long long pairs; /* pairs of the last single-pass fill            */
 };
 
 } // namespace fjsph

@@ -100,6 +100,10 @@ void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, i
 void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, const int64_t *off, int32_t *idx,
                      int2 *pair, const int64_t *slice, const int32_t *counts, int64_t cap, int32_t *status,
                      cudaStream_t s);
+/* Single-pass split-precision lists with wcap entries per slot (multiple of kChunk): sets the
+ * slice offsets, the per-slot counts, dsc->maxcnt / pairs and the overflow status bit. */
+void launch_nbr_fill_fixed(const Params &P, double *const xs[3], const CellGrid &G, int2 *pair, int32_t *counts,
+                           int64_t *slice, int32_t wcap, DevScalars *dsc, cudaStream_t s);
 /* width[s] = kSlice x the largest count of slice s (slices of kSlice slots from slot 0). */
 void launch_slice_width(const int32_t *counts, int64_t n, int32_t *width, cudaStream_t s);
 /* Bucket-ordered hi/lo coordinates for the neighbour walk (after any re-ordering). */

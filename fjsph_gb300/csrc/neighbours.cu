@@ -358,6 +358,68 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
     });
 }
 
+/* Single-pass fill of the split-precision lists: every slice holds kSlice x wcap entries, so a
+ * slot's storage is known before its walk and no counting walk is needed.  The walk writes up
+ * to wcap pairs, records the true count, and the block's largest count and pair total go to
+ * the device scalars; a count above wcap raises kStatusNbrOverflow (the caller re-runs the fill
+ * with a larger wcap). */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_nbr_fill_fixed(Params P, double *xs0, double *xs1, double *xs2,
+                                                              CellGrid G, int2 *pair, int32_t *counts, int32_t wcap,
+                                                              DevScalars *dsc) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool live = i < P.n;
+    __shared__ __align__(16) int2 stage[kThreads][kChunk];
+    int32_t k = 0;
+    if (live) {
+        double *const xs[3] = {xs0, xs1, xs2};
+        const int64_t base = (i / kSlice) * (int64_t)kSlice * wcap + (i % kSlice) * kChunk;
+        float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            const double x = xs[q][i];
+            hi[q] = (float)x;
+            lo[q] = (float)(x - (double)hi[q]);
+        }
+        int2 *buf = stage[threadIdx.x];
+        auto flush = [&](int32_t chunk) {
+            const int4 *src = reinterpret_cast<const int4 *>(buf);
+            int4 *dst = reinterpret_cast<int4 *>(pair + base + (int64_t)chunk * (kSlice * kChunk));
+            dst[0] = src[0];
+            dst[1] = src[1];
+        };
+        walk<D>(P, xs, G, i, [&](int32_t j, int32_t e) {
+            if (k < wcap) {
+                const float4 hj = G.sorted_hi[e], lj = G.sorted_lo[e];
+                const float dx = (hj.x - hi[0]) + (lj.x - lo[0]), dy = (hj.y - hi[1]) + (lj.y - lo[1]);
+                float d2 = dx * dx + dy * dy;
+                if (D == 3) {
+                    const float dz = (hj.z - hi[2]) + (lj.z - lo[2]);
+                    d2 += dz * dz;
+                }
+                buf[k % kChunk] = make_int2(j, __float_as_int(d2));
+                if (k % kChunk == kChunk - 1) flush(k / kChunk);
+            }
+            ++k;
+        });
+        const int32_t kw = k < wcap ? k : wcap;
+        if (kw % kChunk != 0) flush(kw / kChunk);
+        counts[i] = k;
+    }
+    const int32_t kmax = __reduce_max_sync(0xffffffffu, (unsigned)k);
+    const unsigned ksum = __reduce_add_sync(0xffffffffu, (unsigned)k);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&dsc->maxcnt, kmax);
+        atomicAdd(&dsc->pairs, (unsigned long long)ksum);
+        if (kmax > wcap) atomicOr(&dsc->status, kStatusNbrOverflow);
+    }
+}
+
+__global__ void k_slice_fixed(int64_t *slice, int64_t nslices, int64_t per) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s <= nslices) slice[s] = s * per;
+}
+
 /* ---- scans ------------------------------------------------------------------------------------ */
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v) {
@@ -519,6 +581,19 @@ void launch_nbr_fill(const Params &P, double *const xs[3], const CellGrid &G, co
     else
         k_nbr_fill<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, off, idx, pair, slice,
                                                                    counts, cap, status);
+}
+
+void launch_nbr_fill_fixed(const Params &P, double *const xs[3], const CellGrid &G, int2 *pair, int32_t *counts,
+                           int64_t *slice, int32_t wcap, DevScalars *dsc, cudaStream_t s) {
+    if (P.n == 0) return;
+    const int64_t nslices = (P.n + kSlice - 1) / kSlice;
+    k_slice_fixed<<<grid_for(nslices + 1, kThreads), kThreads, 0, s>>>(slice, nslices, (int64_t)kSlice * wcap);
+    if (P.D == 2)
+        k_nbr_fill_fixed<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, pair, counts,
+                                                                         wcap, dsc);
+    else
+        k_nbr_fill_fixed<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G, pair, counts,
+                                                                         wcap, dsc);
 }
 
 void launch_slice_width(const int32_t *counts, int64_t n, int32_t *width, cudaStream_t s) {
