@@ -232,7 +232,10 @@ int dfree(fjsph_ctx *c, T *&p) {
 constexpr int64_t kMinTable = (int64_t)1 << 22;
 constexpr int64_t kMaxTable = (int64_t)1 << 26;
 
+int graph_release(fjsph_ctx *c);
+
 int alloc_table(fjsph_ctx *c, int64_t size) {
+    TRY(graph_release(c)); /* captured launches hold the old arrays */
     CellGrid &G = c->G;
     TRY(dfree(c, G.count));
     TRY(dfree(c, G.start));
@@ -663,6 +666,7 @@ int32_t wcap_for(int64_t maxcnt) {
 
 int grow_pairs(fjsph_ctx *c, int64_t need) {
     if (need <= c->nbr_cap) return FJSPH_OK;
+    TRY(graph_release(c));
     const int64_t ncap = need + need / 8;
     if (ncap >= ((int64_t)1 << 31) * 4) return FJSPH_E_NEIGHBOUR;
     TRY(dfree(c, c->nbr_pair));
@@ -729,6 +733,19 @@ int search(fjsph_ctx *c) {
     Params P = make_params(c);
     Section sec(c, PASS_SEARCH);
     launch_bbox(P, WS(c), c->G, s);
+    if (!c->graph_mode && (c->searches == 0 || c->reorder_pending)) {
+        /* a new particle set: size the bucket table for its grid before the first walk (a
+         * wrapped table makes the walk check every earlier cell for a shared bucket) */
+        int64_t grid[4];
+        CU(cudaMemcpyAsync(&c->hsc->red[10], c->G.grid, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        TRY(sync(c));
+        std::memcpy(grid, &c->hsc->red[10], 4 * sizeof(int64_t));
+        const double ncells = (double)grid[0] * (double)grid[1] * (double)grid[2];
+        if (grid[3] && ncells <= (double)kMaxTable) {
+            TRY(alloc_table(c, next_pow2((int64_t)ncells)));
+            launch_bbox(P, WS(c), c->G, s);
+        }
+    }
     launch_hash_and_count(P, WS(c), c->xs, c->G, s);
     launch_scan_i32(c->G.count, c->G.start, c->G.table_size, c->G.scan_tmp, s);
     launch_scatter_sort(P, c->G, s);
@@ -1845,6 +1862,7 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
     if (c->blocks.empty()) return FJSPH_E_STATE;
     if (c->blocks.back().second != st->n) return FJSPH_E_ARG;
     c->occ_valid = false; /* occlusion statistics belong to the previous state */
+    TRY(graph_release(c));
     std::vector<int64_t> keys;
     if (st->n != c->n || c->n == 0) {
         /* new particle set: identity mapping, re-sort at the next search */

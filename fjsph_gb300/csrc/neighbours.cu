@@ -20,6 +20,10 @@
  */
 #include "kernels.h"
 
+#ifndef CELL_DIV_DEFAULT
+#define CELL_DIV_DEFAULT 1
+#endif
+
 namespace fjsph {
 
 namespace {
@@ -29,7 +33,12 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int64_t kMaxAxis = (int64_t)1 << 20;
 
-__device__ __forceinline__ double cell_edge(const Params &P) { return sqrt(P.sr) * (1.0 + 1e-6); }
+/* Cells are 1/kCellDiv of the support radius 2H and the walk visits (2 kCellDiv + 1)^D cells.
+ * kCellDiv = 2 tests fewer candidates, but on sparse domains (the jet's bounding box is mostly
+ * air) the grid then outgrows the largest bucket table and the wrapped walk is far slower, so
+ * the cells stay at 2H. */
+constexpr int kCellDiv = CELL_DIV_DEFAULT;
+__device__ __forceinline__ double cell_edge(const Params &P) { return sqrt(P.sr) / kCellDiv * (1.0 + 1e-6); }
 
 /* ---- bounding box ----------------------------------------------------------------------------- */
 __global__ void k_bbox_part(Params P, DevState W, double *part) {
@@ -207,15 +216,15 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     const double band = G.bbox[6];
     const float sr_lo = (float)(P.sr * (1.0 - band)), sr_hi = (float)(P.sr * (1.0 + band));
     const uint64_t mask = (uint64_t)(G.table_size - 1);
-    const int zr = (D == 3) ? 1 : 0;
-    const int64_t x0 = c[0] > 0 ? c[0] - 1 : 0;
-    const int64_t x1 = c[0] + 1 < nc[0] ? c[0] + 1 : nc[0] - 1;
+    const int zr = (D == 3) ? kCellDiv : 0, yr = kCellDiv;
+    const int64_t x0 = c[0] > kCellDiv ? c[0] - kCellDiv : 0;
+    const int64_t x1 = c[0] + kCellDiv < nc[0] ? c[0] + kCellDiv : nc[0] - 1;
     /* wrapped table: true if an earlier neighbour cell of this walk hashes to bucket h */
     auto visited_before = [&](int dz, int dy, int64_t cx, uint64_t h) -> bool {
         for (int dz2 = -zr; dz2 <= zr; ++dz2) {
             const int64_t cz2 = c[2] + dz2;
             if (cz2 < 0 || cz2 >= nc[2]) continue;
-            for (int dy2 = -1; dy2 <= 1; ++dy2) {
+            for (int dy2 = -yr; dy2 <= yr; ++dy2) {
                 const int64_t cy2 = c[1] + dy2;
                 if (cy2 < 0 || cy2 >= nc[1]) continue;
                 for (int64_t cx2 = x0; cx2 <= x1; ++cx2) {
@@ -252,7 +261,7 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     for (int dz = -zr; dz <= zr; ++dz) {
         const int64_t cz = c[2] + dz;
         if (cz < 0 || cz >= nc[2]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -yr; dy <= yr; ++dy) {
             const int64_t cy = c[1] + dy;
             if (cy < 0 || cy >= nc[1]) continue;
             if (!wrap) {
