@@ -203,10 +203,20 @@ __device__ __forceinline__ R gradk_scale(R r, R H, R Wc, bool cubic) {
     return R(5) / (H * H) * (b * b * b) * Wc;
 }
 
+/* (rho / rho0)^gamma of the Cole equation of state: gamma = 7 (the reference's default) by
+ * three multiplications (within a few ulp of pow), any other gamma by pow. */
+__device__ __forceinline__ double cole_power(double x, double gam) {
+    if (gam == 7.0) {
+        const double x2 = x * x, x4 = x2 * x2;
+        return x4 * x2 * x;
+    }
+    return pow(x, gam);
+}
+
 /* FLUID::get_pressure / get_density (Var.h:203-236). */
 __device__ __forceinline__ double eos_pressure(const Params &P, double rho) {
     if (P.pressure_rel == FJSPH_ISO_EOS) return P.speed_sound * P.speed_sound * (rho - P.rho_rest) + P.press_back;
-    return P.B * (pow(rho / P.rho_rest, P.gam) - 1.0) + P.press_back;
+    return P.B * (cole_power(rho / P.rho_rest, P.gam) - 1.0) + P.press_back;
 }
 __device__ __forceinline__ double eos_density(const Params &P, double press) {
     if (P.pressure_rel == FJSPH_ISO_EOS) return (press - P.press_back) / (P.speed_sound * P.speed_sound) + P.rho_rest;
