@@ -21,7 +21,7 @@
 #include "kernels.h"
 
 #ifndef CELL_DIV_DEFAULT
-#define CELL_DIV_DEFAULT 1
+#define CELL_DIV_DEFAULT 2
 #endif
 
 namespace fjsph {
@@ -33,12 +33,15 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int64_t kMaxAxis = (int64_t)1 << 20;
 
-/* Cells are 1/kCellDiv of the support radius 2H and the walk visits (2 kCellDiv + 1)^D cells.
- * kCellDiv = 2 tests fewer candidates, but on sparse domains (the jet's bounding box is mostly
- * air) the grid then outgrows the largest bucket table and the wrapped walk is far slower, so
- * the cells stay at 2H. */
+/* Cells are the support radius 2H long along x (the contiguous direction of a bucket row) and
+ * 2H / kCellDiv across it; the walk visits 3 cells of each of (2 kCellDiv + 1)^(D-1) rows.  With
+ * kCellDiv = 2 the visited volume is 6H x 5H x 5H instead of (6H)^3 (30 % fewer candidate tests)
+ * for four times the cells; halving x as well would make sparse domains (the jet's bounding box
+ * is mostly air) outgrow the largest bucket table. */
 constexpr int kCellDiv = CELL_DIV_DEFAULT;
-__device__ __forceinline__ double cell_edge(const Params &P) { return sqrt(P.sr) / kCellDiv * (1.0 + 1e-6); }
+__device__ __forceinline__ double cell_edge(const Params &P, int axis) {
+    return sqrt(P.sr) / (axis == 0 ? 1 : kCellDiv) * (1.0 + 1e-6);
+}
 
 /* ---- bounding box ----------------------------------------------------------------------------- */
 __global__ void k_bbox_part(Params P, DevState W, double *part) {
@@ -87,7 +90,6 @@ __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bb
             lo[k] = fmin(lo[k], sh[k][t]);
             hi[k] = fmax(hi[k], sh[3 + k][t]);
         }
-    const double cs = cell_edge(P);
     int64_t nc[3] = {1, 1, 1};
     double mag = 0.0;
     for (int k = 0; k < P.D; ++k) {
@@ -95,7 +97,7 @@ __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bb
             lo[k] = 0.0;
             hi[k] = 0.0;
         }
-        double c = floor((hi[k] - lo[k]) / cs) + 1.0;
+        double c = floor((hi[k] - lo[k]) / cell_edge(P, k)) + 1.0;
         if (!(c < (double)kMaxAxis)) c = (double)kMaxAxis;
         nc[k] = (int64_t)c;
         mag = fmax(mag, fmax(fabs(lo[k]), fabs(hi[k])));
@@ -122,12 +124,11 @@ __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bb
 template <int D>
 __device__ __forceinline__ void cell_coords(const Params &P, const double *x, const double *lo, const int64_t *nc,
                                             int64_t *c) {
-    const double cs = cell_edge(P);
 #pragma unroll
     for (int k = 0; k < 3; ++k) c[k] = 0;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        double f = floor((x[k] - lo[k]) / cs);
+        double f = floor((x[k] - lo[k]) / cell_edge(P, k));
         int64_t v = (f > 0.0) ? (int64_t)fmin(f, (double)(nc[k] - 1)) : 0;
         c[k] = v;
     }
@@ -217,8 +218,8 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     const float sr_lo = (float)(P.sr * (1.0 - band)), sr_hi = (float)(P.sr * (1.0 + band));
     const uint64_t mask = (uint64_t)(G.table_size - 1);
     const int zr = (D == 3) ? kCellDiv : 0, yr = kCellDiv;
-    const int64_t x0 = c[0] > kCellDiv ? c[0] - kCellDiv : 0;
-    const int64_t x1 = c[0] + kCellDiv < nc[0] ? c[0] + kCellDiv : nc[0] - 1;
+    const int64_t x0 = c[0] > 0 ? c[0] - 1 : 0;
+    const int64_t x1 = c[0] + 1 < nc[0] ? c[0] + 1 : nc[0] - 1;
     /* wrapped table: true if an earlier neighbour cell of this walk hashes to bucket h */
     auto visited_before = [&](int dz, int dy, int64_t cx, uint64_t h) -> bool {
         for (int dz2 = -zr; dz2 <= zr; ++dz2) {
