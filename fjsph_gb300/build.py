@@ -23,6 +23,10 @@ SOURCES = ["capi.cu", "neighbours.cu", "sweeps.cu", "integrate.cu", "state.cu", 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fno-strict-aliasing", "-I", str(ROOT / "include")]
+# The split-precision sweeps run their FP32 pair terms with the hardware's approximate divide and
+# square root and flush FP32 denormals (FP64 arithmetic is unaffected): the pair terms already
+# carry FP32 rounding, and the tests hold them to the FP64 oracle at the stated tolerances.
+PER_FILE = {"sweeps_mixed.cu": ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"]}
 
 
 def _nvcc() -> str:
@@ -45,7 +49,7 @@ def _compile(src: Path, extra: list[str]) -> Path:
         (ROOT / "include" / "fjsph_gb300.h").stat().st_mtime,
     ):
         return obj
-    cmd = [_nvcc(), *ARCH, *NVFLAGS, *extra, "-c", str(src), "-o", str(obj)]
+    cmd = [_nvcc(), *ARCH, *NVFLAGS, *PER_FILE.get(src.name, []), *extra, "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stderr}\n{res.stdout}")

@@ -65,6 +65,14 @@ struct KSum {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+/* cos x for x in [0, 2 pi) on the SFU: folded into [-pi/2, pi/2] by cos x = -cos(x - pi), where
+ * the hardware cosine's absolute error is about 2^-21 (the pairwise surface-tension argument
+ * 3 pi r / (4 H) stays below 1.5 pi) */
+__device__ __forceinline__ float cos_0_2pi(float x) {
+    const float pi = 3.14159265358979f;
+    return x > 0.5f * pi && x < 1.5f * pi ? -__cosf(x - pi) : (x >= 1.5f * pi ? __cosf(x - 2.f * pi) : __cosf(x));
+}
+
 __device__ __forceinline__ int bits_b(int w) { return w & 7; }
 __device__ __forceinline__ int bits_surf(int w) { return (w >> 3) & 1; }
 __device__ __forceinline__ int bits_zone(int w) { return (w >> 4) & 1; }
@@ -347,7 +355,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
                 float u[D];
 #pragma unroll
                 for (int k = 0; k < D; ++k) u[k] = Rji[k] / r;
-                if (acosf(fdot<D>(nh, u)) < (float)(kPi / 4.0)) {
+                /* acos(c) < pi/4  <=>  c > cos(pi/4) (acos decreases on [-1, 1]) */
+                if (fdot<D>(nh, u) > 0.70710678118654752f) {
                     surf = 0;
                     break;
                 }
@@ -846,7 +855,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
         for (int k = 0; k < D; ++k) visc[k] += vc * Vji[k];
         if (st_on) {
             const float fac = (b_i == FJSPH_BOUND || b_j == FJSPH_BOUND) ? fac_bound : 1.f;
-            const float c = -npdm2 * fac * cosf(pi3o4_H * r) / r;
+            const float c = -npdm2 * fac * cos_0_2pi(pi3o4_H * r) / r;
 #pragma unroll
             for (int k = 0; k < D; ++k) st[k] += c * Rji[k];
         }
