@@ -45,11 +45,17 @@ __device__ __forceinline__ void aero_acc(const Params &P, const DevState &W, int
                          double nneigh, double *out) {
 #pragma unroll
     for (int k = 0; k < D; ++k) out[k] = 0.0;
-    const double Vn = vnorm<D, double>(Vd);
     if (P.acase == FJSPH_GISSLER) {
         /* fully occluded (woccl = 1): the exposed area (1 - woccl) * A is exactly zero, so the
-         * force is zero for any finite relative velocity; skip the two pow() of the drag law */
-        if (W.woccl[i] == 1.0 && isfinite(Vn)) return;
+         * force is zero for any finite relative velocity; skip the two pow() of the drag law
+         * (|V| is finite exactly when its components are: they are far below overflow) */
+        bool finite = true;
+#pragma unroll
+        for (int k = 0; k < D; ++k) finite = finite && isfinite(Vd[k]);
+        if (W.woccl[i] == 1.0 && finite) return;
+    }
+    const double Vn = vnorm<D, double>(Vd);
+    if (P.acase == FJSPH_GISSLER) {
         double Cdi, Aun;
         gissler_coeff<D>(P, W.cellRho[i], Vn, dot<D, double>(Vd, Vd), lam, nneigh, Cdi, Aun);
         const double Ai = (1.0 - W.woccl[i]) * Aun;

@@ -427,6 +427,16 @@ void ensure_pack(fjsph_ctx *c) {
     c->dirty_full = c->dirty_all = c->dirty_bound = false;
 }
 
+/* The stage updates write the split-precision inputs of the fluid particles they move when the
+ * packed arrays are current apart from that (no inlet moves buffer particles afterwards); the
+ * packed state is then complete again without a packing pass. */
+const Packed *fused_pack(const fjsph_ctx *c) {
+    return (mixed(c) && c->packed_alloc && c->inlets.empty() && !c->dirty_full && !c->dirty_all) ? &c->K : nullptr;
+}
+void after_update(fjsph_ctx *c) {
+    if (!fused_pack(c)) mark_all(c);
+}
+
 int sync(fjsph_ctx *c) {
     CU(cudaStreamSynchronize(c->stream));
     CU(cudaGetLastError());
@@ -1054,11 +1064,11 @@ int rk_intermediate(fjsph_ctx *c, int stage, double dt_scale) {
     TRY(resid(c, P));
     {
         Section sec(c, PASS_UPDATE);
-        launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, dt_ptr(c), dt_scale, s);
+        launch_rk_stage_update(P, PN(c), WS(c), c->S, stage, dt_ptr(c), dt_scale, fused_pack(c), s);
     }
     c->launches += 2;
     inlet_buffers(c, P, 0, dt_scale);
-    mark_all(c);
+    after_update(c);
     c->pn_equals_W = false;
     return FJSPH_OK;
 }
@@ -1076,11 +1086,11 @@ int rk_final(fjsph_ctx *c) {
         Section sec(c, PASS_UPDATE);
         for (int k = 0; k < c->D; ++k)
             CU(cudaMemcpyAsync(c->S.xsnap[k], WS(c).x[k], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, s));
-        launch_rk_final_update(P, PN(c), WS(c), c->S, dt_ptr(c), s);
+        launch_rk_final_update(P, PN(c), WS(c), c->S, dt_ptr(c), fused_pack(c), s);
     }
     c->launches += 2;
     inlet_buffers(c, P, 1, 1.0);
-    mark_all(c);
+    after_update(c);
     c->pn_equals_W = false;
     return FJSPH_OK;
 }

@@ -9,6 +9,7 @@
  * reference's expressions do.
  */
 #include "kernels.h"
+#include "pack.cuh"
 
 namespace fjsph {
 
@@ -76,7 +77,7 @@ __global__ void k_rk_init_sums(Params P, DevState pn, DevState W, RKScratch S) {
  *   stage 3: Sv += f(st_2), Sr += f(st_2); v_st3 enters Sx in the final step. */
 template <int D>
 __global__ void k_rk_stage_update(Params P, DevState pn, DevState W, RKScratch S, int stage, const double *dt_dev,
-                                  double dt_scale) {
+                                  double dt_scale, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool ale = has(P, FJSPH_VAR_ALE);
@@ -89,16 +90,24 @@ __global__ void k_rk_stage_update(Params P, DevState pn, DevState W, RKScratch S
         for (int k = 0; k < D; ++k) S.Sv[k][i] = S.Sv[k][i] + w * W.acc[k][i];
     }
     if (b > FJSPH_BUFFER) {
+        double xn[D], vn[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const double vv = ale ? (W.v[k][i] + W.vPert[k][i]) : W.v[k][i];
-            W.x[k][i] = pn.x[k][i] + dt * vv;
+            xn[k] = pn.x[k][i] + dt * vv;
         }
 #pragma unroll
-        for (int k = 0; k < D; ++k) W.v[k][i] = pn.v[k][i] + dt * W.acc[k][i];
+        for (int k = 0; k < D; ++k) vn[k] = pn.v[k][i] + dt * W.acc[k][i];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            W.x[k][i] = xn[k];
+            W.v[k][i] = vn[k];
+        }
         const double rho = clamp_rho(P, P.rho_min, pn.rho[i] + dt * W.Rrho[i]);
+        const double p = eos_pressure(P, rho);
         W.rho[i] = rho;
-        W.p[i] = eos_pressure(P, rho);
+        W.p[i] = p;
+        if (K.A) pack_moved<D>(P, W, K, i, xn, vn, rho, p); /* split-precision inputs of the new state */
     }
     if (stage == 2) {
 #pragma unroll
@@ -112,25 +121,34 @@ __global__ void k_rk_stage_update(Params P, DevState pn, DevState W, RKScratch S
 /* Fluid part of do_runge_kutta_final_step (src/Runge_Kutta.cpp:357-394).  W holds st_3 with
  * acc = f(st_3); the sums already hold pn + 2 st_1 + 2 st_2 + st_3 for acc and Rrho. */
 template <int D>
-__global__ void k_rk_final_update(Params P, DevState pn, DevState W, RKScratch S, const double *dt_dev) {
+__global__ void k_rk_final_update(Params P, DevState pn, DevState W, RKScratch S, const double *dt_dev, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool ale = has(P, FJSPH_VAR_ALE);
     const double dt = dt_dev[grp_of(P, i)];
     const int b = W.b[i];
     if (b > FJSPH_BUFFER && b != FJSPH_OUTLET) {
+        double xn[D], vn[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const double v3 = ale ? (W.v[k][i] + W.vPert[k][i]) : W.v[k][i];
-            W.x[k][i] = pn.x[k][i] + (dt / 6.0) * (S.Sx[k][i] + v3);
-            W.v[k][i] = pn.v[k][i] + (dt / 6.0) * S.Sv[k][i];
+            xn[k] = pn.x[k][i] + (dt / 6.0) * (S.Sx[k][i] + v3);
+            vn[k] = pn.v[k][i] + (dt / 6.0) * S.Sv[k][i];
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            W.x[k][i] = xn[k];
+            W.v[k][i] = vn[k];
         }
         const double rho = clamp_rho(P, P.rho_min, pn.rho[i] + (dt / 6.0) * S.Sr[i]);
+        const double p = eos_pressure(P, rho);
         W.rho[i] = rho;
-        W.p[i] = eos_pressure(P, rho);
+        W.p[i] = p;
+        if (K.A) pack_moved<D>(P, W, K, i, xn, vn, rho, p);
     } else if (b == FJSPH_OUTLET) {
 #pragma unroll
         for (int k = 0; k < D; ++k) W.x[k][i] = pn.x[k][i] + dt * W.v[k][i];
+        if (K.A) pack_particle<D>(P, W, K, i);
     }
 }
 
@@ -356,13 +374,16 @@ void launch_rk_init_sums(const Params &P, const DevState &pn, const DevState &W,
     FJSPH_DISPATCH2(P.D, k_rk_init_sums, grid_for(P.n, kThreads), kThreads, P, pn, W, S);
 }
 void launch_rk_stage_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S, int stage,
-                            const double *dt_dev, double dt_scale, cudaStream_t s) {
+                            const double *dt_dev, double dt_scale, const Packed *K, cudaStream_t s) {
+    const Packed none{};
     FJSPH_DISPATCH2(P.D, k_rk_stage_update, grid_for(P.n - P.nb, kThreads), kThreads, P, pn, W, S, stage, dt_dev,
-                    dt_scale);
+                    dt_scale, K ? *K : none);
 }
 void launch_rk_final_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S,
-                            const double *dt_dev, cudaStream_t s) {
-    FJSPH_DISPATCH2(P.D, k_rk_final_update, grid_for(P.n - P.nb, kThreads), kThreads, P, pn, W, S, dt_dev);
+                            const double *dt_dev, const Packed *K, cudaStream_t s) {
+    const Packed none{};
+    FJSPH_DISPATCH2(P.D, k_rk_final_update, grid_for(P.n - P.nb, kThreads), kThreads, P, pn, W, S, dt_dev,
+                    K ? *K : none);
 }
 void launch_nb_update(const Params &P, const DevState &pn, const DevState &W, const double *dt_dev, cudaStream_t s) {
     FJSPH_DISPATCH2(P.D, k_nb_update, grid_for(P.n - P.nb, kThreads), kThreads, P, pn, W, dt_dev);

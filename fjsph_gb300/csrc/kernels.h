@@ -162,10 +162,11 @@ void launch_bound_rho_update(const Params &P, const DevState &pn, const DevState
 /* RK4 accumulator initialisation at Runge_Kutta4 entry (st_1 = W). */
 void launch_rk_init_sums(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S, cudaStream_t s);
 /* Fluid stage update: stage 1..3 intermediate (weight for the sums) or final. */
+/* K (may be null): also write the split-precision inputs of every particle the update moves */
 void launch_rk_stage_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S, int stage,
-                            const double *dt_dev, double dt_scale, cudaStream_t s);
+                            const double *dt_dev, double dt_scale, const Packed *K, cudaStream_t s);
 void launch_rk_final_update(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S,
-                            const double *dt_dev, cudaStream_t s);
+                            const double *dt_dev, const Packed *K, cudaStream_t s);
 void launch_nb_update(const Params &P, const DevState &pn, const DevState &W, const double *dt_dev, cudaStream_t s);
 /* Inlet buffer particles.  mode 0 = RK intermediate, 1 = RK final, 2 = NB. */
 struct DevInlet {

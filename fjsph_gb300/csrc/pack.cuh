@@ -1,0 +1,61 @@
+/*
+ * pack.cuh -- the FP32 split-precision inputs of one particle, packed from its FP64 state
+ * (shared by the packing pass and the integrator's stage updates, which write them as they
+ * produce the new state).
+ */
+#pragma once
+
+#include "kernels.h"
+
+namespace fjsph {
+
+/* A = (fl32(x), vol), B = (x - fl32(x), p / rho^2), C = (fl32(v), rho - rho0),
+ * E = (v - fl32(v), flag bits), F = (vPert, p), bits.  vol and p / rho^2 are FP32 quotients of
+ * the FP32-rounded operands (an FP64 divide per particle costs more than the pass's memory
+ * traffic on this GPU); rounded to nearest in every translation unit. */
+template <int D>
+__device__ __forceinline__ void pack_particle(const Params &P, const DevState &W, const Packed &K, int64_t i) {
+    float xh[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0}, vp[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double x = W.x[k][i], v = W.v[k][i];
+        xh[k] = (float)x;
+        xl[k] = (float)(x - (double)xh[k]);
+        vh[k] = (float)v;
+        vl[k] = (float)(v - (double)vh[k]);
+        vp[k] = (float)W.vPert[k][i];
+    }
+    const double rho = W.rho[i], p = W.p[i];
+    const float rf = (float)rho;
+    K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn((float)W.m[i], rf));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn((float)p, rf * rf));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
+    const int bits = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
+    K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(bits));
+    K.F[i] = make_float4(vp[0], vp[1], vp[2], (float)p);
+    K.bits[i] = bits;
+}
+
+/* The same inputs from a freshly integrated state held in registers (x, v, rho, p); mass,
+ * perturbation velocity and flags are unchanged by an integration stage and are taken from the
+ * current packed arrays. */
+template <int D>
+__device__ __forceinline__ void pack_moved(const Params &P, const DevState &W, const Packed &K, int64_t i,
+                                           const double *x, const double *v, double rho, double p) {
+    float xh[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        xh[k] = (float)x[k];
+        xl[k] = (float)(x[k] - (double)xh[k]);
+        vh[k] = (float)v[k];
+        vl[k] = (float)(v[k] - (double)vh[k]);
+    }
+    const float rf = (float)rho;
+    K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn((float)W.m[i], rf));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn((float)p, rf * rf));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
+    K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(K.bits[i]));
+    reinterpret_cast<float *>(K.F + i)[3] = (float)p;
+}
+
+} // namespace fjsph

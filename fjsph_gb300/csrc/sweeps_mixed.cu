@@ -22,6 +22,7 @@
 #include "closure.cuh"
 #include "kernels.h"
 #include "linalg.cuh"
+#include "pack.cuh"
 
 namespace fjsph {
 
@@ -147,24 +148,7 @@ template <int D>
 __global__ void k_pack_state(Params P, DevState W, Packed K, int64_t i0, int64_t i1, int full) {
     const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= i1) return;
-    float xh[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0}, vp[3] = {0, 0, 0};
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        const double x = W.x[k][i], v = W.v[k][i];
-        xh[k] = (float)x;
-        xl[k] = (float)(x - (double)xh[k]);
-        vh[k] = (float)v;
-        vl[k] = (float)(v - (double)vh[k]);
-        vp[k] = (float)W.vPert[k][i];
-    }
-    const double rho = W.rho[i], p = W.p[i];
-    K.A[i] = make_float4(xh[0], xh[1], xh[2], (float)(W.m[i] / rho));
-    K.B[i] = make_float4(xl[0], xl[1], xl[2], (float)(p / (rho * rho)));
-    K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
-    const int bits = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
-    K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(bits));
-    K.F[i] = make_float4(vp[0], vp[1], vp[2], (float)p);
-    K.bits[i] = bits;
+    pack_particle<D>(P, W, K, i);
     if (full) {
         float g[3] = {0, 0, 0}, n[3] = {0, 0, 0};
 #pragma unroll
@@ -913,13 +897,13 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
 #pragma unroll
         for (int k = 0; k < D; ++k) accd[k] += c * W.norm[k][i];
     }
-    const double inv_m = 1.0 / (double)m_i;
+    const float inv_m = 1.f / m_i; /* the surface-tension sum is FP32 already */
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const double av = nofrozen ? (double)art[k] : W.aVisc[k][i];
         double t = accd[k];
         if (ale) t += acc_ale[k];
-        W.acc[k][i] = t + av + visc[k] + (double)st[k] * inv_m + P.grav[k];
+        W.acc[k][i] = t + av + visc[k] + (double)(st[k] * inv_m) + P.grav[k];
         if (aero_on) W.Af[k][i] = aero[k];
     }
     double R = Rrho.value() * (double)rho_i;
