@@ -21,7 +21,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 CLOSURE_PLAIN, CLOSURE_LEARNED = 0, 1
 CLOSURE_ARM_JUDGE, CLOSURE_ARM_LOG = 1, 2
 MLP_INPUTS, MLP_OUTPUTS = 12, 2
-PN, PNP1 = 0, 1
+PN, PNP1, BOTH = 0, 1, 2
 INLET_ZONE = 6
 MAX_TIMES = 16
 DEFAULT_VAL = 9999999.0

@@ -113,6 +113,9 @@ struct fjsph_ctx {
     double *vtmp[3] = {nullptr, nullptr, nullptr};
     double *npd_part = nullptr;
     double *stage = nullptr;   /* host-transfer staging, capacity * 9 doubles */
+    double *stage2 = nullptr;  /* second staging buffer: field f + 1 moves while field f is gathered */
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t st_copied[2] = {nullptr, nullptr}, st_used[2] = {nullptr, nullptr};
     DevScalars *dsc = nullptr; /* device */
     DevScalars *hsc = nullptr; /* pinned host mirror */
 
@@ -589,6 +592,9 @@ void dev_ptrs(const DevState &S, int D, std::vector<std::vector<void *>> &ptr, s
     type.push_back(2);
 }
 
+/* Host <-> device state transfer, field by field through two staging buffers: the copy of one
+ * field (copy stream) overlaps the reference-order gather / scatter of the previous one (context
+ * stream); events order the reuse of each buffer. */
 int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up) {
     Section sec(c, PASS_TRANSFER);
     std::vector<void *> hp;
@@ -599,23 +605,39 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up) {
     const int64_t n = c->n;
     for (void *p : hp)
         if (!p) return FJSPH_E_ARG;
+    if (!c->copy_stream) {
+        CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            CU(cudaEventCreateWithFlags(&c->st_copied[b], cudaEventDisableTiming));
+            CU(cudaEventCreateWithFlags(&c->st_used[b], cudaEventDisableTiming));
+        }
+    }
+    double *stage[2] = {c->stage, c->stage2};
     for (size_t f = 0; f < dp.size(); ++f) {
+        const int b = (int)(f & 1);
         const int comps = (int)dp[f].size();
         const int es = type[f] == 2 ? 4 : 8;
         const size_t bytes = (size_t)es * comps * n;
         FieldPtrs fp{};
         for (int k = 0; k < comps; ++k) fp.p[k] = dp[f][k];
         if (up) {
-            CU(cudaMemcpyAsync(c->stage, hp[f], bytes, cudaMemcpyHostToDevice, c->stream));
-            launch_field_in(c->stage, comps, es, c->key, fp, n, c->stream);
+            if (f >= 2) CU(cudaStreamWaitEvent(c->copy_stream, c->st_used[b], 0));
+            CU(cudaMemcpyAsync(stage[b], hp[f], bytes, cudaMemcpyHostToDevice, c->copy_stream));
+            CU(cudaEventRecord(c->st_copied[b], c->copy_stream));
+            CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
+            launch_field_in(stage[b], comps, es, c->key, fp, n, c->stream);
+            CU(cudaEventRecord(c->st_used[b], c->stream));
         } else {
-            launch_field_out(c->stage, comps, es, c->key, fp, n, c->stream);
-            CU(cudaMemcpyAsync(hp[f], c->stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+            if (f >= 2) CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
+            launch_field_out(stage[b], comps, es, c->key, fp, n, c->stream);
+            CU(cudaEventRecord(c->st_used[b], c->stream));
+            CU(cudaStreamWaitEvent(c->copy_stream, c->st_used[b], 0));
+            CU(cudaMemcpyAsync(hp[f], stage[b], bytes, cudaMemcpyDeviceToHost, c->copy_stream));
+            CU(cudaEventRecord(c->st_copied[b], c->copy_stream));
         }
-        /* the staging buffer is reused by the next field */
-        CU(cudaStreamSynchronize(c->stream));
     }
-    return FJSPH_OK;
+    CU(cudaStreamSynchronize(c->copy_stream));
+    return sync(c);
 }
 
 /* ---- neighbour search --------------------------------------------------------------------------- */
@@ -1678,6 +1700,7 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     A(dalloc(c, &c->S.part, c->S.part_len));
     A(dalloc(c, &c->npd_part, capacity));
     A(dalloc(c, &c->stage, capacity * 9));
+    A(dalloc(c, &c->stage2, capacity * 9));
     CellGrid &G = c->G;
     A(dalloc(c, &G.hash, capacity));
     A(alloc_table(c, next_pow2(std::max<int64_t>(2 * capacity, kMinTable))));
@@ -1727,6 +1750,12 @@ int fjsph_ctx_destroy(fjsph_ctx *c) {
     for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
     for (cudaEvent_t e : c->user_ev)
         if (e) cudaEventDestroy(e);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    for (int b = 0; b < 2; ++b) {
+        if (c->st_copied[b]) cudaEventDestroy(c->st_copied[b]);
+        if (c->st_used[b]) cudaEventDestroy(c->st_used[b]);
+    }
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->hsc) cudaFreeHost(c->hsc);
     if (c->judge_host) cudaFreeHost(c->judge_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1866,7 +1895,7 @@ int fjsph_update_counts(fjsph_ctx *c, int64_t *inserted, int64_t *deleted) {
 int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) {
     TRY(check_ctx(c));
     TRY(sync(c));
-    if (!st || (which != FJSPH_PN && which != FJSPH_PNP1)) return FJSPH_E_ARG;
+    if (!st || (which != FJSPH_PN && which != FJSPH_PNP1 && which != FJSPH_BOTH)) return FJSPH_E_ARG;
     if (st->n < 0) return FJSPH_E_ARG;
     if (st->n > c->cap) return FJSPH_E_CAPACITY;
     if (c->blocks.empty()) return FJSPH_E_STATE;
@@ -1885,17 +1914,21 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         c->reorder_pending = true;
     }
     TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true));
+    if (which == FJSPH_BOTH) { /* pn = pnp1 = the uploaded state: one transfer, a device copy */
+        launch_copy(state_fields(WS(c), c->D), state_fields(PN(c), c->D), c->n, c->stream);
+        c->launches++;
+    }
     if (grouped(c)) TRY(upload_groups(c));
-    if (which == FJSPH_PNP1 && st->part_id) { /* ids of inserted particles continue from here */
+    if (which != FJSPH_PN && st->part_id) { /* ids of inserted particles continue from here */
         c->part_id_next = 0;
         for (int64_t i = 0; i < st->n; ++i) c->part_id_next = std::max<int64_t>(c->part_id_next, st->part_id[i] + 1);
     }
-    if (which == FJSPH_PNP1) {
+    if (which != FJSPH_PN) {
         c->nbr_valid = false;
         mark_full(c);
     }
-    c->pn_equals_W = false;
-    return FJSPH_OK;
+    c->pn_equals_W = which == FJSPH_BOTH;
+    return sync(c);
 }
 
 int fjsph_state_download(fjsph_ctx *c, int32_t which, fjsph_state_view *st) {

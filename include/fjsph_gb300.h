@@ -173,6 +173,7 @@ typedef struct fjsph_ctx fjsph_ctx;
 /* Which of the two states a call reads or writes: time n (pn) or the working state (pnp1). */
 #define FJSPH_PN 0
 #define FJSPH_PNP1 1
+#define FJSPH_BOTH 2 /* upload only: the state becomes both pn and pnp1 (one host transfer) */
 
 /* ---- settings helpers (src/Var.h defaults, src/IO.cpp:26-128 Set_Values) -------------------- */
 int fjsph_settings_defaults(fjsph_settings *s, int32_t dim);
