@@ -780,7 +780,7 @@ int search(fjsph_ctx *c) {
     }
     launch_hash_and_count(P, WS(c), c->xs, c->G, s);
     launch_scan_i32(c->G.count, c->G.start, c->G.table_size, c->G.scan_tmp, s);
-    launch_scatter_sort(P, c->G, s);
+    launch_scatter_sort(P, c->G, c->xs[0], s);
     c->launches += 2 + 1 + 3 + 2;
     const bool due = c->s.reorder_interval > 0 && (c->reorder_pending || (c->searches % c->s.reorder_interval) == 0);
     if (due) {
@@ -1707,6 +1707,7 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     A(dalloc(c, &G.sorted, capacity));
     A(dalloc(c, &G.sorted_hi, capacity));
     A(dalloc(c, &G.sorted_lo, capacity));
+    A(dalloc(c, &G.sorted_x, capacity));
     A(dalloc(c, &G.bbox, 8));
     A(dalloc(c, &G.grid, 4));
     A(dalloc(c, &c->nbr_counts, capacity));

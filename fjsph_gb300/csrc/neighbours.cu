@@ -7,8 +7,8 @@
  *   2. every particle hashes its cell's linear index into a power-of-two bucket table;
  *      while the grid has no more cells than buckets the hash is the identity, so a row of three
  *      x-adjacent cells is one contiguous bucket range;
- *   3. counting sort of particles by bucket (histogram, exclusive scan, scatter, then an
- *      in-bucket sort by slot so the order is deterministic);
+ *   3. counting sort of particles by bucket (histogram, exclusive scan, scatter, then each
+ *      particle's rank in its bucket by (x, slot)), so buckets are sorted by x;
  *   4. per particle, count and then write its neighbours in CSR form.
  * Membership is the reference's test, d2 < sr with d2 = fma(dz,dz,fma(dy,dy,dx*dx)) in FP64.
  * It is decided first in FP32 on the rounded coordinates, and in FP64 only when the FP32 value
@@ -161,28 +161,41 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
     atomicAdd(&G.count[h], 1);
 }
 
-__global__ void k_scatter(Params P, CellGrid G, int32_t *cursor) {
+/* Order key of a coordinate: the IEEE bits mapped so that unsigned order is numeric order
+ * (a total order, NaN included, so bucket ranks are always a permutation). */
+__device__ __forceinline__ unsigned long long x_key(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+/* Scatter of slots into their buckets in arrival order; each entry's (x key, slot) goes to
+ * sorted_lo, which serves as scratch until the coordinates are written in bucket order. */
+__global__ void k_scatter(Params P, CellGrid G, const double *xs0, int32_t *cursor) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const uint32_t h = G.hash[i];
     const int32_t pos = G.start[h] + atomicAdd(&cursor[h], 1);
-    G.sorted[pos] = (int32_t)i;
+    const unsigned long long k = x_key(xs0[i]);
+    reinterpret_cast<uint4 *>(G.sorted_lo)[pos] = make_uint4((unsigned)k, (unsigned)(k >> 32), (unsigned)i, 0u);
 }
 
-/* Insertion sort of each bucket by slot (deterministic order within a bucket). */
-__global__ void k_bucket_sort(CellGrid G, int64_t nbuckets) {
-    const int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (h >= nbuckets) return;
+/* Each slot's rank in its bucket by (x, slot): buckets come out sorted by x, so a row of
+ * x-adjacent cells is sorted by x and the walk can stop at the edges of the x range it needs;
+ * the slot breaks ties, so the order is deterministic. */
+__global__ void k_bucket_rank(Params P, CellGrid G, const double *xs0) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t h = G.hash[i];
     const int32_t s0 = G.start[h], s1 = G.start[h + 1];
-    for (int32_t a = s0 + 1; a < s1; ++a) {
-        const int32_t v = G.sorted[a];
-        int32_t b = a - 1;
-        while (b >= s0 && G.sorted[b] > v) {
-            G.sorted[b + 1] = G.sorted[b];
-            --b;
-        }
-        G.sorted[b + 1] = v;
+    const unsigned long long k = x_key(xs0[i]);
+    const uint4 *ent = reinterpret_cast<const uint4 *>(G.sorted_lo);
+    int32_t rank = 0;
+    for (int32_t e = s0; e < s1; ++e) {
+        const uint4 q = ent[e];
+        const unsigned long long ke = (unsigned long long)q.x | ((unsigned long long)q.y << 32);
+        rank += (ke < k || (ke == k && (int64_t)q.z < i)) ? 1 : 0;
     }
+    G.sorted[s0 + rank] = (int32_t)i;
 }
 
 /* Coordinates in bucket order: hi = (fl32(x), slot bits), lo = fl32(x - hi). */
@@ -193,6 +206,7 @@ __global__ void k_sorted_pos(Params P, const double *xs0, const double *xs1, con
     const double x0 = xs0[s], x1 = xs1[s], x2 = P.D == 3 ? xs2[s] : 0.0;
     const float h0 = (float)x0, h1 = (float)x1, h2 = (float)x2;
     G.sorted_hi[e] = make_float4(h0, h1, h2, __int_as_float(s));
+    G.sorted_x[e] = h0;
     G.sorted_lo[e] = make_float4((float)(x0 - (double)h0), (float)(x1 - (double)h1), (float)(x2 - (double)h2), 0.f);
 }
 
@@ -237,47 +251,93 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
         }
         return false;
     };
-    auto test = [&](int32_t e) {
-        const float4 fj = G.sorted_hi[e];
+    /* FP32 test with the FP64 decision inside the rounding band */
+    auto member = [&](const float4 fj) -> bool {
         const float dx = fi[0] - fj.x, dy = fi[1] - fj.y;
         float d2f = dx * dx + dy * dy;
         if (D == 3) {
             const float dz = fi[2] - fj.z;
             d2f += dz * dz;
         }
+        if (d2f < sr_lo) return true;
+        if (d2f > sr_hi) return false;
         const int32_t j = __float_as_int(fj.w);
-        bool in;
-        if (d2f < sr_lo)
-            in = true;
-        else if (d2f > sr_hi)
-            in = false;
-        else {
-            double xj[D];
+        double xj[D];
 #pragma unroll
-            for (int k = 0; k < D; ++k) xj[k] = xs[k][j];
-            in = dist2<D>(xi, xj) < P.sr;
-        }
-        if (in) f(j, e);
+        for (int k = 0; k < D; ++k) xj[k] = xs[k][j];
+        return dist2<D>(xi, xj) < P.sr;
     };
+    /* Candidates [e0, e1) in batches of 32: a bit mask of the members first, then f for the
+     * members only, so the lanes of a warp run the (longer) member code together instead of
+     * at every candidate where some lane has a member. */
+    auto range = [&](int32_t e0, int32_t e1) {
+        for (int32_t b = e0; b < e1; b += 32) {
+            const int32_t m = e1 - b < 32 ? e1 - b : 32;
+            unsigned bits = 0u;
+            for (int32_t q = 0; q < m; ++q)
+                if (member(G.sorted_hi[b + q])) bits |= 1u << q;
+            while (bits) {
+                const int q = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                f(__float_as_int(G.sorted_hi[b + q].w), b + q);
+            }
+        }
+    };
+    /* Identity hash: the row's x range.  Buckets are sorted by x, so a row's members lie within
+     * |x_j - x_i| <= r_row with r_row^2 = R^2 - (y gap to the row)^2 - (z gap)^2: the walk tests
+     * the part of the row inside that range and skips rows beyond R.  The bounds are widened by a margin that covers the FP32
+     * rounding of both coordinates and of the bound itself, so no member is ever left out. */
+    const float Rf = sqrtf((float)P.sr);
+    const float r2f = (float)P.sr * (1.f + 1e-5f);
+    const float mx = 5e-7f * (fabsf(fi[0]) + 2.f * Rf) + 1e-5f * Rf;
+    const float ey = (float)cell_edge(P, 1), ez = (float)cell_edge(P, 2);
+    /* position of x_i inside its cell in y and z, in cell edges */
+    const float ty = (float)((xi[1] - lo[1]) / cell_edge(P, 1) - (double)c[1]);
+    const float tz = D == 3 ? (float)((xi[2] - lo[2]) / cell_edge(P, 2) - (double)c[2]) : 0.f;
+    auto gap = [](int d, float t) { /* distance to the band of row offset d, in cell edges */
+        const float g = d > 0 ? (float)d - t : (d < 0 ? t - 1.f - (float)d : 0.f);
+        return fmaxf(0.f, g - 1e-4f);
+    };
+    const bool has_left = c[0] > 0, has_right = c[0] + 1 < nc[0];
     for (int dz = -zr; dz <= zr; ++dz) {
         const int64_t cz = c[2] + dz;
         if (cz < 0 || cz >= nc[2]) continue;
+        const float gz = gap(dz, tz) * ez;
         for (int dy = -yr; dy <= yr; ++dy) {
             const int64_t cy = c[1] + dy;
             if (cy < 0 || cy >= nc[1]) continue;
             if (!wrap) {
-                /* identity hash: cells x0..x1 of this row are consecutive buckets */
-                int64_t cc[3] = {x0, cy, cz};
-                const uint64_t h0 = lin_index(cc, nc);
-                const int32_t e0 = G.start[h0], e1 = G.start[h0 + (x1 - x0) + 1];
-                for (int32_t e = e0; e < e1; ++e) test(e);
+                const float gy = gap(dy, ty) * ey;
+                const float rr2 = r2f - gy * gy - gz * gz;
+                if (rr2 <= 0.f) continue;
+                const float rr = sqrtf(rr2);
+                const float xlo = fi[0] - rr - mx, xhi = fi[0] + rr + mx;
+                int64_t cc[3] = {c[0], cy, cz};
+                const uint64_t hm = lin_index(cc, nc);
+                /* [e0, e1): the left cell's entries from the first x >= xlo, the middle cell,
+                 * the right cell's entries up to the last x <= xhi (counted with independent
+                 * loads of the compact x copy) */
+                int32_t e0 = G.start[hm], e1 = G.start[hm + 1];
+                if (has_left) {
+                    const int32_t l0 = G.start[hm - 1];
+                    int32_t below = 0;
+                    for (int32_t e = l0; e < e0; ++e) below += G.sorted_x[e] < xlo ? 1 : 0;
+                    e0 = l0 + below;
+                }
+                if (has_right) {
+                    const int32_t r1 = G.start[hm + 2];
+                    int32_t within = 0;
+                    for (int32_t e = e1; e < r1; ++e) within += G.sorted_x[e] <= xhi ? 1 : 0;
+                    e1 += within;
+                }
+                range(e0, e1);
             } else {
                 for (int64_t cx = x0; cx <= x1; ++cx) {
                     int64_t cc[3] = {cx, cy, cz};
                     const uint64_t h = lin_index(cc, nc) & mask;
                     if (visited_before(dz, dy, cx, h)) continue;
                     const int32_t e0 = G.start[h], e1 = G.start[h + 1];
-                    for (int32_t e = e0; e < e1; ++e) test(e);
+                    range(e0, e1);
                 }
             }
         }
@@ -565,12 +625,12 @@ void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, c
     scan_exclusive<int32_t, int64_t>(in, out, n, tmp, s);
 }
 
-void launch_scatter_sort(const Params &P, CellGrid &G, cudaStream_t s) {
+void launch_scatter_sort(const Params &P, CellGrid &G, const double *xs0, cudaStream_t s) {
     /* G.count is reused as the scatter cursor */
     cudaMemsetAsync(G.count, 0, sizeof(int32_t) * (G.table_size + 1), s);
     if (P.n == 0) return;
-    k_scatter<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, G.count);
-    k_bucket_sort<<<grid_for(G.table_size, kThreads), kThreads, 0, s>>>(G, G.table_size);
+    k_scatter<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, xs0, G.count);
+    k_bucket_rank<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, xs0);
 }
 
 void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s) {
