@@ -900,23 +900,23 @@ int prestep_passes(fjsph_ctx *c) {
     DevNbr N = make_nbr(c);
     cudaStream_t s = c->stream;
     TRY(prestep_npd(c, P));
+    const bool dissipation = !(c->s.variant & FJSPH_VAR_NOFROZEN);
     {
+        /* split-precision form: the dissipation terms are computed in the surface-normal walk
+         * (they read nothing the surface passes write), timed with the surface section */
         Section sec(c, PASS_SURFACE);
         launch_aero_velocity(P, WS(c), N, s);
         if (mixed(c)) {
-            launch_m_surface(P, WS(c), N, c->K, s);
+            launch_m_surface(P, WS(c), N, c->K, dissipation, s);
             c->occ_valid = true;
         } else {
             launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
         }
         c->launches += 4;
     }
-    if (!(c->s.variant & FJSPH_VAR_NOFROZEN)) {
+    if (dissipation && !mixed(c)) {
         Section sec(c, PASS_DISSIPATION);
-        if (mixed(c))
-            launch_m_dissipation(P, WS(c), N, c->K, s);
-        else
-            launch_dissipation(P, WS(c), N, s);
+        launch_dissipation(P, WS(c), N, s);
         c->launches++;
     }
     if (c->s.variant & FJSPH_VAR_ALE) {
@@ -2039,7 +2039,7 @@ int fjsph_detect_surface(fjsph_ctx *c) {
     TRY(need_nbr(c));
     if (mixed(c)) {
         ensure_pack(c);
-        launch_m_surface(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
+        launch_m_surface(make_params(c), WS(c), make_nbr(c), c->K, false, c->stream);
         c->occ_valid = true;
     } else {
         launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, c->stream);

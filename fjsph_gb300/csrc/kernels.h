@@ -137,7 +137,9 @@ void launch_m_pack(const Params &P, const DevState &W, const Packed &K, int64_t 
 void launch_m_npd(const Params &P, const DevNbr &N, const Packed &K, double *npd_part, cudaStream_t s);
 void launch_m_dsph(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, double *npd_part,
                    cudaStream_t s);
-void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
+/* with_dissipation: the dissipation terms (launch_m_dissipation) are computed in the same walk */
+void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, bool with_dissipation,
+                      cudaStream_t s);
 void launch_m_dissipation(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
 void launch_m_particle_shift(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);
 void launch_m_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s);

@@ -281,13 +281,96 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
 }
 
 /* ------------------------------------------------------------------------------------------ */
+/* artificial viscosity scalar (src/Kernel.h:217-244)                                           */
+/* ------------------------------------------------------------------------------------------ */
+__device__ __forceinline__ float f_art_visc(const Pf &f, float vdotr, float idist2, float rho_i, float rho_j) {
+    if (vdotr > 0.f) return 0.f;
+    const float muij = f.H * vdotr * idist2;
+    const float rhoij = 0.5f * (rho_i + rho_j);
+    const float cbar = 0.5f * (sqrtf(f.Bgam / rho_i) + sqrtf(f.Bgam / rho_j));
+    return f.alpha * cbar * muij / rhoij;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* dissipation_terms (src/Shifting.cpp:126-186)                                                  */
+/* ------------------------------------------------------------------------------------------ */
+/* Per-particle accumulator of the dissipation terms, shared by the stand-alone pass and the
+ * surface-normal pass that carries it (both walk every neighbour j != i of a fluid particle). */
+template <int D>
+struct Dissip {
+    bool linear, nodsph;
+    float4 Ci, Ei;
+    float rho_i;
+    float gRi[D], av[D];
+    KSum Rrhod;
+    __device__ __forceinline__ void init(const Params &P, const Pf &f, const Packed &K, int64_t i) {
+        linear = has(P, FJSPH_VAR_LINEAR);
+        nodsph = has(P, FJSPH_VAR_NODSPH);
+        Ci = K.C[i];
+        Ei = K.E[i];
+        const float4 Gi = K.G[i];
+        rho_i = f.rho0 + Ci.w;
+        gRi[0] = Gi.x;
+        gRi[1] = Gi.y;
+        if (D == 3) gRi[2] = Gi.z;
+#pragma unroll
+        for (int k = 0; k < D; ++k) av[k] = 0.f;
+    }
+    /* pair (i, j): Rji = x_j - x_i, rr = |Rji|^2, gs = f_gscale(r), Gj = K.G[j] */
+    __device__ __forceinline__ void add(const Pf &f, const Packed &K, int32_t j, const float *Rji, float rr, float gs,
+                                        float volj, const float4 Gj) {
+        const float4 Cj = K.C[j], Ej = K.E[j];
+        float Vji[D];
+        sep<D>(Ci, Ei, Cj, Ej, Vji);
+        const float idist2 = 1.f / (rr + 0.0001f * f.H_sq);
+        const float rho_j = f.rho0 + Cj.w;
+        float g[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
+        const bool fl = bits_b(K.bits[j]) > FJSPH_PISTON;
+        if (fl) {
+            const float vdotr = fdot<D>(Vji, Rji);
+            const float c = linear ? volj * idist2 * vdotr : (volj * rho_j) * f_art_visc(f, vdotr, idist2, rho_i, rho_j);
+#pragma unroll
+            for (int k = 0; k < D; ++k) av[k] += c * g[k];
+        }
+        if (!nodsph) {
+            const float rg = fdot<D>(Rji, g);
+            float t = Cj.w - Ci.w;
+            if (fl) {
+                float gsum[D];
+                gsum[0] = gRi[0] + Gj.x;
+                gsum[1] = gRi[1] + Gj.y;
+                if (D == 3) gsum[2] = gRi[2] + Gj.z;
+                t += 0.5f * fdot<D>(gsum, Rji);
+            }
+            Rrhod.add(volj * t * rg * idist2);
+        }
+    }
+    __device__ __forceinline__ void finish(const Params &P, const DevState &W, int64_t i) {
+        if (linear) {
+            const float c = (float)(P.visc_alpha * P.H * P.speed_sound * P.rho_rest) / rho_i;
+#pragma unroll
+            for (int k = 0; k < D; ++k) av[k] *= c;
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) W.aVisc[k][i] = av[k];
+        if (!nodsph) W.deltaD[i] = P.dsph_cont * Rrhod.value();
+    }
+};
+
+/* ------------------------------------------------------------------------------------------ */
 /* Detect_Surface (src/Geometry.cpp:14-280)                                                      */
 /* ------------------------------------------------------------------------------------------ */
-template <int D>
+/* DIS: the dissipation terms ride along in the normal's neighbour loop (one list walk and one
+ * set of position gathers for both; the dissipation reads nothing this pass writes). */
+template <int D, bool DIS>
 __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevState W, DevNbr N, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const Pf f = make_pf(P);
+    Dissip<D> dis;
+    if (DIS) dis.init(P, f, K, i);
     const float h = (float)(1.33 * P.particle_step);
     const float4 Ai = K.A[i], Bi = K.B[i];
     const float4 Ni = K.N[i]; /* dSPH normal, lam_nb */
@@ -360,16 +443,21 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         const int32_t j = pe.x;
         if (j == i) continue;
         float Rji[D];
-        sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
-        const float r = sqrtf(__int_as_float(pe.y));
-        const float volj = K.A[j].w;
+        const float4 Aj = K.A[j];
+        sep<D>(Ai, Bi, Aj, K.B[j], Rji);
+        const float rr = __int_as_float(pe.y);
+        const float r = sqrtf(rr);
+        const float volj = Aj.w;
         const float gs = f_gscale(f, r);
-        const float lj = K.G[j].w;
+        const float4 Gj = K.G[j];
+        const float lj = Gj.w;
         const float w = inside ? volj * (lj - lam) : volj * lj;
         /* GradK(Rij) with Rij = x_i - x_j = -Rji */
 #pragma unroll
         for (int k = 0; k < D; ++k) nrm[k] -= w * (Rji[k] * gs);
+        if (DIS) dis.add(f, K, j, Rji, rr, gs, volj, Gj);
     }
+    if (DIS) dis.finish(P, W, i);
     float n2[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
@@ -475,83 +563,26 @@ __global__ void k_m_surface_zone(Params P, DevState W, DevNbr N, Packed K) {
     if (sz) atomicOr(&K.bits[i], 16);
 }
 
-/* ------------------------------------------------------------------------------------------ */
-/* artificial viscosity scalar (src/Kernel.h:217-244)                                           */
-/* ------------------------------------------------------------------------------------------ */
-__device__ __forceinline__ float f_art_visc(const Pf &f, float vdotr, float idist2, float rho_i, float rho_j) {
-    if (vdotr > 0.f) return 0.f;
-    const float muij = f.H * vdotr * idist2;
-    const float rhoij = 0.5f * (rho_i + rho_j);
-    const float cbar = 0.5f * (sqrtf(f.Bgam / rho_i) + sqrtf(f.Bgam / rho_j));
-    return f.alpha * cbar * muij / rhoij;
-}
-
-/* ------------------------------------------------------------------------------------------ */
-/* dissipation_terms (src/Shifting.cpp:126-186)                                                  */
-/* ------------------------------------------------------------------------------------------ */
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_m_dissipation(Params P, DevState W, DevNbr N, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const Pf f = make_pf(P);
-    const bool linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH);
-    const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Gi = K.G[i];
-    const float rho_i = f.rho0 + Ci.w;
-    float gRi[D];
-    gRi[0] = Gi.x;
-    gRi[1] = Gi.y;
-    if (D == 3) gRi[2] = Gi.z;
-    float av[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) av[k] = 0.f;
-    KSum Rrhod;
+    const float4 Ai = K.A[i], Bi = K.B[i];
+    Dissip<D> dis;
+    dis.init(P, f, K, i);
     const SellList L = sell(N, i);
     for (int32_t e = 0; e < L.n; ++e) {
         const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
-        const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
-        float Rji[D], Vji[D];
+        const float4 Aj = K.A[j], Bj = K.B[j];
+        float Rji[D];
         sep<D>(Ai, Bi, Aj, Bj, Rji);
-        sep<D>(Ci, Ei, Cj, Ej, Vji);
         const float rr = __int_as_float(pe.y);
-        const float r = sqrtf(rr);
-        const float idist2 = 1.f / (rr + 0.0001f * f.H_sq);
-        const float volj = Aj.w;
-        const float rho_j = f.rho0 + Cj.w;
-        const float gs = f_gscale(f, r);
-        float g[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
-        const bool fl = bits_b(K.bits[j]) > FJSPH_PISTON;
-        if (fl) {
-            const float vdotr = fdot<D>(Vji, Rji);
-            const float c = linear ? volj * idist2 * vdotr : (volj * rho_j) * f_art_visc(f, vdotr, idist2, rho_i, rho_j);
-#pragma unroll
-            for (int k = 0; k < D; ++k) av[k] += c * g[k];
-        }
-        if (!nodsph) {
-            const float rg = fdot<D>(Rji, g);
-            float t = Cj.w - Ci.w;
-            if (fl) {
-                const float4 Gj = K.G[j];
-                float gsum[D];
-                gsum[0] = gRi[0] + Gj.x;
-                gsum[1] = gRi[1] + Gj.y;
-                if (D == 3) gsum[2] = gRi[2] + Gj.z;
-                t += 0.5f * fdot<D>(gsum, Rji);
-            }
-            Rrhod.add(volj * t * rg * idist2);
-        }
+        dis.add(f, K, j, Rji, rr, f_gscale(f, sqrtf(rr)), Aj.w, K.G[j]);
     }
-    if (linear) {
-        const float c = (float)(P.visc_alpha * P.H * P.speed_sound * P.rho_rest) / rho_i;
-#pragma unroll
-        for (int k = 0; k < D; ++k) av[k] *= c;
-    }
-#pragma unroll
-    for (int k = 0; k < D; ++k) W.aVisc[k][i] = av[k];
-    if (!nodsph) W.deltaD[i] = P.dsph_cont * Rrhod.value();
+    dis.finish(P, W, i);
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -954,8 +985,21 @@ void launch_m_dsph(const Params &P, const DevState &W, const DevNbr &N, const Pa
                    cudaStream_t s) {
     FJSPH_DISPATCH_M(P, k_m_dsph, agrid(P), P, W, N, K, npd_part);
 }
-void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
-    FJSPH_DISPATCH_M(P, k_m_surface_normal, fgrid(P), P, W, N, K);
+void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, bool with_dissipation,
+                      cudaStream_t s) {
+    if (fgrid(P) > 0) {
+        if (with_dissipation) {
+            if (P.D == 2)
+                k_m_surface_normal<2, true><<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
+            else
+                k_m_surface_normal<3, true><<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
+        } else {
+            if (P.D == 2)
+                k_m_surface_normal<2, false><<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
+            else
+                k_m_surface_normal<3, false><<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
+        }
+    }
     FJSPH_DISPATCH_M(P, k_m_surface_curvature, fgrid(P), P, W, N, K);
     if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fgrid(P) > 0)
         k_m_surface_zone<<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
