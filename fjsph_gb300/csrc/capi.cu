@@ -296,6 +296,10 @@ Params make_params(const fjsph_ctx *c) {
     P.H = s.H;
     P.H_sq = s.H_sq;
     P.sr = s.sr;
+    for (int k = 0; k < 3; ++k) {
+        P.cell_edge[k] = std::sqrt(s.sr) / (k == 0 ? 1 : kCellDiv) * (1.0 + 1e-6);
+        P.cell_inv[k] = 1.0 / P.cell_edge[k];
+    }
     P.W_correc = s.W_correc;
     P.W_dx = s.W_dx;
     P.dx = s.dx;
@@ -779,7 +783,7 @@ int search(fjsph_ctx *c) {
         }
     }
     launch_hash_and_count(P, WS(c), c->xs, c->G, s);
-    launch_scan_i32(c->G.count, c->G.start, c->G.table_size, c->G.scan_tmp, s);
+    launch_scan_buckets(c->G, s);
     launch_scatter_sort(P, c->G, c->xs[0], s);
     c->launches += 2 + 1 + 3 + 2;
     const bool due = c->s.reorder_interval > 0 && (c->reorder_pending || (c->searches % c->s.reorder_interval) == 0);
@@ -1709,7 +1713,7 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     A(dalloc(c, &G.sorted_lo, capacity));
     A(dalloc(c, &G.sorted_x, capacity));
     A(dalloc(c, &G.bbox, 8));
-    A(dalloc(c, &G.grid, 4));
+    A(dalloc(c, &G.grid, 8));
     A(dalloc(c, &c->nbr_counts, capacity));
     A(dalloc(c, &c->nbr_off, capacity + 1));
     A(dalloc(c, &c->slice_w, capacity / kSlice + 2));

@@ -78,7 +78,17 @@ struct Params {
     /* launch configuration of the split-precision pair sweeps (the autotuner's choices) */
     int32_t sweep_threads, resid_threads, list_ahead;
     FConst fc;
+    /* neighbour-search cell edges (support radius along x, radius / kCellDiv across) and their
+     * reciprocals, so cell coordinates cost a multiply instead of an FP64 divide */
+    double cell_edge[3], cell_inv[3];
 };
+
+/* Cells are the support radius long along x (the contiguous direction of a bucket row) and
+ * radius / kCellDiv across it. */
+#ifndef CELL_DIV_DEFAULT
+#define CELL_DIV_DEFAULT 2
+#endif
+constexpr int kCellDiv = CELL_DIV_DEFAULT;
 
 __device__ __forceinline__ int32_t grp_of(const Params &P, int64_t i) { return P.grp ? P.grp[i] : 0; }
 __device__ __forceinline__ double vinf_of(const Params &P, int64_t i, int k) {

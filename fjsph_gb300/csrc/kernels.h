@@ -85,7 +85,7 @@ struct CellGrid {
     float4 *sorted_lo;       /* [cap]  fl32(x - hi) in bucket order           */
     float *sorted_x;         /* [cap]  fl32(x) of the x axis in bucket order  */
     double *bbox;            /* [8]    lo[3], hi[3], band, spare (device)     */
-    int64_t *grid;           /* [4]    nx, ny, nz, wrap flag (device)         */
+    int64_t *grid;           /* [8]    nx, ny, nz, wrap flag, buckets in use  */
     int32_t *scan_tmp;       /* scan partials                                 */
     int64_t scan_tmp_len;
 };
@@ -93,6 +93,8 @@ struct CellGrid {
 void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s);
 void launch_hash_and_count(const Params &P, const DevState &W, double *const xs[3], CellGrid &G, cudaStream_t s);
 void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, cudaStream_t s);
+/* exclusive scan of the bucket counts over the buckets the grid uses (G.grid[4], on the device) */
+void launch_scan_buckets(CellGrid &G, cudaStream_t s);
 void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s);
 void launch_scatter_sort(const Params &P, CellGrid &G, const double *xs0, cudaStream_t s);
 void launch_nbr_count(const Params &P, double *const xs[3], const CellGrid &G, int32_t *counts, cudaStream_t s);

@@ -20,10 +20,6 @@
  */
 #include "kernels.h"
 
-#ifndef CELL_DIV_DEFAULT
-#define CELL_DIV_DEFAULT 2
-#endif
-
 namespace fjsph {
 
 namespace {
@@ -37,10 +33,10 @@ constexpr int64_t kMaxAxis = (int64_t)1 << 20;
  * 2H / kCellDiv across it; the walk visits 3 cells of each of (2 kCellDiv + 1)^(D-1) rows.  With
  * kCellDiv = 2 the visited volume is 6H x 5H x 5H instead of (6H)^3 (30 % fewer candidate tests)
  * for four times the cells; halving x as well would make sparse domains (the jet's bounding box
- * is mostly air) outgrow the largest bucket table. */
-constexpr int kCellDiv = CELL_DIV_DEFAULT;
-__device__ __forceinline__ double cell_edge(const Params &P, int axis) {
-    return sqrt(P.sr) / (axis == 0 ? 1 : kCellDiv) * (1.0 + 1e-6);
+ * is mostly air) outgrow the largest bucket table.  Cell coordinates are floor((x - lo) * inv)
+ * with inv = 1 / edge from the host (Params::cell_inv), the same product everywhere. */
+__device__ __forceinline__ double cell_pos(const Params &P, double x, double lo, int axis) {
+    return (x - lo) * P.cell_inv[axis];
 }
 
 /* ---- bounding box ----------------------------------------------------------------------------- */
@@ -97,7 +93,7 @@ __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bb
             lo[k] = 0.0;
             hi[k] = 0.0;
         }
-        double c = floor((hi[k] - lo[k]) / cell_edge(P, k)) + 1.0;
+        double c = floor(cell_pos(P, hi[k], lo[k], k)) + 1.0;
         if (!(c < (double)kMaxAxis)) c = (double)kMaxAxis;
         nc[k] = (int64_t)c;
         mag = fmax(mag, fmax(fabs(lo[k]), fabs(hi[k])));
@@ -118,6 +114,7 @@ __global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bb
     grid[2] = nc[2];
     const double ncells = (double)nc[0] * (double)nc[1] * (double)nc[2];
     grid[3] = ncells > (double)table ? 1 : 0;
+    grid[4] = ncells > (double)table ? table : (int64_t)ncells; /* buckets in use */
 }
 
 /* ---- hashing ---------------------------------------------------------------------------------- */
@@ -128,7 +125,7 @@ __device__ __forceinline__ void cell_coords(const Params &P, const double *x, co
     for (int k = 0; k < 3; ++k) c[k] = 0;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        double f = floor((x[k] - lo[k]) / cell_edge(P, k));
+        double f = floor(cell_pos(P, x[k], lo[k], k));
         int64_t v = (f > 0.0) ? (int64_t)fmin(f, (double)(nc[k] - 1)) : 0;
         c[k] = v;
     }
@@ -158,7 +155,9 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
     cell_coords<D>(P, x, lo, nc, c);
     const uint32_t h = (uint32_t)(lin_index(c, nc) & (uint64_t)(G.table_size - 1));
     G.hash[i] = h;
-    atomicAdd(&G.count[h], 1);
+    /* lanes of a warp in the same bucket (consecutive slots usually are) add once */
+    const unsigned peers = __match_any_sync(__activemask(), h);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&G.count[h], (int32_t)__popc(peers));
 }
 
 /* Order key of a coordinate: the IEEE bits mapped so that unsigned order is numeric order
@@ -290,10 +289,10 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     const float Rf = sqrtf((float)P.sr);
     const float r2f = (float)P.sr * (1.f + 1e-5f);
     const float mx = 5e-7f * (fabsf(fi[0]) + 2.f * Rf) + 1e-5f * Rf;
-    const float ey = (float)cell_edge(P, 1), ez = (float)cell_edge(P, 2);
+    const float ey = (float)P.cell_edge[1], ez = (float)P.cell_edge[2];
     /* position of x_i inside its cell in y and z, in cell edges */
-    const float ty = (float)((xi[1] - lo[1]) / cell_edge(P, 1) - (double)c[1]);
-    const float tz = D == 3 ? (float)((xi[2] - lo[2]) / cell_edge(P, 2) - (double)c[2]) : 0.f;
+    const float ty = (float)(cell_pos(P, xi[1], lo[1], 1) - (double)c[1]);
+    const float tz = D == 3 ? (float)(cell_pos(P, xi[2], lo[2], 2) - (double)c[2]) : 0.f;
     auto gap = [](int d, float t) { /* distance to the band of row offset d, in cell edges */
         const float g = d > 0 ? (float)d - t : (d < 0 ? t - 1.f - (float)d : 0.f);
         return fmaxf(0.f, g - 1e-4f);
@@ -539,42 +538,70 @@ __device__ TO block_tile_scan(const TI *in, TO *out, int64_t base, int64_t n, TO
     return total;
 }
 
+/* Scans take an optional device-side length n_dev (the bucket table is scanned only up to the
+ * cells the grid has, which the host does not know without a round trip): the scanned length is
+ * min(*n_dev, n), tiles beyond it do nothing, and out[length] receives the total. */
+__device__ __forceinline__ int64_t scan_len(int64_t n, const int64_t *n_dev) {
+    if (!n_dev) return n;
+    const int64_t m = *n_dev;
+    return m < n ? m : n;
+}
+
 template <typename TI, typename TO>
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const TI *in, int64_t n, TO *tile_sums) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const TI *in, int64_t n, const int64_t *n_dev,
+                                                               TO *tile_sums) {
+    const int64_t ne = scan_len(n, n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanThreads * kScanItems;
-    TO t = block_tile_scan<TI, TO>(in, (TO *)nullptr, base, n, (TO)0, false);
+    if (base >= ne) { /* uniform per block */
+        if (threadIdx.x == 0) tile_sums[blockIdx.x] = (TO)0;
+        return;
+    }
+    TO t = block_tile_scan<TI, TO>(in, (TO *)nullptr, base, ne, (TO)0, false);
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = t;
 }
 
 template <typename TO>
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(TO *tile_sums, int64_t ntiles) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(TO *tile_sums, int64_t ntiles, TO *out, int64_t n,
+                                                              const int64_t *n_dev) {
     /* exclusive scan of the tile totals, in place, one block walking tiles of the tile array */
     TO carry = 0;
     for (int64_t base = 0; base < ntiles; base += (int64_t)kScanThreads * kScanItems) {
         TO t = block_tile_scan<TO, TO>(tile_sums, tile_sums, base, ntiles, carry, true);
         carry += t;
     }
-    if (threadIdx.x == 0) tile_sums[ntiles] = carry;
+    if (threadIdx.x == 0) {
+        tile_sums[ntiles] = carry;
+        out[scan_len(n, n_dev)] = carry;
+    }
 }
 
 template <typename TI, typename TO>
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const TI *in, TO *out, int64_t n, const TO *tile_sums) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const TI *in, TO *out, int64_t n, const int64_t *n_dev,
+                                                              const TO *tile_sums) {
+    const int64_t ne = scan_len(n, n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanThreads * kScanItems;
-    block_tile_scan<TI, TO>(in, out, base, n, tile_sums[blockIdx.x], true);
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tile_sums[gridDim.x];
+    if (base >= ne) return;
+    block_tile_scan<TI, TO>(in, out, base, ne, tile_sums[blockIdx.x], true);
 }
 
 template <typename TI, typename TO>
-void scan_exclusive(const TI *in, TO *out, int64_t n, TO *tmp, cudaStream_t s) {
+void scan_exclusive(const TI *in, TO *out, int64_t n, TO *tmp, cudaStream_t s, const int64_t *n_dev = nullptr) {
     const int64_t tile = (int64_t)kScanThreads * kScanItems;
     const int64_t ntiles = (n + tile - 1) / tile;
     if (ntiles == 0) {
         cudaMemsetAsync(out, 0, sizeof(TO), s);
         return;
     }
-    k_scan_reduce<TI, TO><<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tmp);
-    k_scan_tiles<TO><<<1, kScanThreads, 0, s>>>(tmp, ntiles);
-    k_scan_apply<TI, TO><<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, out, n, tmp);
+    k_scan_reduce<TI, TO><<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, n_dev, tmp);
+    k_scan_tiles<TO><<<1, kScanThreads, 0, s>>>(tmp, ntiles, out, n, n_dev);
+    k_scan_apply<TI, TO><<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, out, n, n_dev, tmp);
+}
+
+/* zero a[0 .. min(*n_dev, nmax)] (the bucket counts the grid uses) */
+__global__ void k_zero_counts(int32_t *a, int64_t nmax, const int64_t *n_dev) {
+    const int64_t n = scan_len(nmax, n_dev) + 1;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        a[k] = 0;
 }
 
 /* ---- re-ordering ------------------------------------------------------------------------------ */
@@ -609,8 +636,13 @@ void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s
     k_bbox_finish<<<1, 32, 0, s>>>(P, part, nblk, G.bbox, G.grid, G.table_size);
 }
 
+void zero_counts(CellGrid &G, cudaStream_t s) {
+    const int64_t blocks = std::min<int64_t>((G.table_size + 1 + 255) / 256, 152 * 16);
+    k_zero_counts<<<(unsigned)blocks, 256, 0, s>>>(G.count, G.table_size, G.grid + 4);
+}
+
 void launch_hash_and_count(const Params &P, const DevState &W, double *const xs[3], CellGrid &G, cudaStream_t s) {
-    cudaMemsetAsync(G.count, 0, sizeof(int32_t) * (G.table_size + 1), s);
+    zero_counts(G, s);
     if (P.n == 0) return;
     if (P.D == 2)
         k_hash_count<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, W, xs[0], xs[1], xs[2], G);
@@ -621,13 +653,16 @@ void launch_hash_and_count(const Params &P, const DevState &W, double *const xs[
 void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, cudaStream_t s) {
     scan_exclusive<int32_t, int32_t>(in, out, n, tmp, s);
 }
+void launch_scan_buckets(CellGrid &G, cudaStream_t s) {
+    scan_exclusive<int32_t, int32_t>(G.count, G.start, G.table_size, G.scan_tmp, s, G.grid + 4);
+}
 void launch_scan_i64(const int32_t *in, int64_t *out, int64_t n, int64_t *tmp, cudaStream_t s) {
     scan_exclusive<int32_t, int64_t>(in, out, n, tmp, s);
 }
 
 void launch_scatter_sort(const Params &P, CellGrid &G, const double *xs0, cudaStream_t s) {
     /* G.count is reused as the scatter cursor */
-    cudaMemsetAsync(G.count, 0, sizeof(int32_t) * (G.table_size + 1), s);
+    zero_counts(G, s);
     if (P.n == 0) return;
     k_scatter<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, xs0, G.count);
     k_bucket_rank<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, xs0);
