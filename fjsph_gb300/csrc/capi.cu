@@ -246,7 +246,7 @@ int alloc_table(fjsph_ctx *c, int64_t size) {
     G.table_size = size;
     TRY(dalloc(c, &G.count, G.table_size + 1));
     TRY(dalloc(c, &G.start, G.table_size + 1));
-    G.scan_tmp_len = std::max<int64_t>(G.table_size / 2048 + 16, 304 * 6 * 2 + 16);
+    G.scan_tmp_len = std::max<int64_t>(G.table_size / 2048 + 16, (int64_t)kBboxBlocks * 12 + 16);
     TRY(dalloc(c, &G.scan_tmp, G.scan_tmp_len));
     return FJSPH_OK;
 }

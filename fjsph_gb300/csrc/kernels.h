@@ -90,6 +90,8 @@ struct CellGrid {
     int64_t scan_tmp_len;
 };
 
+/* blocks of the bounding-box reduction; scan_tmp holds 12 int32 words of partials per block */
+constexpr int kBboxBlocks = 1216;
 void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s);
 void launch_hash_and_count(const Params &P, const DevState &W, double *const xs[3], CellGrid &G, cudaStream_t s);
 void launch_scan_i32(const int32_t *in, int32_t *out, int64_t n, int32_t *tmp, cudaStream_t s);

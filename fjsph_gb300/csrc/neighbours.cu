@@ -40,52 +40,80 @@ __device__ __forceinline__ double cell_pos(const Params &P, double x, double lo,
 }
 
 /* ---- bounding box ----------------------------------------------------------------------------- */
-__global__ void k_bbox_part(Params P, DevState W, double *part) {
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+/* Order key of a coordinate: the IEEE bits mapped so that unsigned order is numeric order (a
+ * total order, NaN included, so bucket ranks by key are always a permutation). */
+__device__ __forceinline__ unsigned long long x_key(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_x(unsigned long long k) {
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
+
+/* Per-block minimum and maximum of every axis as order keys (integer compares instead of the
+ * FP64 pipe); NaN coordinates are skipped, as fmin / fmax skip them. */
+template <int D>
+__global__ void __launch_bounds__(256) k_bbox_part(Params P, DevState W, unsigned long long *part) {
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n; i += (int64_t)gridDim.x * blockDim.x) {
-        for (int k = 0; k < P.D; ++k) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
             const double x = W.x[k][i];
-            lo[k] = fmin(lo[k], x);
-            hi[k] = fmax(hi[k], x);
+            if (is_nan_bits(x)) continue;
+            const unsigned long long q = x_key(x);
+            lo[k] = umin64(lo[k], q);
+            hi[k] = umax64(hi[k], q);
         }
     }
-    __shared__ double sh[6][kThreads];
-    for (int k = 0; k < 3; ++k) {
-        sh[k][threadIdx.x] = lo[k];
-        sh[3 + k][threadIdx.x] = hi[k];
-    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = umin64(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = umax64(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    __shared__ unsigned long long sh[6][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sh[k][wid] = lo[k];
+            sh[3 + k][wid] = hi[k];
+        }
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s)
-            for (int k = 0; k < 3; ++k) {
-                sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
-                sh[3 + k][threadIdx.x] = fmax(sh[3 + k][threadIdx.x], sh[3 + k][threadIdx.x + s]);
-            }
-        __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        unsigned long long v = sh[k][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = k < 3 ? umin64(v, sh[k][w]) : umax64(v, sh[k][w]);
+        part[blockIdx.x * 6 + k] = v;
     }
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 6; ++k) part[blockIdx.x * 6 + k] = sh[k][0];
 }
 
-__global__ void k_bbox_finish(Params P, const double *part, int nblk, double *bbox, int64_t *grid, int64_t table) {
-    __shared__ double sh[6][32];
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+__global__ void k_bbox_finish(Params P, const unsigned long long *part, int nblk, double *bbox, int64_t *grid,
+                              int64_t table) {
+    unsigned long long klo[3] = {~0ull, ~0ull, ~0ull}, khi[3] = {0ull, 0ull, 0ull};
     for (int b = threadIdx.x; b < nblk; b += 32)
         for (int k = 0; k < 3; ++k) {
-            lo[k] = fmin(lo[k], part[b * 6 + k]);
-            hi[k] = fmax(hi[k], part[b * 6 + 3 + k]);
+            klo[k] = umin64(klo[k], part[b * 6 + k]);
+            khi[k] = umax64(khi[k], part[b * 6 + 3 + k]);
         }
-    for (int k = 0; k < 3; ++k) {
-        sh[k][threadIdx.x] = lo[k];
-        sh[3 + k][threadIdx.x] = hi[k];
-    }
-    __syncwarp();
+    for (int k = 0; k < 3; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            klo[k] = umin64(klo[k], __shfl_xor_sync(0xffffffffu, klo[k], o));
+            khi[k] = umax64(khi[k], __shfl_xor_sync(0xffffffffu, khi[k], o));
+        }
     if (threadIdx.x != 0) return;
-    for (int t = 1; t < 32; ++t)
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = fmin(lo[k], sh[k][t]);
-            hi[k] = fmax(hi[k], sh[3 + k][t]);
-        }
+    /* an axis without a finite value decodes to NaN bounds and is treated as empty below */
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = klo[k] <= khi[k] ? key_x(klo[k]) : NAN;
+        hi[k] = klo[k] <= khi[k] ? key_x(khi[k]) : NAN;
+    }
     int64_t nc[3] = {1, 1, 1};
     double mag = 0.0;
     for (int k = 0; k < P.D; ++k) {
@@ -158,13 +186,6 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
     /* lanes of a warp in the same bucket (consecutive slots usually are) add once */
     const unsigned peers = __match_any_sync(__activemask(), h);
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&G.count[h], (int32_t)__popc(peers));
-}
-
-/* Order key of a coordinate: the IEEE bits mapped so that unsigned order is numeric order
- * (a total order, NaN included, so bucket ranks are always a permutation). */
-__device__ __forceinline__ unsigned long long x_key(double x) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
 /* Scatter of slots into their buckets in arrival order; each entry's (x key, slot) goes to
@@ -507,11 +528,23 @@ __device__ TO block_tile_scan(const TI *in, TO *out, int64_t base, int64_t n, TO
     __shared__ TO wsum[kScanThreads / 32];
     TO v[kScanItems];
     TO local = 0;
+    const int64_t i0 = base + (int64_t)threadIdx.x * kScanItems;
+    if (sizeof(TI) == 4 && kScanItems == 8 && i0 + kScanItems <= n && (reinterpret_cast<uintptr_t>(in + i0) & 15) == 0) {
+        /* whole, aligned run of 8 32-bit items: two 16-byte loads */
+        const int4 a = reinterpret_cast<const int4 *>(in + i0)[0], b = reinterpret_cast<const int4 *>(in + i0)[1];
+        const int32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        const int64_t idx = base + (int64_t)threadIdx.x * kScanItems + k;
-        v[k] = idx < n ? (TO)in[idx] : (TO)0;
-        local += v[k];
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = (TO)(TI)w[k];
+            local += v[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            const int64_t idx = i0 + k;
+            v[k] = idx < n ? (TO)in[idx] : (TO)0;
+            local += v[k];
+        }
     }
     TO incl = warp_incl_scan<TO>(local);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -527,11 +560,23 @@ __device__ TO block_tile_scan(const TI *in, TO *out, int64_t base, int64_t n, TO
     const TO total = wsum[kScanThreads / 32 - 1];
     if (write) {
         TO run = carry + warp_off + incl - local;
+        if (sizeof(TO) == 4 && kScanItems == 8 && i0 + kScanItems <= n &&
+            (reinterpret_cast<uintptr_t>(out + i0) & 15) == 0) {
+            int32_t w[8];
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            const int64_t idx = base + (int64_t)threadIdx.x * kScanItems + k;
-            if (idx < n) out[idx] = run;
-            run += v[k];
+            for (int k = 0; k < kScanItems; ++k) {
+                w[k] = (int32_t)run;
+                run += v[k];
+            }
+            reinterpret_cast<int4 *>(out + i0)[0] = make_int4(w[0], w[1], w[2], w[3]);
+            reinterpret_cast<int4 *>(out + i0)[1] = make_int4(w[4], w[5], w[6], w[7]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k) {
+                const int64_t idx = i0 + k;
+                if (idx < n) out[idx] = run;
+                run += v[k];
+            }
         }
     }
     __syncthreads();
@@ -628,11 +673,14 @@ void launch_sorted_pos(const Params &P, double *const xs[3], CellGrid &G, cudaSt
 }
 
 void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s) {
-    /* partials live in the upper part of scan_tmp (reinterpreted) */
-    int nblk = (int)std::min<int64_t>(grid_for(P.n, kThreads), 304);
+    /* partials (6 keys per block) live in scan_tmp, which the bucket scan overwrites later */
+    int nblk = (int)std::min<int64_t>(grid_for(P.n, 256), kBboxBlocks);
     if (nblk < 1) nblk = 1;
-    double *part = reinterpret_cast<double *>(G.scan_tmp);
-    k_bbox_part<<<nblk, kThreads, 0, s>>>(P, W, part);
+    unsigned long long *part = reinterpret_cast<unsigned long long *>(G.scan_tmp);
+    if (P.D == 2)
+        k_bbox_part<2><<<nblk, 256, 0, s>>>(P, W, part);
+    else
+        k_bbox_part<3><<<nblk, 256, 0, s>>>(P, W, part);
     k_bbox_finish<<<1, 32, 0, s>>>(P, part, nblk, G.bbox, G.grid, G.table_size);
 }
 
