@@ -305,6 +305,7 @@ Params make_params(const fjsph_ctx *c) {
     P.dx = s.dx;
     P.particle_step = s.particle_step;
     P.rho_rest = s.rho_rest;
+    P.rho_rest_inv = 1.0 / s.rho_rest;
     P.B = s.B;
     P.gam = s.gam;
     P.speed_sound = s.speed_sound;
@@ -1159,7 +1160,8 @@ int find_timestep(fjsph_ctx *c, double *dt_out) {
     c->launches += 2;
     CU(cudaMemcpyAsync(&c->hsc->red[2], &c->dsc->red[2], sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
     TRY(sync(c));
-    const double *r = &c->hsc->red[2];
+    double r[7];
+    timestep_maxima(&c->hsc->red[2], r);
     const fjsph_settings &s = c->s;
     const bool any = c->n > c->nb;
     c->maxf = any ? r[0] : kEps;

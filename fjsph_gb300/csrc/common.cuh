@@ -62,6 +62,7 @@ struct Params {
     uint32_t variant;
     int32_t st_model, pressure_rel, acase, use_lam, use_TAB_def;
     double H, H_sq, sr, W_correc, W_dx, dx, particle_step;
+    double rho_rest_inv; /* 1 / rho_rest: the equation of state multiplies (no FP64 divide) */
     double rho_rest, B, gam, speed_sound, press_back, rho_min, rho_max;
     double visc_alpha, mu, nu, sig, dsph_cont, max_shift_vel;
     double grav[3], v_inf[3];
@@ -226,7 +227,7 @@ __device__ __forceinline__ double cole_power(double x, double gam) {
 /* FLUID::get_pressure / get_density (Var.h:203-236). */
 __device__ __forceinline__ double eos_pressure(const Params &P, double rho) {
     if (P.pressure_rel == FJSPH_ISO_EOS) return P.speed_sound * P.speed_sound * (rho - P.rho_rest) + P.press_back;
-    return P.B * (cole_power(rho / P.rho_rest, P.gam) - 1.0) + P.press_back;
+    return P.B * (cole_power(rho * P.rho_rest_inv, P.gam) - 1.0) + P.press_back;
 }
 __device__ __forceinline__ double eos_density(const Params &P, double press) {
     if (P.pressure_rel == FJSPH_ISO_EOS) return (press - P.press_back) / (P.speed_sound * P.speed_sound) + P.rho_rest;

@@ -85,18 +85,19 @@ __global__ void k_group_timestep(Params P, DevState W, double *red) {
     load3<D>(W.Af, i, af);
     load3<D>(W.v, i, vv);
     double *r = red + 8 * g;
-    atomic_max_nonneg(&r[0], vnorm<D, double>(a));
-    atomic_max_nonneg(&r[1], vnorm<D, double>(af));
+    /* norms as their squares and the surface-tension bound as its square-root argument (the
+     * roots are taken once per group in k_group_dt, as the single-simulation reduction does) */
+    atomic_max_nonneg(&r[0], dot<D, double>(a, a));
+    atomic_max_nonneg(&r[1], dot<D, double>(af, af));
     atomic_max_nonneg(&r[2], fabs(W.Rrho[i]));
     const double rho = W.rho[i];
     atomic_max_nonneg(&r[3], fabs(rho - P.rho_rest));
-    const double st = sqrt(rho * P.dx * P.dx / (2.0 * kPi * P.sig * fabs(W.curve[i])));
-    atomic_min_nonneg(&r[4], st);
-    atomic_max_nonneg(&r[5], vnorm<D, double>(vv));
+    atomic_min_nonneg(&r[4], rho * P.dx * P.dx / (2.0 * kPi * P.sig * fabs(W.curve[i])));
+    atomic_max_nonneg(&r[5], dot<D, double>(vv, vv));
     if (has(P, FJSPH_VAR_ALE)) {
         double vp[D];
         load3<D>(W.vPert, i, vp);
-        atomic_max_nonneg(&r[6], vnorm<D, double>(vp));
+        atomic_max_nonneg(&r[6], dot<D, double>(vp, vp));
     }
 }
 
@@ -104,10 +105,9 @@ __global__ void k_group_red_init(double *red, int32_t G) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
     double *r = red + 8 * g;
-    r[0] = r[1] = r[2] = r[3] = r[5] = kEps;
-    r[4] = 9999999.0;
-    r[6] = 0.0;
-    r[7] = 0.0;
+    r[0] = r[1] = r[5] = r[6] = r[7] = 0.0;
+    r[2] = r[3] = kEps;
+    r[4] = INFINITY;
 }
 
 /* dt per group from its maxima (the host tail of find_timestep) */
@@ -115,8 +115,9 @@ __global__ void k_group_dt(GroupDev G, const double *red, int32_t ng, GroupConst
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const double *r = red + 8 * g;
-    const double maxf = r[0], maxU = r[5], maxdrho = r[2], maxRhoi = r[3], minST = r[4];
-    if (K.ale) G.maxShift[g] = fmax(G.maxShift[g], r[6]);
+    const double maxf = fmax(kEps, sqrt(r[0])), maxU = fmax(kEps, sqrt(r[5])), maxdrho = r[2], maxRhoi = r[3];
+    const double minST = fmin(9999999.0, sqrt(r[4]));
+    if (K.ale) G.maxShift[g] = fmax(G.maxShift[g], sqrt(r[6]));
     G.maxRho_pc[g] = 100 * maxRhoi / K.rho_rest;
     const double fac[6] = {0.25 * sqrt(K.H / maxf),         2 * K.H / maxU, 0.125 * K.H_sq * K.rho_rest / K.mu,
                            0.067 * minST, 0.5 * sqrt(K.H / maxdrho), 1.5 * K.H / K.speed_sound};

@@ -267,8 +267,10 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&op)[NV
 
 template <int NV>
 __global__ void k_finish(const double *part, int64_t nblk, double init0, int opsel, double *out) {
-    /* single block: reduce nblk partial rows of NV values in a fixed order */
-    __shared__ double sh[NV][kRedThreads];
+    /* single block: reduce nblk partial rows of NV values in a fixed order (strided per thread,
+     * then across the warp, then across the warps) */
+    __shared__ double sh[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < NV; ++k) {
         const int op = (opsel >> (2 * k)) & 3;
         double t = op == 0 ? 0.0 : (op == 1 ? -INFINITY : INFINITY);
@@ -276,17 +278,16 @@ __global__ void k_finish(const double *part, int64_t nblk, double init0, int ops
             const double x = part[b * NV + k];
             t = op == 0 ? t + x : (op == 1 ? fmax(t, x) : fmin(t, x));
         }
-        sh[k][threadIdx.x] = t;
+        t = op == 0 ? warp_sum(t) : (op == 1 ? warp_max(t) : warp_min(t));
+        if (lane == 0) sh[k][wid] = t;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < NV; ++k) {
-            const int op = (opsel >> (2 * k)) & 3;
-            double t = sh[k][0];
-            for (int w = 1; w < (int)blockDim.x; ++w)
-                t = op == 0 ? t + sh[k][w] : (op == 1 ? fmax(t, sh[k][w]) : fmin(t, sh[k][w]));
-            out[k] = t;
-        }
+    if ((int)threadIdx.x < NV) {
+        const int k = threadIdx.x;
+        const int op = (opsel >> (2 * k)) & 3;
+        double t = sh[k][0];
+        for (int w = 1; w < nw; ++w) t = op == 0 ? t + sh[k][w] : (op == 1 ? fmax(t, sh[k][w]) : fmin(t, sh[k][w]));
+        out[k] = t;
     }
     (void)init0;
 }
@@ -317,11 +318,15 @@ __global__ void k_sq_disp(Params P, DevState W, const double *r0, const double *
     block_reduce<1>(v, op, part);
 }
 
-/* find_timestep reductions (src/Integration.cpp:384-402). */
+/* find_timestep reductions (src/Integration.cpp:384-402).  Norms and the surface-tension
+ * bound enter as the squares / the square-root arguments they are taken of: the square root is
+ * monotonic and correctly rounded, so the root of the extreme argument is the extreme root,
+ * bit for bit, for one square root per search instead of five per particle
+ * (timestep_maxima applies them). */
 template <int D>
 __global__ void k_timestep(Params P, DevState W, double *part) {
     const bool ale = has(P, FJSPH_VAR_ALE);
-    double v[7] = {kEps, kEps, kEps, kEps, 9999999.0, kEps, 0.0};
+    double v[7] = {0.0, 0.0, kEps, kEps, INFINITY, 0.0, 0.0};
     const int op[7] = {1, 1, 1, 1, 2, 1, 1};
     for (int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -329,18 +334,17 @@ __global__ void k_timestep(Params P, DevState W, double *part) {
         load3<D>(W.acc, i, a);
         load3<D>(W.Af, i, af);
         load3<D>(W.v, i, vv);
-        v[0] = fmax(v[0], vnorm<D, double>(a));
-        v[1] = fmax(v[1], vnorm<D, double>(af));
+        v[0] = fmax(v[0], dot<D, double>(a, a));
+        v[1] = fmax(v[1], dot<D, double>(af, af));
         v[2] = fmax(v[2], fabs(W.Rrho[i]));
         const double rho = W.rho[i];
         v[3] = fmax(v[3], fabs(rho - P.rho_rest));
-        const double st = sqrt(rho * P.dx * P.dx / (2.0 * kPi * P.sig * fabs(W.curve[i])));
-        v[4] = fmin(v[4], st);
-        v[5] = fmax(v[5], vnorm<D, double>(vv));
+        v[4] = fmin(v[4], rho * P.dx * P.dx / (2.0 * kPi * P.sig * fabs(W.curve[i])));
+        v[5] = fmax(v[5], dot<D, double>(vv, vv));
         if (ale) {
             double vp[D];
             load3<D>(W.vPert, i, vp);
-            v[6] = fmax(v[6], vnorm<D, double>(vp));
+            v[6] = fmax(v[6], dot<D, double>(vp, vp));
         }
     }
     block_reduce<7>(v, op, part);
@@ -407,6 +411,16 @@ void launch_sq_disp_sum(const Params &P, const DevState &W, double *const ref[3]
     FJSPH_DISPATCH2(P.D, k_sq_disp, g, kRedThreads, P, W, ref[0], ref[1], ref[2], S.part);
     k_finish<1><<<1, kRedThreads, 0, s>>>(S.part, g, 0.0, 0, out);
 }
+void timestep_maxima(const double *red, double *r) {
+    r[0] = std::max(kEps, std::sqrt(red[0]));
+    r[1] = std::max(kEps, std::sqrt(red[1]));
+    r[2] = red[2];
+    r[3] = red[3];
+    r[4] = std::min(9999999.0, std::sqrt(red[4]));
+    r[5] = std::max(kEps, std::sqrt(red[5]));
+    r[6] = std::sqrt(red[6]);
+}
+
 void launch_timestep_reduce(const Params &P, const DevState &W, RKScratch &S, double *out, cudaStream_t s) {
     const unsigned g = red_grid(P.n - P.nb, S.part_len, 7);
     FJSPH_DISPATCH2(P.D, k_timestep, g, kRedThreads, P, W, S.part);

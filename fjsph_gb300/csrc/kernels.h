@@ -193,6 +193,9 @@ void launch_density_guard(const Params &P, const DevState &W, cudaStream_t s);
 void launch_sum(const double *in, int64_t n, double *part, int64_t part_len, double *out, cudaStream_t s);
 /* find_timestep reductions over fluid slots: out[0..6] = maxf, maxAf, maxdrho, maxRhoi, minST, maxU,
  * maxShift (the last one only if ALE). */
+/* the seven find_timestep maxima from the reduced values (the norms as their squares, the
+ * surface-tension bound as its square-root argument) */
+void timestep_maxima(const double *red, double *r);
 void launch_timestep_reduce(const Params &P, const DevState &W, RKScratch &S, double *out, cudaStream_t s);
 
 /* ---- state.cu ------------------------------------------------------------------------------ */
