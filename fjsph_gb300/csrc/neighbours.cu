@@ -19,6 +19,7 @@
  * accurate to FP32 rounding of the separation (used by the split-precision form).
  */
 #include "kernels.h"
+#include "split.cuh"
 
 namespace fjsph {
 
@@ -224,10 +225,13 @@ __global__ void k_sorted_pos(Params P, const double *xs0, const double *xs1, con
     if (e >= P.n) return;
     const int32_t s = G.sorted[e];
     const double x0 = xs0[s], x1 = xs1[s], x2 = P.D == 3 ? xs2[s] : 0.0;
-    const float h0 = (float)x0, h1 = (float)x1, h2 = (float)x2;
+    float h0, h1, h2, l0, l1, l2;
+    split_f32(x0, h0, l0);
+    split_f32(x1, h1, l1);
+    split_f32(x2, h2, l2);
     G.sorted_hi[e] = make_float4(h0, h1, h2, __int_as_float(s));
     G.sorted_x[e] = h0;
-    G.sorted_lo[e] = make_float4((float)(x0 - (double)h0), (float)(x1 - (double)h1), (float)(x2 - (double)h2), 0.f);
+    G.sorted_lo[e] = make_float4(l0, l1, l2, 0.f);
 }
 
 /* ---- neighbour walk --------------------------------------------------------------------------- */
@@ -247,7 +251,7 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     const bool wrap = G.grid[3] != 0;
     float fi[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < D; ++k) fi[k] = (float)xi[k];
+    for (int k = 0; k < D; ++k) fi[k] = to_f32(xi[k]);
     const double band = G.bbox[6];
     const float sr_lo = (float)(P.sr * (1.0 - band)), sr_hi = (float)(P.sr * (1.0 + band));
     const uint64_t mask = (uint64_t)(G.table_size - 1);
@@ -406,8 +410,7 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill(Params P, double *xs0, do
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const double x = xs[k][i];
-            hi[k] = (float)x;
-            lo[k] = (float)(x - (double)hi[k]);
+            split_f32(x, hi[k], lo[k]);
         }
         /* one chunk per thread staged in shared memory (registers are the walk's) */
         __shared__ __align__(16) int2 stage[kThreads][kChunk];
@@ -468,8 +471,7 @@ __global__ void __launch_bounds__(kThreads) k_nbr_fill_fixed(Params P, double *x
 #pragma unroll
         for (int q = 0; q < D; ++q) {
             const double x = xs[q][i];
-            hi[q] = (float)x;
-            lo[q] = (float)(x - (double)hi[q]);
+            split_f32(x, hi[q], lo[q]);
         }
         int2 *buf = stage[threadIdx.x];
         auto flush = [&](int32_t chunk) {

@@ -6,33 +6,32 @@
 #pragma once
 
 #include "kernels.h"
+#include "split.cuh"
 
 namespace fjsph {
 
 /* A = (fl32(x), vol), B = (x - fl32(x), p / rho^2), C = (fl32(v), rho - rho0),
  * E = (v - fl32(v), flag bits), F = (vPert, p), bits.  vol and p / rho^2 are FP32 quotients of
  * the FP32-rounded operands (an FP64 divide per particle costs more than the pass's memory
- * traffic on this GPU); rounded to nearest in every translation unit. */
+ * traffic on this GPU); rounded to nearest in every translation unit.  The FP64 -> FP32
+ * roundings run in integer arithmetic (split.cuh), bit-identical to the conversions. */
 template <int D>
 __device__ __forceinline__ void pack_particle(const Params &P, const DevState &W, const Packed &K, int64_t i) {
     float xh[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0}, vp[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        const double x = W.x[k][i], v = W.v[k][i];
-        xh[k] = (float)x;
-        xl[k] = (float)(x - (double)xh[k]);
-        vh[k] = (float)v;
-        vl[k] = (float)(v - (double)vh[k]);
-        vp[k] = (float)W.vPert[k][i];
+        split_f32(W.x[k][i], xh[k], xl[k]);
+        split_f32(W.v[k][i], vh[k], vl[k]);
+        vp[k] = to_f32(W.vPert[k][i]);
     }
     const double rho = W.rho[i], p = W.p[i];
-    const float rf = (float)rho;
-    K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn((float)W.m[i], rf));
-    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn((float)p, rf * rf));
-    K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
+    const float rf = to_f32(rho), pf = to_f32(p);
+    K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn(to_f32(W.m[i]), rf));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn(pf, rf * rf));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], to_f32(rho - P.rho_rest));
     const int bits = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
     K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(bits));
-    K.F[i] = make_float4(vp[0], vp[1], vp[2], (float)p);
+    K.F[i] = make_float4(vp[0], vp[1], vp[2], pf);
     K.bits[i] = bits;
 }
 
@@ -45,17 +44,15 @@ __device__ __forceinline__ void pack_moved(const Params &P, const DevState &W, c
     float xh[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        xh[k] = (float)x[k];
-        xl[k] = (float)(x[k] - (double)xh[k]);
-        vh[k] = (float)v[k];
-        vl[k] = (float)(v[k] - (double)vh[k]);
+        split_f32(x[k], xh[k], xl[k]);
+        split_f32(v[k], vh[k], vl[k]);
     }
-    const float rf = (float)rho;
-    K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn((float)W.m[i], rf));
-    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn((float)p, rf * rf));
-    K.C[i] = make_float4(vh[0], vh[1], vh[2], (float)(rho - P.rho_rest));
+    const float rf = to_f32(rho), pf = to_f32(p);
+    K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn(to_f32(W.m[i]), rf));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn(pf, rf * rf));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], to_f32(rho - P.rho_rest));
     K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(K.bits[i]));
-    reinterpret_cast<float *>(K.F + i)[3] = (float)p;
+    reinterpret_cast<float *>(K.F + i)[3] = pf;
 }
 
 } // namespace fjsph
