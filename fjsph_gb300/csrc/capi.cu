@@ -239,13 +239,16 @@ int graph_release(fjsph_ctx *c);
 
 int alloc_table(fjsph_ctx *c, int64_t size) {
     TRY(graph_release(c)); /* captured launches hold the old arrays */
+    if (size > ((int64_t)1 << 30)) return FJSPH_E_CAPACITY; /* bucket ids use 30 bits */
     CellGrid &G = c->G;
     TRY(dfree(c, G.count));
     TRY(dfree(c, G.start));
     TRY(dfree(c, G.scan_tmp));
+    TRY(dfree(c, G.qbin));
     G.table_size = size;
     TRY(dalloc(c, &G.count, G.table_size + 1));
     TRY(dalloc(c, &G.start, G.table_size + 1));
+    TRY(dalloc(c, &G.qbin, G.table_size));
     G.scan_tmp_len = std::max<int64_t>(G.table_size / 2048 + 16, (int64_t)kBboxBlocks * 12 + 16);
     TRY(dalloc(c, &G.scan_tmp, G.scan_tmp_len));
     return FJSPH_OK;
@@ -1713,7 +1716,6 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     A(dalloc(c, &G.sorted, capacity));
     A(dalloc(c, &G.sorted_hi, capacity));
     A(dalloc(c, &G.sorted_lo, capacity));
-    A(dalloc(c, &G.sorted_x, capacity));
     A(dalloc(c, &G.bbox, 8));
     A(dalloc(c, &G.grid, 8));
     A(dalloc(c, &c->nbr_counts, capacity));

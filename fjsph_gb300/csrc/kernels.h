@@ -83,7 +83,7 @@ struct CellGrid {
     int32_t *sorted;         /* [cap]  slots ordered by bucket                */
     float4 *sorted_hi;       /* [cap]  (fl32(x), slot bits) in bucket order   */
     float4 *sorted_lo;       /* [cap]  fl32(x - hi) in bucket order           */
-    float *sorted_x;         /* [cap]  fl32(x) of the x axis in bucket order  */
+    uint32_t *qbin;          /* [table_size] quarter-cell index of the cells  */
     double *bbox;            /* [8]    lo[3], hi[3], band, spare (device)     */
     int64_t *grid;           /* [8]    nx, ny, nz, wrap flag, buckets in use  */
     int32_t *scan_tmp;       /* scan partials                                 */

@@ -146,6 +146,22 @@ __global__ void k_bbox_finish(Params P, const unsigned long long *part, int nblk
     grid[4] = ncells > (double)table ? table : (int64_t)ncells; /* buckets in use */
 }
 
+/* Quarter-cell index of the occupied cells (identity hash only): bits 10 (b - 1) .. 10 b - 1 of
+ * qbin[h] hold the offset from the cell's start of its first entry in x quarter b (b = 1, 2, 3),
+ * kQUnknown when the offset does not fit.  Entries are sorted by x, so quarter b's entries are
+ * [start + o_b, start + o_(b+1)); the walk reads the part of a row it needs from two of these
+ * words instead of searching the cells.  Written by the bucket rank pass from the quarters the
+ * hash pass computes. */
+constexpr uint32_t kQUnknown = 1023u;
+/* hash[i] holds the bucket in its low 30 bits (tables have at most 2^26 buckets) and the x
+ * quarter of the particle in its cell in the top two */
+constexpr int kQuarterShift = 30;
+constexpr uint32_t kBucketMask = (1u << kQuarterShift) - 1u;
+__device__ __forceinline__ int x_quarter(const Params &P, double x, double lo, int64_t cx) {
+    const double u = (cell_pos(P, x, lo, 0) - (double)cx) * 4.0;
+    return u < 1.0 ? 0 : (u < 2.0 ? 1 : (u < 3.0 ? 2 : 3));
+}
+
 /* ---- hashing ---------------------------------------------------------------------------------- */
 template <int D>
 __device__ __forceinline__ void cell_coords(const Params &P, const double *x, const double *lo, const int64_t *nc,
@@ -183,7 +199,7 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
     }
     cell_coords<D>(P, x, lo, nc, c);
     const uint32_t h = (uint32_t)(lin_index(c, nc) & (uint64_t)(G.table_size - 1));
-    G.hash[i] = h;
+    G.hash[i] = h | ((uint32_t)x_quarter(P, x[0], lo[0], c[0]) << kQuarterShift);
     /* lanes of a warp in the same bucket (consecutive slots usually are) add once */
     const unsigned peers = __match_any_sync(__activemask(), h);
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&G.count[h], (int32_t)__popc(peers));
@@ -194,10 +210,11 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
 __global__ void k_scatter(Params P, CellGrid G, const double *xs0, int32_t *cursor) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const uint32_t h = G.hash[i];
+    const uint32_t hq = G.hash[i], h = hq & kBucketMask;
     const int32_t pos = G.start[h] + atomicAdd(&cursor[h], 1);
     const unsigned long long k = x_key(xs0[i]);
-    reinterpret_cast<uint4 *>(G.sorted_lo)[pos] = make_uint4((unsigned)k, (unsigned)(k >> 32), (unsigned)i, 0u);
+    reinterpret_cast<uint4 *>(G.sorted_lo)[pos] =
+        make_uint4((unsigned)k, (unsigned)(k >> 32), (unsigned)i, hq >> kQuarterShift);
 }
 
 /* Each slot's rank in its bucket by (x, slot): buckets come out sorted by x, so a row of
@@ -206,31 +223,41 @@ __global__ void k_scatter(Params P, CellGrid G, const double *xs0, int32_t *curs
 __global__ void k_bucket_rank(Params P, CellGrid G, const double *xs0) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const uint32_t h = G.hash[i];
+    const uint32_t h = G.hash[i] & kBucketMask;
     const int32_t s0 = G.start[h], s1 = G.start[h + 1];
     const unsigned long long k = x_key(xs0[i]);
     const uint4 *ent = reinterpret_cast<const uint4 *>(G.sorted_lo);
     int32_t rank = 0;
+    uint32_t below[4] = {0u, 0u, 0u, 0u}; /* entries in x quarters below 1, 2, 3 */
     for (int32_t e = s0; e < s1; ++e) {
         const uint4 q = ent[e];
         const unsigned long long ke = (unsigned long long)q.x | ((unsigned long long)q.y << 32);
         rank += (ke < k || (ke == k && (int64_t)q.z < i)) ? 1 : 0;
+#pragma unroll
+        for (int b = 1; b <= 3; ++b) below[b] += q.w < (uint32_t)b ? 1u : 0u;
     }
     G.sorted[s0 + rank] = (int32_t)i;
+    if (rank == 0) { /* one writer per bucket: its quarter index (read by the walk when the hash
+                      * is the identity, so a bucket is one cell) */
+#pragma unroll
+        for (int b = 1; b <= 3; ++b)
+            if (below[b] > kQUnknown) below[b] = kQUnknown;
+        G.qbin[h] = below[1] | (below[2] << 10) | (below[3] << 20);
+    }
 }
 
 /* Coordinates in bucket order: hi = (fl32(x), slot bits), lo = fl32(x - hi). */
+template <int D>
 __global__ void k_sorted_pos(Params P, const double *xs0, const double *xs1, const double *xs2, CellGrid G) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= P.n) return;
     const int32_t s = G.sorted[e];
-    const double x0 = xs0[s], x1 = xs1[s], x2 = P.D == 3 ? xs2[s] : 0.0;
+    const double x0 = xs0[s], x1 = xs1[s], x2 = D == 3 ? xs2[s] : 0.0;
     float h0, h1, h2, l0, l1, l2;
     split_f32(x0, h0, l0);
     split_f32(x1, h1, l1);
     split_f32(x2, h2, l2);
     G.sorted_hi[e] = make_float4(h0, h1, h2, __int_as_float(s));
-    G.sorted_x[e] = h0;
     G.sorted_lo[e] = make_float4(l0, l1, l2, 0.f);
 }
 
@@ -309,19 +336,22 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     };
     /* Identity hash: the row's x range.  Buckets are sorted by x, so a row's members lie within
      * |x_j - x_i| <= r_row with r_row^2 = R^2 - (y gap to the row)^2 - (z gap)^2: the walk tests
-     * the part of the row inside that range and skips rows beyond R.  The bounds are widened by a margin that covers the FP32
-     * rounding of both coordinates and of the bound itself, so no member is ever left out. */
+     * the part of the row inside that range, to the quarter cell, and skips rows beyond R.  The
+     * bounds are widened by a margin that covers the FP32 rounding of both coordinates and of
+     * the bound itself, so no member is ever left out. */
     const float Rf = sqrtf((float)P.sr);
     const float r2f = (float)P.sr * (1.f + 1e-5f);
     const float mx = 5e-7f * (fabsf(fi[0]) + 2.f * Rf) + 1e-5f * Rf;
-    const float ey = (float)P.cell_edge[1], ez = (float)P.cell_edge[2];
-    /* position of x_i inside its cell in y and z, in cell edges */
+    const float ey = (float)P.cell_edge[1], ez = (float)P.cell_edge[2], inv_x = (float)P.cell_inv[0];
+    /* position of x_i inside its cell, in cell edges */
+    const float tx = (float)(cell_pos(P, xi[0], lo[0], 0) - (double)c[0]);
     const float ty = (float)(cell_pos(P, xi[1], lo[1], 1) - (double)c[1]);
     const float tz = D == 3 ? (float)(cell_pos(P, xi[2], lo[2], 2) - (double)c[2]) : 0.f;
     auto gap = [](int d, float t) { /* distance to the band of row offset d, in cell edges */
         const float g = d > 0 ? (float)d - t : (d < 0 ? t - 1.f - (float)d : 0.f);
         return fmaxf(0.f, g - 1e-4f);
     };
+    auto quarter = [](float u) { return u < 0.25f ? 0 : (u < 0.5f ? 1 : (u < 0.75f ? 2 : 3)); };
     const bool has_left = c[0] > 0, has_right = c[0] + 1 < nc[0];
     for (int dz = -zr; dz <= zr; ++dz) {
         const int64_t cz = c[2] + dz;
@@ -335,24 +365,40 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
                 const float rr2 = r2f - gy * gy - gz * gz;
                 if (rr2 <= 0.f) continue;
                 const float rr = sqrtf(rr2);
-                const float xlo = fi[0] - rr - mx, xhi = fi[0] + rr + mx;
                 int64_t cc[3] = {c[0], cy, cz};
                 const uint64_t hm = lin_index(cc, nc);
-                /* [e0, e1): the left cell's entries from the first x >= xlo, the middle cell,
-                 * the right cell's entries up to the last x <= xhi (counted with independent
-                 * loads of the compact x copy) */
-                int32_t e0 = G.start[hm], e1 = G.start[hm + 1];
-                if (has_left) {
-                    const int32_t l0 = G.start[hm - 1];
-                    int32_t below = 0;
-                    for (int32_t e = l0; e < e0; ++e) below += G.sorted_x[e] < xlo ? 1 : 0;
-                    e0 = l0 + below;
+                /* x range in cell edges relative to x_i's cell, widened by 1e-4 edges */
+                const float w = (rr + mx) * inv_x;
+                const float ulo = tx - w - 1e-4f, uhi = tx + w + 1e-4f;
+                /* first cell (cl) and quarter (bl) that can hold a member, last cell (ch) and
+                 * quarter (bh) */
+                int cl = 0, bl = 0, ch = 0, bh = 3;
+                if (ulo < 0.f) {
+                    if (has_left) {
+                        cl = -1;
+                        bl = ulo >= -1.f ? quarter(ulo + 1.f) : 0;
+                    }
+                } else {
+                    bl = quarter(ulo);
                 }
-                if (has_right) {
-                    const int32_t r1 = G.start[hm + 2];
-                    int32_t within = 0;
-                    for (int32_t e = e1; e < r1; ++e) within += G.sorted_x[e] <= xhi ? 1 : 0;
-                    e1 += within;
+                if (uhi >= 1.f) {
+                    if (has_right) {
+                        ch = 1;
+                        bh = uhi < 2.f ? quarter(uhi - 1.f) : 3;
+                    }
+                } else {
+                    bh = quarter(uhi);
+                }
+                const int32_t sa = G.start[hm + cl], sb = G.start[hm + cl + 1];
+                const int32_t sc = G.start[hm + ch], sd = G.start[hm + ch + 1];
+                int32_t e0 = sa, e1 = sd;
+                if (bl > 0 && sb > sa) { /* occupied cell: its quarter index is valid */
+                    const uint32_t o = (G.qbin[hm + cl] >> (10 * (bl - 1))) & 1023u;
+                    if (o != kQUnknown) e0 = sa + (int32_t)o;
+                }
+                if (bh < 3 && sd > sc) {
+                    const uint32_t o = (G.qbin[hm + ch] >> (10 * bh)) & 1023u;
+                    if (o != kQUnknown) e1 = sc + (int32_t)o;
                 }
                 range(e0, e1);
             } else {
@@ -671,7 +717,10 @@ __global__ void k_reorder_map(Params P, int32_t *sorted, const int32_t *flag, co
 
 void launch_sorted_pos(const Params &P, double *const xs[3], CellGrid &G, cudaStream_t s) {
     if (P.n == 0) return;
-    k_sorted_pos<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G);
+    if (P.D == 2)
+        k_sorted_pos<2><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G);
+    else
+        k_sorted_pos<3><<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, xs[0], xs[1], xs[2], G);
 }
 
 void launch_bbox(const Params &P, const DevState &W, CellGrid &G, cudaStream_t s) {
