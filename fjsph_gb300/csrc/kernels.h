@@ -13,6 +13,7 @@ namespace fjsph {
 struct Packed {
     float4 *A, *B, *C, *E, *F, *G, *N, *T;
     float4 *O; /* occlusion statistics of the surface-curvature pass (learned-closure inputs 0-3) */
+    float4 *L0, *L1, *L2; /* FP32 renormalisation matrix of the dSPH pre-step (row-major, 9 of 12) */
     int32_t *bits;
 };
 

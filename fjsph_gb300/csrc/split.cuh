@@ -45,6 +45,36 @@ FJSPH_HD float f32_from_bits(uint32_t b) {
 #endif
 }
 
+FJSPH_HD uint32_t f32_bits(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t b;
+    memcpy(&b, &f, sizeof b);
+    return b;
+#endif
+}
+
+FJSPH_HD double f64_from_bits(uint64_t u) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    memcpy(&x, &u, sizeof x);
+    return x;
+#endif
+}
+
+/* (double)f, exact: zeros and normal numbers by moving the fields, the rest by the conversion */
+FJSPH_HD double to_f64(float f) {
+    const uint32_t b = f32_bits(f);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    if ((b & 0x7FFFFFFFu) == 0u) return f64_from_bits(sign);
+    if (e == 0u || e == 0xFFu) return (double)f;
+    return f64_from_bits(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29));
+}
+
 /* Biased FP64 exponents handled by the integer path: |x| in [2^-63, 2^127).  Below, the low
  * part's scale 2^(e - 1075) would leave the FP32 normal range; above, the rounding may overflow
  * to infinity (left to the conversions). */

@@ -63,7 +63,7 @@ struct KSum {
         c = (t - s) - y;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ double value() const { return to_f64(s) - to_f64(c); }
 };
 
 /* cos x for x in [0, 2 pi) on the SFU: folded into [-pi/2, pi/2] by cos x = -cos(x - pi), where
@@ -141,6 +141,34 @@ __device__ __forceinline__ void fnormalized(const float *a, float *o) {
 __device__ __forceinline__ float f_kernel(const Pf &f, float r) { return kernel_w<float>(r, f.H, f.Wc, f.cubic); }
 __device__ __forceinline__ float f_gscale(const Pf &f, float r) { return gradk_scale<float>(r, f.H, f.Wc, f.cubic); }
 
+/* FP32 copy of the renormalisation matrix L (row-major D x D) in three float4 arrays */
+template <int D>
+__device__ __forceinline__ void store_lf(const Packed &K, int64_t i, const float *l) {
+    if (D == 2) {
+        K.L0[i] = make_float4(l[0], l[1], l[2], l[3]);
+    } else {
+        K.L0[i] = make_float4(l[0], l[1], l[2], l[3]);
+        K.L1[i] = make_float4(l[4], l[5], l[6], l[7]);
+        K.L2[i] = make_float4(l[8], 0.f, 0.f, 0.f);
+    }
+}
+template <int D>
+__device__ __forceinline__ void load_lf(const Packed &K, int64_t i, float *l) {
+    const float4 a = K.L0[i];
+    l[0] = a.x;
+    l[1] = a.y;
+    l[2] = a.z;
+    l[3] = a.w;
+    if (D == 3) {
+        const float4 b = K.L1[i];
+        l[4] = b.x;
+        l[5] = b.y;
+        l[6] = b.z;
+        l[7] = b.w;
+        l[8] = K.L2[i].x;
+    }
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* packing                                                                                       */
 /* ------------------------------------------------------------------------------------------ */
@@ -150,14 +178,14 @@ __global__ void k_pack_state(Params P, DevState W, Packed K, int64_t i0, int64_t
     if (i >= i1) return;
     pack_particle<D>(P, W, K, i);
     if (full) {
-        float g[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+        K.G[i] = make_float4(to_f32(W.gradRho[0][i]), to_f32(W.gradRho[1][i]), D == 3 ? to_f32(W.gradRho[2][i]) : 0.f,
+                             to_f32(W.lam[i]));
+        K.N[i] = make_float4(to_f32(W.norm[0][i]), to_f32(W.norm[1][i]), D == 3 ? to_f32(W.norm[2][i]) : 0.f,
+                             to_f32(W.lam_nb[i]));
+        float l[9];
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            g[k] = (float)W.gradRho[k][i];
-            n[k] = (float)W.norm[k][i];
-        }
-        K.G[i] = make_float4(g[0], g[1], g[2], (float)W.lam[i]);
-        K.N[i] = make_float4(n[0], n[1], n[2], (float)W.lam_nb[i]);
+        for (int k = 0; k < D * D; ++k) l[k] = to_f32(W.L[k][i]);
+        store_lf<D>(K, i, l);
     }
 }
 
@@ -257,11 +285,12 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
         }
         g[a] = sg;
         n[a] = sn;
-        W.gradRho[a][i] = sg;
-        W.norm[a][i] = sn;
+        W.gradRho[a][i] = to_f64(sg);
+        W.norm[a][i] = to_f64(sn);
     }
 #pragma unroll
-    for (int k = 0; k < D * D; ++k) W.L[k][i] = Linv[k];
+    for (int k = 0; k < D * D; ++k) W.L[k][i] = to_f64(Linv[k]);
+    store_lf<D>(K, i, Linv);
     float lam, lam_nb;
     if (W.b[i] == FJSPH_BOUND) {
         lam = 1.f;
@@ -270,11 +299,11 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
         lam = min_eig<D, float>(Lm);
         lam_nb = min_eig<D, float>(Lnb);
     }
-    W.lam[i] = lam;
-    W.lam_nb[i] = lam_nb;
-    W.colourG[i] = (lam > 0.7f) ? 2.0 : 2.0 * fmax(1.0, 1.0 / (2.0 * (double)colour));
-    W.kernsum[i] = kernsum;
-    W.colour[i] = colour;
+    W.lam[i] = to_f64(lam);
+    W.lam_nb[i] = to_f64(lam_nb);
+    W.colourG[i] = (lam > 0.7f) ? 2.0 : 2.0 * fmax(1.0, 1.0 / (2.0 * to_f64(colour)));
+    W.kernsum[i] = to_f64(kernsum);
+    W.colour[i] = to_f64(colour);
     npd_part[i] = npd;
     K.G[i] = make_float4(g[0], g[1], D == 3 ? g[2] : 0.f, lam);
     K.N[i] = make_float4(n[0], n[1], D == 3 ? n[2] : 0.f, lam_nb);
@@ -354,7 +383,7 @@ struct Dissip {
             for (int k = 0; k < D; ++k) av[k] *= c;
         }
 #pragma unroll
-        for (int k = 0; k < D; ++k) W.aVisc[k][i] = av[k];
+        for (int k = 0; k < D; ++k) W.aVisc[k][i] = to_f64(av[k]);
         if (!nodsph) W.deltaD[i] = P.dsph_cont * Rrhod.value();
     }
 };
@@ -380,7 +409,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
     if (D == 3) ni[2] = Ni.z;
     fnormalized<D>(ni, nh);
     const int b = W.b[i];
-    const float lam_nb = (float)W.lam_nb[i], lam = K.G[i].w;
+    const float lam_nb = Ni.w, lam = K.G[i].w;
     const SellList L = sell(N, i);
     int surf = W.surf[i];
     if (b < FJSPH_PIPE) {
@@ -458,12 +487,13 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         if (DIS) dis.add(f, K, j, Rji, rr, gs, volj, Gj);
     }
     if (DIS) dis.finish(P, W, i);
-    float n2[D];
+    float Lf[D * D], n2[D];
+    load_lf<D>(K, i, Lf);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         float s = 0.f;
 #pragma unroll
-        for (int c = 0; c < D; ++c) s += (float)W.L[a * D + c][i] * nrm[c];
+        for (int c = 0; c < D; ++c) s += Lf[a * D + c] * nrm[c];
         n2[a] = s;
     }
     float out[D];
@@ -491,14 +521,13 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     if (D == 3) ni[2] = Ti.z;
     const bool occl = (b == FJSPH_FREE) && gissler;
     const bool vd_on = occl && W.cellID[i] != -1;
-    Vdiff[0] = vd_on ? (float)(vinf_of(P, i, 0) - W.v[0][i]) : 0.f;
-    Vdiff[1] = vd_on ? (float)(vinf_of(P, i, 1) - W.v[1][i]) : 0.f;
-    if (D == 3) Vdiff[2] = vd_on ? (float)(vinf_of(P, i, 2) - W.v[2][i]) : 0.f;
+    Vdiff[0] = vd_on ? to_f32(vinf_of(P, i, 0) - W.v[0][i]) : 0.f;
+    Vdiff[1] = vd_on ? to_f32(vinf_of(P, i, 1) - W.v[1][i]) : 0.f;
+    if (D == 3) Vdiff[2] = vd_on ? to_f32(vinf_of(P, i, 2) - W.v[2][i]) : 0.f;
     (void)Ci;
     (void)Ei;
     float Li[D * D];
-#pragma unroll
-    for (int k = 0; k < D * D; ++k) Li[k] = (float)W.L[k][i];
+    load_lf<D>(K, i, Li);
     const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
     float curve = 0.f, woccl_ = 0.f, o0 = 0.f, o1 = 0.f, o2 = 0.f;
     const SellList L = sell(N, i);
@@ -538,14 +567,16 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
             }
         }
     }
-    W.woccl[i] = ((float)W.lam_nb[i] < (float)P.lam_cutoff) ? fmaxf(0.f, fminf(woccl_, 1.f)) : 1.0f;
+    const float lam_nb_i = K.N[i].w;
+    W.woccl[i] = to_f64((lam_nb_i < (float)P.lam_cutoff) ? fmaxf(0.f, fminf(woccl_, 1.f)) : 1.0f);
     K.O[i] = make_float4(o0, o1, o2, woccl_);
 #pragma unroll
-    for (int k = 0; k < D; ++k) W.norm[k][i] = ni[k];
-    W.curve[i] = curve;
-    W.norm_curve[i] = P.dx * (double)curve;
+    for (int k = 0; k < D; ++k) W.norm[k][i] = to_f64(ni[k]);
+    const double curve_d = to_f64(curve);
+    W.curve[i] = curve_d;
+    W.norm_curve[i] = P.dx * curve_d;
     W.pDist[i] = W.lam[i];
-    K.N[i] = make_float4(ni[0], ni[1], D == 3 ? ni[2] : 0.f, (float)W.lam_nb[i]);
+    K.N[i] = make_float4(ni[0], ni[1], D == 3 ? ni[2] : 0.f, lam_nb_i);
 }
 
 __global__ void k_m_surface_zone(Params P, DevState W, DevNbr N, Packed K) {
@@ -921,7 +952,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         accd[k] = aero[k] + acc[k].value();
-        if (linear) accd[k] /= (double)rho_i;
+        if (linear) accd[k] /= to_f64(rho_i);
     }
     if (csf) {
         const double c = 1.0 / W.rho[i] * P.sig * W.curve[i] * W.colourG[i];
@@ -931,13 +962,13 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
     const float inv_m = 1.f / m_i; /* the surface-tension sum is FP32 already */
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        const double av = nofrozen ? (double)art[k] : W.aVisc[k][i];
+        const double av = nofrozen ? to_f64(art[k]) : W.aVisc[k][i];
         double t = accd[k];
-        if (ale) t += acc_ale[k];
-        W.acc[k][i] = t + av + visc[k] + (double)(st[k] * inv_m) + P.grav[k];
+        if (ale) t += to_f64(acc_ale[k]);
+        W.acc[k][i] = t + av + to_f64(visc[k]) + to_f64(st[k] * inv_m) + P.grav[k];
         if (aero_on) W.Af[k][i] = aero[k];
     }
-    double R = Rrho.value() * (double)rho_i;
+    double R = Rrho.value() * to_f64(rho_i);
     if (ale) R += Rrhoc.value();
     if (!nodsph) R += nofrozen ? P.dsph_cont * Rrho_d.value() : W.deltaD[i];
     W.Rrho[i] = R;

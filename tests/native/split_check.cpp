@@ -1,6 +1,7 @@
 // Checks the integer FP64 -> FP32 rounding of fjsph_gb300/csrc/split.cuh against the compiler's
 // conversions: hi = (float)x and lo = (float)(x - (double)hi), bit for bit, over random doubles of
-// every exponent, both signs, rounding ties and the carry into the exponent.  Exit status 0 on
+// every exponent, both signs, rounding ties and the carry into the exponent; and the FP32 -> FP64
+// widening over every FP32 bit pattern.  Exit status 0 on
 // agreement; prints the first mismatch otherwise.
 #include <cstdio>
 #include <cstdint>
@@ -35,9 +36,29 @@ static int check(double x) {
     return 0;
 }
 
+static int check_widen(uint32_t b) {
+    float f;
+    std::memcpy(&f, &b, 4);
+    const double w = fjsph::to_f64(f), w0 = (double)f;
+    uint64_t u, u0;
+    std::memcpy(&u, &w, 8);
+    std::memcpy(&u0, &w0, 8);
+    if (u != u0) {
+        if (w0 != w0 && w != w) return 0; /* NaN payloads */
+        std::printf("widen mismatch bits=%08x %016llx/%016llx\n", b, (unsigned long long)u, (unsigned long long)u0);
+        return 1;
+    }
+    return 0;
+}
+
 int main() {
     std::mt19937_64 rng(12345);
     long bad = 0, n = 0;
+    /* every FP32 bit pattern, widened */
+    for (uint64_t b = 0; b <= 0xFFFFFFFFull; b += 1) {
+        bad += check_widen((uint32_t)b);
+        if (bad > 5) return 1;
+    }
     for (int e = 0; e < 2048; ++e) {
         for (int k = 0; k < 4000; ++k) {
             uint64_t m = rng() & 0xFFFFFFFFFFFFFull;
