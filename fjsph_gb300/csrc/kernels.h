@@ -14,6 +14,10 @@ struct Packed {
     float4 *A, *B, *C, *E, *F, *G, *N, *T;
     float4 *O; /* occlusion statistics of the surface-curvature pass (learned-closure inputs 0-3) */
     float4 *L0, *L1, *L2; /* FP32 renormalisation matrix of the dSPH pre-step (row-major, 9 of 12) */
+    /* The residual's third neighbour input: the low parts of position and velocity as bf16
+     * pairs (x.x|x.y, x.z|v.x, v.y|v.z) and p / rho^2 whose two lowest mantissa bits carry
+     * kLoBound (type FJSPH_BOUND) and kLoFluid (type above FJSPH_PISTON). */
+    float4 *Lo;
     int32_t *bits;
 };
 

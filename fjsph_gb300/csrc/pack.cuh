@@ -5,10 +5,27 @@
  */
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "kernels.h"
 #include "split.cuh"
 
 namespace fjsph {
+
+/* Two bf16 (round to nearest even) in one 32-bit word, the first in the low half. */
+__device__ __forceinline__ float pack_bf16x2(float a, float b) {
+    const uint32_t lo = __bfloat16_as_ushort(__float2bfloat16_rn(a));
+    const uint32_t hi = __bfloat16_as_ushort(__float2bfloat16_rn(b));
+    return __uint_as_float(lo | (hi << 16));
+}
+constexpr uint32_t kLoBound = 1u, kLoFluid = 2u;
+/* the residual's compact inputs (Packed::Lo) */
+__device__ __forceinline__ float4 pack_lo(const float *xl, const float *vl, float pr, int bits) {
+    const int b = bits & 7;
+    const uint32_t flags = (b == FJSPH_BOUND ? kLoBound : 0u) | (b > FJSPH_PISTON ? kLoFluid : 0u);
+    return make_float4(pack_bf16x2(xl[0], xl[1]), pack_bf16x2(xl[2], vl[0]), pack_bf16x2(vl[1], vl[2]),
+                       __uint_as_float((__float_as_uint(pr) & ~3u) | flags));
+}
 
 /* A = (fl32(x), vol), B = (x - fl32(x), p / rho^2), C = (fl32(v), rho - rho0),
  * E = (v - fl32(v), flag bits), F = (vPert, p), bits.  vol and p / rho^2 are FP32 quotients of
@@ -26,12 +43,14 @@ __device__ __forceinline__ void pack_particle(const Params &P, const DevState &W
     }
     const double rho = W.rho[i], p = W.p[i];
     const float rf = to_f32(rho), pf = to_f32(p);
+    const float pr = __fdiv_rn(pf, rf * rf);
     K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn(to_f32(W.m[i]), rf));
-    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn(pf, rf * rf));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], pr);
     K.C[i] = make_float4(vh[0], vh[1], vh[2], to_f32(rho - P.rho_rest));
     const int bits = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
     K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(bits));
     K.F[i] = make_float4(vp[0], vp[1], vp[2], pf);
+    K.Lo[i] = pack_lo(xl, vl, pr, bits);
     K.bits[i] = bits;
 }
 
@@ -48,11 +67,14 @@ __device__ __forceinline__ void pack_moved(const Params &P, const DevState &W, c
         split_f32(v[k], vh[k], vl[k]);
     }
     const float rf = to_f32(rho), pf = to_f32(p);
+    const float pr = __fdiv_rn(pf, rf * rf);
+    const int bits = K.bits[i];
     K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn(to_f32(W.m[i]), rf));
-    K.B[i] = make_float4(xl[0], xl[1], xl[2], __fdiv_rn(pf, rf * rf));
+    K.B[i] = make_float4(xl[0], xl[1], xl[2], pr);
     K.C[i] = make_float4(vh[0], vh[1], vh[2], to_f32(rho - P.rho_rest));
-    K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(K.bits[i]));
+    K.E[i] = make_float4(vl[0], vl[1], vl[2], __int_as_float(bits));
     reinterpret_cast<float *>(K.F + i)[3] = pf;
+    K.Lo[i] = pack_lo(xl, vl, pr, bits);
 }
 
 } // namespace fjsph

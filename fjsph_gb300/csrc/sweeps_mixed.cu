@@ -102,9 +102,8 @@ constexpr int kGatherAhead = FJSPH_GATHER_AHEAD;
 
 __device__ __forceinline__ void prefetch_pair_inputs(const Packed &K, int32_t j, bool f, bool g) {
     prefetch_l1(K.A + j);
-    prefetch_l1(K.B + j);
     prefetch_l1(K.C + j);
-    prefetch_l1(K.E + j);
+    prefetch_l1(K.Lo + j);
     if (f) prefetch_l1(K.F + j);
     if (g) prefetch_l1(K.G + j);
 }
@@ -116,6 +115,25 @@ __device__ __forceinline__ void sep(const float4 &Ai, const float4 &Bi, const fl
     R[1] = (Aj.y - Ai.y) + (Bj.y - Bi.y);
     if (D == 3) R[2] = (Aj.z - Ai.z) + (Bj.z - Bi.z);
 }
+
+/* the residual's compact inputs (Packed::Lo): low parts of x and v, p / rho^2 and type flags */
+template <int D>
+struct LoParts {
+    float xl[3], vl[3], pr;
+    uint32_t flags;
+    __device__ __forceinline__ explicit LoParts(const float4 q) {
+        const uint32_t a = __float_as_uint(q.x), b = __float_as_uint(q.y), c = __float_as_uint(q.z);
+        xl[0] = __uint_as_float(a << 16);
+        xl[1] = __uint_as_float(a & 0xFFFF0000u);
+        xl[2] = __uint_as_float(b << 16);
+        vl[0] = __uint_as_float(b & 0xFFFF0000u);
+        vl[1] = __uint_as_float(c << 16);
+        vl[2] = __uint_as_float(c & 0xFFFF0000u);
+        const uint32_t w = __float_as_uint(q.w);
+        pr = __uint_as_float(w & ~3u);
+        flags = w & 3u;
+    }
+};
 
 template <int D>
 __device__ __forceinline__ float fdot(const float *a, const float *b) {
@@ -812,10 +830,11 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
     }
     const float pi3o4_H = P.fc.pi3o4_H;
     const float fac_bound = P.fc.fac_bound;
-    const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Fi = K.F[i];
+    const float4 Ai = K.A[i], Ci = K.C[i], Fi = K.F[i];
+    const LoParts<D> Li(K.Lo[i]);
     const float rho_i = f.rho0 + Ci.w;
     const float m_i = Ai.w * rho_i;
-    const float pr_i0 = Bi.w;
+    const float pr_i0 = Li.pr;
     const int bits_i = K.bits[i];
     const int b_i = bits_b(bits_i), sz_i = bits_zone(bits_i);
     const float pr_i = (tic && sz_i != 1) ? fabsf(pr_i0) : pr_i0;
@@ -831,9 +850,9 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
         if (D == 3) gRi[2] = Gi.z;
     }
     float vi[D];
-    vi[0] = Ci.x + Ei.x;
-    vi[1] = Ci.y + Ei.y;
-    if (D == 3) vi[2] = Ci.z + Ei.z;
+    vi[0] = Ci.x + Li.vl[0];
+    vi[1] = Ci.y + Li.vl[1];
+    if (D == 3) vi[2] = Ci.z + Li.vl[2];
     const SellList L = sell(N, i);
     KSum acc[D];
     float acc_ale[D], visc[D], st[D], art[D];
@@ -866,7 +885,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
         const int2 pe = q[0];
         if (((e + ahead) % kChunk) == 0 && e + ahead < L.n) prefetch_l1(L.at(e + ahead)); /* next chunk */
         const int32_t j = pe.x;
-        const float4 Aj = K.A[j], Bj = K.B[j], Cj = K.C[j], Ej = K.E[j];
+        const float4 Aj = K.A[j], Cj = K.C[j], Qj = K.Lo[j];
 #pragma unroll
         for (int a = 0; a + 1 < kGatherAhead; ++a) q[a] = q[a + 1];
         if (e + kGatherAhead < L.n) {
@@ -874,16 +893,22 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
             prefetch_pair_inputs(K, q[kGatherAhead - 1].x, linear || ale, nofrozen);
         }
         if (j == i) continue;
+        const LoParts<D> Lj(Qj);
+        /* separations as in sep(): high parts, then the (bf16) low parts */
         float Rji[D], Vji[D];
-        sep<D>(Ai, Bi, Aj, Bj, Rji);
-        sep<D>(Ci, Ei, Cj, Ej, Vji);
+        Rji[0] = (Aj.x - Ai.x) + (Lj.xl[0] - Li.xl[0]);
+        Rji[1] = (Aj.y - Ai.y) + (Lj.xl[1] - Li.xl[1]);
+        if (D == 3) Rji[2] = (Aj.z - Ai.z) + (Lj.xl[2] - Li.xl[2]);
+        Vji[0] = (Cj.x - Ci.x) + (Lj.vl[0] - Li.vl[0]);
+        Vji[1] = (Cj.y - Ci.y) + (Lj.vl[1] - Li.vl[1]);
+        if (D == 3) Vji[2] = (Cj.z - Ci.z) + (Lj.vl[2] - Li.vl[2]);
         const float rr = __int_as_float(pe.y);
         const float r = sqrtf(rr);
         const float idist2 = 1.f / (rr + 0.001f * f.H_sq);
         const float volj = Aj.w;
         const float rho_j = f.rho0 + Cj.w;
         const float m_j = volj * rho_j;
-        const int b_j = bits_b(__float_as_int(Ej.w));
+        const bool bound_j = (Lj.flags & kLoBound) != 0u, fluid_j = (Lj.flags & kLoFluid) != 0u;
         const float gs = f_gscale(f, r);
         float g[D];
 #pragma unroll
@@ -892,7 +917,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
         if (linear)
             pc = (p_i + K.F[j].w) * volj;
         else
-            pc = m_j * (pr_i + Bj.w);
+            pc = m_j * (pr_i + Lj.pr);
 #pragma unroll
         for (int k = 0; k < D; ++k) acc[k].add(-pc * g[k]);
         const float rg = fdot<D>(Rji, g);
@@ -900,7 +925,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
 #pragma unroll
         for (int k = 0; k < D; ++k) visc[k] += vc * Vji[k];
         if (st_on) {
-            const float fac = (b_i == FJSPH_BOUND || b_j == FJSPH_BOUND) ? fac_bound : 1.f;
+            const float fac = (b_i == FJSPH_BOUND || bound_j) ? fac_bound : 1.f;
             const float c = -npdm2 * fac * cos_0_2pi(pi3o4_H * r) / r;
 #pragma unroll
             for (int k = 0; k < D; ++k) st[k] += c * Rji[k];
@@ -911,9 +936,9 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
             vPj[0] = Fj.x;
             vPj[1] = Fj.y;
             if (D == 3) vPj[2] = Fj.z;
-            vj[0] = Cj.x + Ej.x;
-            vj[1] = Cj.y + Ej.y;
-            if (D == 3) vj[2] = Cj.z + Ej.z;
+            vj[0] = Cj.x + Lj.vl[0];
+            vj[1] = Cj.y + Lj.vl[1];
+            if (D == 3) vj[2] = Cj.z + Lj.vl[2];
             const float gj = fdot<D>(vPj, g), gi = fdot<D>(vPi, g);
             float q = 0.f, w1 = 0.f, w2 = 0.f;
 #pragma unroll
@@ -930,7 +955,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
             Rrho.add(-volj * fdot<D>(Vji, g));
         }
         if (nofrozen) {
-            if (b_j > FJSPH_PISTON) {
+            if (fluid_j) {
                 if (!nodsph) {
                     const float4 Gj = K.G[j];
                     float gsum[D];
