@@ -408,7 +408,7 @@ const double *npd_ptr(const fjsph_ctx *c) { return grouped(c) ? c->gs.npd : &c->
 int alloc_packed(fjsph_ctx *c) {
     if (c->packed_alloc) return FJSPH_OK;
     Packed &K = c->K;
-    float4 **arrs[] = {&K.A, &K.B, &K.C, &K.E, &K.F, &K.G, &K.N, &K.T, &K.O, &K.L0, &K.L1, &K.L2, &K.Lo};
+    float4 **arrs[] = {&K.A, &K.C, &K.F, &K.G, &K.N, &K.T, &K.O, &K.L0, &K.L1, &K.L2, &K.Lo};
     for (float4 **a : arrs) TRY(dalloc(c, a, c->cap));
     TRY(dalloc(c, &K.bits, c->cap));
     TRY(dalloc(c, &c->nbr_pair, c->nbr_cap));

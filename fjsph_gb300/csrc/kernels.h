@@ -11,12 +11,13 @@ namespace fjsph {
 
 /* Packed FP32 split-precision inputs of the mixed form (see sweeps_mixed.cu). */
 struct Packed {
-    float4 *A, *B, *C, *E, *F, *G, *N, *T;
+    float4 *A, *C, *F, *G, *N, *T;
     float4 *O; /* occlusion statistics of the surface-curvature pass (learned-closure inputs 0-3) */
     float4 *L0, *L1, *L2; /* FP32 renormalisation matrix of the dSPH pre-step (row-major, 9 of 12) */
-    /* The residual's third neighbour input: the low parts of position and velocity as bf16
-     * pairs (x.x|x.y, x.z|v.x, v.y|v.z) and p / rho^2 whose two lowest mantissa bits carry
-     * kLoBound (type FJSPH_BOUND) and kLoFluid (type above FJSPH_PISTON). */
+    /* The low parts of position and velocity (x - fl32(x), v - fl32(v)) as bf16 pairs
+     * (x.x|x.y, x.z|v.x, v.y|v.z) and p / rho^2 whose two lowest mantissa bits carry kLoBound
+     * (type FJSPH_BOUND) and kLoFluid (type above FJSPH_PISTON): with A and C, the neighbour
+     * inputs of the pair sweeps. */
     float4 *Lo;
     int32_t *bits;
 };

@@ -109,18 +109,12 @@ __device__ __forceinline__ void prefetch_pair_inputs(const Packed &K, int32_t j,
 }
 
 /* separation x_j - x_i from the hi/lo split */
-template <int D>
-__device__ __forceinline__ void sep(const float4 &Ai, const float4 &Bi, const float4 &Aj, const float4 &Bj, float *R) {
-    R[0] = (Aj.x - Ai.x) + (Bj.x - Bi.x);
-    R[1] = (Aj.y - Ai.y) + (Bj.y - Bi.y);
-    if (D == 3) R[2] = (Aj.z - Ai.z) + (Bj.z - Bi.z);
-}
 
-/* the residual's compact inputs (Packed::Lo): low parts of x and v, p / rho^2 and type flags */
-template <int D>
+/* the compact neighbour inputs (Packed::Lo): low parts of x and v, p / rho^2 and type flags */
 struct LoParts {
     float xl[3], vl[3], pr;
     uint32_t flags;
+    __device__ __forceinline__ LoParts() {}
     __device__ __forceinline__ explicit LoParts(const float4 q) {
         const uint32_t a = __float_as_uint(q.x), b = __float_as_uint(q.y), c = __float_as_uint(q.z);
         xl[0] = __uint_as_float(a << 16);
@@ -134,6 +128,20 @@ struct LoParts {
         flags = w & 3u;
     }
 };
+
+/* separations x_j - x_i and v_j - v_i: high parts first, then the low parts */
+template <int D>
+__device__ __forceinline__ void sepx(const float4 &Ai, const LoParts &Li, const float4 &Aj, const LoParts &Lj, float *R) {
+    R[0] = (Aj.x - Ai.x) + (Lj.xl[0] - Li.xl[0]);
+    R[1] = (Aj.y - Ai.y) + (Lj.xl[1] - Li.xl[1]);
+    if (D == 3) R[2] = (Aj.z - Ai.z) + (Lj.xl[2] - Li.xl[2]);
+}
+template <int D>
+__device__ __forceinline__ void sepv(const float4 &Ci, const LoParts &Li, const float4 &Cj, const LoParts &Lj, float *V) {
+    V[0] = (Cj.x - Ci.x) + (Lj.vl[0] - Li.vl[0]);
+    V[1] = (Cj.y - Ci.y) + (Lj.vl[1] - Li.vl[1]);
+    if (D == 3) V[2] = (Cj.z - Ci.z) + (Lj.vl[2] - Li.vl[2]);
+}
 
 template <int D>
 __device__ __forceinline__ float fdot(const float *a, const float *b) {
@@ -234,7 +242,8 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const Pf f = make_pf(P);
-    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float4 Ai = K.A[i];
+    const LoParts Li(K.Lo[i]);
     const float drho_i = K.C[i].w;
     float Lm[D * D], Lnb[D * D], gR[D], nr[D];
 #pragma unroll
@@ -256,14 +265,15 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
             kernsum += f.Wc;
             continue;
         }
-        const float4 Aj = K.A[j], Bj = K.B[j];
+        const float4 Aj = K.A[j];
+        const LoParts Lj(K.Lo[j]);
         float Rji[D];
-        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        sepx<D>(Ai, Li, Aj, Lj, Rji);
         const float r = sqrtf(__int_as_float(pe.y));
         const float volj = Aj.w;
         const float kern = f_kernel(f, r);
         const float gs = f_gscale(f, r);
-        const bool fl = bits_b(K.bits[j]) > FJSPH_PISTON;
+        const bool fl = (Lj.flags & kLoFluid) != 0u;
         const float drho = volj * (K.C[j].w - drho_i);
         /* Lm -= volj Rji (x) Grad with Grad = -Rji gs */
         const float w = volj * gs;
@@ -346,7 +356,8 @@ __device__ __forceinline__ float f_art_visc(const Pf &f, float vdotr, float idis
 template <int D>
 struct Dissip {
     bool linear, nodsph;
-    float4 Ci, Ei;
+    float4 Ci;
+    LoParts Li;
     float rho_i;
     float gRi[D], av[D];
     KSum Rrhod;
@@ -354,7 +365,7 @@ struct Dissip {
         linear = has(P, FJSPH_VAR_LINEAR);
         nodsph = has(P, FJSPH_VAR_NODSPH);
         Ci = K.C[i];
-        Ei = K.E[i];
+        Li = LoParts(K.Lo[i]);
         const float4 Gi = K.G[i];
         rho_i = f.rho0 + Ci.w;
         gRi[0] = Gi.x;
@@ -364,17 +375,17 @@ struct Dissip {
         for (int k = 0; k < D; ++k) av[k] = 0.f;
     }
     /* pair (i, j): Rji = x_j - x_i, rr = |Rji|^2, gs = f_gscale(r), Gj = K.G[j] */
-    __device__ __forceinline__ void add(const Pf &f, const Packed &K, int32_t j, const float *Rji, float rr, float gs,
-                                        float volj, const float4 Gj) {
-        const float4 Cj = K.C[j], Ej = K.E[j];
+    __device__ __forceinline__ void add(const Pf &f, const Packed &K, int32_t j, const LoParts &Lj, const float *Rji,
+                                        float rr, float gs, float volj, const float4 Gj) {
+        const float4 Cj = K.C[j];
         float Vji[D];
-        sep<D>(Ci, Ei, Cj, Ej, Vji);
+        sepv<D>(Ci, Li, Cj, Lj, Vji);
         const float idist2 = 1.f / (rr + 0.0001f * f.H_sq);
         const float rho_j = f.rho0 + Cj.w;
         float g[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
-        const bool fl = bits_b(K.bits[j]) > FJSPH_PISTON;
+        const bool fl = (Lj.flags & kLoFluid) != 0u;
         if (fl) {
             const float vdotr = fdot<D>(Vji, Rji);
             const float c = linear ? volj * idist2 * vdotr : (volj * rho_j) * f_art_visc(f, vdotr, idist2, rho_i, rho_j);
@@ -419,7 +430,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
     Dissip<D> dis;
     if (DIS) dis.init(P, f, K, i);
     const float h = (float)(1.33 * P.particle_step);
-    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float4 Ai = K.A[i];
+    const LoParts Li(K.Lo[i]);
     const float4 Ni = K.N[i]; /* dSPH normal, lam_nb */
     float ni[D], nh[D];
     ni[0] = Ni.x;
@@ -451,7 +463,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         const int32_t j = pe.x;
             if (j == i) continue;
             float Rji[D], xT[D];
-            sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
+            sepx<D>(Ai, Li, K.A[j], LoParts(K.Lo[j]), Rji);
 #pragma unroll
             for (int k = 0; k < D; ++k) xT[k] = Rji[k] - h * nh[k];
             const float r = sqrtf(__int_as_float(pe.y));
@@ -491,7 +503,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         if (j == i) continue;
         float Rji[D];
         const float4 Aj = K.A[j];
-        sep<D>(Ai, Bi, Aj, K.B[j], Rji);
+        const LoParts Lj(K.Lo[j]);
+        sepx<D>(Ai, Li, Aj, Lj, Rji);
         const float rr = __int_as_float(pe.y);
         const float r = sqrtf(rr);
         const float volj = Aj.w;
@@ -502,7 +515,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         /* GradK(Rij) with Rij = x_i - x_j = -Rji */
 #pragma unroll
         for (int k = 0; k < D; ++k) nrm[k] -= w * (Rji[k] * gs);
-        if (DIS) dis.add(f, K, j, Rji, rr, gs, volj, Gj);
+        if (DIS) dis.add(f, K, j, Lj, Rji, rr, gs, volj, Gj);
     }
     if (DIS) dis.finish(P, W, i);
     float Lf[D * D], n2[D];
@@ -531,8 +544,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     const Pf f = make_pf(P);
     const bool gissler = P.acase == FJSPH_GISSLER;
     const int b = W.b[i];
-    const float4 Ai = K.A[i], Bi = K.B[i], Ti = K.T[i];
-    const float4 Ci = K.C[i], Ei = K.E[i];
+    const float4 Ai = K.A[i], Ti = K.T[i];
+    const LoParts Qi(K.Lo[i]);
     float ni[D], Vdiff[D];
     ni[0] = Ti.x;
     ni[1] = Ti.y;
@@ -542,8 +555,6 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     Vdiff[0] = vd_on ? to_f32(vinf_of(P, i, 0) - W.v[0][i]) : 0.f;
     Vdiff[1] = vd_on ? to_f32(vinf_of(P, i, 1) - W.v[1][i]) : 0.f;
     if (D == 3) Vdiff[2] = vd_on ? to_f32(vinf_of(P, i, 2) - W.v[2][i]) : 0.f;
-    (void)Ci;
-    (void)Ei;
     float Li[D * D];
     load_lf<D>(K, i, Li);
     const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
@@ -554,7 +565,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
         const int32_t j = pe.x;
         if (j == i) continue;
         float Rij[D]; /* = x_j - x_i, the reference's naming in this loop */
-        sep<D>(Ai, Bi, K.A[j], K.B[j], Rij);
+        sepx<D>(Ai, Qi, K.A[j], LoParts(K.Lo[j]), Rij);
         const float r = sqrtf(__int_as_float(pe.y));
         const float4 Tj = K.T[j];
         float nj[D];
@@ -617,7 +628,8 @@ __global__ void __launch_bounds__(kThreads) k_m_dissipation(Params P, DevState W
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const Pf f = make_pf(P);
-    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float4 Ai = K.A[i];
+    const LoParts Li(K.Lo[i]);
     Dissip<D> dis;
     dis.init(P, f, K, i);
     const SellList L = sell(N, i);
@@ -625,11 +637,12 @@ __global__ void __launch_bounds__(kThreads) k_m_dissipation(Params P, DevState W
         const int2 pe = L[e];
         const int32_t j = pe.x;
         if (j == i) continue;
-        const float4 Aj = K.A[j], Bj = K.B[j];
+        const float4 Aj = K.A[j];
+        const LoParts Lj(K.Lo[j]);
         float Rji[D];
-        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        sepx<D>(Ai, Li, Aj, Lj, Rji);
         const float rr = __int_as_float(pe.y);
-        dis.add(f, K, j, Rji, rr, f_gscale(f, sqrtf(rr)), Aj.w, K.G[j]);
+        dis.add(f, K, j, Lj, Rji, rr, f_gscale(f, sqrtf(rr)), Aj.w, K.G[j]);
     }
     dis.finish(P, W, i);
 }
@@ -649,15 +662,16 @@ __global__ void __launch_bounds__(kThreads) k_m_particle_shift(Params P, DevStat
         return;
     }
     const Pf f = make_pf(P);
-    const float4 Ai = K.A[i], Bi = K.B[i], Ci = K.C[i], Ei = K.E[i], Ni = K.N[i];
+    const float4 Ai = K.A[i], Ci = K.C[i], Ni = K.N[i];
+    const LoParts Li(K.Lo[i]);
     float ni[D], nh[D], vi[D];
     ni[0] = Ni.x;
     ni[1] = Ni.y;
     if (D == 3) ni[2] = Ni.z;
     fnormalized<D>(ni, nh);
-    vi[0] = Ci.x + Ei.x;
-    vi[1] = Ci.y + Ei.y;
-    if (D == 3) vi[2] = Ci.z + Ei.z;
+    vi[0] = Ci.x + Li.vl[0];
+    vi[1] = Ci.y + Li.vl[1];
+    if (D == 3) vi[2] = Ci.z + Li.vl[2];
     float dU[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) dU[k] = 0.f;
@@ -668,8 +682,9 @@ __global__ void __launch_bounds__(kThreads) k_m_particle_shift(Params P, DevStat
         const int32_t j = pe.x;
         if (j == i) continue;
         float Rji[D], dv[D];
-        sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
-        sep<D>(Ci, Ei, K.C[j], K.E[j], dv);
+        const LoParts Lj(K.Lo[j]);
+        sepx<D>(Ai, Li, K.A[j], Lj, Rji);
+        sepv<D>(Ci, Li, K.C[j], Lj, dv);
         const float r = sqrtf(__int_as_float(pe.y));
         const float volj = K.A[j].w;
         const float kern = f_kernel(f, r);
@@ -730,7 +745,8 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_pressure(Params P, DevStat
     if (i >= P.nb) return;
     if (P.blocks[W.blk[i]].bound_solver != FJSPH_PRESSURE_G) return;
     const Pf f = make_pf(P);
-    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float4 Ai = K.A[i];
+    const LoParts Li(K.Lo[i]);
     int near = 0;
     KSum kernsum, pkern;
     float acck[D];
@@ -742,9 +758,10 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_pressure(Params P, DevStat
         const int32_t j = pe.x;
         const int bj = K.bits[j];
         if (bits_b(bj) <= FJSPH_PISTON) continue;
-        const float4 Aj = K.A[j], Bj = K.B[j];
+        const float4 Aj = K.A[j];
+        const LoParts Lj(K.Lo[j]);
         float Rji[D];
-        sep<D>(Ai, Bi, Aj, Bj, Rji);
+        sepx<D>(Ai, Li, Aj, Lj, Rji);
         const float r = sqrtf(__int_as_float(pe.y));
         const float rho_j = f.rho0 + K.C[j].w;
         const float kern = Aj.w * f_kernel(f, r);
@@ -775,7 +792,8 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
     if (i >= P.nb) return;
     if (P.blocks[W.blk[i]].bound_solver != FJSPH_GHOST) return;
     const Pf f = make_pf(P);
-    const float4 Ai = K.A[i], Bi = K.B[i];
+    const float4 Ai = K.A[i];
+    const LoParts Li(K.Lo[i]);
     /* boundary velocity: set this stage, read from the FP64 state */
     float vi[D];
 #pragma unroll
@@ -790,14 +808,15 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
         const int bj = bits_b(K.bits[j]);
         if (bj == FJSPH_PIPE || bj == FJSPH_FREE) ni = 0;
         float Rji[D];
-        sep<D>(Ai, Bi, K.A[j], K.B[j], Rji);
+        const LoParts Lj(K.Lo[j]);
+        sepx<D>(Ai, Li, K.A[j], Lj, Rji);
         const float r = sqrtf(__int_as_float(pe.y));
         const float gs = f_gscale(f, r);
-        const float4 Cj = K.C[j], Ej = K.E[j];
+        const float4 Cj = K.C[j];
         float s = 0.f;
-        s += ((Cj.x + Ej.x) - vi[0]) * Rji[0];
-        s += ((Cj.y + Ej.y) - vi[1]) * Rji[1];
-        if (D == 3) s += ((Cj.z + Ej.z) - vi[2]) * Rji[2];
+        s += ((Cj.x + Lj.vl[0]) - vi[0]) * Rji[0];
+        s += ((Cj.y + Lj.vl[1]) - vi[1]) * Rji[1];
+        if (D == 3) s += ((Cj.z + Lj.vl[2]) - vi[2]) * Rji[2];
         Rr.add(-K.A[j].w * s * gs);
     }
     near_inlet[i] = ni;
@@ -831,7 +850,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
     const float pi3o4_H = P.fc.pi3o4_H;
     const float fac_bound = P.fc.fac_bound;
     const float4 Ai = K.A[i], Ci = K.C[i], Fi = K.F[i];
-    const LoParts<D> Li(K.Lo[i]);
+    const LoParts Li(K.Lo[i]);
     const float rho_i = f.rho0 + Ci.w;
     const float m_i = Ai.w * rho_i;
     const float pr_i0 = Li.pr;
@@ -893,7 +912,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, D
             prefetch_pair_inputs(K, q[kGatherAhead - 1].x, linear || ale, nofrozen);
         }
         if (j == i) continue;
-        const LoParts<D> Lj(Qj);
+        const LoParts Lj(Qj);
         /* separations as in sep(): high parts, then the (bf16) low parts */
         float Rji[D], Vji[D];
         Rji[0] = (Aj.x - Ai.x) + (Lj.xl[0] - Li.xl[0]);
