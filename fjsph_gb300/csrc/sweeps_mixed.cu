@@ -827,7 +827,7 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
 /* residual (src/Resid.cpp:243-469)                                                               */
 /* ------------------------------------------------------------------------------------------ */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads, 5) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
+__global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
                                                       Closure C) {
     __shared__ __align__(16) MlpWarpSmem mlp_smem[kThreads / 32];
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
