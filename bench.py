@@ -135,15 +135,16 @@ def resid_bytes_per_particle(s) -> int:
     count.  FP64 form (8 B words): x 3, search x 3, v 3, rho, p, m, aVisc 3, deltaD, cellV 3,
     cellP, cellRho, lam_nb, woccl (8 B each), cellID, CSR offset (8 B), b, surfzone (4 B); ALE adds
     vPert 3, NOFROZEN gradRho 3.  Writes acc 3, Af 3, Rrho.
-    FP32 split-precision form: x and v as FP32 hi/lo pairs (8 B per component), rho, p, volume and
-    flags at 4 B; aVisc 3 and deltaD (FP64 state), CSR offset and cellID (8 B); the closure reads
+    FP32 split-precision form: x and v as an FP32 high part and a bf16 low part (6 B per
+    component), rho, p / rho^2 with the type flags and volume at 4 B; aVisc 3 and deltaD (FP64
+    state), CSR offset and cellID (8 B); the closure reads
     cellV 3, cellP, cellRho, m, lam_nb, woccl (8 B), the learned closure also the four occlusion
     inputs, the normal and lambda (4 B each).  Writes acc 3, Af 3, Rrho at 8 B.
     """
     from fjsph_gb300 import _cdefs as d
     D = s.dim
     if s.precision == d.PREC_MIXED:
-        b = 8 * D * 2 + 4 * 4                      # x, v (hi/lo), rho, p, volume, flags
+        b = 6 * D * 2 + 4 * 3                      # x, v (FP32 high, bf16 low), rho, p/rho^2, volume
         b += 8 * (D + 1) + 8 * 2                   # aVisc, deltaD, CSR offset, cellID
         b += 8 * (D + 5)                           # cellV, cellP, cellRho, m, lam_nb, woccl
         if s.aero_closure == d.CLOSURE_LEARNED:
