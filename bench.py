@@ -166,7 +166,7 @@ def resid_bytes_per_particle(s) -> int:
 # DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
 # 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
 # the benchmark's particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 634.07e6 / 620_210}
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 709.41e6 / 620_210}
 
 
 def train_closure(args, log):
