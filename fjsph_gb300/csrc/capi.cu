@@ -1712,6 +1712,9 @@ int fjsph_ctx_create(const fjsph_settings *s, int64_t capacity, fjsph_ctx **out)
     A(dalloc(c, &c->stage2, capacity * 9));
     CellGrid &G = c->G;
     A(dalloc(c, &G.hash, capacity));
+    A(dalloc(c, &G.frac, capacity));
+    A(dalloc(c, &G.hash2, capacity));
+    A(dalloc(c, &G.frac2, capacity));
     A(alloc_table(c, next_pow2(std::max<int64_t>(2 * capacity, kMinTable))));
     A(dalloc(c, &G.sorted, capacity));
     A(dalloc(c, &G.sorted_hi, capacity));

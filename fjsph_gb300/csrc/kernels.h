@@ -83,7 +83,10 @@ int mlp_num_bf16_t();
 /* ---- neighbours.cu ------------------------------------------------------------------------ */
 struct CellGrid {
     int64_t table_size;      /* power of two                                  */
-    uint32_t *hash;          /* [cap]  bucket of each slot                    */
+    uint32_t *hash;          /* [cap]  bucket | x quarter << 30 of each slot   */
+    float4 *frac;            /* [cap]  position inside the cell, cell edges   */
+    uint32_t *hash2;         /* [cap]  re-ordering buffers of hash and frac   */
+    float4 *frac2;
     int32_t *count;          /* [table_size + 1]                              */
     int32_t *start;          /* [table_size + 1] exclusive scan of count      */
     int32_t *sorted;         /* [cap]  slots ordered by bucket                */

@@ -138,6 +138,10 @@ __global__ void k_bbox_finish(Params P, const unsigned long long *part, int nblk
     const double R = sqrt(P.sr);
     const double rel = 2.0 * (P.D * 4.0 * u * mag / R + (3.0 * P.D + 2.0) * u) + 1e-7;
     bbox[6] = rel;
+    /* the FP32 thresholds of the band, for the walk */
+    float *thr = reinterpret_cast<float *>(bbox + 7);
+    thr[0] = (float)(P.sr * (1.0 - rel));
+    thr[1] = (float)(P.sr * (1.0 + rel));
     grid[0] = nc[0];
     grid[1] = nc[1];
     grid[2] = nc[2];
@@ -157,10 +161,6 @@ constexpr uint32_t kQUnknown = 1023u;
  * quarter of the particle in its cell in the top two */
 constexpr int kQuarterShift = 30;
 constexpr uint32_t kBucketMask = (1u << kQuarterShift) - 1u;
-__device__ __forceinline__ int x_quarter(const Params &P, double x, double lo, int64_t cx) {
-    const double u = (cell_pos(P, x, lo, 0) - (double)cx) * 4.0;
-    return u < 1.0 ? 0 : (u < 2.0 ? 1 : (u < 3.0 ? 2 : 3));
-}
 
 /* ---- hashing ---------------------------------------------------------------------------------- */
 template <int D>
@@ -173,6 +173,24 @@ __device__ __forceinline__ void cell_coords(const Params &P, const double *x, co
         double f = floor(cell_pos(P, x[k], lo[k], k));
         int64_t v = (f > 0.0) ? (int64_t)fmin(f, (double)(nc[k] - 1)) : 0;
         c[k] = v;
+    }
+}
+
+/* cell_coords and the position inside the cell in cell edges (the same products) */
+template <int D>
+__device__ __forceinline__ void cell_coords_frac(const Params &P, const double *x, const double *lo, const int64_t *nc,
+                                                 int64_t *c, float *t) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        c[k] = 0;
+        t[k] = 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double u = cell_pos(P, x[k], lo[k], k);
+        const double f = floor(u);
+        c[k] = (f > 0.0) ? (int64_t)fmin(f, (double)(nc[k] - 1)) : 0;
+        t[k] = (float)(u - (double)c[k]);
     }
 }
 
@@ -197,9 +215,12 @@ __global__ void k_hash_count(Params P, DevState W, double *xs0, double *xs1, dou
         x[k] = W.x[k][i];
         xs[k][i] = x[k];
     }
-    cell_coords<D>(P, x, lo, nc, c);
+    float t[3];
+    cell_coords_frac<D>(P, x, lo, nc, c, t);
     const uint32_t h = (uint32_t)(lin_index(c, nc) & (uint64_t)(G.table_size - 1));
-    G.hash[i] = h | ((uint32_t)x_quarter(P, x[0], lo[0], c[0]) << kQuarterShift);
+    const int quarter = t[0] < 0.25f ? 0 : (t[0] < 0.5f ? 1 : (t[0] < 0.75f ? 2 : 3));
+    G.hash[i] = h | ((uint32_t)quarter << kQuarterShift);
+    G.frac[i] = make_float4(t[0], t[1], t[2], 0.f);
     /* lanes of a warp in the same bucket (consecutive slots usually are) add once */
     const unsigned peers = __match_any_sync(__activemask(), h);
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&G.count[h], (int32_t)__popc(peers));
@@ -265,22 +286,37 @@ __global__ void k_sorted_pos(Params P, const double *xs0, const double *xs1, con
 /* Visits every candidate of particle i once and calls f(j) for each member (d2 < sr). */
 template <int D, class F>
 __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const CellGrid &G, int64_t i, F &&f) {
-    double lo[3], xi[3] = {0, 0, 0};
     int64_t nc[3], c[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        lo[k] = G.bbox[k];
-        nc[k] = G.grid[k];
-    }
-#pragma unroll
-    for (int k = 0; k < D; ++k) xi[k] = xs[k][i];
-    cell_coords<D>(P, xi, lo, nc, c);
+    for (int k = 0; k < 3; ++k) nc[k] = G.grid[k];
     const bool wrap = G.grid[3] != 0;
+    /* the particle's cell and its position inside it, from the hash pass (for a wrapped table
+     * the bucket is not the cell: recomputed) */
+    float t[3];
+    {
+        const float4 tf = G.frac[i];
+        t[0] = tf.x;
+        t[1] = tf.y;
+        t[2] = tf.z;
+    }
+    if (!wrap) {
+        const uint64_t h = G.hash[i] & kBucketMask;
+        c[0] = (int64_t)(h % (uint64_t)nc[0]);
+        c[1] = (int64_t)((h / (uint64_t)nc[0]) % (uint64_t)nc[1]);
+        c[2] = (int64_t)(h / ((uint64_t)nc[0] * (uint64_t)nc[1]));
+    } else {
+        double lo[3], xi[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) lo[k] = G.bbox[k];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xi[k] = xs[k][i];
+        cell_coords<D>(P, xi, lo, nc, c);
+    }
     float fi[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < D; ++k) fi[k] = to_f32(xi[k]);
-    const double band = G.bbox[6];
-    const float sr_lo = (float)(P.sr * (1.0 - band)), sr_hi = (float)(P.sr * (1.0 + band));
+    for (int k = 0; k < D; ++k) fi[k] = to_f32(xs[k][i]);
+    const float sr_lo = reinterpret_cast<const float *>(G.bbox + 7)[0];
+    const float sr_hi = reinterpret_cast<const float *>(G.bbox + 7)[1];
     const uint64_t mask = (uint64_t)(G.table_size - 1);
     const int zr = (D == 3) ? kCellDiv : 0, yr = kCellDiv;
     const int64_t x0 = c[0] > 0 ? c[0] - 1 : 0;
@@ -313,9 +349,12 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
         if (d2f < sr_lo) return true;
         if (d2f > sr_hi) return false;
         const int32_t j = __float_as_int(fj.w);
-        double xj[D];
+        double xi[D], xj[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) xj[k] = xs[k][j];
+        for (int k = 0; k < D; ++k) {
+            xi[k] = xs[k][i];
+            xj[k] = xs[k][j];
+        }
         return dist2<D>(xi, xj) < P.sr;
     };
     /* Candidates [e0, e1) in batches of 32: a bit mask of the members first, then f for the
@@ -344,9 +383,7 @@ __device__ __forceinline__ void walk(const Params &P, double *const xs[3], const
     const float mx = 5e-7f * (fabsf(fi[0]) + 2.f * Rf) + 1e-5f * Rf;
     const float ey = (float)P.cell_edge[1], ez = (float)P.cell_edge[2], inv_x = (float)P.cell_inv[0];
     /* position of x_i inside its cell, in cell edges */
-    const float tx = (float)(cell_pos(P, xi[0], lo[0], 0) - (double)c[0]);
-    const float ty = (float)(cell_pos(P, xi[1], lo[1], 1) - (double)c[1]);
-    const float tz = D == 3 ? (float)(cell_pos(P, xi[2], lo[2], 2) - (double)c[2]) : 0.f;
+    const float tx = t[0], ty = t[1], tz = D == 3 ? t[2] : 0.f;
     auto gap = [](int d, float t) { /* distance to the band of row offset d, in cell edges */
         const float g = d > 0 ? (float)d - t : (d < 0 ? t - 1.f - (float)d : 0.f);
         return fmaxf(0.f, g - 1e-4f);
@@ -704,13 +741,17 @@ __global__ void k_bound_flags(Params P, const int32_t *sorted, int32_t *flag) {
     flag[p] = sorted[p] < P.nb ? 1 : 0;
 }
 
-__global__ void k_reorder_map(Params P, int32_t *sorted, const int32_t *flag, const int32_t *ex, int32_t *new_of_old) {
+/* new slot of every particle (boundary slots first, each part in bucket order); the per-slot cell
+ * data of the hash pass follow their particles into the second buffers */
+__global__ void k_reorder_map(Params P, CellGrid G, const int32_t *flag, const int32_t *ex, int32_t *new_of_old) {
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    const int32_t old = sorted[p];
+    const int32_t old = G.sorted[p];
     const int32_t ns = flag[p] ? ex[p] : (int32_t)(P.nb + p - ex[p]);
     new_of_old[old] = ns;
-    sorted[p] = ns;
+    G.sorted[p] = ns;
+    G.hash2[ns] = G.hash[old];
+    G.frac2[ns] = G.frac[old];
 }
 
 } // namespace
@@ -812,7 +853,9 @@ void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old,
     int32_t *flag = tmp, *ex = tmp + P.n, *part = tmp + 2 * P.n + 1;
     k_bound_flags<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G.sorted, flag);
     scan_exclusive<int32_t, int32_t>(flag, ex, P.n, part, s);
-    k_reorder_map<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G.sorted, flag, ex, new_of_old);
+    k_reorder_map<<<grid_for(P.n, kThreads), kThreads, 0, s>>>(P, G, flag, ex, new_of_old);
+    cudaMemcpyAsync(G.hash, G.hash2, sizeof(uint32_t) * P.n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(G.frac, G.frac2, sizeof(float4) * P.n, cudaMemcpyDeviceToDevice, s);
 }
 
 } // namespace fjsph
