@@ -17,6 +17,7 @@ NEWMARK_BETA, RUNGE_KUTTA = 0, 1
 DBC, PRESSURE_G, GHOST = 0, 1, 2
 COLE_EOS, ISO_EOS = 0, 1
 NOAERO, GISSLER, INDUCED_PRESSURE, SKIN_FRIC = 0, 1, 2, 3
+CONST_VEL, MESH_INFL, VLM_INFL = 0, 1, 2  # fjsph_aero_source
 PREC_FP64, PREC_MIXED = 0, 1
 CLOSURE_PLAIN, CLOSURE_LEARNED = 0, 1
 CLOSURE_ARM_JUDGE, CLOSURE_ARM_LOG = 1, 2
@@ -105,3 +106,10 @@ class ClosureReport(C.Structure):
     _fields_ = [("judged", _i64), ("judged_particles", _i64), ("last_rel_rms", _d), ("max_rel_rms", _d),
                 ("judge_tol", _d), ("logged", _i64), ("log_capacity", _i64), ("steps", _i64),
                 ("learned_active", _i32), ("fallback", _i32)]
+
+
+class Vlm(C.Structure):
+    """fjsph_vlm: the vortex-lattice wing of the air source (src/VLM.h)."""
+    _fields_ = [("span", _d), ("chord", _d), ("panels_span", _i32), ("panels_chord", _i32), ("aoa_deg", _d),
+                ("sweep_deg", _d), ("taper", _d), ("flap_start", _i32), ("flap_width", _i32),
+                ("flap_depth", _i32), ("pad", _i32), ("flap_deg", _d), ("max_vel_fac", _d), ("max_vel", _d)]

@@ -84,6 +84,10 @@ PROTOTYPES = {
     "fjsph_closure_arm": (C.c_int, [_P, _i32]),
     "fjsph_closure_report_get": (C.c_int, [_P, C.POINTER(d.ClosureReport)]),
     "fjsph_closure_reset": (C.c_int, [_P]),
+    "fjsph_vlm_defaults": (C.c_int, [C.POINTER(d.Vlm)]),
+    "fjsph_vlm_setup": (C.c_int, [_P, C.POINTER(d.Vlm), _i32p]),
+    "fjsph_vlm_panels": (C.c_int, [_P, _dp, _dp, _i32p]),
+    "fjsph_vlm_velocity": (C.c_int, [_P, _i64, _dp, _dp]),
     "fjsph_find_timestep_noalloc": (C.c_int, [C.POINTER(d.Settings), _i64, C.POINTER(_dp), C.POINTER(_dp), _dp, _dp,
                                               _dp, C.POINTER(_dp), C.POINTER(_dp), _P, _dp, _dp]),
 }

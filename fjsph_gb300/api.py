@@ -342,6 +342,33 @@ class Context:
     def closure_reset(self) -> None:
         check("fjsph_closure_reset", self._lib.fjsph_closure_reset(self._h))
 
+    # ---- vortex-lattice air source (src/VLM.h) ----
+    def vlm_setup(self, vlm: "d.Vlm") -> int:
+        """VLM::Init + GetGamma for the context's v_inf; returns the panel count."""
+        n = C.c_int32(0)
+        check("fjsph_vlm_setup", self._lib.fjsph_vlm_setup(self._h, C.byref(vlm), C.byref(n)))
+        return n.value
+
+    def vlm_panels(self):
+        """(gamma[np], abc[np, 3, 3]): circulations and the vortex ends A, B and control point C."""
+        n = C.c_int32(0)
+        check("fjsph_vlm_panels", self._lib.fjsph_vlm_panels(self._h, None, None, C.byref(n)))
+        g = np.zeros(n.value)
+        abc = np.zeros((n.value, 3, 3))
+        check("fjsph_vlm_panels", self._lib.fjsph_vlm_panels(self._h, _dptr(g), _dptr(abc), C.byref(n)))
+        return g, abc
+
+    def vlm_velocity(self, pos: np.ndarray) -> np.ndarray:
+        """VLM::getVelocity at the rows of pos (n x 3), on the device in the context's precision."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros_like(p)
+        check("fjsph_vlm_velocity", self._lib.fjsph_vlm_velocity(self._h, p.shape[0], _dptr(p), _dptr(out)))
+        return out
+
 
 def _fptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))

@@ -165,6 +165,12 @@ struct fjsph_ctx {
     cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     int64_t graph_launches[4] = {0, 0, 0, 0};
     int64_t graph_uses = 0;
+    /* vortex-lattice air source */
+    std::vector<double> vlm_abc, vlm_gamma; /* host copies: A, B, C per panel; circulations */
+    double *vlm_ab = nullptr, *vlm_g = nullptr;
+    float *vlm_abf = nullptr, *vlm_gf = nullptr;
+    VlmDev vlm{};
+    double *air_v = nullptr; /* 3 per slot */
 };
 
 namespace {
@@ -262,7 +268,7 @@ int validate_settings(const fjsph_settings *s) {
     /* -DNOFROZEN -DLINEAR does not compile upstream (src/Resid.cpp:381 uses fluid.rho0) */
     if ((s->variant & FJSPH_VAR_NOFROZEN) && (s->variant & FJSPH_VAR_LINEAR)) return FJSPH_E_UNSUPPORTED;
     if (s->precision != FJSPH_PREC_FP64 && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
-    if (s->asource != 0) return FJSPH_E_UNSUPPORTED;
+    if (s->asource != FJSPH_CONST_VEL && !(s->asource == FJSPH_VLM_INFL && s->dim == 3)) return FJSPH_E_UNSUPPORTED;
     if (s->aero_closure != FJSPH_CLOSURE_PLAIN && s->aero_closure != FJSPH_CLOSURE_LEARNED) return FJSPH_E_ARG;
     /* the learned closure lives in the split-precision residual */
     if (s->aero_closure == FJSPH_CLOSURE_LEARNED && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
@@ -327,6 +333,7 @@ Params make_params(const fjsph_ctx *c) {
     }
     P.grp = c->ngrp > 0 ? c->grp : nullptr;
     P.g_vinf = c->g_vinf;
+    P.air_v = (s.asource == FJSPH_VLM_INFL && c->vlm.np > 0) ? c->air_v : nullptr;
     P.sweep_threads = c->tune[0];
     P.resid_threads = c->tune[1];
     P.list_ahead = c->tune[2];
@@ -902,6 +909,15 @@ int npd_only(fjsph_ctx *c, const Params &P) {
     return finish_npd(c);
 }
 
+/* the vortex-lattice air velocity of the particles that use it (before the aero velocity pass) */
+int vlm_air(fjsph_ctx *c, const Params &P, const DevNbr &N) {
+    if (c->s.asource != FJSPH_VLM_INFL) return FJSPH_OK;
+    if (c->vlm.np == 0) return FJSPH_E_STATE; /* fjsph_vlm_setup has not run */
+    launch_vlm_air(P, WS(c), N, c->vlm, c->air_v, mixed(c), c->stream);
+    c->launches++;
+    return FJSPH_OK;
+}
+
 int prestep_passes(fjsph_ctx *c) {
     if (!c->nbr_valid) return FJSPH_E_STATE;
     Params P = make_params(c);
@@ -913,6 +929,7 @@ int prestep_passes(fjsph_ctx *c) {
         /* split-precision form: the dissipation terms are computed in the surface-normal walk
          * (they read nothing the surface passes write), timed with the surface section */
         Section sec(c, PASS_SURFACE);
+        TRY(vlm_air(c, P, N));
         launch_aero_velocity(P, WS(c), N, s);
         if (mixed(c)) {
             launch_m_surface(P, WS(c), N, c->K, dissipation, s);
@@ -2041,6 +2058,7 @@ int fjsph_dsph_prestep(fjsph_ctx *c, double *npd) {
 
 int fjsph_get_aero_velocity(fjsph_ctx *c) {
     TRY(need_nbr(c));
+    TRY(vlm_air(c, make_params(c), make_nbr(c)));
     launch_aero_velocity(make_params(c), WS(c), make_nbr(c), c->stream);
     c->pn_equals_W = false;
     return sync(c);
@@ -2295,8 +2313,10 @@ int fjsph_set_groups(fjsph_ctx *c, int32_t ngroups, const int64_t *first, const 
     if (first[0] != 0 || first[ngroups] != n_ref) return FJSPH_E_ARG;
     for (int32_t g = 0; g < ngroups; ++g)
         if (first[g + 1] <= first[g]) return FJSPH_E_ARG;
-    /* the device step of groups covers Runge-Kutta without insertion or deletion */
+    /* the device step of groups covers Runge-Kutta without insertion or deletion, with each
+     * group's uniform v_inf as the air source */
     if (c->s.solver_type != FJSPH_RUNGE_KUTTA || !c->inlets.empty()) return FJSPH_E_UNSUPPORTED;
+    if (c->s.asource != FJSPH_CONST_VEL) return FJSPH_E_UNSUPPORTED;
     for (const fjsph_block &B : c->blocks)
         if (B.delconst != kDefaultVal || B.block_type == kInletZone) return FJSPH_E_UNSUPPORTED;
     TRY(sync(c));
@@ -2657,6 +2677,97 @@ int fjsph_closure_reset(fjsph_ctx *c) {
     c->judged = c->judged_particles = 0;
     c->last_rel_rms = c->max_rel_rms = 0.0;
     return FJSPH_OK;
+}
+
+/* ---- vortex-lattice air source ---------------------------------------------------------------- */
+int fjsph_vlm_defaults(fjsph_vlm *v) {
+    if (!v) return FJSPH_E_ARG;
+    std::memset(v, 0, sizeof(*v));
+    v->span = v->chord = -1.0;
+    v->panels_span = v->panels_chord = -1;
+    v->max_vel_fac = 2.0;
+    v->max_vel = 2.0; /* maxVelFac x |(1, 0, 0)|, the reference's constructor value */
+    return FJSPH_OK;
+}
+
+int fjsph_vlm_setup(fjsph_ctx *c, const fjsph_vlm *v, int32_t *npanels) {
+    TRY(check_ctx(c));
+    if (!v) return FJSPH_E_ARG;
+    if (c->D != 3) return FJSPH_E_UNSUPPORTED;
+    std::vector<double> abc, gamma;
+    TRY(vlm_build(*v, c->s.v_inf, abc, gamma));
+    const int32_t np = (int32_t)gamma.size();
+    TRY(sync(c));
+    TRY(graph_release(c));
+    TRY(dfree(c, c->vlm_ab));
+    TRY(dfree(c, c->vlm_g));
+    TRY(dfree(c, c->vlm_abf));
+    TRY(dfree(c, c->vlm_gf));
+    TRY(dalloc(c, &c->vlm_ab, 6 * (int64_t)np));
+    TRY(dalloc(c, &c->vlm_g, np));
+    TRY(dalloc(c, &c->vlm_abf, 12 * (int64_t)np));
+    TRY(dalloc(c, &c->vlm_gf, np));
+    if (!c->air_v) TRY(dalloc(c, &c->air_v, 3 * c->cap));
+    std::vector<double> ab(6 * (size_t)np);
+    std::vector<float> abf(12 * (size_t)np), gf(np); /* FP32: A hi, A lo, B hi, B lo */
+    for (int32_t q = 0; q < np; ++q) {
+        for (int k = 0; k < 6; ++k) ab[6 * q + k] = abc[9 * q + k];
+        for (int e = 0; e < 2; ++e)
+            for (int k = 0; k < 3; ++k) {
+                const double x = abc[9 * q + 3 * e + k];
+                const float hi = (float)x;
+                abf[12 * q + 6 * e + k] = hi;
+                abf[12 * q + 6 * e + 3 + k] = (float)(x - (double)hi);
+            }
+        gf[q] = (float)gamma[q];
+    }
+    CU(cudaMemcpy(c->vlm_ab, ab.data(), sizeof(double) * ab.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(c->vlm_g, gamma.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(c->vlm_abf, abf.data(), sizeof(float) * abf.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(c->vlm_gf, gf.data(), sizeof(float) * np, cudaMemcpyHostToDevice));
+    VlmDev &V = c->vlm;
+    V.np = np;
+    V.ab = c->vlm_ab;
+    V.gamma = c->vlm_g;
+    V.abf = c->vlm_abf;
+    V.gammaf = c->vlm_gf;
+    for (int k = 0; k < 3; ++k) V.vinf[k] = c->s.v_inf[k];
+    const double vn = std::sqrt(V.vinf[0] * V.vinf[0] + V.vinf[1] * V.vinf[1] + V.vinf[2] * V.vinf[2]);
+    /* src/VLM.cpp:89-90: a velocity limit still at the constructor value becomes the factor
+     * times the freestream speed */
+    V.max_vel = (v->max_vel == 2.0) ? v->max_vel_fac * vn : v->max_vel;
+    c->vlm_abc = std::move(abc);
+    c->vlm_gamma = std::move(gamma);
+    if (npanels) *npanels = np;
+    return FJSPH_OK;
+}
+
+int fjsph_vlm_panels(fjsph_ctx *c, double *gamma, double *abc, int32_t *npanels) {
+    TRY(check_ctx(c));
+    if (npanels) *npanels = c->vlm.np;
+    if (gamma) std::copy(c->vlm_gamma.begin(), c->vlm_gamma.end(), gamma);
+    if (abc) std::copy(c->vlm_abc.begin(), c->vlm_abc.end(), abc);
+    return FJSPH_OK;
+}
+
+int fjsph_vlm_velocity(fjsph_ctx *c, int64_t n, const double *pos, double *vel) {
+    TRY(check_ctx(c));
+    if (c->vlm.np == 0) return FJSPH_E_STATE;
+    if (n < 0 || (n > 0 && (!pos || !vel))) return FJSPH_E_ARG;
+    if (n == 0) return FJSPH_OK;
+    TRY(sync(c));
+    double *d = nullptr;
+    CU(cudaMalloc(&d, sizeof(double) * 6 * (size_t)n));
+    int rc = FJSPH_OK;
+    if (cudaMemcpy(d, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) rc = FJSPH_E_CUDA;
+    if (rc == FJSPH_OK) {
+        launch_vlm_points(c->vlm, n, d, d + 3 * n, mixed(c), c->stream);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess ||
+            cudaMemcpy(vel, d + 3 * n, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = FJSPH_E_CUDA;
+    }
+    cudaFree(d);
+    return rc;
 }
 
 } /* extern "C" */

@@ -76,6 +76,9 @@ struct Params {
      * are then arrays indexed by group. */
     const int32_t *grp;
     const double *g_vinf; /* 3 per group */
+    /* air velocity per slot (3 per slot) when the air source is position dependent; null for
+     * the uniform v_inf */
+    const double *air_v;
     /* launch configuration of the split-precision pair sweeps (the autotuner's choices) */
     int32_t sweep_threads, resid_threads, list_ahead;
     FConst fc;
@@ -93,6 +96,7 @@ constexpr int kCellDiv = CELL_DIV_DEFAULT;
 
 __device__ __forceinline__ int32_t grp_of(const Params &P, int64_t i) { return P.grp ? P.grp[i] : 0; }
 __device__ __forceinline__ double vinf_of(const Params &P, int64_t i, int k) {
+    if (P.air_v) return P.air_v[3 * i + k]; /* position-dependent source (vortex lattice) */
     return P.grp ? P.g_vinf[3 * P.grp[i] + k] : P.v_inf[k];
 }
 

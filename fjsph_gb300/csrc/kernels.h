@@ -4,12 +4,32 @@
  */
 #pragma once
 
+#include <vector>
+
 #include "closure.cuh"
 #include "common.cuh"
 
 namespace fjsph {
 
 /* Packed FP32 split-precision inputs of the mixed form (see sweeps_mixed.cu). */
+/* ---- vlm.cu: vortex-lattice air source -------------------------------------------------------- */
+struct VlmDev {
+    int32_t np;           /* panels                                              */
+    const double *ab;     /* [6 np] vortex ends A, B of every panel (FP64)        */
+    const double *gamma;  /* [np]   circulations                                  */
+    const float *abf;     /* [12 np] FP32: A high, A low, B high, B low           */
+    const float *gammaf;
+    double vinf[3];
+    double max_vel;
+};
+/* panels (A, B, C: 9 doubles each) and circulations of a wing for the freestream vinf */
+int vlm_build(const fjsph_vlm &v, const double *vinf, std::vector<double> &abc, std::vector<double> &gamma);
+/* air[3 i + k] = the VLM velocity of the fluid particles that use it (FP32 sums when fp32) */
+void launch_vlm_air(const Params &P, const DevState &W, const DevNbr &N, const VlmDev &V, double *air, bool fp32,
+                    cudaStream_t s);
+/* vel[3 i + k] at pos[3 i + k], i < n */
+void launch_vlm_points(const VlmDev &V, int64_t n, const double *pos, double *vel, bool fp32, cudaStream_t s);
+
 struct Packed {
     float4 *A, *C, *F, *G, *N, *T;
     float4 *O; /* occlusion statistics of the surface-curvature pass (learned-closure inputs 0-3) */

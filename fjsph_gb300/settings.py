@@ -75,6 +75,7 @@ PARA_KEYS = {
     "Reference density": ("rho_g", "f"),
     "Reference temperature": ("temp_g", "f"),
     "Gas constant gamma": ("gamma_g", "f"),
+    "VLM definition filename": ("vlm_file", "s"),
     "Input fluid definition filename": ("input_fluid_file", "s"),
     "Input boundary definition filename": ("input_bound_file", "s"),
 }
@@ -145,7 +146,51 @@ def apply_para(s: d.Settings, kv: dict) -> dict:
         if extra["aero_case"] not in AERO_CASES:
             raise ValueError("Aerodynamic coupling model is not defined or correct.")
         s.acase = AERO_CASES[extra["aero_case"]]
+    # air source (src/IO.cpp:466-480): a VLM definition file selects the vortex lattice in 3D
+    if extra.get("vlm_file") and s.dim == 3:
+        s.asource = d.VLM_INFL
     return extra
+
+
+# VLM::Init keys (src/VLM.cpp:27-44) -> (field, kind); "v2" = two values into two fields
+VLM_KEYS = {
+    "VLM wing dimensions": (("span", "chord"), "v2"),
+    "VLM panel counts": (("panels_span", "panels_chord"), "v2i"),
+    "VLM angle alpha (degree)": ("aoa_deg", "f"),
+    "VLM sweep angle (degree)": ("sweep_deg", "f"),
+    "VLM taper ratio": ("taper", "f"),
+    "VLM flap start (panels)": ("flap_start", "i"),
+    "VLM flap width (panels)": ("flap_width", "i"),
+    "VLM flap depth (panels)": ("flap_depth", "i"),
+    "VLM flap angle (degree)": ("flap_deg", "f"),
+    "VLM maximum velocity factor": ("max_vel_fac", "f"),
+    "VLM maximum velocity": ("max_vel", "f"),
+}
+
+
+def read_vlm(path: str | Path) -> d.Vlm:
+    """The wing of a VLM definition file (the para file itself for "(thisfile)")."""
+    v = d.Vlm()
+    check("fjsph_vlm_defaults", lib().fjsph_vlm_defaults(C.byref(v)))
+    for raw in Path(path).read_text().splitlines():
+        line = raw.lstrip(" \n\r\t\f\v")
+        pos = line.find(":")
+        if pos == -1:
+            continue
+        key = line[:pos].lstrip(" \n\r\t\f\v")
+        if key not in VLM_KEYS:
+            continue
+        field, kind = VLM_KEYS[key]
+        val = _value(line)
+        if kind in ("v2", "v2i"):
+            parts = [p for p in val.replace(" ", "").split(",") if p != ""]
+            for f, p in zip(field, parts[:2]):
+                setattr(v, f, int(_num(p)) if kind == "v2i" else _num(p))
+        elif kind == "f":
+            setattr(v, field, _num(val))
+        else:
+            setattr(v, field, int(_num(val)))
+    return v
 
 
 def read_para(path: str | Path, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE) -> tuple[d.Settings, dict]:
@@ -154,6 +199,8 @@ def read_para(path: str | Path, dim: int, variant: int = 0, st_model: int = d.ST
     s.variant = variant
     s.st_model = st_model
     extra = apply_para(s, parse_para_text(Path(path).read_text()))
+    if extra.get("vlm_file") == "(thisfile)":
+        extra["vlm_file"] = str(path)
     if s.delta_t_min > 0.0:
         s.delta_t = s.delta_t_min
     derive(s)

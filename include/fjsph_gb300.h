@@ -67,6 +67,9 @@ enum fjsph_solver { FJSPH_NEWMARK_BETA = 0, FJSPH_RUNGE_KUTTA = 1 };
 enum fjsph_bound_solver { FJSPH_DBC = 0, FJSPH_PRESSURE_G = 1, FJSPH_GHOST = 2 };
 enum fjsph_eos { FJSPH_COLE_EOS = 0, FJSPH_ISO_EOS = 1 };
 enum fjsph_aero_case { FJSPH_NOAERO = 0, FJSPH_GISSLER = 1, FJSPH_INDUCED_PRESSURE = 2, FJSPH_SKIN_FRIC = 3 };
+/* Air velocity source (src/VarDefs.h:168-173): uniform v_inf, mesh cells (not built), the
+ * vortex-lattice field of fjsph_vlm_setup (3D). */
+enum fjsph_aero_source { FJSPH_CONST_VEL = 0, FJSPH_MESH_INFL = 1, FJSPH_VLM_INFL = 2 };
 
 /* Arithmetic form of the pair kernels. */
 enum fjsph_precision {
@@ -105,7 +108,7 @@ typedef struct fjsph_settings {
     /* SIM */
     double particle_step, dx, scale;
     double grav[3];
-    int32_t asource;        /* 0 = constVel (only analytic source supported)            */
+    int32_t asource;        /* fjsph_aero_source; FJSPH_VLM_INFL needs fjsph_vlm_setup   */
     int32_t init_hydro_pressure;
     double hydro_height;
     int64_t max_points;
@@ -347,6 +350,36 @@ int fjsph_closure_arm(fjsph_ctx *ctx, int32_t what);
 int fjsph_closure_report_get(fjsph_ctx *ctx, fjsph_closure_report *out);
 /* Clears the fallback flag and the judge statistics. */
 int fjsph_closure_reset(fjsph_ctx *ctx);
+
+/* ---- vortex-lattice air source (src/VLM.h, src/VLM.cpp) ------------------------------------ */
+/* A swept, tapered wing of horseshoe vortices with an optional trailing-edge flap.  Fields keep
+ * the reference's para-file meaning ("VLM wing dimensions", "VLM panel counts", ...):
+ * span and chord are coords[0] (each side of y = 0) and coords[1]; panels_span and panels_chord
+ * the panel counts per side and chordwise; the flap covers span strips
+ * [flap_start, flap_start + flap_width) on each side over its last flap_depth chordwise panels,
+ * deflected by flap_deg.  aoa_deg is read by the reference but not used in the geometry (the
+ * freestream direction carries the incidence).  Velocities are limited to max_vel; max_vel = 2.0
+ * (the reference's default) means max_vel_fac x |v_inf|. */
+typedef struct fjsph_vlm {
+    double span, chord;
+    int32_t panels_span, panels_chord;
+    double aoa_deg, sweep_deg, taper;
+    int32_t flap_start, flap_width, flap_depth, pad;
+    double flap_deg;
+    double max_vel_fac, max_vel;
+} fjsph_vlm;
+/* the reference's VLM defaults (src/VLM.h:36-55); span, chord and panel counts are -1 (required) */
+int fjsph_vlm_defaults(fjsph_vlm *v);
+/* VLM::Init + VLM::GetGamma (src/VLM.cpp:14-118): builds the panels, solves the circulations for
+ * the context's v_inf (3D) and keeps them on the device; the air source of a context whose
+ * settings name FJSPH_VLM_INFL.  Returns the panel count in *npanels (may be null). */
+int fjsph_vlm_setup(fjsph_ctx *ctx, const fjsph_vlm *v, int32_t *npanels);
+/* Circulation of every panel (gamma[npanels]) and the panels' vortex ends and control points
+ * (A, B, C: 9 doubles per panel, may be null); *npanels receives the count. */
+int fjsph_vlm_panels(fjsph_ctx *ctx, double *gamma, double *abc, int32_t *npanels);
+/* VLM::getVelocity (src/VLM.cpp:119-140) at n host points pos[3n] into vel[3n], on the device in
+ * the context's precision (FP64, or FP32 sums for the split-precision form). */
+int fjsph_vlm_velocity(fjsph_ctx *ctx, int64_t n, const double *pos, double *vel);
 
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */

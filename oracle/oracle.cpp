@@ -84,6 +84,10 @@ struct orc_sim {
     double minST = 9999999.0, maxU = kEps, maxShift = kEps;
     int64_t start_index = 0, end_index = 0;
     uint32_t iteration = 0;
+    /* vortex lattice (VLM.h:31-97): panels A, B, C and normal, circulations, limit */
+    std::vector<double> vlm_A, vlm_B, vlm_C, vlm_gamma;
+    double vlm_vinf[3] = {0, 0, 0}, vlm_maxvel = 0.0;
+    bool vlm_ready = false;
 };
 
 namespace {
@@ -613,6 +617,81 @@ double dsph_prestep(orc_sim *o, int64_t end, std::vector<Part> &P) {
 /* ------------------------------------------------------------------------------------------ */
 /* Resid.cpp:569-611 get_aero_velocity, constVel source                                         */
 /* ------------------------------------------------------------------------------------------ */
+/* ------------------------------------------------------------------------------------------ */
+/* VLM.cpp: the vortex-lattice air velocity                                                      */
+/* ------------------------------------------------------------------------------------------ */
+inline void cross3(const double *a, const double *b, double *c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* FindInfluence / FindInfluenceConditioned (VLM.cpp:324-430): velocity of a unit horseshoe with
+ * bound vortex A-B and legs along v_inf; conditioned: zero when P is on one of its lines */
+void vlm_influence(const double *A, const double *B, const double *P, const double *vinf, bool conditioned,
+                   double *out) {
+    const double ipi4 = 1.0 / (4.0 * kPi);
+    zero(out, 3);
+    double seg[3][3];
+    for (int sgm = 0; sgm < 3; ++sgm) {
+        double r0[3], r1[3], r2[3];
+        for (int k = 0; k < 3; ++k) {
+            if (sgm == 0) { /* bound */
+                r0[k] = B[k] - A[k];
+                r1[k] = P[k] - A[k];
+                r2[k] = P[k] - B[k];
+            } else if (sgm == 1) { /* A to infinity */
+                const double inf = A[k] + vinf[k];
+                r2[k] = P[k] - A[k];
+                r1[k] = P[k] - inf;
+                r0[k] = A[k] - inf;
+            } else { /* B to infinity */
+                const double inf = B[k] + vinf[k];
+                r1[k] = P[k] - B[k];
+                r2[k] = P[k] - inf;
+                r0[k] = inf - B[k];
+            }
+        }
+        double u1[3], u2[3], cu[3], c[3];
+        normalized(r1, 3, u1);
+        normalized(r2, 3, u2);
+        if (conditioned) {
+            cross3(u1, u2, cu);
+            if (!(norm(cu, 3) > 1e-12)) return; /* the whole horseshoe is dropped */
+        }
+        cross3(r1, r2, c);
+        const double den = sqnorm(c, 3);
+        double f;
+        if (sgm == 0) {
+            double du[3];
+            for (int k = 0; k < 3; ++k) du[k] = u1[k] - u2[k];
+            f = ipi4 * dot(r0, du, 3) / den;
+        } else if (sgm == 1) {
+            f = ipi4 * norm(r0, 3) * (1.0 - dot(r0, r2, 3) / (norm(r0, 3) * norm(r2, 3))) / den;
+        } else {
+            f = ipi4 * norm(r0, 3) * (dot(r0, r1, 3) / (norm(r1, 3) * norm(r0, 3)) + 1.0) / den;
+        }
+        for (int k = 0; k < 3; ++k) seg[sgm][k] = f * c[k];
+    }
+    for (int k = 0; k < 3; ++k) out[k] = seg[0][k] + seg[2][k] + seg[1][k];
+}
+
+/* VLM::getVelocity (VLM.cpp:119-140) */
+void vlm_velocity(const orc_sim *o, const double *P, double *vel) {
+    for (int k = 0; k < 3; ++k) vel[k] = o->vlm_vinf[k];
+    const size_t np = o->vlm_gamma.size();
+    for (size_t q = 0; q < np; ++q) {
+        double f[3];
+        vlm_influence(&o->vlm_A[3 * q], &o->vlm_B[3 * q], P, o->vlm_vinf, true, f);
+        for (int k = 0; k < 3; ++k) vel[k] += o->vlm_gamma[q] * f[k];
+    }
+    const double n = norm(vel, 3);
+    double u[3];
+    normalized(vel, 3, u);
+    const double m = std::min(n, o->vlm_maxvel);
+    for (int k = 0; k < 3; ++k) vel[k] = u[k] * m;
+}
+
 void get_aero_velocity(orc_sim *o, std::vector<Part> &P) {
     const int D = o->D;
     const fjsph_settings &a = o->s;
@@ -625,7 +704,10 @@ void get_aero_velocity(orc_sim *o, std::vector<Part> &P) {
         else
             on = double(o->outlist[ii].size()) * a.i_n_full < a.lam_cutoff && pi.b == FJSPH_FREE;
         if (on) {
-            for (int k = 0; k < D; ++k) pi.cellV[k] = a.v_inf[k];
+            if (a.asource == FJSPH_VLM_INFL)
+                vlm_velocity(o, pi.xi, pi.cellV);
+            else
+                for (int k = 0; k < D; ++k) pi.cellV[k] = a.v_inf[k];
             pi.cellID = 1;
         } else {
             zero(pi.cellV, D);
@@ -717,8 +799,15 @@ void detect_surface(orc_sim *o, std::vector<Part> &P) {
         Part &pi = P[ii];
         double woccl_ = 0.0;
         double Vdiff[3] = {0, 0, 0};
-        if (pi.cellID != -1 && pi.b == FJSPH_FREE && gissler)
-            for (int k = 0; k < D; ++k) Vdiff[k] = s.v_inf[k] - pi.v[k];
+        if (pi.cellID != -1 && pi.b == FJSPH_FREE && gissler) {
+            if (s.asource == FJSPH_VLM_INFL) { /* Geometry.cpp:158-163 */
+                double vel[3];
+                vlm_velocity(o, pi.xi, vel);
+                for (int k = 0; k < D; ++k) Vdiff[k] = vel[k] - pi.v[k];
+            } else {
+                for (int k = 0; k < D; ++k) Vdiff[k] = s.v_inf[k] - pi.v[k];
+            }
+        }
         double curve = 0.0;
         const double *ni = &norms[3 * ii];
         const double nin = norm(ni, D);
@@ -2026,5 +2115,107 @@ void orc_gradk(const double *Rij, double r, double H, double W_correc, int32_t c
 double orc_min_eig(const double *A, int32_t dim) { return min_eig(A, dim); }
 int32_t orc_qr_inverse(const double *A, int32_t dim, double *inv) { return qr_inverse(A, dim, inv); }
 double orc_get_cd(double Re) { return GetCd(Re); }
+
+/* VLM::Init + MakeMatrix + GetGamma (VLM.cpp:14-117, 180-307) */
+int orc_vlm_setup(orc_sim *o, const fjsph_vlm *v) {
+    if (!v || o->D != 3) return -1;
+    if (v->span <= 0 || v->chord <= 0 || v->panels_span <= 0 || v->panels_chord <= 0) return -1;
+    const double rad = kPi / 180.0;
+    const double sweep = v->sweep_deg * rad, beta = v->flap_deg * rad;
+    const int NS = v->panels_span, NC = v->panels_chord;
+    const double dr0 = v->chord / double(NC), dy0 = v->span / double(NS);
+    std::vector<double> A, B, C;
+    auto add = [&](double ax, double ay, double az, double bx, double by, double bz, double cx, double cy, double cz) {
+        A.insert(A.end(), {ax, ay, az});
+        B.insert(B.end(), {bx, by, bz});
+        C.insert(C.end(), {cx, cy, cz});
+    };
+    for (int i = -NS; i < NS; ++i) {
+        const double y1 = double(i) * dy0, y2 = double(i + 1) * dy0, yh = (double(i) + 0.5) * dy0;
+        const double t = std::tan(sweep);
+        const double fac1 = (1 - std::fabs(y1) / v->span) + v->taper * (std::fabs(y1) / v->span);
+        const double fac2 = (1 - std::fabs(y2) / v->span) + v->taper * (std::fabs(y2) / v->span);
+        const double fac3 = (1 - std::fabs(yh) / v->span) + v->taper * (std::fabs(yh) / v->span);
+        const bool flap = (-i > v->flap_start && -i <= v->flap_width + v->flap_start) ||
+                          (i >= v->flap_start && i < v->flap_width + v->flap_start);
+        const int jend = flap ? NC - v->flap_depth : NC;
+        for (int j = 0; j < jend; ++j)
+            add(t * std::fabs(y1) + dr0 * fac1 * (0.25 + j), y1, 0.0, t * std::fabs(y2) + dr0 * fac2 * (0.25 + j), y2, 0.0,
+                t * std::fabs(yh) + dr0 * fac3 * (0.75 + j), yh, 0.0);
+        if (flap) {
+            const double f0 = double(NC - v->flap_depth);
+            for (int j = 0; j < v->flap_depth; ++j) {
+                auto px = [&](double fac, double y, double w) {
+                    return t * std::fabs(y) + f0 * dr0 * fac + std::cos(beta) * dr0 * fac * w;
+                };
+                auto pz = [&](double fac, double w) { return -std::sin(beta) * dr0 * fac * w; };
+                add(px(fac1, y1, 0.25 + j), y1, pz(fac1, 0.25 + j), px(fac2, y2, 0.25 + j), y2, pz(fac2, 0.25 + j),
+                    px(fac3, yh, 0.75 + j), yh, pz(fac3, 0.75 + j));
+            }
+        }
+    }
+    const int n = int(C.size() / 3);
+    const double *vinf = o->s.v_inf;
+    std::vector<double> nrm(3 * n);
+    for (int p = 0; p < n; ++p) {
+        double ca[3], cb[3], c[3];
+        for (int k = 0; k < 3; ++k) {
+            ca[k] = C[3 * p + k] - A[3 * p + k];
+            cb[k] = C[3 * p + k] - B[3 * p + k];
+        }
+        cross3(ca, cb, c);
+        normalized(c, 3, &nrm[3 * p]);
+    }
+    /* aInf(j, i) = influence of vortex i at control point j, on panel i's normal; RHS(j) = -v . n_j */
+    std::vector<std::vector<double>> M(n, std::vector<double>(n + 1));
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            double f[3];
+            vlm_influence(&A[3 * i], &B[3 * i], &C[3 * j], vinf, false, f);
+            M[j][i] = dot(f, &nrm[3 * i], 3);
+        }
+    for (int j = 0; j < n; ++j) M[j][n] = -dot(vinf, &nrm[3 * j], 3);
+    /* Gauss-Jordan elimination with partial pivoting on the augmented matrix */
+    for (int k = 0; k < n; ++k) {
+        int best = k;
+        for (int r = k + 1; r < n; ++r)
+            if (std::fabs(M[r][k]) > std::fabs(M[best][k])) best = r;
+        if (M[best][k] == 0.0) return -2;
+        std::swap(M[k], M[best]);
+        for (int r = 0; r < n; ++r) {
+            if (r == k || M[r][k] == 0.0) continue;
+            const double l = M[r][k] / M[k][k];
+            for (int c2 = k; c2 <= n; ++c2) M[r][c2] -= l * M[k][c2];
+        }
+    }
+    o->vlm_gamma.resize(n);
+    for (int k = 0; k < n; ++k) o->vlm_gamma[k] = M[k][n] / M[k][k];
+    o->vlm_A = A;
+    o->vlm_B = B;
+    o->vlm_C = C;
+    for (int k = 0; k < 3; ++k) o->vlm_vinf[k] = vinf[k];
+    o->vlm_maxvel = (v->max_vel == 2.0) ? v->max_vel_fac * norm(vinf, 3) : v->max_vel;
+    o->vlm_ready = true;
+    return n;
+}
+
+int orc_vlm_panels(orc_sim *o, double *gamma, double *abc) {
+    const int n = int(o->vlm_gamma.size());
+    for (int p = 0; p < n; ++p) {
+        if (gamma) gamma[p] = o->vlm_gamma[p];
+        if (abc)
+            for (int k = 0; k < 3; ++k) {
+                abc[9 * p + k] = o->vlm_A[3 * p + k];
+                abc[9 * p + 3 + k] = o->vlm_B[3 * p + k];
+                abc[9 * p + 6 + k] = o->vlm_C[3 * p + k];
+            }
+    }
+    return n;
+}
+
+void orc_vlm_velocity(orc_sim *o, int64_t n, const double *pos, double *vel) {
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; ++i) vlm_velocity(o, &pos[3 * i], &vel[3 * i]);
+}
 
 } /* extern "C" */

@@ -63,6 +63,11 @@ void orc_gradk(const double *Rij, double r, double H, double W_correc, int32_t c
 double orc_min_eig(const double *A, int32_t dim);
 int32_t orc_qr_inverse(const double *A, int32_t dim, double *inv);
 double orc_get_cd(double Re);
+/* vortex-lattice air source (VLM.cpp): setup returns the panel count (< 0 on a bad wing or a
+ * singular influence matrix) */
+int orc_vlm_setup(orc_sim *o, const fjsph_vlm *v);
+int orc_vlm_panels(orc_sim *o, double *gamma, double *abc);
+void orc_vlm_velocity(orc_sim *o, int64_t n, const double *pos, double *vel);
 
 #ifdef __cplusplus
 }

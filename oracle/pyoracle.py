@@ -60,6 +60,9 @@ _PROTO = {
     "orc_min_eig": (C.c_double, [_dp, C.c_int32]),
     "orc_qr_inverse": (C.c_int32, [_dp, C.c_int32, _dp]),
     "orc_get_cd": (C.c_double, [C.c_double]),
+    "orc_vlm_setup": (C.c_int, [_P, C.c_void_p]),
+    "orc_vlm_panels": (C.c_int, [_P, _dp, _dp]),
+    "orc_vlm_velocity": (None, [_P, C.c_int64, _dp, _dp]),
 }
 
 
@@ -152,6 +155,26 @@ class Oracle:
 
     def dSPH_PreStep(self) -> float:
         return self._l.orc_dsph_prestep(self._h)
+
+    def vlm_setup(self, vlm) -> int:
+        """VLM::Init + GetGamma for the settings' v_inf (vlm: fjsph_gb300._cdefs.Vlm)."""
+        n = lib().orc_vlm_setup(self._h, C.byref(vlm))
+        if n < 0:
+            raise RuntimeError(f"orc_vlm_setup failed ({n})")
+        return n
+
+    def vlm_panels(self):
+        n = lib().orc_vlm_panels(self._h, None, None)
+        g = np.zeros(n)
+        abc = np.zeros((n, 3, 3))
+        lib().orc_vlm_panels(self._h, g.ctypes.data_as(_dp), abc.ctypes.data_as(_dp))
+        return g, abc
+
+    def vlm_velocity(self, pos):
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros_like(p)
+        lib().orc_vlm_velocity(self._h, p.shape[0], p.ctypes.data_as(_dp), out.ctypes.data_as(_dp))
+        return out
 
     def get_aero_velocity(self):
         self._l.orc_get_aero_velocity(self._h)
