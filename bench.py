@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the plain FP64 form timed beside (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--vlm-points", type=int, default=1 << 20, help="points of the VLM air-source timing (0 = skip)")
     ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--closure", default="learned", choices=["learned", "plain"])
@@ -209,6 +210,57 @@ def timed_steps(ctx, steps: int, ws: int) -> float:
         ctx.integrate()
     ctx.event_record(1)
     return reduce_max(ws, ctx.event_elapsed(0, 1))
+
+
+# Examples/VLM: a 22.3 m half-span, 8.5 m chord wing, sweep 32.5 deg, taper 0.6, 20 deg flap
+VLM_WING = dict(span=22.275, chord=8.491, panels_span=50, panels_chord=14, aoa_deg=5.0, sweep_deg=32.5, taper=0.6,
+                flap_start=3, flap_width=24, flap_depth=6, flap_deg=20.0)
+VLM_VINF = (89.69, 0.0, 7.8466)
+
+
+def run_vlm(args):
+    """Vortex-lattice air source (the Examples/VLM wing, 1400 horseshoes) evaluated at seeded points
+    around the wing: the split-precision form at args.vlm_points points, the FP64 form at 1/16 of
+    them; kernel time from the air_source profile section, setup (panels, influence matrix, LU)
+    on the host timed beside it."""
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d, cases
+    from fjsph_gb300._lib import lib
+    from fjsph_gb300.api import Context
+    c = cases.droplet_3d(diam=6e-4, dx=1e-4)
+    rng = np.random.Generator(np.random.PCG64(5))
+    n = args.vlm_points
+    pts = np.column_stack([rng.uniform(-10, 40, n), rng.uniform(-30, 30, n), rng.uniform(-6, 6, n)])
+    out = {"wing": "Examples/VLM (50 x 14 panels per side, sweep 32.5 deg, taper 0.6, 20 deg flap)",
+           "points": "uniform in [-10, 40] x [-30, 30] x [-6, 6] m around the wing"}
+    for form, prec, m in (("fp32", d.PREC_MIXED, n), ("fp64", d.PREC_FP64, max(n // 16, 1024))):
+        s = c.settings.copy()
+        for k in range(3):
+            s.v_inf[k] = VLM_VINF[k]
+        s.asource = d.VLM_INFL
+        s.precision = prec
+        ctx = Context(s, c.state.n + 64, c.blocks, c.inlets)
+        ctx.set_states(c.state, c.state)
+        v = d.Vlm()
+        lib().fjsph_vlm_defaults(v)
+        for k, val in VLM_WING.items():
+            setattr(v, k, val)
+        t0 = time.perf_counter()
+        npan = ctx.vlm_setup(v)
+        setup_s = time.perf_counter() - t0
+        p = pts[:m]
+        ctx.vlm_velocity(p[:4096])
+        ctx.profile(True)
+        ctx.profile_read()
+        reps = 3
+        for _ in range(reps):
+            ctx.vlm_velocity(p)
+        ms = ctx.profile_read()["air_source"][0] / reps
+        ctx.profile(False)
+        out[form] = {"points": m, "panels": npan, "kernel_ms": round(ms, 4), "evaluations_per_s": m / (ms / 1e3),
+                     "panel_interactions_per_s": m * npan / (ms / 1e3), "setup_s": round(setup_s, 3)}
+        ctx.close()
+    return out
 
 
 def run_droplets(args, ws, rank, weights):
@@ -524,6 +576,7 @@ def main():
         dist.init_process_group("nccl")
     r = run_ours(args, ws, rank, local)
     drops = run_droplets(args, ws, rank, r["weights"]) if args.drops > 0 else None
+    vlm = run_vlm(args) if (args.vlm_points > 0 and rank == 0) else None
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -542,6 +595,7 @@ def main():
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
                 "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"], "closure": r["closure"],
                 "neighbour_pairs": r["pairs"], "autotune": r["tune"], "droplet_batch": drops,
+                "vlm_air_source": vlm,
                 "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
                 "gpu_launches": r["launches"], "passes_ms": r["prof"]}
         print(json.dumps(line))

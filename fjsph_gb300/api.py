@@ -291,7 +291,7 @@ class Context:
 
     def profile_read(self) -> dict:
         """{pass name: (milliseconds, section count)} accumulated since the last read."""
-        npass = 12
+        npass = 13
         ms = (C.c_double * npass)()
         cnt = (C.c_int64 * npass)()
         check("fjsph_profile_read", self._lib.fjsph_profile_read(self._h, ms, cnt))

@@ -60,12 +60,14 @@ enum Pass {
     PASS_REDUCE,
     PASS_COPY,
     PASS_TRANSFER,
+    PASS_AIR,
     PASS_COUNT
 };
 static_assert(PASS_COUNT == FJSPH_NPASS, "pass table");
 const char *kPassNames[PASS_COUNT] = {"neighbour_search", "reorder", "dsph_prestep", "detect_surface",
                                       "dissipation", "particle_shift", "boundary", "residual",
-                                      "stage_update", "reductions", "state_copy", "host_transfer"};
+                                      "stage_update", "reductions", "state_copy", "host_transfer",
+                                      "air_source"};
 
 struct Profiler {
     bool on = false;
@@ -913,6 +915,7 @@ int npd_only(fjsph_ctx *c, const Params &P) {
 int vlm_air(fjsph_ctx *c, const Params &P, const DevNbr &N) {
     if (c->s.asource != FJSPH_VLM_INFL) return FJSPH_OK;
     if (c->vlm.np == 0) return FJSPH_E_STATE; /* fjsph_vlm_setup has not run */
+    Section sec(c, PASS_AIR);
     launch_vlm_air(P, WS(c), N, c->vlm, c->air_v, mixed(c), c->stream);
     c->launches++;
     return FJSPH_OK;
@@ -925,11 +928,11 @@ int prestep_passes(fjsph_ctx *c) {
     cudaStream_t s = c->stream;
     TRY(prestep_npd(c, P));
     const bool dissipation = !(c->s.variant & FJSPH_VAR_NOFROZEN);
+    TRY(vlm_air(c, P, N)); /* position-dependent air velocity, its own section */
     {
         /* split-precision form: the dissipation terms are computed in the surface-normal walk
          * (they read nothing the surface passes write), timed with the surface section */
         Section sec(c, PASS_SURFACE);
-        TRY(vlm_air(c, P, N));
         launch_aero_velocity(P, WS(c), N, s);
         if (mixed(c)) {
             launch_m_surface(P, WS(c), N, c->K, dissipation, s);
@@ -2761,7 +2764,10 @@ int fjsph_vlm_velocity(fjsph_ctx *c, int64_t n, const double *pos, double *vel) 
     int rc = FJSPH_OK;
     if (cudaMemcpy(d, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) rc = FJSPH_E_CUDA;
     if (rc == FJSPH_OK) {
-        launch_vlm_points(c->vlm, n, d, d + 3 * n, mixed(c), c->stream);
+        {
+            Section sec(c, PASS_AIR);
+            launch_vlm_points(c->vlm, n, d, d + 3 * n, mixed(c), c->stream);
+        }
         if (cudaStreamSynchronize(c->stream) != cudaSuccess ||
             cudaMemcpy(vel, d + 3 * n, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
             rc = FJSPH_E_CUDA;

@@ -242,42 +242,41 @@ __device__ __forceinline__ void horseshoe_add(R3<R> A, R3<R> B, R3<R> P, R3<R> v
     acc.z += g * s.z;
 }
 
-/* The horseshoe of the FP32 form from the separations P - A and P - B, each formed as
+/* The horseshoe of the FP32 form from the separations a = P - A and b = P - B, each formed as
  * (P_hi - A_hi) + (P_lo - A_lo) so that it is accurate to FP32 rounding of itself, not of the
  * coordinates (a point near the lattice sits metres from the origin but millimetres from a
- * vortex); the other vectors follow: P - (A + v_inf) = (P - A) - v_inf, A - (A + v_inf) = -v_inf. */
-__device__ __forceinline__ void horseshoe_add_f32(R3<float> rpa, R3<float> rpb, R3<float> ab, R3<float> vinf,
-                                                  float vn, float g, R3<float> &acc) {
-    const float ipi4 = (float)(0.25 / M_PI);
-    if (!seg_ok(rpa, rpb)) return;
-    R3<float> c = cr(rpa, rpb);
-    const float fab = ipi4 * dt(ab, sub(nrmz(rpa), nrmz(rpb))) / dt(c, c);
-    R3<float> s{fab * c.x, fab * c.y, fab * c.z};
-    R3<float> r1 = sub(rpa, vinf); /* leg from A: r1 = P - (A + v), r2 = P - A, r0 = -v */
-    if (!seg_ok(r1, rpa)) return;
-    c = cr(r1, rpa);
-    const float fa = ipi4 * vn * (1.f + dt(vinf, rpa) / (vn * sqrtf(dt(rpa, rpa)))) / dt(c, c);
-    s.x += fa * c.x;
-    s.y += fa * c.y;
-    s.z += fa * c.z;
-    const R3<float> r2 = sub(rpb, vinf); /* leg from B: r1 = P - B, r2 = P - (B + v), r0 = v */
-    if (!seg_ok(rpb, r2)) return;
-    c = cr(rpb, r2);
-    const float fb = ipi4 * vn * (dt(vinf, rpb) / (sqrtf(dt(rpb, rpb)) * vn) + 1.f) / dt(c, c);
-    s.x += fb * c.x;
-    s.y += fb * c.y;
-    s.z += fb * c.z;
-    acc.x += g * s.x;
-    acc.y += g * s.y;
-    acc.z += g * s.z;
+ * vortex).  With the legs' vectors P - (A + v) = a - v and P - (B + v) = b - v, the three cross
+ * products are a x b, (a - v) x a = a x v and b x (b - v) = v x b, and the reference's factors
+ * reduce to (bound) (B - A) . (a/|a| - b/|b|), (leg A) |v| + v . a/|a|, (leg B) |v| + v . b/|b|,
+ * each over the squared cross product and times 1/(4 pi).  A segment drops the horseshoe when
+ * |u1 x u2| <= 1e-12 for the unit vectors of its two separations, tested as
+ * |r1 x r2|^2 <= 1e-24 |r1|^2 |r2|^2. */
+__device__ __forceinline__ void horseshoe_add_f32(R3<float> a, R3<float> b, R3<float> v, float vn, float g,
+                                                  R3<float> &acc) {
+    const float a2 = dt(a, a), b2 = dt(b, b);
+    const R3<float> cab = cr(a, b), cav = cr(a, v), cvb = cr(v, b);
+    const float nab = dt(cab, cab), nav = dt(cav, cav), nvb = dt(cvb, cvb);
+    const R3<float> av = sub(a, v), bv = sub(b, v);
+    if (!(nab > 1e-24f * a2 * b2) || !(nav > 1e-24f * dt(av, av) * a2) || !(nvb > 1e-24f * b2 * dt(bv, bv))) return;
+    const float ia = rsqrtf(a2), ib = rsqrtf(b2);
+    const R3<float> ab = sub(a, b); /* B - A */
+    const float ipi4g = (float)(0.25 / M_PI) * g;
+    const float fab = ipi4g * (dt(ab, a) * ia - dt(ab, b) * ib) / nab;
+    const float fa = ipi4g * (vn + dt(v, a) * ia) / nav;
+    const float fb = ipi4g * (vn + dt(v, b) * ib) / nvb;
+    acc.x += fab * cab.x + fa * cav.x + fb * cvb.x;
+    acc.y += fab * cab.y + fa * cav.y + fb * cvb.y;
+    acc.z += fab * cab.z + fa * cav.z + fb * cvb.z;
 }
 
 /* Induced velocity at P summed over all panels (every thread of the block calls: the panels
  * pass through shared memory kVT at a time), then v = v_inf + induced limited to max_vel. */
 template <typename R>
 __device__ void vlm_velocity(const VlmDev &V, bool need, const double *p, double *out) {
-    constexpr int kW = sizeof(R) == 4 ? 13 : 7; /* FP32: A, B as high/low, B - A, gamma */
-    __shared__ R sp[kVT][kW];
+    /* shared-memory panel records: FP64 form A, B, gamma; FP32 form (A_hi, gamma), (A_lo, 0),
+     * (B_hi, 0), (B_lo, 0) as float4 (one broadcast 16-byte read each) */
+    __shared__ double sd[sizeof(R) == 8 ? kVT : 1][7];
+    __shared__ float4 sf[sizeof(R) == 4 ? kVT : 1][4];
     R3<R> acc{R(0), R(0), R(0)};
     const R3<R> vinf{(R)V.vinf[0], (R)V.vinf[1], (R)V.vinf[2]};
     R3<R> P{(R)p[0], (R)p[1], (R)p[2]}, Pl{R(0), R(0), R(0)};
@@ -292,13 +291,15 @@ __device__ void vlm_velocity(const VlmDev &V, bool need, const double *p, double
         __syncthreads();
         if (q < V.np) {
             if constexpr (sizeof(R) == 4) { /* FP32 copies made on the host */
-#pragma unroll
-                for (int k = 0; k < 12; ++k) sp[threadIdx.x][k] = V.abf[12 * (int64_t)q + k];
-                sp[threadIdx.x][12] = V.gammaf[q];
+                const float *w = V.abf + 12 * (int64_t)q;
+                sf[threadIdx.x][0] = make_float4(w[0], w[1], w[2], V.gammaf[q]);
+                sf[threadIdx.x][1] = make_float4(w[3], w[4], w[5], 0.f);
+                sf[threadIdx.x][2] = make_float4(w[6], w[7], w[8], 0.f);
+                sf[threadIdx.x][3] = make_float4(w[9], w[10], w[11], 0.f);
             } else {
 #pragma unroll
-                for (int k = 0; k < 6; ++k) sp[threadIdx.x][k] = V.ab[6 * (int64_t)q + k];
-                sp[threadIdx.x][6] = V.gamma[q];
+                for (int k = 0; k < 6; ++k) sd[threadIdx.x][k] = V.ab[6 * (int64_t)q + k];
+                sd[threadIdx.x][6] = V.gamma[q];
             }
         }
         __syncthreads();
@@ -306,16 +307,15 @@ __device__ void vlm_velocity(const VlmDev &V, bool need, const double *p, double
         if (need)
             for (int t = 0; t < m; ++t) {
                 if constexpr (sizeof(R) == 4) {
-                    const float *w = sp[t];
-                    const R3<float> rpa{(P.x - w[0]) + (Pl.x - w[3]), (P.y - w[1]) + (Pl.y - w[4]),
-                                        (P.z - w[2]) + (Pl.z - w[5])};
-                    const R3<float> rpb{(P.x - w[6]) + (Pl.x - w[9]), (P.y - w[7]) + (Pl.y - w[10]),
-                                        (P.z - w[8]) + (Pl.z - w[11])};
-                    /* B - A from the separations: (P - A) - (P - B) */
-                    horseshoe_add_f32(rpa, rpb, sub(rpa, rpb), vinf, vn, w[12], acc);
+                    const float4 ah = sf[t][0], al = sf[t][1], bh = sf[t][2], bl = sf[t][3];
+                    const R3<float> rpa{(P.x - ah.x) + (Pl.x - al.x), (P.y - ah.y) + (Pl.y - al.y),
+                                        (P.z - ah.z) + (Pl.z - al.z)};
+                    const R3<float> rpb{(P.x - bh.x) + (Pl.x - bl.x), (P.y - bh.y) + (Pl.y - bl.y),
+                                        (P.z - bh.z) + (Pl.z - bl.z)};
+                    horseshoe_add_f32(rpa, rpb, vinf, vn, ah.w, acc);
                 } else {
-                    const R3<R> A{sp[t][0], sp[t][1], sp[t][2]}, B{sp[t][3], sp[t][4], sp[t][5]};
-                    horseshoe_add<R>(A, B, P, vinf, sp[t][6], acc);
+                    const R3<R> A{sd[t][0], sd[t][1], sd[t][2]}, B{sd[t][3], sd[t][4], sd[t][5]};
+                    horseshoe_add<R>(A, B, P, vinf, sd[t][6], acc);
                 }
             }
     }

@@ -397,7 +397,7 @@ int fjsph_event_elapsed(fjsph_ctx *ctx, int32_t slot_a, int32_t slot_b, double *
 /* Per-pass device time: when enabled, every pass of the step is bracketed by events.
  * fjsph_profile_read fills ms[FJSPH_NPASS] and launches[FJSPH_NPASS] accumulated since the last
  * read (and clears them); fjsph_profile_pass_name names pass k. */
-#define FJSPH_NPASS 12
+#define FJSPH_NPASS 13
 int fjsph_profile_enable(fjsph_ctx *ctx, int32_t on);
 int fjsph_profile_read(fjsph_ctx *ctx, double *ms, int64_t *launches);
 const char *fjsph_profile_pass_name(int32_t k);
