@@ -88,6 +88,8 @@ PROTOTYPES = {
     "fjsph_vlm_setup": (C.c_int, [_P, C.POINTER(d.Vlm), _i32p]),
     "fjsph_vlm_panels": (C.c_int, [_P, _dp, _dp, _i32p]),
     "fjsph_vlm_velocity": (C.c_int, [_P, _i64, _dp, _dp]),
+    "fjsph_restart_write": (C.c_int, [_P, C.c_char_p, _i64]),
+    "fjsph_restart_read": (C.c_int, [_P, C.c_char_p, _i64p]),
     "fjsph_find_timestep_noalloc": (C.c_int, [C.POINTER(d.Settings), _i64, C.POINTER(_dp), C.POINTER(_dp), _dp, _dp,
                                               _dp, C.POINTER(_dp), C.POINTER(_dp), _P, _dp, _dp]),
 }

@@ -342,6 +342,16 @@ class Context:
     def closure_reset(self) -> None:
         check("fjsph_closure_reset", self._lib.fjsph_closure_reset(self._h))
 
+    # ---- restart files (src/H5IO.cpp) ----
+    def restart_write(self, path: str, current_frame: int = 0) -> None:
+        check("fjsph_restart_write", self._lib.fjsph_restart_write(self._h, str(path).encode(), int(current_frame)))
+
+    def restart_read(self, path: str) -> int:
+        """Load a restart file into pn and pnp1; returns the stored frame."""
+        f = C.c_int64(0)
+        check("fjsph_restart_read", self._lib.fjsph_restart_read(self._h, str(path).encode(), C.byref(f)))
+        return f.value
+
     # ---- vortex-lattice air source (src/VLM.h) ----
     def vlm_setup(self, vlm: "d.Vlm") -> int:
         """VLM::Init + GetGamma for the context's v_inf; returns the panel count."""

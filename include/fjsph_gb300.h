@@ -381,6 +381,15 @@ int fjsph_vlm_panels(fjsph_ctx *ctx, double *gamma, double *abc, int32_t *npanel
  * the context's precision (FP64, or FP32 sums for the split-precision form). */
 int fjsph_vlm_velocity(fjsph_ctx *ctx, int64_t n, const double *pos, double *vel);
 
+/* ---- restart files (src/H5IO.cpp:395-523, 1027-1060, 1092-1318) ---------------------------- */
+/* Write_HDF5 / Read_HDF5 content with the reference's group, dataset and attribute names in a
+ * self-describing binary container (no HDF5 library here; the layout is documented in
+ * fjsph_gb300/csrc/restart.cpp).  write: pnp1 and the integrator scalars; read: the file's
+ * particles become pn and pnp1 (the block layout must be the context's), the current time, CFL
+ * and CFL counters are restored, *current_frame receives the frame (may be null). */
+int fjsph_restart_write(fjsph_ctx *ctx, const char *path, int64_t current_frame);
+int fjsph_restart_read(fjsph_ctx *ctx, const char *path, int64_t *current_frame);
+
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
 int fjsph_step_report(fjsph_ctx *ctx, double *out5);
