@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "kernels.h"
@@ -612,13 +613,16 @@ void dev_ptrs(const DevState &S, int D, std::vector<std::vector<void *>> &ptr, s
 /* Host <-> device state transfer, field by field through two staging buffers: the copy of one
  * field (copy stream) overlaps the reference-order gather / scatter of the previous one (context
  * stream); events order the reuse of each buffer. */
-int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up) {
+/* Host <-> device copy of a state view through two staging buffers.  mirror (upload only):
+ * a second state that receives each field by a device copy right after it arrives. */
+int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up, DevState *mirror = nullptr) {
     Section sec(c, PASS_TRANSFER);
     std::vector<void *> hp;
     view_ptrs(v, hp);
-    std::vector<std::vector<void *>> dp;
-    std::vector<int> type;
+    std::vector<std::vector<void *>> dp, dp2;
+    std::vector<int> type, type2;
     dev_ptrs(S, c->D, dp, type);
+    if (mirror) dev_ptrs(*mirror, c->D, dp2, type2);
     const int64_t n = c->n;
     for (void *p : hp)
         if (!p) return FJSPH_E_ARG;
@@ -644,6 +648,9 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up) {
             CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
             launch_field_in(stage[b], comps, es, c->key, fp, n, c->stream);
             CU(cudaEventRecord(c->st_used[b], c->stream));
+            if (mirror)
+                for (int k = 0; k < comps; ++k)
+                    CU(cudaMemcpyAsync(dp2[f][k], dp[f][k], (size_t)es * n, cudaMemcpyDeviceToDevice, c->stream));
         } else {
             if (f >= 2) CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
             launch_field_out(stage[b], comps, es, c->key, fp, n, c->stream);
@@ -1945,16 +1952,23 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         TRY(upload_inlets(c, keys));
         c->reorder_pending = true;
     }
-    TRY(transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true));
-    if (which == FJSPH_BOTH) { /* pn = pnp1 = the uploaded state: one transfer, a device copy */
-        launch_copy(state_fields(WS(c), c->D), state_fields(PN(c), c->D), c->n, c->stream);
-        c->launches++;
-    }
+    /* ids of inserted particles continue from the largest uploaded one: a host scan of the
+     * ids, run on a second thread while the fields transfer */
+    int64_t id_next = 0;
+    std::thread ids;
+    if (which != FJSPH_PN && st->part_id)
+        ids = std::thread([&id_next, st] {
+            int64_t m = 0;
+            for (int64_t i = 0; i < st->n; ++i) m = std::max<int64_t>(m, st->part_id[i] + 1);
+            id_next = m;
+        });
+    /* FJSPH_BOTH: pn = pnp1 = the uploaded state: one host transfer, each field copied on the
+     * device as it arrives */
+    const int rc_t = transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true, which == FJSPH_BOTH ? &PN(c) : nullptr);
+    if (ids.joinable()) ids.join();
+    TRY(rc_t);
     if (grouped(c)) TRY(upload_groups(c));
-    if (which != FJSPH_PN && st->part_id) { /* ids of inserted particles continue from here */
-        c->part_id_next = 0;
-        for (int64_t i = 0; i < st->n; ++i) c->part_id_next = std::max<int64_t>(c->part_id_next, st->part_id[i] + 1);
-    }
+    if (which != FJSPH_PN && st->part_id) c->part_id_next = id_next;
     if (which != FJSPH_PN) {
         c->nbr_valid = false;
         mark_full(c);
