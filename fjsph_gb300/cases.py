@@ -115,6 +115,102 @@ def dam_break_2d(dx: float = 0.01, column=(1.0, 2.0), tank=(4.0, 3.0), layers: i
     return Case("dam_break_2d", s, st, _blocks(len(bound), st.n))
 
 
+def _line_wall(start, end, dx: float, layers: int) -> np.ndarray:
+    """A Line block (src/shapes/line.cpp, grid ordering, 2D): ceil(|end - start| / dx) points
+    along the line from start, `layers` rows offset along (dy, -dx) of the line direction."""
+    start, end = np.asarray(start, float), np.asarray(end, float)
+    delta = (end - start) / np.linalg.norm(end - start) * dx
+    norm = np.array([delta[1], -delta[0]])
+    ni = max(int(math.ceil(np.linalg.norm(end - start) / dx)), 1)
+    ii, kk = np.meshgrid(np.arange(ni), np.arange(layers), indexing="ij")
+    return start + ii.ravel()[:, None] * delta + kk.ravel()[:, None] * norm
+
+
+def _square(start, end, dx: float) -> np.ndarray:
+    """A Square block (src/shapes/square.cpp, grid ordering, 2D): ceil(extent / dx) points per
+    axis from start, x fastest."""
+    start, end = np.asarray(start, float), np.asarray(end, float)
+    ni, nj = (max(int(math.ceil((end[k] - start[k]) / dx)), 1) for k in range(2))
+    jj, ii = np.meshgrid(np.arange(nj), np.arange(ni), indexing="ij")
+    return start + np.stack([ii.ravel(), jj.ravel()], axis=1) * dx
+
+
+def standing_column_2d(dx: float = 0.02, width: float = 0.5, height: float = 1.0, layers: int = 4,
+                       cfl: float = 1.0) -> Case:
+    """Examples/Standing_Column's layout and settings at a coarser spacing: a water column at rest
+    between Line walls (left, bottom, right; Pressure-Gradient), hydrostatic initial pressure
+    (src/Init.cpp:480-493), smoothing length factor 2, artificial viscosity 0.1, no surface
+    tension, the default Newmark-Beta integrator (src/Integration.h:52).  The reference compares
+    p / (rho g H) against depth / H (Ideal.dat: the line through (0, 0) and (1, 1)).  The speed
+    of sound is ten times the column's free-fall speed."""
+    s = defaults(2)
+    s.st_model = d.ST_NOST
+    s.particle_step = dx
+    s.H_fac = 2.0
+    s.rho_rest = 1000.0
+    s.mu = 8.94e-4
+    s.gam = 7.0
+    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * height)
+    s.visc_alpha = 0.1
+    s.sig = 0.0
+    s.grav[:] = [0.0, -9.81, 0.0]
+    s.solver_type = d.NEWMARK_BETA
+    s.cfl = s.cfl_max = cfl
+    s.cfl_min = 0.1 * cfl
+    s.delta_t_min = 1e-9
+    derive(s)
+    top = height + 0.1
+    walls = [_line_wall((0.0, top), (0.0, 0.0), dx, layers),             # left, layers towards -x
+             _line_wall((-(layers - 1) * dx, 0.0), (width + (layers - 1) * dx, 0.0), dx, layers),  # bottom
+             _line_wall((width + dx, 0.0), (width + dx, top), dx, layers)]  # right, layers towards +x
+    fluid = _square((dx, dx), (width + 0.5 * dx, height), dx)
+    bound = np.concatenate(walls)
+    keep = np.ones(len(bound), bool)  # drop wall points that coincide (corner overlaps)
+    _, first = np.unique(np.round(bound / (0.1 * dx)).astype(np.int64), axis=0, return_index=True)
+    keep[:] = False
+    keep[np.sort(first)] = True
+    bound = bound[keep]
+    st = _assemble(s, bound, fluid)
+    _hydrostatic(s, st, 1, height + 0.5 * dx)
+    return Case("standing_column_2d", s, st, _blocks(len(bound), st.n))
+
+
+def couette_2d(dx: float = 0.02, length: float = 3.0, gap: float = 1.0, wall_speed: float = 1e-3,
+               layers: int = 4, cfl: float = 1.0) -> Case:
+    """Examples/Couette's layout: fluid between a fixed bottom wall and a top wall moving at
+    wall_speed along x (Line blocks, Pressure-Gradient, no-slip off), rho = 1, mu = 0.01, c = 1,
+    no gravity.  The steady profile is v_x = wall_speed * y / gap (SteadyState.dat)."""
+    s = defaults(2)
+    s.st_model = d.ST_NOST
+    s.particle_step = dx
+    s.H_fac = 2.0
+    s.rho_rest = 1.0
+    s.mu = 1e-2
+    s.gam = 7.0
+    s.speed_sound = 1.0
+    s.visc_alpha = 0.01
+    s.sig = 0.0
+    s.rho_var = 20.0
+    s.grav[:] = [0.0, 0.0, 0.0]
+    s.solver_type = d.RUNGE_KUTTA
+    s.cfl = s.cfl_min = s.cfl_max = cfl
+    s.delta_t_min = 1e-9
+    s.delta_t_max = 0.5
+    derive(s)
+    bottom = _line_wall((-0.18, 0.0), (length + 0.2, 0.0), dx, layers)
+    top = _line_wall((length + 0.2, gap), (-0.2, gap), dx, layers)
+    fluid = _square((0.0, dx), (length, gap), dx)
+    bound = np.concatenate([bottom, top])
+    st = _assemble(s, bound, fluid)
+    nb0 = len(bottom)
+    blocks = [BlockSpec(0, nb0, False, name="Bottom", bound_solver=d.PRESSURE_G),
+              BlockSpec(nb0, len(bound), False, name="Top", bound_solver=d.PRESSURE_G,
+                        vels=[(wall_speed, 0.0, 0.0)]),
+              BlockSpec(len(bound), st.n, True, name="Fluid")]
+    st.v[nb0:len(bound), 0] = wall_speed
+    return Case("couette_2d", s, st, blocks)
+
+
 def dam_break_3d(dx: float = 0.003, column=(0.6, 0.6, 1.2), tank=(1.6, 0.6, 1.2), layers: int = 3,
                  jitter: float = 0.01, seed: int = 12345, ale: bool = True, solver: int = d.RUNGE_KUTTA,
                  cfl: float = 0.2) -> Case:

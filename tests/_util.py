@@ -53,3 +53,16 @@ def assert_ints(a: SPHState, b: SPHState, fields, sl=slice(None), max_frac=0.0, 
 
 def n_bound(blocks) -> int:
     return sum(b.second - b.first for b in blocks if not b.is_fluid)
+
+
+def hydrostatic_error(st: SPHState, fluid_from: int, rho_rest: float, top: float, g: float = 9.81) -> float:
+    """RMS over depth bins of p / (rho g H) - depth / H (Examples/Standing_Column/Ideal.dat is the
+    line through (0, 0) and (1, 1)); bins away from the free surface and the floor."""
+    y, p = st.xi[fluid_from:, 1], st.p[fluid_from:]
+    depth = (top - y) / top
+    pn = p / (rho_rest * g * top)
+    bins = np.linspace(0.1, 0.95, 12)
+    idx = np.digitize(depth, bins)
+    err = [np.mean(pn[idx == k]) - np.mean(depth[idx == k])
+           for k in range(1, len(bins)) if np.count_nonzero(idx == k) > 10]
+    return float(np.sqrt(np.mean(np.square(err))))
