@@ -113,3 +113,15 @@ class Vlm(C.Structure):
     _fields_ = [("span", _d), ("chord", _d), ("panels_span", _i32), ("panels_chord", _i32), ("aoa_deg", _d),
                 ("sweep_deg", _d), ("taper", _d), ("flap_start", _i32), ("flap_width", _i32),
                 ("flap_depth", _i32), ("pad", _i32), ("flap_deg", _d), ("max_vel_fac", _d), ("max_vel", _d)]
+
+
+class GeometryBlock(C.Structure):
+    """fjsph_geometry_block: one block of the initial-particle generator after check_input."""
+    _fields_ = [("name", C.c_char * 64), ("is_fluid", _i32), ("shape", _i32), ("sub_shape", _i32),
+                ("particle_order", _i32), ("write_data", _i32), ("ni", _i32), ("nj", _i32), ("nk", _i32),
+                ("estimated", _i64), ("generated", _i64), ("kept", _i64), ("radius", _d),
+                ("start", _d * 3), ("end", _d * 3), ("right", _d * 3), ("centre", _d * 3), ("normal", _d * 3)]
+
+
+# shape_type (src/VarDefs.h:116-127)
+LINE_PLANE, SQUARE_CUBE, CIRCLE_SPHERE, CYLINDER, ARC_SECTION, COORD_DEF, INLET_ZONE, HOLLOW, SOLID = range(9)

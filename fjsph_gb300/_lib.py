@@ -90,6 +90,17 @@ PROTOTYPES = {
     "fjsph_vlm_velocity": (C.c_int, [_P, _i64, _dp, _dp]),
     "fjsph_restart_write": (C.c_int, [_P, C.c_char_p, _i64]),
     "fjsph_restart_read": (C.c_int, [_P, C.c_char_p, _i64p]),
+    "fjsph_geometry_create": (C.c_int, [C.POINTER(d.Settings), _pp]),
+    "fjsph_geometry_destroy": (C.c_int, [_P]),
+    "fjsph_geometry_read": (C.c_int, [_P, C.c_char_p, _i32]),
+    "fjsph_geometry_read_file": (C.c_int, [_P, C.c_char_p, _i32]),
+    "fjsph_geometry_build": (C.c_int, [_P]),
+    "fjsph_geometry_sizes": (C.c_int, [_P, _i64p, _i64p, _i32p, _i32p, _i32p]),
+    "fjsph_geometry_state": (C.c_int, [_P, C.POINTER(d.StateView)]),
+    "fjsph_geometry_blocks": (C.c_int, [_P, C.POINTER(d.Block), _i32]),
+    "fjsph_geometry_block_info": (C.c_int, [_P, _i32, C.POINTER(d.GeometryBlock)]),
+    "fjsph_geometry_inlet": (C.c_int, [_P, _i32, C.POINTER(d.Inlet)]),
+    "fjsph_geometry_log": (C.c_int, [_P, C.c_char_p, _i64, _i64p]),
     "fjsph_find_timestep_noalloc": (C.c_int, [C.POINTER(d.Settings), _i64, C.POINTER(_dp), C.POINTER(_dp), _dp, _dp,
                                               _dp, C.POINTER(_dp), C.POINTER(_dp), _P, _dp, _dp]),
 }

@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libfjsph_gb300.so"
 
-SOURCES = ["capi.cu", "neighbours.cu", "sweeps.cu", "integrate.cu", "state.cu", "settings.cpp", "noalloc.cu", "sweeps_mixed.cu", "mlp_train.cu", "update.cu", "groups.cu", "vlm.cu", "restart.cpp"]
+SOURCES = ["capi.cu", "neighbours.cu", "sweeps.cu", "integrate.cu", "state.cu", "settings.cpp", "noalloc.cu", "sweeps_mixed.cu", "mlp_train.cu", "update.cu", "groups.cu", "vlm.cu", "restart.cpp", "shapes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fno-strict-aliasing", "-I", str(ROOT / "include")]

@@ -34,6 +34,7 @@ PARA_KEYS = {
     "SPH surface tension contact angle": ("contangb", "f"),
     "Init hydrostatic pressure (0/1)": ("init_hydro_pressure", "i"),
     "Hydrostatic height": ("hydro_height", "f"),
+    "Grid scale": ("scale", "f"),
     "SPH integration solver": ("solver_name", "s"),
     "SPH equation of state (0=Cole/1=Isothermal)": ("pressure_rel", "i"),
     "SPH solver minimum residual": ("min_residual", "f"),

@@ -390,6 +390,48 @@ int fjsph_vlm_velocity(fjsph_ctx *ctx, int64_t n, const double *pos, double *vel
 int fjsph_restart_write(fjsph_ctx *ctx, const char *path, int64_t current_frame);
 int fjsph_restart_read(fjsph_ctx *ctx, const char *path, int64_t *current_frame);
 
+/* ---- initial particles from block files (src/Init.cpp:61-496, src/shapes/) ------------------- */
+/* Host-side restatement of Init_Particles: the boundary and fluid block files ("bmap" text,
+ * src/shapes/shapes.cpp:400-600) are read, each block checked (check_input) and generated
+ * (generate_points: Line/Plane, Square/Cube, Circle/Sphere, Arc/Arch, Cylinder, Inlet,
+ * Coordinates), points closer than 0.9 dx to a kept point are culled (Check_Intersection), and
+ * the state, the LIMITS entries and the inlet tables are laid out in reference index order,
+ * with the hydrostatic start when the settings ask for it.  The settings are the ones after
+ * fjsph_settings_derive (dx, masses, EOS constants, grid scale).  Errors that make the reference
+ * print and exit(-1) return FJSPH_E_ARG; fjsph_geometry_log holds the reference's messages. */
+typedef struct fjsph_geometry fjsph_geometry;
+typedef struct fjsph_geometry_block {
+    char name[64];
+    int32_t is_fluid, shape, sub_shape; /* shape_type (src/VarDefs.h:116-127), -1 = none   */
+    int32_t particle_order, write_data;  /* 0 grid / 1 HCP; "Write surface data"             */
+    int32_t ni, nj, nk;                  /* counts after check_input                         */
+    int64_t estimated;                   /* check_input's point estimate (npts)               */
+    int64_t generated;                   /* points made by generate_points                   */
+    int64_t kept;                        /* points left by Check_Intersection                */
+    double radius;
+    double start[3], end[3], right[3], centre[3], normal[3]; /* after check_input            */
+} fjsph_geometry_block;
+int fjsph_geometry_create(const fjsph_settings *s, fjsph_geometry **out);
+int fjsph_geometry_destroy(fjsph_geometry *g);
+/* read_shapes_bmap on a file's text / on a file; fluid = 0 for the boundary file, 1 for the
+ * fluid file (boundary blocks come first in the state whatever the call order). */
+int fjsph_geometry_read(fjsph_geometry *g, const char *text, int32_t fluid);
+int fjsph_geometry_read_file(fjsph_geometry *g, const char *path, int32_t fluid);
+/* check_input, Generate_Points, Check_Intersection and the Init_Particles layout. */
+int fjsph_geometry_build(fjsph_geometry *g);
+int fjsph_geometry_sizes(const fjsph_geometry *g, int64_t *n_points, int64_t *n_bound_points,
+                         int32_t *n_bound_blocks, int32_t *n_fluid_blocks, int32_t *n_inlets);
+/* The SPHPart fields Init_Particles sets (src/Var.h:502-548, src/FJSPH.cpp:116-127: position,
+ * velocity, density, pressure, mass, type, id, constant-source cell values, cellID = -3); every
+ * other non-null array of the view is zeroed.  out->n is the arrays' capacity. */
+int fjsph_geometry_state(const fjsph_geometry *g, fjsph_state_view *out);
+int fjsph_geometry_blocks(const fjsph_geometry *g, fjsph_block *blocks, int32_t max_blocks);
+int fjsph_geometry_block_info(const fjsph_geometry *g, int32_t k, fjsph_geometry_block *info);
+/* Inlet k's tables: with back or buffer null, fills n_back and depth only (a size query). */
+int fjsph_geometry_inlet(const fjsph_geometry *g, int32_t k, fjsph_inlet *inlet);
+/* The messages check_input and Generate_Points print upstream; *len = full length. */
+int fjsph_geometry_log(const fjsph_geometry *g, char *buf, int64_t cap, int64_t *len);
+
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
 int fjsph_step_report(fjsph_ctx *ctx, double *out5);
