@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the plain FP64 form timed beside (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--vlm-points", type=int, default=1 << 20, help="points of the VLM air-source timing (0 = skip)")
+    ap.add_argument("--setup-particles", type=int, default=2_000_000,
+                    help="particles of the block-file setup timing (0 = skip)")
     ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--closure", default="learned", choices=["learned", "plain"])
@@ -261,6 +263,45 @@ def run_vlm(args):
                      "panel_interactions_per_s": m * npan / (ms / 1e3), "setup_s": round(setup_s, 3)}
         ctx.close()
     return out
+
+
+def run_case_setup(args):
+    """Init_Particles from block files on the host (fjsph_gb300.geometry over the C ABI): a cube
+    of water on a three-layer floor plane, sized for args.setup_particles, read from bmap text,
+    checked, generated, culled against the floor and laid out; then uploaded once."""
+    from fjsph_gb300.api import Context
+    from fjsph_gb300.geometry import Geometry
+    from fjsph_gb300.settings import defaults, derive
+    side = 1.0
+    dx = side / max(round(args.setup_particles ** (1.0 / 3.0)), 2)
+    s = defaults(3)
+    s.particle_step = dx
+    derive(s)
+    w = 3 * dx
+    bound = (f"Name: Floor\nShape: Plane\nStart coordinate: {-w},0,{-w}\nRight coordinate: {side + w},0,{-w}\n"
+             f"End coordinate: {side + w},0,{side + w}\nWall radial particle count: 3\nblock end\n")
+    fluid = f"Name: Water\nShape: Cube\nStart coordinate: 0,0,0\nEnd coordinate: {side},{side},{side}\nblock end\n"
+    t0 = time.perf_counter()
+    g = Geometry(s)
+    g.read_text(bound, False)
+    g.read_text(fluid, True)
+    g.build()
+    t1 = time.perf_counter()
+    st, blocks = g.state(), g.blocks()
+    t2 = time.perf_counter()
+    ctx = Context(s, st.n + 64, blocks, [])
+    ctx.set_states(st, st)
+    ctx.event_record(0)
+    ctx.event_record(1)
+    ctx.event_elapsed(0, 1)  # waits for the stream
+    t3 = time.perf_counter()
+    info = g.block_info()
+    g.close()
+    ctx.close()
+    return {"case": "water cube on a 3-layer floor plane (bmap text)", "particles": st.n,
+            "generated": int(sum(b["generated"] for b in info)), "dx": dx,
+            "build_s": round(t1 - t0, 3), "state_s": round(t2 - t1, 3), "upload_s": round(t3 - t2, 3),
+            "particles_per_s": st.n / (t1 - t0), "where": "host (one thread), then one upload"}
 
 
 def run_droplets(args, ws, rank, weights):
@@ -577,6 +618,7 @@ def main():
     r = run_ours(args, ws, rank, local)
     drops = run_droplets(args, ws, rank, r["weights"]) if args.drops > 0 else None
     vlm = run_vlm(args) if (args.vlm_points > 0 and rank == 0) else None
+    setup = run_case_setup(args) if (args.setup_particles > 0 and rank == 0) else None
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -595,7 +637,7 @@ def main():
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
                 "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"], "closure": r["closure"],
                 "neighbour_pairs": r["pairs"], "autotune": r["tune"], "droplet_batch": drops,
-                "vlm_air_source": vlm,
+                "vlm_air_source": vlm, "case_setup": setup,
                 "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
                 "gpu_launches": r["launches"], "passes_ms": r["prof"]}
         print(json.dumps(line))
