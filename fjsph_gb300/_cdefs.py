@@ -125,3 +125,12 @@ class GeometryBlock(C.Structure):
 
 # shape_type (src/VarDefs.h:116-127)
 LINE_PLANE, SQUARE_CUBE, CIRCLE_SPHERE, CYLINDER, ARC_SECTION, COORD_DEF, INLET_ZONE, HOLLOW, SOLID = range(9)
+
+
+class Mesh(C.Structure):
+    """fjsph_mesh: a CFD mesh with a solution per cell (the mesh-cell air source)."""
+    _fields_ = [("dim", _i32), ("n_verts", _i64), ("verts", C.POINTER(_d)), ("n_faces", _i64),
+                ("face_offsets", C.POINTER(_i64)), ("face_verts", C.POINTER(_i64)), ("face_right", C.POINTER(_i32)),
+                ("n_cells", _i64), ("cell_face_offsets", C.POINTER(_i64)), ("cell_faces", C.POINTER(_i64)),
+                ("cell_centres", C.POINTER(_d)), ("cell_vel", C.POINTER(_d)), ("cell_p", C.POINTER(_d)),
+                ("cell_rho", C.POINTER(_d))]

@@ -90,6 +90,7 @@ PROTOTYPES = {
     "fjsph_vlm_velocity": (C.c_int, [_P, _i64, _dp, _dp]),
     "fjsph_restart_write": (C.c_int, [_P, C.c_char_p, _i64]),
     "fjsph_restart_read": (C.c_int, [_P, C.c_char_p, _i64p]),
+    "fjsph_mesh_set": (C.c_int, [_P, C.POINTER(d.Mesh)]),
     "fjsph_geometry_create": (C.c_int, [C.POINTER(d.Settings), _pp]),
     "fjsph_geometry_destroy": (C.c_int, [_P]),
     "fjsph_geometry_read": (C.c_int, [_P, C.c_char_p, _i32]),

@@ -353,6 +353,12 @@ class Context:
         return f.value
 
     # ---- vortex-lattice air source (src/VLM.h) ----
+    def mesh_set(self, mesh) -> None:
+        """The mesh-cell air source's mesh (mesh: fjsph_gb300.mesh.CellMesh); the context must have
+        been created with asource = MESH_INFL."""
+        m = mesh.to_c()
+        check("fjsph_mesh_set", self._lib.fjsph_mesh_set(self._h, C.byref(m)))
+
     def vlm_setup(self, vlm: "d.Vlm") -> int:
         """VLM::Init + GetGamma for the context's v_inf; returns the panel count."""
         n = C.c_int32(0)

@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libfjsph_gb300.so"
 
-SOURCES = ["capi.cu", "neighbours.cu", "sweeps.cu", "integrate.cu", "state.cu", "settings.cpp", "noalloc.cu", "sweeps_mixed.cu", "mlp_train.cu", "update.cu", "groups.cu", "vlm.cu", "restart.cpp", "shapes.cpp"]
+SOURCES = ["capi.cu", "neighbours.cu", "sweeps.cu", "integrate.cu", "state.cu", "settings.cpp", "noalloc.cu", "sweeps_mixed.cu", "mlp_train.cu", "update.cu", "groups.cu", "vlm.cu", "restart.cpp", "shapes.cpp", "mesh.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fno-strict-aliasing", "-I", str(ROOT / "include")]
@@ -27,7 +27,9 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcomp
 # divide and square root and flush FP32 denormals (FP64 arithmetic is unaffected): these terms
 # already carry FP32 rounding, and the tests hold them to the FP64 oracle at the stated tolerances.
 PER_FILE = {"sweeps_mixed.cu": ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"],
-            "vlm.cu": ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"]}
+            "vlm.cu": ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"],
+            # the containment tests compare products: no fused multiply-adds, like the oracle
+            "mesh.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:

@@ -590,3 +590,41 @@ def shard_ids(n_drops: int, counts, rank: int, world: int) -> np.ndarray:
         owner[g] = r
         load[r] += counts[g]
     return np.flatnonzero(owner == rank)
+
+
+def droplet_in_mesh(dim: int = 2, diam: float = 1.2e-3, dx: float = 1e-4, air_speed: float = 30.0, seed: int = 11):
+    """A droplet of the config-2 liquid inside a CFD mesh whose cells carry a seeded air solution
+    (the mesh-cell air source, Gissler aero): 2D, a quad mesh with a square hole (inner boundary)
+    downstream of the drop; 3D, a box of tetrahedra.  Returns (case, mesh)."""
+    from .mesh import quad_mesh_2d, tet_mesh_3d
+    s = defaults(dim)
+    _liquid(s)
+    _air(s, air_speed)
+    s.asource = d.MESH_INFL
+    s.particle_step = dx
+    s.H_fac = 1.3
+    s.speed_sound = 40.0
+    s.visc_alpha = 0.05
+    s.grav[:] = [0.0, 0.0, 0.0]
+    s.solver_type = d.RUNGE_KUTTA
+    s.cfl = s.cfl_max = 0.5
+    s.cfl_min = 0.1
+    s.delta_t_min = 1e-12
+    s.delta_t_max = 1e-5
+    derive(s)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    if dim == 2:
+        r = 0.5 * diam
+        g = np.arange(-r, r + 1e-12, dx)
+        gx, gy = np.meshgrid(g, g, indexing="ij")
+        pts = np.stack([gx.ravel(), gy.ravel()], axis=1)
+        pts = pts[np.sum(pts ** 2, axis=1) <= r * r]
+        mesh = quad_mesh_2d(lo=(-2e-3, -2e-3), hi=(6e-3, 3e-3), n=(56, 35), hole=((3.5e-3, -0.6e-3), (4.6e-3, 0.6e-3)),
+                            u0=air_speed, seed=seed)
+    else:
+        pts = _sphere_points(diam, dx)
+        mesh = tet_mesh_3d(lo=(-1.5e-3, -1.5e-3, -1.5e-3), hi=(2.5e-3, 1.5e-3, 1.5e-3), n=(12, 9, 9), u0=air_speed,
+                           seed=seed)
+    pts = pts + rng.uniform(-0.01 * dx, 0.01 * dx, size=pts.shape)
+    st = _assemble(s, np.zeros((0, dim)), pts)
+    return Case(f"droplet_in_mesh_{dim}d", s, st, _blocks(0, st.n)), mesh

@@ -174,6 +174,10 @@ struct fjsph_ctx {
     float *vlm_abf = nullptr, *vlm_gf = nullptr;
     VlmDev vlm{};
     double *air_v = nullptr; /* 3 per slot */
+    /* mesh-cell air source */
+    MeshDev mesh{};
+    bool mesh_ready = false;
+    std::vector<void *> mesh_allocs;
 };
 
 namespace {
@@ -271,7 +275,8 @@ int validate_settings(const fjsph_settings *s) {
     /* -DNOFROZEN -DLINEAR does not compile upstream (src/Resid.cpp:381 uses fluid.rho0) */
     if ((s->variant & FJSPH_VAR_NOFROZEN) && (s->variant & FJSPH_VAR_LINEAR)) return FJSPH_E_UNSUPPORTED;
     if (s->precision != FJSPH_PREC_FP64 && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
-    if (s->asource != FJSPH_CONST_VEL && !(s->asource == FJSPH_VLM_INFL && s->dim == 3)) return FJSPH_E_UNSUPPORTED;
+    if (s->asource != FJSPH_CONST_VEL && s->asource != FJSPH_MESH_INFL && !(s->asource == FJSPH_VLM_INFL && s->dim == 3))
+        return FJSPH_E_UNSUPPORTED;
     if (s->aero_closure != FJSPH_CLOSURE_PLAIN && s->aero_closure != FJSPH_CLOSURE_LEARNED) return FJSPH_E_ARG;
     /* the learned closure lives in the split-precision residual */
     if (s->aero_closure == FJSPH_CLOSURE_LEARNED && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
@@ -336,7 +341,9 @@ Params make_params(const fjsph_ctx *c) {
     }
     P.grp = c->ngrp > 0 ? c->grp : nullptr;
     P.g_vinf = c->g_vinf;
-    P.air_v = (s.asource == FJSPH_VLM_INFL && c->vlm.np > 0) ? c->air_v : nullptr;
+    P.air_v = ((s.asource == FJSPH_VLM_INFL && c->vlm.np > 0) || (s.asource == FJSPH_MESH_INFL && c->mesh_ready))
+                  ? c->air_v
+                  : nullptr;
     P.sweep_threads = c->tune[0];
     P.resid_threads = c->tune[1];
     P.list_ahead = c->tune[2];
@@ -928,6 +935,18 @@ int vlm_air(fjsph_ctx *c, const Params &P, const DevNbr &N) {
     return FJSPH_OK;
 }
 
+/* get_aero_velocity: the uniform / vortex-lattice source, or FindCell for the mesh source */
+int aero_velocity(fjsph_ctx *c, const Params &P, const DevNbr &N) {
+    if (c->s.asource == FJSPH_MESH_INFL) {
+        if (!c->mesh_ready) return FJSPH_E_STATE; /* fjsph_mesh_set has not run */
+        launch_mesh_find(P, WS(c), c->mesh, c->air_v, c->stream);
+    } else {
+        launch_aero_velocity(P, WS(c), N, c->stream);
+    }
+    c->launches++;
+    return FJSPH_OK;
+}
+
 int prestep_passes(fjsph_ctx *c) {
     if (!c->nbr_valid) return FJSPH_E_STATE;
     Params P = make_params(c);
@@ -940,14 +959,14 @@ int prestep_passes(fjsph_ctx *c) {
         /* split-precision form: the dissipation terms are computed in the surface-normal walk
          * (they read nothing the surface passes write), timed with the surface section */
         Section sec(c, PASS_SURFACE);
-        launch_aero_velocity(P, WS(c), N, s);
+        TRY(aero_velocity(c, P, N));
         if (mixed(c)) {
             launch_m_surface(P, WS(c), N, c->K, dissipation, s);
             c->occ_valid = true;
         } else {
             launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
         }
-        c->launches += 4;
+        c->launches += 3; /* plus the aero velocity pass, counted by aero_velocity */
     }
     if (dissipation && !mixed(c)) {
         Section sec(c, PASS_DISSIPATION);
@@ -1444,7 +1463,8 @@ int inlet_advance(fjsph_ctx *c) {
  * close up. */
 int delete_particles(fjsph_ctx *c) {
     DeletePlanes DP{};
-    bool any = false;
+    DP.lost = c->s.asource == FJSPH_MESH_INFL ? 1 : 0;
+    bool any = DP.lost != 0;
     for (size_t b = c->n_bound_blocks; b < c->blocks.size() && b < (size_t)kMaxBlocks; ++b) {
         const fjsph_block &B = c->blocks[b];
         if (B.delconst == kDefaultVal) continue;
@@ -2076,7 +2096,7 @@ int fjsph_dsph_prestep(fjsph_ctx *c, double *npd) {
 int fjsph_get_aero_velocity(fjsph_ctx *c) {
     TRY(need_nbr(c));
     TRY(vlm_air(c, make_params(c), make_nbr(c)));
-    launch_aero_velocity(make_params(c), WS(c), make_nbr(c), c->stream);
+    TRY(aero_velocity(c, make_params(c), make_nbr(c)));
     c->pn_equals_W = false;
     return sync(c);
 }
@@ -2704,6 +2724,68 @@ int fjsph_vlm_defaults(fjsph_vlm *v) {
     v->panels_span = v->panels_chord = -1;
     v->max_vel_fac = 2.0;
     v->max_vel = 2.0; /* maxVelFac x |(1, 0, 0)|, the reference's constructor value */
+    return FJSPH_OK;
+}
+
+int fjsph_mesh_set(fjsph_ctx *c, const fjsph_mesh *m) {
+    if (!c || !m) return FJSPH_E_ARG;
+    if (c->s.asource != FJSPH_MESH_INFL || m->dim != c->D) return FJSPH_E_ARG;
+    MeshHost h;
+    TRY(mesh_build(*m, h));
+    TRY(sync(c));
+    TRY(graph_release(c));
+    for (void *q : c->mesh_allocs) {
+        char *qq = static_cast<char *>(q);
+        TRY(dfree(c, qq));
+    }
+    c->mesh_allocs.clear();
+    c->mesh_ready = false;
+    const int D = c->D;
+    const int64_t nc = m->n_cells, nf = m->n_faces;
+    auto put = [&](auto **dst, const auto *src, int64_t count) -> int {
+        TRY(dalloc(c, dst, count));
+        c->mesh_allocs.push_back((void *)*dst);
+        if (count > 0) CU(cudaMemcpy((void *)*dst, src, sizeof(**dst) * (size_t)count, cudaMemcpyHostToDevice));
+        return FJSPH_OK;
+    };
+    double *verts, *centre, *cvel, *cp, *crho, *rad2;
+    int64_t *face_off, *face_verts, *cell_off, *cell_faces, *bucket_off, *bucket_cells;
+    int32_t *face_right;
+    TRY(put(&verts, m->verts, D * m->n_verts));
+    TRY(put(&face_off, m->face_offsets, nf + 1));
+    TRY(put(&face_verts, m->face_verts, m->face_offsets[nf]));
+    TRY(put(&face_right, m->face_right, nf));
+    TRY(put(&cell_off, m->cell_face_offsets, nc + 1));
+    TRY(put(&cell_faces, m->cell_faces, m->cell_face_offsets[nc]));
+    TRY(put(&centre, m->cell_centres, D * nc));
+    TRY(put(&cvel, m->cell_vel, D * nc));
+    TRY(put(&cp, m->cell_p, nc));
+    TRY(put(&crho, m->cell_rho, nc));
+    TRY(put(&rad2, h.rad2.data(), nc));
+    TRY(put(&bucket_off, h.bucket_off.data(), (int64_t)h.bucket_off.size()));
+    TRY(put(&bucket_cells, h.bucket_cells.data(), (int64_t)h.bucket_cells.size()));
+    if (!c->air_v) TRY(dalloc(c, &c->air_v, 3 * c->cap));
+    MeshDev &M = c->mesh;
+    M.ncells = nc;
+    M.verts = verts;
+    M.face_off = face_off;
+    M.face_verts = face_verts;
+    M.face_right = face_right;
+    M.cell_off = cell_off;
+    M.cell_faces = cell_faces;
+    M.centre = centre;
+    M.cvel = cvel;
+    M.cp = cp;
+    M.crho = crho;
+    M.rad2 = rad2;
+    M.bucket_off = bucket_off;
+    M.bucket_cells = bucket_cells;
+    for (int k = 0; k < 3; ++k) {
+        M.lo[k] = h.lo[k];
+        M.dims[k] = h.dims[k];
+    }
+    M.inv_h = 1.0 / h.h;
+    c->mesh_ready = true;
     return FJSPH_OK;
 }
 

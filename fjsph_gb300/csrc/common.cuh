@@ -25,6 +25,9 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kEps = 2.220446049250313080847e-16; /* numeric_limits<double>::epsilon() */
 constexpr double kDefaultVal = 9999999.0;
 constexpr int64_t kNoCell = -3;
+/* cellID of a particle that left the mesh through its outer boundary (deleted with the step's
+ * other deletions) */
+constexpr int64_t kMeshLost = -4;
 constexpr int kInletZone = 6;
 constexpr int kMaxBlocks = 32;
 

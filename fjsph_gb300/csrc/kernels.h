@@ -12,6 +12,30 @@
 namespace fjsph {
 
 /* Packed FP32 split-precision inputs of the mixed form (see sweeps_mixed.cu). */
+/* ---- mesh.cu: mesh-cell air source ----------------------------------------------------------- */
+struct MeshDev {
+    int64_t ncells;
+    const double *verts;                        /* dim per vertex                              */
+    const int64_t *face_off, *face_verts;       /* CSR vertices of every face                  */
+    const int32_t *face_right;                  /* right cell, -1 inner / -2 outer boundary    */
+    const int64_t *cell_off, *cell_faces;       /* CSR faces of every cell                     */
+    const double *centre, *cvel, *cp, *crho;    /* dim per cell for centre and velocity        */
+    const double *rad2;                         /* squared bounding-sphere radius per cell     */
+    const int64_t *bucket_off, *bucket_cells;   /* uniform grid over the spheres' boxes        */
+    double lo[3], inv_h;
+    int32_t dims[3];
+};
+struct MeshHost {
+    std::vector<double> rad2;
+    std::vector<int64_t> bucket_off, bucket_cells;
+    double lo[3], h;
+    int32_t dims[3];
+};
+/* validates the mesh's index arrays and builds the bounding spheres and the bucket grid */
+int mesh_build(const fjsph_mesh &m, MeshHost &h);
+/* FindCell for the fluid slots; air[3 i + k] = the resulting cellV (the occlusion's air velocity) */
+void launch_mesh_find(const Params &P, const DevState &W, const MeshDev &M, double *air, cudaStream_t s);
+
 /* ---- vlm.cu: vortex-lattice air source -------------------------------------------------------- */
 struct VlmDev {
     int32_t np;           /* panels                                              */
@@ -54,6 +78,7 @@ struct InsertOp {
     double norm[3];           /* insertion normal of the block                       */
 };
 struct DeletePlanes {
+    int32_t lost; /* also delete particles whose cellID is kMeshLost (mesh air source) */
     int32_t on[kMaxBlocks];
     double norm[kMaxBlocks][3];
     double c[kMaxBlocks];

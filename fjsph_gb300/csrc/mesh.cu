@@ -1,0 +1,276 @@
+/*
+ * mesh.cu -- the mesh-cell air source: which cell of a CFD mesh each free particle is in, and
+ * that cell's velocity, pressure and density (src/Containment.cpp:385-421 CheckCell,
+ * :579-821 FindCell, src/Resid.cpp:477-519, src/Geometry.cpp:151-157).
+ *
+ * Containment is the reference's test: a ray from the particle along +x (2D: Crossings2D per
+ * edge; 3D: Crossings3D per face, signed volumes of the face's first three vertices, ray end
+ * point + 1e5 x) toggles an inside flag, and the second crossing ends the test (convex cells).
+ * The particle's previous cell is tried first.  The reference then walks the 5 and the 500
+ * nearest cell centres of a KD tree; here the candidates are the cells whose bounding sphere
+ * (centre, largest centre-vertex distance) holds the particle -- every cell that can contain it
+ * -- taken from a uniform grid over the spheres' boxes, and the containing candidate with the
+ * nearest centre wins (ties: the lower index), which is the cell the nearest-centre walk finds.
+ * A particle inside no cell is outside the mesh: the segment to the nearest centre among the
+ * cells whose doubled sphere holds it is tested against that cell's boundary faces; an outer-boundary crossing marks the particle
+ * for deletion (cellID = kMeshLost, removed with the step's other deletions), an inner-boundary
+ * crossing or no crossing leaves it with its previous cell values.
+ */
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "kernels.h"
+
+namespace fjsph {
+
+namespace {
+
+constexpr int kT = 128;
+
+template <int D>
+__device__ __forceinline__ double vert(const MeshDev &M, int64_t v, int k) {
+    return M.verts[v * D + k];
+}
+
+/* Crossings2D (src/Geometry.cpp:354-397): does the +x ray from (tx, ty) cross edge (a, b)? */
+__device__ __forceinline__ bool crosses_2d(double ax, double ay, double bx, double by, double tx, double ty) {
+    const bool y0 = ay >= ty, y1 = by >= ty;
+    if (y0 == y1) return false;
+    return ((by - ty) * (bx - ax) >= (bx - tx) * (by - ay)) == y1;
+}
+
+/* sign test of the 4x4 determinant |p 1; a 1; b 1; c 1| < 0, i.e. det(a - p, b - p, c - p) > 0 */
+__device__ __forceinline__ bool neg_vol(const double *p, const double *a, const double *b, const double *c) {
+    const double ax = a[0] - p[0], ay = a[1] - p[1], az = a[2] - p[2];
+    const double bx = b[0] - p[0], by = b[1] - p[1], bz = b[2] - p[2];
+    const double cx = c[0] - p[0], cy = c[1] - p[1], cz = c[2] - p[2];
+    const double det = ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx);
+    return det > 0.0;
+}
+
+/* Crossings3D (src/Geometry.cpp:485-574): does segment p -> q cross the face's first triangle? */
+__device__ bool crosses_3d(const MeshDev &M, int64_t f, const double *p, const double *q) {
+    const int64_t f0 = M.face_off[f], f1 = M.face_off[f + 1];
+    double v[3][3], last[3];
+    for (int t = 0; t < 3; ++t)
+        for (int k = 0; k < 3; ++k) v[t][k] = vert<3>(M, M.face_verts[f0 + t], k);
+    for (int k = 0; k < 3; ++k) last[k] = vert<3>(M, M.face_verts[f1 - 1], k);
+    if (neg_vol(p, v[0], v[1], v[2]) == neg_vol(q, v[0], v[1], v[2])) return false;
+    /* edges (last, v0), (v0, v1), (v1, v2): the sign of every tet must agree */
+    const bool s3 = neg_vol(p, last, v[0], q);
+    if (neg_vol(p, v[0], v[1], q) != s3) return false;
+    if (neg_vol(p, v[1], v[2], q) != s3) return false;
+    return true;
+}
+
+template <int D>
+__device__ bool check_cell(const MeshDev &M, int64_t cell, const double *p) {
+    bool inside = false, line = false;
+    double ray[3] = {p[0] + 1e5, p[1], D == 3 ? p[2] : 0.0};
+    for (int64_t e = M.cell_off[cell]; e < M.cell_off[cell + 1]; ++e) {
+        const int64_t f = M.cell_faces[e];
+        bool hit;
+        if (D == 2) {
+            const int64_t a = M.face_verts[M.face_off[f]], b = M.face_verts[M.face_off[f] + 1];
+            hit = crosses_2d(vert<2>(M, a, 0), vert<2>(M, a, 1), vert<2>(M, b, 0), vert<2>(M, b, 1), p[0], p[1]);
+        } else {
+            hit = crosses_3d(M, f, p, ray);
+        }
+        if (hit) {
+            inside = !inside;
+            if (line) break; /* convex cells: at most two crossings */
+            line = true;
+        }
+    }
+    return inside;
+}
+
+/* get_line_intersection (src/Geometry.cpp:312-343): does segment p -> c cross edge (e1, e2)?
+ * Only one orientation of the pair counts (a denominator below epsilon returns "no"). */
+__device__ bool seg_cross_2d(const MeshDev &M, int64_t f, const double *p, const double *c) {
+    const int64_t a = M.face_verts[M.face_off[f]], b = M.face_verts[M.face_off[f] + 1];
+    const double e1x = vert<2>(M, a, 0), e1y = vert<2>(M, a, 1), e2x = vert<2>(M, b, 0), e2y = vert<2>(M, b, 1);
+    const double sx = c[0] - p[0], sy = c[1] - p[1], rx = e2x - e1x, ry = e2y - e1y;
+    const double denom = -rx * sy + sx * ry;
+    if (denom < 2.220446049250313e-16) return false;
+    const double u = (-sy * (p[0] - e1x) + sx * (p[1] - e1y)) / denom;
+    const double t = (rx * (p[1] - e1y) - ry * (p[0] - e1x)) / denom;
+    return u > 0 && u < 1 && t > 0 && t < 1;
+}
+
+template <int D>
+__device__ __forceinline__ void assign(const MeshDev &M, DevState &W, int64_t i, int64_t cell) {
+    W.cellID[i] = cell;
+#pragma unroll
+    for (int k = 0; k < D; ++k) W.cellV[k][i] = M.cvel[cell * D + k];
+    W.cellP[i] = M.cp[cell];
+    W.cellRho[i] = M.crho[cell];
+}
+
+template <int D>
+__global__ void k_mesh_find(Params P, DevState W, MeshDev M, double *air) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    if (W.b[i] != FJSPH_FREE || W.lam_nb[i] > P.lam_cutoff) {
+        W.cellID[i] = kNoCell;
+    } else if (W.cellID[i] != kMeshLost) {
+        double p[3] = {W.x[0][i], W.x[1][i], D == 3 ? W.x[2][i] : 0.0};
+        const int64_t cur = W.cellID[i];
+        if (cur >= 0 && cur < M.ncells && check_cell<D>(M, cur, p)) {
+            assign<D>(M, W, i, cur);
+        } else {
+            int gi[3] = {0, 0, 0};
+            bool in_grid = true;
+            for (int k = 0; k < D; ++k) {
+                const double g = floor((p[k] - M.lo[k]) * M.inv_h);
+                if (!(g >= 0.0 && g < (double)M.dims[k])) in_grid = false;
+                gi[k] = in_grid ? (int)g : 0;
+            }
+            int64_t best = -1, nearest = -1;
+            double best_d = 0.0, near_d = 0.0;
+            if (in_grid) {
+                const int64_t bucket = D == 3 ? ((int64_t)gi[2] * M.dims[1] + gi[1]) * M.dims[0] + gi[0]
+                                              : (int64_t)gi[1] * M.dims[0] + gi[0];
+                for (int64_t e = M.bucket_off[bucket]; e < M.bucket_off[bucket + 1]; ++e) {
+                    const int64_t c = M.bucket_cells[e];
+                    double d2 = 0.0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const double dd = p[k] - M.centre[c * D + k];
+                        d2 += dd * dd;
+                    }
+                    if (d2 > 4.0 * M.rad2[c]) continue; /* beyond twice the bounding sphere */
+                    if (nearest < 0 || d2 < near_d || (d2 == near_d && c < nearest)) {
+                        nearest = c;
+                        near_d = d2;
+                    }
+                    if (d2 > M.rad2[c]) continue; /* outside the cell's bounding sphere */
+                    if ((best < 0 || d2 < best_d || (d2 == best_d && c < best)) && check_cell<D>(M, c, p)) {
+                        best = c;
+                        best_d = d2;
+                    }
+                }
+            }
+            if (best >= 0) {
+                assign<D>(M, W, i, best);
+            } else if (nearest >= 0) {
+                /* outside every cell: did the particle cross the nearest cell's boundary? */
+                double cc[3] = {M.centre[nearest * D], M.centre[nearest * D + 1], D == 3 ? M.centre[nearest * D + 2] : 0.0};
+                for (int64_t e = M.cell_off[nearest]; e < M.cell_off[nearest + 1]; ++e) {
+                    const int64_t f = M.cell_faces[e];
+                    const int32_t side = M.face_right[f];
+                    if (side >= 0) continue;
+                    const bool hit = D == 2 ? seg_cross_2d(M, f, p, cc) : crosses_3d(M, f, p, cc);
+                    if (!hit) continue;
+                    if (side == -2) W.cellID[i] = kMeshLost; /* crossed the outer boundary */
+                    break;
+                }
+            }
+        }
+    }
+    if (air) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) air[3 * i + k] = k < D ? W.cellV[k][i] : 0.0;
+    }
+}
+
+} // namespace
+
+int mesh_build(const fjsph_mesh &m, MeshHost &h) {
+    const int D = m.dim;
+    if ((D != 2 && D != 3) || m.n_cells <= 0 || m.n_faces <= 0 || m.n_verts <= 0) return FJSPH_E_ARG;
+    if (!m.verts || !m.face_offsets || !m.face_verts || !m.face_right || !m.cell_face_offsets || !m.cell_faces ||
+        !m.cell_centres || !m.cell_vel || !m.cell_p || !m.cell_rho)
+        return FJSPH_E_ARG;
+    const int64_t nc = m.n_cells, nf = m.n_faces;
+    /* check the index arrays before anything reads through them */
+    if (m.face_offsets[0] != 0 || m.cell_face_offsets[0] != 0) return FJSPH_E_ARG;
+    for (int64_t f = 0; f < nf; ++f) {
+        const int64_t a = m.face_offsets[f], b = m.face_offsets[f + 1];
+        if (b - a < (D == 2 ? 2 : 3) || (D == 2 && b - a != 2)) return FJSPH_E_ARG;
+        if (m.face_right[f] < -2 || m.face_right[f] >= nc) return FJSPH_E_ARG;
+    }
+    for (int64_t q = 0; q < m.face_offsets[nf]; ++q)
+        if (m.face_verts[q] < 0 || m.face_verts[q] >= m.n_verts) return FJSPH_E_ARG;
+    for (int64_t c = 0; c < nc; ++c)
+        if (m.cell_face_offsets[c + 1] <= m.cell_face_offsets[c]) return FJSPH_E_ARG;
+    for (int64_t q = 0; q < m.cell_face_offsets[nc]; ++q)
+        if (m.cell_faces[q] < 0 || m.cell_faces[q] >= nf) return FJSPH_E_ARG;
+    /* bounding spheres: the largest distance from a cell's centre to one of its vertices */
+    h.rad2.assign((size_t)nc, 0.0);
+    double rmean = 0.0;
+    std::vector<double> lo(D, 1e300), hi(D, -1e300);
+    for (int64_t c = 0; c < nc; ++c) {
+        double r2 = 0.0;
+        for (int64_t e = m.cell_face_offsets[c]; e < m.cell_face_offsets[c + 1]; ++e) {
+            const int64_t f = m.cell_faces[e];
+            for (int64_t q = m.face_offsets[f]; q < m.face_offsets[f + 1]; ++q) {
+                double d2 = 0.0;
+                for (int k = 0; k < D; ++k) {
+                    const double dd = m.verts[m.face_verts[q] * D + k] - m.cell_centres[c * D + k];
+                    d2 += dd * dd;
+                }
+                r2 = std::max(r2, d2);
+            }
+        }
+        r2 *= 1.0 + 1e-9; /* covers the rounding of the containment test at the sphere's edge */
+        h.rad2[(size_t)c] = r2;
+        rmean += std::sqrt(r2);
+        for (int k = 0; k < D; ++k) {
+            lo[k] = std::min(lo[k], m.cell_centres[c * D + k] - 2.0 * std::sqrt(r2));
+            hi[k] = std::max(hi[k], m.cell_centres[c * D + k] + 2.0 * std::sqrt(r2));
+        }
+    }
+    rmean /= double(nc);
+    /* grid edge: twice the mean radius, raised until the grid has at most 2^24 buckets */
+    double hgrid = 2.0 * rmean;
+    for (;;) {
+        double nb = 1.0;
+        for (int k = 0; k < D; ++k) nb *= std::floor((hi[k] - lo[k]) / hgrid) + 1.0;
+        if (nb <= double(1 << 24)) break;
+        hgrid *= 1.5;
+    }
+    h.h = hgrid;
+    for (int k = 0; k < 3; ++k) {
+        h.lo[k] = k < D ? lo[k] : 0.0;
+        h.dims[k] = k < D ? (int32_t)(std::floor((hi[k] - lo[k]) / hgrid) + 1.0) : 1;
+    }
+    const int64_t nbk = (int64_t)h.dims[0] * h.dims[1] * h.dims[2];
+    std::vector<int64_t> count((size_t)nbk + 1, 0);
+    auto span = [&](int64_t c, int k, int &a, int &b) { /* boxes of twice the bounding sphere */
+        const double r = 2.0 * std::sqrt(h.rad2[(size_t)c]);
+        /* one bucket of margin each side: the query's bucket index rounds differently */
+        a = std::max(0, (int)std::floor((m.cell_centres[c * D + k] - r - h.lo[k]) / hgrid) - 1);
+        b = std::min(h.dims[k] - 1, (int)std::floor((m.cell_centres[c * D + k] + r - h.lo[k]) / hgrid) + 1);
+    };
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            for (int64_t q = 0; q < nbk; ++q) count[(size_t)q + 1] += count[(size_t)q];
+            h.bucket_off = count;
+            h.bucket_cells.assign((size_t)count[(size_t)nbk], 0);
+        }
+        std::vector<int64_t> fill = pass == 1 ? h.bucket_off : std::vector<int64_t>();
+        for (int64_t c = 0; c < nc; ++c) {
+            int a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+            for (int k = 0; k < D; ++k) span(c, k, a[k], b[k]);
+            for (int z = a[2]; z <= b[2]; ++z)
+                for (int y = a[1]; y <= b[1]; ++y)
+                    for (int x = a[0]; x <= b[0]; ++x) {
+                        const int64_t q = ((int64_t)z * h.dims[1] + y) * h.dims[0] + x;
+                        if (pass == 0) count[(size_t)q + 1]++;
+                        else h.bucket_cells[(size_t)fill[(size_t)q]++] = c;
+                    }
+        }
+    }
+    return FJSPH_OK;
+}
+
+void launch_mesh_find(const Params &P, const DevState &W, const MeshDev &M, double *air, cudaStream_t s) {
+    const int64_t nf = P.n - P.nb;
+    if (nf <= 0) return;
+    if (P.D == 2) k_mesh_find<2><<<grid_for(nf, kT), kT, 0, s>>>(P, W, M, air);
+    else k_mesh_find<3><<<grid_for(nf, kT), kT, 0, s>>>(P, W, M, air);
+}
+
+} // namespace fjsph

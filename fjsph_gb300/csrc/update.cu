@@ -73,6 +73,7 @@ __global__ void k_delete_flags(Params P, DevState W, DeletePlanes DP, int32_t *f
     if (s >= P.nb) {
         const int b = W.blk[s];
         if (DP.on[b] && plane_dot(W, P.D, s, DP.norm[b]) > DP.c[b]) f = 1;
+        if (DP.lost && W.cellID[s] == kMeshLost) f = 1;
     }
     flag[s] = f;
     keep[s] = 1 - f;

@@ -381,6 +381,33 @@ int fjsph_vlm_panels(fjsph_ctx *ctx, double *gamma, double *abc, int32_t *npanel
  * the context's precision (FP64, or FP32 sums for the split-precision form). */
 int fjsph_vlm_velocity(fjsph_ctx *ctx, int64_t n, const double *pos, double *vel);
 
+/* ---- mesh-cell air source (src/Containment.cpp:385-821, src/Resid.cpp:477-519) -------------- */
+/* A CFD mesh with a solution per cell (the MESH of src/Var.h:396-451 after the TAU / OpenFOAM
+ * readers): vertices, faces as vertex lists (2D: edges of two vertices; 3D: polygons whose first
+ * three vertices are the ones the containment test uses, as upstream), each face's right-hand
+ * cell (-1 = inner boundary, -2 = outer boundary), each cell's faces, centre, velocity, pressure
+ * and density.  Arrays are host pointers, copied by fjsph_mesh_set. */
+typedef struct fjsph_mesh {
+    int32_t dim;
+    int64_t n_verts;
+    const double *verts;             /* [dim * n_verts]                                      */
+    int64_t n_faces;
+    const int64_t *face_offsets;     /* [n_faces + 1] into face_verts                        */
+    const int64_t *face_verts;
+    const int32_t *face_right;       /* [n_faces]                                            */
+    int64_t n_cells;
+    const int64_t *cell_face_offsets; /* [n_cells + 1] into cell_faces                       */
+    const int64_t *cell_faces;
+    const double *cell_centres;      /* [dim * n_cells]                                      */
+    const double *cell_vel;          /* [dim * n_cells]                                      */
+    const double *cell_p, *cell_rho; /* [n_cells]                                            */
+} fjsph_mesh;
+/* Hands the mesh to a context created with asource = FJSPH_MESH_INFL.  FindCell then runs in
+ * place of the uniform-source aero velocity pass: free particles below the lambda cutoff take
+ * the velocity, pressure and density of the cell they are in (cellID = the cell); a particle
+ * that leaves through the outer boundary is deleted at the end of the step. */
+int fjsph_mesh_set(fjsph_ctx *ctx, const fjsph_mesh *mesh);
+
 /* ---- restart files (src/H5IO.cpp:395-523, 1027-1060, 1092-1318) ---------------------------- */
 /* Write_HDF5 / Read_HDF5 content with the reference's group, dataset and attribute names in a
  * self-describing binary container (no HDF5 library here; the layout is documented in

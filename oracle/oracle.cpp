@@ -88,6 +88,11 @@ struct orc_sim {
     std::vector<double> vlm_A, vlm_B, vlm_C, vlm_gamma;
     double vlm_vinf[3] = {0, 0, 0}, vlm_maxvel = 0.0;
     bool vlm_ready = false;
+    /* mesh-cell air source (MESH, Var.h:396-451) */
+    std::vector<double> m_verts, m_centre, m_vel, m_p, m_rho, m_rad2;
+    std::vector<int64_t> m_face_off, m_face_verts, m_cell_off, m_cell_faces;
+    std::vector<int32_t> m_face_right;
+    int64_t m_ncells = 0;
 };
 
 namespace {
@@ -692,9 +697,141 @@ void vlm_velocity(const orc_sim *o, const double *P, double *vel) {
     for (int k = 0; k < 3; ++k) vel[k] = u[k] * m;
 }
 
+/* ------------------------------------------------------------------------------------------ */
+/* Containment.cpp:385-421 CheckCell, Geometry.cpp:312-574 crossing tests, Containment.cpp:579-821 */
+/* FindCell.  The candidate cells are those whose bounding sphere (largest centre-vertex        */
+/* distance) holds the particle, scanned in full here; the containing one with the nearest      */
+/* centre (then the lower index) is taken, as the nearest-centre walk of the reference finds.   */
+/* Outside every cell, the boundary test uses the nearest centre among the cells whose doubled  */
+/* sphere holds the particle.                                                                   */
+/* ------------------------------------------------------------------------------------------ */
+constexpr int64_t kMeshLost = -4;
+
+bool m_cross_2d(const double *a, const double *b, double tx, double ty) {
+    const bool y0 = a[1] >= ty, y1 = b[1] >= ty;
+    if (y0 == y1) return false;
+    return ((b[1] - ty) * (b[0] - a[0]) >= (b[0] - tx) * (b[1] - a[1])) == y1;
+}
+
+/* |p 1; a 1; b 1; c 1| < 0 */
+bool m_neg_vol(const double *p, const double *a, const double *b, const double *c) {
+    const double ax = a[0] - p[0], ay = a[1] - p[1], az = a[2] - p[2];
+    const double bx = b[0] - p[0], by = b[1] - p[1], bz = b[2] - p[2];
+    const double cx = c[0] - p[0], cy = c[1] - p[1], cz = c[2] - p[2];
+    const double det = ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx);
+    return det > 0.0;
+}
+
+bool m_cross_3d(const orc_sim *o, int64_t f, const double *p, const double *q) {
+    const int64_t f0 = o->m_face_off[f], f1 = o->m_face_off[f + 1];
+    const double *v0 = &o->m_verts[3 * o->m_face_verts[f0]], *v1 = &o->m_verts[3 * o->m_face_verts[f0 + 1]];
+    const double *v2 = &o->m_verts[3 * o->m_face_verts[f0 + 2]], *last = &o->m_verts[3 * o->m_face_verts[f1 - 1]];
+    if (m_neg_vol(p, v0, v1, v2) == m_neg_vol(q, v0, v1, v2)) return false;
+    const bool s3 = m_neg_vol(p, last, v0, q);
+    if (m_neg_vol(p, v0, v1, q) != s3) return false;
+    if (m_neg_vol(p, v1, v2, q) != s3) return false;
+    return true;
+}
+
+bool m_check_cell(const orc_sim *o, int64_t cell, const double *p) {
+    const int D = o->D;
+    bool inside = false, line = false;
+    const double ray[3] = {p[0] + 1e5, p[1], D == 3 ? p[2] : 0.0};
+    for (int64_t e = o->m_cell_off[cell]; e < o->m_cell_off[cell + 1]; ++e) {
+        const int64_t f = o->m_cell_faces[e];
+        bool hit;
+        if (D == 2) {
+            const int64_t a = o->m_face_verts[o->m_face_off[f]], b = o->m_face_verts[o->m_face_off[f] + 1];
+            hit = m_cross_2d(&o->m_verts[2 * a], &o->m_verts[2 * b], p[0], p[1]);
+        } else {
+            hit = m_cross_3d(o, f, p, ray);
+        }
+        if (hit) {
+            inside = !inside;
+            if (line) break;
+            line = true;
+        }
+    }
+    return inside;
+}
+
+bool m_seg_cross_2d(const orc_sim *o, int64_t f, const double *p, const double *c) {
+    const int64_t a = o->m_face_verts[o->m_face_off[f]], b = o->m_face_verts[o->m_face_off[f] + 1];
+    const double *e1 = &o->m_verts[2 * a], *e2 = &o->m_verts[2 * b];
+    const double sx = c[0] - p[0], sy = c[1] - p[1], rx = e2[0] - e1[0], ry = e2[1] - e1[1];
+    const double denom = -rx * sy + sx * ry;
+    if (denom < kEps) return false;
+    const double u = (-sy * (p[0] - e1[0]) + sx * (p[1] - e1[1])) / denom;
+    const double t = (rx * (p[1] - e1[1]) - ry * (p[0] - e1[0])) / denom;
+    return u > 0 && u < 1 && t > 0 && t < 1;
+}
+
+void find_cell(orc_sim *o, std::vector<Part> &P) {
+    const int D = o->D;
+    const fjsph_settings &a = o->s;
+    auto assign = [&](Part &pi, int64_t c) {
+        pi.cellID = c;
+        for (int k = 0; k < D; ++k) pi.cellV[k] = o->m_vel[c * D + k];
+        pi.cellP = o->m_p[c];
+        pi.cellRho = o->m_rho[c];
+    };
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t ii = o->start_index; ii < o->end_index; ++ii) {
+        Part &pi = P[ii];
+        if (pi.b != FJSPH_FREE || pi.lam_nb > a.lam_cutoff) {
+            pi.cellID = kNoCell;
+            continue;
+        }
+        if (pi.cellID == kMeshLost) continue;
+        const double p[3] = {pi.xi[0], pi.xi[1], D == 3 ? pi.xi[2] : 0.0};
+        if (pi.cellID >= 0 && pi.cellID < o->m_ncells && m_check_cell(o, pi.cellID, p)) {
+            assign(pi, pi.cellID);
+            continue;
+        }
+        int64_t best = -1, nearest = -1;
+        double best_d = 0.0, near_d = 0.0;
+        for (int64_t c = 0; c < o->m_ncells; ++c) {
+            double d2 = 0.0;
+            for (int k = 0; k < D; ++k) {
+                const double dd = p[k] - o->m_centre[c * D + k];
+                d2 += dd * dd;
+            }
+            if (d2 > 4.0 * o->m_rad2[c]) continue; /* the nearest cell within twice its sphere */
+            if (nearest < 0 || d2 < near_d) {
+                nearest = c;
+                near_d = d2;
+            }
+            if (d2 > o->m_rad2[c]) continue;
+            if ((best < 0 || d2 < best_d) && m_check_cell(o, c, p)) {
+                best = c;
+                best_d = d2;
+            }
+        }
+        if (best >= 0) {
+            assign(pi, best);
+        } else if (nearest >= 0) {
+            const double cc[3] = {o->m_centre[nearest * D], o->m_centre[nearest * D + 1],
+                                  D == 3 ? o->m_centre[nearest * D + 2] : 0.0};
+            for (int64_t e = o->m_cell_off[nearest]; e < o->m_cell_off[nearest + 1]; ++e) {
+                const int64_t f = o->m_cell_faces[e];
+                const int32_t side = o->m_face_right[f];
+                if (side >= 0) continue;
+                const bool hit = D == 2 ? m_seg_cross_2d(o, f, p, cc) : m_cross_3d(o, f, p, cc);
+                if (!hit) continue;
+                if (side == -2) pi.cellID = kMeshLost;
+                break;
+            }
+        }
+    }
+}
+
 void get_aero_velocity(orc_sim *o, std::vector<Part> &P) {
     const int D = o->D;
     const fjsph_settings &a = o->s;
+    if (a.asource == FJSPH_MESH_INFL) { /* Resid.cpp:479-519: FindCell */
+        find_cell(o, P);
+        return;
+    }
 #pragma omp parallel for
     for (int64_t ii = o->start_index; ii < o->end_index; ++ii) {
         Part &pi = P[ii];
@@ -800,7 +937,9 @@ void detect_surface(orc_sim *o, std::vector<Part> &P) {
         double woccl_ = 0.0;
         double Vdiff[3] = {0, 0, 0};
         if (pi.cellID != -1 && pi.b == FJSPH_FREE && gissler) {
-            if (s.asource == FJSPH_VLM_INFL) { /* Geometry.cpp:158-163 */
+            if (s.asource == FJSPH_MESH_INFL) { /* Geometry.cpp:154-157 */
+                for (int k = 0; k < D; ++k) Vdiff[k] = pi.cellV[k] - pi.v[k];
+            } else if (s.asource == FJSPH_VLM_INFL) { /* Geometry.cpp:158-163 */
                 double vel[3];
                 vlm_velocity(o, pi.xi, vel);
                 for (int k = 0; k < D; ++k) Vdiff[k] = vel[k] - pi.v[k];
@@ -1758,11 +1897,15 @@ void update_data(orc_sim *o) {
     std::vector<int64_t> to_del;
     const int64_t nb = o->n_bound_blocks, nblk = o->n_bound_blocks + o->n_fluid_blocks;
     std::vector<int64_t> n_del(o->limits.size(), 0);
+    const bool mesh = o->s.asource == FJSPH_MESH_INFL;
     for (int64_t blk = nb; blk < nblk; ++blk) {
         const fjsph_block &B = o->limits[blk].d;
-        if (B.delconst == kDefaultVal) continue;
+        const bool plane = B.delconst != kDefaultVal;
+        if (!plane && !mesh) continue;
         for (int64_t ii = B.first; ii < B.second; ++ii)
-            if (dot(o->pnp1[ii].xi, B.delete_norm, D) > B.delconst) {
+            /* plane deletion, and particles that left the mesh through its outer boundary */
+            if ((plane && dot(o->pnp1[ii].xi, B.delete_norm, D) > B.delconst) ||
+                (mesh && o->pnp1[ii].cellID == kMeshLost)) {
                 to_del.push_back(ii);
                 n_del[blk]++;
             }
@@ -2115,6 +2258,41 @@ void orc_gradk(const double *Rij, double r, double H, double W_correc, int32_t c
 double orc_min_eig(const double *A, int32_t dim) { return min_eig(A, dim); }
 int32_t orc_qr_inverse(const double *A, int32_t dim, double *inv) { return qr_inverse(A, dim, inv); }
 double orc_get_cd(double Re) { return GetCd(Re); }
+
+/* the MESH the reference's readers build (Var.h:396-451), with each cell's bounding sphere */
+int orc_mesh_set(orc_sim *o, const fjsph_mesh *m) {
+    const int D = o->D;
+    if (!m || m->dim != D || m->n_cells <= 0) return FJSPH_E_ARG;
+    const int64_t nc = m->n_cells, nf = m->n_faces;
+    o->m_ncells = nc;
+    o->m_verts.assign(m->verts, m->verts + D * m->n_verts);
+    o->m_face_off.assign(m->face_offsets, m->face_offsets + nf + 1);
+    o->m_face_verts.assign(m->face_verts, m->face_verts + m->face_offsets[nf]);
+    o->m_face_right.assign(m->face_right, m->face_right + nf);
+    o->m_cell_off.assign(m->cell_face_offsets, m->cell_face_offsets + nc + 1);
+    o->m_cell_faces.assign(m->cell_faces, m->cell_faces + m->cell_face_offsets[nc]);
+    o->m_centre.assign(m->cell_centres, m->cell_centres + D * nc);
+    o->m_vel.assign(m->cell_vel, m->cell_vel + D * nc);
+    o->m_p.assign(m->cell_p, m->cell_p + nc);
+    o->m_rho.assign(m->cell_rho, m->cell_rho + nc);
+    o->m_rad2.assign(nc, 0.0);
+    for (int64_t c = 0; c < nc; ++c) {
+        double r2 = 0.0;
+        for (int64_t e = o->m_cell_off[c]; e < o->m_cell_off[c + 1]; ++e) {
+            const int64_t f = o->m_cell_faces[e];
+            for (int64_t q = o->m_face_off[f]; q < o->m_face_off[f + 1]; ++q) {
+                double d2 = 0.0;
+                for (int k = 0; k < D; ++k) {
+                    const double dd = o->m_verts[o->m_face_verts[q] * D + k] - o->m_centre[c * D + k];
+                    d2 += dd * dd;
+                }
+                r2 = std::max(r2, d2);
+            }
+        }
+        o->m_rad2[c] = r2 * (1.0 + 1e-9);
+    }
+    return FJSPH_OK;
+}
 
 /* VLM::Init + MakeMatrix + GetGamma (VLM.cpp:14-117, 180-307) */
 int orc_vlm_setup(orc_sim *o, const fjsph_vlm *v) {

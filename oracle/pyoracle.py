@@ -61,6 +61,7 @@ _PROTO = {
     "orc_qr_inverse": (C.c_int32, [_dp, C.c_int32, _dp]),
     "orc_get_cd": (C.c_double, [C.c_double]),
     "orc_vlm_setup": (C.c_int, [_P, C.c_void_p]),
+    "orc_mesh_set": (C.c_int, [_P, C.c_void_p]),
     "orc_vlm_panels": (C.c_int, [_P, _dp, _dp]),
     "orc_vlm_velocity": (None, [_P, C.c_int64, _dp, _dp]),
 }
@@ -155,6 +156,13 @@ class Oracle:
 
     def dSPH_PreStep(self) -> float:
         return self._l.orc_dsph_prestep(self._h)
+
+    def mesh_set(self, mesh) -> None:
+        """The mesh-cell air source's mesh (mesh: fjsph_gb300.mesh.CellMesh)."""
+        m = mesh.to_c()
+        rc = lib().orc_mesh_set(self._h, C.byref(m))
+        if rc != 0:
+            raise RuntimeError(f"orc_mesh_set failed ({rc})")
 
     def vlm_setup(self, vlm) -> int:
         """VLM::Init + GetGamma for the settings' v_inf (vlm: fjsph_gb300._cdefs.Vlm)."""
