@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the plain FP64 form timed beside (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--vlm-points", type=int, default=1 << 20, help="points of the VLM air-source timing (0 = skip)")
+    ap.add_argument("--mesh-cell", type=float, default=8e-4,
+                    help="cube edge of the tetrahedral air mesh over the jet (0 = skip)")
     ap.add_argument("--setup-particles", type=int, default=2_000_000,
                     help="particles of the block-file setup timing (0 = skip)")
     ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
@@ -302,6 +304,72 @@ def run_case_setup(args):
             "generated": int(sum(b["generated"] for b in info)), "dx": dx,
             "build_s": round(t1 - t0, 3), "state_s": round(t2 - t1, 3), "upload_s": round(t3 - t2, 3),
             "particles_per_s": st.n / (t1 - t0), "where": "host (one thread), then one upload"}
+
+
+def run_mesh(args, case):
+    """The mesh-cell air source on the jet: a tetrahedral mesh over the jet's bounding box carries
+    a seeded air solution; FindCell (containment of every free surface particle, in place of the
+    uniform aero velocity) timed alone, and whole steps of the FP32 form with the plain closure."""
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300.api import Context
+    from fjsph_gb300.mesh import tet_mesh_3d
+    st = case.state
+    lo, hi = st.xi.min(axis=0) - 1e-4, st.xi.max(axis=0) + 1e-4
+    h = args.mesh_cell
+    n = tuple(int(max(1, np.ceil((hi[k] - lo[k]) / h))) for k in range(3))
+    t0 = time.perf_counter()
+    mesh = tet_mesh_3d(lo=tuple(lo), hi=tuple(lo + np.array(n) * h), n=n, u0=50.0, seed=3)
+    build_s = time.perf_counter() - t0
+    s = case.settings.copy()
+    s.asource = d.MESH_INFL
+    s.precision = d.PREC_MIXED
+    s.aero_closure = d.CLOSURE_PLAIN
+    ctx = Context(s, st.n + 1024, case.blocks)
+    t0 = time.perf_counter()
+    ctx.mesh_set(mesh)
+    set_s = time.perf_counter() - t0
+    ctx.set_states(st, st)
+    ctx.integrate()
+    ctx.update_neighbours()
+    ctx.dSPH_PreStep()
+    reps = 5
+    ctx.get_aero_velocity()  # every active particle located once (later calls start from its cell)
+    ctx.event_record(2)
+    for _ in range(reps):
+        ctx.get_aero_velocity()
+    ctx.event_record(3)
+    find_ms = ctx.event_elapsed(2, 3) / reps
+    got = ctx.download()
+    active = int(np.count_nonzero(got.cellID >= 0))
+    ctx.close()
+
+    def steps_ms(settings, with_mesh):
+        """whole steps after three warm-up steps, this context alone on the GPU"""
+        cx = Context(settings, st.n + 1024, case.blocks)
+        if with_mesh:
+            cx.mesh_set(mesh)
+        cx.set_states(st, st)
+        for _ in range(3):
+            cx.integrate()
+        cx.event_record(4)
+        for _ in range(3):
+            cx.integrate()
+        cx.event_record(5)
+        ms = cx.event_elapsed(4, 5) / 3
+        cx.close()
+        return ms
+
+    step_ms = steps_ms(s, True)
+    s_uniform = s.copy()
+    s_uniform.asource = d.CONST_VEL
+    uniform_ms = steps_ms(s_uniform, False)
+    return {"mesh": f"{mesh.n_cells} tetrahedra ({n[0]} x {n[1]} x {n[2]} cubes of {h * 1e3:.2f} mm, six each)",
+            "particles": st.n, "located": active, "find_cell_ms": round(find_ms, 4),
+            "located_per_s": active / (find_ms / 1e3) if find_ms > 0 else None,
+            "fp32_step_ms": round(step_ms, 3), "particle_steps_per_s": case.n_fluid / (step_ms / 1e3),
+            "fp32_step_ms_uniform_source": round(uniform_ms, 3),
+            "mesh_build_s": round(build_s, 2), "mesh_set_s": round(set_s, 3)}
 
 
 def run_droplets(args, ws, rank, weights):
@@ -619,6 +687,7 @@ def main():
     drops = run_droplets(args, ws, rank, r["weights"]) if args.drops > 0 else None
     vlm = run_vlm(args) if (args.vlm_points > 0 and rank == 0) else None
     setup = run_case_setup(args) if (args.setup_particles > 0 and rank == 0) else None
+    mesh = run_mesh(args, r["case"]) if (args.mesh_cell > 0 and rank == 0) else None
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -637,7 +706,7 @@ def main():
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
                 "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"], "closure": r["closure"],
                 "neighbour_pairs": r["pairs"], "autotune": r["tune"], "droplet_batch": drops,
-                "vlm_air_source": vlm, "case_setup": setup,
+                "vlm_air_source": vlm, "mesh_air_source": mesh, "case_setup": setup,
                 "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
                 "gpu_launches": r["launches"], "passes_ms": r["prof"]}
         print(json.dumps(line))

@@ -2749,7 +2749,7 @@ int fjsph_mesh_set(fjsph_ctx *c, const fjsph_mesh *m) {
         return FJSPH_OK;
     };
     double *verts, *centre, *cvel, *cp, *crho, *rad2;
-    int64_t *face_off, *face_verts, *cell_off, *cell_faces, *bucket_off, *bucket_cells;
+    int64_t *face_off, *face_verts, *cell_off, *cell_faces;
     int32_t *face_right;
     TRY(put(&verts, m->verts, D * m->n_verts));
     TRY(put(&face_off, m->face_offsets, nf + 1));
@@ -2762,10 +2762,20 @@ int fjsph_mesh_set(fjsph_ctx *c, const fjsph_mesh *m) {
     TRY(put(&cp, m->cell_p, nc));
     TRY(put(&crho, m->cell_rho, nc));
     TRY(put(&rad2, h.rad2.data(), nc));
-    TRY(put(&bucket_off, h.bucket_off.data(), (int64_t)h.bucket_off.size()));
-    TRY(put(&bucket_cells, h.bucket_cells.data(), (int64_t)h.bucket_cells.size()));
-    if (!c->air_v) TRY(dalloc(c, &c->air_v, 3 * c->cap));
     MeshDev &M = c->mesh;
+    for (int g = 0; g < 2; ++g) {
+        int64_t *off, *cells;
+        TRY(put(&off, h.g[g].off.data(), (int64_t)h.g[g].off.size()));
+        TRY(put(&cells, h.g[g].cells.data(), (int64_t)h.g[g].cells.size()));
+        M.g[g].off = off;
+        M.g[g].cells = cells;
+        M.g[g].inv_h = h.g[g].inv_h;
+        for (int k = 0; k < 3; ++k) {
+            M.g[g].lo[k] = h.g[g].lo[k];
+            M.g[g].dims[k] = h.g[g].dims[k];
+        }
+    }
+    if (!c->air_v) TRY(dalloc(c, &c->air_v, 3 * c->cap));
     M.ncells = nc;
     M.verts = verts;
     M.face_off = face_off;
@@ -2778,13 +2788,6 @@ int fjsph_mesh_set(fjsph_ctx *c, const fjsph_mesh *m) {
     M.cp = cp;
     M.crho = crho;
     M.rad2 = rad2;
-    M.bucket_off = bucket_off;
-    M.bucket_cells = bucket_cells;
-    for (int k = 0; k < 3; ++k) {
-        M.lo[k] = h.lo[k];
-        M.dims[k] = h.dims[k];
-    }
-    M.inv_h = 1.0 / h.h;
     c->mesh_ready = true;
     return FJSPH_OK;
 }

@@ -21,15 +21,22 @@ struct MeshDev {
     const int64_t *cell_off, *cell_faces;       /* CSR faces of every cell                     */
     const double *centre, *cvel, *cp, *crho;    /* dim per cell for centre and velocity        */
     const double *rad2;                         /* squared bounding-sphere radius per cell     */
-    const int64_t *bucket_off, *bucket_cells;   /* uniform grid over the spheres' boxes        */
-    double lo[3], inv_h;
-    int32_t dims[3];
+    /* two uniform grids listing every cell in the buckets its box overlaps: g[0] the bounding
+     * sphere's box (containment candidates), g[1] the box of the doubled sphere (the nearest
+     * cell of a particle outside the mesh) */
+    struct Grid {
+        const int64_t *off, *cells;
+        double lo[3], inv_h;
+        int32_t dims[3];
+    } g[2];
 };
 struct MeshHost {
     std::vector<double> rad2;
-    std::vector<int64_t> bucket_off, bucket_cells;
-    double lo[3], h;
-    int32_t dims[3];
+    struct Grid {
+        std::vector<int64_t> off, cells;
+        double lo[3], inv_h;
+        int32_t dims[3];
+    } g[2];
 };
 /* validates the mesh's index arrays and builds the bounding spheres and the bucket grid */
 int mesh_build(const fjsph_mesh &m, MeshHost &h);

@@ -12,9 +12,10 @@
  * -- taken from a uniform grid over the spheres' boxes, and the containing candidate with the
  * nearest centre wins (ties: the lower index), which is the cell the nearest-centre walk finds.
  * A particle inside no cell is outside the mesh: the segment to the nearest centre among the
- * cells whose doubled sphere holds it is tested against that cell's boundary faces; an outer-boundary crossing marks the particle
- * for deletion (cellID = kMeshLost, removed with the step's other deletions), an inner-boundary
- * crossing or no crossing leaves it with its previous cell values.
+ * cells whose doubled sphere holds it (a second grid) is tested against that cell's boundary
+ * faces; an outer-boundary crossing marks the particle for deletion (cellID = kMeshLost, removed
+ * with the step's other deletions), an inner-boundary crossing or no crossing leaves it with its
+ * previous cell values.
  */
 #include <algorithm>
 #include <cmath>
@@ -108,6 +109,30 @@ __device__ __forceinline__ void assign(const MeshDev &M, DevState &W, int64_t i,
     W.cellRho[i] = M.crho[cell];
 }
 
+/* bucket of p in grid G, or -1 outside it (the same expression the build uses for the spans) */
+template <int D>
+__device__ __forceinline__ int64_t bucket_of(const MeshDev::Grid &G, const double *p) {
+    int64_t q = 0, stride = 1;
+    for (int k = 0; k < D; ++k) {
+        const double g = floor((p[k] - G.lo[k]) * G.inv_h);
+        if (!(g >= 0.0 && g < (double)G.dims[k])) return -1;
+        q += (int64_t)g * stride;
+        stride *= G.dims[k];
+    }
+    return q;
+}
+
+template <int D>
+__device__ __forceinline__ double centre_d2(const MeshDev &M, int64_t c, const double *p) {
+    double d2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double dd = p[k] - M.centre[c * D + k];
+        d2 += dd * dd;
+    }
+    return d2;
+}
+
 template <int D>
 __global__ void k_mesh_find(Params P, DevState W, MeshDev M, double *air) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -120,51 +145,50 @@ __global__ void k_mesh_find(Params P, DevState W, MeshDev M, double *air) {
         if (cur >= 0 && cur < M.ncells && check_cell<D>(M, cur, p)) {
             assign<D>(M, W, i, cur);
         } else {
-            int gi[3] = {0, 0, 0};
-            bool in_grid = true;
-            for (int k = 0; k < D; ++k) {
-                const double g = floor((p[k] - M.lo[k]) * M.inv_h);
-                if (!(g >= 0.0 && g < (double)M.dims[k])) in_grid = false;
-                gi[k] = in_grid ? (int)g : 0;
-            }
-            int64_t best = -1, nearest = -1;
-            double best_d = 0.0, near_d = 0.0;
-            if (in_grid) {
-                const int64_t bucket = D == 3 ? ((int64_t)gi[2] * M.dims[1] + gi[1]) * M.dims[0] + gi[0]
-                                              : (int64_t)gi[1] * M.dims[0] + gi[0];
-                for (int64_t e = M.bucket_off[bucket]; e < M.bucket_off[bucket + 1]; ++e) {
-                    const int64_t c = M.bucket_cells[e];
-                    double d2 = 0.0;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) {
-                        const double dd = p[k] - M.centre[c * D + k];
-                        d2 += dd * dd;
-                    }
-                    if (d2 > 4.0 * M.rad2[c]) continue; /* beyond twice the bounding sphere */
-                    if (nearest < 0 || d2 < near_d || (d2 == near_d && c < nearest)) {
-                        nearest = c;
-                        near_d = d2;
-                    }
-                    if (d2 > M.rad2[c]) continue; /* outside the cell's bounding sphere */
+            /* the containing cell among those whose bounding sphere holds p, nearest centre first */
+            int64_t best = -1;
+            double best_d = 0.0;
+            const int64_t q = bucket_of<D>(M.g[0], p);
+            if (q >= 0)
+                for (int64_t e = M.g[0].off[q]; e < M.g[0].off[q + 1]; ++e) {
+                    const int64_t c = M.g[0].cells[e];
+                    const double d2 = centre_d2<D>(M, c, p);
+                    if (d2 > M.rad2[c]) continue;
                     if ((best < 0 || d2 < best_d || (d2 == best_d && c < best)) && check_cell<D>(M, c, p)) {
                         best = c;
                         best_d = d2;
                     }
                 }
-            }
             if (best >= 0) {
                 assign<D>(M, W, i, best);
-            } else if (nearest >= 0) {
-                /* outside every cell: did the particle cross the nearest cell's boundary? */
-                double cc[3] = {M.centre[nearest * D], M.centre[nearest * D + 1], D == 3 ? M.centre[nearest * D + 2] : 0.0};
-                for (int64_t e = M.cell_off[nearest]; e < M.cell_off[nearest + 1]; ++e) {
-                    const int64_t f = M.cell_faces[e];
-                    const int32_t side = M.face_right[f];
-                    if (side >= 0) continue;
-                    const bool hit = D == 2 ? seg_cross_2d(M, f, p, cc) : crosses_3d(M, f, p, cc);
-                    if (!hit) continue;
-                    if (side == -2) W.cellID[i] = kMeshLost; /* crossed the outer boundary */
-                    break;
+            } else {
+                /* outside every cell: the nearest centre among the cells whose doubled sphere
+                 * holds p, and did the particle cross that cell's boundary? */
+                int64_t nearest = -1;
+                double near_d = 0.0;
+                const int64_t q2 = bucket_of<D>(M.g[1], p);
+                if (q2 >= 0)
+                    for (int64_t e = M.g[1].off[q2]; e < M.g[1].off[q2 + 1]; ++e) {
+                        const int64_t c = M.g[1].cells[e];
+                        const double d2 = centre_d2<D>(M, c, p);
+                        if (d2 > 4.0 * M.rad2[c]) continue;
+                        if (nearest < 0 || d2 < near_d || (d2 == near_d && c < nearest)) {
+                            nearest = c;
+                            near_d = d2;
+                        }
+                    }
+                if (nearest >= 0) {
+                    double cc[3] = {M.centre[nearest * D], M.centre[nearest * D + 1],
+                                    D == 3 ? M.centre[nearest * D + 2] : 0.0};
+                    for (int64_t e = M.cell_off[nearest]; e < M.cell_off[nearest + 1]; ++e) {
+                        const int64_t f = M.cell_faces[e];
+                        const int32_t side = M.face_right[f];
+                        if (side >= 0) continue;
+                        const bool hit = D == 2 ? seg_cross_2d(M, f, p, cc) : crosses_3d(M, f, p, cc);
+                        if (!hit) continue;
+                        if (side == -2) W.cellID[i] = kMeshLost; /* crossed the outer boundary */
+                        break;
+                    }
                 }
             }
         }
@@ -200,7 +224,6 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
     /* bounding spheres: the largest distance from a cell's centre to one of its vertices */
     h.rad2.assign((size_t)nc, 0.0);
     double rmean = 0.0;
-    std::vector<double> lo(D, 1e300), hi(D, -1e300);
     for (int64_t c = 0; c < nc; ++c) {
         double r2 = 0.0;
         for (int64_t e = m.cell_face_offsets[c]; e < m.cell_face_offsets[c + 1]; ++e) {
@@ -217,50 +240,65 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
         r2 *= 1.0 + 1e-9; /* covers the rounding of the containment test at the sphere's edge */
         h.rad2[(size_t)c] = r2;
         rmean += std::sqrt(r2);
-        for (int k = 0; k < D; ++k) {
-            lo[k] = std::min(lo[k], m.cell_centres[c * D + k] - 2.0 * std::sqrt(r2));
-            hi[k] = std::max(hi[k], m.cell_centres[c * D + k] + 2.0 * std::sqrt(r2));
-        }
     }
     rmean /= double(nc);
-    /* grid edge: twice the mean radius, raised until the grid has at most 2^24 buckets */
-    double hgrid = 2.0 * rmean;
-    for (;;) {
-        double nb = 1.0;
-        for (int k = 0; k < D; ++k) nb *= std::floor((hi[k] - lo[k]) / hgrid) + 1.0;
-        if (nb <= double(1 << 24)) break;
-        hgrid *= 1.5;
-    }
-    h.h = hgrid;
-    for (int k = 0; k < 3; ++k) {
-        h.lo[k] = k < D ? lo[k] : 0.0;
-        h.dims[k] = k < D ? (int32_t)(std::floor((hi[k] - lo[k]) / hgrid) + 1.0) : 1;
-    }
-    const int64_t nbk = (int64_t)h.dims[0] * h.dims[1] * h.dims[2];
-    std::vector<int64_t> count((size_t)nbk + 1, 0);
-    auto span = [&](int64_t c, int k, int &a, int &b) { /* boxes of twice the bounding sphere */
-        const double r = 2.0 * std::sqrt(h.rad2[(size_t)c]);
-        /* one bucket of margin each side: the query's bucket index rounds differently */
-        a = std::max(0, (int)std::floor((m.cell_centres[c * D + k] - r - h.lo[k]) / hgrid) - 1);
-        b = std::min(h.dims[k] - 1, (int)std::floor((m.cell_centres[c * D + k] + r - h.lo[k]) / hgrid) + 1);
-    };
-    for (int pass = 0; pass < 2; ++pass) {
-        if (pass == 1) {
-            for (int64_t q = 0; q < nbk; ++q) count[(size_t)q + 1] += count[(size_t)q];
-            h.bucket_off = count;
-            h.bucket_cells.assign((size_t)count[(size_t)nbk], 0);
+    /* grid g (0: spheres, 1: doubled spheres) with edge h, at most 2^22 buckets; a cell is listed
+     * in every bucket its box overlaps, with the query's own bucket expression, so a point inside
+     * a sphere always finds that cell in its bucket */
+    for (int g = 0; g < 2; ++g) {
+        const double grow = g == 0 ? 1.0 : 2.0;
+        MeshHost::Grid &G = h.g[g];
+        double glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
+        for (int k = 0; k < D; ++k) {
+            glo[k] = 1e300;
+            ghi[k] = -1e300;
         }
-        std::vector<int64_t> fill = pass == 1 ? h.bucket_off : std::vector<int64_t>();
-        for (int64_t c = 0; c < nc; ++c) {
-            int a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
-            for (int k = 0; k < D; ++k) span(c, k, a[k], b[k]);
-            for (int z = a[2]; z <= b[2]; ++z)
-                for (int y = a[1]; y <= b[1]; ++y)
-                    for (int x = a[0]; x <= b[0]; ++x) {
-                        const int64_t q = ((int64_t)z * h.dims[1] + y) * h.dims[0] + x;
-                        if (pass == 0) count[(size_t)q + 1]++;
-                        else h.bucket_cells[(size_t)fill[(size_t)q]++] = c;
-                    }
+        for (int64_t c = 0; c < nc; ++c)
+            for (int k = 0; k < D; ++k) {
+                const double r = grow * std::sqrt(h.rad2[(size_t)c]);
+                glo[k] = std::min(glo[k], m.cell_centres[c * D + k] - r);
+                ghi[k] = std::max(ghi[k], m.cell_centres[c * D + k] + r);
+            }
+        double edge = grow * rmean;
+        for (;;) {
+            double nbk = 1.0;
+            for (int k = 0; k < D; ++k) nbk *= std::floor((ghi[k] - glo[k]) / edge) + 1.0;
+            if (nbk <= double(1 << 22)) break;
+            edge *= 1.25;
+        }
+        G.inv_h = 1.0 / edge;
+        for (int k = 0; k < 3; ++k) {
+            G.lo[k] = k < D ? glo[k] : 0.0;
+            G.dims[k] = k < D ? (int32_t)(std::floor((ghi[k] - glo[k]) * G.inv_h) + 1.0) : 1;
+        }
+        const int64_t nbk = (int64_t)G.dims[0] * G.dims[1] * G.dims[2];
+        auto cellq = [&](double x, int k) {
+            const double q = std::floor((x - G.lo[k]) * G.inv_h);
+            return (int)std::min(std::max(q, 0.0), (double)(G.dims[k] - 1));
+        };
+        G.off.assign((size_t)nbk + 1, 0);
+        for (int pass = 0; pass < 2; ++pass) {
+            std::vector<int64_t> fill;
+            if (pass == 1) {
+                for (int64_t q = 0; q < nbk; ++q) G.off[(size_t)q + 1] += G.off[(size_t)q];
+                G.cells.assign((size_t)G.off[(size_t)nbk], 0);
+                fill.assign(G.off.begin(), G.off.end() - 1);
+            }
+            for (int64_t c = 0; c < nc; ++c) {
+                int a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+                const double r = grow * std::sqrt(h.rad2[(size_t)c]);
+                for (int k = 0; k < D; ++k) {
+                    a[k] = cellq(m.cell_centres[c * D + k] - r, k);
+                    b[k] = cellq(m.cell_centres[c * D + k] + r, k);
+                }
+                for (int z = a[2]; z <= b[2]; ++z)
+                    for (int y = a[1]; y <= b[1]; ++y)
+                        for (int x = a[0]; x <= b[0]; ++x) {
+                            const int64_t q = ((int64_t)z * G.dims[1] + y) * G.dims[0] + x;
+                            if (pass == 0) G.off[(size_t)q + 1]++;
+                            else G.cells[(size_t)fill[(size_t)q]++] = c;
+                        }
+            }
         }
     }
     return FJSPH_OK;
