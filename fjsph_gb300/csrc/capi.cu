@@ -177,6 +177,7 @@ struct fjsph_ctx {
     /* mesh-cell air source */
     MeshDev mesh{};
     bool mesh_ready = false;
+    int32_t *mesh_list = nullptr, *mesh_count = nullptr; /* active particles of FindCell */
     std::vector<void *> mesh_allocs;
 };
 
@@ -939,7 +940,8 @@ int vlm_air(fjsph_ctx *c, const Params &P, const DevNbr &N) {
 int aero_velocity(fjsph_ctx *c, const Params &P, const DevNbr &N) {
     if (c->s.asource == FJSPH_MESH_INFL) {
         if (!c->mesh_ready) return FJSPH_E_STATE; /* fjsph_mesh_set has not run */
-        launch_mesh_find(P, WS(c), c->mesh, c->air_v, c->stream);
+        launch_mesh_find(P, WS(c), c->mesh, c->air_v, c->mesh_list, c->mesh_count, c->stream);
+        c->launches++; /* two launches: mark, then the listed particles */
     } else {
         launch_aero_velocity(P, WS(c), N, c->stream);
     }
@@ -2776,6 +2778,8 @@ int fjsph_mesh_set(fjsph_ctx *c, const fjsph_mesh *m) {
         }
     }
     if (!c->air_v) TRY(dalloc(c, &c->air_v, 3 * c->cap));
+    if (!c->mesh_list) TRY(dalloc(c, &c->mesh_list, c->cap));
+    if (!c->mesh_count) TRY(dalloc(c, &c->mesh_count, 1));
     M.ncells = nc;
     M.verts = verts;
     M.face_off = face_off;

@@ -40,8 +40,10 @@ struct MeshHost {
 };
 /* validates the mesh's index arrays and builds the bounding spheres and the bucket grid */
 int mesh_build(const fjsph_mesh &m, MeshHost &h);
-/* FindCell for the fluid slots; air[3 i + k] = the resulting cellV (the occlusion's air velocity) */
-void launch_mesh_find(const Params &P, const DevState &W, const MeshDev &M, double *air, cudaStream_t s);
+/* FindCell for the fluid slots; air[3 i + k] = the resulting cellV (the occlusion's air velocity);
+ * list (capacity slots) and count are scratch for the active particles */
+void launch_mesh_find(const Params &P, const DevState &W, const MeshDev &M, double *air, int32_t *list,
+                      int32_t *count, cudaStream_t s);
 
 /* ---- vlm.cu: vortex-lattice air source -------------------------------------------------------- */
 struct VlmDev {

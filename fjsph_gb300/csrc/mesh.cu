@@ -133,70 +133,101 @@ __device__ __forceinline__ double centre_d2(const MeshDev &M, int64_t c, const d
     return d2;
 }
 
+/* FindCell for one active particle (free, at or below the lambda cutoff, not lost) */
 template <int D>
-__global__ void k_mesh_find(Params P, DevState W, MeshDev M, double *air) {
-    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    if (W.b[i] != FJSPH_FREE || W.lam_nb[i] > P.lam_cutoff) {
-        W.cellID[i] = kNoCell;
-    } else if (W.cellID[i] != kMeshLost) {
-        double p[3] = {W.x[0][i], W.x[1][i], D == 3 ? W.x[2][i] : 0.0};
-        const int64_t cur = W.cellID[i];
-        if (cur >= 0 && cur < M.ncells && check_cell<D>(M, cur, p)) {
-            assign<D>(M, W, i, cur);
-        } else {
-            /* the containing cell among those whose bounding sphere holds p, nearest centre first */
-            int64_t best = -1;
-            double best_d = 0.0;
-            const int64_t q = bucket_of<D>(M.g[0], p);
-            if (q >= 0)
-                for (int64_t e = M.g[0].off[q]; e < M.g[0].off[q + 1]; ++e) {
-                    const int64_t c = M.g[0].cells[e];
-                    const double d2 = centre_d2<D>(M, c, p);
-                    if (d2 > M.rad2[c]) continue;
-                    if ((best < 0 || d2 < best_d || (d2 == best_d && c < best)) && check_cell<D>(M, c, p)) {
-                        best = c;
-                        best_d = d2;
-                    }
-                }
-            if (best >= 0) {
-                assign<D>(M, W, i, best);
-            } else {
-                /* outside every cell: the nearest centre among the cells whose doubled sphere
-                 * holds p, and did the particle cross that cell's boundary? */
-                int64_t nearest = -1;
-                double near_d = 0.0;
-                const int64_t q2 = bucket_of<D>(M.g[1], p);
-                if (q2 >= 0)
-                    for (int64_t e = M.g[1].off[q2]; e < M.g[1].off[q2 + 1]; ++e) {
-                        const int64_t c = M.g[1].cells[e];
-                        const double d2 = centre_d2<D>(M, c, p);
-                        if (d2 > 4.0 * M.rad2[c]) continue;
-                        if (nearest < 0 || d2 < near_d || (d2 == near_d && c < nearest)) {
-                            nearest = c;
-                            near_d = d2;
-                        }
-                    }
-                if (nearest >= 0) {
-                    double cc[3] = {M.centre[nearest * D], M.centre[nearest * D + 1],
-                                    D == 3 ? M.centre[nearest * D + 2] : 0.0};
-                    for (int64_t e = M.cell_off[nearest]; e < M.cell_off[nearest + 1]; ++e) {
-                        const int64_t f = M.cell_faces[e];
-                        const int32_t side = M.face_right[f];
-                        if (side >= 0) continue;
-                        const bool hit = D == 2 ? seg_cross_2d(M, f, p, cc) : crosses_3d(M, f, p, cc);
-                        if (!hit) continue;
-                        if (side == -2) W.cellID[i] = kMeshLost; /* crossed the outer boundary */
-                        break;
-                    }
-                }
+__device__ void find_one(const MeshDev &M, DevState &W, int64_t i) {
+    double p[3] = {W.x[0][i], W.x[1][i], D == 3 ? W.x[2][i] : 0.0};
+    const int64_t cur = W.cellID[i];
+    if (cur >= 0 && cur < M.ncells && check_cell<D>(M, cur, p)) {
+        assign<D>(M, W, i, cur);
+        return;
+    }
+    /* the containing cell among those whose bounding sphere holds p, nearest centre first */
+    int64_t best = -1;
+    double best_d = 0.0;
+    const int64_t q = bucket_of<D>(M.g[0], p);
+    if (q >= 0)
+        for (int64_t e = M.g[0].off[q]; e < M.g[0].off[q + 1]; ++e) {
+            const int64_t c = M.g[0].cells[e];
+            const double d2 = centre_d2<D>(M, c, p);
+            if (d2 > M.rad2[c]) continue;
+            if ((best < 0 || d2 < best_d || (d2 == best_d && c < best)) && check_cell<D>(M, c, p)) {
+                best = c;
+                best_d = d2;
             }
         }
+    if (best >= 0) {
+        assign<D>(M, W, i, best);
+        return;
     }
+    /* outside every cell: the nearest centre among the cells whose doubled sphere holds p, and
+     * did the particle cross that cell's boundary? */
+    int64_t nearest = -1;
+    double near_d = 0.0;
+    const int64_t q2 = bucket_of<D>(M.g[1], p);
+    if (q2 >= 0)
+        for (int64_t e = M.g[1].off[q2]; e < M.g[1].off[q2 + 1]; ++e) {
+            const int64_t c = M.g[1].cells[e];
+            const double d2 = centre_d2<D>(M, c, p);
+            if (d2 > 4.0 * M.rad2[c]) continue;
+            if (nearest < 0 || d2 < near_d || (d2 == near_d && c < nearest)) {
+                nearest = c;
+                near_d = d2;
+            }
+        }
+    if (nearest < 0) return;
+    double cc[3] = {M.centre[nearest * D], M.centre[nearest * D + 1], D == 3 ? M.centre[nearest * D + 2] : 0.0};
+    for (int64_t e = M.cell_off[nearest]; e < M.cell_off[nearest + 1]; ++e) {
+        const int64_t f = M.cell_faces[e];
+        const int32_t side = M.face_right[f];
+        if (side >= 0) continue;
+        const bool hit = D == 2 ? seg_cross_2d(M, f, p, cc) : crosses_3d(M, f, p, cc);
+        if (!hit) continue;
+        if (side == -2) W.cellID[i] = kMeshLost; /* crossed the outer boundary */
+        break;
+    }
+}
+
+template <int D>
+__device__ __forceinline__ void put_air(const DevState &W, double *air, int64_t i) {
     if (air) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) air[3 * i + k] = k < D ? W.cellV[k][i] : 0.0;
     }
+}
+
+/* first pass: inactive particles lose their cell; the active ones are listed (warp-aggregated
+ * appends), so the containment tests run on dense warps -- their FP64 work dominates */
+template <int D>
+__global__ void k_mesh_mark(Params P, DevState W, double *air, int32_t *list, int32_t *count) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    bool active = false;
+    if (i < P.n) {
+        if (W.b[i] != FJSPH_FREE || W.lam_nb[i] > P.lam_cutoff) {
+            W.cellID[i] = kNoCell;
+            put_air<D>(W, air, i);
+        } else if (W.cellID[i] == kMeshLost) {
+            put_air<D>(W, air, i);
+        } else {
+            active = true;
+        }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (active) list[base + __popc(mask & ((1u << lane) - 1u))] = (int32_t)i;
+}
+
+template <int D>
+__global__ void k_mesh_find(DevState W, MeshDev M, double *air, const int32_t *list, const int32_t *count) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= *count) return;
+    const int64_t i = list[t];
+    find_one<D>(M, W, i);
+    put_air<D>(W, air, i);
 }
 
 } // namespace
@@ -304,11 +335,19 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
     return FJSPH_OK;
 }
 
-void launch_mesh_find(const Params &P, const DevState &W, const MeshDev &M, double *air, cudaStream_t s) {
+void launch_mesh_find(const Params &P, const DevState &W, const MeshDev &M, double *air, int32_t *list,
+                      int32_t *count, cudaStream_t s) {
     const int64_t nf = P.n - P.nb;
     if (nf <= 0) return;
-    if (P.D == 2) k_mesh_find<2><<<grid_for(nf, kT), kT, 0, s>>>(P, W, M, air);
-    else k_mesh_find<3><<<grid_for(nf, kT), kT, 0, s>>>(P, W, M, air);
+    cudaMemsetAsync(count, 0, sizeof(int32_t), s);
+    const unsigned g = grid_for(nf, kT);
+    if (P.D == 2) {
+        k_mesh_mark<2><<<g, kT, 0, s>>>(P, W, air, list, count);
+        k_mesh_find<2><<<g, kT, 0, s>>>(W, M, air, list, count);
+    } else {
+        k_mesh_mark<3><<<g, kT, 0, s>>>(P, W, air, list, count);
+        k_mesh_find<3><<<g, kT, 0, s>>>(W, M, air, list, count);
+    }
 }
 
 } // namespace fjsph
