@@ -84,17 +84,21 @@ class Context:
     def settings(self, s: d.Settings) -> None:
         check("fjsph_set_settings", self._lib.fjsph_set_settings(self._h, C.byref(s)))
 
-    def upload(self, which: int, st: SPHState) -> None:
-        v = st.view()
+    def upload(self, which: int, st: SPHState, fields=None) -> None:
+        """fields: names to transfer (None = all); the device keeps its copy of the others."""
+        v = st.view(fields)
         check("fjsph_state_upload", self._lib.fjsph_state_upload(self._h, which, C.byref(v)))
 
-    def download(self, which: int = d.PNP1) -> SPHState:
-        n = C.c_int64()
-        check("fjsph_particle_count", self._lib.fjsph_particle_count(self._h, C.byref(n), None))
-        st = SPHState(n.value, self.dim)
-        v = st.view()
+    def download(self, which: int = d.PNP1, fields=None, out: SPHState | None = None) -> SPHState:
+        """The state (fields: names to transfer, None = all; out: a state of the right size to
+        fill in place)."""
+        if out is None:
+            n = C.c_int64()
+            check("fjsph_particle_count", self._lib.fjsph_particle_count(self._h, C.byref(n), None))
+            out = SPHState(n.value, self.dim)
+        v = out.view(fields)
         check("fjsph_state_download", self._lib.fjsph_state_download(self._h, which, C.byref(v)))
-        return st
+        return out
 
     def set_states(self, pn: SPHState, pnp1: SPHState) -> None:
         self.upload(d.PNP1, pnp1)

@@ -632,8 +632,9 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up, DevS
     dev_ptrs(S, c->D, dp, type);
     if (mirror) dev_ptrs(*mirror, c->D, dp2, type2);
     const int64_t n = c->n;
-    for (void *p : hp)
-        if (!p) return FJSPH_E_ARG;
+    bool any = false;
+    for (void *p : hp) any = any || p != nullptr;
+    if (!any) return FJSPH_E_ARG;
     if (!c->copy_stream) {
         CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         for (int b = 0; b < 2; ++b) {
@@ -642,15 +643,19 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up, DevS
         }
     }
     double *stage[2] = {c->stage, c->stage2};
+    int moved = 0; /* fields copied so far: null host arrays are skipped */
     for (size_t f = 0; f < dp.size(); ++f) {
-        const int b = (int)(f & 1);
+        if (!hp[f]) continue;
+        const int b = moved & 1;
+        const bool reuse = moved >= 2;
+        ++moved;
         const int comps = (int)dp[f].size();
         const int es = type[f] == 2 ? 4 : 8;
         const size_t bytes = (size_t)es * comps * n;
         FieldPtrs fp{};
         for (int k = 0; k < comps; ++k) fp.p[k] = dp[f][k];
         if (up) {
-            if (f >= 2) CU(cudaStreamWaitEvent(c->copy_stream, c->st_used[b], 0));
+            if (reuse) CU(cudaStreamWaitEvent(c->copy_stream, c->st_used[b], 0));
             CU(cudaMemcpyAsync(stage[b], hp[f], bytes, cudaMemcpyHostToDevice, c->copy_stream));
             CU(cudaEventRecord(c->st_copied[b], c->copy_stream));
             CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
@@ -660,7 +665,7 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up, DevS
                 for (int k = 0; k < comps; ++k)
                     CU(cudaMemcpyAsync(dp2[f][k], dp[f][k], (size_t)es * n, cudaMemcpyDeviceToDevice, c->stream));
         } else {
-            if (f >= 2) CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
+            if (reuse) CU(cudaStreamWaitEvent(c->stream, c->st_copied[b], 0));
             launch_field_out(stage[b], comps, es, c->key, fp, n, c->stream);
             CU(cudaEventRecord(c->st_used[b], c->stream));
             CU(cudaStreamWaitEvent(c->copy_stream, c->st_used[b], 0));

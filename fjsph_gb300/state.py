@@ -12,6 +12,10 @@ import numpy as np
 
 from ._cdefs import VIEW_F64, VIEW_I32, VIEW_I64, StateView, Block, DEFAULT_VAL, MAX_TIMES
 
+# the fields a step reads before writing them (FJSPH_STEP_FIELDS of the C header)
+STEP_FIELDS = ("xi", "v", "acc", "Rrho", "rho", "p", "m", "cellV", "cellP", "cellRho", "vPert", "aVisc", "deltaD",
+               "woccl", "lam", "lam_nb", "curve", "norm", "norm_curve", "b", "part_id", "cellID", "surf", "surfzone")
+
 VECTOR_FIELDS = ["xi", "v", "acc", "Af", "aVisc", "cellV", "gradRho", "norm", "vPert"]
 MATRIX_FIELDS = ["L"]
 SCALAR_FIELDS = ["Rrho", "rho", "p", "m", "curve", "norm_curve", "woccl", "pDist", "deltaD", "cellP", "cellRho",
@@ -44,19 +48,30 @@ class SPHState:
             setattr(out, f, getattr(self, f).copy())
         return out
 
-    def view(self) -> StateView:
-        """ctypes view over this state's arrays (valid while the arrays are alive and unchanged)."""
+    def view(self, fields=None) -> StateView:
+        """ctypes view over this state's arrays (valid while the arrays are alive and unchanged);
+        with `fields`, only those names (the others stay null: transfers skip them)."""
         v = StateView()
         v.n = self.n
+        if fields is not None:
+            unknown = set(fields) - set(VIEW_F64) - set(VIEW_I64) - set(VIEW_I32)
+            if unknown:
+                raise KeyError(f"unknown state fields {sorted(unknown)}")
         for f in VIEW_F64:
+            if fields is not None and f not in fields:
+                continue
             a = getattr(self, f)
             assert a.dtype == np.float64 and a.flags.c_contiguous
             setattr(v, f, a.ctypes.data_as(C.POINTER(C.c_double)))
         for f in VIEW_I64:
+            if fields is not None and f not in fields:
+                continue
             a = getattr(self, f)
             assert a.dtype == np.int64 and a.flags.c_contiguous
             setattr(v, f, a.ctypes.data_as(C.POINTER(C.c_int64)))
         for f in VIEW_I32:
+            if fields is not None and f not in fields:
+                continue
             a = getattr(self, f)
             assert a.dtype == np.int32 and a.flags.c_contiguous
             setattr(v, f, a.ctypes.data_as(C.POINTER(C.c_int32)))

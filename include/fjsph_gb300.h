@@ -67,8 +67,8 @@ enum fjsph_solver { FJSPH_NEWMARK_BETA = 0, FJSPH_RUNGE_KUTTA = 1 };
 enum fjsph_bound_solver { FJSPH_DBC = 0, FJSPH_PRESSURE_G = 1, FJSPH_GHOST = 2 };
 enum fjsph_eos { FJSPH_COLE_EOS = 0, FJSPH_ISO_EOS = 1 };
 enum fjsph_aero_case { FJSPH_NOAERO = 0, FJSPH_GISSLER = 1, FJSPH_INDUCED_PRESSURE = 2, FJSPH_SKIN_FRIC = 3 };
-/* Air velocity source (src/VarDefs.h:168-173): uniform v_inf, mesh cells (not built), the
- * vortex-lattice field of fjsph_vlm_setup (3D). */
+/* Air velocity source (src/VarDefs.h:168-173): uniform v_inf, the cells of the mesh given to
+ * fjsph_mesh_set, the vortex-lattice field of fjsph_vlm_setup (3D). */
 enum fjsph_aero_source { FJSPH_CONST_VEL = 0, FJSPH_MESH_INFL = 1, FJSPH_VLM_INFL = 2 };
 
 /* Arithmetic form of the pair kernels. */
@@ -198,9 +198,22 @@ int fjsph_get_inlet(fjsph_ctx *ctx, fjsph_inlet *inlet); /* current tables, refe
 int fjsph_get_limits(fjsph_ctx *ctx, fjsph_block *blocks, int32_t max_blocks, int32_t *nblocks);
 /* Particles inserted and deleted by update_data since the context was created. */
 int fjsph_update_counts(fjsph_ctx *ctx, int64_t *inserted, int64_t *deleted);
-/* Replaces the SPHState hand-over between Integrator and its callers (src/Integration.h:15-68). */
+/* Replaces the SPHState hand-over between Integrator and its callers (src/Integration.h:15-68).
+ * A null array in the view skips that field: an upload leaves the device copy as it is, a
+ * download leaves the host array unwritten (at least one array must be given).  Every field a
+ * step reads before writing it (FJSPH_STEP_FIELDS below) has to be uploaded before the first
+ * step; the others are recomputed inside the step. */
 int fjsph_state_upload(fjsph_ctx *ctx, int32_t which, const fjsph_state_view *st);
 int fjsph_state_download(fjsph_ctx *ctx, int32_t which, fjsph_state_view *st);
+/* The fields a step reads before it writes them: positions, velocities, the previous step's
+ * acceleration and density rate (Runge-Kutta and Newmark-Beta weights), density, pressure,
+ * mass, the air cell values, the shifting velocity, the frozen dissipation terms and the
+ * previous surface detection (the first stage uses them, src/Runge_Kutta.cpp:461-476), the
+ * particle type, id and cell.  The rest (Af, gradRho, L, kernsum, colour, colourG, pDist) is
+ * recomputed before it is read. */
+#define FJSPH_STEP_FIELDS \
+    "xi v acc Rrho rho p m cellV cellP cellRho vPert aVisc deltaD woccl lam lam_nb curve norm norm_curve " \
+    "b part_id cellID surf surfzone"
 int fjsph_particle_count(fjsph_ctx *ctx, int64_t *n_total, int64_t *n_bound);
 
 /* ---- neighbour search (src/Neighbours.cpp:7-47) ------------------------------------------- */
