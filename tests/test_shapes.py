@@ -214,3 +214,30 @@ def test_reference_examples_build():
         assert c.state.n > 0 and np.all(np.isfinite(c.state.xi)), rel
     c = load_case(REF_EXAMPLES / "Standing_Column/para", 2)
     assert [b.second - b.first for b in c.blocks] == [840, 417, 840, 19800]
+
+
+def test_grid_scale_matches_oracle():
+    """A grid scale multiplies the block coordinates and plane constants (not radii or lengths,
+    shapes.cpp:24-49)."""
+    st, blocks, inlets, g, ref = _compare(2, (GOLD / "2d_bound.bmap").read_text(), (GOLD / "2d_fluid.bmap").read_text(),
+                                          scale=1.5)
+    jet = [b for b in blocks if b.name == "Jet"][0]
+    assert jet.delconst == pytest.approx(4.5)  # 3.0 scaled
+
+
+def test_json_coordinates_and_motion(tmp_path):
+    import json
+    from fjsph_gb300.geometry import build_particles
+    s = _settings(2)
+    data = {"Pts": {"Shape": "Coordinates", "Coordinate data": [[0.0, 0.0], [0.5, 0.25], [1.0, 0.5]]},
+            "Lid": {"Shape": "Line", "Start coordinates": [0.0, 2.0], "End coordinates": [1.0, 2.0],
+                    "Wall radial particle count": 1, "Time data": [0.0, 1.0, 2.0],
+                    "Position data": [[0.0, 2.0], [0.5, 2.0], [0.5, 2.5]]}}
+    fl = {"W": {"Shape": "Square", "Start coordinates": [3.0, 0.0], "End coordinates": [3.3, 0.3]}}
+    (tmp_path / "b.json").write_text(json.dumps(data))
+    (tmp_path / "f.json").write_text(json.dumps(fl))
+    st, blocks, inlets, g = build_particles(s, tmp_path / "b.json", tmp_path / "f.json")
+    np.testing.assert_allclose(st.xi[:3], [[0.0, 0.0], [0.5, 0.25], [1.0, 0.5]], atol=0)
+    lid = blocks[1]
+    assert lid.times == [0.0, 1.0, 2.0]
+    assert lid.vels[0] == pytest.approx((0.5, 0.0, 0.0)) and lid.vels[1] == pytest.approx((0.0, 0.5, 0.0))
