@@ -255,6 +255,7 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
     /* bounding spheres: the largest distance from a cell's centre to one of its vertices */
     h.rad2.assign((size_t)nc, 0.0);
     double rmean = 0.0;
+    int64_t nvalid = 0;
     for (int64_t c = 0; c < nc; ++c) {
         double r2 = 0.0;
         for (int64_t e = m.cell_face_offsets[c]; e < m.cell_face_offsets[c + 1]; ++e) {
@@ -269,10 +270,18 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
             }
         }
         r2 *= 1.0 + 1e-9; /* covers the rounding of the containment test at the sphere's edge */
+        /* a cell with a vertex at a fill value (e.g. NetCDF's 9.97e36) contains nothing: no
+         * candidate, no grid entry */
+        if (!(r2 < 1e60)) {
+            h.rad2[(size_t)c] = -1.0;
+            continue;
+        }
         h.rad2[(size_t)c] = r2;
         rmean += std::sqrt(r2);
+        ++nvalid;
     }
-    rmean /= double(nc);
+    if (nvalid == 0) return FJSPH_E_ARG;
+    rmean /= double(nvalid);
     /* grid g (0: spheres, 1: doubled spheres) with edge h, at most 2^22 buckets; a cell is listed
      * in every bucket its box overlaps, with the query's own bucket expression, so a point inside
      * a sphere always finds that cell in its bucket */
@@ -286,6 +295,7 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
         }
         for (int64_t c = 0; c < nc; ++c)
             for (int k = 0; k < D; ++k) {
+                if (h.rad2[(size_t)c] < 0.0) break;
                 const double r = grow * std::sqrt(h.rad2[(size_t)c]);
                 glo[k] = std::min(glo[k], m.cell_centres[c * D + k] - r);
                 ghi[k] = std::max(ghi[k], m.cell_centres[c * D + k] + r);
@@ -316,6 +326,7 @@ int mesh_build(const fjsph_mesh &m, MeshHost &h) {
                 fill.assign(G.off.begin(), G.off.end() - 1);
             }
             for (int64_t c = 0; c < nc; ++c) {
+                if (h.rad2[(size_t)c] < 0.0) continue;
                 int a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
                 const double r = grow * std::sqrt(h.rad2[(size_t)c]);
                 for (int k = 0; k < D; ++k) {

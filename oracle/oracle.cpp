@@ -2289,7 +2289,8 @@ int orc_mesh_set(orc_sim *o, const fjsph_mesh *m) {
                 r2 = std::max(r2, d2);
             }
         }
-        o->m_rad2[c] = r2 * (1.0 + 1e-9);
+        r2 *= 1.0 + 1e-9;
+        o->m_rad2[c] = r2 < 1e60 ? r2 : -1.0; /* a vertex at a fill value: the cell contains nothing */
     }
     return FJSPH_OK;
 }

@@ -80,6 +80,31 @@ def test_droplet_steps_match_oracle(dim):
     assert_fields(g, o, ["xi", "v", "rho", "p", "Af"], RTOL_STEP, slice(0, None), label=f"mesh {dim}d")
 
 
+def test_fill_value_cells_contain_nothing():
+    """Cells with a vertex at a fill value (NetCDF's 9.97e36, as in the RAE2822 example's far field)
+    are never candidates, on the device as in the oracle."""
+    c, mesh = cases.droplet_in_mesh(2)
+    m = mesh
+    m.verts = m.verts.copy()
+    top = m.verts[:, 1] > 2.9e-3
+    m.verts[top, 1] = 9.969209968386869e36
+    fo, fv, co, cf = m.face_offsets, m.face_verts, m.cell_face_offsets, m.cell_faces
+    for cc in range(m.n_cells):  # centres as the reader makes them: vertex averages
+        vs = np.unique([fv[q] for f in cf[co[cc]:co[cc + 1]] for q in range(fo[f], fo[f + 1])])
+        m.centres[cc] = m.verts[vs].mean(axis=0)
+    rng = np.random.Generator(np.random.PCG64(31))
+    st = _points(c, rng.uniform((-2e-3, -2e-3), (6e-3, 3e-3), size=(3000, 2)))
+    ctx, orc = _pair(c, m, st, [BlockSpec(0, st.n, True, name="fluid")])
+    for h in (ctx, orc):
+        h.update_neighbours()
+        h.get_aero_velocity()
+    g, o = ctx.download(), orc.download()
+    np.testing.assert_array_equal(g.cellID, o.cellID)
+    np.testing.assert_array_equal(g.cellV, o.cellV)
+    near_top = st.xi[:, 1] > 3e-3 - 5e-3 / 35 + 1e-9  # the top row of cells, now fill cells
+    assert np.all(g.cellID[near_top] < 0) and (g.cellID[~near_top] >= 0).mean() > 0.9
+
+
 def test_leaving_particles_are_deleted():
     c, mesh = cases.droplet_in_mesh(2)
     st = c.state.copy()
