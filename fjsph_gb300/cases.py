@@ -33,6 +33,7 @@ class Case:
     state: SPHState
     blocks: list[BlockSpec]
     inlets: list[InletSpec] = field(default_factory=list)
+    mesh: object = None  # the air mesh of a mesh-source case (fjsph_gb300.mesh.CellMesh)
 
     @property
     def n_fluid(self) -> int:

@@ -207,9 +207,11 @@ def build_particles(settings: d.Settings, boundary, fluid):
     return g.state(), g.blocks(), g.inlets(), g
 
 
-def load_case(para, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE, name: str | None = None):
+def load_case(para, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE, name: str | None = None,
+              tau_solution: str | None = None):
     """A reference case directory's starting point: settings from `para` and the particles of the
-    fluid and boundary block files it names."""
+    fluid and boundary block files it names; for a 2D TAU mesh case also the air mesh (the
+    solution file from the para's "Restart-data prefix", or `tau_solution`)."""
     from .cases import Case
     from .settings import read_para
     para = Path(para)
@@ -221,4 +223,12 @@ def load_case(para, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE, n
         raise ValueError("the para file names no fluid or boundary definition file")
     st, blocks, inlets, g = build_particles(s, root / bound_file, root / fluid_file)
     g.close()
-    return Case(name or para.parent.name, s, st, blocks, inlets)
+    mesh = None
+    if s.asource == d.MESH_INFL and dim == 2:
+        from .tau import read_tau_2d
+        sol = tau_solution or extra.get("tau_sol")
+        if not sol:
+            raise ValueError("the para file names a TAU grid but no solution file")
+        axis = int(str(extra.get("offset_axis", "2")).split()[0] or 2)
+        mesh = read_tau_2d(root / extra["tau_mesh"], root / sol, offset_axis=axis, scale=s.scale)
+    return Case(name or para.parent.name, s, st, blocks, inlets, mesh)

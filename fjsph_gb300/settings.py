@@ -79,6 +79,10 @@ PARA_KEYS = {
     "VLM definition filename": ("vlm_file", "s"),
     "Input fluid definition filename": ("input_fluid_file", "s"),
     "Input boundary definition filename": ("input_bound_file", "s"),
+    "Primary grid face filename": ("tau_mesh", "s"),
+    "Restart-data prefix": ("tau_sol", "s"),
+    "Boundary mapping filename": ("tau_bmap", "s"),
+    "2D offset vector (0 / x=1,y=2,z=3)": ("offset_axis", "s"),
 }
 
 AERO_CASES = {"(none)": d.NOAERO, "Gissler": d.GISSLER, "Induced_pressure": d.INDUCED_PRESSURE,
@@ -147,8 +151,11 @@ def apply_para(s: d.Settings, kv: dict) -> dict:
         if extra["aero_case"] not in AERO_CASES:
             raise ValueError("Aerodynamic coupling model is not defined or correct.")
         s.acase = AERO_CASES[extra["aero_case"]]
-    # air source (src/IO.cpp:466-480): a VLM definition file selects the vortex lattice in 3D
-    if extra.get("vlm_file") and s.dim == 3:
+    # air source (src/IO.cpp:462-500): a TAU grid file selects the mesh cells, else a VLM
+    # definition file the vortex lattice (3D)
+    if extra.get("tau_mesh"):
+        s.asource = d.MESH_INFL
+    elif extra.get("vlm_file") and s.dim == 3:
         s.asource = d.VLM_INFL
     return extra
 

@@ -64,3 +64,22 @@ def test_cell_centres_are_inside_their_cells(mesh):
     out = o.download()
     np.testing.assert_array_equal(out.cellID[:-2], idx)
     np.testing.assert_array_equal(out.cellV[:-2], mesh.vel[idx])
+
+
+def test_rae2822_case_steps_on_the_oracle():
+    """Examples/RAE2822 as shipped (para, block files, TAU mesh; the solution file named here
+    because the para names none): the liquid jet near the aerofoil takes its air from the mesh
+    cells and steps."""
+    from fjsph_gb300.geometry import load_case
+    from oracle.pyoracle import Oracle
+    c = load_case(EX / "para", 2, tau_solution="sol.pval.10000")
+    assert c.settings.asource == d.MESH_INFL and c.mesh is not None and c.mesh.n_cells == 23552
+    o = Oracle(c.settings, c.blocks, c.inlets)
+    o.mesh_set(c.mesh)
+    o.set_states(c.state, c.state)
+    for _ in range(5):
+        o.integrate()
+    st = o.download()
+    assert np.all(np.isfinite(st.xi))
+    fl = st.b == d.FREE
+    assert (st.cellID[fl] >= 0).sum() > 0 or fl.sum() == 0
