@@ -224,7 +224,14 @@ def load_case(para, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE, n
     st, blocks, inlets, g = build_particles(s, root / bound_file, root / fluid_file)
     g.close()
     mesh = None
-    if s.asource == d.MESH_INFL and dim == 2:
+    if s.asource == d.MESH_INFL and extra.get("foam_dir"):
+        from .foam import read_foam
+        if dim != 3:
+            raise ValueError("OpenFOAM meshes are read in 3D only (as upstream)")
+        mesh = read_foam(root / extra["foam_dir"], extra.get("foam_sol", ""),
+                         buoyant=str(extra.get("foam_buoyant", "0")).strip().startswith("1"), rho=s.rho_g,
+                         scale=s.scale)
+    elif s.asource == d.MESH_INFL and dim == 2:
         from .tau import read_tau_2d
         sol = tau_solution or extra.get("tau_sol")
         if not sol:

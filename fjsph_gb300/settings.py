@@ -83,6 +83,9 @@ PARA_KEYS = {
     "Restart-data prefix": ("tau_sol", "s"),
     "Boundary mapping filename": ("tau_bmap", "s"),
     "2D offset vector (0 / x=1,y=2,z=3)": ("offset_axis", "s"),
+    "OpenFOAM input directory": ("foam_dir", "s"),
+    "OpenFOAM solution directory": ("foam_sol", "s"),
+    "OpenFOAM buoyant (0/1)": ("foam_buoyant", "s"),
 }
 
 AERO_CASES = {"(none)": d.NOAERO, "Gissler": d.GISSLER, "Induced_pressure": d.INDUCED_PRESSURE,
@@ -153,7 +156,7 @@ def apply_para(s: d.Settings, kv: dict) -> dict:
         s.acase = AERO_CASES[extra["aero_case"]]
     # air source (src/IO.cpp:462-500): a TAU grid file selects the mesh cells, else a VLM
     # definition file the vortex lattice (3D)
-    if extra.get("tau_mesh"):
+    if extra.get("tau_mesh") or extra.get("foam_dir"):
         s.asource = d.MESH_INFL
     elif extra.get("vlm_file") and s.dim == 3:
         s.asource = d.VLM_INFL
