@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=2_000_000, help="target particle count of the jet")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the plain FP64 form timed beside (0 = skip)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--vlm-points", type=int, default=1 << 20, help="points of the VLM air-source timing (0 = skip)")
     ap.add_argument("--mesh-cell", type=float, default=8e-4,
                     help="cube edge of the tetrahedral air mesh over the jet (0 = skip)")
