@@ -40,3 +40,21 @@ def test_reference_examples_parse(built_lib):
     assert s3.acase == d.GISSLER
     assert list(s3.v_inf) == [128.5, 0.0, 0.0]
     assert s3.rho_g == pytest.approx(1.2262)
+
+
+def test_mesh_source_keys(tmp_path):
+    """A TAU grid or an OpenFOAM directory in the para file selects the mesh-cell air source
+    (src/IO.cpp:462-500); a VLM definition selects the vortex lattice only without them."""
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300.settings import read_para
+    base = "SPH initial spacing: 0.01\nVLM definition filename: (thisfile)\n"
+    cases = {"Primary grid face filename: mesh.grid\n2D offset vector (0 / x=1,y=2,z=3): 2\n": d.MESH_INFL,
+             "OpenFOAM input directory: foam\nOpenFOAM solution directory: 100\n": d.MESH_INFL,
+             "": d.VLM_INFL}
+    for extra_lines, want in cases.items():
+        p = tmp_path / "para"
+        p.write_text(base + extra_lines)
+        s, extra = read_para(p, 3)
+        assert s.asource == want, extra_lines
+    s, extra = read_para(p, 2)
+    assert s.asource == d.CONST_VEL  # the vortex lattice is 3D only
