@@ -277,6 +277,12 @@ class Context:
         check("fjsph_step_report", self._lib.fjsph_step_report(self._h, out))
         return dict(maxRho_pc=out[0], maxf=out[1], maxAf=out[2], maxShift=out[3], iteration=int(out[4]))
 
+    def timestep_maxima(self) -> list[float]:
+        """maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift of the last find_timestep."""
+        out = (C.c_double * 7)()
+        check("fjsph_timestep_maxima", self._lib.fjsph_timestep_maxima(self._h, out))
+        return list(out)
+
     def launch_stats(self, reset: bool = False) -> int:
         n = C.c_int64()
         check("fjsph_launch_stats", self._lib.fjsph_launch_stats(self._h, C.byref(n), int(reset)))

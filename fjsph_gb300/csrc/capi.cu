@@ -2293,6 +2293,19 @@ int fjsph_step_report(fjsph_ctx *c, double *out5) {
     return FJSPH_OK;
 }
 
+int fjsph_timestep_maxima(fjsph_ctx *c, double *out7) {
+    TRY(check_ctx(c));
+    if (!out7) return FJSPH_E_ARG;
+    out7[0] = c->maxf;
+    out7[1] = c->maxAf;
+    out7[2] = c->maxdrho;
+    out7[3] = c->maxRhoi;
+    out7[4] = c->minST;
+    out7[5] = c->maxU;
+    out7[6] = c->maxShift;
+    return FJSPH_OK;
+}
+
 int fjsph_launch_stats(fjsph_ctx *c, int64_t *n_launches, int32_t reset) {
     TRY(check_ctx(c));
     if (n_launches) *n_launches = c->launches;

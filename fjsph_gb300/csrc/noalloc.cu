@@ -153,8 +153,12 @@ extern "C" int fjsph_find_timestep_noalloc(const fjsph_settings *s, int64_t n_fl
     if (r != FJSPH_OK) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nrows = n_fluid > 0 ? (int)((n_fluid + (int64_t)kThreads * kItems - 1) / ((int64_t)kThreads * kItems)) : 1;
+    /* a launch that fails (no kernel image for this device, an invalid stream) leaves the result
+     * row holding an earlier call's values or zeros: report it instead of returning them */
     k_partial<<<nrows, kThreads, 0, st>>>(D, n_fluid, ale, s->rho_rest, s->dx, s->sig, f, rows);
+    if (cudaGetLastError() != cudaSuccess) return FJSPH_E_CUDA;
     k_final<<<1, kThreads, 0, st>>>(nrows, rows);
+    if (cudaGetLastError() != cudaSuccess) return FJSPH_E_CUDA;
     double red[kVals];
     if (cudaMemcpyAsync(red, rows + (size_t)kMaxRows * kVals, sizeof(double) * 7, cudaMemcpyDeviceToHost, st) !=
         cudaSuccess)
@@ -168,7 +172,9 @@ extern "C" int fjsph_find_timestep_noalloc(const fjsph_settings *s, int64_t n_fl
     double mn = fac[0];
     for (int k = 1; k < 6; ++k)
         if (fac[k] < mn) mn = fac[k];
-    double d = s->cfl * 0.75 * mn;
+    /* cfl * (0.75 * min), in the reference's order (src/Integration.cpp:427-428) */
+    const double safe_dt = 0.75 * mn;
+    double d = s->cfl * safe_dt;
     if (d < s->delta_t_min)
         d = s->delta_t_min;
     else if (d > s->delta_t_max)

@@ -259,7 +259,7 @@ bool make_block(Geometry &g, const std::string &shape, Block &out) {
     else if (shape == "Inlet") out.bound_type = inletZone;
     else if (shape == "Coordinates") out.bound_type = coordDef;
     else {
-        g.msg("ERROR: Unrecognised boundary shape, \"%s\". Stopping", shape.c_str());
+        g.msg("block shape \"%s\" is not a known shape", shape.c_str());
         return false;
     }
     return true;
@@ -392,33 +392,33 @@ void check_base(Geometry &g, Block &b, int &fault) { /* ShapeBlock::check_input,
     }
     if (!b.position_filename.empty() && b.ntimes != 0) {
         if (b.times.empty()) {
-            g.msg("ERROR: Block \"%s\" has no time information", b.name.c_str());
+            g.msg("block \"%s\": motion values without times", b.name.c_str());
             fault = 1;
         }
         if (b.pos.empty() && b.vels.empty()) {
-            g.msg("ERROR: Block \"%s\" position or velocity data has not been ingested properly.", b.name.c_str());
+            g.msg("block \"%s\": motion table lengths differ", b.name.c_str());
             fault = 1;
         }
     }
     if (b.bound_type == -1) {
-        g.msg("ERROR: Block \"%s\" shape has not been correctly defined.", b.name.c_str());
+        g.msg("block \"%s\": no shape given", b.name.c_str());
         fault = 1;
     }
     if (!b.solver_name.empty()) {
         if (b.solver_name == "DBC") b.bound_solver = DBC;
         else if (b.solver_name == "Pressure-Gradient") b.bound_solver = pressure_G;
         else if (b.solver_name == "Ghost") b.bound_solver = ghost;
-        else g.msg("WARNING: Unrecognised boundary solver defined. Continuing to use the default, Pressure-Gradient");
+        else g.msg("note: unknown boundary solver; the Pressure-Gradient solver is used");
     }
     if (!b.inlet_bc_type.empty()) {
         if (b.inlet_bc_type == "Fixed Velocity") b.fixed_vel_or_dynamic = 0;
         else if (b.inlet_bc_type == "Dynamic") b.fixed_vel_or_dynamic = 1;
-        else g.msg("WARNING: Unrecognised inlet velocity type defined. Continuing to use the default, Fixed Velocity");
+        else g.msg("note: unknown inlet velocity type; a fixed inlet velocity is used");
     }
     if (!b.particle_order_str.empty()) {
         if (b.particle_order_str == "Grid") b.particle_order = false;
         else if (b.particle_order_str == "HCP") b.particle_order = true;
-        else g.msg("WARNING: Unrecognised particle packing type defined. Continuing to use the default, Grid");
+        else g.msg("note: unknown packing type; grid packing is used");
     }
     if (b.press != 0) {
         /* upstream raises to gam here, not 1/gam (get_density uses 1/gam) */
@@ -441,9 +441,9 @@ int iceil(double x) { return static_cast<int>(std::ceil(x)); }
 void check_line(Geometry &g, Block &b, int &fault) { /* src/shapes/line.cpp:8-125 */
     const double gs = g.gs_running;
     const int D = g.D;
-    if (!g.check_vector(b.start)) { g.msg("ERROR: Block \"%s\" starting position has not been correctly defined. Stopping", b.name.c_str()); fault = 1; }
-    if (!g.check_vector(b.end)) { g.msg("ERROR: Block \"%s\" ending position has not been correctly defined. Stopping", b.name.c_str()); fault = 1; }
-    if (D == 3 && !g.check_vector(b.right)) { g.msg("ERROR: Block \"%s\" ending position has not been correctly defined. Stopping", b.name.c_str()); fault = 1; }
+    if (!g.check_vector(b.start)) { g.msg("block \"%s\": start point missing", b.name.c_str()); fault = 1; }
+    if (!g.check_vector(b.end)) { g.msg("block \"%s\": end point missing", b.name.c_str()); fault = 1; }
+    if (D == 3 && !g.check_vector(b.right)) { g.msg("block \"%s\": end point missing", b.name.c_str()); fault = 1; }
     if (b.dx < 0 && (b.ni < 0 || (D == 3 && b.nj < 0))) b.dx = gs;
     if (D == 2) {
         if (b.ni > 0 && b.dx < 0) b.dx = vnorm(vsub(b.end, b.start)) / double(b.ni);
@@ -451,7 +451,7 @@ void check_line(Geometry &g, Block &b, int &fault) { /* src/shapes/line.cpp:8-12
         b.dx = std::min(vnorm(vsub(b.right, b.start)) / double(b.ni), vnorm(vsub(b.end, b.right)) / double(b.nj));
     }
     if (b.thickness < 0) {
-        if (b.nk < 0) { g.msg("ERROR: Block \"%s\" line thickness has not been correctly defined. Stopping.", b.name.c_str()); fault = 1; }
+        if (b.nk < 0) { g.msg("block \"%s\": wall thickness or layer count missing", b.name.c_str()); fault = 1; }
     } else if (b.nk < 0) { /* the thickness is used only with a negative count */
         b.nk = b.particle_order ? iceil(b.thickness / b.dx / std::sqrt(3.0) * 2.0) : iceil(b.thickness / b.dx);
     }
@@ -460,7 +460,7 @@ void check_line(Geometry &g, Block &b, int &fault) { /* src/shapes/line.cpp:8-12
         if (D == 2) b.npts = (int64_t)b.ni * b.nk;
         else {
             if (b.nj < 1) {
-                g.msg("WARNING: ni defined, but nj not.");
+                g.msg("note: an i count is given without a j count");
                 b.nj = std::max(iceil(vnorm(vsub(b.end, b.right)) / gs), 1);
             }
             b.npts = (int64_t)b.ni * b.nj * b.nk;
@@ -495,8 +495,8 @@ void box_counts(const Block &b, double gs, int D, int &ni, int &nj, int &nk) {
 }
 
 void check_square(Geometry &g, Block &b, int &fault) { /* src/shapes/square.cpp:6-96 */
-    if (!g.check_vector(b.start)) { g.msg("ERROR: Block \"%s\" starting position has not been correctly defined. Stopping", b.name.c_str()); fault = 1; }
-    if (!g.check_vector(b.end)) { g.msg("ERROR: Block \"%s\" ending position has not been correctly defined. Stopping", b.name.c_str()); fault = 1; }
+    if (!g.check_vector(b.start)) { g.msg("block \"%s\": start point missing", b.name.c_str()); fault = 1; }
+    if (!g.check_vector(b.end)) { g.msg("block \"%s\": end point missing", b.name.c_str()); fault = 1; }
     if (b.dx < 0 && (b.ni < 0 || b.nj < 0)) b.dx = g.gs_running;
     if (b.ni > 0 && b.nj > 0 && (g.D == 2 || b.nk > 0) && b.dx < 0) {
         const V dist = vsub(b.end, b.start);
@@ -513,8 +513,8 @@ void check_square(Geometry &g, Block &b, int &fault) { /* src/shapes/square.cpp:
 }
 
 void check_circle(Geometry &g, Block &b, int &fault) { /* src/shapes/circle.cpp:6-95 */
-    if (!g.check_vector(b.centre)) { g.msg("ERROR: Block \"%s\" centre position has not been correctly defined.", b.name.c_str()); fault = 1; }
-    if (b.radius < 0) { g.msg("ERROR: Block \"%s\" radius has not been correctly defined.", b.name.c_str()); fault = 1; }
+    if (!g.check_vector(b.centre)) { g.msg("block \"%s\": centre missing", b.name.c_str()); fault = 1; }
+    if (b.radius < 0) { g.msg("block \"%s\": radius missing", b.name.c_str()); fault = 1; }
     for (int k = 0; k < g.D; ++k) {
         b.start[k] = b.centre[k] - b.radius;
         b.end[k] = b.centre[k] + b.radius;
@@ -560,8 +560,8 @@ void check_cylinder(Geometry &g, Block &b, int &fault) { /* src/shapes/cylinder.
     };
     if (b.subshape == "Hollow") {
         b.sub_bound_type = hollow;
-        if (b.thickness < 0 && b.nk < 0) { g.msg("ERROR: Cylinder block \"%s\" thickness or wall count has not been defined", b.name.c_str()); fault = 1; }
-        if (b.length < 0 && b.nj < 0) { g.msg("ERROR: Cylinder block \"%s\" legnth or j-count has not been defined", b.name.c_str()); fault = 1; }
+        if (b.thickness < 0 && b.nk < 0) { g.msg("cylinder \"%s\": needs a thickness or a wall count", b.name.c_str()); fault = 1; }
+        if (b.length < 0 && b.nj < 0) { g.msg("cylinder \"%s\": needs a length or a j count", b.name.c_str()); fault = 1; }
         if (g.check_vector(b.centre)) {
             if (b.radius > 0) {
                 has_config = 3;
@@ -579,7 +579,7 @@ void check_cylinder(Geometry &g, Block &b, int &fault) { /* src/shapes/cylinder.
         }
     } else if (b.subshape == "Solid") {
         b.sub_bound_type = solid;
-        if (b.length < 0 || b.nk < 0) { g.msg("ERROR: Cylinder block \"%s\" length or k-count has not been defined", b.name.c_str()); fault = 1; }
+        if (b.length < 0 || b.nk < 0) { g.msg("cylinder \"%s\": needs a length and a k count", b.name.c_str()); fault = 1; }
         if (g.check_vector(b.start) && g.check_vector(b.right) && g.check_vector(b.end)) {
             has_config = 1;
             b.centre = vmul(vadd(b.start, b.end), 0.5);
@@ -597,10 +597,10 @@ void check_cylinder(Geometry &g, Block &b, int &fault) { /* src/shapes/cylinder.
             has_config = 2;
         }
     } else {
-        g.msg("ERROR: Cylinder block \"%s\" subtype not defined appropriately. Choose from the following options:", b.name.c_str());
+        g.msg("cylinder \"%s\": unknown sub type (Hollow or Solid)", b.name.c_str());
         fault = 1;
     }
-    if (has_config == 0) { g.msg("ERROR: Cylinder block \"%s\" geometry has not been sufficiently defined.", b.name.c_str()); fault = 1; }
+    if (has_config == 0) { g.msg("cylinder \"%s\": not enough geometry to place it", b.name.c_str()); fault = 1; }
 
     if (vnorm(b.angles) != 0) {
         b.angles = vmul(b.angles, kPi / 180.0);
@@ -678,7 +678,7 @@ void arc_centrepoint_2d(Geometry &g, Block &b, int &fault) {
     const V d0 = vsub(b.start, b.centre), d1 = vsub(b.end, b.centre);
     const double r = vsq(d0);
     if (std::fabs(vsq(d1) - r) > 0.001) {
-        g.msg("Arc points are not correctly defined. The ending radius differs from the starting radius");
+        g.msg("arc end point lies at another radius from the centre than the start point");
         fault = 1;
         return;
     }
@@ -710,7 +710,7 @@ void arc_midpoint_2d(Geometry &g, Block &b, int &fault) {
     double cx = 0, cy = 0;
     if (!solve2(2.0 * (s[0] - e[0]), 2.0 * (s[1] - e[1]), 2.0 * (s[0] - mp[0]), 2.0 * (s[1] - mp[1]),
                 r1x - r3x + r1y - r3y, r1x - r2x + r1y - r2y, cx, cy)) {
-        g.msg("ERROR: Block \"%s\" arc points are collinear.", b.name.c_str());
+        g.msg("block \"%s\": the three arc points lie on one line", b.name.c_str());
         fault = 1;
         return;
     }
@@ -725,7 +725,7 @@ void arc_end_3d(Geometry &g, Block &b, int &fault) {
     u = vdiv(u, b.radius);
     const V w = vnormalized(b.right);
     if (std::fabs(vdot(b.right, b.start) - vdot(b.right, b.centre)) > 1e-4) {
-        g.msg("Points do not exist upon the plane defined by the provided normal");
+        g.msg("arc points are not in the plane of the given normal");
         fault = 1;
         return;
     }
@@ -738,7 +738,7 @@ void arc_centrepoint_3d(Geometry &g, Block &b, int &fault) {
     V d1 = vsub(b.start, b.centre), d2 = vsub(b.end, b.centre);
     const double r = vsq(d1);
     if (std::fabs(vsq(d2) - r) > 0.001) {
-        g.msg("Arc points are not correctly defined. The ending radius differs from the starting radius");
+        g.msg("arc end point lies at another radius from the centre than the start point");
         fault = 1;
         return;
     }
@@ -793,10 +793,10 @@ void check_arc(Geometry &g, Block &b, int &fault) { /* src/shapes/arc.cpp:364-55
             arc_defined = 1;
         }
     }
-    if (!has_config) { g.msg("ERROR: Block \"%s\" arc geometry has not been sufficiently defined. Stopping.", b.name.c_str()); fault = 1; }
+    if (!has_config) { g.msg("block \"%s\": not enough arc geometry to place it", b.name.c_str()); fault = 1; }
     if (b.dx < 0) b.dx = b.ni < 0 ? gs : (2.0 * b.radius) / double(b.ni);
     if (b.thickness < 0) {
-        if (b.nk < 0) { g.msg("ERROR: Block \"%s\" arc thickness has not been correctly defined. Stopping.", b.name.c_str()); fault = 1; }
+        if (b.nk < 0) { g.msg("block \"%s\": arc wall thickness or layer count missing", b.name.c_str()); fault = 1; }
     } else if (b.nk < 0) {
         b.nk = b.particle_order ? iceil(b.thickness / gs / std::sqrt(3.0) * 2.0) : iceil(b.thickness / gs);
     }
@@ -814,7 +814,7 @@ void check_arc(Geometry &g, Block &b, int &fault) { /* src/shapes/arc.cpp:364-55
     b.npts = (int64_t)(ni + smax + emax) * b.nk;
     if (D == 3) {
         if (b.length < 0) {
-            if (b.nj < 0) { g.msg("ERROR: Block \"%s\" arch length has not been correctly defined. Stopping.", b.name.c_str()); fault = 1; }
+            if (b.nj < 0) { g.msg("block \"%s\": arch length or j count missing", b.name.c_str()); fault = 1; }
         } else if (b.nj < 0) {
             b.nj = b.particle_order ? iceil(b.length / gs / std::sqrt(6.0) * 3.0) : iceil(b.length / gs);
             b.nj = std::max(b.nj, 1);
@@ -862,7 +862,7 @@ void check_inlet(Geometry &g, Block &b, int &fault) { /* src/shapes/inlet.cpp:7-
                 b.right = vadd(b.centre, vmul(v, 0.5));
             }
         } else {
-            g.msg("ERROR: Inlet block \"%s\" sub shape type has not been correctly defined.", b.name.c_str());
+            g.msg("inlet \"%s\": unknown section shape", b.name.c_str());
             fault = 1;
         }
     } else {
@@ -878,7 +878,7 @@ void check_inlet(Geometry &g, Block &b, int &fault) { /* src/shapes/inlet.cpp:7-
             b.end[1] += b.radius;
         }
     }
-    if (has_config == 0) { g.msg("ERROR: Inlet block \"%s\" geometry not sufficiently defined", b.name.c_str()); fault = 1; }
+    if (has_config == 0) { g.msg("inlet \"%s\": not enough geometry to place it", b.name.c_str()); fault = 1; }
     b.dx = gs;
     if (vnorm(b.angles) != 0) {
         b.angles = vmul(b.angles, kPi / 180.0);
@@ -947,7 +947,7 @@ void check_inlet(Geometry &g, Block &b, int &fault) { /* src/shapes/inlet.cpp:7-
 void check_coords(Geometry &g, Block &b, int &fault) { /* src/shapes/coordinates.cpp:8-29 */
     if (b.filename.empty()) {
         if (b.coords.empty()) {
-            g.msg("ERROR: Block \"%s\" coordinates have not been ingested properly. Stopping.", b.name.c_str());
+            g.msg("block \"%s\": coordinate list is incomplete", b.name.c_str());
             fault = 1;
         } else {
             b.npts = (int64_t)b.coords.size();
@@ -1469,7 +1469,7 @@ int assemble(Geometry &g) {
     auto set_times = [&](fjsph_block &L, const Block &blk, const std::vector<V> &vels, const V &v0) {
         if (!blk.times.empty()) {
             if ((size_t)blk.ntimes > FJSPH_MAX_TIMES || vels.size() > FJSPH_MAX_TIMES) {
-                g.msg("ERROR: Block \"%s\" has %lld motion times; at most %d are supported.", blk.name.c_str(),
+                g.msg("block \"%s\": %lld motion times, more than the %d supported", blk.name.c_str(),
                       (long long)blk.ntimes, FJSPH_MAX_TIMES);
                 return false;
             }
@@ -1495,7 +1495,7 @@ int assemble(Geometry &g) {
                 for (size_t t = 0; t + 1 < (size_t)blk.ntimes; ++t)
                     vels.push_back(vdiv(vsub(blk.pos[t + 1], blk.pos[t]), blk.times[t + 1] - blk.times[t]));
             } else if (blk.vels.empty()) {
-                g.msg("No velocity or position data available for boundary block %zu even though times were defined.", k);
+                g.msg("boundary block %zu has motion times but no positions or velocities for them", k);
                 return FJSPH_E_ARG;
             }
         }
@@ -1510,7 +1510,7 @@ int assemble(Geometry &g) {
         if (blk.bound_type == inletZone) {
             if (blk.particle_order) {
                 /* Init_Particles takes five buffer layers for HCP inlets, the generator makes four */
-                g.msg("ERROR: Inlet block \"%s\" with HCP ordering: the reference reads a fifth buffer layer that its "
+                g.msg("inlet \"%s\" with HCP ordering: the reference reads a fifth buffer layer that its "
                       "inlet generator does not make.", blk.name.c_str());
                 return FJSPH_E_UNSUPPORTED;
             }
@@ -1574,11 +1574,11 @@ int build(Geometry &g) {
         for (Block &b : *set) {
             int f = 0;
             check_input(g, b, f);
-            if (f) g.msg("Check of parameters for block \"%s\" finished with errors.", b.name.c_str());
+            if (f) g.msg("block \"%s\" failed its input check", b.name.c_str());
             fault |= f;
         }
     if (fault) {
-        g.msg("Check of parameters for geometry blocks finished with errors.");
+        g.msg("block input check failed");
         return FJSPH_E_ARG;
     }
     for (auto *set : {&g.bound, &g.fluid})
@@ -1587,7 +1587,7 @@ int build(Geometry &g) {
             generate(g, b);
             b.generated = (int64_t)b.coords.size();
             if (b.generated != b.npts)
-                g.msg("Number of boundary points generated for block \"%s\" differs from expected amount by %d",
+                g.msg("block \"%s\": generated point count is off from the expected count by %d",
                       b.name.c_str(), (int)(b.npts - b.generated));
             b.npts = b.generated;
         }
@@ -1630,7 +1630,7 @@ int fjsph_geometry_read_file(fjsph_geometry *h, const char *path, int32_t fluid)
     if (!h || !path) return FJSPH_E_ARG;
     std::ifstream in(path, std::ios::in | std::ios::binary);
     if (!in.is_open()) {
-        h->g.msg("%s file missing", path);
+        h->g.msg("cannot open block file %s", path);
         return FJSPH_E_ARG;
     }
     std::stringstream ss;

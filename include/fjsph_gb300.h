@@ -268,7 +268,9 @@ int fjsph_integrate_n(fjsph_ctx *ctx, int32_t n_steps, double *last_error);
  *   - n_fluid <= 16,777,216; larger counts return FJSPH_E_CAPACITY.
  *   - dt (host) receives the time step of src/Integration.cpp:370-443 under the settings' cfl,
  *     dt limits and frame time; maxima7 (host) receives maxf, maxAf, maxdrho, maxRhoi, minST,
- *     maxU, maxShift.
+ *     maxU, maxShift.  maxShift here is the largest shifting velocity of this call's particles
+ *     only; fjsph_find_timestep keeps a running maximum over the context's calls, as the
+ *     reference's never-reset member does.
  *   - stream: a cudaStream_t (NULL = default stream); the call synchronises it before returning.
  *   - The first call on a device looks up the scratch array's device address (once per device,
  *     with that device current); make that first call before any stream capture.
@@ -475,6 +477,9 @@ int fjsph_geometry_log(const fjsph_geometry *g, char *buf, int64_t cap, int64_t 
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
 int fjsph_step_report(fjsph_ctx *ctx, double *out5);
+/* The seven maxima of the last fjsph_find_timestep (Integrator members, src/Integration.h):
+ * maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift (the running maximum). */
+int fjsph_timestep_maxima(fjsph_ctx *ctx, double *out7);
 /* Count and total duration (ms) of kernel launches recorded since the last reset. */
 int fjsph_launch_stats(fjsph_ctx *ctx, int64_t *n_launches, int32_t reset);
 /* CUDA stream of the context (a cudaStream_t), for callers that time with events. */

@@ -1,6 +1,9 @@
 """Shared helpers of the parity tests: matched oracle / device pairs and field comparison."""
 from __future__ import annotations
 
+import os
+from pathlib import Path
+
 import numpy as np
 
 from fjsph_gb300 import _cdefs as d
@@ -66,3 +69,10 @@ def hydrostatic_error(st: SPHState, fluid_from: int, rho_rest: float, top: float
     err = [np.mean(pn[idx == k]) - np.mean(depth[idx == k])
            for k in range(1, len(bins)) if np.count_nonzero(idx == k) > 10]
     return float(np.sqrt(np.mean(np.square(err))))
+
+
+def reference_examples() -> Path | None:
+    """The reference's Examples folder, named by the FJSPH_REFERENCE_EXAMPLES environment variable;
+    None when the variable is unset or names no folder (the tests that read it then skip)."""
+    p = os.environ.get("FJSPH_REFERENCE_EXAMPLES")
+    return Path(p) if p and Path(p).is_dir() else None

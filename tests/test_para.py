@@ -7,7 +7,9 @@ from fjsph_gb300 import _cdefs as d
 from fjsph_gb300 import settings as S
 
 HERE = Path(__file__).resolve().parent
-REF_EXAMPLES = Path("/root/reference/Examples")
+from tests._util import reference_examples
+
+REF_EXAMPLES = reference_examples()
 
 
 def test_fixture_para(built_lib):
@@ -31,7 +33,7 @@ def test_unparsed_key_keeps_default(built_lib):
     assert s.rho_max == pytest.approx(1500.0)
 
 
-@pytest.mark.skipif(not REF_EXAMPLES.exists(), reason="reference examples not mounted")
+@pytest.mark.skipif(REF_EXAMPLES is None, reason="FJSPH_REFERENCE_EXAMPLES is not set")
 def test_reference_examples_parse(built_lib):
     s, extra = S.read_para(REF_EXAMPLES / "Dam_2D" / "para_n_1", 2)
     assert s.particle_step == 0.01 and s.speed_sound == 100.0 and s.visc_alpha == 0.01

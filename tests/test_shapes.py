@@ -18,7 +18,9 @@ from fjsph_gb300.settings import defaults, derive
 
 ROOT = Path(__file__).resolve().parents[1]
 GOLD = ROOT / "tests" / "golden" / "shapes"
-REF_EXAMPLES = Path("/root/reference/Examples")
+from tests._util import reference_examples
+
+REF_EXAMPLES = reference_examples()
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -163,7 +165,7 @@ def test_errors_are_reported():
     from fjsph_gb300.geometry import Geometry
     s = _settings(2)
     g = Geometry(s)
-    with pytest.raises(ValueError, match="Unrecognised boundary shape"):
+    with pytest.raises(ValueError, match="is not a known shape"):
         g.read_text("Name: X\nShape: Hexagon\nblock end\n", False)
     g = Geometry(s)
     g.read_text("Name: X\nShape: Line\nStart coordinate: 0,0\nblock end\n", False)
@@ -198,7 +200,7 @@ def test_json_block_files(tmp_path):
     assert blocks[0].bound_solver == d.DBC and blocks[0].name == "Walls"
 
 
-@pytest.mark.skipif(not REF_EXAMPLES.exists(), reason="reference examples not present")
+@pytest.mark.skipif(REF_EXAMPLES is None, reason="FJSPH_REFERENCE_EXAMPLES is not set")
 def test_reference_examples_build():
     """Every shipped example whose para file names existing block files builds; the standing
     column's counts are the ones its block files give by hand (walls 210 x 4 and 105 x 4 at

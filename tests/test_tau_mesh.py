@@ -8,8 +8,11 @@ import pytest
 
 from fjsph_gb300 import _cdefs as d
 
-EX = Path("/root/reference/Examples/RAE2822")
-pytestmark = pytest.mark.skipif(not EX.exists(), reason="reference examples not present")
+from tests._util import reference_examples
+
+_EXAMPLES = reference_examples()
+EX = _EXAMPLES / "RAE2822" if _EXAMPLES else Path("RAE2822")
+pytestmark = pytest.mark.skipif(_EXAMPLES is None or not EX.exists(), reason="FJSPH_REFERENCE_EXAMPLES is not set")
 
 
 @pytest.fixture(scope="module", autouse=True)
