@@ -169,7 +169,7 @@ def test_errors_are_reported():
         g.read_text("Name: X\nShape: Hexagon\nblock end\n", False)
     g = Geometry(s)
     g.read_text("Name: X\nShape: Line\nStart coordinate: 0,0\nblock end\n", False)
-    with pytest.raises(ValueError, match="ending position"):
+    with pytest.raises(ValueError, match="end point missing"):
         g.build()
     s3 = _settings(3)
     g = Geometry(s3)  # HCP inlets: Init_Particles reads a buffer layer the generator never makes
