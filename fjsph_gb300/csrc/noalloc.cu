@@ -39,29 +39,37 @@ struct Fields {
     const double *acc[3], *Af[3], *Rrho, *rho, *curve, *v[3], *vPert[3];
 };
 
-/* max/min over one block's chunk of kThreads*kItems particles; ops: max,max,max,max,min,max,max */
-__global__ void __launch_bounds__(kThreads) k_partial(int D, int64_t n, int ale, double rho_rest, double dx,
-                                                       double sig, Fields f, double *rows) {
+/* max/min over one block's chunk of kThreads*kItems particles; ops: max,max,max,max,min,max,max.
+ * The squared norms are formed exactly as the context's reduction forms them (fjsph::dot over
+ * loaded components, compile-time D), so both give bit-identical maxima. */
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_partial(int64_t n, int ale, double rho_rest, double dx, double sig,
+                                                       Fields f, double *rows) {
     double v[7] = {kEps, kEps, kEps, kEps, 9999999.0, kEps, 0.0};
     const int64_t base = (int64_t)blockIdx.x * kThreads * kItems;
     for (int it = 0; it < kItems; ++it) {
         const int64_t i = base + (int64_t)it * kThreads + threadIdx.x;
         if (i >= n) break;
-        double a2 = 0.0, f2 = 0.0, u2 = 0.0, s2 = 0.0;
+        double a[D], af[D], vv[D];
+#pragma unroll
         for (int k = 0; k < D; ++k) {
-            a2 += f.acc[k][i] * f.acc[k][i];
-            f2 += f.Af[k][i] * f.Af[k][i];
-            u2 += f.v[k][i] * f.v[k][i];
-            if (ale) s2 += f.vPert[k][i] * f.vPert[k][i];
+            a[k] = f.acc[k][i];
+            af[k] = f.Af[k][i];
+            vv[k] = f.v[k][i];
         }
-        v[0] = fmax(v[0], sqrt(a2));
-        v[1] = fmax(v[1], sqrt(f2));
+        v[0] = fmax(v[0], sqrt(fjsph::dot<D, double>(a, a)));
+        v[1] = fmax(v[1], sqrt(fjsph::dot<D, double>(af, af)));
         v[2] = fmax(v[2], fabs(f.Rrho[i]));
         const double rho = f.rho[i];
         v[3] = fmax(v[3], fabs(rho - rho_rest));
         v[4] = fmin(v[4], sqrt(rho * dx * dx / (2.0 * kPi * sig * fabs(f.curve[i]))));
-        v[5] = fmax(v[5], sqrt(u2));
-        if (ale) v[6] = fmax(v[6], sqrt(s2));
+        v[5] = fmax(v[5], sqrt(fjsph::dot<D, double>(vv, vv)));
+        if (ale) {
+            double vp[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) vp[k] = f.vPert[k][i];
+            v[6] = fmax(v[6], sqrt(fjsph::dot<D, double>(vp, vp)));
+        }
     }
     __shared__ double sh[7][kThreads];
     for (int k = 0; k < 7; ++k) sh[k][threadIdx.x] = v[k];
@@ -155,7 +163,10 @@ extern "C" int fjsph_find_timestep_noalloc(const fjsph_settings *s, int64_t n_fl
     const int nrows = n_fluid > 0 ? (int)((n_fluid + (int64_t)kThreads * kItems - 1) / ((int64_t)kThreads * kItems)) : 1;
     /* a launch that fails (no kernel image for this device, an invalid stream) leaves the result
      * row holding an earlier call's values or zeros: report it instead of returning them */
-    k_partial<<<nrows, kThreads, 0, st>>>(D, n_fluid, ale, s->rho_rest, s->dx, s->sig, f, rows);
+    if (D == 2)
+        k_partial<2><<<nrows, kThreads, 0, st>>>(n_fluid, ale, s->rho_rest, s->dx, s->sig, f, rows);
+    else
+        k_partial<3><<<nrows, kThreads, 0, st>>>(n_fluid, ale, s->rho_rest, s->dx, s->sig, f, rows);
     if (cudaGetLastError() != cudaSuccess) return FJSPH_E_CUDA;
     k_final<<<1, kThreads, 0, st>>>(nrows, rows);
     if (cudaGetLastError() != cudaSuccess) return FJSPH_E_CUDA;
