@@ -19,6 +19,7 @@ COLE_EOS, ISO_EOS = 0, 1
 NOAERO, GISSLER, INDUCED_PRESSURE, SKIN_FRIC = 0, 1, 2, 3
 CONST_VEL, MESH_INFL, VLM_INFL = 0, 1, 2  # fjsph_aero_source
 PREC_FP64, PREC_MIXED = 0, 1
+PAIRS_TILES, PAIRS_LISTS = 0, 1
 CLOSURE_PLAIN, CLOSURE_LEARNED = 0, 1
 CLOSURE_ARM_JUDGE, CLOSURE_ARM_LOG = 1, 2
 MLP_INPUTS, MLP_OUTPUTS = 12, 2

@@ -57,6 +57,8 @@ PROTOTYPES = {
     "fjsph_integrate_n": (C.c_int, [_P, _i32, _dp]),
     "fjsph_step_report": (C.c_int, [_P, _dp]),
     "fjsph_timestep_maxima": (C.c_int, [_P, _dp]),
+    "fjsph_set_pair_mode": (C.c_int, [_P, _i32]),
+    "fjsph_get_pair_mode": (C.c_int, [_P, _i32p, _i32p]),
     "fjsph_launch_stats": (C.c_int, [_P, _i64p, _i32]),
     "fjsph_ctx_stream": (C.c_int, [_P, _pp]),
     "fjsph_status_string": (C.c_char_p, [C.c_int]),

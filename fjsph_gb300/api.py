@@ -277,6 +277,16 @@ class Context:
         check("fjsph_step_report", self._lib.fjsph_step_report(self._h, out))
         return dict(maxRho_pc=out[0], maxf=out[1], maxAf=out[2], maxShift=out[3], iteration=int(out[4]))
 
+    def set_pair_mode(self, mode: int) -> None:
+        """d.PAIRS_LISTS (pair lists, default) or d.PAIRS_TILES (shared-memory tiles for the residual)."""
+        check("fjsph_set_pair_mode", self._lib.fjsph_set_pair_mode(self._h, int(mode)))
+
+    def pair_mode(self) -> tuple[int, bool]:
+        """(mode, whether the last search built tiles)."""
+        m, t = C.c_int32(), C.c_int32()
+        check("fjsph_get_pair_mode", self._lib.fjsph_get_pair_mode(self._h, C.byref(m), C.byref(t)))
+        return m.value, bool(t.value)
+
     def timestep_maxima(self) -> list[float]:
         """maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift of the last find_timestep."""
         out = (C.c_double * 7)()

@@ -174,6 +174,11 @@ struct fjsph_ctx {
     float *vlm_abf = nullptr, *vlm_gf = nullptr;
     VlmDev vlm{};
     double *air_v = nullptr; /* 3 per slot */
+    /* shared-memory tiles of the split-precision sweeps (tiles.cuh) */
+    TileDev T{};
+    int32_t pair_mode = FJSPH_PAIRS_LISTS; /* FJSPH_PAIRS_*                               */
+    bool tiles_valid = false;              /* the last search built the tile masks        */
+    int64_t tiles_table = 0;               /* bucket table size the tile arrays fit       */
     /* mesh-cell air source */
     MeshDev mesh{};
     bool mesh_ready = false;
@@ -430,6 +435,11 @@ int alloc_packed(fjsph_ctx *c) {
     for (float4 **a : arrs) TRY(dalloc(c, a, c->cap));
     TRY(dalloc(c, &K.bits, c->cap));
     TRY(dalloc(c, &c->nbr_pair, c->nbr_cap));
+    TRY(dalloc(c, &c->T.mask, (int64_t)kMaskWords * c->cap));
+    TRY(dalloc(c, &c->T.count, 4));
+    TRY(dalloc(c, &c->T.ntot, 2));
+    c->T.stride = c->cap;
+    c->T.smax = 1280;
     c->packed_alloc = true;
     c->dirty_full = true;
     return FJSPH_OK;
@@ -748,6 +758,40 @@ int grow_pairs(fjsph_ctx *c, int64_t need) {
     return FJSPH_OK;
 }
 
+/* Tiles and member masks of the split-precision sweeps for this search.  A grid that outgrew the
+ * bucket table or a particle with more candidates than a mask holds leaves the sweeps on the pair
+ * lists for this search (tiles_valid false). */
+int tile_search(fjsph_ctx *c, const Params &P) {
+    cudaStream_t s = c->stream;
+    TRY(alloc_packed(c));
+    if (c->tiles_table != c->G.table_size) {
+        TRY(dfree(c, c->T.list));
+        TRY(dfree(c, c->T.scan));
+        TRY(dalloc(c, &c->T.list, c->G.table_size + 1));
+        TRY(dalloc(c, &c->T.scan, c->G.table_size + 1));
+        c->tiles_table = c->G.table_size;
+    }
+    c->T.flag = c->G.count; /* free after the scatter */
+    if (!c->graph_mode) CU(cudaMemsetAsync(&c->dsc->status, 0, sizeof(int32_t), s));
+    CU(cudaMemsetAsync(&c->dsc->tile_pairs, 0, sizeof(unsigned long long) + sizeof(int32_t), s));
+    launch_tile_build(P, c->G, c->T, &c->dsc->status, s);
+    launch_tile_masks(P, c->xs, c->G, c->K, c->T, c->dsc, s);
+    c->launches += 6;
+    if (!c->graph_mode) {
+        CU(cudaMemcpyAsync(&c->hsc->status, &c->dsc->status, sizeof(DevScalars) - offsetof(DevScalars, status),
+                           cudaMemcpyDeviceToHost, s));
+        TRY(sync(c));
+        if (c->hsc->status & kStatusTileOverflow) {
+            CU(cudaMemsetAsync(&c->dsc->status, 0, sizeof(int32_t), s));
+            c->hsc->status = 0;
+            c->tiles_valid = false;
+            return FJSPH_OK;
+        }
+    }
+    c->tiles_valid = true;
+    return FJSPH_OK;
+}
+
 /* Split-precision lists in one walk: wcap entries of storage per slot, a re-run with a larger
  * wcap if any slot has more neighbours. */
 int search_fixed(fjsph_ctx *c, const Params &P) {
@@ -827,6 +871,8 @@ int search(fjsph_ctx *c) {
     }
     c->searches++;
     launch_sorted_pos(P, c->xs, c->G, s);
+    c->tiles_valid = false;
+    if (mixed(c) && c->pair_mode == FJSPH_PAIRS_TILES && c->D >= 2) TRY(tile_search(c, P));
     if (mixed(c) && c->wcap > 0) return search_fixed(c, P);
     launch_nbr_count(P, c->xs, c->G, c->nbr_counts, s);
     launch_scan_i64(c->nbr_counts, c->nbr_off, c->n, c->scan_tmp64, s);
@@ -1102,7 +1148,10 @@ int resid(fjsph_ctx *c, const Params &P) {
         ensure_pack(c);
         const Closure C = next_closure(c);
         if (C.mode == kClosureJudge) CU(cudaMemsetAsync(c->judge_dev, 0, 3 * sizeof(double), c->stream));
-        launch_m_resid(P, WS(c), make_nbr(c), c->K, npd_ptr(c), C, c->stream);
+        if (c->tiles_valid)
+            launch_t_resid(P, WS(c), c->G, c->T, c->K, npd_ptr(c), C, c->stream);
+        else
+            launch_m_resid(P, WS(c), make_nbr(c), c->K, npd_ptr(c), C, c->stream);
         if (C.mode == kClosureJudge) {
             CU(cudaMemcpyAsync(c->judge_host, c->judge_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
             c->judge_pending = true;
@@ -2035,7 +2084,37 @@ int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double
     std::vector<int64_t> off(n + 1);
     std::vector<int32_t> id(c->n_pairs);
     std::vector<double> xs(c->D * n);
-    if (mixed(c)) { /* offsets from the per-slot counts (single-pass lists keep no CSR) */
+    if (mixed(c) && c->tiles_valid) { /* the member masks of the tiles, decoded on the device */
+        const Params P = make_params(c);
+        std::vector<int32_t> cnt(n);
+        launch_tile_export(P, c->xs, c->G, c->K, c->T, 0, c->nbr_counts, nullptr, nullptr, nullptr, c->stream);
+        CU(cudaMemcpyAsync(cnt.data(), c->nbr_counts, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+        TRY(sync(c));
+        off[0] = 0;
+        for (int64_t i = 0; i < n; ++i) off[i + 1] = off[i] + cnt[i];
+        const int64_t total = off[n];
+        /* the caller sized its buffers from the pair count the search reported */
+        if (total != c->n_pairs) return FJSPH_E_NEIGHBOUR;
+        id.assign(total, 0);
+        int64_t *didx = nullptr, *doff = nullptr;
+        double *dd2 = nullptr;
+        if (total > 0) {
+            CU(cudaMalloc(&didx, sizeof(int64_t) * total));
+            CU(cudaMalloc(&dd2, sizeof(double) * total));
+            CU(cudaMalloc(&doff, sizeof(int64_t) * (n + 1)));
+            CU(cudaMemcpy(doff, off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+            launch_tile_export(P, c->xs, c->G, c->K, c->T, 1, nullptr, doff, didx, dd2, c->stream);
+            std::vector<int64_t> id64(total);
+            const cudaError_t e1 = cudaMemcpyAsync(id64.data(), didx, sizeof(int64_t) * total, cudaMemcpyDeviceToHost,
+                                                   c->stream);
+            const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+            cudaFree(didx);
+            cudaFree(dd2);
+            cudaFree(doff);
+            if (e1 != cudaSuccess || e2 != cudaSuccess) return FJSPH_E_CUDA;
+            for (int64_t k = 0; k < total; ++k) id[k] = (int32_t)id64[k];
+        }
+    } else if (mixed(c)) { /* offsets from the per-slot counts (single-pass lists keep no CSR) */
         std::vector<int32_t> cnt(n);
         CU(cudaMemcpy(cnt.data(), c->nbr_counts, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
         off[0] = 0;
@@ -2043,7 +2122,7 @@ int fjsph_neighbours_export(fjsph_ctx *c, int64_t *offsets, int64_t *idx, double
     } else {
         CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
     }
-    if (c->n_pairs) {
+    if (c->n_pairs && !(mixed(c) && c->tiles_valid)) {
         if (mixed(c)) { /* sliced-ELL -> CSR */
             const int64_t nslices = (n + kSlice - 1) / kSlice;
             std::vector<int2> pr(c->nbr_storage);
@@ -2290,6 +2369,25 @@ int fjsph_step_report(fjsph_ctx *c, double *out5) {
     out5[2] = c->maxAf;
     out5[3] = c->maxShift;
     out5[4] = (double)c->iteration;
+    return FJSPH_OK;
+}
+
+int fjsph_set_pair_mode(fjsph_ctx *c, int32_t mode) {
+    TRY(check_ctx(c));
+    if (mode != FJSPH_PAIRS_TILES && mode != FJSPH_PAIRS_LISTS) return FJSPH_E_ARG;
+    if (mode != c->pair_mode) {
+        TRY(graph_release(c));
+        c->pair_mode = mode;
+        c->nbr_valid = false; /* the next sweep needs a search in the new mode */
+        c->tiles_valid = false;
+    }
+    return FJSPH_OK;
+}
+
+int fjsph_get_pair_mode(fjsph_ctx *c, int32_t *mode, int32_t *tiles_in_use) {
+    TRY(check_ctx(c));
+    if (mode) *mode = c->pair_mode;
+    if (tiles_in_use) *tiles_in_use = c->tiles_valid ? 1 : 0;
     return FJSPH_OK;
 }
 

@@ -266,6 +266,9 @@ struct DevScalars {
     int32_t status;    /* device-side error bits                               */
     int32_t maxcnt;    /* largest neighbour count of the last single-pass fill */
     unsigned long long pairs; /* pairs of the last single-pass fill            */
+    unsigned long long tile_pairs; /* members counted by the last tile mask pass   */
+    int32_t tile_maxcnt;           /* largest member count of the last mask pass    */
+    int32_t pad;
 };
 
 } // namespace fjsph

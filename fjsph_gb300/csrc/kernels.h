@@ -180,6 +180,37 @@ void launch_sorted_pos(const Params &P, double *const xs[3], CellGrid &G, cudaSt
 void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old, int32_t *tmp, int64_t tmp_len,
                         cudaStream_t s);
 
+/* candidates per particle: at most 32 kMaskWords (the search reports more as an overflow) */
+constexpr int kMaskWords = 16;
+constexpr int kTileThreads = 128;
+constexpr int32_t kStatusTileOverflow = 2; /* DevScalars::status bit */
+
+/* The tile structure of one search (device arrays, sized by the bucket table). */
+struct TileDev {
+    int32_t *list;   /* occupied tiles (linear ids over the tile grid), in id order     */
+    int32_t *count;  /* [1] number of occupied tiles                                      */
+    int64_t *ntot;   /* [1] tiles of the grid (the scan length)                            */
+    int32_t *flag;   /* [table] occupancy flag per tile, then its exclusive scan (scratch)  */
+    int32_t *scan;   /* [table + 1]                                                        */
+    uint32_t *mask;  /* word w of cell-sorted entry g at mask[w * stride + g]              */
+    int64_t stride;
+    int32_t smax;    /* staged particles per CTA that fit the launch's shared memory      */
+};
+
+/* Tiles of the split-precision sweeps (tiles.cuh): occupancy flags, the list of occupied tiles,
+ * then the member masks of every particle; a wrapped bucket table or more than 32 kMaskWords
+ * candidates of a particle raise kStatusTileOverflow in *status. */
+void launch_tile_build(const Params &P, CellGrid &G, TileDev &T, int32_t *status, cudaStream_t s);
+void launch_tile_masks(const Params &P, double *const xs[3], const CellGrid &G, const Packed &K, const TileDev &T,
+                       DevScalars *dsc, cudaStream_t s);
+/* pass 0: counts[slot] = members; pass 1: idx / d2 (FP64) of the members at off[slot] */
+void launch_tile_export(const Params &P, double *const xs[3], const CellGrid &G, const Packed &K, const TileDev &T,
+                        int pass, int32_t *counts, const int64_t *off, int64_t *idx, double *d2, cudaStream_t s);
+
+/* residual of the split-precision form over the tiles (sweeps_mixed.cu) */
+void launch_t_resid(const Params &P, const DevState &W, const CellGrid &G, const TileDev &T, const Packed &K,
+                    const double *npd_dev, const Closure &C, cudaStream_t s);
+
 /* ---- sweeps.cu ---------------------------------------------------------------------------- */
 void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s);
 void launch_npd_only(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s);

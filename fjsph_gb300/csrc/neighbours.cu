@@ -859,3 +859,272 @@ void launch_reorder_map(const Params &P, const CellGrid &G, int32_t *new_of_old,
 }
 
 } // namespace fjsph
+
+/* ---- tiles of the split-precision sweeps (tiles.cuh) ------------------------------------------ */
+#include "tiles.cuh"
+
+namespace fjsph {
+
+namespace {
+
+/* Occupancy of every tile of the grid (a tile is occupied when one of its cells holds a particle);
+ * a wrapped bucket table (buckets are not cells) leaves no tile and reports the overflow bit. */
+template <int D>
+__global__ void k_tile_flags(CellGrid G, TileDev T, int32_t *status) {
+    using TT = Tile<D>;
+    const TileGrid tg = tile_grid<D>(G);
+    const bool wrap = G.grid[3] != 0;
+    const int64_t ntiles = wrap ? 0 : tg.nt[0] * tg.nt[1] * tg.nt[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *T.ntot = ntiles;
+        if (wrap) atomicOr(status, kStatusTileOverflow);
+    }
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t tx = t % tg.nt[0], ty = (t / tg.nt[0]) % tg.nt[1], tz = t / (tg.nt[0] * tg.nt[1]);
+        const int64_t x0 = tx * TT::TX;
+        const int64_t x1 = (x0 + TT::TX < tg.nc[0] ? x0 + TT::TX : tg.nc[0]) - 1;
+        int occ = 0;
+        for (int oz = 0; oz < TT::TZ && !occ; ++oz) {
+            const int64_t cz = tz * TT::TZ + oz;
+            if (cz >= tg.nc[2]) break;
+            for (int oy = 0; oy < TT::TY; ++oy) {
+                const int64_t cy = ty * TT::TY + oy;
+                if (cy >= tg.nc[1]) break;
+                const int64_t row = tg.nc[0] * (cy + tg.nc[1] * cz);
+                if (G.start[row + x1 + 1] > G.start[row + x0]) {
+                    occ = 1;
+                    break;
+                }
+            }
+        }
+        T.flag[t] = occ;
+    }
+}
+
+__global__ void k_tile_list(TileDev T) {
+    const int64_t n = *T.ntot;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        if (T.flag[t]) T.list[T.scan[t]] = (int32_t)t;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *T.count = n > 0 ? T.scan[n] : 0;
+}
+
+/* Member masks: every own particle of every tile tests its candidates in stencil order (FP32 on
+ * the in-cell positions, the FP64 test of the reference inside the rounding band) and writes one
+ * bit per candidate.  A stencil row whose y/z gap alone exceeds the radius keeps zero bits without
+ * tests.  One uniform loop over candidates keeps the lanes of a warp in step. */
+template <int D>
+__global__ void __launch_bounds__(kTileThreads) k_tile_masks(Params P, CellGrid G, TileDev T, Packed K,
+                                                              const double *xs0, const double *xs1,
+                                                              const double *xs2, DevScalars *dsc) {
+    using TT = Tile<D>;
+    extern __shared__ __align__(16) unsigned char tsm[];
+    TileSmem ts = tile_smem<D>(tsm, T.smax, kStageS);
+    const TileGrid tg = tile_grid<D>(G);
+    const double *const xs[3] = {xs0, xs1, xs2};
+    const float edge[3] = {(float)P.cell_edge[0], (float)P.cell_edge[1], (float)P.cell_edge[2]};
+    const float thr_lo = (float)(P.sr * (1.0 - 2e-5)), thr_hi = (float)(P.sr * (1.0 + 2e-5));
+    const float row_cut = (float)(P.sr * (1.0 + 1e-4));
+    const int lane = threadIdx.x & 31;
+    unsigned long long pairs = 0;
+    int maxcnt = 0;
+    const int ntl = *T.count;
+    for (int it = blockIdx.x; it < ntl; it += gridDim.x) {
+        tile_setup<D>(P, G, K, tg, T.list[it], kStageS, kOwnAll, ts);
+        const bool over = ts.over();
+        if (threadIdx.x == 0 && ts.head[3]) atomicOr(&dsc->status, kStatusTileOverflow);
+        const int nown = ts.nown();
+        for (int base = threadIdx.x - lane; base < nown; base += blockDim.x) {
+            const int k = base + lane;
+            if (k >= nown) continue;
+            const TileOwnRef o = tile_own<D>(ts, k);
+            const float4 Si = tile_ld_s(ts, G, o.e, o.hc / TT::HX, over);
+            const int32_t si = __float_as_int(Si.w);
+            double xi[3] = {0, 0, 0};
+            bool xi_loaded = false;
+            uint32_t word = 0u;
+            int pos = 0, wi = 0, nm = 0;
+            auto flush = [&]() {
+                if (wi < kMaskWords) T.mask[wi * T.stride + o.g] = word;
+                ++wi;
+                word = 0u;
+            };
+            TileCursor<D> cur;
+            cur.init(ts, o, nullptr, 0);
+            for (;;) {
+                while (cur.left == 0) {
+                    if (!cur.open_row()) break;
+                    /* the row's y/z gap from the particle, in metres */
+                    const float gy = cur.dy > 0 ? (float)cur.dy - Si.y : (cur.dy < 0 ? Si.y - 1.f - (float)cur.dy : 0.f);
+                    const float gz = cur.dz > 0 ? (float)cur.dz - Si.z : (cur.dz < 0 ? Si.z - 1.f - (float)cur.dz : 0.f);
+                    const float a = fmaxf(gy, 0.f) * edge[1], b = D == 3 ? fmaxf(gz, 0.f) * edge[2] : 0.f;
+                    if (a * a + b * b > row_cut) { /* out of reach: zero bits */
+                        int n = cur.left;
+                        while (n > 0) {
+                            const int take = n < 32 - (pos & 31) ? n : 32 - (pos & 31);
+                            pos += take;
+                            n -= take;
+                            if ((pos & 31) == 0) flush();
+                        }
+                        cur.left = 0;
+                    }
+                }
+                if (cur.left == 0) break;
+                TileNbr n;
+                cur.next_cand(n);
+                const float4 Sj = tile_ld_s(ts, G, n.e, n.row, over);
+                const float ax = ((float)n.dc[0] + (Sj.x - Si.x)) * edge[0];
+                const float ay = ((float)n.dc[1] + (Sj.y - Si.y)) * edge[1];
+                float d2 = ax * ax + ay * ay;
+                if (D == 3) {
+                    const float az = ((float)n.dc[2] + (Sj.z - Si.z)) * edge[2];
+                    d2 += az * az;
+                }
+                bool m = d2 < thr_lo;
+                if (!m && d2 <= thr_hi) { /* inside the rounding band: the FP64 test */
+                    if (!xi_loaded) {
+#pragma unroll
+                        for (int q = 0; q < D; ++q) xi[q] = xs[q][si];
+                        xi_loaded = true;
+                    }
+                    const int32_t sj = __float_as_int(Sj.w);
+                    double xj[3] = {0, 0, 0};
+#pragma unroll
+                    for (int q = 0; q < D; ++q) xj[q] = xs[q][sj];
+                    m = dist2<D>(xi, xj) < P.sr;
+                }
+                nm += m ? 1 : 0;
+                word |= (m ? 1u : 0u) << (pos & 31);
+                ++pos;
+                if ((pos & 31) == 0) flush();
+            }
+            if (pos & 31) flush();
+            for (; wi < kMaskWords; ++wi) T.mask[wi * T.stride + o.g] = 0u;
+            if (pos > 32 * kMaskWords) atomicOr(&dsc->status, kStatusTileOverflow);
+            pairs += (unsigned long long)nm;
+            maxcnt = nm > maxcnt ? nm : maxcnt;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+        const int m2 = __shfl_xor_sync(0xffffffffu, maxcnt, o);
+        maxcnt = m2 > maxcnt ? m2 : maxcnt;
+    }
+    if (lane == 0) {
+        if (pairs) atomicAdd(&dsc->tile_pairs, pairs);
+        atomicMax(&dsc->tile_maxcnt, maxcnt);
+    }
+}
+
+/* Members written out per slot (the neighbour export of the tile path): pass 0 counts, pass 1
+ * writes the neighbour slots and their FP64 squared distances at off[slot]. */
+template <int D>
+__global__ void __launch_bounds__(kTileThreads) k_tile_export(Params P, CellGrid G, TileDev T, Packed K,
+                                                               const double *xs0, const double *xs1,
+                                                               const double *xs2, int pass, int32_t *counts,
+                                                               const int64_t *off, int64_t *idx, double *d2) {
+    using TT = Tile<D>;
+    extern __shared__ __align__(16) unsigned char tsm[];
+    TileSmem ts = tile_smem<D>(tsm, T.smax, kStageS);
+    const TileGrid tg = tile_grid<D>(G);
+    const double *const xs[3] = {xs0, xs1, xs2};
+    const int ntl = *T.count;
+    for (int it = blockIdx.x; it < ntl; it += gridDim.x) {
+        tile_setup<D>(P, G, K, tg, T.list[it], kStageS, kOwnAll, ts);
+        const bool over = ts.over();
+        const int nown = ts.nown();
+        for (int k = threadIdx.x; k < nown; k += blockDim.x) {
+            const TileOwnRef o = tile_own<D>(ts, k);
+            const float4 Si = tile_ld_s(ts, G, o.e, o.hc / TT::HX, over);
+            const int32_t si = __float_as_int(Si.w);
+            if (pass == 0) {
+                counts[si] = tile_member_count(T.mask, T.stride, o.g);
+                continue;
+            }
+            double xi[3] = {0, 0, 0};
+#pragma unroll
+            for (int q = 0; q < D; ++q) xi[q] = xs[q][si];
+            int64_t w = off[si];
+            TileCursor<D> cur;
+            cur.init(ts, o, T.mask, T.stride);
+            TileNbr n;
+            while (cur.next_member(n)) {
+                const float4 Sj = tile_ld_s(ts, G, n.e, n.row, over);
+                const int32_t sj = __float_as_int(Sj.w);
+                double xj[3] = {0, 0, 0};
+#pragma unroll
+                for (int q = 0; q < D; ++q) xj[q] = xs[q][sj];
+                idx[w] = sj;
+                d2[w] = dist2<D>(xi, xj);
+                ++w;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+/* CTAs of a persistent tile launch: the resident count per SM times the SMs */
+template <class KernelT>
+unsigned tile_grid_size(KernelT kernel, size_t smem) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kTileThreads, smem) != cudaSuccess || per < 1)
+        per = 1;
+    return (unsigned)(sms * per);
+}
+
+template <class KernelT>
+void tile_attr(KernelT kernel, size_t smem) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+} // namespace
+
+void launch_tile_build(const Params &P, CellGrid &G, TileDev &T, int32_t *status, cudaStream_t s) {
+    const unsigned g = 152 * 8;
+    if (P.D == 2)
+        k_tile_flags<2><<<g, 256, 0, s>>>(G, T, status);
+    else
+        k_tile_flags<3><<<g, 256, 0, s>>>(G, T, status);
+    scan_exclusive<int32_t, int32_t>(T.flag, T.scan, G.table_size, G.scan_tmp, s, T.ntot);
+    k_tile_list<<<g, 256, 0, s>>>(T);
+}
+
+void launch_tile_masks(const Params &P, double *const xs[3], const CellGrid &G, const Packed &K, const TileDev &T,
+                       DevScalars *dsc, cudaStream_t s) {
+    if (P.D == 2) {
+        const size_t sm = tile_smem_bytes<2>(T.smax, kStageS);
+        tile_attr(k_tile_masks<2>, sm);
+        k_tile_masks<2><<<tile_grid_size(k_tile_masks<2>, sm), kTileThreads, sm, s>>>(P, G, T, K, xs[0], xs[1], xs[2],
+                                                                                       dsc);
+    } else {
+        const size_t sm = tile_smem_bytes<3>(T.smax, kStageS);
+        tile_attr(k_tile_masks<3>, sm);
+        k_tile_masks<3><<<tile_grid_size(k_tile_masks<3>, sm), kTileThreads, sm, s>>>(P, G, T, K, xs[0], xs[1], xs[2],
+                                                                                       dsc);
+    }
+}
+
+void launch_tile_export(const Params &P, double *const xs[3], const CellGrid &G, const Packed &K, const TileDev &T,
+                        int pass, int32_t *counts, const int64_t *off, int64_t *idx, double *d2, cudaStream_t s) {
+    if (P.D == 2) {
+        const size_t sm = tile_smem_bytes<2>(T.smax, kStageS);
+        tile_attr(k_tile_export<2>, sm);
+        k_tile_export<2><<<tile_grid_size(k_tile_export<2>, sm), kTileThreads, sm, s>>>(
+            P, G, T, K, xs[0], xs[1], xs[2], pass, counts, off, idx, d2);
+    } else {
+        const size_t sm = tile_smem_bytes<3>(T.smax, kStageS);
+        tile_attr(k_tile_export<3>, sm);
+        k_tile_export<3><<<tile_grid_size(k_tile_export<3>, sm), kTileThreads, sm, s>>>(
+            P, G, T, K, xs[0], xs[1], xs[2], pass, counts, off, idx, d2);
+    }
+}
+
+} // namespace fjsph

@@ -23,6 +23,7 @@
 #include "kernels.h"
 #include "linalg.cuh"
 #include "pack.cuh"
+#include "tiles.cuh"
 
 namespace fjsph {
 
@@ -826,108 +827,77 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
 /* ------------------------------------------------------------------------------------------ */
 /* residual (src/Resid.cpp:243-469)                                                               */
 /* ------------------------------------------------------------------------------------------ */
+/* Per-particle accumulator of the residual's pair sums: the same arithmetic for the pair-list
+ * sweep and the shared-memory tile sweep.  Each supplies the separations x_j - x_i, v_j - v_i
+ * (and the absolute velocities under ALE) in its own representation; F and G of a neighbour are
+ * read by slot when a variant needs them. */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
-                                                      Closure C) {
-    __shared__ __align__(16) MlpWarpSmem mlp_smem[kThreads / 32];
-    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const bool live = i < P.n;
-    /* the aerodynamic term first: the learned closure runs on whole warps */
-    double aero[D];
-    bool aero_on;
-    closure_aero<D>(P, W, C, K.N, K.G, i, live, double(N.cnt[i]), mlp_smem[threadIdx.x >> 5],
-                    aero_on, aero);
-    if (!live) return;
-    const Pf f = make_pf(P);
-    constexpr bool ale = ALE, nofrozen = NOFROZEN;
-    const bool linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH), tic = has(P, FJSPH_VAR_TIC);
-    const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE, csf = P.st_model == FJSPH_ST_CSF;
-    float npdm2 = 0.f;
-    if (pairwise) {
-        const double npd = npd_dev[grp_of(P, i)];
-        npdm2 = (float)P.fc.st_coef / (float)(npd * npd);
-    }
-    const float pi3o4_H = P.fc.pi3o4_H;
-    const float fac_bound = P.fc.fac_bound;
-    const float4 Ai = K.A[i], Ci = K.C[i], Fi = K.F[i];
-    const LoParts Li(K.Lo[i]);
-    const float rho_i = f.rho0 + Ci.w;
-    const float m_i = Ai.w * rho_i;
-    const float pr_i0 = Li.pr;
-    const int bits_i = K.bits[i];
-    const int b_i = bits_b(bits_i), sz_i = bits_zone(bits_i);
-    const float pr_i = (tic && sz_i != 1) ? fabsf(pr_i0) : pr_i0;
-    const float p_i = (tic && sz_i != 1) ? fabsf(Fi.w) : Fi.w;
-    float vPi[D], gRi[D];
-    vPi[0] = Fi.x;
-    vPi[1] = Fi.y;
-    if (D == 3) vPi[2] = Fi.z;
-    if (nofrozen) {
-        const float4 Gi = K.G[i];
-        gRi[0] = Gi.x;
-        gRi[1] = Gi.y;
-        if (D == 3) gRi[2] = Gi.z;
-    }
-    float vi[D];
-    vi[0] = Ci.x + Li.vl[0];
-    vi[1] = Ci.y + Li.vl[1];
-    if (D == 3) vi[2] = Ci.z + Li.vl[2];
-    const SellList L = sell(N, i);
+struct ResidAcc {
+    float rho_i, m_i, pr_i, p_i, npdm2, pi3o4_H, fac_bound, drho_i;
+    int b_i, sz_i;
+    bool linear, nodsph, tic, st_on, csf;
+    float vPi[D], gRi[D], vi[D];
     KSum acc[D];
     float acc_ale[D], visc[D], st[D], art[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        acc_ale[k] = 0.f;
-        visc[k] = 0.f;
-        st[k] = 0.f;
-        art[k] = 0.f;
-    }
     KSum Rrho, Rrhoc, Rrho_d;
-    const bool st_on = pairwise && (!ale || sz_i == 1);
-    /* software pipeline: after this pair's own gathers are issued, the next pair is read and its
-     * neighbour's packed inputs are prefetched into L1 while this pair is computed; list rows
-     * are fetched kListAhead ahead */
-    const int32_t ahead = P.list_ahead > 0 ? P.list_ahead : kListAhead;
-    /* the next kGatherAhead pairs wait in registers; the newest one's neighbour inputs are
-     * prefetched into L1 when it is read, kGatherAhead iterations before they are gathered */
-    int2 q[kGatherAhead];
-#pragma unroll
-    for (int a = 0; a < kGatherAhead; ++a) {
-        q[a] = make_int2((int32_t)i, 0);
-        if (a < L.n) {
-            q[a] = L[a];
-            if (a > 0) prefetch_pair_inputs(K, q[a].x, linear || ale, nofrozen);
+
+    /* vol_i = m / rho, drho = rho - rho0, pr = p / rho^2 (packed, flags in the low bits),
+     * v = absolute velocity (used under ALE) */
+    __device__ __forceinline__ void init(const Params &P, const Pf &f, const Packed &K, int64_t i, float vol_i,
+                                         float drho, float pr, const float *v, const double *npd_dev) {
+        linear = has(P, FJSPH_VAR_LINEAR);
+        nodsph = has(P, FJSPH_VAR_NODSPH);
+        tic = has(P, FJSPH_VAR_TIC);
+        const bool pairwise = P.st_model == FJSPH_ST_PAIRWISE;
+        csf = P.st_model == FJSPH_ST_CSF;
+        npdm2 = 0.f;
+        if (pairwise) {
+            const double npd = npd_dev[grp_of(P, i)];
+            npdm2 = (float)P.fc.st_coef / (float)(npd * npd);
         }
+        pi3o4_H = P.fc.pi3o4_H;
+        fac_bound = P.fc.fac_bound;
+        const float4 Fi = K.F[i];
+        drho_i = drho;
+        rho_i = f.rho0 + drho;
+        m_i = vol_i * rho_i;
+        const int bits_i = K.bits[i];
+        b_i = bits_b(bits_i);
+        sz_i = bits_zone(bits_i);
+        pr_i = (tic && sz_i != 1) ? fabsf(pr) : pr;
+        p_i = (tic && sz_i != 1) ? fabsf(Fi.w) : Fi.w;
+        vPi[0] = Fi.x;
+        vPi[1] = Fi.y;
+        if (D == 3) vPi[2] = Fi.z;
+        if (NOFROZEN) {
+            const float4 Gi = K.G[i];
+            gRi[0] = Gi.x;
+            gRi[1] = Gi.y;
+            if (D == 3) gRi[2] = Gi.z;
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            vi[k] = v[k];
+            acc_ale[k] = 0.f;
+            visc[k] = 0.f;
+            st[k] = 0.f;
+            art[k] = 0.f;
+        }
+        st_on = pairwise && (!ALE || sz_i == 1);
     }
-    for (int32_t r_ = kChunk; r_ < ahead && r_ < L.n; r_ += kChunk) prefetch_l1(L.at(r_));
-    for (int32_t e = 0; e < L.n; ++e) {
-        const int2 pe = q[0];
-        if (((e + ahead) % kChunk) == 0 && e + ahead < L.n) prefetch_l1(L.at(e + ahead)); /* next chunk */
-        const int32_t j = pe.x;
-        const float4 Aj = K.A[j], Cj = K.C[j], Qj = K.Lo[j];
-#pragma unroll
-        for (int a = 0; a + 1 < kGatherAhead; ++a) q[a] = q[a + 1];
-        if (e + kGatherAhead < L.n) {
-            q[kGatherAhead - 1] = L[e + kGatherAhead];
-            prefetch_pair_inputs(K, q[kGatherAhead - 1].x, linear || ale, nofrozen);
-        }
-        if (j == i) continue;
-        const LoParts Lj(Qj);
-        /* separations as in sep(): high parts, then the (bf16) low parts */
-        float Rji[D], Vji[D];
-        Rji[0] = (Aj.x - Ai.x) + (Lj.xl[0] - Li.xl[0]);
-        Rji[1] = (Aj.y - Ai.y) + (Lj.xl[1] - Li.xl[1]);
-        if (D == 3) Rji[2] = (Aj.z - Ai.z) + (Lj.xl[2] - Li.xl[2]);
-        Vji[0] = (Cj.x - Ci.x) + (Lj.vl[0] - Li.vl[0]);
-        Vji[1] = (Cj.y - Ci.y) + (Lj.vl[1] - Li.vl[1]);
-        if (D == 3) Vji[2] = (Cj.z - Ci.z) + (Lj.vl[2] - Li.vl[2]);
-        const float rr = __int_as_float(pe.y);
+
+    /* slot j is read only by the variants that need F or G of the neighbour */
+    __device__ __forceinline__ bool needs_slot() const { return ALE || NOFROZEN || linear; }
+
+    /* pair (i, j), j != i: Rji = x_j - x_i, Vji = v_j - v_i, vj = v_j (ALE), rr = search-time r^2 */
+    __device__ __forceinline__ void pair(const Pf &f, const Packed &K, int32_t j, const float *Rji, const float *Vji,
+                                         const float *vj, float volj, float drho_j, float prj, uint32_t flags_j,
+                                         float rr) {
         const float r = sqrtf(rr);
         const float idist2 = 1.f / (rr + 0.001f * f.H_sq);
-        const float volj = Aj.w;
-        const float rho_j = f.rho0 + Cj.w;
+        const float rho_j = f.rho0 + drho_j;
         const float m_j = volj * rho_j;
-        const bool bound_j = (Lj.flags & kLoBound) != 0u, fluid_j = (Lj.flags & kLoFluid) != 0u;
+        const bool bound_j = (flags_j & kLoBound) != 0u, fluid_j = (flags_j & kLoFluid) != 0u;
         const float gs = f_gscale(f, r);
         float g[D];
 #pragma unroll
@@ -936,7 +906,7 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, D
         if (linear)
             pc = (p_i + K.F[j].w) * volj;
         else
-            pc = m_j * (pr_i + Lj.pr);
+            pc = m_j * (pr_i + prj);
 #pragma unroll
         for (int k = 0; k < D; ++k) acc[k].add(-pc * g[k]);
         const float rg = fdot<D>(Rji, g);
@@ -949,15 +919,12 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, D
 #pragma unroll
             for (int k = 0; k < D; ++k) st[k] += c * Rji[k];
         }
-        if (ale) {
+        if (ALE) {
             const float4 Fj = K.F[j];
-            float vPj[D], vj[D];
+            float vPj[D];
             vPj[0] = Fj.x;
             vPj[1] = Fj.y;
             if (D == 3) vPj[2] = Fj.z;
-            vj[0] = Cj.x + Lj.vl[0];
-            vj[1] = Cj.y + Lj.vl[1];
-            if (D == 3) vj[2] = Cj.z + Lj.vl[2];
             const float gj = fdot<D>(vPj, g), gi = fdot<D>(vPi, g);
             float q = 0.f, w1 = 0.f, w2 = 0.f;
 #pragma unroll
@@ -973,7 +940,7 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, D
         } else {
             Rrho.add(-volj * fdot<D>(Vji, g));
         }
-        if (nofrozen) {
+        if (NOFROZEN) {
             if (fluid_j) {
                 if (!nodsph) {
                     const float4 Gj = K.G[j];
@@ -981,41 +948,190 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, D
                     gsum[0] = gRi[0] + Gj.x;
                     gsum[1] = gRi[1] + Gj.y;
                     if (D == 3) gsum[2] = gRi[2] + Gj.z;
-                    Rrho_d.add(volj * ((Cj.w - Ci.w) + 0.5f * fdot<D>(gsum, Rji)) * rg * idist2);
+                    Rrho_d.add(volj * ((drho_j - drho_i) + 0.5f * fdot<D>(gsum, Rji)) * rg * idist2);
                 }
                 const float vdotr = fdot<D>(Vji, Rji);
                 const float c = m_j * f_art_visc(f, vdotr, idist2, rho_i, rho_j);
 #pragma unroll
                 for (int k = 0; k < D; ++k) art[k] += c * g[k];
             } else if (!nodsph) {
-                Rrho_d.add(volj * (Cj.w - Ci.w) * rg * idist2);
+                Rrho_d.add(volj * (drho_j - drho_i) * rg * idist2);
             }
         }
     }
-    double accd[D];
+
+    __device__ __forceinline__ void finish(const Params &P, const DevState &W, int64_t i, const double *aero,
+                                           bool aero_on) {
+        double accd[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-        accd[k] = aero[k] + acc[k].value();
-        if (linear) accd[k] /= to_f64(rho_i);
-    }
-    if (csf) {
-        const double c = 1.0 / W.rho[i] * P.sig * W.curve[i] * W.colourG[i];
+        for (int k = 0; k < D; ++k) {
+            accd[k] = aero[k] + acc[k].value();
+            if (linear) accd[k] /= to_f64(rho_i);
+        }
+        if (csf) {
+            const double c = 1.0 / W.rho[i] * P.sig * W.curve[i] * W.colourG[i];
 #pragma unroll
-        for (int k = 0; k < D; ++k) accd[k] += c * W.norm[k][i];
-    }
-    const float inv_m = 1.f / m_i; /* the surface-tension sum is FP32 already */
+            for (int k = 0; k < D; ++k) accd[k] += c * W.norm[k][i];
+        }
+        const float inv_m = 1.f / m_i; /* the surface-tension sum is FP32 already */
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-        const double av = nofrozen ? to_f64(art[k]) : W.aVisc[k][i];
-        double t = accd[k];
-        if (ale) t += to_f64(acc_ale[k]);
-        W.acc[k][i] = t + av + to_f64(visc[k]) + to_f64(st[k] * inv_m) + P.grav[k];
-        if (aero_on) W.Af[k][i] = aero[k];
+        for (int k = 0; k < D; ++k) {
+            const double av = NOFROZEN ? to_f64(art[k]) : W.aVisc[k][i];
+            double t = accd[k];
+            if (ALE) t += to_f64(acc_ale[k]);
+            W.acc[k][i] = t + av + to_f64(visc[k]) + to_f64(st[k] * inv_m) + P.grav[k];
+            if (aero_on) W.Af[k][i] = aero[k];
+        }
+        double R = Rrho.value() * to_f64(rho_i);
+        if (ALE) R += Rrhoc.value();
+        if (!nodsph) R += NOFROZEN ? P.dsph_cont * Rrho_d.value() : W.deltaD[i];
+        W.Rrho[i] = R;
     }
-    double R = Rrho.value() * to_f64(rho_i);
-    if (ale) R += Rrhoc.value();
-    if (!nodsph) R += nofrozen ? P.dsph_cont * Rrho_d.value() : W.deltaD[i];
-    W.Rrho[i] = R;
+};
+
+template <int D, bool ALE, bool NOFROZEN>
+__global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
+                                                      Closure C) {
+    __shared__ __align__(16) MlpWarpSmem mlp_smem[kThreads / 32];
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool live = i < P.n;
+    /* the aerodynamic term first: the learned closure runs on whole warps */
+    double aero[D];
+    bool aero_on;
+    closure_aero<D>(P, W, C, K.N, K.G, i, live, double(N.cnt[i]), mlp_smem[threadIdx.x >> 5],
+                    aero_on, aero);
+    if (!live) return;
+    const Pf f = make_pf(P);
+    const bool linear = has(P, FJSPH_VAR_LINEAR);
+    const float4 Ai = K.A[i], Ci = K.C[i];
+    const LoParts Li(K.Lo[i]);
+    ResidAcc<D, ALE, NOFROZEN> ra;
+    {
+        float vi[3];
+        vi[0] = Ci.x + Li.vl[0];
+        vi[1] = Ci.y + Li.vl[1];
+        vi[2] = Ci.z + Li.vl[2];
+        ra.init(P, f, K, i, Ai.w, Ci.w, Li.pr, vi, npd_dev);
+    }
+    const SellList L = sell(N, i);
+    /* software pipeline: after this pair's own gathers are issued, the next pair is read and its
+     * neighbour's packed inputs are prefetched into L1 while this pair is computed; list rows
+     * are fetched kListAhead ahead */
+    const int32_t ahead = P.list_ahead > 0 ? P.list_ahead : kListAhead;
+    /* the next kGatherAhead pairs wait in registers; the newest one's neighbour inputs are
+     * prefetched into L1 when it is read, kGatherAhead iterations before they are gathered */
+    int2 q[kGatherAhead];
+#pragma unroll
+    for (int a = 0; a < kGatherAhead; ++a) {
+        q[a] = make_int2((int32_t)i, 0);
+        if (a < L.n) {
+            q[a] = L[a];
+            if (a > 0) prefetch_pair_inputs(K, q[a].x, linear || ALE, NOFROZEN);
+        }
+    }
+    for (int32_t r_ = kChunk; r_ < ahead && r_ < L.n; r_ += kChunk) prefetch_l1(L.at(r_));
+    for (int32_t e = 0; e < L.n; ++e) {
+        const int2 pe = q[0];
+        if (((e + ahead) % kChunk) == 0 && e + ahead < L.n) prefetch_l1(L.at(e + ahead)); /* next chunk */
+        const int32_t j = pe.x;
+        const float4 Aj = K.A[j], Cj = K.C[j], Qj = K.Lo[j];
+#pragma unroll
+        for (int a = 0; a + 1 < kGatherAhead; ++a) q[a] = q[a + 1];
+        if (e + kGatherAhead < L.n) {
+            q[kGatherAhead - 1] = L[e + kGatherAhead];
+            prefetch_pair_inputs(K, q[kGatherAhead - 1].x, linear || ALE, NOFROZEN);
+        }
+        if (j == i) continue;
+        const LoParts Lj(Qj);
+        /* separations: high parts, then the (bf16) low parts */
+        float Rji[D], Vji[D], vj[D];
+        Rji[0] = (Aj.x - Ai.x) + (Lj.xl[0] - Li.xl[0]);
+        Rji[1] = (Aj.y - Ai.y) + (Lj.xl[1] - Li.xl[1]);
+        if (D == 3) Rji[2] = (Aj.z - Ai.z) + (Lj.xl[2] - Li.xl[2]);
+        Vji[0] = (Cj.x - Ci.x) + (Lj.vl[0] - Li.vl[0]);
+        Vji[1] = (Cj.y - Ci.y) + (Lj.vl[1] - Li.vl[1]);
+        if (D == 3) Vji[2] = (Cj.z - Ci.z) + (Lj.vl[2] - Li.vl[2]);
+        if (ALE) {
+            vj[0] = Cj.x + Lj.vl[0];
+            vj[1] = Cj.y + Lj.vl[1];
+            if (D == 3) vj[2] = Cj.z + Lj.vl[2];
+        }
+        ra.pair(f, K, j, Rji, Vji, vj, Aj.w, Cj.w, Lj.pr, Lj.flags, __int_as_float(pe.y));
+    }
+    ra.finish(P, W, i, aero, aero_on);
+}
+
+/* The residual over shared-memory tiles: each CTA stages a tile's halo as tile-relative records
+ * and every lane walks one fluid particle's members with a cursor over its mask, the lanes of a
+ * warp in step through the pair arithmetic. */
+template <int D, bool ALE, bool NOFROZEN>
+__global__ void __launch_bounds__(kTileThreads, 3) k_t_resid(Params P, DevState W, CellGrid G, TileDev T, Packed K,
+                                                              const double *npd_dev, Closure C) {
+    using TT = Tile<D>;
+    extern __shared__ __align__(16) unsigned char tsm[];
+    __shared__ __align__(16) MlpWarpSmem mlp_smem[kTileThreads / 32];
+    TileSmem ts = tile_smem<D>(tsm, T.smax, kStageRel);
+    const TileGrid tg = tile_grid<D>(G);
+    const Pf f = make_pf(P);
+    const float edge[3] = {(float)P.cell_edge[0], (float)P.cell_edge[1], (float)P.cell_edge[2]};
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int ntl = *T.count;
+    for (int it = blockIdx.x; it < ntl; it += gridDim.x) {
+        tile_setup<D>(P, G, K, tg, T.list[it], kStageRel, kOwnFluid, ts);
+        const bool over = ts.over();
+        const int nown = ts.nown();
+        for (int base = wid * 32; base < nown; base += kTileThreads) {
+            const int k = base + lane;
+            const bool live = k < nown;
+            TileOwnRef o{};
+            int64_t i = 0;
+            int nn = 0;
+            if (live) {
+                o = tile_own<D>(ts, k);
+                i = tile_slot(G, ts, o.e, o.hc / TT::HX);
+                nn = tile_member_count(T.mask, T.stride, o.g);
+            }
+            double aero[D];
+            bool aero_on;
+            closure_aero<D>(P, W, C, K.N, K.G, i, live, double(nn), mlp_smem[wid], aero_on, aero);
+            if (!live) continue;
+            float4 Pi, Vi, Ti;
+            tile_ld_rel<D>(ts, G, K, o.e, o.hc / TT::HX, over, Pi, Vi, Ti);
+            const float *fr = ts.frame;
+            float vi[3];
+            vi[0] = fr[6] + (fr[9] + Vi.x);
+            vi[1] = fr[7] + (fr[10] + Vi.y);
+            vi[2] = fr[8] + (fr[11] + Vi.z);
+            ResidAcc<D, ALE, NOFROZEN> ra;
+            ra.init(P, f, K, i, Pi.w, Vi.w, __uint_as_float(__float_as_uint(Ti.w) & ~3u), vi, npd_dev);
+            TileCursor<D> cur;
+            cur.init(ts, o, T.mask, T.stride);
+            TileNbr n;
+            while (cur.next_member(n)) {
+                if (n.e == o.e) continue;
+                float4 Pj, Vj, Tj;
+                tile_ld_rel<D>(ts, G, K, n.e, n.row, over, Pj, Vj, Tj);
+                float Rji[D], Vji[D], vj[D];
+                Rji[0] = Pj.x - Pi.x;
+                Rji[1] = Pj.y - Pi.y;
+                if (D == 3) Rji[2] = Pj.z - Pi.z;
+                Vji[0] = Vj.x - Vi.x;
+                Vji[1] = Vj.y - Vi.y;
+                if (D == 3) Vji[2] = Vj.z - Vi.z;
+                if (ALE) {
+                    vj[0] = fr[6] + (fr[9] + Vj.x);
+                    vj[1] = fr[7] + (fr[10] + Vj.y);
+                    if (D == 3) vj[2] = fr[8] + (fr[11] + Vj.z);
+                }
+                const uint32_t tw = __float_as_uint(Tj.w);
+                const int32_t j = ra.needs_slot() ? tile_slot(G, ts, n.e, n.row) : 0;
+                ra.pair(f, K, j, Rji, Vji, vj, Pj.w, Vj.w, __uint_as_float(tw & ~3u), tw & 3u,
+                        tile_r2<D>(Ti, Tj, n, edge));
+            }
+            ra.finish(P, W, i, aero, aero_on);
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void k_permute_f4(const float4 *src, float4 *dst, const int32_t *new_of_old, int64_t n) {
@@ -1110,6 +1226,43 @@ void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const P
             nf ? FJSPH_RESID_M(3, false, true) : FJSPH_RESID_M(3, false, false);
     }
 #undef FJSPH_RESID_M
+}
+
+template <int D, bool A, bool NF>
+void t_resid_launch(const Params &P, const DevState &W, const CellGrid &G, const TileDev &T, const Packed &K,
+                    const double *npd_dev, const Closure &C, cudaStream_t s) {
+    const size_t sm = tile_smem_bytes<D>(T.smax, kStageRel);
+    static bool attr = false;
+    static unsigned grid = 0;
+    if (!attr) {
+        if (sm > 48 * 1024)
+            cudaFuncSetAttribute(k_t_resid<D, A, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        int dev = 0, sms = 1, per = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_t_resid<D, A, NF>, kTileThreads, sm) != cudaSuccess ||
+            per < 1)
+            per = 1;
+        grid = (unsigned)(sms * per);
+        attr = true;
+    }
+    k_t_resid<D, A, NF><<<grid, kTileThreads, sm, s>>>(P, W, G, T, K, npd_dev, C);
+}
+
+void launch_t_resid(const Params &P, const DevState &W, const CellGrid &G, const TileDev &T, const Packed &K,
+                    const double *npd_dev, const Closure &C, cudaStream_t s) {
+    const bool ale = has(P, FJSPH_VAR_ALE), nf = has(P, FJSPH_VAR_NOFROZEN);
+    if (P.D == 2) {
+        if (ale)
+            nf ? t_resid_launch<2, true, true>(P, W, G, T, K, npd_dev, C, s) : t_resid_launch<2, true, false>(P, W, G, T, K, npd_dev, C, s);
+        else
+            nf ? t_resid_launch<2, false, true>(P, W, G, T, K, npd_dev, C, s) : t_resid_launch<2, false, false>(P, W, G, T, K, npd_dev, C, s);
+    } else {
+        if (ale)
+            nf ? t_resid_launch<3, true, true>(P, W, G, T, K, npd_dev, C, s) : t_resid_launch<3, true, false>(P, W, G, T, K, npd_dev, C, s);
+        else
+            nf ? t_resid_launch<3, false, true>(P, W, G, T, K, npd_dev, C, s) : t_resid_launch<3, false, false>(P, W, G, T, K, npd_dev, C, s);
+    }
 }
 
 } // namespace fjsph

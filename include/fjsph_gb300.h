@@ -477,6 +477,17 @@ int fjsph_geometry_log(const fjsph_geometry *g, char *buf, int64_t cap, int64_t 
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Step report of src/Integration.cpp:253-265: maxRho_pc, maxf, maxAf, maxShift, iteration. */
 int fjsph_step_report(fjsph_ctx *ctx, double *out5);
+/* Pair sweeps of the split-precision form (no reference counterpart: a property of this
+ * implementation).  FJSPH_PAIRS_LISTS (default): explicit (neighbour, squared distance) lists
+ * gathered through the caches.  FJSPH_PAIRS_TILES: the residual stages each tile of cells with
+ * its halo in shared memory and walks per-particle member masks (the other sweeps keep the
+ * lists).  Both give the same neighbour sets (the reference's FP64 membership test).  A grid too
+ * large for the bucket table falls back to lists for that search; tiles_in_use reports what the
+ * last search built. */
+#define FJSPH_PAIRS_TILES 0
+#define FJSPH_PAIRS_LISTS 1
+int fjsph_set_pair_mode(fjsph_ctx *ctx, int32_t mode);
+int fjsph_get_pair_mode(fjsph_ctx *ctx, int32_t *mode, int32_t *tiles_in_use);
 /* The seven maxima of the last fjsph_find_timestep (Integrator members, src/Integration.h):
  * maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift (the running maximum). */
 int fjsph_timestep_maxima(fjsph_ctx *ctx, double *out7);
