@@ -80,16 +80,18 @@ def _hydrostatic(s: d.Settings, st: SPHState, axis: int, height: float) -> None:
     st.rho[:] = _eos_density(s, p)
 
 
-def dam_break_2d(dx: float = 0.01, column=(1.0, 2.0), tank=(4.0, 3.0), layers: int = 3,
-                 solver: int = d.RUNGE_KUTTA, cfl: float = 0.2) -> Case:
-    """Config 0: 1.0 x 2.0 m column in a 4.0 x 3.0 m tank, dx = 0.01 (20,000 fluid particles)."""
+def dam_break_2d_settings(dx: float = 0.01, column_height: float = 2.0, solver: int = d.RUNGE_KUTTA,
+                          cfl: float = 0.2) -> d.Settings:
+    """Settings of config 0: Wendland C2 at H = 1.3 dx, Cole EOS (rho0 1000, gamma 7,
+    c0 = 10 sqrt(2 g H_column)), delta-SPH 0.1, artificial viscosity 0.01, no surface tension,
+    fixed CFL."""
     s = defaults(2)
     s.st_model = d.ST_NOST
     s.particle_step = dx
     s.H_fac = 1.3
     s.rho_rest = 1000.0
     s.gam = 7.0
-    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * column[1])
+    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * column_height)
     s.dsph_delta = 0.1
     s.visc_alpha = 0.01
     s.sig = 0.0
@@ -97,7 +99,13 @@ def dam_break_2d(dx: float = 0.01, column=(1.0, 2.0), tank=(4.0, 3.0), layers: i
     s.solver_type = solver
     s.cfl = s.cfl_min = s.cfl_max = cfl
     s.delta_t_min = 1e-9
-    derive(s)
+    return derive(s)
+
+
+def dam_break_2d(dx: float = 0.01, column=(1.0, 2.0), tank=(4.0, 3.0), layers: int = 3,
+                 solver: int = d.RUNGE_KUTTA, cfl: float = 0.2) -> Case:
+    """Config 0: 1.0 x 2.0 m column in a 4.0 x 3.0 m tank, dx = 0.01 (20,000 fluid particles)."""
+    s = dam_break_2d_settings(dx, column[1], solver, cfl)
     nx, ny = int(round(column[0] / dx)), int(round(column[1] / dx))
     fx, fy = np.meshgrid((np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dx, indexing="ij")
     fluid = np.stack([fx.ravel(), fy.ravel()], axis=1)
@@ -212,16 +220,15 @@ def couette_2d(dx: float = 0.02, length: float = 3.0, gap: float = 1.0, wall_spe
     return Case("couette_2d", s, st, blocks)
 
 
-def dam_break_3d(dx: float = 0.003, column=(0.6, 0.6, 1.2), tank=(1.6, 0.6, 1.2), layers: int = 3,
-                 jitter: float = 0.01, seed: int = 12345, ale: bool = True, solver: int = d.RUNGE_KUTTA,
-                 cfl: float = 0.2) -> Case:
-    """Config 1: 0.6 x 0.6 x 1.2 m column in a 1.6 x 0.6 x 1.2 m tank (dx = 3 mm: 16M fluid)."""
+def dam_break_3d_settings(dx: float = 0.003, column_height: float = 1.2, ale: bool = True,
+                          solver: int = d.RUNGE_KUTTA, cfl: float = 0.2) -> d.Settings:
+    """Settings of config 1: config 0's physics in 3D, with ALE shifting."""
     s = defaults(3)
     s.variant = d.VAR_ALE if ale else 0
     s.st_model = d.ST_NOST
     s.particle_step = dx
     s.H_fac = 1.3
-    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * column[2])
+    s.speed_sound = 10.0 * math.sqrt(2.0 * 9.81 * column_height)
     s.dsph_delta = 0.1
     s.visc_alpha = 0.01
     s.sig = 0.0
@@ -230,7 +237,14 @@ def dam_break_3d(dx: float = 0.003, column=(0.6, 0.6, 1.2), tank=(1.6, 0.6, 1.2)
     s.cfl = s.cfl_min = s.cfl_max = cfl
     s.delta_t_min = 1e-9
     s.max_shift_vel = 5.0
-    derive(s)
+    return derive(s)
+
+
+def dam_break_3d(dx: float = 0.003, column=(0.6, 0.6, 1.2), tank=(1.6, 0.6, 1.2), layers: int = 3,
+                 jitter: float = 0.01, seed: int = 12345, ale: bool = True, solver: int = d.RUNGE_KUTTA,
+                 cfl: float = 0.2) -> Case:
+    """Config 1: 0.6 x 0.6 x 1.2 m column in a 1.6 x 0.6 x 1.2 m tank (dx = 3 mm: 16M fluid)."""
+    s = dam_break_3d_settings(dx, column[2], ale, solver, cfl)
     rng = np.random.Generator(np.random.PCG64(seed))
     n = [int(round(column[k] / dx)) for k in range(3)]
     g = np.meshgrid(*[(np.arange(n[k]) + 0.5) * dx for k in range(3)], indexing="ij")
@@ -284,9 +298,9 @@ def _sphere_points(diam: float, dx: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray
     return pts + np.asarray(centre)
 
 
-def droplet_3d(diam: float = 1e-3, dx: float = 5e-5, air_speed: float = 30.0, seed: int = 7,
-               solver: int = d.RUNGE_KUTTA, cfl: float = 0.5, ale: bool = False) -> Case:
-    """A spherical droplet of the config-2 liquid in a uniform air stream (config 4 unit)."""
+def droplet_settings(dx: float = 5e-5, air_speed: float = 30.0, solver: int = d.RUNGE_KUTTA, cfl: float = 0.5,
+                     ale: bool = False) -> d.Settings:
+    """Settings of a config-4 droplet: the config-2 liquid and air, no gravity."""
     s = defaults(3)
     _liquid(s)
     _air(s, air_speed)
@@ -302,7 +316,13 @@ def droplet_3d(diam: float = 1e-3, dx: float = 5e-5, air_speed: float = 30.0, se
     s.cfl_max = cfl
     s.delta_t_min = 1e-12
     s.delta_t_max = 1e-5
-    derive(s)
+    return derive(s)
+
+
+def droplet_3d(diam: float = 1e-3, dx: float = 5e-5, air_speed: float = 30.0, seed: int = 7,
+               solver: int = d.RUNGE_KUTTA, cfl: float = 0.5, ale: bool = False) -> Case:
+    """A spherical droplet of the config-2 liquid in a uniform air stream (config 4 unit)."""
+    s = droplet_settings(dx, air_speed, solver, cfl, ale)
     rng = np.random.Generator(np.random.PCG64(seed))
     pts = _sphere_points(diam, dx)
     pts += rng.uniform(-0.01 * dx, 0.01 * dx, size=pts.shape)
@@ -310,16 +330,10 @@ def droplet_3d(diam: float = 1e-3, dx: float = 5e-5, air_speed: float = 30.0, se
     return Case("droplet_3d", s, st, _blocks(0, st.n))
 
 
-def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, jet_speed: float = 10.0,
-                  air_speed: float = 50.0, seed: int = 2024, ale: bool = False, solver: int = d.RUNGE_KUTTA,
-                  pipe_layers: int = 2) -> Case:
-    """Config-2 liquid jet in crossflow, ~n_target particles.
-
-    A ghost-walled pipe (diameter D) feeds a column that rises along +z and bends downstream along
-    +x with the crossflow; past the bend the column is broken into ligaments and droplets of
-    log-uniform diameter.  Liquid rho = 800, mu = 1.5e-3, sigma = 0.025; air 1.225 kg/m^3 moving at
-    air_speed along +x.  Fluid particles carry the jet velocity plus the local crossflow drift.
-    """
+def jet_settings(dx: float = 5e-5, jet_speed: float = 10.0, air_speed: float = 50.0, ale: bool = False,
+                 solver: int = d.RUNGE_KUTTA, max_points: int = 2_000_000) -> d.Settings:
+    """Settings of config 2: the liquid (rho 800, mu 1.5e-3, sigma 0.025, pairwise surface
+    tension), air at air_speed with the Gissler closure, c0 = 10 x the jet speed."""
     s = defaults(3)
     _liquid(s)
     _air(s, air_speed)
@@ -335,8 +349,41 @@ def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, 
     s.cfl_max = 0.5
     s.delta_t_min = 1e-12
     s.delta_t_max = 1e-5
-    s.max_points = 2_000_000
-    derive(s)
+    s.max_points = max_points
+    return derive(s)
+
+
+def settings_for(config: int) -> d.Settings:
+    """Settings of the five benchmark configurations: 0 the 2D dam break, 1 the 3D dam break with
+    ALE, 2 the jet in crossflow, 3 the same jet in the FP32 form with the learned closure, 4 a
+    droplet of the batched breakup sweep."""
+    if config == 0:
+        return dam_break_2d_settings()
+    if config == 1:
+        return dam_break_3d_settings()
+    if config == 2:
+        return jet_settings()
+    if config == 3:
+        s = jet_settings()
+        s.precision = d.PREC_MIXED
+        s.aero_closure = d.CLOSURE_LEARNED
+        return s
+    if config == 4:
+        return droplet_settings()
+    raise ValueError(f"no configuration {config}")
+
+
+def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, jet_speed: float = 10.0,
+                  air_speed: float = 50.0, seed: int = 2024, ale: bool = False, solver: int = d.RUNGE_KUTTA,
+                  pipe_layers: int = 2) -> Case:
+    """Config-2 liquid jet in crossflow, ~n_target particles.
+
+    A ghost-walled pipe (diameter D) feeds a column that rises along +z and bends downstream along
+    +x with the crossflow; past the bend the column is broken into ligaments and droplets of
+    log-uniform diameter.  Liquid rho = 800, mu = 1.5e-3, sigma = 0.025; air 1.225 kg/m^3 moving at
+    air_speed along +x.  Fluid particles carry the jet velocity plus the local crossflow drift.
+    """
+    s = jet_settings(dx, jet_speed, air_speed, ale, solver)
     rng = np.random.Generator(np.random.PCG64(seed))
     R = 0.5 * D
     m = int(math.ceil(R / dx)) + 1

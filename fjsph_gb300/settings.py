@@ -204,8 +204,10 @@ def read_vlm(path: str | Path) -> d.Vlm:
     return v
 
 
-def read_para(path: str | Path, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE) -> tuple[d.Settings, dict]:
-    """Settings from a reference para file, with Set_Values applied."""
+def read_para(path: str | Path, dim: int, variant: int = 0, st_model: int = d.ST_PAIRWISE,
+              apply_set_values: bool = True) -> tuple[d.Settings, dict]:
+    """Settings from a reference para file, with Set_Values applied (unless apply_set_values is
+    false: the file's values over the defaults, before any derivation)."""
     s = defaults(dim)
     s.variant = variant
     s.st_model = st_model
@@ -214,5 +216,6 @@ def read_para(path: str | Path, dim: int, variant: int = 0, st_model: int = d.ST
         extra["vlm_file"] = str(path)
     if s.delta_t_min > 0.0:
         s.delta_t = s.delta_t_min
-    derive(s)
+    if apply_set_values:
+        derive(s)
     return s, extra

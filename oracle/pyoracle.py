@@ -1,6 +1,8 @@
 """ctypes binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Mirrors fjsph_gb300.api.Context method by method so that parity tests call both the same way.
+Loads only oracle/libfjsph_oracle.so; the derived settings come from oracle/settings_ref.py, not
+from the library under test.
 Parity status: unpinned (see oracle.cpp).
 """
 from __future__ import annotations
@@ -13,6 +15,7 @@ from fjsph_gb300 import _cdefs as d
 from fjsph_gb300.state import BlockSpec, InletSpec, SPHState, blocks_to_c
 
 from .build import build
+from .settings_ref import derive as derive_settings
 
 _lib = None
 _P = C.c_void_p
@@ -89,7 +92,10 @@ class Oracle:
     def __init__(self, settings: d.Settings, blocks: list[BlockSpec], inlets: list[InletSpec] = ()):
         self._l = lib()
         self.dim = settings.dim
-        self._h = self._l.orc_create(C.byref(settings))
+        # the oracle derives the reference's derived settings itself (Set_Values, GetYcoef,
+        # get_n_full: oracle/settings_ref.py) from the case's inputs
+        own = derive_settings(settings.copy())
+        self._h = self._l.orc_create(C.byref(own))
         self.blocks = list(blocks)
         arr = blocks_to_c(self.blocks)
         nbb = sum(1 for b in blocks if not b.is_fluid)

@@ -13,6 +13,7 @@ import pytest
 
 from fjsph_gb300 import _cdefs as d
 from fjsph_gb300 import cases
+from fjsph_gb300.settings import derive
 from tests._util import assert_fields, assert_ints, n_bound, perturb, rel_err
 
 pytestmark = pytest.mark.gpu
@@ -181,6 +182,7 @@ def test_variant_residual(label, over):
         setattr(s, k, v)
     if s.st_model != d.ST_NOST:
         s.sig = 0.0728
+    derive(s)  # the derived settings follow the variant (kernel normalisation, pipe density, ycoef)
     c.settings = s
     ctx, orc, npds = _prepared(c, st)
     nb = n_bound(c.blocks)
