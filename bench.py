@@ -1,22 +1,33 @@
-"""Benchmark of the GB300 WCSPH hot path on the 2M-particle 3D jet in crossflow.
+"""Benchmark of the GB300 WCSPH hot path on config 2: the 2M-particle 3D jet in crossflow.
 
-One step = one Integrator::integrate (src/Integration.cpp:233): CFL time step, two neighbour
-searches, the pre-passes, and a full Runge-Kutta-4 step with its four residual evaluations.
-The input state is a seeded synthetic jet (fjsph_gb300.cases.jet_crossflow), resident in HBM
-when the timed region starts; the state and neighbour arrays exceed the 129 MB L2, so no flush
-is needed between steps.
+Workload (fjsph_gb300.cases.jet_crossflow_live, seeded synthetic inputs): a live inlet at dx =
+50 um feeds the jet through a ghost-walled 2 mm pipe -- BACK particles crossing the inlet plane
+insert new BUFFER particles, particles leaving the 20D x 20D x 10D domain downstream are deleted,
+insertions stop at 2M live particles -- into a 50 m/s crossflow with a 1/7-power-law boundary
+layer of thickness 5 mm (the analytic air field, settings asource FJSPH_POWER_LAW); pairwise
+surface tension and the Gissler aero closure.  The run starts from the jet already emitted (the
+bent column and droplets) at ~1.95M particles.
 
-The headline form is FP32 split precision with the learned aerodynamic closure.  Before the
-timed region (untimed) the closure network is trained on the GPU: samples are logged from seeded
-plain-closure jets (jet speed ~ U(5, 20) m/s, crossflow ~ U(30, 80) m/s) and fitted by the
-library's own BF16 training kernels.  The plain FP64 form and the FP32 form with the plain
-closure are timed beside it on the same state.
+One step = one Integrator::integrate (src/Integration.cpp:233): CFL time step, neighbour searches,
+the pre-passes, a Runge-Kutta-4 step with its four residual evaluations, and update_data
+(insertion and deletion).  Particle-steps count the fluid particles each step processed.  The
+state is resident in HBM when the timed region starts and is larger than the 129 MB L2, so no
+flush is needed between steps.
+
+The headline form is FP32 split precision with the learned aerodynamic closure; its network is
+trained untimed before the run on the GPU from samples logged by seeded plain-closure runs of the
+same workload (jet speed ~ U(5, 20) m/s, crossflow ~ U(30, 80) m/s).  The plain FP64 form and the
+FP32 form with the plain closure are timed beside it from the same start.  Side sections: the
+per-step error of the FP32 form against the FP64 oracle on a cut of the workload (`parity`),
+config 0 (2D dam break, 2000 steps, GPU and the CPU restatement on all host cores), config 1 (3D
+dam break, 16M fluid, FP32 against FP64 on identical states), config 4 (256 droplets), the air
+sources and host set-up.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n PARTICLES]
 
-Prints one JSON line (rank 0).  `--impl reference` times the CPU restatement of the reference
-algorithm (the oracle; the reference itself cannot be built here) on the host cores, on a bounded
-sample of the same workload.
+Prints one JSON line (rank 0).  `--impl reference` runs the CPU restatement of the reference
+algorithm (the oracle; the reference itself cannot be built here) on the same workload, all host
+cores, without loading the GPU library.
 """
 from __future__ import annotations
 
@@ -35,6 +46,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-steps/s, 2M-particle jet: FP32+learned aero vs plain FP64, same GB300"
 UNIT = "particle-steps/s"
+WORKLOAD = "jet_in_crossflow_3d_live_inlet"
 
 
 def parse():
@@ -43,7 +55,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=2_000_000, help="target particle count of the jet")
+    ap.add_argument("--n", type=int, default=2_000_000, help="particle cap of the live jet (max_points)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the plain FP64 form timed beside (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=4)
@@ -52,7 +64,8 @@ def parse():
                     help="cube edge of the tetrahedral air mesh over the jet (0 = skip)")
     ap.add_argument("--setup-particles", type=int, default=2_000_000,
                     help="particles of the block-file setup timing (0 = skip)")
-    ap.add_argument("--cpu-sample", type=int, default=120_000, help="particles in the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=110_000, help="fluid particles in the CPU baseline cut")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="oracle steps on the cut (baseline and parity)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--closure", default="learned", choices=["learned", "plain"])
     ap.add_argument("--train-samples", type=int, default=5_000_000)
@@ -64,18 +77,18 @@ def parse():
     ap.add_argument("--drops", type=int, default=256, help="droplets of the batched workload (0 = skip)")
     ap.add_argument("--drop-steps", type=int, default=10)
     ap.add_argument("--drop-steps-fp64", type=int, default=3)
+    ap.add_argument("--drop-long", type=int, default=3000, help="steps of the long FP32 droplet run (0 = skip)")
     ap.add_argument("--drop-sample", type=int, default=16, help="droplets timed alone for the per-droplet times")
+    ap.add_argument("--config0-steps", type=int, default=2000, help="2D dam-break steps (0 = skip)")
+    ap.add_argument("--no-config0-cpu", action="store_true")
+    ap.add_argument("--config1-dx", type=float, default=0.003, help="spacing of the 3D dam break (0 = skip)")
+    ap.add_argument("--config1-steps", type=int, default=3, help="timed FP32 steps of the 3D dam break")
+    ap.add_argument("--config1-long", type=int, default=0, help="a long FP32 run of the 3D dam break (steps)")
     ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
 
 # ---------------------------------------------------------------------------------------------
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
-
 
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
@@ -123,103 +136,6 @@ class Clocks:
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
-
-
-def measured_peaks() -> dict:
-    p = ROOT / "MEASURED_PEAKS.json"
-    if p.exists():
-        return json.loads(p.read_text())
-    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
-
-
-# ---------------------------------------------------------------------------------------------
-def resid_bytes_per_particle(s) -> int:
-    """Algorithmic bytes of one residual evaluation per fluid particle.
-
-    Each logical field is counted once per launch; neighbour re-reads and the pair list do not
-    count.  FP64 form (8 B words): x 3, search x 3, v 3, rho, p, m, aVisc 3, deltaD, cellV 3,
-    cellP, cellRho, lam_nb, woccl (8 B each), cellID, CSR offset (8 B), b, surfzone (4 B); ALE adds
-    vPert 3, NOFROZEN gradRho 3.  Writes acc 3, Af 3, Rrho.
-    FP32 split-precision form: x and v as an FP32 high part and a bf16 low part (6 B per
-    component), rho, p / rho^2 with the type flags and volume at 4 B; aVisc 3 and deltaD (FP64
-    state), CSR offset and cellID (8 B); the closure reads
-    cellV 3, cellP, cellRho, m, lam_nb, woccl (8 B), the learned closure also the four occlusion
-    inputs, the normal and lambda (4 B each).  Writes acc 3, Af 3, Rrho at 8 B.
-    """
-    from fjsph_gb300 import _cdefs as d
-    D = s.dim
-    if s.precision == d.PREC_MIXED:
-        b = 6 * D * 2 + 4 * 3                      # x, v (FP32 high, bf16 low), rho, p/rho^2, volume
-        b += 8 * (D + 1) + 8 * 2                   # aVisc, deltaD, CSR offset, cellID
-        b += 8 * (D + 5)                           # cellV, cellP, cellRho, m, lam_nb, woccl
-        if s.aero_closure == d.CLOSURE_LEARNED:
-            b += 4 * (4 + D + 1)                   # occlusion inputs, normal, lambda
-        if s.variant & d.VAR_ALE:
-            b += 4 * D
-        if s.variant & d.VAR_NOFROZEN:
-            b += 4 * D
-        return b + 8 * (2 * D + 1)
-    r8 = 3 * D + 3 + 3 + D + 1 + D + 2 + 2 + 2 + 1
-    if s.variant & d.VAR_ALE:
-        r8 += D
-    if s.variant & d.VAR_NOFROZEN:
-        r8 += D
-    w8 = 2 * D + 1
-    return 8 * (r8 + w8) + 4 * 2
-
-
-# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
-# 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
-# the benchmark's particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 709.41e6 / 620_210}
-
-
-def train_closure(args, log):
-    """Untimed: log samples from seeded plain-closure jets and train the network on the GPU."""
-    import numpy as np
-    from fjsph_gb300 import closure as cl
-    info = {}
-    if args.closure_weights and Path(args.closure_weights).exists():
-        info["weights"] = f"loaded from {args.closure_weights}"
-        return np.load(args.closure_weights).astype(np.float32), info
-    t0 = time.perf_counter()
-    specs = cl.jet_specs(args.train_jets, 800_000, seed=2024)
-    X, T = cl.collect_samples(specs, args.train_samples, steps=8)
-    t1 = time.perf_counter()
-    p0 = cl.init_params(X, T, seed=7)
-    p, loss = cl.train(p0, X, T, epochs=args.train_epochs, batch=4096, lr=2e-3, seed=8)
-    t2 = time.perf_counter()
-    info.update(samples=int(len(X)), jets=len(specs), log_s=round(t1 - t0, 2), train_s=round(t2 - t1, 2),
-                epochs=args.train_epochs, final_loss=loss,
-                jet_speeds=[round(sp.jet_speed, 2) for sp in specs], air_speeds=[round(sp.air_speed, 2) for sp in specs])
-    if args.save_weights:
-        np.save(args.save_weights, p)
-    log(f"closure trained: {info}")
-    return p, info
-
-
-def make_case(n_target: int, precision: str, closure: str = "plain"):
-    from fjsph_gb300 import cases, _cdefs as d
-    c = cases.jet_crossflow(n_target=n_target)
-    if precision == "mixed":
-        c.settings.precision = d.PREC_MIXED
-        if closure == "learned":
-            c.settings.aero_closure = d.CLOSURE_LEARNED
-    return c
-
-
-def timed_steps(ctx, steps: int, ws: int) -> float:
-    ctx.event_record(0)
-    for _ in range(steps):
-        ctx.integrate()
-    ctx.event_record(1)
-    return reduce_max(ws, ctx.event_elapsed(0, 1))
-
-
-# Examples/VLM: a 22.3 m half-span, 8.5 m chord wing, sweep 32.5 deg, taper 0.6, 20 deg flap
-VLM_WING = dict(span=22.275, chord=8.491, panels_span=50, panels_chord=14, aoa_deg=5.0, sweep_deg=32.5, taper=0.6,
-                flap_start=3, flap_width=24, flap_depth=6, flap_deg=20.0)
-VLM_VINF = (89.69, 0.0, 7.8466)
 
 
 def run_vlm(args):
@@ -325,7 +241,7 @@ def run_mesh(args, case):
     s.asource = d.MESH_INFL
     s.precision = d.PREC_MIXED
     s.aero_closure = d.CLOSURE_PLAIN
-    ctx = Context(s, st.n + 1024, case.blocks)
+    ctx = Context(s, s.max_points + 1024, case.blocks, case.inlets)
     t0 = time.perf_counter()
     ctx.mesh_set(mesh)
     set_s = time.perf_counter() - t0
@@ -346,7 +262,7 @@ def run_mesh(args, case):
 
     def steps_ms(settings, with_mesh):
         """whole steps after three warm-up steps, this context alone on the GPU"""
-        cx = Context(settings, st.n + 1024, case.blocks)
+        cx = Context(settings, settings.max_points + 1024, case.blocks, case.inlets)
         if with_mesh:
             cx.mesh_set(mesh)
         cx.set_states(st, st)
@@ -370,205 +286,6 @@ def run_mesh(args, case):
             "fp32_step_ms": round(step_ms, 3), "particle_steps_per_s": case.n_fluid / (step_ms / 1e3),
             "fp32_step_ms_uniform_source": round(uniform_ms, 3),
             "mesh_build_s": round(build_s, 2), "mesh_set_s": round(set_s, 3)}
-
-
-def run_droplets(args, ws, rank, weights):
-    """Config 4: a batch of independent droplets in one context per GPU (droplets shared out over
-    the ranks with no exchange), each step one CUDA-graph replay; plain FP64, FP32 with the plain
-    closure and FP32 with the learned closure.  Rank 0 also times a sample of droplets alone (one
-    context each) for the per-droplet step times of the unbatched form."""
-    import numpy as np
-    from fjsph_gb300 import _cdefs as d
-    from fjsph_gb300 import cases
-    from fjsph_gb300.api import Context
-    full = cases.droplet_batch(n_drops=args.drops)
-    ids = cases.shard_ids(len(full.counts), full.counts, rank, ws)
-    b = full.subset(ids) if ws > 1 else full
-    n = b.case.state.n
-    total = full.case.state.n
-    out = {"droplets": int(len(full.counts)), "particles": int(total), "counts_range": [int(full.counts.min()),
-           int(full.counts.max())], "we_range": [round(float(full.we.min()), 1), round(float(full.we.max()), 1)],
-           "sharding": f"{ws} rank(s), greedy particle balance, no collective but the final timing max",
-           "config_steps": 3000, "forms": {}}
-    forms = [("fp64", d.PREC_FP64, d.CLOSURE_PLAIN, args.drop_steps_fp64),
-             ("fp32_plain_closure", d.PREC_MIXED, d.CLOSURE_PLAIN, args.drop_steps),
-             ("fp32_learned_closure", d.PREC_MIXED, d.CLOSURE_LEARNED, args.drop_steps)]
-    for name, prec, closure, steps in forms:
-        if closure == d.CLOSURE_LEARNED and weights is None:
-            continue
-        s = b.case.settings.copy()
-        s.precision = prec
-        s.aero_closure = closure
-        ctx = Context(s, n + 64, b.case.blocks)
-        ctx.set_groups(b.first, b.v_inf)
-        ctx.set_states(b.case.state, b.case.state)
-        if closure == d.CLOSURE_LEARNED:
-            ctx.closure_set_weights(weights, 0.05)
-        tune = ctx.autotune(3)["chosen"] if prec == d.PREC_MIXED and not args.no_tune else None
-        ctx.integrate_groups(2, graph=True)  # one ordinary step, then the graph capture
-        barrier(ws)
-        ctx.launch_stats(reset=True)
-        ctx.event_record(0)
-        ctx.integrate_groups(steps, graph=True)
-        ctx.event_record(1)
-        ms = reduce_max(ws, ctx.event_elapsed(0, 1))
-        rep = ctx.group_report()
-        out["forms"][name] = {"value": total * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
-                              "steps": steps, "gpu_launches_per_step": ctx.launch_stats() / steps,
-                              "graph": True, "autotune": tune,
-                              "per_droplet_step_ms": {"p50": ms / steps, "p99": ms / steps},
-                              "dt_range": [float(rep["dt"].min()), float(rep["dt"].max())]}
-        ctx.close()
-    if rank == 0 and args.drop_sample > 0:
-        order = np.argsort(full.counts)
-        pick = order[np.linspace(0, len(order) - 1, min(args.drop_sample, len(order))).astype(int)]
-        t_ms, ns = [], []
-        for g in pick:
-            c = full.single(int(g))
-            s = c.settings.copy()
-            s.precision = d.PREC_MIXED
-            ctx = Context(s, c.state.n + 64, c.blocks)
-            ctx.set_states(c.state, c.state)
-            for _ in range(2):
-                ctx.integrate()
-            ctx.event_record(0)
-            for _ in range(3):
-                ctx.integrate()
-            ctx.event_record(1)
-            t_ms.append(ctx.event_elapsed(0, 1) / 3)
-            ns.append(c.state.n)
-            ctx.close()
-        t_ms, ns = np.array(t_ms), np.array(ns, dtype=np.float64)
-        a, b0 = np.polyfit(ns, t_ms, 1)
-        seq_ms = float(np.sum(np.maximum(a * full.counts + b0, t_ms.min())))
-        out["alone_fp32_plain_closure"] = {
-            "sample": f"{len(pick)} droplets spread over the count range, one context each, 3 steps",
-            "per_droplet_step_ms": {"p50": float(np.percentile(t_ms, 50)), "p99": float(np.percentile(t_ms, 99))},
-            "sequential_step_ms_all_droplets": seq_ms,
-            "value": total / (seq_ms / 1e3), "unit": UNIT}
-    return out
-
-
-def run_ours(args, ws, rank, local):
-    import numpy as np
-    from fjsph_gb300 import _cdefs as d
-    from fjsph_gb300.api import Context
-
-    learned = args.precision == "mixed" and args.closure == "learned"
-    weights, closure_info = (train_closure(args, lambda m: print(m, file=sys.stderr)) if learned else (None, None))
-    c = make_case(args.n, args.precision, args.closure)
-    s = c.settings
-    nf = c.n_fluid
-    ctx = Context(s, c.state.n + 1024, c.blocks)
-    ctx.set_states(c.state, c.state)
-    if learned:
-        ctx.closure_set_weights(weights, 0.05)
-    for _ in range(args.warmup):
-        ctx.integrate()
-    tune = ctx.autotune(3) if s.precision == d.PREC_MIXED and not args.no_tune else None
-    if tune:
-        ctx.integrate()  # one more warm-up step under the chosen configuration
-    barrier(ws)
-    clocks = Clocks(local)
-    clocks.start()
-    ctx.profile(True)
-    ctx.launch_stats(reset=True)
-    ctx.event_record(0)
-    for _ in range(args.steps):
-        ctx.integrate()
-    ctx.event_record(1)
-    ms = ctx.event_elapsed(0, 1)
-    launches = ctx.launch_stats()
-    n_pairs = ctx.update_neighbours()  # pairs of the last search (outside the timed region)
-    prof = ctx.profile_read()
-    ctx.profile(False)
-    clk = clocks.stop()
-    ms = reduce_max(ws, ms)
-    rep = ctx.step_report()
-    value = nf * args.steps * ws / (ms / 1e3)
-
-    # roofline of the dominant kernel: the residual
-    peaks = measured_peaks()
-    r_ms, r_cnt = prof["residual"]
-    bpp = resid_bytes_per_particle(s)
-    per_launch = r_ms / max(r_cnt, 1) / 1e3
-    achieved = bpp * nf / per_launch / 1e9
-    tkey = "fp64" if s.precision == d.PREC_FP64 else ("mixed_learned" if learned else None)
-    traffic = round(RESID_TRAFFIC_PER_PARTICLE[tkey] * nf) if tkey else None
-    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-            "frac": round(achieved / peaks.get("hbm_gbs", 6800.0), 4), "traffic": traffic,
-            "traffic_source": "ncu capture on the 634k-particle jet, scaled by fluid particles" if tkey else None,
-            "kernel": ("k_m_resid" if s.precision == d.PREC_MIXED else "k_resid") + " (get_acc_and_Rrho)", "launch_ms": round(per_launch * 1e3, 3),
-            "bytes_per_launch": bpp * nf, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
-
-    # the learned closure judged against the plain one on the state the timed steps reached
-    if learned:
-        ctx.closure_arm(d.CLOSURE_ARM_JUDGE)
-        ctx.integrate()
-        rep_c = ctx.closure_report()
-        closure_info.update(judge_rel_rms=rep_c["last_rel_rms"], judge_particles=rep_c["judged_particles"],
-                            judged=rep_c["judged"], fallback=bool(rep_c["fallback"]),
-                            learned_active=bool(rep_c["learned_active"]),
-                            judge_interval_steps=s.learned_judge_interval)
-
-    # end to end through the public API with host buffers in pinned memory: upload the step's
-    # input fields (FJSPH_STEP_FIELDS, as both pn and pnp1), one step, download the same fields of
-    # the new state, every step
-    e2e = None
-    if args.e2e_steps > 0:
-        from fjsph_gb300.state import STEP_FIELDS
-        host = pinned_state(ctx.download())
-        ctx.event_record(2)
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            ctx.upload(d.BOTH, host, fields=STEP_FIELDS)  # pn = pnp1 at a step's start
-            ctx.integrate()
-            download_into(ctx, host, STEP_FIELDS)
-        ctx.event_record(3)
-        e2e_ms = ctx.event_elapsed(2, 3)
-        wall = time.perf_counter() - t0
-        e2e_ms = reduce_max(ws, max(e2e_ms, wall * 1e3))
-        nbytes = state_bytes(host, STEP_FIELDS)
-        e2e = {"value": nf * args.e2e_steps * ws / (e2e_ms / 1e3), "unit": UNIT,
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "pinned": host._pinned,
-               "fields": "FJSPH_STEP_FIELDS (the state a step reads; the rest is recomputed inside it)"}
-
-    # the FP32 form with the plain closure on the same state
-    plain = None
-    if learned and args.plain_steps > 0:
-        sp_ = s.copy()
-        sp_.aero_closure = d.CLOSURE_PLAIN
-        cp = Context(sp_, c.state.n + 1024, c.blocks)
-        cp.set_states(c.state, c.state)
-        cp.integrate()
-        cp.profile(True)
-        msp = timed_steps(cp, args.plain_steps, ws)
-        pp = cp.profile_read()
-        plain = {"value": nf * args.plain_steps * ws / (msp / 1e3), "ms_per_step": msp / args.plain_steps,
-                 "residual_ms_per_launch": round(pp["residual"][0] / max(pp["residual"][1], 1), 4),
-                 "steps": args.plain_steps}
-        cp.close()
-
-    # the plain FP64 form on the same state, same GPU
-    fp64 = None
-    if args.fp64_steps > 0 and s.precision != d.PREC_FP64:
-        s64 = s.copy()
-        s64.precision = d.PREC_FP64
-        s64.aero_closure = d.CLOSURE_PLAIN
-        c64 = Context(s64, c.state.n + 1024, c.blocks)
-        c64.set_states(c.state, c.state)
-        c64.integrate()
-        c64.event_record(0)
-        for _ in range(args.fp64_steps):
-            c64.integrate()
-        c64.event_record(1)
-        ms64 = reduce_max(ws, c64.event_elapsed(0, 1))
-        fp64 = {"value": nf * args.fp64_steps * ws / (ms64 / 1e3), "ms_per_step": ms64 / args.fp64_steps,
-                "steps": args.fp64_steps}
-        c64.close()
-    return dict(value=value, ms=ms, nf=nf, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches, fp64=fp64,
-                prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s, case=c,
-                plain=plain, closure=closure_info, pairs=n_pairs, tune=tune, weights=weights)
 
 
 def pinned_state(st):
@@ -602,46 +319,6 @@ def state_bytes(st, fields=None) -> int:
     return int(sum(getattr(st, f).nbytes for f in (fields or ALL_FIELDS)))
 
 
-def cpu_sample_case(c, n_sample: int):
-    """A spatially contiguous cut of the workload: the fluid particles nearest the pipe exit plus
-    the walls they touch, about n_sample particles."""
-    import numpy as np
-    from fjsph_gb300.state import BlockSpec
-    st = c.state
-    nb = sum(b.second - b.first for b in c.blocks if not b.is_fluid)
-    fl = np.arange(nb, st.n)
-    order = fl[np.argsort(np.linalg.norm(st.xi[fl] - np.array([0.0, 0.0, 0.0]), axis=1))]
-    keep_f = np.sort(order[: max(n_sample - nb // 4, 1000)])
-    xmax = np.linalg.norm(st.xi[keep_f], axis=1).max() + 4 * c.settings.H
-    wb = np.arange(nb)
-    keep_b = wb[np.linalg.norm(st.xi[wb], axis=1) < xmax]
-    idx = np.concatenate([keep_b, keep_f])
-    sub = st.take(idx)
-    sub.part_id[:] = np.arange(sub.n)
-    blocks = []
-    if len(keep_b):
-        b0 = [b for b in c.blocks if not b.is_fluid][0]
-        blocks.append(BlockSpec(0, len(keep_b), False, bound_solver=b0.bound_solver))
-    fb = [b for b in c.blocks if b.is_fluid][0]
-    blocks.append(BlockSpec(len(keep_b), sub.n, True, aero_norm=fb.aero_norm, aeroconst=fb.aeroconst))
-    return sub, blocks, len(keep_f)
-
-
-def run_cpu(c, steps: int, warmup: int, n_sample: int, threads: int):
-    from oracle.pyoracle import Oracle, set_threads
-    set_threads(threads)
-    sub, blocks, nf = cpu_sample_case(c, n_sample)
-    o = Oracle(c.settings, blocks)
-    o.set_states(sub, sub)
-    for _ in range(warmup):
-        o.integrate()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        o.integrate()
-    dt = time.perf_counter() - t0
-    return nf * steps / dt, nf, dt
-
-
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -658,6 +335,600 @@ def reduce_max(ws, x: float) -> float:
     return float(t.item())
 
 
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+# ---------------------------------------------------------------------------------------------
+
+
+def resid_bytes_per_particle(s) -> int:
+    """Algorithmic bytes of one residual evaluation per fluid particle.
+
+    Each logical field is counted once per launch; neighbour re-reads and the pair list do not
+    count.  FP64 form (8 B words): x 3, search x 3, v 3, rho, p, m, aVisc 3, deltaD, cellV 3,
+    cellP, cellRho, lam_nb, woccl (8 B each), cellID, CSR offset (8 B), b, surfzone (4 B); ALE adds
+    vPert 3, NOFROZEN gradRho 3.  Writes acc 3, Af 3, Rrho.
+    FP32 split-precision form: x and v as an FP32 high part and a bf16 low part (6 B per
+    component), rho, p / rho^2 with the type flags and volume at 4 B; aVisc 3 and deltaD (FP64
+    state), CSR offset and cellID (8 B); the closure reads
+    cellV 3, cellP, cellRho, m, lam_nb, woccl (8 B), the learned closure also the four occlusion
+    inputs, the normal and lambda (4 B each).  Writes acc 3, Af 3, Rrho at 8 B.
+    """
+    from fjsph_gb300 import _cdefs as d
+    D = s.dim
+    if s.precision == d.PREC_MIXED:
+        b = 6 * D * 2 + 4 * 3                      # x, v (FP32 high, bf16 low), rho, p/rho^2, volume
+        b += 8 * (D + 1) + 8 * 2                   # aVisc, deltaD, CSR offset, cellID
+        b += 8 * (D + 5)                           # cellV, cellP, cellRho, m, lam_nb, woccl
+        if s.aero_closure == d.CLOSURE_LEARNED:
+            b += 4 * (4 + D + 1)                   # occlusion inputs, normal, lambda
+        if s.variant & d.VAR_ALE:
+            b += 4 * D
+        if s.variant & d.VAR_NOFROZEN:
+            b += 4 * D
+        return b + 8 * (2 * D + 1)
+    r8 = 3 * D + 3 + 3 + D + 1 + D + 2 + 2 + 2 + 1
+    if s.variant & d.VAR_ALE:
+        r8 += D
+    if s.variant & d.VAR_NOFROZEN:
+        r8 += D
+    w8 = 2 * D + 1
+    return 8 * (r8 + w8) + 4 * 2
+
+
+# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
+# 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
+# the benchmark's particle count (traffic grows with the particle and pair counts).
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 709.41e6 / 620_210}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
+# 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
+# the benchmark's particle count (traffic grows with the particle and pair counts).
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 709.41e6 / 620_210}
+
+# Examples/VLM: a 22.3 m half-span, 8.5 m chord wing, sweep 32.5 deg, taper 0.6, 20 deg flap
+VLM_WING = dict(span=22.275, chord=8.491, panels_span=50, panels_chord=14, aoa_deg=5.0, sweep_deg=32.5, taper=0.6,
+                flap_start=3, flap_width=24, flap_depth=6, flap_deg=20.0)
+VLM_VINF = (89.69, 0.0, 7.8466)
+
+
+def train_closure(args, log):
+    """Untimed: log samples from seeded plain-closure runs of the workload and train the network
+    on the GPU."""
+    import numpy as np
+    from fjsph_gb300 import closure as cl
+    info = {}
+    if args.closure_weights and Path(args.closure_weights).exists():
+        info["weights"] = f"loaded from {args.closure_weights}"
+        return np.load(args.closure_weights).astype(np.float32), info
+    t0 = time.perf_counter()
+    specs = cl.jet_specs(args.train_jets, 800_000, seed=2024, live=True)
+    X, T = cl.collect_samples(specs, args.train_samples, steps=8)
+    t1 = time.perf_counter()
+    p0 = cl.init_params(X, T, seed=7)
+    p, loss = cl.train(p0, X, T, epochs=args.train_epochs, batch=4096, lr=2e-3, seed=8)
+    t2 = time.perf_counter()
+    info.update(samples=int(len(X)), jets=len(specs), log_s=round(t1 - t0, 2), train_s=round(t2 - t1, 2),
+                epochs=args.train_epochs, final_loss=loss,
+                jet_speeds=[round(sp.jet_speed, 2) for sp in specs], air_speeds=[round(sp.air_speed, 2) for sp in specs])
+    if args.save_weights:
+        np.save(args.save_weights, p)
+    log(f"closure trained: {info}")
+    return p, info
+
+
+def make_case(n_cap: int, precision: str, closure: str = "plain"):
+    from fjsph_gb300 import cases, _cdefs as d
+    c = cases.jet_crossflow_live(n_target=n_cap, cap=n_cap)
+    if precision == "mixed":
+        c.settings.precision = d.PREC_MIXED
+        if closure == "learned":
+            c.settings.aero_closure = d.CLOSURE_LEARNED
+    return c
+
+
+def new_ctx(settings, c, state=None):
+    """A context for case c under `settings` (capacity: the insertion cap), with the case's inlet
+    tables and analytic air field, holding `state` (default: the case's start)."""
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300.api import Context
+    ctx = Context(settings, settings.max_points + 1024, c.blocks, c.inlets)
+    if settings.asource == d.POWER_LAW and c.power_law_params:
+        ctx.air_power_law(*c.power_law_params)
+    st = state if state is not None else c.state
+    ctx.set_states(st, st)
+    return ctx
+
+
+def counted_steps(ctx, steps: int, nb: int) -> tuple[float, int]:
+    """steps integrate() calls between two events on the context's stream; returns the device
+    time (ms) and the fluid particle-steps processed (the count changes with insertion and
+    deletion: each step counts the particles it started with)."""
+    ps = 0
+    ctx.event_record(0)
+    for _ in range(steps):
+        ps += ctx.particle_count() - nb
+        ctx.integrate()
+    ctx.event_record(1)
+    return ctx.event_elapsed(0, 1), ps
+
+
+def prefix_state(big, n: int):
+    """The first n particles of a (pinned) state, as a state sharing its memory."""
+    from fjsph_gb300.state import ALL_FIELDS, SPHState
+    out = SPHState.__new__(SPHState)
+    out.n, out.dim = int(n), big.dim
+    for f in ALL_FIELDS:
+        setattr(out, f, getattr(big, f)[:n])
+    out._pinned = getattr(big, "_pinned", False)
+    return out
+
+
+
+
+def pinned_buffer(n: int, dim: int):
+    """A zeroed state of n particles in page-locked host memory (torch only allocates)."""
+    from fjsph_gb300.state import SPHState
+    return pinned_state(SPHState(n, dim))
+
+
+def roofline(s, prof, nf_mean: float, peaks: dict, learned: bool) -> dict:
+    """The residual (the dominant kernel): algorithmic bytes per fluid particle x the fluid
+    particles of a launch, over the launch's mean device time from the profile events."""
+    from fjsph_gb300 import _cdefs as d
+    r_ms, r_cnt = prof["residual"]
+    bpp = resid_bytes_per_particle(s)
+    per_launch = r_ms / max(r_cnt, 1) / 1e3
+    achieved = bpp * nf_mean / per_launch / 1e9
+    tkey = "fp64" if s.precision == d.PREC_FP64 else ("mixed_learned" if learned else None)
+    traffic = round(RESID_TRAFFIC_PER_PARTICLE[tkey] * nf_mean) if tkey else None
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "traffic_source": "ncu capture on the 634k-particle jet, scaled by fluid particles" if tkey else None,
+            "kernel": ("k_m_resid" if s.precision == d.PREC_MIXED else "k_resid") + " (get_acc_and_Rrho)",
+            "launch_ms": round(per_launch * 1e3, 3), "bytes_per_launch": round(bpp * nf_mean),
+            "bytes_per_particle": bpp, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300.state import STEP_FIELDS
+
+    learned = args.precision == "mixed" and args.closure == "learned"
+    weights, closure_info = (train_closure(args, lambda m: print(m, file=sys.stderr)) if learned else (None, None))
+    c = make_case(args.n, args.precision, args.closure)
+    s = c.settings
+    nb = c.state.n - c.n_fluid
+    ctx = new_ctx(s, c)
+    if learned:
+        ctx.closure_set_weights(weights, 0.05)
+    for _ in range(args.warmup):
+        ctx.integrate()
+    tune = ctx.autotune(3) if s.precision == d.PREC_MIXED and not args.no_tune else None
+    if tune:
+        ctx.integrate()  # one more warm-up step under the chosen configuration
+    barrier(ws)
+    clocks = Clocks(local)
+    clocks.start()
+    ctx.profile(True)
+    ctx.launch_stats(reset=True)
+    ins0, del0 = ctx.update_counts()
+    ms, ps = counted_steps(ctx, args.steps, nb)
+    launches = ctx.launch_stats()
+    ins1, del1 = ctx.update_counts()
+    n_pairs = ctx.update_neighbours()  # pairs of the last search (outside the timed region)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    clk = clocks.stop()
+    ms = reduce_max(ws, ms)
+    value = ps * ws / (ms / 1e3)
+    nf_mean = ps / args.steps
+    rep = ctx.step_report()
+    roof = roofline(s, prof, nf_mean, measured_peaks(), learned)
+    live = {"particles_at_start": int(c.state.n), "particles_at_end": int(ctx.particle_count()),
+            "inserted_in_timed_steps": int(ins1 - ins0), "deleted_in_timed_steps": int(del1 - del0),
+            "inserted_total": int(ins1), "deleted_total": int(del1), "cap": int(s.max_points),
+            "mean_fluid_per_step": round(nf_mean, 1)}
+
+    # the learned closure judged against the plain one on the state the timed steps reached
+    if learned:
+        ctx.closure_arm(d.CLOSURE_ARM_JUDGE)
+        ctx.integrate()
+        rep_c = ctx.closure_report()
+        closure_info.update(judge_rel_rms=rep_c["last_rel_rms"], judge_particles=rep_c["judged_particles"],
+                            judged=rep_c["judged"], fallback=bool(rep_c["fallback"]),
+                            learned_active=bool(rep_c["learned_active"]),
+                            judge_interval_steps=s.learned_judge_interval)
+
+    # end to end through the public API with host buffers in pinned memory: every step uploads the
+    # step's input fields (FJSPH_STEP_FIELDS, as both pn and pnp1) and downloads the same fields
+    # of the new state; the particle count follows the inlet and the deletion plane
+    e2e = None
+    if args.e2e_steps > 0:
+        host = pinned_buffer(s.max_points + 1024, s.dim)
+        ctx.download(d.PNP1, out=prefix_state(host, ctx.particle_count()))
+        h2d = d2h = 0
+        ps_e = 0
+        ctx.event_record(2)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            n = ctx.particle_count()
+            st = prefix_state(host, n)
+            ctx.upload(d.BOTH, st, fields=STEP_FIELDS)  # pn = pnp1 at a step's start
+            ctx.integrate()
+            st2 = prefix_state(host, ctx.particle_count())
+            ctx.download(d.PNP1, fields=STEP_FIELDS, out=st2)
+            h2d += state_bytes(st, STEP_FIELDS)
+            d2h += state_bytes(st2, STEP_FIELDS)
+            ps_e += n - nb
+        ctx.event_record(3)
+        e2e_ms = ctx.event_elapsed(2, 3)
+        wall = time.perf_counter() - t0
+        e2e_ms = reduce_max(ws, max(e2e_ms, wall * 1e3))
+        e2e = {"value": ps_e * ws / (e2e_ms / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
+               "pinned": host._pinned,
+               "fields": "FJSPH_STEP_FIELDS (the state a step reads; the rest is recomputed inside it)"}
+    ctx.close()
+
+    def other_form(settings, steps):
+        cx = new_ctx(settings, c)
+        cx.integrate()
+        cx.profile(True)
+        msx, psx = counted_steps(cx, steps, nb)
+        msx = reduce_max(ws, msx)
+        pp = cx.profile_read()
+        cx.close()
+        return {"value": psx * ws / (msx / 1e3), "ms_per_step": msx / steps, "steps": steps,
+                "residual_ms_per_launch": round(pp["residual"][0] / max(pp["residual"][1], 1), 4)}
+
+    plain = None
+    if learned and args.plain_steps > 0:
+        sp_ = s.copy()
+        sp_.aero_closure = d.CLOSURE_PLAIN
+        plain = other_form(sp_, args.plain_steps)
+    fp64 = None
+    if args.fp64_steps > 0 and s.precision != d.PREC_FP64:
+        s64 = s.copy()
+        s64.precision = d.PREC_FP64
+        s64.aero_closure = d.CLOSURE_PLAIN
+        fp64 = other_form(s64, args.fp64_steps)
+    return dict(value=value, ms=ms, nf=c.n_fluid, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches,
+                fp64=fp64, prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s,
+                case=c, plain=plain, closure=closure_info, pairs=n_pairs, tune=tune, weights=weights, live=live,
+                ps=ps)
+
+
+def _rel_rms(a, b) -> float:
+    import numpy as np
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    den = float(np.sqrt(np.mean(b * b))) if b.size else 0.0
+    return float(np.sqrt(np.mean((a - b) ** 2)) / den) if den > 0 else 0.0
+
+
+def run_cpu_parity(args, c, threads: int):
+    """The CPU restatement (oracle, FP64, OpenMP on all host cores) on a contiguous cut of the
+    workload -- the cpu_baseline timing -- and, on the same cut and states, the error of the FP32
+    form against it: the residual on the oracle's pre-pass outputs, then each timed oracle step
+    against one FP32 step from the same state (both time levels)."""
+    import dataclasses
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300 import cases
+    from oracle.pyoracle import Oracle, set_threads
+    set_threads(threads)
+    cc = cases.cut(c, args.cpu_sample)
+    s64 = cc.settings.copy()
+    s64.precision = d.PREC_FP64
+    s64.aero_closure = d.CLOSURE_PLAIN
+    cc = dataclasses.replace(cc, settings=s64)
+    s32 = s64.copy()
+    s32.precision = d.PREC_MIXED
+    nb = sum(b.second - b.first for b in cc.blocks if not b.is_fluid)
+    nf = cc.state.n - nb
+
+    def oracle():
+        o = Oracle(cc.settings, cc.blocks)
+        if cc.power_law_params:
+            o.air_power_law(*cc.power_law_params)
+        o.set_states(cc.state, cc.state)
+        return o
+
+    # the residual alone on the oracle's pre-pass outputs
+    o = oracle()
+    o.update_neighbours()
+    npd = o.dSPH_PreStep()
+    o.get_aero_velocity()
+    o.Detect_Surface()
+    o.dissipation_terms()
+    o.Boundary_Ghost()
+    prepared = o.download()
+    o.get_acc_and_Rrho(npd)
+    ref = o.download()
+    o.close()
+    g_ctx = new_ctx(s32, cc, prepared)
+    g_ctx.update_neighbours()
+    g_ctx.get_acc_and_Rrho(npd)
+    g = g_ctx.download()
+    g_ctx.close()
+    sl = slice(nb, None)
+    resid = {"Rrho": _rel_rms(g.Rrho[sl], ref.Rrho[sl]), "acc": _rel_rms(g.acc[sl], ref.acc[sl]),
+             "Af": _rel_rms(g.Af[sl], ref.Af[sl])}
+    # timed oracle steps (the baseline), each compared with one FP32 step from the same state
+    o = oracle()
+    steps, t_cpu, e_x, e_rho = [], 0.0, [], []
+    for k in range(args.cpu_steps):
+        pn, pnp1, sk = o.download(d.PN), o.download(d.PNP1), o.settings
+        t0 = time.perf_counter()
+        o.integrate()
+        t_cpu += time.perf_counter() - t0
+        r = o.download()
+        sk.precision = d.PREC_MIXED
+        gx = new_ctx(sk, cc, pnp1)
+        gx.upload(d.PN, pn)
+        gx.integrate()
+        gs = gx.download()
+        gx.close()
+        e_x.append(_rel_rms(gs.xi[sl] - pnp1.xi[sl], r.xi[sl] - pnp1.xi[sl]))
+        e_rho.append(_rel_rms(gs.rho[sl] - pnp1.rho[sl], r.rho[sl] - pnp1.rho[sl]))
+    o.close()
+    cpu = {"value": nf * args.cpu_steps / t_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{args.cpu_steps} Integrator::integrate steps of the {nf} fluid particles nearest the pipe "
+                     f"exit cut from the workload (CPU restatement, {t_cpu:.1f} s)"}
+    parity = {"reference": "oracle (FP64 CPU restatement)", "cut_fluid_particles": nf, "form": "FP32, plain closure",
+              "residual_rel_rms": resid, "step_displacement_rel_rms": e_x, "step_density_change_rel_rms": e_rho,
+              "targets": {"Rrho": 1e-5, "acc": 1e-3}}
+    return cpu, parity
+
+
+def run_config0(args, threads: int, rank: int):
+    """Config 0: the 2D dam break (20,000 fluid particles, RK4, CFL 0.2) for its full step count on
+    the GPU (FP64 and FP32 forms) and on the host cores (the CPU restatement)."""
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300 import cases
+    steps = args.config0_steps
+    c = cases.dam_break_2d()
+    nb = c.state.n - c.n_fluid
+    out = {"case": "2D dam break: 1.0 x 2.0 m column, 4.0 x 3.0 m tank, dx 0.01, 3 wall layers, RK4, CFL 0.2",
+           "particles": int(c.state.n), "fluid": int(c.n_fluid), "steps": steps}
+    finals = {}
+    for name, prec in (("gpu_fp64", d.PREC_FP64), ("gpu_fp32", d.PREC_MIXED)):
+        s = c.settings.copy()
+        s.precision = prec
+        warm = new_ctx(s, c)  # first launches and allocations outside the timing
+        for _ in range(3):
+            warm.integrate()
+        warm.close()
+        ctx = new_ctx(s, c)
+        pairs = ctx.update_neighbours()
+        t0 = time.perf_counter()
+        ms, ps = counted_steps(ctx, steps, nb)
+        wall = time.perf_counter() - t0
+        finals[name] = ctx.download()
+        out[name] = {"value": ps / (ms / 1e3), "unit": UNIT, "wall_s": round(wall, 3),
+                     "neighbour_pairs_per_s": pairs * steps / (ms / 1e3),
+                     "sim_time_s": ctx.settings.current_time}
+        ctx.close()
+    if rank == 0 and not args.no_config0_cpu:
+        from oracle.pyoracle import Oracle, set_threads
+        set_threads(threads)
+        o = Oracle(c.settings, c.blocks)
+        o.set_states(c.state, c.state)
+        pairs = o.update_neighbours()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.integrate()
+        wall = time.perf_counter() - t0
+        r = o.download()
+        out["cpu"] = {"value": c.n_fluid * steps / wall, "unit": UNIT, "cores": threads, "kind": "port",
+                      "wall_s": round(wall, 2), "neighbour_pairs_per_s": pairs * steps / wall,
+                      "sim_time_s": o.settings.current_time}
+        sl = slice(nb, None)
+        out["final_state_gpu_fp64_vs_cpu"] = {
+            "x_rel_rms": _rel_rms(finals["gpu_fp64"].xi[sl], r.xi[sl]),
+            "rho_rel_rms": _rel_rms(finals["gpu_fp64"].rho[sl], r.rho[sl])}
+        out["final_state_gpu_fp32_vs_cpu"] = {
+            "x_rel_rms": _rel_rms(finals["gpu_fp32"].xi[sl], r.xi[sl]),
+            "rho_rel_rms": _rel_rms(finals["gpu_fp32"].rho[sl], r.rho[sl])}
+        o.close()
+    return out
+
+
+def run_config1(args):
+    """Config 1: the 3D dam break (0.6 x 0.6 x 1.2 m column, 1.6 x 0.6 x 1.2 m tank, dx 3 mm: ~16M
+    fluid and ~2.1M wall particles, lattice jittered by +-0.01 dx, ALE shifting) on one GPU: FP32
+    and FP64 forms timed, and one step of each from the identical start compared."""
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300 import cases
+    t0 = time.perf_counter()
+    c = cases.dam_break_3d(dx=args.config1_dx)
+    build_s = time.perf_counter() - t0
+    nb = c.state.n - c.n_fluid
+    out = {"case": f"3D dam break, dx {args.config1_dx * 1e3:g} mm, ALE, jitter +-0.01 dx, RK4, CFL 0.2",
+           "particles": int(c.state.n), "fluid": int(c.n_fluid), "build_s": round(build_s, 1)}
+    fields = ["xi", "rho", "acc", "Rrho"]
+    first = {}
+    for name, prec, steps in (("fp32", d.PREC_MIXED, args.config1_steps), ("fp64", d.PREC_FP64, 1)):
+        s = c.settings.copy()
+        s.precision = prec
+        ctx = new_ctx(s, c)
+        ctx.integrate()
+        first[name] = ctx.download(d.PNP1, fields=fields)
+        pairs = ctx.update_neighbours()
+        ctx.profile(True)
+        ms, ps = counted_steps(ctx, steps, nb)
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        out[name] = {"value": ps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+                     "neighbour_pairs": int(pairs), "neighbour_pairs_per_s": pairs * steps / (ms / 1e3),
+                     "passes_ms_per_step": {k: round(v[0] / steps, 3) for k, v in prof.items() if v[1]}}
+        if name == "fp32" and args.config1_long > 0:
+            ms_l, ps_l = counted_steps(ctx, args.config1_long, nb)
+            out["fp32_long"] = {"steps": args.config1_long, "value": ps_l / (ms_l / 1e3), "unit": UNIT,
+                                "wall_s": round(ms_l / 1e3, 1), "sim_time_s": ctx.settings.current_time}
+        ctx.close()
+    sl = slice(nb, None)
+    a, b = first["fp32"], first["fp64"]
+    x0 = c.state.xi[sl]
+    out["step_error_fp32_vs_fp64"] = {
+        "displacement_rel_rms": _rel_rms(a.xi[sl] - x0, b.xi[sl] - x0),
+        "density_change_rel_rms": _rel_rms(a.rho[sl] - c.state.rho[sl], b.rho[sl] - c.state.rho[sl]),
+        "acc_rel_rms": _rel_rms(a.acc[sl], b.acc[sl]), "Rrho_rel_rms": _rel_rms(a.Rrho[sl], b.Rrho[sl]),
+        "note": "one integrate step of each form from the identical start; the FP64 form is checked against "
+                "the oracle on cuts (tests/test_gpu_scale.py)"}
+    out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def run_droplets(args, ws, rank, weights):
+    """Config 4: a batch of independent droplets in one context per GPU (droplets shared out over
+    the ranks with no exchange), each step one CUDA-graph replay; plain FP64, FP32 with the plain
+    closure and FP32 with the learned closure.  Per-droplet work: each droplet's share of the
+    batch step by its neighbour pairs.  Rank 0 also times a sample of droplets alone (one context
+    each) and runs the FP32 batch for the configuration's 3000 steps."""
+    import numpy as np
+    from fjsph_gb300 import _cdefs as d
+    from fjsph_gb300 import cases
+    from fjsph_gb300.api import Context
+    full = cases.droplet_batch(n_drops=args.drops)
+    ids = cases.shard_ids(len(full.counts), full.counts, rank, ws)
+    b = full.subset(ids) if ws > 1 else full
+    n = b.case.state.n
+    total = full.case.state.n
+    out = {"droplets": int(len(full.counts)), "particles": int(total), "counts_range": [int(full.counts.min()),
+           int(full.counts.max())], "we_range": [round(float(full.we.min()), 1), round(float(full.we.max()), 1)],
+           "sharding": f"{ws} rank(s), greedy particle balance, no collective but the final timing max",
+           "config_steps": 3000, "forms": {},
+           "launch": "each pass one launch over all droplets, a step one CUDA-graph replay (no persistent kernel)"}
+    forms = [("fp64", d.PREC_FP64, d.CLOSURE_PLAIN, args.drop_steps_fp64),
+             ("fp32_plain_closure", d.PREC_MIXED, d.CLOSURE_PLAIN, args.drop_steps),
+             ("fp32_learned_closure", d.PREC_MIXED, d.CLOSURE_LEARNED, args.drop_steps)]
+    long_form = None
+    for name, prec, closure, steps in forms:
+        if closure == d.CLOSURE_LEARNED and weights is None:
+            continue
+        s = b.case.settings.copy()
+        s.precision = prec
+        s.aero_closure = closure
+        ctx = Context(s, n + 64, b.case.blocks)
+        ctx.set_groups(b.first, b.v_inf)
+        ctx.set_states(b.case.state, b.case.state)
+        if closure == d.CLOSURE_LEARNED:
+            ctx.closure_set_weights(weights, 0.05)
+        tune = ctx.autotune(3)["chosen"] if prec == d.PREC_MIXED and not args.no_tune else None
+        ctx.integrate_groups(2, graph=True)  # one ordinary step, then the graph capture
+        barrier(ws)
+        ctx.launch_stats(reset=True)
+        ctx.event_record(0)
+        ctx.integrate_groups(steps, graph=True)
+        ctx.event_record(1)
+        ms = reduce_max(ws, ctx.event_elapsed(0, 1))
+        rep = ctx.group_report()
+        ctx.update_neighbours()
+        cnt = ctx.neighbour_counts().astype(np.float64)
+        pairs_g = np.add.reduceat(cnt, b.first[:-1])
+        work = (ms / steps) * pairs_g / pairs_g.sum()  # each droplet's share of the batch step
+        out["forms"][name] = {"value": total * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                              "steps": steps, "gpu_launches_per_step": ctx.launch_stats() / steps,
+                              "graph": True, "autotune": tune,
+                              "batch_step_ms": ms / steps,
+                              "per_droplet_work_ms": {"p50": float(np.percentile(work, 50)),
+                                                      "p99": float(np.percentile(work, 99)),
+                                                      "basis": "share of the batch step by neighbour pairs"},
+                              "dt_range": [float(rep["dt"].min()), float(rep["dt"].max())]}
+        if rank == 0 and args.drop_long > 0 and prec == d.PREC_MIXED and (closure == d.CLOSURE_LEARNED or
+                                                                            weights is None):
+            long_form = name
+            t0 = time.perf_counter()
+            ctx.event_record(2)
+            ctx.integrate_groups(args.drop_long, graph=True)
+            ctx.event_record(3)
+            ms_l = ctx.event_elapsed(2, 3)
+            rep_l = ctx.group_report()
+            out["long_run"] = {"form": name, "steps": args.drop_long, "value": total * args.drop_long / (ms_l / 1e3),
+                               "unit": UNIT, "ms_per_step": ms_l / args.drop_long,
+                               "wall_s": round(time.perf_counter() - t0, 1),
+                               "sim_time_range_s": [float(rep_l["time"].min()), float(rep_l["time"].max())]}
+        ctx.close()
+    if rank == 0 and args.drop_sample > 0:
+        order = np.argsort(full.counts)
+        pick = order[np.linspace(0, len(order) - 1, min(args.drop_sample, len(order))).astype(int)]
+        t_ms, ns = [], []
+        for g in pick:
+            c = full.single(int(g))
+            s = c.settings.copy()
+            s.precision = d.PREC_MIXED
+            ctx = Context(s, c.state.n + 64, c.blocks)
+            ctx.set_states(c.state, c.state)
+            for _ in range(2):
+                ctx.integrate()
+            ctx.event_record(0)
+            for _ in range(3):
+                ctx.integrate()
+            ctx.event_record(1)
+            t_ms.append(ctx.event_elapsed(0, 1) / 3)
+            ns.append(c.state.n)
+            ctx.close()
+        t_ms, ns = np.array(t_ms), np.array(ns, dtype=np.float64)
+        a, b0 = np.polyfit(ns, t_ms, 1)
+        seq_ms = float(np.sum(np.maximum(a * full.counts + b0, t_ms.min())))
+        out["alone_fp32_plain_closure"] = {
+            "sample": f"{len(pick)} droplets spread over the count range, one context each, 3 steps",
+            "per_droplet_step_ms": {"p50": float(np.percentile(t_ms, 50)), "p99": float(np.percentile(t_ms, 99))},
+            "sequential_step_ms_all_droplets": seq_ms,
+            "value": total / (seq_ms / 1e3), "unit": UNIT}
+    return out
+
+
+def run_reference(args, threads: int, ws: int) -> dict:
+    """The CPU restatement of the reference algorithm (the oracle) on the same workload: the live
+    jet at the same cap, built with the oracle's own settings derivation (no GPU library is
+    loaded), stepped with OpenMP on all host cores; each step counts the fluid particles it
+    started with."""
+    from fjsph_gb300 import cases
+    from oracle import settings_ref
+    from oracle.pyoracle import Oracle, set_threads
+    cases.defaults, cases.derive = settings_ref.defaults, settings_ref.derive
+    c = cases.jet_crossflow_live(n_target=args.n, cap=args.n)
+    nb = c.state.n - c.n_fluid
+    set_threads(threads)
+    o = Oracle(c.settings, c.blocks, c.inlets)
+    o.air_power_law(*c.power_law_params)
+    o.set_states(c.state, c.state)
+    for _ in range(min(args.warmup, 1)):
+        o.integrate()
+    ps = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ps += o.particle_count() - nb
+        o.integrate()
+    dt = time.perf_counter() - t0
+    v = ps / dt
+    sample = (f"the live-inlet jet itself ({c.state.n} particles at the start, cap {args.n}), "
+              f"{args.steps} Integrator::integrate steps after {min(args.warmup, 1)} warm-up, OpenMP")
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "particles": int(c.state.n), "fluid": int(c.n_fluid), "cap": args.n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -665,17 +936,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        c = make_case(args.n, "fp64")
-        v, nf, dt = run_cpu(c, args.steps, min(args.warmup, 1), args.cpu_sample, threads)
-        sample = (f"{nf} fluid particles nearest the pipe exit cut from the {c.n_fluid}-particle jet, "
-                  f"{args.steps} Integrator::integrate steps, OpenMP")
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "jet_in_crossflow_3d", "particles": c.state.n, "fluid": c.n_fluid},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(run_reference(args, threads, ws)))
         return 0
     if ws > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
@@ -688,27 +949,31 @@ def main():
     vlm = run_vlm(args) if (args.vlm_points > 0 and rank == 0) else None
     setup = run_case_setup(args) if (args.setup_particles > 0 and rank == 0) else None
     mesh = run_mesh(args, r["case"]) if (args.mesh_cell > 0 and rank == 0) else None
+    cfg0 = run_config0(args, threads, rank) if (args.config0_steps > 0 and rank == 0) else None
+    cfg1 = run_config1(args) if (args.config1_dx > 0 and rank == 0) else None
     if rank == 0:
-        cpu = None
+        cpu = parity = None
         if not args.no_cpu:
-            v, nf, dt = run_cpu(r["case"], 1, 0, args.cpu_sample, threads)
-            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"1 integrate step of {nf} fluid particles cut from the jet (CPU restatement, "
-                             f"{dt:.1f} s)"}
+            cpu, parity = run_cpu_parity(args, r["case"], threads)
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else ("f32+f64+bf16" if args.closure == "learned" else "f32+f64"),
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else ("f32+f64+bf16" if args.closure == "learned" else "f32+f64"),
                 "data": "synthetic",
-                "config": {"workload": "jet_in_crossflow_3d", "particles": r["n"], "fluid": r["nf"],
+                "config": {"workload": WORKLOAD, "particles": r["n"], "fluid": r["nf"], "cap": args.n,
+                           "air": "50 m/s crossflow, 1/7-power-law boundary layer 5 mm over z = 0",
                            "form": args.precision, "closure": args.closure if args.precision == "mixed" else "plain",
                            "integrator": "runge_kutta4",
                            "l2": "inputs larger than L2 (state ~1 GB)", "parallelism": f"replicas{ws}"},
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
-                "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"], "closure": r["closure"],
-                "neighbour_pairs": r["pairs"], "autotune": r["tune"], "droplet_batch": drops,
-                "vlm_air_source": vlm, "mesh_air_source": mesh, "case_setup": setup,
+                "parity": parity, "live_inlet": r["live"],
+                "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"],
+                "speedup_vs_fp64_form": (r["value"] / r["fp64"]["value"]) if r["fp64"] else None,
+                "closure": r["closure"], "neighbour_pairs": r["pairs"], "autotune": r["tune"],
                 "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
-                "gpu_launches": r["launches"], "passes_ms": r["prof"]}
+                "gpu_launches": r["launches"], "passes_ms": r["prof"],
+                "config0_dam_break_2d": cfg0, "config1_dam_break_3d": cfg1, "droplet_batch": drops,
+                "vlm_air_source": vlm, "mesh_air_source": mesh, "case_setup": setup}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist

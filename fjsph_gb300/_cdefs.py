@@ -18,6 +18,7 @@ DBC, PRESSURE_G, GHOST = 0, 1, 2
 COLE_EOS, ISO_EOS = 0, 1
 NOAERO, GISSLER, INDUCED_PRESSURE, SKIN_FRIC = 0, 1, 2, 3
 CONST_VEL, MESH_INFL, VLM_INFL = 0, 1, 2  # fjsph_aero_source
+POWER_LAW = 100  # analytic boundary-layer air field (fjsph_air_power_law)
 PREC_FP64, PREC_MIXED = 0, 1
 PAIRS_TILES, PAIRS_LISTS = 0, 1
 CLOSURE_PLAIN, CLOSURE_LEARNED = 0, 1

@@ -58,6 +58,8 @@ PROTOTYPES = {
     "fjsph_step_report": (C.c_int, [_P, _dp]),
     "fjsph_timestep_maxima": (C.c_int, [_P, _dp]),
     "fjsph_set_pair_mode": (C.c_int, [_P, _i32]),
+    "fjsph_air_power_law": (C.c_int, [_P, _dp]),
+    "fjsph_neighbour_counts": (C.c_int, [_P, _i32p]),
     "fjsph_get_pair_mode": (C.c_int, [_P, _i32p, _i32p]),
     "fjsph_launch_stats": (C.c_int, [_P, _i64p, _i32]),
     "fjsph_ctx_stream": (C.c_int, [_P, _pp]),

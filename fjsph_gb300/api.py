@@ -204,6 +204,18 @@ class Context:
         check("fjsph_integrate_n", self._lib.fjsph_integrate_n(self._h, int(n_steps), C.byref(r)))
         return r.value
 
+    def neighbour_counts(self) -> np.ndarray:
+        """Neighbours (self included) of every particle in reference order, from the last search."""
+        out = np.zeros(self.particle_count(), dtype=np.int32)
+        check("fjsph_neighbour_counts", self._lib.fjsph_neighbour_counts(self._h, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def particle_count(self) -> int:
+        """Particles in the context now (insertions and deletions included)."""
+        n = C.c_int64()
+        check("fjsph_particle_count", self._lib.fjsph_particle_count(self._h, C.byref(n), None))
+        return n.value
+
     def limits(self) -> list:
         """(first, second) of every LIMITS entry as update_data left them."""
         nb = C.c_int32()
@@ -276,6 +288,12 @@ class Context:
         out = (C.c_double * 5)()
         check("fjsph_step_report", self._lib.fjsph_step_report(self._h, out))
         return dict(maxRho_pc=out[0], maxf=out[1], maxAf=out[2], maxShift=out[3], iteration=int(out[4]))
+
+    def air_power_law(self, axis: int, wall: float, thickness: float, exponent: float = 1.0 / 7.0) -> None:
+        """The analytic boundary-layer air field of a context with asource = FJSPH_POWER_LAW:
+        v_inf * clamp((x[axis] - wall) / thickness, 0, 1)^exponent."""
+        p = (C.c_double * 4)(float(axis), wall, thickness, exponent)
+        check("fjsph_air_power_law", self._lib.fjsph_air_power_law(self._h, p))
 
     def set_pair_mode(self, mode: int) -> None:
         """d.PAIRS_LISTS (pair lists, default) or d.PAIRS_TILES (shared-memory tiles for the residual)."""

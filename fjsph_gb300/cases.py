@@ -34,6 +34,7 @@ class Case:
     blocks: list[BlockSpec]
     inlets: list[InletSpec] = field(default_factory=list)
     mesh: object = None  # the air mesh of a mesh-source case (fjsph_gb300.mesh.CellMesh)
+    power_law_params: tuple = None  # (axis, wall, thickness, exponent) of an FJSPH_POWER_LAW case
 
     @property
     def n_fluid(self) -> int:
@@ -385,34 +386,69 @@ def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, 
     """
     s = jet_settings(dx, jet_speed, air_speed, ale, solver)
     rng = np.random.Generator(np.random.PCG64(seed))
-    R = 0.5 * D
-    m = int(math.ceil(R / dx)) + 1
-    ax = np.arange(-m, m + 1) * dx
-    gx, gy = np.meshgrid(ax, ax, indexing="ij")
-    disk = np.stack([gx.ravel(), gy.ravel()], axis=1)
-    disk = disk[np.einsum("ij,ij->i", disk, disk) <= R * R]
+    disk = _disk(0.5 * D, dx)
     # pipe walls: rings from R + dx/2 outward, z in [-4D, 0)
     pipe_len = 4.0 * D
     zs = (np.arange(int(pipe_len / dx)) + 0.5) * dx - pipe_len
-    wall = []
-    for k in range(pipe_layers):
-        rr = R + (k + 0.5) * dx
-        nth = int(round(2 * math.pi * rr / dx))
-        th = np.arange(nth) * 2 * math.pi / nth
-        ring = np.stack([rr * np.cos(th), rr * np.sin(th)], axis=1)
-        for z in zs:
-            wall.append(np.concatenate([ring, np.full((nth, 1), z)], axis=1))
-    bound = np.concatenate(wall)
+    bound = _pipe_walls(0.5 * D, dx, zs, pipe_layers)
     parts, vels, types = [], [], []
     # liquid inside the pipe: PIPE particles
     for z in zs:
         parts.append(np.concatenate([disk, np.full((len(disk), 1), z)], axis=1))
         vels.append(np.tile([0.0, 0.0, jet_speed], (len(disk), 1)))
         types.append(np.full(len(disk), d.PIPE))
-    # intact column: centreline bends from +z towards +x over a quarter circle of radius 5D
+    n_now = sum(len(p) for p in parts)
+    col, colv, drops, dropv = _jet_free_parts(disk, D, dx, jet_speed, air_speed, n_target - n_now, rng)
+    parts += [col, drops]
+    vels += [colv, dropv]
+    types += [np.full(len(col), d.FREE), np.full(len(drops), d.FREE)]
+    fluid = np.concatenate(parts)
+    v = np.concatenate(vels)
+    b = np.concatenate(types)
+    fluid += rng.uniform(-0.01 * dx, 0.01 * dx, size=fluid.shape)
+    st = _assemble(s, bound, fluid)
+    st.v[len(bound):] = v
+    st.b[len(bound):] = b
+    blocks = _blocks(len(bound), st.n, bound_solver=d.GHOST)
+    fl = blocks[-1]
+    fl.aero_norm = (0.0, 0.0, 1.0)
+    fl.aeroconst = 0.0
+    return Case("jet_crossflow", s, st, blocks)
+
+
+def _disk(R: float, dx: float) -> np.ndarray:
+    """Lattice points of spacing dx inside a disk of radius R (the pipe's cross-section)."""
+    m = int(math.ceil(R / dx)) + 1
+    ax = np.arange(-m, m + 1) * dx
+    gx, gy = np.meshgrid(ax, ax, indexing="ij")
+    disk = np.stack([gx.ravel(), gy.ravel()], axis=1)
+    return disk[np.einsum("ij,ij->i", disk, disk) <= R * R]
+
+
+def _pipe_walls(R: float, dx: float, zs: np.ndarray, layers: int) -> np.ndarray:
+    """Ghost-wall rings of a pipe along z: `layers` rings from R + dx/2 outward at every z."""
+    wall = []
+    for k in range(layers):
+        rr = R + (k + 0.5) * dx
+        nth = int(round(2 * math.pi * rr / dx))
+        th = np.arange(nth) * 2 * math.pi / nth
+        ring = np.stack([rr * np.cos(th), rr * np.sin(th)], axis=1)
+        for z in zs:
+            wall.append(np.concatenate([ring, np.full((nth, 1), z)], axis=1))
+    return np.concatenate(wall)
+
+
+def _jet_free_parts(disk: np.ndarray, D: float, dx: float, jet_speed: float, air_speed: float, n_free: int,
+                    rng) -> tuple:
+    """The emitted jet above the pipe exit: an intact column whose centreline bends from +z to +x
+    over a quarter circle of radius 5D, then droplets of log-uniform diameter (6 dx .. 0.9 D)
+    downstream of the bend, x in [5.5D, 20D], |y| < 4D, z in [3D, 9D], kept 2 dx apart, until
+    about n_free particles.  Returns (column points, their velocities, droplet points, velocities);
+    the column is ordered from the exit outward."""
     Rb = 5.0 * D
     arc = 0.5 * math.pi * Rb
     nlay = int(arc / dx)
+    col, colv = [], []
     for k in range(nlay):
         phi = (k * dx) / Rb
         c = np.array([Rb * (1 - math.cos(phi)), 0.0, Rb * math.sin(phi)])
@@ -420,18 +456,16 @@ def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, 
         e1 = np.array([math.cos(phi), 0.0, -math.sin(phi)])
         e2 = np.array([0.0, 1.0, 0.0])
         pts = c + disk[:, :1] * e1 + disk[:, 1:2] * e2
-        parts.append(pts)
-        vels.append(np.tile(jet_speed * t + np.array([0.2 * air_speed * math.sin(phi), 0.0, 0.0]), (len(pts), 1)))
-        types.append(np.full(len(pts), d.FREE))
-    n_now = sum(len(p) for p in parts)
-    # droplets downstream of the bend, x in [5.5D, 20D], |y| < 4D, z in [3D, 9D]; an occupancy grid
-    # at the lattice spacing keeps droplets at least 2 dx apart
+        col.append(pts)
+        colv.append(np.tile(jet_speed * t + np.array([0.2 * air_speed * math.sin(phi), 0.0, 0.0]), (len(pts), 1)))
+    n_now = sum(len(p) for p in col)
     lo = np.array([Rb + 0.5 * D - D, -5 * D, 2 * D])
     hi = np.array([21 * D, 5 * D, 10 * D])
     shape = tuple(np.ceil((hi - lo) / dx).astype(int) + 1)
     occ = np.zeros(shape, dtype=bool)
     tries = 0
-    while n_now < n_target and tries < 200000:
+    drops, dropv = [], []
+    while n_now < n_free and tries < 200000:
         tries += 1
         dd = math.exp(rng.uniform(math.log(6 * dx), math.log(0.9 * D)))
         centre = np.array([rng.uniform(Rb + 0.5 * D, 20 * D), rng.uniform(-4 * D, 4 * D), rng.uniform(3 * D, 9 * D)])
@@ -447,23 +481,91 @@ def jet_crossflow(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, 
                     g2 = gi + np.array([ox, oy, oz])
                     g2 = np.clip(g2, 0, np.array(shape) - 1)
                     occ[g2[:, 0], g2[:, 1], g2[:, 2]] = True
-        parts.append(pts)
+        drops.append(pts)
         drift = 0.5 * air_speed * (centre[0] - Rb) / (20 * D - Rb)
-        vels.append(np.tile([jet_speed * 0.3 + drift, 0.0, 0.2 * jet_speed], (len(pts), 1)))
-        types.append(np.full(len(pts), d.FREE))
+        dropv.append(np.tile([jet_speed * 0.3 + drift, 0.0, 0.2 * jet_speed], (len(pts), 1)))
         n_now += len(pts)
+    cat = lambda a, w: np.concatenate(a) if a else np.zeros((0, w))
+    return cat(col, 3), cat(colv, 3), cat(drops, 3), cat(dropv, 3)
+
+
+BL_THICKNESS = 5e-3  # boundary-layer thickness of the config-2 crossflow (m)
+
+
+def jet_crossflow_live(n_target: int = 2_000_000, D: float = 2e-3, dx: float = 5e-5, jet_speed: float = 10.0,
+                       air_speed: float = 50.0, seed: int = 2024, cap: int = 2_000_000, headroom: int = 50_000,
+                       pipe_layers: int = 80, depth: int = 4, solver: int = d.RUNGE_KUTTA) -> Case:
+    """Config 2 as specified: the jet in crossflow fed by a live inlet.
+
+    One fluid block of type inletZone (src/shapes/inlet.cpp): a pipe of diameter D along +z with
+    ghost walls, `depth` BUFFER layers below the BACK layer at z_b = -pipe_layers dx, PIPE layers
+    up to the exit at z = 0, and above it the jet already emitted (the bent column and droplets of
+    jet_crossflow), about n_target - headroom particles in all.  The insertion plane lies 0.02 dx
+    above BACK, so every column inserts a BUFFER particle whenever its BACK particle crosses it;
+    particles crossing x = 20.5 D (the downstream end of the 20D x 20D x 10D domain) are deleted;
+    insertions stop at `cap` particles (max_points; raised to the start's count + headroom when the
+    emitted column alone exceeds it).  The air is the analytic crossflow: 50 m/s
+    along +x with a 1/7-power-law boundary layer of thickness 5 mm over the wall z = 0 (settings
+    asource FJSPH_POWER_LAW; apply with Context.air_power_law(*power_law_params)).  Fluid order is by
+    age as insertion produces it (the reference's table bookkeeping depends on it): droplets, the
+    column from its far end, the PIPE layers from the top, BACK, the BUFFER layers.
+    """
+    s = jet_settings(dx, jet_speed, air_speed, False, solver, max_points=cap)
+    s.asource = d.POWER_LAW
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R = 0.5 * D
+    disk = _disk(R, dx)
+    nd = len(disk)
+    z_b = -pipe_layers * dx
+    zs = z_b - depth * dx + np.arange(pipe_layers + depth + 1) * dx
+    bound = _pipe_walls(R, dx, zs, 2)
+
+    def layer(z):
+        return np.concatenate([disk, np.full((nd, 1), z)], axis=1)
+
+    n_inlet = (pipe_layers + depth) * nd
+    col, colv, drops, dropv = _jet_free_parts(disk, D, dx, jet_speed, air_speed,
+                                              n_target - headroom - n_inlet - len(bound), rng)
+    # oldest first: droplets furthest downstream first, then the column from its far end
+    order = np.argsort(-drops[:, 0], kind="stable") if len(drops) else np.zeros(0, dtype=np.int64)
+    drops, dropv = drops[order], dropv[order]
+    col, colv = col[::-1], colv[::-1]
+    parts = [drops, col]
+    vels = [dropv, colv]
+    types = [np.full(len(drops), d.FREE), np.full(len(col), d.FREE)]
+    for k in reversed(range(1, pipe_layers)):
+        parts.append(layer(z_b + k * dx))
+        vels.append(np.tile([0.0, 0.0, jet_speed], (nd, 1)))
+        types.append(np.full(nd, d.PIPE))
+    parts.append(layer(z_b))
+    vels.append(np.tile([0.0, 0.0, jet_speed], (nd, 1)))
+    types.append(np.full(nd, d.BACK))
+    for j in range(depth):  # buffer layer j is (j + 1) dx below BACK
+        parts.append(layer(z_b - (j + 1) * dx))
+        vels.append(np.tile([0.0, 0.0, jet_speed], (nd, 1)))
+        types.append(np.full(nd, d.BUFFER))
     fluid = np.concatenate(parts)
-    v = np.concatenate(vels)
-    b = np.concatenate(types)
-    fluid += rng.uniform(-0.01 * dx, 0.01 * dx, size=fluid.shape)
+    fluid[:, :2] += rng.uniform(-0.01 * dx, 0.01 * dx, size=(len(fluid), 2))
     st = _assemble(s, bound, fluid)
-    st.v[len(bound):] = v
-    st.b[len(bound):] = b
-    blocks = _blocks(len(bound), st.n, bound_solver=d.GHOST)
+    nb = len(bound)
+    st.v[nb:] = np.concatenate(vels)
+    st.b[nb:] = np.concatenate(types)
+    s.max_points = max(cap, st.n + headroom)  # the emitted column alone may exceed a small cap
+    blocks = _blocks(nb, st.n, bound_solver=d.GHOST)
     fl = blocks[-1]
+    fl.block_type = 6  # inletZone
+    fl.insert_norm = (0.0, 0.0, 1.0)
+    fl.insconst = z_b + 0.02 * dx
+    fl.delete_norm = (1.0, 0.0, 0.0)
+    fl.delconst = 20.5 * D
     fl.aero_norm = (0.0, 0.0, 1.0)
     fl.aeroconst = 0.0
-    return Case("jet_crossflow", s, st, blocks)
+    first_back = nb + len(drops) + len(col) + (pipe_layers - 1) * nd
+    back = first_back + np.arange(nd)
+    buffer = np.stack([first_back + (j + 1) * nd + np.arange(nd) for j in range(depth)], axis=1)
+    c = Case("jet_crossflow_live", s, st, blocks, [InletSpec(len(blocks) - 1, back, buffer)])
+    c.power_law_params = (2, 0.0, BL_THICKNESS, 1.0 / 7.0)
+    return c
 
 
 def jet_inlet(D: float = 1e-3, dx: float = 5e-5, jet_speed: float = 10.0, air_speed: float = 50.0,
@@ -676,3 +778,33 @@ def droplet_in_mesh(dim: int = 2, diam: float = 1.2e-3, dx: float = 1e-4, air_sp
     pts = pts + rng.uniform(-0.01 * dx, 0.01 * dx, size=pts.shape)
     st = _assemble(s, np.zeros((0, dim)), pts)
     return Case(f"droplet_in_mesh_{dim}d", s, st, _blocks(0, st.n)), mesh
+
+
+def cut(c: Case, n_sample: int, centre=(0.0, 0.0, 0.0)) -> Case:
+    """A spatially contiguous cut of a case at the same spacing and coordinates: the fluid
+    particles nearest `centre` (about n_sample of them) and the boundary particles within reach of
+    them, as one boundary block (the case's first boundary solver) and one plain fluid block (the
+    case's aero plane; no inlet).  Particle types, velocities and densities are kept."""
+    st = c.state
+    nb = sum(b.second - b.first for b in c.blocks if not b.is_fluid)
+    ctr = np.asarray(centre, dtype=np.float64)[: st.dim]
+    fl = np.arange(nb, st.n)
+    dist = np.linalg.norm(st.xi[fl] - ctr, axis=1)
+    keep_f = np.sort(fl[np.argsort(dist, kind="stable")[:n_sample]])
+    reach = np.linalg.norm(st.xi[keep_f] - ctr, axis=1).max() + 4 * c.settings.H
+    wb = np.arange(nb)
+    keep_b = wb[np.linalg.norm(st.xi[wb] - ctr, axis=1) < reach]
+    sub = st.take(np.concatenate([keep_b, keep_f]))
+    sub.part_id[:] = np.arange(sub.n)
+    blocks = []
+    if len(keep_b):
+        b0 = [b for b in c.blocks if not b.is_fluid][0]
+        blocks.append(BlockSpec(0, len(keep_b), False, bound_solver=b0.bound_solver))
+    fb = [b for b in c.blocks if b.is_fluid][0]
+    blocks.append(BlockSpec(len(keep_b), sub.n, True, aero_norm=fb.aero_norm, aeroconst=fb.aeroconst))
+    s = c.settings.copy()
+    s.max_points = sub.n
+    out = Case(c.name + "_cut", s, sub, blocks)
+    out.power_law_params = c.power_law_params
+    return out
+

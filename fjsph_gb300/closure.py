@@ -129,19 +129,26 @@ class JetSpec:
     air_speed: float
     seed: int
     D: float = 2e-3
+    live: bool = False  # config 2 as specified: live inlet and power-law crossflow
 
 
-def jet_specs(n_runs: int, n_target: int, seed: int = 0, D: float = 2e-3) -> list[JetSpec]:
+def jet_specs(n_runs: int, n_target: int, seed: int = 0, D: float = 2e-3, live: bool = False) -> list[JetSpec]:
     """Seeded jet-in-crossflow runs with jet speed ~ U(5, 20) m/s and crossflow ~ U(30, 80) m/s."""
     rng = np.random.Generator(np.random.PCG64(seed))
     return [JetSpec(n_target, float(rng.uniform(5.0, 20.0)), float(rng.uniform(30.0, 80.0)),
-                    int(rng.integers(1 << 30)), D) for _ in range(n_runs)]
+                    int(rng.integers(1 << 30)), D, live) for _ in range(n_runs)]
 
 
 def jet_case(sp: JetSpec, closure: int = d.CLOSURE_PLAIN):
-    """The split-precision jet of a spec, with the given closure selected."""
-    from .cases import jet_crossflow
-    c = jet_crossflow(n_target=sp.n_target, D=sp.D, jet_speed=sp.jet_speed, air_speed=sp.air_speed, seed=sp.seed)
+    """The split-precision jet of a spec, with the given closure selected: the live-inlet jet in
+    the power-law crossflow (cases.jet_crossflow_live) or the static jet (cases.jet_crossflow)."""
+    from .cases import jet_crossflow, jet_crossflow_live
+    if sp.live:
+        c = jet_crossflow_live(n_target=sp.n_target, D=sp.D, jet_speed=sp.jet_speed, air_speed=sp.air_speed,
+                               seed=sp.seed, cap=sp.n_target)
+    else:
+        c = jet_crossflow(n_target=sp.n_target, D=sp.D, jet_speed=sp.jet_speed, air_speed=sp.air_speed,
+                          seed=sp.seed)
     c.settings.precision = d.PREC_MIXED
     c.settings.aero_closure = closure
     return c
@@ -155,8 +162,11 @@ def collect_samples(specs: list[JetSpec], n_samples: int, steps: int = 6, capaci
     Xs, Ts, held = [], [], 0
     for sp in specs:
         c = jet_case(sp)
-        ctx = Context(c.settings, c.state.n + 64, c.blocks)
+        cap = c.settings.max_points + 1024 if c.inlets else c.state.n + 64  # room for insertions
+        ctx = Context(c.settings, cap, c.blocks, c.inlets)
         try:
+            if c.power_law_params:
+                ctx.air_power_law(*c.power_law_params)
             ctx.set_states(c.state, c.state)
             ctx.closure_log(capacity or 4 * c.state.n, every)
             for _ in range(steps):

@@ -174,6 +174,9 @@ struct fjsph_ctx {
     float *vlm_abf = nullptr, *vlm_gf = nullptr;
     VlmDev vlm{};
     double *air_v = nullptr; /* 3 per slot */
+    /* analytic boundary-layer air field (FJSPH_POWER_LAW): axis, wall, thickness, exponent */
+    double power_law[4] = {2.0, 0.0, 1.0, 1.0 / 7.0};
+    bool power_law_ready = false;
     /* shared-memory tiles of the split-precision sweeps (tiles.cuh) */
     TileDev T{};
     int32_t pair_mode = FJSPH_PAIRS_LISTS; /* FJSPH_PAIRS_*                               */
@@ -281,7 +284,8 @@ int validate_settings(const fjsph_settings *s) {
     /* -DNOFROZEN -DLINEAR does not compile upstream (src/Resid.cpp:381 uses fluid.rho0) */
     if ((s->variant & FJSPH_VAR_NOFROZEN) && (s->variant & FJSPH_VAR_LINEAR)) return FJSPH_E_UNSUPPORTED;
     if (s->precision != FJSPH_PREC_FP64 && s->precision != FJSPH_PREC_MIXED) return FJSPH_E_UNSUPPORTED;
-    if (s->asource != FJSPH_CONST_VEL && s->asource != FJSPH_MESH_INFL && !(s->asource == FJSPH_VLM_INFL && s->dim == 3))
+    if (s->asource != FJSPH_CONST_VEL && s->asource != FJSPH_MESH_INFL && s->asource != FJSPH_POWER_LAW &&
+        !(s->asource == FJSPH_VLM_INFL && s->dim == 3))
         return FJSPH_E_UNSUPPORTED;
     if (s->aero_closure != FJSPH_CLOSURE_PLAIN && s->aero_closure != FJSPH_CLOSURE_LEARNED) return FJSPH_E_ARG;
     /* the learned closure lives in the split-precision residual */
@@ -347,7 +351,8 @@ Params make_params(const fjsph_ctx *c) {
     }
     P.grp = c->ngrp > 0 ? c->grp : nullptr;
     P.g_vinf = c->g_vinf;
-    P.air_v = ((s.asource == FJSPH_VLM_INFL && c->vlm.np > 0) || (s.asource == FJSPH_MESH_INFL && c->mesh_ready))
+    P.air_v = ((s.asource == FJSPH_VLM_INFL && c->vlm.np > 0) || (s.asource == FJSPH_MESH_INFL && c->mesh_ready) ||
+               (s.asource == FJSPH_POWER_LAW && c->power_law_ready))
                   ? c->air_v
                   : nullptr;
     P.sweep_threads = c->tune[0];
@@ -977,8 +982,16 @@ int npd_only(fjsph_ctx *c, const Params &P) {
     return finish_npd(c);
 }
 
-/* the vortex-lattice air velocity of the particles that use it (before the aero velocity pass) */
+/* the position-dependent air velocity of the particles that use it (before the aero velocity
+ * pass): the vortex lattice or the analytic boundary layer */
 int vlm_air(fjsph_ctx *c, const Params &P, const DevNbr &N) {
+    if (c->s.asource == FJSPH_POWER_LAW) {
+        if (!c->power_law_ready) return FJSPH_E_STATE; /* fjsph_air_power_law has not run */
+        Section sec(c, PASS_AIR);
+        launch_power_law_air(P, WS(c), c->power_law, c->air_v, mixed(c), c->stream);
+        c->launches++;
+        return FJSPH_OK;
+    }
     if (c->s.asource != FJSPH_VLM_INFL) return FJSPH_OK;
     if (c->vlm.np == 0) return FJSPH_E_STATE; /* fjsph_vlm_setup has not run */
     Section sec(c, PASS_AIR);
@@ -2372,6 +2385,18 @@ int fjsph_step_report(fjsph_ctx *c, double *out5) {
     return FJSPH_OK;
 }
 
+int fjsph_air_power_law(fjsph_ctx *c, const double *params4) {
+    TRY(check_ctx(c));
+    if (!params4 || c->s.asource != FJSPH_POWER_LAW) return FJSPH_E_ARG;
+    const double axis = params4[0];
+    if (!(axis == 0.0 || axis == 1.0 || axis == 2.0) || axis >= c->D) return FJSPH_E_ARG;
+    if (!(params4[2] > 0.0) || !(params4[3] > 0.0) || !std::isfinite(params4[1])) return FJSPH_E_ARG;
+    for (int k = 0; k < 4; ++k) c->power_law[k] = params4[k];
+    if (!c->air_v) TRY(dalloc(c, &c->air_v, 3 * c->cap));
+    c->power_law_ready = true;
+    return FJSPH_OK;
+}
+
 int fjsph_set_pair_mode(fjsph_ctx *c, int32_t mode) {
     TRY(check_ctx(c));
     if (mode != FJSPH_PAIRS_TILES && mode != FJSPH_PAIRS_LISTS) return FJSPH_E_ARG;
@@ -2388,6 +2413,25 @@ int fjsph_get_pair_mode(fjsph_ctx *c, int32_t *mode, int32_t *tiles_in_use) {
     TRY(check_ctx(c));
     if (mode) *mode = c->pair_mode;
     if (tiles_in_use) *tiles_in_use = c->tiles_valid ? 1 : 0;
+    return FJSPH_OK;
+}
+
+int fjsph_neighbour_counts(fjsph_ctx *c, int32_t *counts) {
+    TRY(need_nbr(c));
+    if (!counts) return FJSPH_E_ARG;
+    TRY(sync(c));
+    const int64_t n = c->n;
+    std::vector<int32_t> cnt(n);
+    if (mixed(c)) {
+        CU(cudaMemcpy(cnt.data(), c->nbr_counts, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<int64_t> off(n + 1);
+        CU(cudaMemcpy(off.data(), c->nbr_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; ++i) cnt[i] = (int32_t)(off[i + 1] - off[i]);
+    }
+    std::vector<int64_t> keys;
+    TRY(download_keys(c, keys));
+    for (int64_t s = 0; s < n; ++s) counts[keys[s]] = cnt[s];
     return FJSPH_OK;
 }
 

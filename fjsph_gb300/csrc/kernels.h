@@ -60,6 +60,10 @@ int vlm_build(const fjsph_vlm &v, const double *vinf, std::vector<double> &abc, 
 /* air[3 i + k] = the VLM velocity of the fluid particles that use it (FP32 sums when fp32) */
 void launch_vlm_air(const Params &P, const DevState &W, const DevNbr &N, const VlmDev &V, double *air, bool fp32,
                     cudaStream_t s);
+/* air[3 i + k] = v_inf[k] f(x_i) for the fluid slots, f the boundary-layer profile of
+ * pl = {axis, wall, thickness, exponent} (FP32 power in the split-precision form) */
+void launch_power_law_air(const Params &P, const DevState &W, const double *pl, double *air, bool fp32,
+                          cudaStream_t s);
 /* vel[3 i + k] at pos[3 i + k], i < n */
 void launch_vlm_points(const VlmDev &V, int64_t n, const double *pos, double *vel, bool fp32, cudaStream_t s);
 

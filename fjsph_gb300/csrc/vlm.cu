@@ -359,7 +359,31 @@ __global__ void __launch_bounds__(kVT) k_vlm_points(VlmDev V, int64_t n, const d
         for (int k = 0; k < 3; ++k) vel[3 * i + k] = out[k];
 }
 
+/* Boundary-layer air field: v_inf (s)^n with s = (x[axis] - wall) / thickness clamped to [0, 1];
+ * the same value the oracle computes with pow in FP64 (FP32 powf in the split-precision form). */
+template <typename R>
+__global__ void k_power_law_air(Params P, DevState W, int axis, double wall, double inv_thick, double expo,
+                                double *air) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double t = (W.x[axis][i] - wall) * inv_thick;
+    t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+    const double f = (t == 1.0) ? 1.0 : (double)pow((R)t, (R)expo);
+    for (int k = 0; k < 3; ++k) air[3 * i + k] = P.v_inf[k] * f;
+}
+
 } // namespace
+
+void launch_power_law_air(const Params &P, const DevState &W, const double *pl, double *air, bool fp32,
+                          cudaStream_t s) {
+    const unsigned g = grid_for(P.n - P.nb, 256);
+    if (g == 0) return;
+    const int axis = (int)pl[0];
+    if (fp32)
+        k_power_law_air<float><<<g, 256, 0, s>>>(P, W, axis, pl[1], 1.0 / pl[2], pl[3], air);
+    else
+        k_power_law_air<double><<<g, 256, 0, s>>>(P, W, axis, pl[1], 1.0 / pl[2], pl[3], air);
+}
 
 void launch_vlm_air(const Params &P, const DevState &W, const DevNbr &N, const VlmDev &V, double *air, bool fp32,
                     cudaStream_t s) {

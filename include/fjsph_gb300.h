@@ -69,7 +69,10 @@ enum fjsph_eos { FJSPH_COLE_EOS = 0, FJSPH_ISO_EOS = 1 };
 enum fjsph_aero_case { FJSPH_NOAERO = 0, FJSPH_GISSLER = 1, FJSPH_INDUCED_PRESSURE = 2, FJSPH_SKIN_FRIC = 3 };
 /* Air velocity source (src/VarDefs.h:168-173): uniform v_inf, the cells of the mesh given to
  * fjsph_mesh_set, the vortex-lattice field of fjsph_vlm_setup (3D). */
-enum fjsph_aero_source { FJSPH_CONST_VEL = 0, FJSPH_MESH_INFL = 1, FJSPH_VLM_INFL = 2 };
+enum fjsph_aero_source { FJSPH_CONST_VEL = 0, FJSPH_MESH_INFL = 1, FJSPH_VLM_INFL = 2,
+                         /* analytic boundary-layer air field (no reference counterpart):
+                          * fjsph_air_power_law */
+                         FJSPH_POWER_LAW = 100 };
 
 /* Arithmetic form of the pair kernels. */
 enum fjsph_precision {
@@ -417,6 +420,15 @@ typedef struct fjsph_mesh {
     const double *cell_vel;          /* [dim * n_cells]                                      */
     const double *cell_p, *cell_rho; /* [n_cells]                                            */
 } fjsph_mesh;
+/* No reference counterpart: the analytic air field of a context created with asource =
+ * FJSPH_POWER_LAW, a boundary layer over a wall normal to axis `axis` (0, 1, 2) at coordinate
+ * `wall`: the air velocity at position x is v_inf * min(max((x[axis] - wall) / thickness, 0), 1)^exponent
+ * (exponent 1/7: the turbulent 1/7-power law).  It takes the place of the uniform v_inf wherever
+ * the reference's constVel source uses it: the aero velocity of get_aero_velocity
+ * (src/Resid.cpp:569-611) and the relative air velocity of the Gissler occlusion in
+ * Detect_Surface (src/Geometry.cpp:151-164).  params4 = {axis, wall, thickness, exponent};
+ * thickness > 0, exponent > 0. */
+int fjsph_air_power_law(fjsph_ctx *ctx, const double *params4);
 /* Hands the mesh to a context created with asource = FJSPH_MESH_INFL.  FindCell then runs in
  * place of the uniform-source aero velocity pass: free particles below the lambda cutoff take
  * the velocity, pressure and density of the cell they are in (cellID = the cell); a particle
@@ -488,6 +500,9 @@ int fjsph_step_report(fjsph_ctx *ctx, double *out5);
 #define FJSPH_PAIRS_LISTS 1
 int fjsph_set_pair_mode(fjsph_ctx *ctx, int32_t mode);
 int fjsph_get_pair_mode(fjsph_ctx *ctx, int32_t *mode, int32_t *tiles_in_use);
+/* Neighbour count (self included) of every particle, in reference order, from the last search
+ * (counts: particle-count entries).  No reference counterpart: a diagnostic of the search. */
+int fjsph_neighbour_counts(fjsph_ctx *ctx, int32_t *counts);
 /* The seven maxima of the last fjsph_find_timestep (Integrator members, src/Integration.h):
  * maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift (the running maximum). */
 int fjsph_timestep_maxima(fjsph_ctx *ctx, double *out7);

@@ -88,6 +88,10 @@ struct orc_sim {
     std::vector<double> vlm_A, vlm_B, vlm_C, vlm_gamma;
     double vlm_vinf[3] = {0, 0, 0}, vlm_maxvel = 0.0;
     bool vlm_ready = false;
+    /* analytic boundary-layer air field (a synthetic input; no reference counterpart): axis, wall,
+     * thickness, exponent */
+    double pl[4] = {2.0, 0.0, 1.0, 1.0 / 7.0};
+    bool pl_ready = false;
     /* mesh-cell air source (MESH, Var.h:396-451) */
     std::vector<double> m_verts, m_centre, m_vel, m_p, m_rho, m_rad2;
     std::vector<int64_t> m_face_off, m_face_verts, m_cell_off, m_cell_faces;
@@ -825,6 +829,16 @@ void find_cell(orc_sim *o, std::vector<Part> &P) {
     }
 }
 
+/* The boundary-layer air field in place of v_inf: v_inf s^n, s = (x[axis] - wall) / thickness
+ * clamped to [0, 1] (n = 1/7: the turbulent power law). */
+void power_law_velocity(const orc_sim *o, const double *x, double *vel) {
+    const int axis = int(o->pl[0]);
+    double t = (x[axis] - o->pl[1]) / o->pl[2];
+    t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+    const double f = t == 1.0 ? 1.0 : std::pow(t, o->pl[3]);
+    for (int k = 0; k < 3; ++k) vel[k] = o->s.v_inf[k] * f;
+}
+
 void get_aero_velocity(orc_sim *o, std::vector<Part> &P) {
     const int D = o->D;
     const fjsph_settings &a = o->s;
@@ -843,6 +857,8 @@ void get_aero_velocity(orc_sim *o, std::vector<Part> &P) {
         if (on) {
             if (a.asource == FJSPH_VLM_INFL)
                 vlm_velocity(o, pi.xi, pi.cellV);
+            else if (a.asource == FJSPH_POWER_LAW)
+                power_law_velocity(o, pi.xi, pi.cellV);
             else
                 for (int k = 0; k < D; ++k) pi.cellV[k] = a.v_inf[k];
             pi.cellID = 1;
@@ -942,6 +958,10 @@ void detect_surface(orc_sim *o, std::vector<Part> &P) {
             } else if (s.asource == FJSPH_VLM_INFL) { /* Geometry.cpp:158-163 */
                 double vel[3];
                 vlm_velocity(o, pi.xi, vel);
+                for (int k = 0; k < D; ++k) Vdiff[k] = vel[k] - pi.v[k];
+            } else if (s.asource == FJSPH_POWER_LAW) {
+                double vel[3];
+                power_law_velocity(o, pi.xi, vel);
                 for (int k = 0; k < D; ++k) Vdiff[k] = vel[k] - pi.v[k];
             } else {
                 for (int k = 0; k < D; ++k) Vdiff[k] = s.v_inf[k] - pi.v[k];
@@ -2296,6 +2316,13 @@ int orc_mesh_set(orc_sim *o, const fjsph_mesh *m) {
 }
 
 /* VLM::Init + MakeMatrix + GetGamma (VLM.cpp:14-117, 180-307) */
+int orc_air_power_law(orc_sim *o, const double *params4) {
+    if (!o || !params4 || o->s.asource != FJSPH_POWER_LAW) return FJSPH_E_ARG;
+    for (int k = 0; k < 4; ++k) o->pl[k] = params4[k];
+    o->pl_ready = true;
+    return FJSPH_OK;
+}
+
 int orc_vlm_setup(orc_sim *o, const fjsph_vlm *v) {
     if (!v || o->D != 3) return -1;
     if (v->span <= 0 || v->chord <= 0 || v->panels_span <= 0 || v->panels_chord <= 0) return -1;

@@ -66,6 +66,7 @@ double orc_get_cd(double Re);
 /* vortex-lattice air source (VLM.cpp): setup returns the panel count (< 0 on a bad wing or a
  * singular influence matrix) */
 int orc_vlm_setup(orc_sim *o, const fjsph_vlm *v);
+int orc_air_power_law(orc_sim *o, const double *params4);
 int orc_mesh_set(orc_sim *o, const fjsph_mesh *m);
 int orc_vlm_panels(orc_sim *o, double *gamma, double *abc);
 void orc_vlm_velocity(orc_sim *o, int64_t n, const double *pos, double *vel);

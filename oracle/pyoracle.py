@@ -64,6 +64,7 @@ _PROTO = {
     "orc_qr_inverse": (C.c_int32, [_dp, C.c_int32, _dp]),
     "orc_get_cd": (C.c_double, [C.c_double]),
     "orc_vlm_setup": (C.c_int, [_P, C.c_void_p]),
+    "orc_air_power_law": (C.c_int, [_P, _dp]),
     "orc_mesh_set": (C.c_int, [_P, C.c_void_p]),
     "orc_vlm_panels": (C.c_int, [_P, _dp, _dp]),
     "orc_vlm_velocity": (None, [_P, C.c_int64, _dp, _dp]),
@@ -147,6 +148,9 @@ class Oracle:
         self.upload(d.PNP1, pnp1)
         self.upload(d.PN, pn)
 
+    def particle_count(self) -> int:
+        return int(self._l.orc_particle_count(self._h))
+
     def update_neighbours(self) -> int:
         self._n_pairs = int(self._l.orc_update_neighbours(self._h))
         return self._n_pairs
@@ -162,6 +166,12 @@ class Oracle:
 
     def dSPH_PreStep(self) -> float:
         return self._l.orc_dsph_prestep(self._h)
+
+    def air_power_law(self, axis: int, wall: float, thickness: float, exponent: float = 1.0 / 7.0) -> None:
+        """The analytic boundary-layer air field (settings asource = FJSPH_POWER_LAW)."""
+        p = (C.c_double * 4)(float(axis), wall, thickness, exponent)
+        if self._l.orc_air_power_law(self._h, p) != 0:
+            raise ValueError("air_power_law: the settings do not name the power-law source")
 
     def mesh_set(self, mesh) -> None:
         """The mesh-cell air source's mesh (mesh: fjsph_gb300.mesh.CellMesh)."""
