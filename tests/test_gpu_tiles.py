@@ -81,6 +81,9 @@ def test_tile_step_matches_list_step():
         ctx.integrate()
         out.append(ctx.download())
     a, b = out
-    for f, tol in (("xi", 1e-12), ("v", 1e-6), ("rho", 1e-8), ("acc", 1e-4), ("Rrho", 1e-4)):
+    nb = n_bound(c.blocks)
+    e = rel_rms(b.xi[nb:] - st.xi[nb:], a.xi[nb:] - st.xi[nb:])
+    assert e <= 1e-5, f"displacement: {e:.2e}"
+    for f, tol in (("v", 1e-6), ("rho", 1e-8), ("acc", 1e-4), ("Rrho", 1e-4)):
         e = rel_rms(getattr(b, f), getattr(a, f))
         assert e <= tol, f"{f}: {e:.2e}"
