@@ -84,6 +84,8 @@ def parse():
     ap.add_argument("--config1-dx", type=float, default=0.003, help="spacing of the 3D dam break (0 = skip)")
     ap.add_argument("--config1-steps", type=int, default=3, help="timed FP32 steps of the 3D dam break")
     ap.add_argument("--config1-long", type=int, default=0, help="a long FP32 run of the 3D dam break (steps)")
+    ap.add_argument("--pairs", default="lists", choices=["lists", "tiles"],
+                    help="pair sweeps of the FP32 form: pair lists or shared-memory tiles (residual)")
     ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
@@ -484,7 +486,7 @@ def pinned_buffer(n: int, dim: int):
     return pinned_state(SPHState(n, dim))
 
 
-def roofline(s, prof, nf_mean: float, peaks: dict, learned: bool) -> dict:
+def roofline(s, prof, nf_mean: float, peaks: dict, learned: bool, tiles: bool = False) -> dict:
     """The residual (the dominant kernel): algorithmic bytes per fluid particle x the fluid
     particles of a launch, over the launch's mean device time from the profile events."""
     from fjsph_gb300 import _cdefs as d
@@ -498,7 +500,8 @@ def roofline(s, prof, nf_mean: float, peaks: dict, learned: bool) -> dict:
     return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "traffic_source": "ncu capture on the 634k-particle jet, scaled by fluid particles" if tkey else None,
-            "kernel": ("k_m_resid" if s.precision == d.PREC_MIXED else "k_resid") + " (get_acc_and_Rrho)",
+            "kernel": (("k_t_resid" if tiles else "k_m_resid") if s.precision == d.PREC_MIXED else "k_resid")
+            + " (get_acc_and_Rrho)",
             "launch_ms": round(per_launch * 1e3, 3), "bytes_per_launch": round(bpp * nf_mean),
             "bytes_per_particle": bpp, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
 
@@ -514,6 +517,8 @@ def run_ours(args, ws, rank, local):
     s = c.settings
     nb = c.state.n - c.n_fluid
     ctx = new_ctx(s, c)
+    if args.pairs == "tiles":
+        ctx.set_pair_mode(d.PAIRS_TILES)
     if learned:
         ctx.closure_set_weights(weights, 0.05)
     for _ in range(args.warmup):
@@ -538,7 +543,7 @@ def run_ours(args, ws, rank, local):
     value = ps * ws / (ms / 1e3)
     nf_mean = ps / args.steps
     rep = ctx.step_report()
-    roof = roofline(s, prof, nf_mean, measured_peaks(), learned)
+    roof = roofline(s, prof, nf_mean, measured_peaks(), learned, args.pairs == "tiles")
     live = {"particles_at_start": int(c.state.n), "particles_at_end": int(ctx.particle_count()),
             "inserted_in_timed_steps": int(ins1 - ins0), "deleted_in_timed_steps": int(del1 - del0),
             "inserted_total": int(ins1), "deleted_total": int(del1), "cap": int(s.max_points),
@@ -963,7 +968,7 @@ def main():
                 "config": {"workload": WORKLOAD, "particles": r["n"], "fluid": r["nf"], "cap": args.n,
                            "air": "50 m/s crossflow, 1/7-power-law boundary layer 5 mm over z = 0",
                            "form": args.precision, "closure": args.closure if args.precision == "mixed" else "plain",
-                           "integrator": "runge_kutta4",
+                           "integrator": "runge_kutta4", "pairs": args.pairs,
                            "l2": "inputs larger than L2 (state ~1 GB)", "parallelism": f"replicas{ws}"},
                 "roofline": r["roof"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
                 "parity": parity, "live_inlet": r["live"],
