@@ -442,14 +442,16 @@ def make_case(n_cap: int, precision: str, closure: str = "plain"):
 
 
 def new_ctx(settings, c, state=None):
-    """A context for case c under `settings` (capacity: the insertion cap), with the case's inlet
-    tables and analytic air field, holding `state` (default: the case's start)."""
+    """A context for case c under `settings` (capacity: the insertion cap for a case with inlets,
+    else the particles), with the case's inlet tables and analytic air field, holding `state`
+    (default: the case's start)."""
     from fjsph_gb300 import _cdefs as d
     from fjsph_gb300.api import Context
-    ctx = Context(settings, settings.max_points + 1024, c.blocks, c.inlets)
+    st = state if state is not None else c.state
+    cap = max(settings.max_points, st.n) + 1024 if c.inlets else st.n + 1024  # insertions need room
+    ctx = Context(settings, cap, c.blocks, c.inlets)
     if settings.asource == d.POWER_LAW and c.power_law_params:
         ctx.air_power_law(*c.power_law_params)
-    st = state if state is not None else c.state
     ctx.set_states(st, st)
     return ctx
 
@@ -934,6 +936,17 @@ def run_reference(args, threads: int, ws: int) -> dict:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def side(fn, *a):
+    """A side section of the line: its result, or {"error": ...} when it fails (the headline and
+    the other sections are still reported)."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001 -- reported in the line, not swallowed
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -950,16 +963,17 @@ def main():
         torch.cuda.set_device(0)
         dist.init_process_group("nccl")
     r = run_ours(args, ws, rank, local)
-    drops = run_droplets(args, ws, rank, r["weights"]) if args.drops > 0 else None
-    vlm = run_vlm(args) if (args.vlm_points > 0 and rank == 0) else None
-    setup = run_case_setup(args) if (args.setup_particles > 0 and rank == 0) else None
-    mesh = run_mesh(args, r["case"]) if (args.mesh_cell > 0 and rank == 0) else None
-    cfg0 = run_config0(args, threads, rank) if (args.config0_steps > 0 and rank == 0) else None
-    cfg1 = run_config1(args) if (args.config1_dx > 0 and rank == 0) else None
+    drops = side(run_droplets, args, ws, rank, r["weights"]) if args.drops > 0 else None
+    vlm = side(run_vlm, args) if (args.vlm_points > 0 and rank == 0) else None
+    setup = side(run_case_setup, args) if (args.setup_particles > 0 and rank == 0) else None
+    mesh = side(run_mesh, args, r["case"]) if (args.mesh_cell > 0 and rank == 0) else None
+    cfg0 = side(run_config0, args, threads, rank) if (args.config0_steps > 0 and rank == 0) else None
+    cfg1 = side(run_config1, args) if (args.config1_dx > 0 and rank == 0) else None
     if rank == 0:
         cpu = parity = None
         if not args.no_cpu:
-            cpu, parity = run_cpu_parity(args, r["case"], threads)
+            got = side(run_cpu_parity, args, r["case"], threads)
+            cpu, parity = (got, got) if isinstance(got, dict) else got
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
