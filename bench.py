@@ -47,6 +47,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "particle-steps/s, 2M-particle jet: FP32+learned aero vs plain FP64, same GB300"
 UNIT = "particle-steps/s"
 WORKLOAD = "jet_in_crossflow_3d_live_inlet"
+JET_SPEED = 10.0  # m/s, the inlet velocity of config 2
 
 
 def parse():
@@ -433,7 +434,7 @@ def train_closure(args, log):
 
 def make_case(n_cap: int, precision: str, closure: str = "plain"):
     from fjsph_gb300 import cases, _cdefs as d
-    c = cases.jet_crossflow_live(n_target=n_cap, cap=n_cap)
+    c = cases.jet_crossflow_live(n_target=n_cap, cap=n_cap, jet_speed=JET_SPEED)
     if precision == "mixed":
         c.settings.precision = d.PREC_MIXED
         if closure == "learned":
@@ -534,9 +535,11 @@ def run_ours(args, ws, rank, local):
     ctx.profile(True)
     ctx.launch_stats(reset=True)
     ins0, del0 = ctx.update_counts()
+    t_sim0 = ctx.settings.current_time
     ms, ps = counted_steps(ctx, args.steps, nb)
     launches = ctx.launch_stats()
     ins1, del1 = ctx.update_counts()
+    t_sim1 = ctx.settings.current_time
     n_pairs = ctx.update_neighbours()  # pairs of the last search (outside the timed region)
     prof = ctx.profile_read()
     ctx.profile(False)
@@ -549,7 +552,12 @@ def run_ours(args, ws, rank, local):
     live = {"particles_at_start": int(c.state.n), "particles_at_end": int(ctx.particle_count()),
             "inserted_in_timed_steps": int(ins1 - ins0), "deleted_in_timed_steps": int(del1 - del0),
             "inserted_total": int(ins1), "deleted_total": int(del1), "cap": int(s.max_points),
-            "mean_fluid_per_step": round(nf_mean, 1)}
+            "mean_fluid_per_step": round(nf_mean, 1),
+            "simulated_us_in_timed_steps": round((t_sim1 - t_sim0) * 1e6, 3),
+            "insertion_interval_us": round(s.particle_step / JET_SPEED * 1e6, 3),
+            "note": "a column inserts a layer each time its BACK particle has travelled one dx at the jet "
+                    "speed (src/shapes/inlet.cpp:578-640); the time step is set by the inlet's deepest "
+                    "buffer layer, as upstream, whose find_timestep includes the buffer"}
 
     # the learned closure judged against the plain one on the state the timed steps reached
     if learned:
