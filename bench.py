@@ -386,7 +386,10 @@ def resid_bytes_per_particle(s) -> int:
 # DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
 # 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
 # the benchmark's particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 709.41e6 / 620_210}
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed": (472.477e6 + 111.826e6) / 547_607}
+TRAFFIC_SOURCE = {"fp64": "ncu capture of k_resid on the 634k-particle static jet, scaled by fluid particles",
+                  "mixed": "ncu capture of k_m_resid (plain closure) on the 570k-particle live jet, scaled by "
+                           "fluid particles"}
 
 
 def dist_env():
@@ -399,7 +402,10 @@ def dist_env():
 # DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
 # 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
 # the benchmark's particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed_learned": 709.41e6 / 620_210}
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed": (472.477e6 + 111.826e6) / 547_607}
+TRAFFIC_SOURCE = {"fp64": "ncu capture of k_resid on the 634k-particle static jet, scaled by fluid particles",
+                  "mixed": "ncu capture of k_m_resid (plain closure) on the 570k-particle live jet, scaled by "
+                           "fluid particles"}
 
 # Examples/VLM: a 22.3 m half-span, 8.5 m chord wing, sweep 32.5 deg, taper 0.6, 20 deg flap
 VLM_WING = dict(span=22.275, chord=8.491, panels_span=50, panels_chord=14, aoa_deg=5.0, sweep_deg=32.5, taper=0.6,
@@ -497,12 +503,12 @@ def roofline(s, prof, nf_mean: float, peaks: dict, learned: bool, tiles: bool = 
     bpp = resid_bytes_per_particle(s)
     per_launch = r_ms / max(r_cnt, 1) / 1e3
     achieved = bpp * nf_mean / per_launch / 1e9
-    tkey = "fp64" if s.precision == d.PREC_FP64 else ("mixed_learned" if learned else None)
+    tkey = "fp64" if s.precision == d.PREC_FP64 else ("mixed" if not tiles else None)
     traffic = round(RESID_TRAFFIC_PER_PARTICLE[tkey] * nf_mean) if tkey else None
     peak = peaks.get("hbm_gbs", 6800.0)
     return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "traffic_source": "ncu capture on the 634k-particle jet, scaled by fluid particles" if tkey else None,
+            "traffic_source": TRAFFIC_SOURCE.get(tkey),
             "kernel": (("k_t_resid" if tiles else "k_m_resid") if s.precision == d.PREC_MIXED else "k_resid")
             + " (get_acc_and_Rrho)",
             "launch_ms": round(per_launch * 1e3, 3), "bytes_per_launch": round(bpp * nf_mean),
