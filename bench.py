@@ -790,6 +790,7 @@ def run_config1(args):
         ctx = new_ctx(s, c)
         ctx.integrate()
         first[name] = ctx.download(d.PNP1, fields=fields)
+        tune = ctx.autotune(3)["chosen"] if prec == d.PREC_MIXED and not args.no_tune else None
         pairs = ctx.update_neighbours()
         ctx.profile(True)
         ms, ps = counted_steps(ctx, steps, nb)
@@ -798,6 +799,8 @@ def run_config1(args):
         out[name] = {"value": ps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
                      "neighbour_pairs": int(pairs), "neighbour_pairs_per_s": pairs * steps / (ms / 1e3),
                      "passes_ms_per_step": {k: round(v[0] / steps, 3) for k, v in prof.items() if v[1]}}
+        if tune:
+            out[name]["autotune"] = tune
         if name == "fp32" and args.config1_long > 0:
             ms_l, ps_l = counted_steps(ctx, args.config1_long, nb)
             out["fp32_long"] = {"steps": args.config1_long, "value": ps_l / (ms_l / 1e3), "unit": UNIT,

@@ -21,6 +21,7 @@ CONST_VEL, MESH_INFL, VLM_INFL = 0, 1, 2  # fjsph_aero_source
 POWER_LAW = 100  # analytic boundary-layer air field (fjsph_air_power_law)
 PREC_FP64, PREC_MIXED = 0, 1
 PAIRS_TILES, PAIRS_LISTS = 0, 1
+ORDER_GRID, ORDER_SM = 0, 1
 CLOSURE_PLAIN, CLOSURE_LEARNED = 0, 1
 CLOSURE_ARM_JUDGE, CLOSURE_ARM_LOG = 1, 2
 MLP_INPUTS, MLP_OUTPUTS = 12, 2

@@ -61,6 +61,9 @@ PROTOTYPES = {
     "fjsph_air_power_law": (C.c_int, [_P, _dp]),
     "fjsph_neighbour_counts": (C.c_int, [_P, _i32p]),
     "fjsph_get_pair_mode": (C.c_int, [_P, _i32p, _i32p]),
+    "fjsph_set_sweep_order": (C.c_int, [_P, _i32]),
+    "fjsph_get_sweep_order": (C.c_int, [_P, _i32p]),
+    "fjsph_autotune_order": (C.c_int, [_P, _i32, _i32p, _dp]),
     "fjsph_launch_stats": (C.c_int, [_P, _i64p, _i32]),
     "fjsph_ctx_stream": (C.c_int, [_P, _pp]),
     "fjsph_status_string": (C.c_char_p, [C.c_int]),

@@ -260,13 +260,19 @@ class Context:
 
     # ---- launch-configuration autotuner --------------------------------------------------------
     def autotune(self, repeats: int = 3) -> dict:
-        """Pick the fastest pair-sweep / residual launch configuration on the current state."""
+        """Pick the fastest pair-sweep / residual launch configuration on the current state, then
+        the faster work order of the residual with it."""
         cfg = (C.c_int32 * 3)()
         ms = (C.c_double * 8)()
         check("fjsph_autotune", self._lib.fjsph_autotune(self._h, int(repeats), cfg, ms))
         tried = [("sweep", b, None) for b in (64, 128)] + [("resid", b, a) for b in (64, 128) for a in (2, 4, 8)]
-        return {"chosen": {"sweep_threads": cfg[0], "resid_threads": cfg[1], "list_ahead": cfg[2]},
-                "trials_ms": [dict(kind=k, threads=b, list_ahead=a, ms=ms[i]) for i, (k, b, a) in enumerate(tried)]}
+        trials = [dict(kind=k, threads=b, list_ahead=a, ms=ms[i]) for i, (k, b, a) in enumerate(tried)]
+        order, oms = C.c_int32(), (C.c_double * 2)()
+        check("fjsph_autotune_order", self._lib.fjsph_autotune_order(self._h, int(repeats), C.byref(order), oms))
+        trials += [dict(kind="resid order", order=name, ms=oms[i]) for i, name in enumerate(("grid", "sm"))]
+        return {"chosen": {"sweep_threads": cfg[0], "resid_threads": cfg[1], "list_ahead": cfg[2],
+                           "order": "sm" if order.value == d.ORDER_SM else "grid"},
+                "trials_ms": trials}
 
     def tuning(self, cfg=None):
         """Get (cfg None) or set the launch configuration (sweep threads, residual threads, rows ahead)."""
@@ -304,6 +310,15 @@ class Context:
         m, t = C.c_int32(), C.c_int32()
         check("fjsph_get_pair_mode", self._lib.fjsph_get_pair_mode(self._h, C.byref(m), C.byref(t)))
         return m.value, bool(t.value)
+
+    def set_sweep_order(self, order: int) -> None:
+        """d.ORDER_GRID (grid order, default) or d.ORDER_SM (SM-local chunks) for the residual."""
+        check("fjsph_set_sweep_order", self._lib.fjsph_set_sweep_order(self._h, int(order)))
+
+    def sweep_order(self) -> int:
+        o = C.c_int32()
+        check("fjsph_get_sweep_order", self._lib.fjsph_get_sweep_order(self._h, C.byref(o)))
+        return o.value
 
     def timestep_maxima(self) -> list[float]:
         """maxf, maxAf, maxdrho, maxRhoi, minST, maxU, maxShift of the last find_timestep."""

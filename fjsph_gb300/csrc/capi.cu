@@ -180,6 +180,8 @@ struct fjsph_ctx {
     /* shared-memory tiles of the split-precision sweeps (tiles.cuh) */
     TileDev T{};
     int32_t pair_mode = FJSPH_PAIRS_LISTS; /* FJSPH_PAIRS_*                               */
+    int32_t sweep_order = FJSPH_ORDER_GRID; /* FJSPH_ORDER_*                              */
+    int32_t *region_next = nullptr;         /* kMaxRegions chunk counters of the SM order */
     bool tiles_valid = false;              /* the last search built the tile masks        */
     int64_t tiles_table = 0;               /* bucket table size the tile arrays fit       */
     /* mesh-cell air source */
@@ -358,6 +360,8 @@ Params make_params(const fjsph_ctx *c) {
     P.sweep_threads = c->tune[0];
     P.resid_threads = c->tune[1];
     P.list_ahead = c->tune[2];
+    P.sm_order = (c->sweep_order == FJSPH_ORDER_SM && c->region_next) ? 1 : 0;
+    P.region_next = c->region_next;
     {
         FConst &f = P.fc;
         f.H = (float)s.H;
@@ -2416,6 +2420,24 @@ int fjsph_get_pair_mode(fjsph_ctx *c, int32_t *mode, int32_t *tiles_in_use) {
     return FJSPH_OK;
 }
 
+int fjsph_set_sweep_order(fjsph_ctx *c, int32_t order) {
+    TRY(check_ctx(c));
+    if (order != FJSPH_ORDER_GRID && order != FJSPH_ORDER_SM) return FJSPH_E_ARG;
+    if (order == FJSPH_ORDER_SM && !c->region_next) TRY(dalloc(c, &c->region_next, kMaxRegions));
+    if (order != c->sweep_order) {
+        TRY(graph_release(c)); /* captured launches carry the order */
+        c->sweep_order = order;
+    }
+    return FJSPH_OK;
+}
+
+int fjsph_get_sweep_order(fjsph_ctx *c, int32_t *order) {
+    TRY(check_ctx(c));
+    if (!order) return FJSPH_E_ARG;
+    *order = c->sweep_order;
+    return FJSPH_OK;
+}
+
 int fjsph_neighbour_counts(fjsph_ctx *c, int32_t *counts) {
     TRY(need_nbr(c));
     if (!counts) return FJSPH_E_ARG;
@@ -2765,6 +2787,31 @@ int fjsph_autotune(fjsph_ctx *c, int32_t repeats, int32_t *chosen3, double *time
     c->prof.on = prof;
     TRY(rc);
     if (chosen3) std::copy(c->tune, c->tune + 3, chosen3);
+    return sync(c);
+}
+
+int fjsph_autotune_order(fjsph_ctx *c, int32_t repeats, int32_t *chosen, double *times_ms) {
+    TRY(need_state(c));
+    if (!mixed(c)) return FJSPH_E_UNSUPPORTED;
+    if (repeats <= 0) return FJSPH_E_ARG;
+    if (!c->nbr_valid) TRY(search(c));
+    if (!c->region_next) TRY(dalloc(c, &c->region_next, kMaxRegions));
+    TRY(sync(c));
+    TRY(graph_release(c));
+    const bool prof = c->prof.on;
+    c->prof.on = false;
+    const int32_t orders[2] = {FJSPH_ORDER_GRID, FJSPH_ORDER_SM};
+    double ms[2] = {0.0, 0.0};
+    int rc = FJSPH_OK;
+    for (int k = 0; k < 2 && rc == FJSPH_OK; ++k) {
+        c->sweep_order = orders[k];
+        rc = time_ms(c, repeats, [&] { return resid(c, make_params(c)); }, &ms[k]);
+    }
+    c->sweep_order = (rc == FJSPH_OK && ms[1] < ms[0]) ? FJSPH_ORDER_SM : FJSPH_ORDER_GRID;
+    c->prof.on = prof;
+    TRY(rc);
+    if (chosen) *chosen = c->sweep_order;
+    if (times_ms) std::copy(ms, ms + 2, times_ms);
     return sync(c);
 }
 

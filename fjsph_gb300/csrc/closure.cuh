@@ -43,10 +43,15 @@ struct Closure {
     int64_t log_cap;
 };
 
-struct MlpWarpSmem {
-    __nv_bfloat16 X[32][mlp::kInP];
-    float Y[32][2];
-};
+/* Lane of the r-th set bit (r counted from 0, r < popc(bal)): the largest s with fewer than r + 1
+ * set bits below it, found by binary search on popc. */
+__device__ __forceinline__ int nth_set_lane(unsigned bal, int r) {
+    int s = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+        if (__popc(bal & ((1u << (s + step)) - 1u)) <= r) s += step;
+    return s;
+}
 
 template <int D>
 __device__ __forceinline__ void closure_inputs(const Params &P, float4 occ, double nneigh, const double *U,
@@ -74,41 +79,70 @@ __device__ __forceinline__ void closure_inputs(const Params &P, float4 occ, doub
     x[11] = lam;
 }
 
-/* Network outputs for the lanes with `want` set; every lane of the warp must call. */
-__device__ __forceinline__ void mlp_warp(const mlp::DevMlp &M, bool want, const float (&x)[mlp::kIn],
-                                         MlpWarpSmem &S, float &y0, float &y1) {
+/* Network outputs for the lanes with `want` set; every lane of the warp must call.  The covered
+ * lanes form the rows of 16-row tiles in lane order (row r is the lane of the r-th set bit of the
+ * ballot; rows past the count are zero).  A lane builds its tile's input A fragment from the
+ * source rows' packed inputs and takes its outputs from the C fragment by shuffles, so the network
+ * holds no shared memory and the kernel's L1 keeps its whole capacity for the neighbour gathers. */
+__device__ __forceinline__ void mlp_warp(const mlp::DevMlp &M, bool want, const float (&x)[mlp::kIn], float &y0,
+                                         float &y1) {
     const unsigned bal = __ballot_sync(0xffffffffu, want);
     if (bal == 0u) return;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int cnt = __popc(bal);
     const int rank = __popc(bal & ((1u << lane) - 1u));
-    uint4 *Xz = reinterpret_cast<uint4 *>(&S.X[0][0]); /* 32 rows x 32 B */
-    Xz[lane] = make_uint4(0u, 0u, 0u, 0u);
-    Xz[lane + 32] = make_uint4(0u, 0u, 0u, 0u);
-    __syncwarp();
-    if (want) {
+    /* this lane's normalised inputs as BF16 pairs: word q holds columns 2q (low half) and 2q + 1;
+     * words 6 and 7 (columns 12-15) are the zero padding */
+    uint32_t p[mlp::kIn / 2];
 #pragma unroll
-        for (int c = 0; c < mlp::kIn; ++c)
-            S.X[rank][c] =
-                __float2bfloat16_rn((x[c] - __ldg(M.params + mlp::oInShift + c)) * __ldg(M.params + mlp::oInScale + c));
-    }
-    __syncwarp();
-    for (int tile = 0; tile * 16 < cnt; ++tile) {
-        float Y[4];
-        mlp::forward_tile(M, &S.X[tile * 16][0], Y);
-        if (t == 0) {
-            S.Y[tile * 16 + g][0] = Y[0];
-            S.Y[tile * 16 + g][1] = Y[1];
-            S.Y[tile * 16 + g + 8][0] = Y[2];
-            S.Y[tile * 16 + g + 8][1] = Y[3];
+    for (int q = 0; q < mlp::kIn / 2; ++q) {
+        p[q] = 0u;
+        if (want) {
+            const int c = 2 * q;
+            p[q] = mlp::pack2((x[c] - __ldg(M.params + mlp::oInShift + c)) * __ldg(M.params + mlp::oInScale + c),
+                              (x[c + 1] - __ldg(M.params + mlp::oInShift + c + 1)) *
+                                  __ldg(M.params + mlp::oInScale + c + 1));
         }
     }
-    __syncwarp();
-    if (want) {
-        y0 = S.Y[rank][0];
-        y1 = S.Y[rank][1];
+    for (int tile = 0; tile * 16 < cnt; ++tile) {
+        const int r0 = tile * 16 + g, r1 = r0 + 8;
+        const int s0 = r0 < cnt ? nth_set_lane(bal, r0) : lane;
+        const int s1 = r1 < cnt ? nth_set_lane(bal, r1) : lane;
+        /* A fragment: reg0 = row r0 word t, reg1 = row r1 word t, reg2 = row r0 word t + 4,
+         * reg3 = row r1 word t + 4 */
+        uint32_t A[1][4] = {{0u, 0u, 0u, 0u}};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t a0 = __shfl_sync(0xffffffffu, p[q], s0);
+            const uint32_t a1 = __shfl_sync(0xffffffffu, p[q], s1);
+            if (q == t) {
+                A[0][0] = a0;
+                A[0][1] = a1;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) { /* words 4 and 5; 6 and 7 stay zero */
+            const uint32_t a2 = __shfl_sync(0xffffffffu, p[q + 4], s0);
+            const uint32_t a3 = __shfl_sync(0xffffffffu, p[q + 4], s1);
+            if (q == t) {
+                A[0][2] = a2;
+                A[0][3] = a3;
+            }
+        }
+        if (r0 >= cnt) A[0][0] = A[0][2] = 0u;
+        if (r1 >= cnt) A[0][1] = A[0][3] = 0u;
+        float Y[4];
+        mlp::forward_frag(M, A, Y);
+        /* row rr of this tile: outputs in lane 4 (rr % 8), Y[0..1] for rr < 8, Y[2..3] above */
+        const int rr = rank - tile * 16;
+        const int src = 4 * (rr & 7);
+        const float v0 = __shfl_sync(0xffffffffu, Y[0], src), v1 = __shfl_sync(0xffffffffu, Y[1], src);
+        const float v2 = __shfl_sync(0xffffffffu, Y[2], src), v3 = __shfl_sync(0xffffffffu, Y[3], src);
+        if (want && rr >= 0 && rr < 16) {
+            y0 = rr < 8 ? v0 : v2;
+            y1 = rr < 8 ? v1 : v3;
+        }
     }
-    __syncwarp();
 }
 
 /* Aerodynamic acceleration of a live, aero-active particle from the closure outputs. */
@@ -128,8 +162,8 @@ __device__ __forceinline__ void learned_acc(const Params &P, const DevState &W, 
  * Not inlined: the residual's register allocation then does not absorb the network's. */
 template <int D>
 __device__ __noinline__ void closure_aero(const Params &P, const DevState &W, const Closure &C, const float4 *Kn,
-                                             const float4 *Kg, int64_t i, bool live, double nneigh, MlpWarpSmem &S,
-                                             bool &aero_on, double *aero) {
+                                             const float4 *Kg, int64_t i, bool live, double nneigh, bool &aero_on,
+                                             double *aero) {
 #pragma unroll
     for (int k = 0; k < D; ++k) aero[k] = 0.0;
     aero_on = live && W.cellID[i] != -1;
@@ -167,7 +201,7 @@ __device__ __noinline__ void closure_aero(const Params &P, const DevState &W, co
         return;
     }
     float y0 = 0.f, y1 = 0.f;
-    mlp_warp(C.M, want, x, S, y0, y1);
+    mlp_warp(C.M, want, x, y0, y1);
     if (want)
         learned_acc<D>(P, W, i, U, y0, y1, aero);
     else if (aero_on)

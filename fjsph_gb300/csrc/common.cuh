@@ -84,6 +84,10 @@ struct Params {
     const double *air_v;
     /* launch configuration of the split-precision pair sweeps (the autotuner's choices) */
     int32_t sweep_threads, resid_threads, list_ahead;
+    /* SM-local work order of the residual (0 = grid order): warps claim 32-particle chunks from
+     * per-SM regions through these counters (kMaxRegions, zeroed before each launch) */
+    int32_t sm_order;
+    int32_t *region_next;
     FConst fc;
     /* neighbour-search cell edges (support radius along x, radius / kCellDiv across) and their
      * reciprocals, so cell coordinates cost a multiply instead of an FP64 divide */
@@ -122,6 +126,63 @@ struct DevNbr {
     const int64_t *slice; /* split-precision form: first entry per slice  */
     const double *xs[3];
 };
+
+/* SM-local work order of a particle sweep.  The sweep's 32-particle chunks are grouped in
+ * super-chunks of kSuperChunk consecutive chunks, dealt round robin to one region per SM (%nsmid
+ * regions, at most kMaxRegions): region r holds super-chunks r, r + R, r + 2R, ...  A warp takes
+ * the region's next chunk of the SM it runs on, so the warps resident on an SM work on about
+ * kSuperChunk * 32 consecutive particles and share their neighbours' records in L1, while all SMs
+ * advance through the array together and share the rest in L2, as grid order does.  Once its
+ * region is used up a warp takes a chunk of the next region that still has one (the lanes look at
+ * 32 regions per round, so a warp that finds everything taken gives up after ceil(R / 32) rounds
+ * of loads).  Every chunk is handed out exactly once whatever %smid reads (it only picks the
+ * region tried first), and no warp waits on another. */
+constexpr int kMaxRegions = 256;
+constexpr int kSuperChunk = 32;
+/* chunk of the t-th claim of region r (of R); past the last chunk once the region is used up */
+FJSPH_HD int64_t region_chunk(int r, int R, int64_t t) {
+    return ((t / kSuperChunk) * R + r) * (int64_t)kSuperChunk + t % kSuperChunk;
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ int64_t claim_chunk(int32_t *next, int64_t chunks) {
+    const int lane = threadIdx.x & 31;
+    unsigned sm, nsm;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+    asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+    const int R = (int)min(max(nsm, 1u), (unsigned)kMaxRegions);
+    const int r0 = (int)(sm % (unsigned)R);
+    int64_t got = -1;
+    if (lane == 0) {
+        /* counters only grow, and a region's chunks grow with its counter */
+        if (region_chunk(r0, R, *(volatile int32_t *)(next + r0)) < chunks) {
+            const int64_t g = region_chunk(r0, R, atomicAdd(next + r0, 1));
+            if (g < chunks) got = g;
+        }
+    }
+    got = __shfl_sync(0xffffffffu, got, 0);
+    if (got >= 0) return got;
+    for (int base = 1; base < R; base += 32) {
+        const int k = base + lane;
+        int r = 0;
+        bool avail = false;
+        if (k < R) {
+            r = r0 + k < R ? r0 + k : r0 + k - R;
+            avail = region_chunk(r, R, *(volatile int32_t *)(next + r)) < chunks;
+        }
+        for (unsigned m = __ballot_sync(0xffffffffu, avail); m; m &= m - 1u) {
+            const int src = __ffs(m) - 1;
+            int64_t g = -1;
+            if (lane == src) {
+                g = region_chunk(r, R, atomicAdd(next + r, 1));
+                if (g >= chunks) g = -1;
+            }
+            g = __shfl_sync(0xffffffffu, g, src);
+            if (g >= 0) return g;
+        }
+    }
+    return -1;
+}
+#endif
 
 FJSPH_HD int64_t sell_entry(int64_t slot_base, int32_t k) {
     return slot_base + (int64_t)(k / kChunk) * (kSlice * kChunk) + (k % kChunk);

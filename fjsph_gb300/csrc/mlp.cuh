@@ -157,11 +157,10 @@ __device__ __forceinline__ void load_a16(const __nv_bfloat16 *X, uint32_t (&A)[1
     A[0][3] = X32[(g + 8) * 8 + 4 + t];
 }
 
-/* Forward pass of one 16-sample tile; Y receives the (un-normalised) 2 outputs of row g and g+8
- * for lanes with t == 0 (Y[0], Y[1] of row g; Y[2], Y[3] of row g+8). */
-__device__ __forceinline__ void forward_tile(const DevMlp &M, const __nv_bfloat16 *X, float (&Y)[4]) {
-    uint32_t A0[1][4];
-    load_a16(X, A0);
+/* Forward pass of one 16-sample tile from its input A fragment (normalised, BF16); Y receives the
+ * (un-normalised) 2 outputs of row g and g+8 for lanes with t == 0 (Y[0], Y[1] of row g; Y[2],
+ * Y[3] of row g+8). */
+__device__ __forceinline__ void forward_frag(const DevMlp &M, const uint32_t (&A0)[1][4], float (&Y)[4]) {
     float C1[kHid / 8][4];
     layer<kInP, kHid>(A0, M.w + bW1, M.params + oB1, C1);
     uint32_t A1[kHid / 16][4];
@@ -182,6 +181,13 @@ __device__ __forceinline__ void forward_tile(const DevMlp &M, const __nv_bfloat1
     Y[1] = C4[0][1] * s1 + h1;
     Y[2] = C4[0][2] * s0 + h0;
     Y[3] = C4[0][3] * s1 + h1;
+}
+
+/* The same from a shared tile X[16][16]. */
+__device__ __forceinline__ void forward_tile(const DevMlp &M, const __nv_bfloat16 *X, float (&Y)[4]) {
+    uint32_t A0[1][4];
+    load_a16(X, A0);
+    forward_frag(M, A0, Y);
 }
 
 } // namespace mlp

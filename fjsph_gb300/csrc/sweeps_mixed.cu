@@ -18,6 +18,9 @@
  *   F = (vPert, p)     G = (gradRho, lam)   N = (surface normal, 0)     T = (normal from pass 1)
  *   bits = b | surf << 3 | surfzone << 4
  */
+#include <algorithm>
+#include <atomic>
+
 #include "aero.cuh"
 #include "closure.cuh"
 #include "kernels.h"
@@ -989,17 +992,15 @@ struct ResidAcc {
     }
 };
 
+/* The residual of slot i; called by whole warps (the learned closure runs on whole warps), lanes
+ * with live == false contribute nothing. */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
-                                                      Closure C) {
-    __shared__ __align__(16) MlpWarpSmem mlp_smem[kThreads / 32];
-    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const bool live = i < P.n;
-    /* the aerodynamic term first: the learned closure runs on whole warps */
+__device__ __forceinline__ void resid_slot(const Params &P, const DevState &W, const DevNbr &N, const Packed &K,
+                                           const double *npd_dev, const Closure &C, int64_t i, bool live) {
+    /* the aerodynamic term first */
     double aero[D];
     bool aero_on;
-    closure_aero<D>(P, W, C, K.N, K.G, i, live, double(N.cnt[i]), mlp_smem[threadIdx.x >> 5],
-                    aero_on, aero);
+    closure_aero<D>(P, W, C, K.N, K.G, i, live, live ? double(N.cnt[i]) : 0.0, aero_on, aero);
     if (!live) return;
     const Pf f = make_pf(P);
     const bool linear = has(P, FJSPH_VAR_LINEAR);
@@ -1061,6 +1062,26 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, D
     ra.finish(P, W, i, aero, aero_on);
 }
 
+template <int D, bool ALE, bool NOFROZEN>
+__global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
+                                                      Closure C) {
+    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    resid_slot<D, ALE, NOFROZEN>(P, W, N, K, npd_dev, C, i, i < P.n);
+}
+
+/* The same over one resident grid in the SM-local order (claim_chunk).  A separate kernel: the
+ * compiler contracts the particle body's products and sums into fused multiply-adds per copy,
+ * so the two orders agree to FP32 rounding, not bit for bit. */
+template <int D, bool ALE, bool NOFROZEN>
+__global__ void __launch_bounds__(kThreads, 7) k_m_resid_sm(Params P, DevState W, DevNbr N, Packed K,
+                                                         const double *npd_dev, Closure C) {
+    const int64_t chunks = (P.n - P.nb + 31) / 32;
+    for (int64_t c = claim_chunk(P.region_next, chunks); c >= 0; c = claim_chunk(P.region_next, chunks)) {
+        const int64_t i = P.nb + 32 * c + (threadIdx.x & 31);
+        resid_slot<D, ALE, NOFROZEN>(P, W, N, K, npd_dev, C, i, i < P.n);
+    }
+}
+
 /* The residual over shared-memory tiles: each CTA stages a tile's halo as tile-relative records
  * and every lane walks one fluid particle's members with a cursor over its mask, the lanes of a
  * warp in step through the pair arithmetic. */
@@ -1069,7 +1090,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_t_resid(Params P, DevState 
                                                               const double *npd_dev, Closure C) {
     using TT = Tile<D>;
     extern __shared__ __align__(16) unsigned char tsm[];
-    __shared__ __align__(16) MlpWarpSmem mlp_smem[kTileThreads / 32];
     TileSmem ts = tile_smem<D>(tsm, T.smax, kStageRel);
     const TileGrid tg = tile_grid<D>(G);
     const Pf f = make_pf(P);
@@ -1093,7 +1113,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_t_resid(Params P, DevState 
             }
             double aero[D];
             bool aero_on;
-            closure_aero<D>(P, W, C, K.N, K.G, i, live, double(nn), mlp_smem[wid], aero_on, aero);
+            closure_aero<D>(P, W, C, K.N, K.G, i, live, double(nn), aero_on, aero);
             if (!live) continue;
             float4 Pi, Vi, Ti;
             tile_ld_rel<D>(ts, G, K, o.e, o.hc / TT::HX, over, Pi, Vi, Ti);
@@ -1208,12 +1228,43 @@ void launch_m_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, c
                           cudaStream_t s) {
     FJSPH_DISPATCH_M(P, k_m_bound_ghost, bgrid(P), P, W, N, K, near_inlet);
 }
+/* Blocks of `bs` threads of `kernel` resident on the whole device at once: the grid of the
+ * SM-local order. */
+template <typename F>
+unsigned resident_grid(F kernel, int bs) {
+    int dev = 0, sms = 1, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs, 0) != cudaSuccess || per < 1) per = 1;
+    return (unsigned)(sms * per);
+}
+
+template <int D, bool A, bool NF>
+void m_resid_launch(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
+                    const Closure &C, unsigned g, cudaStream_t s) {
+    const int bs = resid_bs(P);
+    if (!P.sm_order) {
+        k_m_resid<D, A, NF><<<g, bs, 0, s>>>(P, W, N, K, npd_dev, C);
+        return;
+    }
+    /* resident blocks, computed once per instantiation and block size (64 or 128) */
+    static std::atomic<unsigned> cached[2] = {0u, 0u};
+    std::atomic<unsigned> &cg = cached[bs == 64 ? 0 : 1];
+    unsigned rg = cg.load(std::memory_order_relaxed);
+    if (rg == 0u || (bs != 64 && bs != 128)) {
+        rg = resident_grid(k_m_resid_sm<D, A, NF>, bs);
+        if (bs == 64 || bs == 128) cg.store(rg, std::memory_order_relaxed);
+    }
+    cudaMemsetAsync(P.region_next, 0, sizeof(int32_t) * kMaxRegions, s);
+    k_m_resid_sm<D, A, NF><<<std::min(g, rg), bs, 0, s>>>(P, W, N, K, npd_dev, C);
+}
+
 void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, const double *npd_dev,
                     const Closure &C, cudaStream_t s) {
     const unsigned g = grid_for(P.n - P.nb, resid_bs(P));
     if (g == 0) return;
     const bool ale = has(P, FJSPH_VAR_ALE), nf = has(P, FJSPH_VAR_NOFROZEN);
-#define FJSPH_RESID_M(DD, A, NF) k_m_resid<DD, A, NF><<<g, resid_bs(P), 0, s>>>(P, W, N, K, npd_dev, C)
+#define FJSPH_RESID_M(DD, A, NF) m_resid_launch<DD, A, NF>(P, W, N, K, npd_dev, C, g, s)
     if (P.D == 2) {
         if (ale)
             nf ? FJSPH_RESID_M(2, true, true) : FJSPH_RESID_M(2, true, false);

@@ -310,6 +310,10 @@ int fjsph_get_tuning(fjsph_ctx *ctx, int32_t *cfg3);
  * times on the current state and neighbour lists, keeps the fastest and returns it in chosen3;
  * times_ms (8 doubles, may be NULL) receives the mean time of every candidate in that order. */
 int fjsph_autotune(fjsph_ctx *ctx, int32_t repeats, int32_t *chosen3, double *times_ms);
+/* Times the residual in grid order and in the SM-local order (fjsph_set_sweep_order) `repeats`
+ * times each with the current tuning, keeps the faster order and returns it in chosen; times_ms
+ * (2 doubles, may be NULL) receives the mean time of each, grid order first. */
+int fjsph_autotune_order(fjsph_ctx *ctx, int32_t repeats, int32_t *chosen, double *times_ms);
 
 /* ---- learned aerodynamic closure ------------------------------------------------------------ */
 /* No counterpart in the reference: a 12 -> 64 -> 64 -> 64 -> 2 GELU network (BF16 weights, FP32
@@ -500,6 +504,15 @@ int fjsph_step_report(fjsph_ctx *ctx, double *out5);
 #define FJSPH_PAIRS_LISTS 1
 int fjsph_set_pair_mode(fjsph_ctx *ctx, int32_t mode);
 int fjsph_get_pair_mode(fjsph_ctx *ctx, int32_t *mode, int32_t *tiles_in_use);
+/* Work order of the split-precision residual (no reference counterpart: a property of this
+ * implementation; results are identical in both).  FJSPH_ORDER_GRID (default): one thread per
+ * particle in launch-grid order.  FJSPH_ORDER_SM: one resident grid whose warps take 32-particle
+ * chunks from a contiguous region per SM, so that the warps sharing an SM's L1 work on
+ * neighbouring particles. */
+#define FJSPH_ORDER_GRID 0
+#define FJSPH_ORDER_SM 1
+int fjsph_set_sweep_order(fjsph_ctx *ctx, int32_t order);
+int fjsph_get_sweep_order(fjsph_ctx *ctx, int32_t *order);
 /* Neighbour count (self included) of every particle, in reference order, from the last search
  * (counts: particle-count entries).  No reference counterpart: a diagnostic of the search. */
 int fjsph_neighbour_counts(fjsph_ctx *ctx, int32_t *counts);

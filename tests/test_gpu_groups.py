@@ -106,6 +106,10 @@ def test_autotune_choice_and_identical_results():
     out = ctx.autotune(2)
     ch = out["chosen"]
     assert ch["sweep_threads"] in (64, 128) and ch["resid_threads"] in (64, 128) and ch["list_ahead"] in (2, 4, 8)
-    assert len(out["trials_ms"]) == 8 and all(t["ms"] > 0 for t in out["trials_ms"])
+    assert len(out["trials_ms"]) == 10 and all(t["ms"] > 0 for t in out["trials_ms"])
     assert ctx.tuning() == (ch["sweep_threads"], ch["resid_threads"], ch["list_ahead"])
+    # the residual's work order: the faster of the two timed orders is kept
+    grid_ms, sm_ms = (t["ms"] for t in out["trials_ms"][8:])
+    assert ch["order"] == ("sm" if sm_ms < grid_ms else "grid")
+    assert ctx.sweep_order() == (d.ORDER_SM if ch["order"] == "sm" else d.ORDER_GRID)
     ctx.close()
