@@ -113,3 +113,34 @@ def test_autotune_choice_and_identical_results():
     assert ch["order"] == ("sm" if sm_ms < grid_ms else "grid")
     assert ctx.sweep_order() == (d.ORDER_SM if ch["order"] == "sm" else d.ORDER_GRID)
     ctx.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_one_group_with_walls_equals_context(graph):
+    """A context holding one simulation with walls (the 2D dam break) as its only group steps as
+    the ordinary context does: FP64 displacements and density changes within 1e-8 relative, the
+    same time and CFL number; with and without the CUDA-graph replay."""
+    from fjsph_gb300.api import Context
+    c = cases.dam_break_2d(dx=0.04)
+    steps = 20
+    s = c.settings.copy()
+    ctx = Context(s, c.state.n + 64, c.blocks)
+    ctx.set_states(c.state, c.state)
+    for _ in range(steps):
+        ctx.integrate()
+    ref, rset = ctx.download(), ctx.settings
+    ctx.close()
+    ctx = Context(s, c.state.n + 64, c.blocks)
+    ctx.set_groups([0, c.state.n], [list(s.v_inf)])
+    ctx.set_states(c.state, c.state)
+    ctx.integrate_groups(steps, graph=graph)
+    got, rep = ctx.download(), ctx.group_report()
+    ctx.close()
+    nb = c.state.n - c.n_fluid
+    sl = slice(nb, None)
+    assert rep["steps"][0] == steps
+    assert rel_err(got.xi[sl] - c.state.xi[sl], ref.xi[sl] - c.state.xi[sl]) < 1e-8
+    assert rel_err(got.rho[sl] - c.state.rho[sl], ref.rho[sl] - c.state.rho[sl]) < 1e-8
+    np.testing.assert_array_equal(got.xi[:nb], ref.xi[:nb])  # the walls stay put
+    assert rep["time"][0] == pytest.approx(rset.current_time, rel=1e-12)
+    assert rep["cfl"][0] == pytest.approx(rset.cfl, rel=1e-12)
