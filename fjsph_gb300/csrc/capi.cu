@@ -475,11 +475,11 @@ void ensure_pack(fjsph_ctx *c) {
     c->dirty_full = c->dirty_all = c->dirty_bound = false;
 }
 
-/* The stage updates write the split-precision inputs of the fluid particles they move when the
- * packed arrays are current apart from that (no inlet moves buffer particles afterwards); the
- * packed state is then complete again without a packing pass. */
+/* The stage updates write the split-precision inputs of the fluid particles they move, and the
+ * inlet buffer moves those of the buffer particles they place, when the packed arrays are current
+ * apart from that; the packed state is then complete again without a packing pass. */
 const Packed *fused_pack(const fjsph_ctx *c) {
-    return (mixed(c) && c->packed_alloc && c->inlets.empty() && !c->dirty_full && !c->dirty_all) ? &c->K : nullptr;
+    return (mixed(c) && c->packed_alloc && !c->dirty_full && !c->dirty_all) ? &c->K : nullptr;
 }
 void after_update(fjsph_ctx *c) {
     if (!fused_pack(c)) mark_all(c);
@@ -1053,9 +1053,10 @@ int prestep_passes(fjsph_ctx *c) {
     }
     {
         Section sec(c, PASS_UPDATE);
-        launch_pipe_outlet(P, WS(c), s);
+        const Packed *K = fused_pack(c);
+        launch_pipe_outlet(P, WS(c), K ? K->bits : nullptr, s);
         c->launches++;
-        mark_all(c);
+        if (!K) mark_all(c);
     }
     c->pn_equals_W = false;
     return FJSPH_OK;
@@ -1195,7 +1196,8 @@ DevInlet dev_inlet(const fjsph_ctx *c, const HostInlet &I) {
 void inlet_buffers(fjsph_ctx *c, const Params &P, int mode, double dt_scale) {
     for (const HostInlet &I : c->inlets) {
         if (I.n_back == 0 || I.depth == 0) continue;
-        launch_inlet_buffers(P, PN(c), WS(c), c->S, dev_inlet(c, I), mode, dt_ptr(c), dt_scale, c->stream);
+        launch_inlet_buffers(P, PN(c), WS(c), c->S, dev_inlet(c, I), mode, dt_ptr(c), dt_scale, fused_pack(c),
+                             c->stream);
         c->launches++;
     }
 }
@@ -1451,7 +1453,8 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
  * BUFFER particle becomes BACK and the column shifts; while the particle count is below
  * max_points (and the context capacity), a new BUFFER particle one dx upstream of the column's
  * last one is inserted at the end of the block's reference range. */
-int inlet_advance(fjsph_ctx *c) {
+int inlet_advance(fjsph_ctx *c, bool &moved) {
+    moved = false;
     if (c->inlets.empty()) return FJSPH_OK;
     const int64_t limit = std::min<int64_t>(c->s.max_points, c->cap);
     const int64_t n_old = c->n;
@@ -1508,6 +1511,7 @@ int inlet_advance(fjsph_ctx *c) {
         }
     }
     if (ops.empty()) return FJSPH_OK;
+    moved = true;
     /* existing particles of later blocks move up by the insertions before them */
     BlockShift sh{};
     int64_t acc = 0;
@@ -1600,15 +1604,16 @@ int delete_particles(fjsph_ctx *c) {
  * (:116-124), deletion; the neighbour lists and packed inputs are stale afterwards. */
 int update_data(fjsph_ctx *c) {
     const int64_t n0 = c->n;
-    TRY(inlet_advance(c));
-    launch_density_guard(make_params(c), WS(c), c->stream);
+    bool moved = false;
+    TRY(inlet_advance(c, moved));
+    launch_density_guard(make_params(c), WS(c), fused_pack(c), c->stream);
     c->launches++;
     TRY(delete_particles(c));
     if (c->n != n0) {
         c->nbr_valid = false;
         mark_full(c);
     }
-    mark_all(c);
+    if (moved) mark_all(c); /* inlet columns advanced: types changed, particles inserted */
     return FJSPH_OK;
 }
 
@@ -1717,7 +1722,7 @@ int group_step(fjsph_ctx *c) {
     TRY(rk_intermediate(c, 3, 1.0));
     TRY(rk_final(c));
     TRY(group_err(c, c->S.xsnap, 1));
-    launch_density_guard(make_params(c), WS(c), c->stream);
+    launch_density_guard(make_params(c), WS(c), nullptr, c->stream);
     c->launches++;
     mark_all(c);
     TRY(copy_state(c, c->iW, c->ipn));
@@ -2244,7 +2249,7 @@ int fjsph_particle_shift(fjsph_ctx *c) {
 
 int fjsph_check_pipe_outlet(fjsph_ctx *c) {
     TRY(need_state(c));
-    launch_pipe_outlet(make_params(c), WS(c), c->stream);
+    launch_pipe_outlet(make_params(c), WS(c), nullptr, c->stream);
     c->pn_equals_W = false;
     mark_all(c);
     return sync(c);

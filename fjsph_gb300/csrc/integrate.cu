@@ -184,7 +184,7 @@ __global__ void k_nb_update(Params P, DevState pn, DevState W, const double *dt_
  * One thread per back particle walks its buffer column. */
 template <int D>
 __global__ void k_inlet_buffers(Params P, DevState pn, DevState W, RKScratch S, DevInlet I, int mode,
-                                const double *dt_dev, double dt_scale) {
+                                const double *dt_dev, double dt_scale, Packed K) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= I.n_back) return;
     const double dt = dt_scale * (*dt_dev);
@@ -199,6 +199,7 @@ __global__ void k_inlet_buffers(Params P, DevState pn, DevState W, RKScratch S, 
             }
             W.rho[bid] = W.rho[back];
             W.p[bid] = W.p[back];
+            if (K.A) pack_slot<D>(P, W, K, bid); /* the split-precision inputs of the moved particle */
         }
     } else {
         for (int64_t jj = 0; jj < I.depth; ++jj) {
@@ -215,15 +216,20 @@ __global__ void k_inlet_buffers(Params P, DevState pn, DevState W, RKScratch S, 
             W.p[bid] = eos_pressure(P, rho);
 #pragma unroll
             for (int k = 0; k < D; ++k) W.x[k][bid] = pn.x[k][bid] + dt * pn.v[k][bid];
+            if (K.A) pack_slot<D>(P, W, K, bid);
         }
     }
 }
 
 /* update_data's zero-density guard (src/Integration.cpp:116-124). */
-__global__ void k_density_guard(Params P, DevState W) {
+template <int D>
+__global__ void k_density_guard(Params P, DevState W, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    if (W.rho[i] < 0.0001) W.rho[i] = P.rho_rest;
+    if (W.rho[i] < 0.0001) {
+        W.rho[i] = P.rho_rest;
+        if (K.A) pack_slot<D>(P, W, K, i); /* the split-precision inputs of the reset particle */
+    }
 }
 
 /* ---- reductions ------------------------------------------------------------------------------- */
@@ -393,12 +399,15 @@ void launch_nb_update(const Params &P, const DevState &pn, const DevState &W, co
     FJSPH_DISPATCH2(P.D, k_nb_update, grid_for(P.n - P.nb, kThreads), kThreads, P, pn, W, dt_dev);
 }
 void launch_inlet_buffers(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S,
-                          const DevInlet &I, int mode, const double *dt_dev, double dt_scale, cudaStream_t s) {
-    FJSPH_DISPATCH2(P.D, k_inlet_buffers, grid_for(I.n_back, 64), 64, P, pn, W, S, I, mode, dt_dev, dt_scale);
+                          const DevInlet &I, int mode, const double *dt_dev, double dt_scale, const Packed *K,
+                          cudaStream_t s) {
+    const Packed none{};
+    FJSPH_DISPATCH2(P.D, k_inlet_buffers, grid_for(I.n_back, 64), 64, P, pn, W, S, I, mode, dt_dev, dt_scale,
+                    K ? *K : none);
 }
-void launch_density_guard(const Params &P, const DevState &W, cudaStream_t s) {
-    const unsigned g = grid_for(P.n - P.nb, kThreads);
-    if (g) k_density_guard<<<g, kThreads, 0, s>>>(P, W);
+void launch_density_guard(const Params &P, const DevState &W, const Packed *K, cudaStream_t s) {
+    const Packed none{};
+    FJSPH_DISPATCH2(P.D, k_density_guard, grid_for(P.n - P.nb, kThreads), kThreads, P, W, K ? *K : none);
 }
 void launch_sum(const double *in, int64_t n, double *part, int64_t part_len, double *out, cudaStream_t s) {
     const unsigned g = red_grid(n, part_len, 1);

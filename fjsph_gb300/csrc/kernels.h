@@ -223,7 +223,8 @@ void launch_detect_surface(const Params &P, const DevState &W, const DevNbr &N, 
                            cudaStream_t s);
 void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
 void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
-void launch_pipe_outlet(const Params &P, const DevState &W, cudaStream_t s);
+/* kbits: the packed flags to keep current (null: the caller repacks) */
+void launch_pipe_outlet(const Params &P, const DevState &W, int32_t *kbits, cudaStream_t s);
 /* boundary passes over slots [0, nb) */
 void launch_bound_velocity(const Params &P, const DevState &W, int nb_rule, cudaStream_t s);
 void launch_no_slip(const Params &P, const DevState &W, const DevNbr &N, double *const vtmp[3], cudaStream_t s);
@@ -282,11 +283,13 @@ struct DevInlet {
     double unorm[3];
 };
 void launch_inlet_buffers(const Params &P, const DevState &pn, const DevState &W, const RKScratch &S,
-                          const DevInlet &I, int mode, const double *dt_dev, double dt_scale, cudaStream_t s);
+                          const DevInlet &I, int mode, const double *dt_dev, double dt_scale, const Packed *K,
+                          cudaStream_t s);
 /* Sum over fluid slots of |W.x - ref|^2, written to out[0]. */
 void launch_sq_disp_sum(const Params &P, const DevState &W, double *const ref[3], RKScratch &S, double *out,
                         cudaStream_t s);
-void launch_density_guard(const Params &P, const DevState &W, cudaStream_t s);
+/* K: packed inputs to keep current for the particles the guard resets (null: the caller repacks) */
+void launch_density_guard(const Params &P, const DevState &W, const Packed *K, cudaStream_t s);
 /* Sum of an array over [0, n) into out[0], deterministic (two-pass). */
 void launch_sum(const double *in, int64_t n, double *part, int64_t part_len, double *out, cudaStream_t s);
 /* find_timestep reductions over fluid slots: out[0..6] = maxf, maxAf, maxdrho, maxRhoi, minST, maxU,

@@ -73,4 +73,16 @@ __device__ __forceinline__ void pack_moved(const Params &P, const DevState &W, c
     K.Lo[i] = pack_lo(xl, vl, pr, bits);
 }
 
+/* pack_moved of slot i from its current x, v, rho and p in W */
+template <int D>
+__device__ __forceinline__ void pack_slot(const Params &P, const DevState &W, const Packed &K, int64_t i) {
+    double x[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        x[k] = W.x[k][i];
+        v[k] = W.v[k][i];
+    }
+    pack_moved<D>(P, W, K, i, x, v, W.rho[i], W.p[i]);
+}
+
 } // namespace fjsph

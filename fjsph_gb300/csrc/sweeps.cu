@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(kThreads) k_particle_shift(Params P, DevState 
 /* Check_Pipe_Outlet (src/Containment.cpp:822-894), analytic air source                        */
 /* ------------------------------------------------------------------------------------------ */
 template <int D>
-__global__ void k_pipe_outlet(Params P, DevState W) {
+__global__ void k_pipe_outlet(Params P, DevState W, int32_t *kbits) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     if (W.b[i] != FJSPH_PIPE) return;
@@ -505,7 +505,11 @@ __global__ void k_pipe_outlet(Params P, DevState W) {
     double s = W.x[0][i] * B.aero_norm[0];
 #pragma unroll
     for (int k = 1; k < D; ++k) s += W.x[k][i] * B.aero_norm[k];
-    if (s > B.aeroconst) W.b[i] = FJSPH_FREE;
+    if (s > B.aeroconst) {
+        W.b[i] = FJSPH_FREE;
+        /* the packed type bits follow (the packed fluid flag is set for both types) */
+        if (kbits) kbits[i] = (kbits[i] & ~7) | FJSPH_FREE;
+    }
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -826,8 +830,8 @@ void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, cud
 void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
     FJSPH_DISPATCH(P, k_particle_shift, fluid_grid(P), P, W, N);
 }
-void launch_pipe_outlet(const Params &P, const DevState &W, cudaStream_t s) {
-    FJSPH_DISPATCH(P, k_pipe_outlet, fluid_grid(P), P, W);
+void launch_pipe_outlet(const Params &P, const DevState &W, int32_t *kbits, cudaStream_t s) {
+    FJSPH_DISPATCH(P, k_pipe_outlet, fluid_grid(P), P, W, kbits);
 }
 void launch_bound_velocity(const Params &P, const DevState &W, int nb_rule, cudaStream_t s) {
     FJSPH_DISPATCH(P, k_bound_velocity, bound_grid(P), P, W, nb_rule);
