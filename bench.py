@@ -88,6 +88,8 @@ def parse():
     ap.add_argument("--pairs", default="lists", choices=["lists", "tiles"],
                     help="pair sweeps of the FP32 form: pair lists or shared-memory tiles (residual)")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--order", default="auto", choices=["auto", "grid", "sm"],
+                    help="work order of the FP32 residual on the jet: the autotuner's choice, grid or SM-local")
     return ap.parse_args()
 
 
@@ -533,8 +535,11 @@ def run_ours(args, ws, rank, local):
     for _ in range(args.warmup):
         ctx.integrate()
     tune = ctx.autotune(3) if s.precision == d.PREC_MIXED and not args.no_tune else None
-    if tune:
+    if s.precision == d.PREC_MIXED and args.order != "auto":
+        ctx.set_sweep_order(d.ORDER_SM if args.order == "sm" else d.ORDER_GRID)
+    if tune or args.order != "auto":
         ctx.integrate()  # one more warm-up step under the chosen configuration
+    order = ("sm" if ctx.sweep_order() == d.ORDER_SM else "grid") if s.precision == d.PREC_MIXED else None
     barrier(ws)
     clocks = Clocks(local)
     clocks.start()
@@ -631,7 +636,7 @@ def run_ours(args, ws, rank, local):
     return dict(value=value, ms=ms, nf=c.n_fluid, n=c.state.n, roof=roof, e2e=e2e, clocks=clk, launches=launches,
                 fp64=fp64, prof={k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]}, rep=rep, settings=s,
                 case=c, plain=plain, closure=closure_info, pairs=n_pairs, tune=tune, weights=weights, live=live,
-                ps=ps)
+                ps=ps, order=order)
 
 
 def _rel_rms(a, b) -> float:
@@ -1031,6 +1036,7 @@ def main():
                 "fp64_form": r["fp64"], "fp32_plain_closure_form": r["plain"],
                 "speedup_vs_fp64_form": (r["value"] / r["fp64"]["value"]) if r["fp64"] else None,
                 "closure": r["closure"], "neighbour_pairs": r["pairs"], "autotune": r["tune"],
+                "residual_order": r["order"],
                 "neighbour_pairs_per_s": r["pairs"] * args.steps * ws / (r["ms"] / 1e3),
                 "gpu_launches": r["launches"], "passes_ms": r["prof"],
                 "config0_dam_break_2d": cfg0, "config1_dam_break_3d": cfg1, "droplet_batch": drops,
