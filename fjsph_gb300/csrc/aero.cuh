@@ -7,6 +7,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "split.cuh"
 
 namespace fjsph {
 
@@ -145,6 +146,43 @@ __device__ __forceinline__ void aero_acc(const Params &P, const DevState &W, int
             }
         }
     }
+}
+
+/* The Gissler closure of aero_acc evaluated in FP32, for the split-precision form (whose aero
+ * force is held to 1e-3 of the FP64 oracle): the same formula on FP32 operands with the
+ * constants of FConst, powf for the sphere drag law.  On this GPU the FP64 pipe issues a warp
+ * instruction every 16 cycles per SM, and the FP64 drag law (two pow, a square root, divides) of
+ * the exposed particles kept it a third busy in the residual.  U = cellV - v; one_m_woccl =
+ * 1 - woccl; nneigh the neighbour count (self included). */
+template <int D>
+__device__ __forceinline__ void gissler_acc_f32(const Params &P, const float *U, float cellRho, float cellP,
+                                                float one_m_woccl, float m, float lam, float nneigh, float *out) {
+    const FConst &c = P.fc;
+    float V2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) V2 += U[k] * U[k];
+    const float Vn = sqrtf(V2);
+    const float Re = c.re_coef * cellRho * Vn;
+    const float frac2 = P.use_lam ? fminf(c.interp_fac * lam, 1.f) : fminf(c.interp_fac * nneigh * c.i_n_full, 1.f);
+    const float frac1 = 1.f - frac2;
+    const float Cds = (1.f + 0.197f * powf(Re, 0.63f) + 2.6e-04f * powf(Re, 1.38f)) * (24.f / (Re + 0.00001f));
+    float Cdl = Cds, Adrop = c.A_sphere;
+    if (P.use_TAB_def) {
+        const float ymax = fminf(V2 * c.ycoef, 1.f);
+        Cdl = Cds * (1.f + 2.632f * ymax);
+        if (D == 3) {
+            const float t = c.L + c.CbL * ymax;
+            Adrop = (float)kPi * t * t;
+        } else {
+            Adrop = c.A_sphere + 2.f * (c.CbL * ymax);
+        }
+    }
+    const float Cdi = frac1 * Cdl + frac2;
+    const float Aun = frac1 * Adrop + frac2 * c.A_plate;
+    const float tail = c.force_coef * cellP * Cdi * (one_m_woccl * Aun) / m;
+    const float cc = 0.5f * Vn * tail;
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = cc * U[k];
 }
 
 } // namespace fjsph

@@ -381,6 +381,19 @@ Params make_params(const fjsph_ctx *c) {
         const double H2 = 2.0 * s.H;
         const double lam = (6.0 / 81.0 * (H2 * H2 * H2) / (pi * pi * pi * pi) * (9.0 / 4.0 * (pi * pi * pi) - 6.0 * pi - 4.0));
         f.st_coef = 0.5 * s.sig / lam;
+        f.st_coef_f = (float)f.st_coef;
+        f.re_coef = (float)(2.0 * s.L / s.mu_g);
+        f.interp_fac = (float)s.interp_fac;
+        f.i_n_full = (float)s.i_n_full;
+        f.ycoef = (float)s.ycoef;
+        f.L = (float)s.L;
+        f.CbL = (float)(s.Cb * s.L);
+        f.A_sphere = (float)s.A_sphere;
+        f.A_plate = (float)s.A_plate;
+        f.force_coef = (float)(s.gamma_g / (s.sos * s.sos));
+        f.we_coef = s.sig > 0.0 ? (float)(s.L / s.sig) : 0.f;
+        f.surf_h = (float)(1.33 * s.particle_step);
+        f.lam_cutoff = (float)s.lam_cutoff;
     }
     P.L = s.L;
     P.A_sphere = s.A_sphere;

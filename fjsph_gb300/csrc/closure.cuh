@@ -53,28 +53,32 @@ __device__ __forceinline__ int nth_set_lane(unsigned bal, int r) {
     return s;
 }
 
+/* The 12 network inputs of particle i (FP32; U = cellV - v, nneigh the neighbour count). */
 template <int D>
-__device__ __forceinline__ void closure_inputs(const Params &P, float4 occ, double nneigh, const double *U,
-                                               double cellRho, float4 nrm, float lam, float (&x)[mlp::kIn]) {
-    const double U2 = dot<D, double>(U, U);
-    const double Un = sqrt(U2);
+__device__ __forceinline__ void closure_inputs(const Params &P, float4 occ, float nneigh, const float *U,
+                                               float cellRho, float4 nrm, float lam, float (&x)[mlp::kIn]) {
+    const FConst &c = P.fc;
+    float U2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) U2 += U[k] * U[k];
+    const float Un = sqrtf(U2);
     x[0] = occ.x;
     x[1] = occ.y;
     x[2] = occ.z;
     x[3] = occ.w;
-    x[4] = (float)(nneigh * P.i_n_full);
-    x[5] = log10f(1.f + (float)Un);
-    x[6] = P.sig > 0.0 ? log10f(1.f + (float)(cellRho * U2 * P.L / P.sig)) : 0.f;
-    x[7] = log10f(1.f + (float)(2.0 * cellRho * Un * P.L / P.mu_g));
+    x[4] = nneigh * c.i_n_full;
+    x[5] = log10f(1.f + Un);
+    x[6] = c.we_coef > 0.f ? log10f(1.f + cellRho * U2 * c.we_coef) : 0.f;
+    x[7] = log10f(1.f + c.re_coef * cellRho * Un);
     const float n[3] = {nrm.x, nrm.y, nrm.z};
     float nn = 0.f, nu = 0.f;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         nn += n[k] * n[k];
-        nu += n[k] * (float)U[k];
+        nu += n[k] * U[k];
     }
     x[8] = sqrtf(nn);
-    x[9] = Un > 0.0 ? nu / (float)Un : 0.f;
+    x[9] = Un > 0.f ? nu / Un : 0.f;
     x[10] = nrm.w;
     x[11] = lam;
 }
@@ -145,16 +149,48 @@ __device__ __forceinline__ void mlp_warp(const mlp::DevMlp &M, bool want, const 
     }
 }
 
-/* Aerodynamic acceleration of a live, aero-active particle from the closure outputs. */
+/* Aerodynamic acceleration of a live, aero-active particle from the closure outputs (FP32,
+ * U = cellV - v). */
 template <int D>
-__device__ __forceinline__ void learned_acc(const Params &P, const DevState &W, int64_t i, const double *U, float y0,
+__device__ __forceinline__ void learned_acc(const Params &P, const DevState &W, int64_t i, const float *U, float y0,
                                             float y1, double *out) {
-    const double Un = vnorm<D, double>(U);
-    const double CdA = (double)exp10f(y0) * P.A_sphere;
-    const double wo = (double)fminf(fmaxf(y1, 0.f), 1.f);
-    const double tail = P.gamma_g * W.cellP[i] * CdA * (1.0 - wo) / W.m[i];
+    float U2 = 0.f;
 #pragma unroll
-    for (int k = 0; k < D; ++k) out[k] = 0.5 * Un * U[k] / (P.sos * P.sos) * tail;
+    for (int k = 0; k < D; ++k) U2 += U[k] * U[k];
+    const float Un = sqrtf(U2);
+    const float CdA = exp10f(y0) * P.fc.A_sphere;
+    const float wo = fminf(fmaxf(y1, 0.f), 1.f);
+    const float tail = P.fc.force_coef * to_f32(W.cellP[i]) * CdA * (1.f - wo) / to_f32(W.m[i]);
+    const float cc = 0.5f * Un * tail;
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = to_f64(cc * U[k]);
+}
+
+/* The plain closure in the split-precision form: Gissler's in FP32 (gissler_acc_f32), the other
+ * closures in FP64 (aero_acc).  A fully occluded particle (woccl exactly 1) gets no force, as in
+ * aero_acc. */
+template <int D>
+__device__ __forceinline__ void plain_acc(const Params &P, const DevState &W, int64_t i, const float *U,
+                                          double nneigh, double *out) {
+    if (P.acase != FJSPH_GISSLER) {
+        double Ud[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Ud[k] = W.cellV[k][i] - W.v[k][i];
+        aero_acc<D>(P, W, i, Ud, W.lam_nb[i], nneigh, out);
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = 0.0;
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) finite = finite && isfinite(U[k]);
+    const double wo = W.woccl[i];
+    if (__double_as_longlong(wo) == __double_as_longlong(1.0) && finite) return;
+    float o[3];
+    gissler_acc_f32<D>(P, U, to_f32(W.cellRho[i]), to_f32(W.cellP[i]), to_f32(1.0 - wo), to_f32(W.m[i]),
+                       to_f32(W.lam_nb[i]), to_f32(nneigh), o);
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = to_f64(o[k]);
 }
 
 /* The aerodynamic term of the residual for particle i under the closure mode.  All lanes of the
@@ -167,19 +203,22 @@ __device__ __noinline__ void closure_aero(const Params &P, const DevState &W, co
 #pragma unroll
     for (int k = 0; k < D; ++k) aero[k] = 0.0;
     aero_on = live && W.cellID[i] != -1;
-    double U[D];
+    /* relative air velocity in FP32, from the integer FP64 -> FP32 roundings */
+    float U[3] = {0.f, 0.f, 0.f};
+    if (aero_on) {
 #pragma unroll
-    for (int k = 0; k < D; ++k) U[k] = aero_on ? W.cellV[k][i] - W.v[k][i] : 0.0;
+        for (int k = 0; k < D; ++k) U[k] = to_f32(W.cellV[k][i]) - to_f32(W.v[k][i]);
+    }
     if (C.mode == kClosurePlain) {
-        if (aero_on) aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, aero);
+        if (aero_on) plain_acc<D>(P, W, i, U, nneigh, aero);
         return;
     }
     /* the network covers the particles whose occlusion factor is not fixed at 1 by lambda_nb */
-    const bool want = aero_on && (float)W.lam_nb[i] < (float)P.lam_cutoff;
+    const bool want = aero_on && to_f32(W.lam_nb[i]) < to_f32(P.lam_cutoff);
     float x[mlp::kIn];
-    if (want) closure_inputs<D>(P, C.occ[i], nneigh, U, W.cellRho[i], Kn[i], Kg[i].w, x);
+    if (want) closure_inputs<D>(P, C.occ[i], to_f32(nneigh), U, to_f32(W.cellRho[i]), Kn[i], Kg[i].w, x);
     if (C.mode == kClosureLog) {
-        if (aero_on) aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, aero);
+        if (aero_on) plain_acc<D>(P, W, i, U, nneigh, aero);
         const unsigned bal = __ballot_sync(0xffffffffu, want);
         if (bal == 0u) return;
         const int lane = threadIdx.x & 31;
@@ -189,9 +228,12 @@ __device__ __noinline__ void closure_aero(const Params &P, const DevState &W, co
         if (want) {
             const unsigned long long slot = base + (unsigned long long)__popc(bal & ((1u << lane) - 1u));
             if (slot < (unsigned long long)C.log_cap) {
-                double Cdi, Aun;
-                const double Un = vnorm<D, double>(U);
-                gissler_coeff<D>(P, W.cellRho[i], Un, dot<D, double>(U, U), W.lam_nb[i], nneigh, Cdi, Aun);
+                /* the targets: the plain closure's own coefficients (FP64) */
+                double Ud[D], Cdi, Aun;
+#pragma unroll
+                for (int k = 0; k < D; ++k) Ud[k] = W.cellV[k][i] - W.v[k][i];
+                const double Un = vnorm<D, double>(Ud);
+                gissler_coeff<D>(P, W.cellRho[i], Un, dot<D, double>(Ud, Ud), W.lam_nb[i], nneigh, Cdi, Aun);
 #pragma unroll
                 for (int c = 0; c < mlp::kIn; ++c) C.logX[slot * mlp::kIn + c] = x[c];
                 C.logT[slot * 2] = (float)log10(Cdi * Aun / P.A_sphere);
@@ -205,12 +247,15 @@ __device__ __noinline__ void closure_aero(const Params &P, const DevState &W, co
     if (want)
         learned_acc<D>(P, W, i, U, y0, y1, aero);
     else if (aero_on)
-        aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, aero);
+        plain_acc<D>(P, W, i, U, nneigh, aero);
     if (C.mode == kClosureJudge) {
         double d2 = 0.0, p2 = 0.0, cnt = 0.0;
         if (want) {
-            double ref[D];
-            aero_acc<D>(P, W, i, U, W.lam_nb[i], nneigh, ref);
+            /* the reference: the plain closure in FP64 */
+            double ref[D], Ud[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) Ud[k] = W.cellV[k][i] - W.v[k][i];
+            aero_acc<D>(P, W, i, Ud, W.lam_nb[i], nneigh, ref);
 #pragma unroll
             for (int k = 0; k < D; ++k) {
                 d2 += (aero[k] - ref[k]) * (aero[k] - ref[k]);

@@ -57,6 +57,14 @@ struct FConst {
     float fac_bound; /* 1 + cos(7 pi / 18) / 2 (Kernel.h:88-113) */
     float pad;
     double st_coef;  /* sigma / (2 lambda) of the pairwise model: npdm2 = st_coef / npd^2 */
+    /* the Gissler closure's constants for the split-precision form's FP32 evaluation */
+    float re_coef;   /* 2 L / mu_air: Re = re_coef rho_air |U|        */
+    float interp_fac, i_n_full, ycoef, L, CbL, A_sphere, A_plate;
+    float force_coef; /* gamma_air / sos^2                              */
+    float st_coef_f;  /* st_coef in FP32                                */
+    float we_coef;    /* L / sigma (0 without surface tension): We = we_coef rho_air |U|^2 */
+    float surf_h;     /* 1.33 dx, the surface test's offset (src/Geometry.cpp)       */
+    float lam_cutoff; /* lambda_nb below which the occlusion factor is computed      */
 };
 
 /* Everything a kernel reads that is constant over one launch. */

@@ -157,22 +157,51 @@ __device__ __forceinline__ void load_a16(const __nv_bfloat16 *X, uint32_t (&A)[1
     A[0][3] = X32[(g + 8) * 8 + 4 + t];
 }
 
+/* A hidden layer (K inputs -> N outputs) with GELU, straight into the next layer's A fragments:
+ * the output fragments are computed two at a time (one 16-wide k-tile of the next layer), so 8
+ * accumulators are live instead of N / 2 -- the same MMAs, bias, GELU and BF16 packing as
+ * `layer` followed by `gelu_to_a`, in fewer registers (the network runs inside the force kernel
+ * under its register budget).  The next fragment's weights are fetched one ahead. */
+template <int K, int N>
+__device__ __forceinline__ void layer_gelu(const uint32_t (&A)[K / 16][4], const __nv_bfloat16 *Wf, const float *bias,
+                                           uint32_t (&Aout)[N / 16][4]) {
+    constexpr int KS = K / 16, NT = N / 8;
+    const int lane = threadIdx.x & 31, t = lane & 3;
+    const uint32_t *base = reinterpret_cast<const uint32_t *>(Wf) + lane * (2 * KS);
+#pragma unroll
+    for (int ko = 0; ko < N / 16; ++ko) {
+        float C[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int nt = 2 * ko + h;
+            uint32_t b[2][2 * KS];
+            load_b<KS>(base + nt * 32 * (2 * KS), b[nt & 1]);
+            float b0, b1;
+            asm volatile("ld.global.nc.v2.f32 {%0,%1}, [%2];\n" : "=f"(b0), "=f"(b1) : "l"(bias + nt * 8 + 2 * t));
+            C[h][0] = b0;
+            C[h][1] = b1;
+            C[h][2] = b0;
+            C[h][3] = b1;
+#pragma unroll
+            for (int ks = 0; ks < KS; ++ks) mma16816(C[h], A[ks], b[nt & 1][2 * ks], b[nt & 1][2 * ks + 1]);
+        }
+        Aout[ko][0] = pack2(gelu(C[0][0]), gelu(C[0][1]));
+        Aout[ko][1] = pack2(gelu(C[0][2]), gelu(C[0][3]));
+        Aout[ko][2] = pack2(gelu(C[1][0]), gelu(C[1][1]));
+        Aout[ko][3] = pack2(gelu(C[1][2]), gelu(C[1][3]));
+    }
+}
+
 /* Forward pass of one 16-sample tile from its input A fragment (normalised, BF16); Y receives the
  * (un-normalised) 2 outputs of row g and g+8 for lanes with t == 0 (Y[0], Y[1] of row g; Y[2],
  * Y[3] of row g+8). */
 __device__ __forceinline__ void forward_frag(const DevMlp &M, const uint32_t (&A0)[1][4], float (&Y)[4]) {
-    float C1[kHid / 8][4];
-    layer<kInP, kHid>(A0, M.w + bW1, M.params + oB1, C1);
     uint32_t A1[kHid / 16][4];
-    gelu_to_a<kHid>(C1, A1);
-    float C2[kHid / 8][4];
-    layer<kHid, kHid>(A1, M.w + bW2, M.params + oB2, C2);
+    layer_gelu<kInP, kHid>(A0, M.w + bW1, M.params + oB1, A1);
     uint32_t A2[kHid / 16][4];
-    gelu_to_a<kHid>(C2, A2);
-    float C3[kHid / 8][4];
-    layer<kHid, kHid>(A2, M.w + bW3, M.params + oB3, C3);
+    layer_gelu<kHid, kHid>(A1, M.w + bW2, M.params + oB2, A2);
     uint32_t A3[kHid / 16][4];
-    gelu_to_a<kHid>(C3, A3);
+    layer_gelu<kHid, kHid>(A2, M.w + bW3, M.params + oB3, A3);
     float C4[1][4];
     layer<kHid, kOutP>(A3, M.w + bW4, M.params + oB4, C4);
     const float s0 = __ldg(M.params + oOutScale), s1 = __ldg(M.params + oOutScale + 1);

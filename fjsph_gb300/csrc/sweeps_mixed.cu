@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
     const Pf f = make_pf(P);
     Dissip<D> dis;
     if (DIS) dis.init(P, f, K, i);
-    const float h = (float)(1.33 * P.particle_step);
+    const float h = P.fc.surf_h;
     const float4 Ai = K.A[i];
     const LoParts Li(K.Lo[i]);
     const float4 Ni = K.N[i]; /* dSPH normal, lam_nb */
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
         }
     }
     const float lam_nb_i = K.N[i].w;
-    W.woccl[i] = to_f64((lam_nb_i < (float)P.lam_cutoff) ? fmaxf(0.f, fminf(woccl_, 1.f)) : 1.0f);
+    W.woccl[i] = to_f64((lam_nb_i < P.fc.lam_cutoff) ? fmaxf(0.f, fminf(woccl_, 1.f)) : 1.0f);
     K.O[i] = make_float4(o0, o1, o2, woccl_);
 #pragma unroll
     for (int k = 0; k < D; ++k) W.norm[k][i] = to_f64(ni[k]);
@@ -658,7 +658,7 @@ template <int D>
 __global__ void __launch_bounds__(kThreads) k_m_particle_shift(Params P, DevState W, DevNbr N, Packed K) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const float lam_nb = (float)W.lam_nb[i];
+    const float lam_nb = to_f32(W.lam_nb[i]);
     if (lam_nb < 0.55f || W.b[i] == FJSPH_BUFFER) {
 #pragma unroll
         for (int k = 0; k < D; ++k) W.vPert[k][i] = 0.0;
@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(kThreads) k_m_bound_ghost(Params P, DevState W
     /* boundary velocity: set this stage, read from the FP64 state */
     float vi[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) vi[k] = (float)W.v[k][i];
+    for (int k = 0; k < D; ++k) vi[k] = to_f32(W.v[k][i]);
     KSum Rr;
     int ni = 1;
     const SellList L = sell(N, i);
@@ -855,8 +855,8 @@ struct ResidAcc {
         csf = P.st_model == FJSPH_ST_CSF;
         npdm2 = 0.f;
         if (pairwise) {
-            const double npd = npd_dev[grp_of(P, i)];
-            npdm2 = (float)P.fc.st_coef / (float)(npd * npd);
+            const float npd = to_f32(npd_dev[grp_of(P, i)]);
+            npdm2 = P.fc.st_coef_f / (npd * npd);
         }
         pi3o4_H = P.fc.pi3o4_H;
         fac_bound = P.fc.fac_bound;
@@ -1063,8 +1063,9 @@ __device__ __forceinline__ void resid_slot(const Params &P, const DevState &W, c
 }
 
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, DevNbr N, Packed K, const double *npd_dev,
-                                                      Closure C) {
+__global__ void __launch_bounds__(kThreads, 7) k_m_resid(const __grid_constant__ Params P, const __grid_constant__ DevState W,
+                                                      const __grid_constant__ DevNbr N, const __grid_constant__ Packed K,
+                                                      const double *npd_dev, const __grid_constant__ Closure C) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     resid_slot<D, ALE, NOFROZEN>(P, W, N, K, npd_dev, C, i, i < P.n);
 }
@@ -1073,8 +1074,11 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid(Params P, DevState W, D
  * compiler contracts the particle body's products and sums into fused multiply-adds per copy,
  * so the two orders agree to FP32 rounding, not bit for bit. */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kThreads, 7) k_m_resid_sm(Params P, DevState W, DevNbr N, Packed K,
-                                                         const double *npd_dev, Closure C) {
+__global__ void __launch_bounds__(kThreads, 7) k_m_resid_sm(const __grid_constant__ Params P,
+                                                         const __grid_constant__ DevState W,
+                                                         const __grid_constant__ DevNbr N,
+                                                         const __grid_constant__ Packed K, const double *npd_dev,
+                                                         const __grid_constant__ Closure C) {
     const int64_t chunks = (P.n - P.nb + 31) / 32;
     for (int64_t c = claim_chunk(P.region_next, chunks); c >= 0; c = claim_chunk(P.region_next, chunks)) {
         const int64_t i = P.nb + 32 * c + (threadIdx.x & 31);
@@ -1086,8 +1090,10 @@ __global__ void __launch_bounds__(kThreads, 7) k_m_resid_sm(Params P, DevState W
  * and every lane walks one fluid particle's members with a cursor over its mask, the lanes of a
  * warp in step through the pair arithmetic. */
 template <int D, bool ALE, bool NOFROZEN>
-__global__ void __launch_bounds__(kTileThreads, 3) k_t_resid(Params P, DevState W, CellGrid G, TileDev T, Packed K,
-                                                              const double *npd_dev, Closure C) {
+__global__ void __launch_bounds__(kTileThreads, 3) k_t_resid(const __grid_constant__ Params P,
+                                                              const __grid_constant__ DevState W, CellGrid G, TileDev T,
+                                                              const __grid_constant__ Packed K, const double *npd_dev,
+                                                              const __grid_constant__ Closure C) {
     using TT = Tile<D>;
     extern __shared__ __align__(16) unsigned char tsm[];
     TileSmem ts = tile_smem<D>(tsm, T.smax, kStageRel);
