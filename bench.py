@@ -385,15 +385,6 @@ def resid_bytes_per_particle(s) -> int:
     return 8 * (r8 + w8) + 4 * 2
 
 
-# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
-# 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
-# the benchmark's particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed": (472.477e6 + 111.826e6) / 547_607}
-TRAFFIC_SOURCE = {"fp64": "ncu capture of k_resid on the 634k-particle static jet, scaled by fluid particles",
-                  "mixed": "ncu capture of k_m_resid (plain closure) on the 570k-particle live jet, scaled by "
-                           "fluid particles"}
-
-
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -401,13 +392,18 @@ def dist_env():
     return ws, rank, local
 
 
-# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture on the
-# 634k-particle jet (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to
-# the benchmark's particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed": (472.477e6 + 111.826e6) / 547_607}
+# DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to the benchmark's
+# particle count (traffic grows with the particle and pair counts).
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed": (469.264e6 + 55.326e6) / 547_607}
 TRAFFIC_SOURCE = {"fp64": "ncu capture of k_resid on the 634k-particle static jet, scaled by fluid particles",
-                  "mixed": "ncu capture of k_m_resid (plain closure) on the 570k-particle live jet, scaled by "
-                           "fluid particles"}
+                  "mixed": "ncu capture of k_m_resid (plain closure, grid order) on the 570k-particle live jet, "
+                           "scaled by fluid particles"}
+# Both fractions of the split-precision residual from the same capture (pct of peak, elapsed): the
+# memory side and the compute pipes, and the unit that binds.
+RESID_PIPES_MIXED = {"dram": 0.167, "l1tex": 0.713, "lts": 0.715, "fp32_fma": 0.323, "alu": 0.236, "xu": 0.136,
+                     "fp64": 0.123, "tensor": 0.0, "binding": "l1tex/lts: three 16-byte neighbour gathers per pair",
+                     "source": "ncu capture of k_m_resid (plain closure, grid order) on the 570k-particle live jet"}
 
 # Examples/VLM: a 22.3 m half-span, 8.5 m chord wing, sweep 32.5 deg, taper 0.6, 20 deg flap
 VLM_WING = dict(span=22.275, chord=8.491, panels_span=50, panels_chord=14, aoa_deg=5.0, sweep_deg=32.5, taper=0.6,
@@ -514,7 +510,8 @@ def roofline(s, prof, nf_mean: float, peaks: dict, learned: bool, tiles: bool = 
             "kernel": (("k_t_resid" if tiles else "k_m_resid") if s.precision == d.PREC_MIXED else "k_resid")
             + " (get_acc_and_Rrho)",
             "launch_ms": round(per_launch * 1e3, 3), "bytes_per_launch": round(bpp * nf_mean),
-            "bytes_per_particle": bpp, "peak_source": "measured" if not peaks.get("fallback") else "fallback"}
+            "bytes_per_particle": bpp, "peak_source": "measured" if not peaks.get("fallback") else "fallback",
+            "pipes_ncu": RESID_PIPES_MIXED if tkey == "mixed" else None}
 
 
 def run_ours(args, ws, rank, local):
