@@ -161,11 +161,13 @@ __device__ __forceinline__ void load_a16(const __nv_bfloat16 *X, uint32_t (&A)[1
  * the output fragments are computed two at a time (one 16-wide k-tile of the next layer), so 8
  * accumulators are live instead of N / 2 -- the same MMAs, bias, GELU and BF16 packing as
  * `layer` followed by `gelu_to_a`, in fewer registers (the network runs inside the force kernel
- * under its register budget).  The next fragment's weights are fetched one ahead. */
+ * under its register budget).  Each fragment's weights are fetched right before its MMAs: a
+ * fetch one fragment ahead measured slower here (its registers cost more spills than the
+ * latency it hides). */
 template <int K, int N>
 __device__ __forceinline__ void layer_gelu(const uint32_t (&A)[K / 16][4], const __nv_bfloat16 *Wf, const float *bias,
                                            uint32_t (&Aout)[N / 16][4]) {
-    constexpr int KS = K / 16, NT = N / 8;
+    constexpr int KS = K / 16;
     const int lane = threadIdx.x & 31, t = lane & 3;
     const uint32_t *base = reinterpret_cast<const uint32_t *>(Wf) + lane * (2 * KS);
 #pragma unroll
@@ -174,8 +176,8 @@ __device__ __forceinline__ void layer_gelu(const uint32_t (&A)[K / 16][4], const
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int nt = 2 * ko + h;
-            uint32_t b[2][2 * KS];
-            load_b<KS>(base + nt * 32 * (2 * KS), b[nt & 1]);
+            uint32_t b[2 * KS];
+            load_b<KS>(base + nt * 32 * (2 * KS), b);
             float b0, b1;
             asm volatile("ld.global.nc.v2.f32 {%0,%1}, [%2];\n" : "=f"(b0), "=f"(b1) : "l"(bias + nt * 8 + 2 * t));
             C[h][0] = b0;
@@ -183,7 +185,7 @@ __device__ __forceinline__ void layer_gelu(const uint32_t (&A)[K / 16][4], const
             C[h][2] = b0;
             C[h][3] = b1;
 #pragma unroll
-            for (int ks = 0; ks < KS; ++ks) mma16816(C[h], A[ks], b[nt & 1][2 * ks], b[nt & 1][2 * ks + 1]);
+            for (int ks = 0; ks < KS; ++ks) mma16816(C[h], A[ks], b[2 * ks], b[2 * ks + 1]);
         }
         Aout[ko][0] = pack2(gelu(C[0][0]), gelu(C[0][1]));
         Aout[ko][1] = pack2(gelu(C[0][2]), gelu(C[0][3]));
