@@ -96,6 +96,33 @@ def test_mixed_residual_on_oracle_state(name):
     _check(g, ref, ["acc"], ACC_TOL, slice(nb, None), f"{name} residual acceleration")
 
 
+@pytest.mark.parametrize("aero", [d.GISSLER, d.INDUCED_PRESSURE, d.SKIN_FRIC])
+def test_mixed_aero_closures(aero):
+    """The residual's aero force under each closure on the droplet, from the oracle's pre-pass
+    outputs: the Gissler closure runs in FP32 in this form, the other two in FP64 on the same
+    inputs; aero force and acceleration within the acceleration tolerance."""
+    c, st = _case("drop")
+    s = c.settings.copy()
+    s.acase = aero
+    c.settings = s
+    o = _oracle(c, st)
+    o.update_neighbours()
+    npd = o.dSPH_PreStep()
+    o.get_aero_velocity()
+    o.Detect_Surface()
+    o.dissipation_terms()
+    prepared = o.download()
+    o.get_acc_and_Rrho(npd)
+    ref = o.download()
+    assert np.any(ref.Af != 0.0), "the case exposes particles to the air"
+    ctx = _ctx(c, prepared, _mixed(s))
+    ctx.update_neighbours()
+    ctx.get_acc_and_Rrho(npd)
+    g = ctx.download()
+    _check(g, ref, ["Af", "acc"], ACC_TOL, slice(None), f"aero closure {aero}")
+    _check(g, ref, ["Rrho"], RRHO_TOL, slice(None), f"aero closure {aero}")
+
+
 @pytest.mark.parametrize("name", ["2d", "3d", "drop"])
 def test_mixed_prepasses(name):
     c, st = _case(name)
