@@ -182,6 +182,7 @@ struct fjsph_ctx {
     int32_t pair_mode = FJSPH_PAIRS_LISTS; /* FJSPH_PAIRS_*                               */
     int32_t sweep_order = FJSPH_ORDER_GRID; /* FJSPH_ORDER_*                              */
     int32_t *region_next = nullptr;         /* kMaxRegions chunk counters of the SM order */
+    ResidQuot *resid_q = nullptr;           /* FP64 residual: per-particle quotients      */
     bool tiles_valid = false;              /* the last search built the tile masks        */
     int64_t tiles_table = 0;               /* bucket table size the tile arrays fit       */
     /* mesh-cell air source */
@@ -1188,7 +1189,9 @@ int resid(fjsph_ctx *c, const Params &P) {
             c->judge_pending = true;
         }
     } else {
-        launch_resid(P, WS(c), make_nbr(c), npd_ptr(c), c->stream);
+        if (!c->resid_q) TRY(dalloc(c, &c->resid_q, c->cap));
+        launch_resid(P, WS(c), make_nbr(c), npd_ptr(c), c->resid_q, c->stream);
+        c->launches++;
     }
     return FJSPH_OK;
 }

@@ -232,7 +232,14 @@ void launch_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, 
 void launch_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, int32_t *near_inlet, cudaStream_t s);
 void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s);
 /* residual (src/Resid.cpp:426) over fluid slots */
-void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, cudaStream_t s);
+/* Per-particle quotients the FP64 residual's pair terms gather: m / rho, p / rho^2, 1 / rho (one
+ * 32-byte sector per neighbour) */
+struct __align__(32) ResidQuot {
+    double vol, pr, inv_rho, pad;
+};
+/* Q: scratch of the particle count */
+void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, ResidQuot *Q,
+                  cudaStream_t s);
 
 /* ---- sweeps_mixed.cu (FP32 split-precision form) ------------------------------------------ */
 void launch_m_pack(const Params &P, const DevState &W, const Packed &K, int64_t i0, int64_t i1, int full,

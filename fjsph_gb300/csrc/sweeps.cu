@@ -647,8 +647,26 @@ __global__ void k_bound_dbc(Params P, DevState W) {
 /* ------------------------------------------------------------------------------------------ */
 /* Residual (src/Resid.cpp:243-469, src/Kernel.h:153-269, src/Aero.h:10-263), fluid slots       */
 /* ------------------------------------------------------------------------------------------ */
+/* The per-particle quotients the residual's pair terms take from their neighbour: volume m / rho,
+ * p / rho^2 and 1 / rho, once per particle and launch instead of once per pair (on this GPU the
+ * FP64 form is bound by its FP64 pipe, and a divide is a long sequence on it). */
+__global__ void k_resid_quotients(Params P, DevState W, ResidQuot *Q) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const double rho = W.rho[i];
+    Q[i] = ResidQuot{W.m[i] / rho, W.p[i] / (rho * rho), 1.0 / rho, 0.0};
+}
+
+/* Wendland gradient scale of gradk_scale from q = r / H and c5 = 5 / H^2 */
+__device__ __forceinline__ double wendland_gscale(double q, double c5, double Wc) {
+    if (q < 1e-12) return 0.0;
+    const double b = 1.0 - 0.5 * q;
+    return c5 * (b * b * b) * Wc;
+}
+
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr N, const double *npd_dev) {
+__global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr N, const double *npd_dev,
+                                                    const ResidQuot *Q) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool cubic = has(P, FJSPH_VAR_CUBIC), ale = has(P, FJSPH_VAR_ALE), linear = has(P, FJSPH_VAR_LINEAR),
@@ -662,13 +680,14 @@ __global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr
                             (9.0 / 4.0 * (kPi * kPi * kPi) - 6.0 * kPi - 4.0));
         npdm2 = (0.5 * P.sig / lam) / (npd * npd);
     }
-    const double pi3o4 = 3.0 * kPi / 4.0;
+    /* uniform factors, once per thread: the pair loop multiplies instead of dividing */
+    const double inv_H = 1.0 / P.H, c5 = 5.0 / (P.H * P.H), pi3o4_H = 3.0 * kPi / 4.0 * inv_H;
     double xi[D], vi[D], vPi[D], gRi[D];
     load3<D>(W.x, i, xi);
     load3<D>(W.v, i, vi);
     if (ale) load3<D>(W.vPert, i, vPi);
     if (nofrozen) load3<D>(W.gradRho, i, gRi);
-    const double rho_i = W.rho[i], p_i = W.p[i], m_i = W.m[i];
+    const double rho_i = W.rho[i], p_i = W.p[i], m_i = W.m[i], inv_rho_i = Q[i].inv_rho;
     const int b_i = W.b[i], sz_i = W.surfzone[i];
     const int64_t pid_i = W.part_id[i];
     const int64_t e0 = N.off[i], e1 = N.off[i + 1];
@@ -709,26 +728,28 @@ __global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr
         const double rr = pair_rr<D>(N, i, j);
         const double r = sqrt(rr);
         const double idist2 = 1.0 / (rr + 0.001 * P.H_sq);
-        const double rho_j = W.rho[j], m_j = W.m[j], p_j = W.p[j];
+        const double rho_j = W.rho[j], m_j = W.m[j];
+        const ResidQuot qj = Q[j];
         const int b_j = W.b[j];
-        const double volj = m_j / rho_j;
-        const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
+        const double volj = qj.vol;
+        const double gs = cubic ? gradk_scale<double>(r, P.H, P.W_correc, true) : wendland_gscale(r * inv_H, c5, P.W_correc);
         double g[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) g[k] = Rji[k] * gs;
         /* pressure (PressureContrib, src/Resid.cpp:188-210) */
-        const double pc = linear ? (p_lin_i + p_j) * volj : m_j * (a_i + p_j / (rho_j * rho_j));
+        const double pc = linear ? (p_lin_i + W.p[j]) * volj : m_j * (a_i + qj.pr);
 #pragma unroll
         for (int k = 0; k < D; ++k) acc[k] -= pc * g[k];
         /* laminar viscosity (Morris), src/Kernel.h:262-269 */
         const double rg = dot<D, double>(Rji, g);
-        const double vc = m_j * (P.nu * (rho_i + rho_j) / (rho_i * rho_j) * rg * idist2);
+        /* (rho_i + rho_j) / (rho_i rho_j) = 1 / rho_i + 1 / rho_j */
+        const double vc = m_j * (P.nu * (inv_rho_i + qj.inv_rho) * rg * idist2);
 #pragma unroll
         for (int k = 0; k < D; ++k) visc[k] += vc * Vji[k];
         /* pairwise surface tension (Nair & Poeschel), src/Kernel.h:88-113 */
         if (st_on) {
             const double fac = (b_i == FJSPH_BOUND || b_j == FJSPH_BOUND) ? 1.0 + 0.5 * cos(0.5 * kPi * 7.0 / 9.0) : 1.0;
-            const double c = -npdm2 * fac * cos(pi3o4 * r / P.H) / r;
+            const double c = -npdm2 * fac * cos(pi3o4_H * r) / r;
 #pragma unroll
             for (int k = 0; k < D; ++k) st[k] += c * Rji[k];
         }
@@ -849,8 +870,10 @@ void launch_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, int
 void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s) {
     FJSPH_DISPATCH(P, k_bound_dbc, bound_grid(P), P, W);
 }
-void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, cudaStream_t s) {
-    FJSPH_DISPATCH(P, k_resid, fluid_grid(P), P, W, N, npd_dev);
+void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, ResidQuot *Q,
+                  cudaStream_t s) {
+    if (all_grid(P) > 0) k_resid_quotients<<<all_grid(P), kThreads, 0, s>>>(P, W, Q);
+    FJSPH_DISPATCH(P, k_resid, fluid_grid(P), P, W, N, npd_dev, Q);
 }
 
 } // namespace fjsph
