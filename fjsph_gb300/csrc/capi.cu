@@ -468,6 +468,14 @@ int alloc_packed(fjsph_ctx *c) {
     return FJSPH_OK;
 }
 
+/* The FP64 pair sweeps' per-particle quotients (ResidQuot), allocated with the first FP64 sweep;
+ * quot() after ensure_quot(). */
+int ensure_quot(fjsph_ctx *c) {
+    if (!c->resid_q) TRY(dalloc(c, &c->resid_q, c->cap));
+    return FJSPH_OK;
+}
+ResidQuot *quot(fjsph_ctx *c) { return c->resid_q; }
+
 void mark_full(fjsph_ctx *c) { c->dirty_full = true; }
 void mark_all(fjsph_ctx *c) { c->dirty_all = true; }
 void mark_bound(fjsph_ctx *c) { c->dirty_bound = true; }
@@ -983,7 +991,8 @@ int prestep_npd(fjsph_ctx *c, const Params &P) {
         ensure_pack(c);
         launch_m_dsph(P, WS(c), make_nbr(c), c->K, c->npd_part, c->stream);
     } else {
-        launch_dsph_prestep(P, WS(c), make_nbr(c), c->npd_part, c->stream);
+        TRY(ensure_quot(c));
+        launch_dsph_prestep(P, WS(c), make_nbr(c), c->npd_part, quot(c), c->stream);
     }
     return finish_npd(c);
 }
@@ -1048,21 +1057,25 @@ int prestep_passes(fjsph_ctx *c) {
             launch_m_surface(P, WS(c), N, c->K, dissipation, s);
             c->occ_valid = true;
         } else {
-            launch_detect_surface(P, WS(c), N, c->nrm_tmp, s);
+            TRY(ensure_quot(c));
+            launch_detect_surface(P, WS(c), N, c->nrm_tmp, quot(c), s);
         }
         c->launches += 3; /* plus the aero velocity pass, counted by aero_velocity */
     }
     if (dissipation && !mixed(c)) {
         Section sec(c, PASS_DISSIPATION);
-        launch_dissipation(P, WS(c), N, s);
+        TRY(ensure_quot(c));
+        launch_dissipation(P, WS(c), N, quot(c), s);
         c->launches++;
     }
     if (c->s.variant & FJSPH_VAR_ALE) {
         Section sec(c, PASS_SHIFT);
-        if (mixed(c))
+        if (mixed(c)) {
             launch_m_particle_shift(P, WS(c), N, c->K, s);
-        else
-            launch_particle_shift(P, WS(c), N, s);
+        } else {
+            TRY(ensure_quot(c));
+            launch_particle_shift(P, WS(c), N, quot(c), s);
+        }
         c->launches++;
     }
     {
@@ -1189,8 +1202,8 @@ int resid(fjsph_ctx *c, const Params &P) {
             c->judge_pending = true;
         }
     } else {
-        if (!c->resid_q) TRY(dalloc(c, &c->resid_q, c->cap));
-        launch_resid(P, WS(c), make_nbr(c), npd_ptr(c), c->resid_q, c->stream);
+        TRY(ensure_quot(c));
+        launch_resid(P, WS(c), make_nbr(c), npd_ptr(c), quot(c), c->stream);
         c->launches++;
     }
     return FJSPH_OK;
@@ -2232,7 +2245,8 @@ int fjsph_detect_surface(fjsph_ctx *c) {
         launch_m_surface(make_params(c), WS(c), make_nbr(c), c->K, false, c->stream);
         c->occ_valid = true;
     } else {
-        launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, c->stream);
+        TRY(ensure_quot(c));
+        launch_detect_surface(make_params(c), WS(c), make_nbr(c), c->nrm_tmp, quot(c), c->stream);
     }
     c->pn_equals_W = false;
     return sync(c);
@@ -2244,7 +2258,8 @@ int fjsph_dissipation_terms(fjsph_ctx *c) {
         ensure_pack(c);
         launch_m_dissipation(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
     } else {
-        launch_dissipation(make_params(c), WS(c), make_nbr(c), c->stream);
+        TRY(ensure_quot(c));
+        launch_dissipation(make_params(c), WS(c), make_nbr(c), quot(c), c->stream);
     }
     c->pn_equals_W = false;
     return sync(c);
@@ -2257,7 +2272,8 @@ int fjsph_particle_shift(fjsph_ctx *c) {
         ensure_pack(c);
         launch_m_particle_shift(make_params(c), WS(c), make_nbr(c), c->K, c->stream);
     } else {
-        launch_particle_shift(make_params(c), WS(c), make_nbr(c), c->stream);
+        TRY(ensure_quot(c));
+        launch_particle_shift(make_params(c), WS(c), make_nbr(c), quot(c), c->stream);
     }
     c->pn_equals_W = false;
     return sync(c);

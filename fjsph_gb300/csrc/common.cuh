@@ -253,10 +253,11 @@ __device__ __forceinline__ void normalized(const R *a, R *out) {
     }
 }
 
-/* (1 - q/2)^n for the Wendland C2 kernel, q = r/H. */
+/* (1 - q/2)^n for the Wendland C2 kernel, q = r/H, formed as r (1/H): the reciprocal is the same
+ * for every pair of a sweep, so the compiler forms it once per thread. */
 template <typename R>
 __device__ __forceinline__ R wend_base(R r, R H) {
-    return R(1) - R(0.5) * r / H;
+    return R(1) - R(0.5) * (r * (R(1) / H));
 }
 
 /* Kernel.h:37-45 / :11-21 */
@@ -273,7 +274,7 @@ __device__ __forceinline__ R kernel_w(R r, R H, R Wc, bool cubic) {
     }
     R b = wend_base(r, H);
     R b2 = b * b;
-    return b2 * b2 * (R(2) * r / H + R(1)) * Wc;
+    return b2 * b2 * (R(2) * (r * (R(1) / H)) + R(1)) * Wc;
 }
 
 /* Kernel.h:48-61 / :23-33: gradient = Rij * (returned scalar). */
@@ -285,7 +286,7 @@ __device__ __forceinline__ R gradk_scale(R r, R H, R Wc, bool cubic) {
         if (q < R(2)) return Wc * R(-0.75) * (R(2) - q) * (R(2) - q) / (r * H);
         return R(0);
     }
-    if (r / H < R(1e-12)) return R(0);
+    if (r * (R(1) / H) < R(1e-12)) return R(0);
     R b = wend_base(r, H);
     return R(5) / (H * H) * (b * b * b) * Wc;
 }

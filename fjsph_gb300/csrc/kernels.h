@@ -216,13 +216,21 @@ void launch_t_resid(const Params &P, const DevState &W, const CellGrid &G, const
                     const double *npd_dev, const Closure &C, cudaStream_t s);
 
 /* ---- sweeps.cu ---------------------------------------------------------------------------- */
-void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s);
+/* Per-particle quotients the FP64 pair sweeps gather from their neighbours instead of dividing per
+ * pair: m / rho, p / rho^2, 1 / rho and the artificial viscosity's sound speed sqrt(B gamma / rho)
+ * (one 32-byte sector per neighbour).  The FP64 sweep launchers that take Q (scratch of the particle
+ * count) fill it first. */
+struct __align__(32) ResidQuot {
+    double vol, pr, inv_rho, cs;
+};
+void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, ResidQuot *Q,
+                         cudaStream_t s);
 void launch_npd_only(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s);
 void launch_aero_velocity(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
 void launch_detect_surface(const Params &P, const DevState &W, const DevNbr &N, double *const nrm_tmp[3],
-                           cudaStream_t s);
-void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
-void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s);
+                           ResidQuot *Q, cudaStream_t s);
+void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, ResidQuot *Q, cudaStream_t s);
+void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, ResidQuot *Q, cudaStream_t s);
 /* kbits: the packed flags to keep current (null: the caller repacks) */
 void launch_pipe_outlet(const Params &P, const DevState &W, int32_t *kbits, cudaStream_t s);
 /* boundary passes over slots [0, nb) */
@@ -232,12 +240,7 @@ void launch_bound_pressure(const Params &P, const DevState &W, const DevNbr &N, 
 void launch_bound_ghost(const Params &P, const DevState &W, const DevNbr &N, int32_t *near_inlet, cudaStream_t s);
 void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s);
 /* residual (src/Resid.cpp:426) over fluid slots */
-/* Per-particle quotients the FP64 residual's pair terms gather: m / rho, p / rho^2, 1 / rho (one
- * 32-byte sector per neighbour) */
-struct __align__(32) ResidQuot {
-    double vol, pr, inv_rho, pad;
-};
-/* Q: scratch of the particle count */
+/* Q: scratch of the particle count, filled first */
 void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, ResidQuot *Q,
                   cudaStream_t s);
 

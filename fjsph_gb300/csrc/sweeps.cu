@@ -31,8 +31,20 @@ __device__ __forceinline__ double pair_rr(const DevNbr &N, int64_t i, int64_t j)
 /* ------------------------------------------------------------------------------------------ */
 /* dSPH_PreStep (src/Shifting.cpp:12-123), all slots                                            */
 /* ------------------------------------------------------------------------------------------ */
+/* The per-particle quotients the FP64 pair sweeps take from their neighbour (ResidQuot): m / rho,
+ * p / rho^2, 1 / rho and sqrt(B gamma / rho), once per particle and sweep instead of once per pair
+ * (on this GPU the FP64 form is bound by its FP64 pipe, and a divide or a square root is a long
+ * sequence on it).  Each is the expression the pair term evaluated, so the values are unchanged. */
+__global__ void k_resid_quotients(Params P, DevState W, ResidQuot *Q) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const double rho = W.rho[i];
+    Q[i] = ResidQuot{W.m[i] / rho, W.p[i] / (rho * rho), 1.0 / rho, sqrt((P.B * P.gam) / rho)};
+}
+
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_dsph_prestep(Params P, DevState W, DevNbr N, double *npd_part) {
+__global__ void __launch_bounds__(kThreads) k_dsph_prestep(Params P, DevState W, DevNbr N, double *npd_part,
+                                                            const ResidQuot *Q) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool cubic = has(P, FJSPH_VAR_CUBIC);
@@ -62,7 +74,7 @@ __global__ void __launch_bounds__(kThreads) k_dsph_prestep(Params P, DevState W,
 #pragma unroll
         for (int k = 0; k < D; ++k) Rji[k] = W.x[k][j] - xi[k];
         const double r = sqrt(pair_rr<D>(N, i, j));
-        const double volj = W.m[j] / W.rho[j];
+        const double volj = Q[j].vol;
         const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);
         const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
         double Grad[D];
@@ -162,7 +174,7 @@ __global__ void k_aero_velocity(Params P, DevState W, DevNbr N) {
 /* pass 1: surface flag (Marrone et al. 2010) and the eigenvalue-gradient normal */
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_surface_normal(Params P, DevState W, DevNbr N, double *nrm0,
-                                                              double *nrm1, double *nrm2) {
+                                                              double *nrm1, double *nrm2, const ResidQuot *Q) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     double *const nrm_tmp[3] = {nrm0, nrm1, nrm2};
@@ -235,7 +247,7 @@ __global__ void __launch_bounds__(kThreads) k_surface_normal(Params P, DevState 
 #pragma unroll
         for (int k = 0; k < D; ++k) Rij[k] = xi[k] - W.x[k][j];
         const double r = sqrt(pair_rr<D>(N, i, j));
-        const double volj = W.m[j] / W.rho[j];
+        const double volj = Q[j].vol;
         const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
         const double w = inside ? volj * (W.lam[j] - lam) : volj * W.lam[j];
 #pragma unroll
@@ -263,7 +275,8 @@ __global__ void __launch_bounds__(kThreads) k_surface_normal(Params P, DevState 
 /* pass 2: curvature from the normals and the Gissler occlusion factor */
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_surface_curvature(Params P, DevState W, DevNbr N, const double *nrm0,
-                                                                 const double *nrm1, const double *nrm2) {
+                                                                 const double *nrm1, const double *nrm2,
+                                                                 const ResidQuot *Q) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const double *const nt[3] = {nrm0, nrm1, nrm2};
@@ -295,7 +308,7 @@ __global__ void __launch_bounds__(kThreads) k_surface_curvature(Params P, DevSta
 #pragma unroll
         for (int k = 0; k < D; ++k) nj[k] = nt[k][j];
         if (nin > 0.0 && vnorm<D, double>(nj) > 0.0) {
-            const double volj = W.m[j] / W.rho[j];
+            const double volj = Q[j].vol;
             const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
             double s = 0.0;
 #pragma unroll
@@ -336,12 +349,13 @@ __global__ void k_surface_zone(Params P, DevState W, DevNbr N) {
 /* ------------------------------------------------------------------------------------------ */
 /* Artificial viscosity (src/Kernel.h:217-244): returns the scalar multiplying gradK.           */
 /* ------------------------------------------------------------------------------------------ */
+/* cs_i, cs_j: sqrt(B gamma / rho) of both particles (ResidQuot::cs) */
 __device__ __forceinline__ double art_visc_scale(const Params &P, double vdotr, double idist2, double rho_i,
-                                                 double rho_j) {
+                                                 double rho_j, double cs_i, double cs_j) {
     if (vdotr > 0.0) return 0.0;
     const double muij = P.H * vdotr * idist2;
     const double rhoij = 0.5 * (rho_i + rho_j);
-    const double cbar = 0.5 * (sqrt((P.B * P.gam) / rho_i) + sqrt((P.B * P.gam) / rho_j));
+    const double cbar = 0.5 * (cs_i + cs_j);
     return P.visc_alpha * cbar * muij / rhoij;
 }
 
@@ -349,7 +363,7 @@ __device__ __forceinline__ double art_visc_scale(const Params &P, double vdotr, 
 /* dissipation_terms (src/Shifting.cpp:126-186), fluid slots                                   */
 /* ------------------------------------------------------------------------------------------ */
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, DevNbr N) {
+__global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, DevNbr N, const ResidQuot *Q) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const bool cubic = has(P, FJSPH_VAR_CUBIC), linear = has(P, FJSPH_VAR_LINEAR), nodsph = has(P, FJSPH_VAR_NODSPH);
@@ -357,7 +371,7 @@ __global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, 
     load3<D>(W.x, i, xi);
     load3<D>(W.v, i, vi);
     load3<D>(W.gradRho, i, gRi);
-    const double rho_i = W.rho[i];
+    const double rho_i = W.rho[i], cs_i = Q[i].cs;
     double av[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) av[k] = 0.0;
@@ -376,7 +390,7 @@ __global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, 
         const double r = sqrt(rr);
         const double idist2 = 1.0 / (rr + 0.0001 * P.H_sq);
         const double rho_j = W.rho[j];
-        const double volj = W.m[j] / rho_j;
+        const double volj = Q[j].vol;
         const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
         double g[D];
 #pragma unroll
@@ -384,7 +398,8 @@ __global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, 
         const bool fl = W.b[j] > FJSPH_PISTON;
         if (fl) {
             const double vdotr = dot<D, double>(Vji, Rji);
-            const double c = linear ? volj * idist2 * vdotr : W.m[j] * art_visc_scale(P, vdotr, idist2, rho_i, rho_j);
+            const double c =
+                linear ? volj * idist2 * vdotr : W.m[j] * art_visc_scale(P, vdotr, idist2, rho_i, rho_j, cs_i, Q[j].cs);
 #pragma unroll
             for (int k = 0; k < D; ++k) av[k] += c * g[k];
         }
@@ -414,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_dissipation(Params P, DevState W, 
 /* particle_shift (src/Shifting.cpp:189-290, -DALE), fluid slots                               */
 /* ------------------------------------------------------------------------------------------ */
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_particle_shift(Params P, DevState W, DevNbr N) {
+__global__ void __launch_bounds__(kThreads) k_particle_shift(Params P, DevState W, DevNbr N, const ResidQuot *Q) {
     const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const double lam_nb = W.lam_nb[i];
@@ -444,7 +459,7 @@ __global__ void __launch_bounds__(kThreads) k_particle_shift(Params P, DevState 
             dv[k] = W.v[k][j] - vi[k];
         }
         const double r = sqrt(pair_rr<D>(N, i, j));
-        const double volj = W.m[j] / W.rho[j];
+        const double volj = Q[j].vol;
         const double kern = kernel_w<double>(r, P.H, P.W_correc, cubic);
         const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
         const double q = kern / P.W_dx;
@@ -647,16 +662,6 @@ __global__ void k_bound_dbc(Params P, DevState W) {
 /* ------------------------------------------------------------------------------------------ */
 /* Residual (src/Resid.cpp:243-469, src/Kernel.h:153-269, src/Aero.h:10-263), fluid slots       */
 /* ------------------------------------------------------------------------------------------ */
-/* The per-particle quotients the residual's pair terms take from their neighbour: volume m / rho,
- * p / rho^2 and 1 / rho, once per particle and launch instead of once per pair (on this GPU the
- * FP64 form is bound by its FP64 pipe, and a divide is a long sequence on it). */
-__global__ void k_resid_quotients(Params P, DevState W, ResidQuot *Q) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const double rho = W.rho[i];
-    Q[i] = ResidQuot{W.m[i] / rho, W.p[i] / (rho * rho), 1.0 / rho, 0.0};
-}
-
 /* Wendland gradient scale of gradk_scale from q = r / H and c5 = 5 / H^2 */
 __device__ __forceinline__ double wendland_gscale(double q, double c5, double Wc) {
     if (q < 1e-12) return 0.0;
@@ -785,7 +790,8 @@ __global__ void __launch_bounds__(kThreads) k_resid(Params P, DevState W, DevNbr
                     Rrho_d += volj * ((rho_j - rho_i) + 0.5 * dot<D, double>(gsum, Rji)) * rg * idist2;
                 }
                 const double vdotr = dot<D, double>(Vji, Rji);
-                const double c = linear ? volj * idist2 * vdotr : m_j * art_visc_scale(P, vdotr, idist2, rho_i, rho_j);
+                const double c = linear ? volj * idist2 * vdotr
+                                        : m_j * art_visc_scale(P, vdotr, idist2, rho_i, rho_j, Q[i].cs, qj.cs);
 #pragma unroll
                 for (int k = 0; k < D; ++k) art[k] += c * g[k];
             } else if (!nodsph) {
@@ -829,8 +835,15 @@ inline unsigned all_grid(const Params &P) { return grid_for(P.n, kThreads); }
             KERNEL<3><<<(GRID), kThreads, 0, s>>>(__VA_ARGS__);                           \
     } while (0)
 
-void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s) {
-    FJSPH_DISPATCH(P, k_dsph_prestep, all_grid(P), P, W, N, npd_part);
+/* the quotients of every particle, before a sweep that gathers them */
+inline void quotients(const Params &P, const DevState &W, ResidQuot *Q, cudaStream_t s) {
+    if (all_grid(P) > 0) k_resid_quotients<<<all_grid(P), kThreads, 0, s>>>(P, W, Q);
+}
+
+void launch_dsph_prestep(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, ResidQuot *Q,
+                         cudaStream_t s) {
+    quotients(P, W, Q, s);
+    FJSPH_DISPATCH(P, k_dsph_prestep, all_grid(P), P, W, N, npd_part, Q);
 }
 void launch_npd_only(const Params &P, const DevState &W, const DevNbr &N, double *npd_part, cudaStream_t s) {
     FJSPH_DISPATCH(P, k_npd_only, all_grid(P), P, W, N, npd_part);
@@ -839,17 +852,20 @@ void launch_aero_velocity(const Params &P, const DevState &W, const DevNbr &N, c
     FJSPH_DISPATCH(P, k_aero_velocity, fluid_grid(P), P, W, N);
 }
 void launch_detect_surface(const Params &P, const DevState &W, const DevNbr &N, double *const nrm_tmp[3],
-                           cudaStream_t s) {
-    FJSPH_DISPATCH(P, k_surface_normal, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2]);
-    FJSPH_DISPATCH(P, k_surface_curvature, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2]);
+                           ResidQuot *Q, cudaStream_t s) {
+    quotients(P, W, Q, s);
+    FJSPH_DISPATCH(P, k_surface_normal, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2], Q);
+    FJSPH_DISPATCH(P, k_surface_curvature, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2], Q);
     if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fluid_grid(P) > 0)
         k_surface_zone<<<fluid_grid(P), kThreads, 0, s>>>(P, W, N);
 }
-void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
-    FJSPH_DISPATCH(P, k_dissipation, fluid_grid(P), P, W, N);
+void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, ResidQuot *Q, cudaStream_t s) {
+    quotients(P, W, Q, s);
+    FJSPH_DISPATCH(P, k_dissipation, fluid_grid(P), P, W, N, Q);
 }
-void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, cudaStream_t s) {
-    FJSPH_DISPATCH(P, k_particle_shift, fluid_grid(P), P, W, N);
+void launch_particle_shift(const Params &P, const DevState &W, const DevNbr &N, ResidQuot *Q, cudaStream_t s) {
+    quotients(P, W, Q, s);
+    FJSPH_DISPATCH(P, k_particle_shift, fluid_grid(P), P, W, N, Q);
 }
 void launch_pipe_outlet(const Params &P, const DevState &W, int32_t *kbits, cudaStream_t s) {
     FJSPH_DISPATCH(P, k_pipe_outlet, fluid_grid(P), P, W, kbits);
@@ -872,7 +888,7 @@ void launch_bound_dbc(const Params &P, const DevState &W, cudaStream_t s) {
 }
 void launch_resid(const Params &P, const DevState &W, const DevNbr &N, const double *npd_dev, ResidQuot *Q,
                   cudaStream_t s) {
-    if (all_grid(P) > 0) k_resid_quotients<<<all_grid(P), kThreads, 0, s>>>(P, W, Q);
+    quotients(P, W, Q, s);
     FJSPH_DISPATCH(P, k_resid, fluid_grid(P), P, W, N, npd_dev, Q);
 }
 
