@@ -396,8 +396,9 @@ def dist_env():
 # DRAM bytes (read + write) per fluid particle of one residual launch, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum / fluid particles); scaled to the benchmark's
 # particle count (traffic grows with the particle and pair counts).
-RESID_TRAFFIC_PER_PARTICLE = {"fp64": 349.1e6 / 592_026, "mixed": (469.264e6 + 55.326e6) / 547_607}
-TRAFFIC_SOURCE = {"fp64": "ncu capture of k_resid on the 634k-particle static jet, scaled by fluid particles",
+RESID_TRAFFIC_PER_PARTICLE = {"fp64": 42.100e9 * 7.8264e-3 / 547_607, "mixed": (469.264e6 + 55.326e6) / 547_607}
+TRAFFIC_SOURCE = {"fp64": "ncu capture of k_resid on the 570k-particle live jet (dram__bytes.sum.per_second x "
+                          "gpu__time_duration.sum), scaled by fluid particles",
                   "mixed": "ncu capture of k_m_resid (plain closure, grid order) on the 570k-particle live jet, "
                            "scaled by fluid particles"}
 # Both fractions of the split-precision residual from the same capture (pct of peak, elapsed): the
