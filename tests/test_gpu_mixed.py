@@ -14,7 +14,8 @@ import pytest
 
 from fjsph_gb300 import _cdefs as d
 from tests._util import assert_ints, n_bound, rel_rms
-from tests.test_gpu_parity import _case
+from fjsph_gb300.settings import derive
+from tests.test_gpu_parity import VARIANTS, _case
 
 pytestmark = pytest.mark.gpu
 
@@ -95,6 +96,40 @@ def test_mixed_residual_on_oracle_state(name):
     nb = n_bound(c.blocks)
     _check(g, ref, ["Rrho"], RRHO_TOL, slice(nb, None), f"{name} residual density rate")
     _check(g, ref, ["acc"], ACC_TOL, slice(nb, None), f"{name} residual acceleration")
+
+
+@pytest.mark.parametrize("label,over", VARIANTS, ids=[v[0] for v in VARIANTS])
+def test_mixed_variant_residual(label, over):
+    """The residual under each build-flag variant the FP64 form is checked on (linear pressure,
+    inline artificial viscosity, no delta-SPH, TIC, cubic spline, ALE with TIC, CSF and pairwise
+    surface tension, isothermal EOS), from the oracle's pre-pass outputs on the 2D case."""
+    c, st = _case("2d")
+    s = c.settings.copy()
+    for k, v in over.items():
+        setattr(s, k, v)
+    if s.st_model != d.ST_NOST:
+        s.sig = 0.0728
+    derive(s)
+    c.settings = s
+    o = _oracle(c, st)
+    o.update_neighbours()
+    npd = o.dSPH_PreStep()
+    o.get_aero_velocity()
+    o.Detect_Surface()
+    o.dissipation_terms()
+    if s.variant & d.VAR_ALE:
+        o.particle_shift()
+    o.Get_Boundary_Pressure()
+    prepared = o.download()
+    o.get_acc_and_Rrho(npd)
+    ref = o.download()
+    ctx = _ctx(c, prepared, _mixed(s))
+    ctx.update_neighbours()
+    ctx.get_acc_and_Rrho(npd)
+    g = ctx.download()
+    nb = n_bound(c.blocks)
+    _check(g, ref, ["Rrho"], RRHO_TOL, slice(nb, None), f"{label} residual density rate")
+    _check(g, ref, ["acc"], ACC_TOL, slice(nb, None), f"{label} residual acceleration")
 
 
 @pytest.mark.parametrize("aero", [d.GISSLER, d.INDUCED_PRESSURE, d.SKIN_FRIC])
