@@ -13,7 +13,8 @@ import numpy as np
 import pytest
 
 from fjsph_gb300 import _cdefs as d
-from tests._util import assert_ints, n_bound, rel_rms
+from fjsph_gb300 import cases
+from tests._util import assert_ints, n_bound, perturb, rel_rms
 from fjsph_gb300.settings import derive
 from tests.test_gpu_parity import VARIANTS, _case
 
@@ -96,6 +97,52 @@ def test_mixed_residual_on_oracle_state(name):
     nb = n_bound(c.blocks)
     _check(g, ref, ["Rrho"], RRHO_TOL, slice(nb, None), f"{name} residual density rate")
     _check(g, ref, ["acc"], ACC_TOL, slice(nb, None), f"{name} residual acceleration")
+
+
+@pytest.mark.parametrize("solver", [d.PRESSURE_G, d.GHOST, d.DBC])
+def test_mixed_boundary_solvers(solver):
+    """The boundary passes of the split-precision form from the oracle's pre-pass outputs (2D dam
+    break, perturbed, no-slip walls): the no-slip mirror velocities (FP64 in both forms) to 1e-12,
+    the pressure-gradient solver's wall pressure and density, the ghost solver's wall density rate
+    (with the same near-inlet flags) and the DBC accelerations within the pre-pass tolerance."""
+    c = cases.dam_break_2d(dx=0.04)
+    for b in c.blocks:
+        if not b.is_fluid:
+            b.bound_solver = solver
+            b.no_slip = 1
+    nb = n_bound(c.blocks)
+    st = perturb(c.state, 4, 0.3, 0.002, nb)
+    o = _oracle(c, st)
+    o.update_neighbours()
+    o.dSPH_PreStep()
+    o.get_aero_velocity()
+    o.Detect_Surface()
+    o.dissipation_terms()
+    prepared = o.download()
+    ctx = _ctx(c, prepared, _mixed(c.settings))
+    ctx.update_neighbours()
+    res = []
+    for h in (ctx, o):
+        h.Set_No_Slip()
+        if solver == d.PRESSURE_G:
+            h.Get_Boundary_Pressure()
+            ni = None
+        elif solver == d.GHOST:
+            ni = h.Boundary_Ghost()
+        else:
+            h.Boundary_DBC()
+            ni = None
+        res.append((ni, h.download()))
+    (n1, g), (n2, r) = res
+    walls = slice(0, nb)
+    _check(g, r, ["v"], 1e-12, walls, "Set_No_Slip")
+    if solver == d.PRESSURE_G:
+        _check(g, r, ["p", "rho"], PASS_TOL, walls, "Get_Boundary_Pressure")
+    elif solver == d.GHOST:
+        np.testing.assert_array_equal(n1, n2)
+        _check(g, r, ["Rrho"], PASS_TOL, walls, "Boundary_Ghost")
+    else:
+        _check(g, r, ["acc"], PASS_TOL, walls, "Boundary_DBC")
 
 
 @pytest.mark.parametrize("label,over", VARIANTS, ids=[v[0] for v in VARIANTS])
