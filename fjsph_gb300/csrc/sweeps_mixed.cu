@@ -1288,10 +1288,10 @@ void launch_m_resid(const Params &P, const DevState &W, const DevNbr &N, const P
 template <int D, bool A, bool NF>
 void t_resid_launch(const Params &P, const DevState &W, const CellGrid &G, const TileDev &T, const Packed &K,
                     const double *npd_dev, const Closure &C, cudaStream_t s) {
-    const size_t sm = tile_smem_bytes<D>(T.smax, kStageRel);
-    static bool attr = false;
-    static unsigned grid = 0;
-    if (!attr) {
+    const size_t sm = tile_smem_bytes<D>(T.smax, kStageRel); /* smax is fixed for a context */
+    /* the shared-memory attribute and the resident grid, set once per instantiation (a function-local
+     * static is initialised exactly once, whichever host thread gets here first) */
+    static const unsigned grid = [sm] {
         if (sm > 48 * 1024)
             cudaFuncSetAttribute(k_t_resid<D, A, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         int dev = 0, sms = 1, per = 1;
@@ -1300,9 +1300,8 @@ void t_resid_launch(const Params &P, const DevState &W, const CellGrid &G, const
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_t_resid<D, A, NF>, kTileThreads, sm) != cudaSuccess ||
             per < 1)
             per = 1;
-        grid = (unsigned)(sms * per);
-        attr = true;
-    }
+        return (unsigned)(sms * per);
+    }();
     k_t_resid<D, A, NF><<<grid, kTileThreads, sm, s>>>(P, W, G, T, K, npd_dev, C);
 }
 
