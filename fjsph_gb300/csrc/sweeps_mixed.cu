@@ -446,14 +446,17 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
     const float lam_nb = Ni.w, lam = K.G[i].w;
     const SellList L = sell(N, i);
     int surf = W.surf[i];
+    /* the geometric test of the surface band runs inside the normal's walk below: a neighbour
+     * inside the test region clears the flag, and once it is clear the test is skipped (the
+     * flag a walk that stops at the first such neighbour would give) */
+    bool test = false;
+    float th[D];
     if (b < FJSPH_PIPE) {
         surf = 0;
         W.woccl[i] = 1.0;
     } else if (lam_nb < 0.2f) {
         surf = 1;
     } else if (lam_nb < 0.75f) {
-        /* x_j - pointT = (x_j - x_i) - h n_hat */
-        float th[D];
         if (D == 2) {
             float tau[D];
             tau[0] = ni[1];
@@ -461,42 +464,11 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
             fnormalized<D>(tau, th);
         }
         surf = 1;
-        const float sq2h = sqrtf(2.f) * h;
-        for (int32_t e = 0; e < L.n; ++e) {
-            const int2 pe = L[e];
-        const int32_t j = pe.x;
-            if (j == i) continue;
-            float Rji[D], xT[D];
-            sepx<D>(Ai, Li, K.A[j], LoParts(K.Lo[j]), Rji);
-#pragma unroll
-            for (int k = 0; k < D; ++k) xT[k] = Rji[k] - h * nh[k];
-            const float r = sqrtf(__int_as_float(pe.y));
-            if (r >= sq2h) {
-                if (sqrtf(fdot<D>(xT, xT)) < h) {
-                    surf = 0;
-                    break;
-                }
-            } else if (D == 2) {
-                if (fabsf(fdot<D>(nh, xT)) + fabsf(fdot<D>(th, xT)) < h) {
-                    surf = 0;
-                    break;
-                }
-            } else {
-                float u[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) u[k] = Rji[k] / r;
-                /* acos(c) < pi/4  <=>  c > cos(pi/4) (acos decreases on [-1, 1]) */
-                if (fdot<D>(nh, u) > 0.70710678118654752f) {
-                    surf = 0;
-                    break;
-                }
-            }
-        }
+        test = true;
     } else {
         surf = 0;
     }
-    W.surf[i] = surf;
-    K.bits[i] = (K.bits[i] & ~8) | (surf << 3);
+    const float sq2h = sqrtf(2.f) * h;
     float nrm[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) nrm[k] = 0.f;
@@ -511,6 +483,23 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         sepx<D>(Ai, Li, Aj, Lj, Rji);
         const float rr = __int_as_float(pe.y);
         const float r = sqrtf(rr);
+        if (test && surf) {
+            /* x_j - pointT = (x_j - x_i) - h n_hat */
+            float xT[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) xT[k] = Rji[k] - h * nh[k];
+            if (r >= sq2h) {
+                if (sqrtf(fdot<D>(xT, xT)) < h) surf = 0;
+            } else if (D == 2) {
+                if (fabsf(fdot<D>(nh, xT)) + fabsf(fdot<D>(th, xT)) < h) surf = 0;
+            } else {
+                float u[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) u[k] = Rji[k] / r;
+                /* acos(c) < pi/4  <=>  c > cos(pi/4) (acos decreases on [-1, 1]) */
+                if (fdot<D>(nh, u) > 0.70710678118654752f) surf = 0;
+            }
+        }
         const float volj = Aj.w;
         const float gs = f_gscale(f, r);
         const float4 Gj = K.G[j];
@@ -522,6 +511,8 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_normal(Params P, DevStat
         if (DIS) dis.add(f, K, j, Lj, Rji, rr, gs, volj, Gj);
     }
     if (DIS) dis.finish(P, W, i);
+    W.surf[i] = surf;
+    K.bits[i] = (K.bits[i] & ~8) | (surf << 3);
     float Lf[D * D], n2[D];
     load_lf<D>(K, i, Lf);
 #pragma unroll
