@@ -187,54 +187,27 @@ __global__ void __launch_bounds__(kThreads) k_surface_normal(Params P, DevState 
     const int b = W.b[i];
     const double lam_nb = W.lam_nb[i], lam = W.lam[i];
     const int64_t e0 = N.off[i], e1 = N.off[i + 1];
+    /* the geometric test of the surface band runs inside the normal's walk below: a neighbour
+     * inside the test region clears the flag, and once it is clear the test is skipped (the flag
+     * a walk that stops at the first such neighbour gives, src/Geometry.cpp) */
+    int surf = 0;
+    bool test = false;
+    double pointT[D], th[D];
     if (b < FJSPH_PIPE) {
-        W.surf[i] = 0;
         W.woccl[i] = 1.0;
     } else if (lam_nb < 0.2) {
-        W.surf[i] = 1;
+        surf = 1;
     } else if (lam_nb < 0.75) {
-        double pointT[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) pointT[k] = xi[k] + h * nh[k];
-        double th[D];
         if (D == 2) {
             double tau[D];
             tau[0] = ni[1];
             tau[1] = -ni[0];
             normalized<D, double>(tau, th);
         }
-        int surf = 1;
-        for (int64_t e = e0; e < e1; ++e) {
-            const int64_t j = N.idx[e];
-            if (j == i) continue;
-            double xj[D], x_jT[D];
-            load3<D>(W.x, j, xj);
-#pragma unroll
-            for (int k = 0; k < D; ++k) x_jT[k] = xj[k] - pointT[k];
-            const double r = sqrt(pair_rr<D>(N, i, j));
-            if (r >= sqrt(2.0) * h) {
-                if (vnorm<D, double>(x_jT) < h) {
-                    surf = 0;
-                    break;
-                }
-            } else if (D == 2) {
-                if ((fabs(dot<D, double>(nh, x_jT)) + fabs(dot<D, double>(th, x_jT))) < h) {
-                    surf = 0;
-                    break;
-                }
-            } else {
-                double u[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) u[k] = -(xi[k] - xj[k]) / r;
-                if (acos(dot<D, double>(nh, u)) < kPi / 4.0) {
-                    surf = 0;
-                    break;
-                }
-            }
-        }
-        W.surf[i] = surf;
-    } else {
-        W.surf[i] = 0;
+        surf = 1;
+        test = true;
     }
     double nrm[D];
 #pragma unroll
@@ -243,16 +216,33 @@ __global__ void __launch_bounds__(kThreads) k_surface_normal(Params P, DevState 
     for (int64_t e = e0; e < e1; ++e) {
         const int64_t j = N.idx[e];
         if (j == i) continue;
-        double Rij[D];
+        double xj[D], Rij[D];
+        load3<D>(W.x, j, xj);
 #pragma unroll
-        for (int k = 0; k < D; ++k) Rij[k] = xi[k] - W.x[k][j];
+        for (int k = 0; k < D; ++k) Rij[k] = xi[k] - xj[k];
         const double r = sqrt(pair_rr<D>(N, i, j));
+        if (test && surf) {
+            double x_jT[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) x_jT[k] = xj[k] - pointT[k];
+            if (r >= sqrt(2.0) * h) {
+                if (vnorm<D, double>(x_jT) < h) surf = 0;
+            } else if (D == 2) {
+                if ((fabs(dot<D, double>(nh, x_jT)) + fabs(dot<D, double>(th, x_jT))) < h) surf = 0;
+            } else {
+                double u[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) u[k] = -(xi[k] - xj[k]) / r;
+                if (acos(dot<D, double>(nh, u)) < kPi / 4.0) surf = 0;
+            }
+        }
         const double volj = Q[j].vol;
         const double gs = gradk_scale<double>(r, P.H, P.W_correc, cubic);
         const double w = inside ? volj * (W.lam[j] - lam) : volj * W.lam[j];
 #pragma unroll
         for (int k = 0; k < D; ++k) nrm[k] += w * (Rij[k] * gs);
     }
+    W.surf[i] = surf;
     double n2[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
@@ -296,9 +286,13 @@ __global__ void __launch_bounds__(kThreads) k_surface_curvature(Params P, DevSta
     for (int k = 0; k < D * D; ++k) Li[k] = W.L[k][i];
     const double nin = vnorm<D, double>(ni), vdn = vnorm<D, double>(Vdiff);
     double curve = 0.0, woccl_ = 0.0;
+    /* ALE/TIC builds: the surface zone (any neighbour, self included, on the surface) rides along */
+    const bool zone = has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC);
+    int sz = 0;
     const int64_t e0 = N.off[i], e1 = N.off[i + 1];
     for (int64_t e = e0; e < e1; ++e) {
         const int64_t j = N.idx[e];
+        if (zone && !sz && W.surf[j] == 1) sz = 1;
         if (j == i) continue;
         double Rij[D];
 #pragma unroll
@@ -331,19 +325,7 @@ __global__ void __launch_bounds__(kThreads) k_surface_curvature(Params P, DevSta
     W.curve[i] = curve;
     W.norm_curve[i] = P.dx * curve;
     W.pDist[i] = W.lam[i];
-}
-
-/* pass 3 (ALE/TIC builds): surface zone = any neighbour (self included) on the surface */
-__global__ void k_surface_zone(Params P, DevState W, DevNbr N) {
-    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    int sz = 0;
-    for (int64_t e = N.off[i]; e < N.off[i + 1]; ++e)
-        if (W.surf[N.idx[e]] == 1) {
-            sz = 1;
-            break;
-        }
-    W.surfzone[i] = sz;
+    if (zone) W.surfzone[i] = sz;
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -856,8 +838,6 @@ void launch_detect_surface(const Params &P, const DevState &W, const DevNbr &N, 
     quotients(P, W, Q, s);
     FJSPH_DISPATCH(P, k_surface_normal, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2], Q);
     FJSPH_DISPATCH(P, k_surface_curvature, fluid_grid(P), P, W, N, nrm_tmp[0], nrm_tmp[1], nrm_tmp[2], Q);
-    if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fluid_grid(P) > 0)
-        k_surface_zone<<<fluid_grid(P), kThreads, 0, s>>>(P, W, N);
 }
 void launch_dissipation(const Params &P, const DevState &W, const DevNbr &N, ResidQuot *Q, cudaStream_t s) {
     quotients(P, W, Q, s);

@@ -554,10 +554,14 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     load_lf<D>(K, i, Li);
     const float nin = sqrtf(fdot<D>(ni, ni)), vdn = sqrtf(fdot<D>(Vdiff, Vdiff));
     float curve = 0.f, woccl_ = 0.f, o0 = 0.f, o1 = 0.f, o2 = 0.f;
+    /* ALE/TIC builds: the surface zone (any neighbour, self included, on the surface) rides along */
+    const bool zone = has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC);
+    int sz = 0;
     const SellList L = sell(N, i);
     for (int32_t e = 0; e < L.n; ++e) {
         const int2 pe = L[e];
         const int32_t j = pe.x;
+        if (zone && !sz && bits_surf(K.bits[j])) sz = 1;
         if (j == i) continue;
         float Rij[D]; /* = x_j - x_i, the reference's naming in this loop */
         sepx<D>(Ai, Qi, K.A[j], LoParts(K.Lo[j]), Rij);
@@ -601,21 +605,11 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
     W.norm_curve[i] = P.dx * curve_d;
     W.pDist[i] = W.lam[i];
     K.N[i] = make_float4(ni[0], ni[1], D == 3 ? ni[2] : 0.f, lam_nb_i);
-}
-
-__global__ void k_m_surface_zone(Params P, DevState W, DevNbr N, Packed K) {
-    const int64_t i = P.nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    int sz = 0;
-    const SellList L = sell(N, i);
-    for (int32_t e = 0; e < L.n; ++e)
-        if (bits_surf(K.bits[L[e].x])) {
-            sz = 1;
-            break;
-        }
-    W.surfzone[i] = sz;
-    atomicAnd(&K.bits[i], ~16);
-    if (sz) atomicOr(&K.bits[i], 16);
+    if (zone) { /* bit 4 of the own record; the other threads read only bit 3 of it */
+        W.surfzone[i] = sz;
+        atomicAnd(&K.bits[i], ~16);
+        if (sz) atomicOr(&K.bits[i], 16);
+    }
 }
 
 template <int D>
@@ -1209,8 +1203,6 @@ void launch_m_surface(const Params &P, const DevState &W, const DevNbr &N, const
         }
     }
     FJSPH_DISPATCH_M(P, k_m_surface_curvature, fgrid(P), P, W, N, K);
-    if ((has(P, FJSPH_VAR_ALE) || has(P, FJSPH_VAR_TIC)) && fgrid(P) > 0)
-        k_m_surface_zone<<<fgrid(P), sweep_bs(P), 0, s>>>(P, W, N, K);
 }
 void launch_m_dissipation(const Params &P, const DevState &W, const DevNbr &N, const Packed &K, cudaStream_t s) {
     FJSPH_DISPATCH_M(P, k_m_dissipation, fgrid(P), P, W, N, K);
