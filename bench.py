@@ -593,12 +593,10 @@ def run_ours(args, ws, rank, local):
         for _ in range(args.e2e_steps):
             n = ctx.particle_count()
             st = prefix_state(host, n)
-            ctx.upload(d.BOTH, st, fields=STEP_FIELDS)  # pn = pnp1 at a step's start
-            ctx.integrate()
-            st2 = prefix_state(host, ctx.particle_count())
-            ctx.download(d.PNP1, fields=STEP_FIELDS, out=st2)
+            # fjsph_step_host: pn = pnp1 = st, one step, pnp1 back into the same pinned arrays
+            n2 = ctx.step_host(st, host, fields=STEP_FIELDS)
             h2d += state_bytes(st, STEP_FIELDS)
-            d2h += state_bytes(st2, STEP_FIELDS)
+            d2h += state_bytes(prefix_state(host, n2), STEP_FIELDS)
             ps_e += n - nb
         ctx.event_record(3)
         e2e_ms = ctx.event_elapsed(2, 3)
@@ -607,7 +605,9 @@ def run_ours(args, ws, rank, local):
         e2e = {"value": ps_e * ws / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
                "pinned": host._pinned,
-               "fields": "FJSPH_STEP_FIELDS (the state a step reads; the rest is recomputed inside it)"}
+               "fields": "FJSPH_STEP_FIELDS (the state a step reads; the rest is recomputed inside it)",
+               "call": "fjsph_step_host: upload as pn and pnp1, one step, download; the fields a step first "
+                       "reads after its first neighbour search travel while that search runs"}
     ctx.close()
 
     def other_form(settings, steps):

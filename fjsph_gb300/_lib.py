@@ -54,6 +54,7 @@ PROTOTYPES = {
     "fjsph_newmark_beta": (C.c_int, [_P, C.c_double, _dp, _i32p, _dp]),
     "fjsph_integrate_no_update": (C.c_int, [_P, _dp]),
     "fjsph_integrate": (C.c_int, [_P, _dp]),
+    "fjsph_step_host": (C.c_int, [_P, C.POINTER(d.StateView), C.POINTER(d.StateView), _dp]),
     "fjsph_integrate_n": (C.c_int, [_P, _i32, _dp]),
     "fjsph_step_report": (C.c_int, [_P, _dp]),
     "fjsph_timestep_maxima": (C.c_int, [_P, _dp]),

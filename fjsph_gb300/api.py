@@ -199,6 +199,16 @@ class Context:
         check("fjsph_integrate", self._lib.fjsph_integrate(self._h, C.byref(r)))
         return r.value
 
+    def step_host(self, st_in: SPHState, out: SPHState, fields=None) -> int:
+        """One step on a host state: upload st_in as pn and pnp1, integrate, download pnp1 into
+        `out` (fields: names to transfer both ways, None = all; out's arrays must hold the
+        particle count after the step).  Returns the particle count after the step."""
+        vi = st_in.view(fields)
+        vo = out.view(fields)
+        r = C.c_double()
+        check("fjsph_step_host", self._lib.fjsph_step_host(self._h, C.byref(vi), C.byref(vo), C.byref(r)))
+        return int(vo.n)
+
     def integrate_n(self, n_steps: int) -> float:
         r = C.c_double()
         check("fjsph_integrate_n", self._lib.fjsph_integrate_n(self._h, int(n_steps), C.byref(r)))

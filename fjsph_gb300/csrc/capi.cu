@@ -119,6 +119,29 @@ struct fjsph_ctx {
     double *stage2 = nullptr;  /* second staging buffer: field f + 1 moves while field f is gathered */
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t st_copied[2] = {nullptr, nullptr}, st_used[2] = {nullptr, nullptr};
+    /* fjsph_step_host: fields in flight on the copy stream while the step runs its first search
+     * (view_ptrs index, offset in late_stage in doubles, host array, bytes), sent by send_late
+     * and applied by apply_late */
+    struct LateField {
+        int f;
+        int64_t off;
+        const void *host;
+        size_t bytes;
+    };
+    std::vector<LateField> late;
+    bool late_sent = false;
+    double *late_stage = nullptr;
+    int64_t late_cap = 0;
+    cudaEvent_t late_ev = nullptr;
+    /* fjsph_step_host: fields final after the second search's pre-passes, copied out while the
+     * remaining stages run (offset in out_stage, host array, bytes); out_sent: the copies went
+     * out for out_n particles */
+    std::vector<LateField> early_out;
+    bool out_sent = false;
+    int64_t out_n = 0;
+    double *out_stage = nullptr;
+    int64_t out_cap = 0;
+    cudaEvent_t out_ready = nullptr;
     DevScalars *dsc = nullptr; /* device */
     DevScalars *hsc = nullptr; /* pinned host mirror */
 
@@ -718,8 +741,110 @@ int transfer(fjsph_ctx *c, DevState &S, const fjsph_state_view *v, bool up, DevS
     return sync(c);
 }
 
+/* bytes per particle of field f (view_ptrs order) */
+int64_t es_bytes_of(fjsph_ctx *c, int f) {
+    std::vector<std::vector<void *>> dp;
+    std::vector<int> type;
+    dev_ptrs(WS(c), c->D, dp, type);
+    return (int64_t)(type[f] == 2 ? 4 : 8) * (int64_t)dp[f].size();
+}
+
+/* The fields a step first reads after its first search and the npd pass behind it (view_ptrs
+ * order): the frozen dissipation terms, the air cell values, the previous surface detection and
+ * the particle id and cell.  The time-step reduction, the search and the packing read only the
+ * others. */
+bool late_field(size_t f) {
+    static const int kLate[] = {4 /* aVisc */, 5 /* cellV */, 7 /* norm */, 15 /* norm_curve */,
+                                16 /* woccl */, 18 /* deltaD */, 19 /* cellP */, 20 /* cellRho */,
+                                23 /* lam */, 24 /* lam_nb */, 26 /* part_id */, 27 /* cellID */};
+    for (int k : kLate)
+        if ((size_t)k == f) return true;
+    return false;
+}
+
+/* The late fields' host-to-device copies of fjsph_step_host.  Sent after the time-step
+ * reduction has read its maxima back: a device-to-host read-back issued behind them could wait
+ * for them on the copy engine. */
+int send_late(fjsph_ctx *c) {
+    if (c->late.empty() || c->late_sent) return FJSPH_OK;
+    for (const auto &L : c->late)
+        CU(cudaMemcpyAsync(c->late_stage + L.off, L.host, L.bytes, cudaMemcpyHostToDevice, c->copy_stream));
+    CU(cudaEventRecord(c->late_ev, c->copy_stream));
+    c->late_sent = true;
+    return FJSPH_OK;
+}
+
+/* The late fields of fjsph_step_host into pnp1 and pn, once their host copies have landed. */
+int apply_late(fjsph_ctx *c) {
+    if (c->late.empty()) return FJSPH_OK;
+    TRY(send_late(c));
+    cudaStream_t s = c->stream;
+    CU(cudaStreamWaitEvent(s, c->late_ev, 0));
+    std::vector<std::vector<void *>> dp, dp2;
+    std::vector<int> type, type2;
+    dev_ptrs(WS(c), c->D, dp, type);
+    dev_ptrs(PN(c), c->D, dp2, type2);
+    for (const auto &L : c->late) {
+        const size_t f = (size_t)L.f;
+        const int comps = (int)dp[f].size();
+        const int es = type[f] == 2 ? 4 : 8;
+        FieldPtrs fp{};
+        for (int k = 0; k < comps; ++k) fp.p[k] = dp[f][k];
+        launch_field_in(c->late_stage + L.off, comps, es, c->key, fp, c->n, s);
+        for (int k = 0; k < comps; ++k)
+            CU(cudaMemcpyAsync(dp2[f][k], dp[f][k], (size_t)es * c->n, cudaMemcpyDeviceToDevice, s));
+        c->launches++;
+    }
+    c->late.clear();
+    c->late_sent = false;
+    return FJSPH_OK;
+}
+
+/* The fields a Runge-Kutta step does not write after the pre-passes of its second search (view_ptrs
+ * order): the surface detection, the dSPH eigenvalues, the air cell values, the shifting velocity
+ * and, with frozen dissipation, the dissipation terms.  The stages and the final update leave
+ * them; an insertion or a deletion moves the slots, after which they are copied out again with
+ * the rest. */
+bool early_out_field(size_t f, int32_t variant) {
+    static const int kOut[] = {5 /* cellV */, 7 /* norm */, 8 /* vPert */, 14 /* curve */, 15 /* norm_curve */,
+                               16 /* woccl */, 19 /* cellP */, 20 /* cellRho */, 23 /* lam */, 24 /* lam_nb */,
+                               27 /* cellID */, 29 /* surf */, 30 /* surfzone */};
+    for (int k : kOut)
+        if ((size_t)k == f) return true;
+    if (!(variant & FJSPH_VAR_NOFROZEN) && (f == 4 /* aVisc */ || f == 18 /* deltaD */)) return true;
+    return false;
+}
+
+/* fjsph_step_host: the early fields gathered into reference order and sent to the host on the
+ * copy stream (called once the second search's pre-passes are enqueued) */
+int send_early_out(fjsph_ctx *c) {
+    if (c->early_out.empty() || c->out_sent) return FJSPH_OK;
+    cudaStream_t s = c->stream;
+    std::vector<std::vector<void *>> dp;
+    std::vector<int> type;
+    dev_ptrs(WS(c), c->D, dp, type);
+    for (const auto &E : c->early_out) {
+        const size_t f = (size_t)E.f;
+        const int comps = (int)dp[f].size();
+        const int es = type[f] == 2 ? 4 : 8;
+        FieldPtrs fp{};
+        for (int k = 0; k < comps; ++k) fp.p[k] = dp[f][k];
+        launch_field_out(c->out_stage + E.off, comps, es, c->key, fp, c->n, s);
+        c->launches++;
+    }
+    CU(cudaEventRecord(c->out_ready, s));
+    CU(cudaStreamWaitEvent(c->copy_stream, c->out_ready, 0));
+    for (const auto &E : c->early_out)
+        CU(cudaMemcpyAsync(const_cast<void *>(E.host), c->out_stage + E.off, (size_t)es_bytes_of(c, E.f) * c->n,
+                           cudaMemcpyDeviceToHost, c->copy_stream));
+    c->out_sent = true;
+    c->out_n = c->n;
+    return FJSPH_OK;
+}
+
 /* ---- neighbour search --------------------------------------------------------------------------- */
 int reorder_states(fjsph_ctx *c, const Params &P) {
+    TRY(apply_late(c)); /* the permutation moves every field */
     cudaStream_t s = c->stream;
     launch_reorder_map(P, c->G, c->new_of_old, c->reorder_tmp, c->reorder_tmp_len, s);
     c->launches += 5;
@@ -1446,6 +1571,7 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
     rms_error = 0.0;
     double dt = 0.0;
     TRY(find_timestep(c, &dt));
+    TRY(send_late(c));
     c->s.delta_t = dt;
     TRY(set_dt_device(c));
     TRY(search(c));
@@ -1455,7 +1581,9 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
             Params P = make_params(c);
             TRY(npd_only(c, P));
         }
+        TRY(apply_late(c));
     } else {
+        TRY(apply_late(c));
         TRY(prestep_passes(c));
     }
     if (rk) {
@@ -1470,6 +1598,7 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
     TRY(search(c));
     TRY(prestep_passes(c));
     if (rk) {
+        TRY(send_early_out(c));
         TRY(runge_kutta4(c, logbase, rms_error));
     } else {
         TRY(newmark_beta_loop(c, logbase, rms_error));
@@ -1921,6 +2050,8 @@ int fjsph_ctx_destroy(fjsph_ctx *c) {
         if (c->st_copied[b]) cudaEventDestroy(c->st_copied[b]);
         if (c->st_used[b]) cudaEventDestroy(c->st_used[b]);
     }
+    if (c->late_ev) cudaEventDestroy(c->late_ev);
+    if (c->out_ready) cudaEventDestroy(c->out_ready);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->hsc) cudaFreeHost(c->hsc);
     if (c->judge_host) cudaFreeHost(c->judge_host);
@@ -2110,6 +2241,117 @@ int fjsph_state_download(fjsph_ctx *c, int32_t which, fjsph_state_view *st) {
     if (st->n != c->n) return FJSPH_E_ARG;
     TRY(sync(c));
     return transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, false);
+}
+
+int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *out, double *rms_error) {
+    TRY(check_ctx(c));
+    if (!in || !out || !c->late.empty()) return FJSPH_E_ARG;
+    if (c->ngrp > 0) return FJSPH_E_STATE; /* independent simulations step through the groups */
+    std::vector<void *> hp;
+    view_ptrs(in, hp);
+    fjsph_state_view early = *in;
+    {
+        std::vector<void *> ep;
+        bool any_early = false;
+        /* null the late arrays of the early view: view_ptrs order is the struct's field order */
+        double **f64[] = {&early.xi,     &early.v,     &early.acc,    &early.Af,     &early.aVisc,  &early.cellV,
+                          &early.gradRho, &early.norm, &early.vPert,  &early.L,      &early.Rrho,   &early.rho,
+                          &early.p,      &early.m,     &early.curve,  &early.norm_curve, &early.woccl, &early.pDist,
+                          &early.deltaD, &early.cellP, &early.cellRho, &early.colourG, &early.colour, &early.lam,
+                          &early.lam_nb, &early.kernsum};
+        for (size_t f = 0; f < 26; ++f)
+            if (late_field(f)) *f64[f] = nullptr;
+        early.part_id = nullptr;
+        early.cellID = nullptr;
+        view_ptrs(&early, ep);
+        for (void *q : ep) any_early = any_early || q != nullptr;
+        if (!any_early) return FJSPH_E_ARG; /* positions at least */
+    }
+    /* pn = pnp1 = in: the early fields now (bookkeeping of a new particle set included) */
+    TRY(fjsph_state_upload(c, FJSPH_BOTH, &early));
+    /* the late fields on the copy stream, applied after the first search */
+    std::vector<std::vector<void *>> dp;
+    std::vector<int> type;
+    dev_ptrs(WS(c), c->D, dp, type);
+    const int64_t n = c->n;
+    int64_t need = 0;
+    for (size_t f = 0; f < hp.size(); ++f)
+        if (hp[f] && late_field(f)) need += ((type[f] == 2 ? 4 : 8) * (int64_t)dp[f].size() * n + 15) / 16 * 2;
+    if (need > c->late_cap) {
+        TRY(dfree(c, c->late_stage));
+        TRY(dalloc(c, &c->late_stage, need));
+        c->late_cap = need;
+    }
+    if (!c->late_ev) CU(cudaEventCreateWithFlags(&c->late_ev, cudaEventDisableTiming));
+    int64_t off = 0;
+    for (size_t f = 0; f < hp.size(); ++f) {
+        if (!hp[f] || !late_field(f)) continue;
+        const size_t bytes = (size_t)(type[f] == 2 ? 4 : 8) * dp[f].size() * n;
+        c->late.push_back({(int)f, off, hp[f], bytes});
+        off += ((int64_t)bytes + 15) / 16 * 2;
+    }
+    c->late_sent = false;
+    /* the output fields that are final after the second search's pre-passes go out during the
+     * remaining stages (Runge-Kutta; room for the particles the state holds now) */
+    std::vector<void *> op;
+    view_ptrs(out, op);
+    c->early_out.clear();
+    c->out_sent = false;
+    if (c->s.solver_type == FJSPH_RUNGE_KUTTA && out->n >= n) {
+        int64_t oneed = 0;
+        for (size_t f = 0; f < op.size(); ++f)
+            if (op[f] && early_out_field(f, c->s.variant)) {
+                c->early_out.push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n});
+                oneed += (es_bytes_of(c, (int)f) * c->cap + 15) / 16 * 2;
+            }
+        if (oneed > c->out_cap) {
+            TRY(dfree(c, c->out_stage));
+            TRY(dalloc(c, &c->out_stage, oneed));
+            c->out_cap = oneed;
+        }
+        if (!c->out_ready) CU(cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming));
+    }
+    const int64_t ins0 = c->inserted, del0 = c->deleted;
+    double r = 0.0;
+    const int rc = integrate(c, r);
+    const int rc_late = apply_late(c); /* a step that stopped early */
+    const bool sent = c->out_sent;
+    c->early_out.clear();
+    c->out_sent = false;
+    if (rc != FJSPH_OK || rc_late != FJSPH_OK) { /* no copy into the caller's arrays outlives the call */
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamSynchronize(c->stream);
+        return rc != FJSPH_OK ? rc : rc_late;
+    }
+    if (rms_error) *rms_error = r;
+    if (out->n < c->n) {
+        TRY(sync(c));
+        CU(cudaStreamSynchronize(c->copy_stream));
+        return FJSPH_E_CAPACITY;
+    }
+    out->n = c->n;
+    TRY(sync(c));
+    fjsph_state_view rest = *out;
+    if (sent && c->n == c->out_n && c->inserted == ins0 && c->deleted == del0) {
+        /* the early fields are on their way: the rest only */
+        double **f64[] = {&rest.xi,     &rest.v,     &rest.acc,    &rest.Af,     &rest.aVisc,  &rest.cellV,
+                          &rest.gradRho, &rest.norm, &rest.vPert,  &rest.L,      &rest.Rrho,   &rest.rho,
+                          &rest.p,      &rest.m,     &rest.curve,  &rest.norm_curve, &rest.woccl, &rest.pDist,
+                          &rest.deltaD, &rest.cellP, &rest.cellRho, &rest.colourG, &rest.colour, &rest.lam,
+                          &rest.lam_nb, &rest.kernsum};
+        for (size_t f = 0; f < 26; ++f)
+            if (early_out_field(f, c->s.variant)) *f64[f] = nullptr;
+        if (early_out_field(27, c->s.variant)) rest.cellID = nullptr;
+        if (early_out_field(29, c->s.variant)) rest.surf = nullptr;
+        if (early_out_field(30, c->s.variant)) rest.surfzone = nullptr;
+    }
+    std::vector<void *> rp;
+    view_ptrs(&rest, rp);
+    bool any = false;
+    for (void *q : rp) any = any || q != nullptr;
+    const int rc_t = any ? transfer(c, WS(c), &rest, false) : FJSPH_OK;
+    CU(cudaStreamSynchronize(c->copy_stream)); /* the early copies too */
+    return rc_t;
 }
 
 int fjsph_particle_count(fjsph_ctx *c, int64_t *n_total, int64_t *n_bound) {

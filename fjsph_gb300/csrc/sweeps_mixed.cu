@@ -566,11 +566,14 @@ __global__ void __launch_bounds__(kThreads) k_m_surface_curvature(Params P, DevS
         float Rij[D]; /* = x_j - x_i, the reference's naming in this loop */
         sepx<D>(Ai, Qi, K.A[j], LoParts(K.Lo[j]), Rij);
         const float r = sqrtf(__int_as_float(pe.y));
-        const float4 Tj = K.T[j];
+        /* a particle without a normal (the interior) needs no neighbour normals */
         float nj[D];
-        nj[0] = Tj.x;
-        nj[1] = Tj.y;
-        if (D == 3) nj[2] = Tj.z;
+        if (nin > 0.f) {
+            const float4 Tj = K.T[j];
+            nj[0] = Tj.x;
+            nj[1] = Tj.y;
+            if (D == 3) nj[2] = Tj.z;
+        }
         if (nin > 0.f && fdot<D>(nj, nj) > 0.f) {
             const float volj = K.A[j].w;
             const float gs = f_gscale(f, r);

@@ -214,6 +214,15 @@ int fjsph_state_download(fjsph_ctx *ctx, int32_t which, fjsph_state_view *st);
  * previous surface detection (the first stage uses them, src/Runge_Kutta.cpp:461-476), the
  * particle type, id and cell.  The rest (Af, gradRho, L, kernsum, colour, colourG, pDist) is
  * recomputed before it is read. */
+/* One Integrator::integrate on a host state (src/Integration.h:15-68 with the SPHState in host
+ * memory): uploads `in` as pn and pnp1, steps, and downloads pnp1 into `out` (null arrays are
+ * skipped both ways; `in` and `out` may share arrays).  The same results as fjsph_state_upload
+ * (FJSPH_BOTH), fjsph_integrate and fjsph_state_download, but the fields a step reads only after
+ * its first neighbour search (aVisc cellV norm norm_curve woccl deltaD cellP cellRho lam lam_nb
+ * part_id cellID) travel while that search runs.  out->n: on entry the particles its arrays can
+ * hold (FJSPH_E_CAPACITY after the step if insertion outgrew it), on return the particle count.
+ * Not for contexts holding independent simulations (fjsph_set_groups). */
+int fjsph_step_host(fjsph_ctx *ctx, const fjsph_state_view *in, fjsph_state_view *out, double *rms_error);
 #define FJSPH_STEP_FIELDS \
     "xi v acc Rrho rho p m cellV cellP cellRho vPert aVisc deltaD woccl lam lam_nb curve norm norm_curve " \
     "b part_id cellID surf surfzone"

@@ -107,3 +107,92 @@ def test_step_fields_are_the_step_inputs(idx):
     # before it is written, they would differ after two steps
     for f in STEP_FIELDS:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f"{label}: {f}")
+
+
+def _prefix(big, n):
+    """The first n particles of a state, sharing its memory."""
+    from fjsph_gb300.state import SPHState
+    out = SPHState.__new__(SPHState)
+    out.n, out.dim = int(n), big.dim
+    for f in ALL_FIELDS:
+        setattr(out, f, getattr(big, f)[:n])
+    return out
+
+
+@pytest.mark.parametrize("idx", range(7))
+def test_step_host_equals_separate_calls(idx):
+    """fjsph_step_host (upload as pn and pnp1, step, download, the late fields in flight during the
+    first search) equals the three calls, bit for bit, over three steps, on a context whose device
+    state started as garbage: a late field read before it landed would show.  Its input and output
+    share their arrays.  The first step re-orders at its first search, the others do not."""
+    from fjsph_gb300.api import Context
+    from fjsph_gb300.mesh import CellMesh
+    from fjsph_gb300.state import SPHState, STEP_FIELDS
+    label, c, st, extra = _cases()[idx]
+    s = extra if isinstance(extra, d.Settings) else c.settings
+    mesh = extra if isinstance(extra, CellMesh) else None
+    cap = st.n + 4096
+    ctxs = []
+    for _ in range(2):
+        ctx = Context(s, cap, c.blocks, c.inlets)
+        if mesh is not None:
+            ctx.mesh_set(mesh)
+        ctx.upload(d.BOTH, _garbage(st, 5))
+        ctxs.append(ctx)
+    fused, plain = ctxs
+    big = SPHState(cap, st.dim)
+    for f in STEP_FIELDS:
+        getattr(big, f)[:st.n] = getattr(st, f)
+    cur_a = _prefix(big, st.n)
+    cur_b = st
+    for step in range(3):
+        n_a = fused.step_host(cur_a, big, fields=STEP_FIELDS)
+        cur_a = _prefix(big, n_a)
+        plain.upload(d.BOTH, cur_b, fields=STEP_FIELDS)
+        plain.integrate()
+        cur_b = plain.download(fields=STEP_FIELDS)
+        assert cur_a.n == cur_b.n
+        for f in STEP_FIELDS:
+            np.testing.assert_array_equal(getattr(cur_a, f), getattr(cur_b, f), err_msg=f"{label} step {step}: {f}")
+    for ctx in ctxs:
+        ctx.close()
+
+
+def test_step_host_live_jet_inserts():
+    """The live-inlet jet (FP32 form, power-law air): its first step inserts a layer, so the fields
+    copied out after the pre-passes are copied again in the new order; the next steps keep them.
+    fjsph_step_host equals the three calls bit for bit."""
+    from fjsph_gb300 import cases
+    from fjsph_gb300.api import Context
+    from fjsph_gb300.state import SPHState, STEP_FIELDS
+    c = cases.jet_crossflow_live(n_target=60_000, cap=70_000)
+    s = c.settings.copy()
+    s.precision = d.PREC_MIXED
+    st = c.state
+    cap = max(s.max_points, st.n) + 1024
+    ctxs = []
+    for _ in range(2):
+        ctx = Context(s, cap, c.blocks, c.inlets)
+        if c.power_law_params:
+            ctx.air_power_law(*c.power_law_params)
+        ctx.set_states(st, st)
+        ctxs.append(ctx)
+    fused, plain = ctxs
+    big = SPHState(cap, st.dim)
+    for f in STEP_FIELDS:
+        getattr(big, f)[:st.n] = getattr(st, f)
+    cur_a, cur_b = _prefix(big, st.n), st
+    counts = []
+    for step in range(3):
+        n_a = fused.step_host(cur_a, big, fields=STEP_FIELDS)
+        cur_a = _prefix(big, n_a)
+        plain.upload(d.BOTH, cur_b, fields=STEP_FIELDS)
+        plain.integrate()
+        cur_b = plain.download(fields=STEP_FIELDS)
+        assert cur_a.n == cur_b.n
+        counts.append(cur_a.n)
+        for f in STEP_FIELDS:
+            np.testing.assert_array_equal(getattr(cur_a, f), getattr(cur_b, f), err_msg=f"step {step}: {f}")
+    assert counts[0] > st.n  # the first step inserted
+    for ctx in ctxs:
+        ctx.close()
