@@ -801,14 +801,16 @@ int apply_late(fjsph_ctx *c) {
 }
 
 /* The fields a Runge-Kutta step does not write after the pre-passes of its second search (view_ptrs
- * order): the surface detection, the dSPH eigenvalues, the air cell values, the shifting velocity
- * and, with frozen dissipation, the dissipation terms.  The stages and the final update leave
- * them; an insertion or a deletion moves the slots, after which they are copied out again with
- * the rest. */
+ * order): the surface detection, the dSPH eigenvalues, the air cell values, the shifting velocity,
+ * mass, id and type (the pipe-outlet pass is a pre-pass) and, with frozen dissipation, the
+ * dissipation terms.  The stages and the final update leave them; an insertion or a deletion
+ * moves the slots (and retypes the inlet's particles), after which they are copied out again
+ * with the rest. */
 bool early_out_field(size_t f, int32_t variant) {
-    static const int kOut[] = {5 /* cellV */, 7 /* norm */, 8 /* vPert */, 14 /* curve */, 15 /* norm_curve */,
-                               16 /* woccl */, 19 /* cellP */, 20 /* cellRho */, 23 /* lam */, 24 /* lam_nb */,
-                               27 /* cellID */, 29 /* surf */, 30 /* surfzone */};
+    static const int kOut[] = {5 /* cellV */, 7 /* norm */, 8 /* vPert */, 13 /* m */, 14 /* curve */,
+                               15 /* norm_curve */, 16 /* woccl */, 19 /* cellP */, 20 /* cellRho */, 23 /* lam */,
+                               24 /* lam_nb */, 26 /* part_id */, 27 /* cellID */, 28 /* b */, 29 /* surf */,
+                               30 /* surfzone */};
     for (int k : kOut)
         if ((size_t)k == f) return true;
     if (!(variant & FJSPH_VAR_NOFROZEN) && (f == 4 /* aVisc */ || f == 18 /* deltaD */)) return true;
@@ -2341,7 +2343,9 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
                           &rest.lam_nb, &rest.kernsum};
         for (size_t f = 0; f < 26; ++f)
             if (early_out_field(f, c->s.variant)) *f64[f] = nullptr;
+        if (early_out_field(26, c->s.variant)) rest.part_id = nullptr;
         if (early_out_field(27, c->s.variant)) rest.cellID = nullptr;
+        if (early_out_field(28, c->s.variant)) rest.b = nullptr;
         if (early_out_field(29, c->s.variant)) rest.surf = nullptr;
         if (early_out_field(30, c->s.variant)) rest.surfzone = nullptr;
     }
