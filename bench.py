@@ -607,7 +607,8 @@ def run_ours(args, ws, rank, local):
                "pinned": host._pinned,
                "fields": "FJSPH_STEP_FIELDS (the state a step reads; the rest is recomputed inside it)",
                "call": "fjsph_step_host: upload as pn and pnp1, one step, download; the fields a step first "
-                       "reads after its first neighbour search travel while that search runs"}
+                       "reads after its first neighbour search travel in while that search runs, the fields "
+                       "final after the second search's pre-passes travel out during the last stages"}
     ctx.close()
 
     def other_form(settings, steps):
