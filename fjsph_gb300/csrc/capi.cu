@@ -119,25 +119,33 @@ struct fjsph_ctx {
     double *stage2 = nullptr;  /* second staging buffer: field f + 1 moves while field f is gathered */
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t st_copied[2] = {nullptr, nullptr}, st_used[2] = {nullptr, nullptr};
-    /* fjsph_step_host: fields in flight on the copy stream while the step runs its first search
-     * (view_ptrs index, offset in late_stage in doubles, host array, bytes), sent by send_late
-     * and applied by apply_late */
+    /* fjsph_step_host: input fields in flight on the copy stream, in four groups by their first
+     * reader (in_grp: view_ptrs index, offset in in_stage in doubles, host array, bytes), each
+     * applied by apply_in just before that reader */
     struct LateField {
         int f;
         int64_t off;
         const void *host;
         size_t bytes;
     };
-    std::vector<LateField> late;
-    bool late_sent = false;
-    double *late_stage = nullptr;
-    int64_t late_cap = 0;
-    cudaEvent_t late_ev = nullptr;
+    std::vector<LateField> in_grp[4];
+    cudaEvent_t in_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    /* the groups are placed into pnp1 and pn on place_stream as they land (in_placed); the
+     * compute stream waits for a group where it first reads it (in_wait: not waited for yet) */
+    cudaStream_t place_stream = nullptr;
+    cudaEvent_t place_after = nullptr; /* the compute stream's work before the placement */
+    cudaEvent_t in_placed[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool in_wait[4] = {false, false, false, false};
+    double *in_stage = nullptr;
+    int64_t in_cap = 0;
+    /* the scan of the uploaded ids, joined before update_data needs the next id */
+    std::thread id_scan;
+    int64_t id_scan_next = 0;
     /* fjsph_step_host: fields final after the second search's pre-passes, copied out while the
      * remaining stages run (offset in out_stage, host array, bytes); out_sent: the copies went
      * out for out_n particles */
-    std::vector<LateField> early_out;
-    bool out_sent = false;
+    std::vector<LateField> early_out, final_out; /* after the pre-passes; after the last residual */
+    bool out_sent = false, final_sent = false;
     int64_t out_n = 0;
     double *out_stage = nullptr;
     int64_t out_cap = 0;
@@ -749,55 +757,75 @@ int64_t es_bytes_of(fjsph_ctx *c, int f) {
     return (int64_t)(type[f] == 2 ? 4 : 8) * (int64_t)dp[f].size();
 }
 
-/* The fields a step first reads after its first search and the npd pass behind it (view_ptrs
- * order): the frozen dissipation terms, the air cell values, the previous surface detection and
- * the particle id and cell.  The time-step reduction, the search and the packing read only the
- * others. */
-bool late_field(size_t f) {
-    static const int kLate[] = {4 /* aVisc */, 5 /* cellV */, 7 /* norm */, 15 /* norm_curve */,
-                                16 /* woccl */, 18 /* deltaD */, 19 /* cellP */, 20 /* cellRho */,
-                                23 /* lam */, 24 /* lam_nb */, 26 /* part_id */, 27 /* cellID */};
-    for (int k : kLate)
-        if ((size_t)k == f) return true;
-    return false;
+/* The input groups of fjsph_step_host, by the first pass that reads them (view_ptrs order):
+ *   kInPos    the neighbour search: the positions;
+ *   kInStep   the time-step reduction: acc, Af, v, Rrho, rho, curve (and vPert under ALE);
+ *   kInPack   the npd pass and the packing of the split-precision inputs: p, m, type, surface flags
+ *             (and the fields the pre-passes recompute before reading, when given);
+ *   kInLate   the first stage: the frozen dissipation terms, the air cell values, the previous
+ *             surface detection, the particle id and cell. */
+enum { kInPos = 0, kInStep = 1, kInPack = 2, kInLate = 3 }; /* the order they travel in */
+int in_group(size_t f, int32_t variant) {
+    switch (f) {
+    case 2: case 3: case 1: case 10: case 11: case 14: /* acc Af v Rrho rho curve */
+        return kInStep;
+    case 8: /* vPert: the time-step reduction reads it under ALE, the packing always */
+        return (variant & FJSPH_VAR_ALE) ? kInStep : kInPack;
+    case 0: /* xi */
+        return kInPos;
+    case 4: case 5: case 7: case 15: case 16: case 18: case 19: case 20: case 23: case 24: case 26: case 27:
+        /* aVisc cellV norm norm_curve woccl deltaD cellP cellRho lam lam_nb part_id cellID */
+        return kInLate;
+    default:
+        return kInPack;
+    }
 }
 
-/* The late fields' host-to-device copies of fjsph_step_host.  Sent after the time-step
- * reduction has read its maxima back: a device-to-host read-back issued behind them could wait
- * for them on the copy engine. */
-int send_late(fjsph_ctx *c) {
-    if (c->late.empty() || c->late_sent) return FJSPH_OK;
-    for (const auto &L : c->late)
-        CU(cudaMemcpyAsync(c->late_stage + L.off, L.host, L.bytes, cudaMemcpyHostToDevice, c->copy_stream));
-    CU(cudaEventRecord(c->late_ev, c->copy_stream));
-    c->late_sent = true;
-    return FJSPH_OK;
-}
-
-/* The late fields of fjsph_step_host into pnp1 and pn, once their host copies have landed. */
-int apply_late(fjsph_ctx *c) {
-    if (c->late.empty()) return FJSPH_OK;
-    TRY(send_late(c));
-    cudaStream_t s = c->stream;
-    CU(cudaStreamWaitEvent(s, c->late_ev, 0));
+/* One input group of fjsph_step_host into pnp1 and pn on place_stream, once its host copies have
+ * landed (enqueued at once for every group). */
+int place_in(fjsph_ctx *c, int g) {
+    if (c->in_grp[g].empty()) return FJSPH_OK;
+    cudaStream_t s = c->place_stream;
+    CU(cudaStreamWaitEvent(s, c->in_ev[g], 0));
     std::vector<std::vector<void *>> dp, dp2;
     std::vector<int> type, type2;
     dev_ptrs(WS(c), c->D, dp, type);
     dev_ptrs(PN(c), c->D, dp2, type2);
-    for (const auto &L : c->late) {
+    for (const auto &L : c->in_grp[g]) {
         const size_t f = (size_t)L.f;
         const int comps = (int)dp[f].size();
         const int es = type[f] == 2 ? 4 : 8;
         FieldPtrs fp{};
         for (int k = 0; k < comps; ++k) fp.p[k] = dp[f][k];
-        launch_field_in(c->late_stage + L.off, comps, es, c->key, fp, c->n, s);
+        launch_field_in(c->in_stage + L.off, comps, es, c->key, fp, c->n, s);
         for (int k = 0; k < comps; ++k)
             CU(cudaMemcpyAsync(dp2[f][k], dp[f][k], (size_t)es * c->n, cudaMemcpyDeviceToDevice, s));
         c->launches++;
     }
-    c->late.clear();
-    c->late_sent = false;
+    CU(cudaEventRecord(c->in_placed[g], s));
+    c->in_grp[g].clear();
+    c->in_wait[g] = true;
     return FJSPH_OK;
+}
+
+/* The compute stream waits for input group g of fjsph_step_host (before its first reader). */
+int apply_in(fjsph_ctx *c, int g) {
+    if (!c->in_wait[g]) return FJSPH_OK;
+    CU(cudaStreamWaitEvent(c->stream, c->in_placed[g], 0));
+    c->in_wait[g] = false;
+    return FJSPH_OK;
+}
+
+int apply_all_in(fjsph_ctx *c) {
+    for (int g = 0; g < 4; ++g) TRY(apply_in(c, g));
+    return FJSPH_OK;
+}
+
+/* the ids of fjsph_step_host's upload, scanned on a host thread during the step */
+void join_id_scan(fjsph_ctx *c) {
+    if (!c->id_scan.joinable()) return;
+    c->id_scan.join();
+    c->part_id_next = c->id_scan_next;
 }
 
 /* The fields a Runge-Kutta step does not write after the pre-passes of its second search (view_ptrs
@@ -817,15 +845,19 @@ bool early_out_field(size_t f, int32_t variant) {
     return false;
 }
 
-/* fjsph_step_host: the early fields gathered into reference order and sent to the host on the
- * copy stream (called once the second search's pre-passes are enqueued) */
-int send_early_out(fjsph_ctx *c) {
-    if (c->early_out.empty() || c->out_sent) return FJSPH_OK;
+/* The fields a Runge-Kutta step writes last in its final residual (acceleration and density
+ * rate): sent while the final update, the inlet and update_data run. */
+bool final_out_field(size_t f) { return f == 2 /* acc */ || f == 10 /* Rrho */; }
+
+/* fjsph_step_host: fields gathered into reference order and sent to the host on the copy stream
+ * (list: the early fields once the second search's pre-passes are enqueued, the final ones after
+ * the last residual) */
+int send_out(fjsph_ctx *c, const std::vector<fjsph_ctx::LateField> &list) {
     cudaStream_t s = c->stream;
     std::vector<std::vector<void *>> dp;
     std::vector<int> type;
     dev_ptrs(WS(c), c->D, dp, type);
-    for (const auto &E : c->early_out) {
+    for (const auto &E : list) {
         const size_t f = (size_t)E.f;
         const int comps = (int)dp[f].size();
         const int es = type[f] == 2 ? 4 : 8;
@@ -836,17 +868,30 @@ int send_early_out(fjsph_ctx *c) {
     }
     CU(cudaEventRecord(c->out_ready, s));
     CU(cudaStreamWaitEvent(c->copy_stream, c->out_ready, 0));
-    for (const auto &E : c->early_out)
+    for (const auto &E : list)
         CU(cudaMemcpyAsync(const_cast<void *>(E.host), c->out_stage + E.off, (size_t)es_bytes_of(c, E.f) * c->n,
                            cudaMemcpyDeviceToHost, c->copy_stream));
+    return FJSPH_OK;
+}
+
+int send_early_out(fjsph_ctx *c) {
+    if (c->early_out.empty() || c->out_sent) return FJSPH_OK;
+    TRY(send_out(c, c->early_out));
     c->out_sent = true;
     c->out_n = c->n;
     return FJSPH_OK;
 }
 
+int send_final_out(fjsph_ctx *c) {
+    if (c->final_out.empty() || !c->out_sent || c->final_sent || c->n != c->out_n) return FJSPH_OK;
+    TRY(send_out(c, c->final_out));
+    c->final_sent = true;
+    return FJSPH_OK;
+}
+
 /* ---- neighbour search --------------------------------------------------------------------------- */
 int reorder_states(fjsph_ctx *c, const Params &P) {
-    TRY(apply_late(c)); /* the permutation moves every field */
+    TRY(apply_all_in(c)); /* the permutation moves every field */
     cudaStream_t s = c->stream;
     launch_reorder_map(P, c->G, c->new_of_old, c->reorder_tmp, c->reorder_tmp_len, s);
     c->launches += 5;
@@ -995,6 +1040,8 @@ int search_fixed(fjsph_ctx *c, const Params &P) {
 
 int search(fjsph_ctx *c) {
     if (c->n == 0) return FJSPH_E_STATE;
+    TRY(apply_in(c, kInPos));
+    if (c->pair_mode == FJSPH_PAIRS_TILES) TRY(apply_in(c, kInPack)); /* the masks read packed inputs */
     if (c->table_want > c->G.table_size) {
         TRY(sync(c));
         TRY(alloc_table(c, c->table_want));
@@ -1389,6 +1436,7 @@ int rk_final(fjsph_ctx *c) {
         c->launches++;
     }
     TRY(resid(c, P));
+    TRY(send_final_out(c));
     {
         Section sec(c, PASS_UPDATE);
         for (int k = 0; k < c->D; ++k)
@@ -1572,20 +1620,33 @@ int integrate_no_update(fjsph_ctx *c, double &rms_error, bool skip_dead) {
     double logbase = 0.0;
     rms_error = 0.0;
     double dt = 0.0;
-    TRY(find_timestep(c, &dt));
-    TRY(send_late(c));
-    c->s.delta_t = dt;
-    TRY(set_dt_device(c));
-    TRY(search(c));
+    if (c->in_wait[kInPos]) {
+        /* a fjsph_step_host upload in flight: its positions land first, so the search runs while
+         * the time-step reduction's inputs travel.  The search reads neither the time step nor
+         * those inputs, and the reduction (maxima and a minimum) gives the same bits in any
+         * particle order, so the results are those of the reference order. */
+        TRY(search(c));
+        TRY(apply_in(c, kInStep));
+        TRY(find_timestep(c, &dt));
+        c->s.delta_t = dt;
+        TRY(set_dt_device(c));
+    } else {
+        TRY(apply_in(c, kInStep));
+        TRY(find_timestep(c, &dt));
+        c->s.delta_t = dt;
+        TRY(set_dt_device(c));
+        TRY(search(c));
+    }
+    TRY(apply_in(c, kInPack));
     const bool rk = c->s.solver_type == FJSPH_RUNGE_KUTTA;
     if (rk && skip_dead) {
         if (c->s.st_model == FJSPH_ST_PAIRWISE) {
             Params P = make_params(c);
             TRY(npd_only(c, P));
         }
-        TRY(apply_late(c));
+        TRY(apply_in(c, kInLate));
     } else {
-        TRY(apply_late(c));
+        TRY(apply_in(c, kInLate));
         TRY(prestep_passes(c));
     }
     if (rk) {
@@ -1790,6 +1851,7 @@ int integrate(fjsph_ctx *c, double &step_error) {
     TRY(integrate_no_update(c, step_error, true));
     c->arm = 0;
     TRY(closure_collect(c));
+    join_id_scan(c); /* insertion numbers new particles from the uploaded ids */
     TRY(update_data(c));
     TRY(copy_state(c, c->iW, c->ipn));
     c->pn_equals_W = true;
@@ -2052,7 +2114,16 @@ int fjsph_ctx_destroy(fjsph_ctx *c) {
         if (c->st_copied[b]) cudaEventDestroy(c->st_copied[b]);
         if (c->st_used[b]) cudaEventDestroy(c->st_used[b]);
     }
-    if (c->late_ev) cudaEventDestroy(c->late_ev);
+    join_id_scan(c);
+    for (cudaEvent_t e : c->in_ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->in_placed)
+        if (e) cudaEventDestroy(e);
+    if (c->place_after) cudaEventDestroy(c->place_after);
+    if (c->place_stream) {
+        cudaStreamSynchronize(c->place_stream);
+        cudaStreamDestroy(c->place_stream);
+    }
     if (c->out_ready) cudaEventDestroy(c->out_ready);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->hsc) cudaFreeHost(c->hsc);
@@ -2191,10 +2262,10 @@ int fjsph_update_counts(fjsph_ctx *c, int64_t *inserted, int64_t *deleted) {
     return FJSPH_OK;
 }
 
-int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) {
-    TRY(check_ctx(c));
+/* The bookkeeping of an upload before its fields move: checks, a new particle set's keys, block
+ * and inlet tables, and the scan of the ids (on a second thread while the fields transfer). */
+int upload_begin(fjsph_ctx *c, const fjsph_state_view *st, std::thread &ids, int64_t &id_next, bool scan_ids = true) {
     TRY(sync(c));
-    if (!st || (which != FJSPH_PN && which != FJSPH_PNP1 && which != FJSPH_BOTH)) return FJSPH_E_ARG;
     if (st->n < 0) return FJSPH_E_ARG;
     if (st->n > c->cap) return FJSPH_E_CAPACITY;
     if (c->blocks.empty()) return FJSPH_E_STATE;
@@ -2212,28 +2283,43 @@ int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) 
         TRY(upload_inlets(c, keys));
         c->reorder_pending = true;
     }
-    /* ids of inserted particles continue from the largest uploaded one: a host scan of the
-     * ids, run on a second thread while the fields transfer */
-    int64_t id_next = 0;
-    std::thread ids;
-    if (which != FJSPH_PN && st->part_id)
+    /* ids of inserted particles continue from the largest uploaded one */
+    if (scan_ids && st->part_id)
         ids = std::thread([&id_next, st] {
             int64_t m = 0;
             for (int64_t i = 0; i < st->n; ++i) m = std::max<int64_t>(m, st->part_id[i] + 1);
             id_next = m;
         });
-    /* FJSPH_BOTH: pn = pnp1 = the uploaded state: one host transfer, each field copied on the
-     * device as it arrives */
-    const int rc_t = transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true, which == FJSPH_BOTH ? &PN(c) : nullptr);
-    if (ids.joinable()) ids.join();
-    TRY(rc_t);
+    return FJSPH_OK;
+}
+
+/* The bookkeeping after the fields of an upload are enqueued. */
+int upload_end(fjsph_ctx *c, int32_t which, const fjsph_state_view *st, std::thread *ids, int64_t id_next) {
+    if (ids && ids->joinable()) ids->join();
     if (grouped(c)) TRY(upload_groups(c));
-    if (which != FJSPH_PN && st->part_id) c->part_id_next = id_next;
+    if (ids && which != FJSPH_PN && st->part_id) c->part_id_next = id_next;
     if (which != FJSPH_PN) {
         c->nbr_valid = false;
         mark_full(c);
     }
     c->pn_equals_W = which == FJSPH_BOTH;
+    return FJSPH_OK;
+}
+
+int fjsph_state_upload(fjsph_ctx *c, int32_t which, const fjsph_state_view *st) {
+    TRY(check_ctx(c));
+    if (!st || (which != FJSPH_PN && which != FJSPH_PNP1 && which != FJSPH_BOTH)) return FJSPH_E_ARG;
+    int64_t id_next = 0;
+    std::thread ids;
+    TRY(upload_begin(c, st, ids, id_next, which != FJSPH_PN));
+    /* FJSPH_BOTH: pn = pnp1 = the uploaded state: one host transfer, each field copied on the
+     * device as it arrives */
+    const int rc_t = transfer(c, which == FJSPH_PN ? PN(c) : WS(c), st, true, which == FJSPH_BOTH ? &PN(c) : nullptr);
+    if (rc_t != FJSPH_OK) {
+        if (ids.joinable()) ids.join();
+        return rc_t;
+    }
+    TRY(upload_end(c, which, st, &ids, id_next));
     return sync(c);
 }
 
@@ -2247,65 +2333,95 @@ int fjsph_state_download(fjsph_ctx *c, int32_t which, fjsph_state_view *st) {
 
 int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *out, double *rms_error) {
     TRY(check_ctx(c));
-    if (!in || !out || !c->late.empty()) return FJSPH_E_ARG;
+    if (!in || !out) return FJSPH_E_ARG;
     if (c->ngrp > 0) return FJSPH_E_STATE; /* independent simulations step through the groups */
+    for (const auto &g : c->in_grp)
+        if (!g.empty()) return FJSPH_E_STATE;
     std::vector<void *> hp;
     view_ptrs(in, hp);
-    fjsph_state_view early = *in;
-    {
-        std::vector<void *> ep;
-        bool any_early = false;
-        /* null the late arrays of the early view: view_ptrs order is the struct's field order */
-        double **f64[] = {&early.xi,     &early.v,     &early.acc,    &early.Af,     &early.aVisc,  &early.cellV,
-                          &early.gradRho, &early.norm, &early.vPert,  &early.L,      &early.Rrho,   &early.rho,
-                          &early.p,      &early.m,     &early.curve,  &early.norm_curve, &early.woccl, &early.pDist,
-                          &early.deltaD, &early.cellP, &early.cellRho, &early.colourG, &early.colour, &early.lam,
-                          &early.lam_nb, &early.kernsum};
-        for (size_t f = 0; f < 26; ++f)
-            if (late_field(f)) *f64[f] = nullptr;
-        early.part_id = nullptr;
-        early.cellID = nullptr;
-        view_ptrs(&early, ep);
-        for (void *q : ep) any_early = any_early || q != nullptr;
-        if (!any_early) return FJSPH_E_ARG; /* positions at least */
-    }
-    /* pn = pnp1 = in: the early fields now (bookkeeping of a new particle set included) */
-    TRY(fjsph_state_upload(c, FJSPH_BOTH, &early));
-    /* the late fields on the copy stream, applied after the first search */
+    if (!in->xi) return FJSPH_E_ARG; /* positions at least */
+    /* pn = pnp1 = in: the bookkeeping of an upload now, the fields on the copy stream in four
+     * groups, each applied just before the pass that first reads it */
+    join_id_scan(c);
+    TRY(upload_begin(c, in, c->id_scan, c->id_scan_next));
     std::vector<std::vector<void *>> dp;
     std::vector<int> type;
     dev_ptrs(WS(c), c->D, dp, type);
     const int64_t n = c->n;
     int64_t need = 0;
     for (size_t f = 0; f < hp.size(); ++f)
-        if (hp[f] && late_field(f)) need += ((type[f] == 2 ? 4 : 8) * (int64_t)dp[f].size() * n + 15) / 16 * 2;
-    if (need > c->late_cap) {
-        TRY(dfree(c, c->late_stage));
-        TRY(dalloc(c, &c->late_stage, need));
-        c->late_cap = need;
+        if (hp[f]) need += ((type[f] == 2 ? 4 : 8) * (int64_t)dp[f].size() * n + 15) / 16 * 2;
+    int rc_up = FJSPH_OK;
+    if (need > c->in_cap) {
+        rc_up = dfree(c, c->in_stage);
+        if (rc_up == FJSPH_OK) rc_up = dalloc(c, &c->in_stage, need);
+        c->in_cap = rc_up == FJSPH_OK ? need : 0;
     }
-    if (!c->late_ev) CU(cudaEventCreateWithFlags(&c->late_ev, cudaEventDisableTiming));
+    if (!c->copy_stream && rc_up == FJSPH_OK) {
+        if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) rc_up = FJSPH_E_CUDA;
+        for (int b = 0; b < 2 && rc_up == FJSPH_OK; ++b)
+            if (cudaEventCreateWithFlags(&c->st_copied[b], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&c->st_used[b], cudaEventDisableTiming) != cudaSuccess)
+                rc_up = FJSPH_E_CUDA;
+    }
+    if (!c->place_stream && rc_up == FJSPH_OK) {
+        /* the highest priority: the placement's blocks go ahead of the search's waiting ones */
+        int lo = 0, hi = 0;
+        if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&c->place_stream, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->place_after, cudaEventDisableTiming) != cudaSuccess)
+            rc_up = FJSPH_E_CUDA;
+    }
+    /* the placement reads the keys and writes pnp1 and pn after everything the compute stream
+     * has enqueued so far */
+    if (rc_up == FJSPH_OK && (cudaEventRecord(c->place_after, c->stream) != cudaSuccess ||
+                              cudaStreamWaitEvent(c->place_stream, c->place_after, 0) != cudaSuccess))
+        rc_up = FJSPH_E_CUDA;
     int64_t off = 0;
-    for (size_t f = 0; f < hp.size(); ++f) {
-        if (!hp[f] || !late_field(f)) continue;
-        const size_t bytes = (size_t)(type[f] == 2 ? 4 : 8) * dp[f].size() * n;
-        c->late.push_back({(int)f, off, hp[f], bytes});
-        off += ((int64_t)bytes + 15) / 16 * 2;
+    for (int g = 0; g < 4 && rc_up == FJSPH_OK; ++g) {
+        if ((!c->in_ev[g] && cudaEventCreateWithFlags(&c->in_ev[g], cudaEventDisableTiming) != cudaSuccess) ||
+            (!c->in_placed[g] && cudaEventCreateWithFlags(&c->in_placed[g], cudaEventDisableTiming) != cudaSuccess)) {
+            rc_up = FJSPH_E_CUDA;
+            break;
+        }
+        for (size_t f = 0; f < hp.size(); ++f) {
+            if (!hp[f] || in_group(f, c->s.variant) != g) continue;
+            const size_t bytes = (size_t)(type[f] == 2 ? 4 : 8) * dp[f].size() * n;
+            if (cudaMemcpyAsync(c->in_stage + off, hp[f], bytes, cudaMemcpyHostToDevice, c->copy_stream) !=
+                cudaSuccess) {
+                rc_up = FJSPH_E_CUDA;
+                break;
+            }
+            c->in_grp[g].push_back({(int)f, off, hp[f], bytes});
+            off += ((int64_t)bytes + 15) / 16 * 2;
+        }
+        if (rc_up == FJSPH_OK && cudaEventRecord(c->in_ev[g], c->copy_stream) != cudaSuccess) rc_up = FJSPH_E_CUDA;
     }
-    c->late_sent = false;
+    for (int g = 0; g < 4 && rc_up == FJSPH_OK; ++g) rc_up = place_in(c, g);
+    const int rc_end = upload_end(c, FJSPH_BOTH, in, nullptr, 0);
+    if (rc_up != FJSPH_OK || rc_end != FJSPH_OK) {
+        for (auto &g : c->in_grp) g.clear();
+        for (bool &w : c->in_wait) w = false;
+        if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+        if (c->place_stream) cudaStreamSynchronize(c->place_stream);
+        join_id_scan(c);
+        return rc_up != FJSPH_OK ? rc_up : rc_end;
+    }
     /* the output fields that are final after the second search's pre-passes go out during the
      * remaining stages (Runge-Kutta; room for the particles the state holds now) */
     std::vector<void *> op;
     view_ptrs(out, op);
     c->early_out.clear();
-    c->out_sent = false;
+    c->final_out.clear();
+    c->out_sent = c->final_sent = false;
     if (c->s.solver_type == FJSPH_RUNGE_KUTTA && out->n >= n) {
         int64_t oneed = 0;
-        for (size_t f = 0; f < op.size(); ++f)
-            if (op[f] && early_out_field(f, c->s.variant)) {
-                c->early_out.push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n});
-                oneed += (es_bytes_of(c, (int)f) * c->cap + 15) / 16 * 2;
-            }
+        for (size_t f = 0; f < op.size(); ++f) {
+            const bool e = early_out_field(f, c->s.variant), fi = final_out_field(f);
+            if (!op[f] || !(e || fi)) continue;
+            (e ? c->early_out : c->final_out).push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n});
+            oneed += (es_bytes_of(c, (int)f) * c->cap + 15) / 16 * 2;
+        }
         if (oneed > c->out_cap) {
             TRY(dfree(c, c->out_stage));
             TRY(dalloc(c, &c->out_stage, oneed));
@@ -2316,10 +2432,12 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
     const int64_t ins0 = c->inserted, del0 = c->deleted;
     double r = 0.0;
     const int rc = integrate(c, r);
-    const int rc_late = apply_late(c); /* a step that stopped early */
-    const bool sent = c->out_sent;
+    const int rc_late = apply_all_in(c); /* a step that stopped early */
+    join_id_scan(c);
+    const bool sent = c->out_sent, fsent = c->final_sent;
     c->early_out.clear();
-    c->out_sent = false;
+    c->final_out.clear();
+    c->out_sent = c->final_sent = false;
     if (rc != FJSPH_OK || rc_late != FJSPH_OK) { /* no copy into the caller's arrays outlives the call */
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamSynchronize(c->stream);
@@ -2348,6 +2466,10 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
         if (early_out_field(28, c->s.variant)) rest.b = nullptr;
         if (early_out_field(29, c->s.variant)) rest.surf = nullptr;
         if (early_out_field(30, c->s.variant)) rest.surfzone = nullptr;
+        if (fsent) {
+            rest.acc = nullptr;
+            rest.Rrho = nullptr;
+        }
     }
     std::vector<void *> rp;
     view_ptrs(&rest, rp);

@@ -217,9 +217,11 @@ int fjsph_state_download(fjsph_ctx *ctx, int32_t which, fjsph_state_view *st);
 /* One Integrator::integrate on a host state (src/Integration.h:15-68 with the SPHState in host
  * memory): uploads `in` as pn and pnp1, steps, and downloads pnp1 into `out` (null arrays are
  * skipped both ways; `in` and `out` may share arrays).  The same results as fjsph_state_upload
- * (FJSPH_BOTH), fjsph_integrate and fjsph_state_download, but the fields a step reads only after
- * its first neighbour search (aVisc cellV norm norm_curve woccl deltaD cellP cellRho lam lam_nb
- * part_id cellID) travel while that search runs.  out->n: on entry the particles its arrays can
+ * (FJSPH_BOTH), fjsph_integrate and fjsph_state_download, but the copies overlap the step: the
+ * inputs travel in groups ordered by their first reader (positions, time-step inputs, packing
+ * inputs, the rest) while the search runs, and under Runge-Kutta the fields final after the
+ * second search's pre-passes and the last residual travel out during the remaining work.
+ * out->n: on entry the particles its arrays can
  * hold (FJSPH_E_CAPACITY after the step if insertion outgrew it), on return the particle count.
  * Not for contexts holding independent simulations (fjsph_set_groups). */
 int fjsph_step_host(fjsph_ctx *ctx, const fjsph_state_view *in, fjsph_state_view *out, double *rms_error);
