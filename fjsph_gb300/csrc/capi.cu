@@ -127,9 +127,10 @@ struct fjsph_ctx {
         int64_t off;
         const void *host;
         size_t bytes;
+        int ev; /* input fields: index of the landing event in in_ev */
     };
     std::vector<LateField> in_grp[4];
-    cudaEvent_t in_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> in_ev; /* one per input field: its host copy has landed */
     /* the groups are placed into pnp1 and pn on place_stream as they land (in_placed); the
      * compute stream waits for a group where it first reads it (in_wait: not waited for yet) */
     cudaStream_t place_stream = nullptr;
@@ -144,8 +145,10 @@ struct fjsph_ctx {
     /* fjsph_step_host: fields final after the second search's pre-passes, copied out while the
      * remaining stages run (offset in out_stage, host array, bytes); out_sent: the copies went
      * out for out_n particles */
-    std::vector<LateField> early_out, final_out; /* after the pre-passes; after the last residual */
-    bool out_sent = false, final_sent = false;
+    std::vector<LateField> early_out, final_out, last_out; /* after the pre-passes; after the last
+                                                              * residual; after update_data */
+    bool out_sent = false, final_sent = false, last_sent = false;
+    int64_t out_ins0 = 0, out_del0 = 0; /* insertions and deletions before the step */
     int64_t out_n = 0;
     double *out_stage = nullptr;
     int64_t out_cap = 0;
@@ -781,17 +784,17 @@ int in_group(size_t f, int32_t variant) {
     }
 }
 
-/* One input group of fjsph_step_host into pnp1 and pn on place_stream, once its host copies have
- * landed (enqueued at once for every group). */
+/* One input group of fjsph_step_host into pnp1 and pn on place_stream, each field once its host
+ * copy has landed (enqueued at once for every group). */
 int place_in(fjsph_ctx *c, int g) {
     if (c->in_grp[g].empty()) return FJSPH_OK;
     cudaStream_t s = c->place_stream;
-    CU(cudaStreamWaitEvent(s, c->in_ev[g], 0));
     std::vector<std::vector<void *>> dp, dp2;
     std::vector<int> type, type2;
     dev_ptrs(WS(c), c->D, dp, type);
     dev_ptrs(PN(c), c->D, dp2, type2);
     for (const auto &L : c->in_grp[g]) {
+        CU(cudaStreamWaitEvent(s, c->in_ev[L.ev], 0)); /* each field as it lands */
         const size_t f = (size_t)L.f;
         const int comps = (int)dp[f].size();
         const int es = type[f] == 2 ? 4 : 8;
@@ -879,6 +882,19 @@ int send_early_out(fjsph_ctx *c) {
     TRY(send_out(c, c->early_out));
     c->out_sent = true;
     c->out_n = c->n;
+    return FJSPH_OK;
+}
+
+/* The fields update_data writes last (positions, velocities, density, pressure): sent when it has
+ * run without inserting or deleting, while the state is copied to pn. */
+bool last_out_field(size_t f) { return f == 0 || f == 1 || f == 11 || f == 12; }
+
+int send_last_out(fjsph_ctx *c) {
+    if (c->last_out.empty() || !c->out_sent || c->last_sent || c->n != c->out_n || c->inserted != c->out_ins0 ||
+        c->deleted != c->out_del0)
+        return FJSPH_OK;
+    TRY(send_out(c, c->last_out));
+    c->last_sent = true;
     return FJSPH_OK;
 }
 
@@ -1853,6 +1869,7 @@ int integrate(fjsph_ctx *c, double &step_error) {
     TRY(closure_collect(c));
     join_id_scan(c); /* insertion numbers new particles from the uploaded ids */
     TRY(update_data(c));
+    TRY(send_last_out(c));
     TRY(copy_state(c, c->iW, c->ipn));
     c->pn_equals_W = true;
     fjsph_settings &I = c->s;
@@ -2115,8 +2132,7 @@ int fjsph_ctx_destroy(fjsph_ctx *c) {
         if (c->st_used[b]) cudaEventDestroy(c->st_used[b]);
     }
     join_id_scan(c);
-    for (cudaEvent_t e : c->in_ev)
-        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->in_ev) cudaEventDestroy(e);
     for (cudaEvent_t e : c->in_placed)
         if (e) cudaEventDestroy(e);
     if (c->place_after) cudaEventDestroy(c->place_after);
@@ -2378,24 +2394,33 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
                               cudaStreamWaitEvent(c->place_stream, c->place_after, 0) != cudaSuccess))
         rc_up = FJSPH_E_CUDA;
     int64_t off = 0;
+    int nev = 0;
     for (int g = 0; g < 4 && rc_up == FJSPH_OK; ++g) {
-        if ((!c->in_ev[g] && cudaEventCreateWithFlags(&c->in_ev[g], cudaEventDisableTiming) != cudaSuccess) ||
-            (!c->in_placed[g] && cudaEventCreateWithFlags(&c->in_placed[g], cudaEventDisableTiming) != cudaSuccess)) {
+        if (!c->in_placed[g] && cudaEventCreateWithFlags(&c->in_placed[g], cudaEventDisableTiming) != cudaSuccess) {
             rc_up = FJSPH_E_CUDA;
             break;
         }
         for (size_t f = 0; f < hp.size(); ++f) {
             if (!hp[f] || in_group(f, c->s.variant) != g) continue;
+            if ((size_t)nev == c->in_ev.size()) {
+                cudaEvent_t e = nullptr;
+                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                    rc_up = FJSPH_E_CUDA;
+                    break;
+                }
+                c->in_ev.push_back(e);
+            }
             const size_t bytes = (size_t)(type[f] == 2 ? 4 : 8) * dp[f].size() * n;
             if (cudaMemcpyAsync(c->in_stage + off, hp[f], bytes, cudaMemcpyHostToDevice, c->copy_stream) !=
-                cudaSuccess) {
+                    cudaSuccess ||
+                cudaEventRecord(c->in_ev[nev], c->copy_stream) != cudaSuccess) {
                 rc_up = FJSPH_E_CUDA;
                 break;
             }
-            c->in_grp[g].push_back({(int)f, off, hp[f], bytes});
+            c->in_grp[g].push_back({(int)f, off, hp[f], bytes, nev});
+            ++nev;
             off += ((int64_t)bytes + 15) / 16 * 2;
         }
-        if (rc_up == FJSPH_OK && cudaEventRecord(c->in_ev[g], c->copy_stream) != cudaSuccess) rc_up = FJSPH_E_CUDA;
     }
     for (int g = 0; g < 4 && rc_up == FJSPH_OK; ++g) rc_up = place_in(c, g);
     const int rc_end = upload_end(c, FJSPH_BOTH, in, nullptr, 0);
@@ -2413,13 +2438,17 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
     view_ptrs(out, op);
     c->early_out.clear();
     c->final_out.clear();
-    c->out_sent = c->final_sent = false;
+    c->last_out.clear();
+    c->out_sent = c->final_sent = c->last_sent = false;
+    c->out_ins0 = c->inserted;
+    c->out_del0 = c->deleted;
     if (c->s.solver_type == FJSPH_RUNGE_KUTTA && out->n >= n) {
         int64_t oneed = 0;
         for (size_t f = 0; f < op.size(); ++f) {
-            const bool e = early_out_field(f, c->s.variant), fi = final_out_field(f);
-            if (!op[f] || !(e || fi)) continue;
-            (e ? c->early_out : c->final_out).push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n});
+            const bool e = early_out_field(f, c->s.variant), fi = final_out_field(f), la = last_out_field(f);
+            if (!op[f] || !(e || fi || la)) continue;
+            (e ? c->early_out : (fi ? c->final_out : c->last_out))
+                .push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n, -1});
             oneed += (es_bytes_of(c, (int)f) * c->cap + 15) / 16 * 2;
         }
         if (oneed > c->out_cap) {
@@ -2434,10 +2463,11 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
     const int rc = integrate(c, r);
     const int rc_late = apply_all_in(c); /* a step that stopped early */
     join_id_scan(c);
-    const bool sent = c->out_sent, fsent = c->final_sent;
+    const bool sent = c->out_sent, fsent = c->final_sent, lsent = c->last_sent;
     c->early_out.clear();
     c->final_out.clear();
-    c->out_sent = c->final_sent = false;
+    c->last_out.clear();
+    c->out_sent = c->final_sent = c->last_sent = false;
     if (rc != FJSPH_OK || rc_late != FJSPH_OK) { /* no copy into the caller's arrays outlives the call */
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamSynchronize(c->stream);
@@ -2469,6 +2499,12 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
         if (fsent) {
             rest.acc = nullptr;
             rest.Rrho = nullptr;
+        }
+        if (lsent) {
+            rest.xi = nullptr;
+            rest.v = nullptr;
+            rest.rho = nullptr;
+            rest.p = nullptr;
         }
     }
     std::vector<void *> rp;
