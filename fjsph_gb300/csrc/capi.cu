@@ -2373,6 +2373,40 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
         if (rc_up == FJSPH_OK) rc_up = dalloc(c, &c->in_stage, need);
         c->in_cap = rc_up == FJSPH_OK ? need : 0;
     }
+    /* the output fields that go out before the step ends (Runge-Kutta; room for the particles
+     * the state holds now): after the second search's pre-passes, after the last residual, after
+     * update_data */
+    std::vector<void *> op;
+    view_ptrs(out, op);
+    c->early_out.clear();
+    c->final_out.clear();
+    c->last_out.clear();
+    c->out_sent = c->final_sent = c->last_sent = false;
+    c->out_ins0 = c->inserted;
+    c->out_del0 = c->deleted;
+    if (rc_up == FJSPH_OK && c->s.solver_type == FJSPH_RUNGE_KUTTA && out->n >= n) {
+        int64_t oneed = 0;
+        for (size_t f = 0; f < op.size(); ++f) {
+            const bool e = early_out_field(f, c->s.variant), fi = final_out_field(f), la = last_out_field(f);
+            if (!op[f] || !(e || fi || la)) continue;
+            (e ? c->early_out : (fi ? c->final_out : c->last_out))
+                .push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n, -1});
+            oneed += (es_bytes_of(c, (int)f) * c->cap + 15) / 16 * 2;
+        }
+        if (oneed > c->out_cap) {
+            rc_up = dfree(c, c->out_stage);
+            if (rc_up == FJSPH_OK) rc_up = dalloc(c, &c->out_stage, oneed);
+            c->out_cap = rc_up == FJSPH_OK ? oneed : 0;
+        }
+        if (rc_up == FJSPH_OK && !c->out_ready &&
+            cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming) != cudaSuccess)
+            rc_up = FJSPH_E_CUDA;
+        if (rc_up != FJSPH_OK) {
+            c->early_out.clear();
+            c->final_out.clear();
+            c->last_out.clear();
+        }
+    }
     if (!c->copy_stream && rc_up == FJSPH_OK) {
         if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) rc_up = FJSPH_E_CUDA;
         for (int b = 0; b < 2 && rc_up == FJSPH_OK; ++b)
@@ -2427,36 +2461,13 @@ int fjsph_step_host(fjsph_ctx *c, const fjsph_state_view *in, fjsph_state_view *
     if (rc_up != FJSPH_OK || rc_end != FJSPH_OK) {
         for (auto &g : c->in_grp) g.clear();
         for (bool &w : c->in_wait) w = false;
+        c->early_out.clear();
+        c->final_out.clear();
+        c->last_out.clear();
         if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
         if (c->place_stream) cudaStreamSynchronize(c->place_stream);
         join_id_scan(c);
         return rc_up != FJSPH_OK ? rc_up : rc_end;
-    }
-    /* the output fields that are final after the second search's pre-passes go out during the
-     * remaining stages (Runge-Kutta; room for the particles the state holds now) */
-    std::vector<void *> op;
-    view_ptrs(out, op);
-    c->early_out.clear();
-    c->final_out.clear();
-    c->last_out.clear();
-    c->out_sent = c->final_sent = c->last_sent = false;
-    c->out_ins0 = c->inserted;
-    c->out_del0 = c->deleted;
-    if (c->s.solver_type == FJSPH_RUNGE_KUTTA && out->n >= n) {
-        int64_t oneed = 0;
-        for (size_t f = 0; f < op.size(); ++f) {
-            const bool e = early_out_field(f, c->s.variant), fi = final_out_field(f), la = last_out_field(f);
-            if (!op[f] || !(e || fi || la)) continue;
-            (e ? c->early_out : (fi ? c->final_out : c->last_out))
-                .push_back({(int)f, oneed, op[f], (size_t)es_bytes_of(c, (int)f) * n, -1});
-            oneed += (es_bytes_of(c, (int)f) * c->cap + 15) / 16 * 2;
-        }
-        if (oneed > c->out_cap) {
-            TRY(dfree(c, c->out_stage));
-            TRY(dalloc(c, &c->out_stage, oneed));
-            c->out_cap = oneed;
-        }
-        if (!c->out_ready) CU(cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming));
     }
     const int64_t ins0 = c->inserted, del0 = c->deleted;
     double r = 0.0;
