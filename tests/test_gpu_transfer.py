@@ -196,3 +196,36 @@ def test_step_host_live_jet_inserts():
     assert counts[0] > st.n  # the first step inserted
     for ctx in ctxs:
         ctx.close()
+
+
+def test_step_host_then_plain_steps_and_capacity():
+    """After fjsph_step_host the context holds the same pn and pnp1 as after the three calls: a
+    plain fjsph_integrate that follows gives the same state bit for bit.  An output smaller than
+    the particle count is refused with FJSPH_E_CAPACITY after the step, and the context steps on."""
+    from fjsph_gb300._lib import FJSPHError
+    from fjsph_gb300.api import Context
+    from fjsph_gb300.state import SPHState, STEP_FIELDS
+    label, c, st, s = _cases()[2]  # the 3D dam break, FP32 form, ALE
+    cap = st.n + 4096
+    fused = Context(s, cap, c.blocks, c.inlets)
+    plain = Context(s, cap, c.blocks, c.inlets)
+    for ctx in (fused, plain):
+        ctx.upload(d.BOTH, _garbage(st, 7))
+    big = SPHState(cap, st.dim)
+    for f in STEP_FIELDS:
+        getattr(big, f)[:st.n] = getattr(st, f)
+    fused.step_host(_prefix(big, st.n), big, fields=STEP_FIELDS)
+    plain.upload(d.BOTH, st, fields=STEP_FIELDS)
+    plain.integrate()
+    for ctx in (fused, plain):
+        ctx.integrate()
+    a, b = fused.download(), plain.download()
+    for f in STEP_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f"{label} after a plain step: {f}")
+    small = SPHState(st.n - 1, st.dim)
+    with pytest.raises(FJSPHError, match="capacity"):
+        fused.step_host(a, small, fields=STEP_FIELDS)
+    fused.integrate()  # still usable
+    assert np.isfinite(fused.download(fields=["xi"]).xi).all()
+    fused.close()
+    plain.close()
