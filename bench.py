@@ -586,6 +586,8 @@ def run_ours(args, ws, rank, local):
     if args.e2e_steps > 0:
         host = pinned_buffer(s.max_points + 1024, s.dim)
         ctx.download(d.PNP1, out=prefix_state(host, ctx.particle_count()))
+        # one untimed call first: it sizes the call's staging buffers and creates its streams
+        ctx.step_host(prefix_state(host, ctx.particle_count()), host, fields=STEP_FIELDS)
         h2d = d2h = 0
         ps_e = 0
         ctx.event_record(2)
