@@ -490,6 +490,7 @@ int alloc_packed(fjsph_ctx *c) {
     Packed &K = c->K;
     float4 **arrs[] = {&K.A, &K.C, &K.F, &K.G, &K.N, &K.T, &K.O, &K.L0, &K.L1, &K.L2, &K.Lo};
     for (float4 **a : arrs) TRY(dalloc(c, a, c->cap));
+    TRY(dalloc(c, &K.R, c->cap));
     TRY(dalloc(c, &K.bits, c->cap));
     TRY(dalloc(c, &c->nbr_pair, c->nbr_cap));
     TRY(dalloc(c, &c->T.mask, (int64_t)kMaskWords * c->cap));

@@ -76,6 +76,7 @@ struct Packed {
      * (type FJSPH_BOUND) and kLoFluid (type above FJSPH_PISTON): with A and C, the neighbour
      * inputs of the pair sweeps. */
     float4 *Lo;
+    float *R; /* rho - rho0 of the C record, dense: the dSPH pass's one use of C */
     int32_t *bits;
 };
 

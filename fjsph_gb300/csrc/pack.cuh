@@ -27,10 +27,11 @@ __device__ __forceinline__ float4 pack_lo(const float *xl, const float *vl, floa
                        __uint_as_float((__float_as_uint(pr) & ~3u) | flags));
 }
 
-/* A = (fl32(x), vol), C = (fl32(v), rho - rho0), F = (vPert, p), Lo = (bf16 of x - fl32(x) and
- * v - fl32(v), p / rho^2 with type flags), bits.  vol and p / rho^2 are FP32 quotients of
- * the FP32-rounded operands (an FP64 divide per particle costs more than the pass's memory
- * traffic on this GPU); rounded to nearest in every translation unit.  The FP64 -> FP32
+/* A = (fl32(x), vol), C = (fl32(v), rho - rho0), R = rho - rho0, F = (vPert, p),
+ * Lo = (bf16 of x - fl32(x) and v - fl32(v), p / rho^2 with type flags), bits.  vol and
+ * p / rho^2 are FP32 quotients of the FP32-rounded operands (an FP64 divide per particle costs
+ * more than the pass's memory traffic on this GPU); rounded to nearest in every translation
+ * unit.  The FP64 -> FP32
  * roundings run in integer arithmetic (split.cuh), bit-identical to the conversions. */
 template <int D>
 __device__ __forceinline__ void pack_particle(const Params &P, const DevState &W, const Packed &K, int64_t i) {
@@ -44,8 +45,10 @@ __device__ __forceinline__ void pack_particle(const Params &P, const DevState &W
     const double rho = W.rho[i], p = W.p[i];
     const float rf = to_f32(rho), pf = to_f32(p);
     const float pr = __fdiv_rn(pf, rf * rf);
+    const float dr = to_f32(rho - P.rho_rest);
     K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn(to_f32(W.m[i]), rf));
-    K.C[i] = make_float4(vh[0], vh[1], vh[2], to_f32(rho - P.rho_rest));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], dr);
+    K.R[i] = dr;
     const int bits = (W.b[i] & 7) | ((W.surf[i] & 1) << 3) | ((W.surfzone[i] & 1) << 4);
     K.F[i] = make_float4(vp[0], vp[1], vp[2], pf);
     K.Lo[i] = pack_lo(xl, vl, pr, bits);
@@ -67,8 +70,10 @@ __device__ __forceinline__ void pack_moved(const Params &P, const DevState &W, c
     const float rf = to_f32(rho), pf = to_f32(p);
     const float pr = __fdiv_rn(pf, rf * rf);
     const int bits = K.bits[i];
+    const float dr = to_f32(rho - P.rho_rest);
     K.A[i] = make_float4(xh[0], xh[1], xh[2], __fdiv_rn(to_f32(W.m[i]), rf));
-    K.C[i] = make_float4(vh[0], vh[1], vh[2], to_f32(rho - P.rho_rest));
+    K.C[i] = make_float4(vh[0], vh[1], vh[2], dr);
+    K.R[i] = dr;
     reinterpret_cast<float *>(K.F + i)[3] = pf;
     K.Lo[i] = pack_lo(xl, vl, pr, bits);
 }

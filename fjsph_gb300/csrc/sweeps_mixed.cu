@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
     const Pf f = make_pf(P);
     const float4 Ai = K.A[i];
     const LoParts Li(K.Lo[i]);
-    const float drho_i = K.C[i].w;
+    const float drho_i = K.R[i];
     float Lm[D * D], Lnb[D * D], gR[D], nr[D];
 #pragma unroll
     for (int k = 0; k < D * D; ++k) {
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kThreads) k_m_dsph(Params P, DevState W, DevNb
         const float kern = f_kernel(f, r);
         const float gs = f_gscale(f, r);
         const bool fl = (Lj.flags & kLoFluid) != 0u;
-        const float drho = volj * (K.C[j].w - drho_i);
+        const float drho = volj * (K.R[j] - drho_i);
         /* Lm -= volj Rji (x) Grad with Grad = -Rji gs */
         const float w = volj * gs;
 #pragma unroll
